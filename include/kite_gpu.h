@@ -1,0 +1,166 @@
+/*
+ * kite_gpu.h — C ABI of the GB300 exact k-mer counting library
+ * (libkite_gpu.so, hand-written sm_103a CUDA kernels).
+ *
+ * The reference (jiehua1995/Kite v0.7.5) is a monolithic Rust binary with no
+ * FFI.  These entry points replace its internal counting and merging seams,
+ * and keep their argument meaning:
+ *
+ *   kite_gpu_count_submit   <- CountWorker::process_chunk(&[u8])
+ *                              src/count/worker.rs:196 (a chunk starts at a
+ *                              FASTQ record boundary, src/count/bgzf.rs:109-121;
+ *                              a chunk not starting with '@' contributes
+ *                              nothing, src/count/worker.rs:217)
+ *   kite_gpu_count_finish   <- CountWorker::flush_all src/count/worker.rs:284
+ *                              + flush_bucket :296-449 (sort, RLE, DVLE)
+ *   kite_gpu_emit_fn        <- ConcurrentKiteWriter::append_chunk
+ *                              src/count/writer.rs:285-348 (same fields)
+ *   kite_gpu_merge          <- build_merge_partition_chunk
+ *                              src/merge/mod.rs:198-214 over all partitions
+ *                              (load_partition_counts, per-input filter,
+ *                              merge_vectors_total, serialize_partition_chunk
+ *                              src/kiteops/mod.rs:433-859)
+ *
+ * Conventions: every function returns 0 (KITE_OK) or a negative KITE_ERR_*
+ * code; no exception crosses the ABI; a context owns all of its device memory
+ * and streams; one host thread drives one context; every host-side wait is
+ * bounded by cfg.timeout_ms and returns KITE_ERR_TIMEOUT instead of hanging.
+ * There is no CPU fallback: without a usable CUDA device kite_gpu_open fails.
+ */
+#ifndef KITE_GPU_H
+#define KITE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KITE_GPU_ABI_VERSION 1
+
+enum {
+  KITE_OK = 0,
+  KITE_ERR_CUDA = -1,           /* a CUDA runtime call failed */
+  KITE_ERR_OOM = -2,            /* device or pinned allocation failed */
+  KITE_ERR_TIMEOUT = -3,        /* a bounded wait ran out */
+  KITE_ERR_BAD_INPUT = -4,      /* invalid argument or malformed payload */
+  KITE_ERR_COUNT_OVERFLOW = -5, /* merged count exceeds u32 (merge) */
+  KITE_ERR_UNSUPPORTED = -6,    /* k > 64, unknown codec, ... */
+  KITE_ERR_DEVICE = -7,         /* a kernel reported a failure status */
+  KITE_ERR_CALLBACK = -8,       /* the emit callback returned non-zero */
+  KITE_ERR_STATE = -9           /* call out of order */
+};
+
+enum { KITE_SPLIT_AUTO = 0, KITE_SPLIT_SAMPLED = 1, KITE_SPLIT_LEARNED = 2 };
+
+/* Codec bits of a chunk (src/format/run_block.rs:1-3). */
+enum { KITE_CODEC_RAW = 1, KITE_CODEC_DVLE = 2, KITE_CODEC_ZSTD = 4 };
+
+typedef struct kite_gpu_ctx kite_gpu_ctx;
+
+typedef struct {
+  int device;                /* CUDA device ordinal */
+  int k;                     /* 1..64 (u64 keys for k <= 31, u128 for 32..64) */
+  int canonical;             /* 0 or 1 */
+  uint32_t partitions;       /* power of two >= 2: hash buckets of the .kite file */
+  int splitter_mode;         /* KITE_SPLIT_* : how key-range tiles are cut */
+  double imbalance_bound;    /* learned splitters fall back above this max/mean (0 = 1.10) */
+  uint64_t arena_bytes;      /* FASTQ bytes held on device before a flush (0 = auto) */
+  uint32_t timeout_ms;       /* bound on every host-side wait (0 = 600000) */
+  void* stream;              /* optional cudaStream_t to run on (NULL = own stream) */
+} kite_gpu_cfg;
+
+/* One emitted chunk: the arguments of ConcurrentKiteWriter::append_chunk. */
+typedef struct {
+  uint32_t partition_id;
+  uint32_t codec;            /* KITE_CODEC_DVLE for u64/u128 keys */
+  uint64_t row_count;
+  uint64_t raw_bytes;        /* payload length (fast mode: no zstd) */
+  uint64_t key_min_lo[2];    /* u128 key_min_lo as (low 64, high 64) */
+  uint64_t key_min_hi[2];    /* u128 key_min_hi (0 for k <= 64) */
+  uint64_t key_max_lo[2];
+  uint64_t key_max_hi[2];
+} kite_chunk_meta;
+
+/* Called once per non-empty partition, in ascending partition order.  `data`
+ * is valid only during the call.  Return 0 to continue, non-zero to abort
+ * (the API call then returns KITE_ERR_CALLBACK). */
+typedef int (*kite_gpu_emit_fn)(void* user, const kite_chunk_meta* meta, const uint8_t* data, size_t len);
+
+typedef struct {
+  uint64_t reads, bases, kmers;      /* the summary line fields (src/count/mod.rs:598-612) */
+  uint64_t rows, payload_bytes;      /* unique (key,count) rows and DVLE bytes of the last finish */
+  uint32_t tiles, big_tiles, tiles_per_bucket, segments;
+  double tile_imbalance;             /* max / mean keys per non-empty tile */
+  int splitter_used;                 /* KITE_SPLIT_SAMPLED or KITE_SPLIT_LEARNED */
+  double stage_ms[12];               /* per-stage device time of the last finish (events) */
+  uint64_t h2d_bytes, d2h_bytes;
+} kite_gpu_stats;
+
+/* Merge input: one .kite file's partition table, with payloads in host memory
+ * (e.g. an mmap of the file).  Chunks of partition p are chunk_meta[first[p]
+ * .. first[p]+count[p]) and their payload bytes start at base + file_offset. */
+typedef struct {
+  const uint8_t* base;               /* file image */
+  uint64_t base_len;
+  const uint64_t* chunk_offset;      /* per chunk: file offset of the payload */
+  const uint64_t* chunk_len;         /* per chunk: encoded bytes */
+  const uint64_t* chunk_rows;        /* per chunk: row count */
+  const uint32_t* chunk_codec;       /* per chunk: codec bits */
+  const uint64_t* part_first;        /* per partition: first chunk index */
+  const uint64_t* part_count;        /* per partition: number of chunks */
+  int has_min, has_max;              /* header count filters (src/format/header.rs:30-31) */
+  uint32_t min_count, max_count;
+} kite_gpu_merge_input;
+
+int kite_gpu_abi_version(void);
+int kite_gpu_device_count(void);
+
+int kite_gpu_open(const kite_gpu_cfg* cfg, kite_gpu_ctx** out);
+void kite_gpu_close(kite_gpu_ctx* ctx);
+const char* kite_gpu_last_error(const kite_gpu_ctx* ctx);
+
+/* Page-locked host buffers for submit (faster, truly asynchronous copies). */
+void* kite_gpu_alloc_pinned(size_t bytes);
+void kite_gpu_free_pinned(void* p);
+
+/* Queue one FASTQ chunk (host memory).  Returns a ticket >= 0; the buffer may
+ * be reused after kite_gpu_wait_ticket(ticket) returns.  Returns
+ * KITE_ERR_STATE if the device arena is full: call kite_gpu_count_finish to
+ * flush the counted segment, then submit again. */
+int64_t kite_gpu_count_submit(kite_gpu_ctx* ctx, const uint8_t* fastq, size_t len);
+int kite_gpu_wait_ticket(kite_gpu_ctx* ctx, int64_t ticket);
+
+/* Register chunks that already live in device memory (no copy).  Each chunk
+ * start must be 16-byte aligned and 16 readable bytes must follow the last
+ * chunk.  Used by benchmarks that time the kernels on HBM-resident input. */
+int kite_gpu_count_submit_device(kite_gpu_ctx* ctx, const uint8_t* d_fastq, size_t len);
+
+/* Count everything submitted since the last finish: emit one DVLE chunk per
+ * non-empty partition (ascending), then reset for the next segment.  With
+ * emit == NULL the results stay on the device (kite_gpu_result_*). */
+int kite_gpu_count_finish(kite_gpu_ctx* ctx, kite_gpu_emit_fn emit, void* user);
+
+/* Results of the last finish kept on device: partition metadata and the
+ * device address of its payload. */
+int kite_gpu_result_partition(kite_gpu_ctx* ctx, uint32_t partition, kite_chunk_meta* meta,
+                              const uint8_t** device_payload, size_t* len);
+
+/* K-way merge of n inputs (same k, canonical, partitions and key width):
+ * per-input header filter before summing, u64 sums, u32 overflow is an error
+ * (KITE_ERR_COUNT_OVERFLOW, message names the key), one DVLE chunk per
+ * non-empty partition, emitted in partition order. */
+int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n, kite_gpu_emit_fn emit,
+                   void* user);
+
+int kite_gpu_get_stats(kite_gpu_ctx* ctx, kite_gpu_stats* out);
+
+/* Device-side timing of the last count/merge, summed per kernel family. */
+int kite_gpu_synchronize(kite_gpu_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KITE_GPU_H */

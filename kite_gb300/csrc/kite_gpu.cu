@@ -1,0 +1,726 @@
+// C-ABI implementation of libkite_gpu.so: context, device arena, the staged
+// count pipeline and result emission.  See include/kite_gpu.h for the
+// contract and the reference seams each entry point replaces.
+//
+// Count pipeline of one segment (everything submitted since the last finish):
+//   K1  newline count per 16 KiB block + scan        -> line phase at each block
+//   K2  extract (histogram pass): rolling canonical k-mers, hash-bucket counts,
+//       reads/bases/kmers, key sample from the segment's first chunk
+//   K3  extract (scatter pass): k-mers into their hash-bucket regions
+//   K3b tile split: each bucket cut into key-range tiles by splitters
+//   K4  tile sort + run-length reduction on chip (oversized tiles: K4b)
+//   K7  DVLE encode of every bucket's rows into one payload per partition
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "kite_gpu.h"
+#include "kite_internal.h"
+#include "merge.h"
+#include "splitters.h"
+#include "mlp.h"
+
+using namespace kite;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes + bytes / 8 + 256;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    cap = want;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class U> U* as() const { return static_cast<U*>(p); }
+};
+
+struct HostBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes + bytes / 8 + 256;
+    cudaError_t e = cudaMallocHost(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    cap = want;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class U> U* as() const { return static_cast<U*>(p); }
+};
+
+struct Chunk {
+  uint64_t off;  // offset from the arena base
+  uint64_t len;
+};
+
+enum Stage { ST_LINES = 0, ST_HIST, ST_SCATTER, ST_SPLIT, ST_SORT, ST_BIG, ST_ENCODE, ST_D2H, ST_COUNT };
+
+}  // namespace
+
+struct kite_gpu_ctx {
+  kite_gpu_cfg cfg{};
+  std::string err;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaStream_t copy_stream = nullptr;
+
+  // FASTQ arena (host submissions are copied here)
+  DevBuf arena;
+  uint64_t arena_used = 0;
+  const uint8_t* ext_base = nullptr;  // device submissions: caller-owned base
+  bool ext_mode = false;
+  std::vector<Chunk> chunks;
+  std::vector<cudaEvent_t> ticket_events;
+  int64_t next_ticket = 0;
+
+  // scratch
+  DevBuf blocks, nl, scan_tmp, bucket_count, bucket_off, bucket_fill, totals, status;
+  DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, hist16;
+  DevBuf slices, tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
+  HostBuf h_blocks, h_small, h_tiles, h_out;
+  std::vector<cudaEvent_t> ev;  // stage events
+
+  // results of the last finish
+  std::vector<BucketMeta> res_meta;
+  uint64_t res_bytes = 0;
+  kite_gpu_stats stats{};
+  MlpModel* mlp = nullptr;
+};
+
+namespace {
+
+int fail(kite_gpu_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define KCU(call)                                                                       \
+  do {                                                                                  \
+    cudaError_t _e = (call);                                                            \
+    if (_e != cudaSuccess)                                                              \
+      return fail(ctx, _e == cudaErrorMemoryAllocation ? KITE_ERR_OOM : KITE_ERR_CUDA, \
+                  std::string(#call) + ": " + cudaGetErrorString(_e));                  \
+  } while (0)
+
+// Bounded wait for all work queued on `s`.
+int wait_stream(kite_gpu_ctx* ctx, cudaStream_t s) {
+  cudaEvent_t e;
+  KCU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  KCU(cudaEventRecord(e, s));
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(ctx->cfg.timeout_ms);
+  int spins = 0;
+  for (;;) {
+    cudaError_t q = cudaEventQuery(e);
+    if (q == cudaSuccess) break;
+    if (q != cudaErrorNotReady) {
+      cudaEventDestroy(e);
+      return fail(ctx, KITE_ERR_CUDA, std::string("stream wait: ") + cudaGetErrorString(q));
+    }
+    if (std::chrono::steady_clock::now() > deadline) {
+      cudaEventDestroy(e);
+      return fail(ctx, KITE_ERR_TIMEOUT, "device work did not finish within timeout_ms");
+    }
+    if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  cudaEventDestroy(e);
+  return KITE_OK;
+}
+
+int check_status(kite_gpu_ctx* ctx, const char* where) {
+  DevStatus st{};
+  KCU(cudaMemcpyAsync(&st, ctx->status.p, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
+  int rc = wait_stream(ctx, ctx->stream);
+  if (rc) return rc;
+  if (st.code != KITE_DEV_OK) {
+    char buf[256];
+    snprintf(buf, sizeof buf, "%s: device status %u (%u, %u, %u)", where, st.code, st.a, st.b, st.c);
+    return fail(ctx, KITE_ERR_DEVICE, buf);
+  }
+  return KITE_OK;
+}
+
+uint32_t log2u(uint64_t v) {
+  uint32_t r = 0;
+  while ((1ull << r) < v) r++;
+  return r;
+}
+
+const uint8_t* arena_base(kite_gpu_ctx* ctx) {
+  return ctx->ext_mode ? ctx->ext_base : ctx->arena.as<const uint8_t>();
+}
+
+void reset_segment(kite_gpu_ctx* ctx) {
+  ctx->chunks.clear();
+  ctx->arena_used = 0;
+  ctx->ext_mode = false;
+  ctx->ext_base = nullptr;
+}
+
+template <class T>
+int run_count(kite_gpu_ctx* ctx) {
+  cudaStream_t s = ctx->stream;
+  const uint32_t P = ctx->cfg.partitions;
+  const uint32_t k = (uint32_t)ctx->cfg.k;
+  const uint32_t CAP = tile_capacity<T>();
+  auto& st = ctx->stats;
+  const uint64_t prev_h2d = st.h2d_bytes, prev_d2h = st.d2h_bytes;
+  const uint32_t prev_segments = st.segments;
+  std::memset(&st, 0, sizeof st);
+  st.h2d_bytes = prev_h2d;
+  st.d2h_bytes = prev_d2h;
+  st.segments = prev_segments + 1;
+  for (auto& e : ctx->ev) cudaEventRecord(e, s);  // reset so unused stages read 0
+  KCU(cudaEventRecord(ctx->ev[0], s));
+
+  // ---- blocks -------------------------------------------------------------
+  uint32_t blk = sizeof(T) == 8 ? 16384 : 8192;
+  while (blk > 1024 && extract_smem_bytes(sizeof(T), blk, P, true) > 200 * 1024) blk >>= 1;
+  if (extract_smem_bytes(sizeof(T), blk, P, true) > 220 * 1024)
+    return fail(ctx, KITE_ERR_UNSUPPORTED, "partition count too large for the extraction kernel");
+  std::vector<BlockDesc> hb;
+  uint64_t chunk0_len = 0;
+  for (size_t c = 0; c < ctx->chunks.size(); ++c) {
+    const Chunk& ch = ctx->chunks[c];
+    if (ch.len == 0) continue;
+    const uint32_t first = (uint32_t)hb.size();
+    if (hb.empty()) chunk0_len = ch.len;
+    for (uint64_t o = 0; o < ch.len; o += blk) {
+      BlockDesc d;
+      d.start = ch.off + o;
+      d.end = ch.off + std::min<uint64_t>(o + blk, ch.len);
+      d.chunk_start = ch.off;
+      d.first_block = first;
+      d.flags = (first == 0) ? 2u : 0u;
+      hb.push_back(d);
+    }
+  }
+  const uint32_t nblocks = (uint32_t)hb.size();
+  if (nblocks == 0) {
+    ctx->res_meta.assign(P, BucketMeta{});
+    ctx->res_bytes = 0;
+    return KITE_OK;
+  }
+  KCU(ctx->h_blocks.ensure(hb.size() * sizeof(BlockDesc)));
+  std::memcpy(ctx->h_blocks.p, hb.data(), hb.size() * sizeof(BlockDesc));
+  KCU(ctx->blocks.ensure(hb.size() * sizeof(BlockDesc)));
+  KCU(cudaMemcpyAsync(ctx->blocks.p, ctx->h_blocks.p, hb.size() * sizeof(BlockDesc), cudaMemcpyHostToDevice, s));
+  KCU(ctx->nl.ensure((size_t)nblocks * 8));
+  KCU(ctx->scan_tmp.ensure(scan_tmp_elems(std::max<size_t>((size_t)nblocks, (size_t)P * 4096)) * 8 + 64));
+  KCU(ctx->status.ensure(sizeof(DevStatus)));
+  KCU(cudaMemsetAsync(ctx->status.p, 0, sizeof(DevStatus), s));
+  const uint8_t* base = arena_base(ctx);
+  launch_newline_count(base, ctx->blocks.as<BlockDesc>(), nblocks, ctx->nl.as<unsigned long long>(), s);
+  exclusive_scan_u64(ctx->nl.as<unsigned long long>(), ctx->nl.as<unsigned long long>(), nblocks,
+                     ctx->scan_tmp.as<unsigned long long>(), s);
+  KCU(cudaEventRecord(ctx->ev[1], s));
+
+  // ---- K2 histogram pass --------------------------------------------------
+  const uint32_t sample_cap = 1u << 20;
+  KCU(ctx->bucket_count.ensure((size_t)P * 8));
+  KCU(ctx->totals.ensure(sizeof(CountTotals)));
+  KCU(ctx->sample.ensure((size_t)sample_cap * sizeof(T)));
+  KCU(ctx->sample_count.ensure(8));
+  KCU(cudaMemsetAsync(ctx->bucket_count.p, 0, (size_t)P * 8, s));
+  KCU(cudaMemsetAsync(ctx->totals.p, 0, sizeof(CountTotals), s));
+  KCU(cudaMemsetAsync(ctx->sample_count.p, 0, 8, s));
+  // keep ~2^20 of the first chunk's k-mer positions (about one k-mer per 2.5 bytes)
+  uint64_t est = std::max<uint64_t>(chunk0_len * 2 / 5, 1);
+  uint32_t mask = 0;
+  while ((est >> log2u((uint64_t)mask + 1)) > sample_cap && mask < (1u << 30)) mask = mask * 2 + 1;
+  ExtractParams<T> ep{};
+  ep.arena = base;
+  ep.blocks = ctx->blocks.as<BlockDesc>();
+  ep.block_nl_excl = ctx->nl.as<unsigned long long>();
+  ep.k = k;
+  ep.canonical = ctx->cfg.canonical ? 1u : 0u;
+  ep.shift = 64 - log2u(P);
+  ep.partitions = P;
+  ep.blk_bytes = blk;
+  ep.bucket_count = ctx->bucket_count.as<unsigned long long>();
+  ep.totals = ctx->totals.as<CountTotals>();
+  ep.sample = ctx->sample.as<T>();
+  ep.sample_count = ctx->sample_count.as<unsigned int>();
+  ep.sample_cap = sample_cap;
+  ep.sample_mask = mask;
+  ep.status = ctx->status.as<DevStatus>();
+  launch_extract_hist<T>(ep, nblocks, s);
+  KCU(cudaGetLastError());
+  KCU(cudaEventRecord(ctx->ev[2], s));
+
+  // bring bucket counts, totals and the sample count to the host
+  const size_t small_bytes = (size_t)P * 8 + sizeof(CountTotals) + 8;
+  KCU(ctx->h_small.ensure(small_bytes + (size_t)P * 8));
+  uint8_t* hs = ctx->h_small.as<uint8_t>();
+  KCU(cudaMemcpyAsync(hs, ctx->bucket_count.p, (size_t)P * 8, cudaMemcpyDeviceToHost, s));
+  KCU(cudaMemcpyAsync(hs + (size_t)P * 8, ctx->totals.p, sizeof(CountTotals), cudaMemcpyDeviceToHost, s));
+  KCU(cudaMemcpyAsync(hs + (size_t)P * 8 + sizeof(CountTotals), ctx->sample_count.p, 4, cudaMemcpyDeviceToHost, s));
+  int rc = wait_stream(ctx, s);
+  if (rc) return rc;
+  std::vector<uint64_t> bcount(P);
+  std::memcpy(bcount.data(), hs, (size_t)P * 8);
+  CountTotals tot;
+  std::memcpy(&tot, hs + (size_t)P * 8, sizeof tot);
+  uint32_t nsample = 0;
+  std::memcpy(&nsample, hs + (size_t)P * 8 + sizeof(CountTotals), 4);
+  nsample = std::min(nsample, sample_cap);
+  st.reads = tot.reads;
+  st.bases = tot.bases;
+  st.kmers = tot.kmers;
+  const uint64_t N = tot.kmers;
+  if (N == 0) {
+    ctx->res_meta.assign(P, BucketMeta{});
+    ctx->res_bytes = 0;
+    return KITE_OK;
+  }
+
+  // ---- K3 scatter pass ----------------------------------------------------
+  std::vector<uint64_t> boff(P);
+  uint64_t acc = 0, maxb = 0;
+  for (uint32_t b = 0; b < P; ++b) {
+    boff[b] = acc;
+    acc += bcount[b];
+    maxb = std::max(maxb, bcount[b]);
+  }
+  std::memcpy(hs + small_bytes, boff.data(), (size_t)P * 8);
+  KCU(ctx->bucket_off.ensure((size_t)P * 8));
+  KCU(ctx->bucket_fill.ensure((size_t)P * 8));
+  KCU(cudaMemcpyAsync(ctx->bucket_off.p, hs + small_bytes, (size_t)P * 8, cudaMemcpyHostToDevice, s));
+  KCU(cudaMemsetAsync(ctx->bucket_fill.p, 0, (size_t)P * 8, s));
+  KCU(ctx->keys_a.ensure(N * sizeof(T)));
+  KCU(ctx->keys_b.ensure(N * sizeof(T)));
+  KCU(ctx->counts.ensure(N * 4));
+  ep.bucket_off = ctx->bucket_off.as<unsigned long long>();
+  ep.bucket_fill = ctx->bucket_fill.as<unsigned long long>();
+  ep.keys_out = ctx->keys_a.as<T>();
+  launch_extract_scatter<T>(ep, nblocks, s);
+  KCU(cudaGetLastError());
+  KCU(cudaEventRecord(ctx->ev[3], s));
+
+  // ---- K3b tile split -----------------------------------------------------
+  const double fill = 0.5;  // target mean tile load as a fraction of capacity
+  uint32_t S = 1;
+  while ((double)maxb / S > fill * CAP && S < 4096) S <<= 1;
+  st.tiles_per_bucket = S;
+  T* sorted = ctx->keys_a.as<T>();
+  T* scratch = ctx->keys_b.as<T>();
+  std::vector<TileDesc> ht;
+  if (S == 1) {
+    for (uint32_t b = 0; b < P; ++b) ht.push_back(TileDesc{boff[b], (uint32_t)bcount[b], b});
+  } else {
+    KCU(ctx->splitters.ensure((size_t)S * sizeof(T)));
+    KCU(ctx->hist16.ensure((size_t)65536 * 4));
+    bool learned = false;
+    const int mode = ctx->cfg.splitter_mode;
+    if (mode == KITE_SPLIT_LEARNED || mode == KITE_SPLIT_AUTO) {
+      int lrc = mlp_splitters<T>(ctx->mlp, ctx->sample.as<T>(), nsample, 2 * k, S, ctx->splitters.as<T>(),
+                                 ctx->cfg.imbalance_bound, s, &learned);
+      if (lrc) return fail(ctx, KITE_ERR_CUDA, "learned splitter training failed");
+    }
+    if (!learned)
+      compute_hist_splitters<T>(ctx->sample.as<T>(), nsample, 2 * k, S, ctx->splitters.as<T>(),
+                                ctx->hist16.as<unsigned>(), s);
+    st.splitter_used = learned ? KITE_SPLIT_LEARNED : KITE_SPLIT_SAMPLED;
+    const uint32_t sk = split_slice_keys(sizeof(T));
+    std::vector<SliceDesc> hsl;
+    for (uint32_t b = 0; b < P; ++b)
+      for (uint64_t o = 0; o < bcount[b]; o += sk)
+        hsl.push_back(SliceDesc{boff[b] + o, (uint32_t)std::min<uint64_t>(sk, bcount[b] - o), b});
+    const size_t nt = (size_t)P * S;
+    KCU(ctx->slices.ensure(hsl.size() * sizeof(SliceDesc)));
+    KCU(ctx->h_tiles.ensure(std::max(hsl.size() * sizeof(SliceDesc), nt * (sizeof(TileDesc) + 8))));
+    std::memcpy(ctx->h_tiles.p, hsl.data(), hsl.size() * sizeof(SliceDesc));
+    KCU(cudaMemcpyAsync(ctx->slices.p, ctx->h_tiles.p, hsl.size() * sizeof(SliceDesc), cudaMemcpyHostToDevice, s));
+    KCU(ctx->tile_count.ensure(nt * 8));
+    KCU(ctx->tile_off.ensure(nt * 8));
+    KCU(ctx->tile_fill.ensure(nt * 8));
+    KCU(ctx->scan_tmp.ensure(scan_tmp_elems(nt) * 8 + 64));
+    KCU(cudaMemsetAsync(ctx->tile_count.p, 0, nt * 8, s));
+    KCU(cudaMemsetAsync(ctx->tile_fill.p, 0, nt * 8, s));
+    TileSplitParams<T> tp{};
+    tp.keys_in = ctx->keys_a.as<T>();
+    tp.keys_out = ctx->keys_b.as<T>();
+    tp.slices = ctx->slices.as<SliceDesc>();
+    tp.splitters = ctx->splitters.as<T>();
+    tp.S = S;
+    tp.tile_count = ctx->tile_count.as<unsigned long long>();
+    tp.tile_off = ctx->tile_off.as<unsigned long long>();
+    tp.tile_fill = ctx->tile_fill.as<unsigned long long>();
+    tp.status = ctx->status.as<DevStatus>();
+    launch_tile_hist<T>(tp, (uint32_t)hsl.size(), sk, s);
+    exclusive_scan_u64(tp.tile_count, ctx->tile_off.as<unsigned long long>(), nt,
+                       ctx->scan_tmp.as<unsigned long long>(), s);
+    launch_tile_scatter<T>(tp, (uint32_t)hsl.size(), sk, s);
+    KCU(cudaGetLastError());
+    // tile counts/offsets to host to build the tile list
+    uint64_t* htc = reinterpret_cast<uint64_t*>(ctx->h_tiles.as<uint8_t>() + nt * sizeof(TileDesc));
+    KCU(cudaMemcpyAsync(htc, ctx->tile_count.p, nt * 8, cudaMemcpyDeviceToHost, s));
+    rc = wait_stream(ctx, s);
+    if (rc) return rc;
+    ht.resize(nt);
+    uint64_t a2 = 0;
+    for (size_t t = 0; t < nt; ++t) {
+      ht[t] = TileDesc{a2, (uint32_t)htc[t], (uint32_t)(t / S)};
+      a2 += htc[t];
+    }
+    sorted = ctx->keys_b.as<T>();
+    scratch = ctx->keys_a.as<T>();
+  }
+  KCU(cudaEventRecord(ctx->ev[4], s));
+  const uint32_t ntiles = (uint32_t)ht.size();
+  std::vector<uint32_t> big;
+  uint64_t tmax = 0, tsum = 0, tne = 0;
+  for (uint32_t t = 0; t < ntiles; ++t) {
+    if (ht[t].len > CAP) big.push_back(t);
+    if (ht[t].len) {
+      tmax = std::max<uint64_t>(tmax, ht[t].len);
+      tsum += ht[t].len;
+      tne++;
+    }
+  }
+  st.tiles = ntiles;
+  st.big_tiles = (uint32_t)big.size();
+  st.tile_imbalance = tne ? (double)tmax / ((double)tsum / (double)tne) : 0.0;
+  KCU(ctx->h_tiles.ensure(ht.size() * sizeof(TileDesc) + big.size() * 4 + 64));
+  std::memcpy(ctx->h_tiles.p, ht.data(), ht.size() * sizeof(TileDesc));
+  std::memcpy(ctx->h_tiles.as<uint8_t>() + ht.size() * sizeof(TileDesc), big.data(), big.size() * 4);
+  KCU(ctx->tiles.ensure(ht.size() * sizeof(TileDesc)));
+  KCU(ctx->big_ids.ensure(big.size() * 4 + 4));
+  KCU(cudaMemcpyAsync(ctx->tiles.p, ctx->h_tiles.p, ht.size() * sizeof(TileDesc), cudaMemcpyHostToDevice, s));
+  if (!big.empty())
+    KCU(cudaMemcpyAsync(ctx->big_ids.p, ctx->h_tiles.as<uint8_t>() + ht.size() * sizeof(TileDesc), big.size() * 4,
+                        cudaMemcpyHostToDevice, s));
+  KCU(ctx->tile_out.ensure((size_t)ntiles * sizeof(TileOut<T>)));
+
+  // ---- K4 tile sort + RLE ---------------------------------------------------
+  launch_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ntiles,
+                      ctx->tile_out.as<TileOut<T>>(), ctx->status.as<DevStatus>(), s);
+  KCU(cudaGetLastError());
+  KCU(cudaEventRecord(ctx->ev[5], s));
+  launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(),
+                          ctx->big_ids.as<uint32_t>(), (uint32_t)big.size(), ctx->tile_out.as<TileOut<T>>(),
+                          ctx->status.as<DevStatus>(), s);
+  KCU(cudaGetLastError());
+  KCU(cudaEventRecord(ctx->ev[6], s));
+
+  // ---- K7 DVLE encode -------------------------------------------------------
+  const uint32_t Sl = ntiles / P;
+  KCU(ctx->tile_boff.ensure((size_t)ntiles * 8));
+  KCU(ctx->tile_prev.ensure((size_t)ntiles * sizeof(T)));
+  KCU(ctx->meta.ensure((size_t)P * sizeof(BucketMeta)));
+  launch_tile_link<T>(ctx->tile_out.as<TileOut<T>>(), P, Sl, ctx->tile_boff.as<unsigned long long>(),
+                      ctx->tile_prev.as<T>(), ctx->meta.as<BucketMeta>(), s);
+  launch_bucket_offsets(ctx->meta.as<BucketMeta>(), P, nullptr, s);
+  ctx->res_meta.resize(P);
+  KCU(cudaMemcpyAsync(ctx->res_meta.data(), ctx->meta.p, (size_t)P * sizeof(BucketMeta), cudaMemcpyDeviceToHost, s));
+  rc = wait_stream(ctx, s);
+  if (rc) return rc;
+  rc = check_status(ctx, "count");
+  if (rc) return rc;
+  uint64_t total_bytes = 0, rows = 0;
+  for (uint32_t b = 0; b < P; ++b) {
+    total_bytes += ctx->res_meta[b].bytes;
+    rows += ctx->res_meta[b].rows;
+  }
+  KCU(ctx->out.ensure(total_bytes + 16));
+  launch_encode<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ctx->tile_out.as<TileOut<T>>(),
+                   ctx->tile_boff.as<unsigned long long>(), ctx->tile_prev.as<T>(), ctx->meta.as<BucketMeta>(), ntiles,
+                   ctx->out.as<uint8_t>(), total_bytes, ctx->status.as<DevStatus>(), s);
+  KCU(cudaGetLastError());
+  KCU(cudaEventRecord(ctx->ev[7], s));
+  rc = check_status(ctx, "encode");
+  if (rc) return rc;
+  ctx->res_bytes = total_bytes;
+  st.rows = rows;
+  st.payload_bytes = total_bytes;
+  // stage times
+  static const int map[7] = {ST_LINES, ST_HIST, ST_SCATTER, ST_SPLIT, ST_SORT, ST_BIG, ST_ENCODE};
+  for (int i = 0; i < 7; ++i) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
+    st.stage_ms[map[i]] = ms;
+  }
+  return KITE_OK;
+}
+
+int emit_results(kite_gpu_ctx* ctx, kite_gpu_emit_fn emit, void* user) {
+  if (!emit) return KITE_OK;
+  const uint32_t P = (uint32_t)ctx->res_meta.size();
+  if (ctx->res_bytes) {
+    KCU(ctx->h_out.ensure(ctx->res_bytes));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, ctx->stream);
+    KCU(cudaMemcpyAsync(ctx->h_out.p, ctx->out.p, ctx->res_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    cudaEventRecord(e1, ctx->stream);
+    int rc = wait_stream(ctx, ctx->stream);
+    if (rc) return rc;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ctx->stats.stage_ms[ST_D2H] = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->stats.d2h_bytes += ctx->res_bytes;
+  }
+  for (uint32_t b = 0; b < P; ++b) {
+    const BucketMeta& m = ctx->res_meta[b];
+    if (m.rows == 0) continue;
+    kite_chunk_meta cm{};
+    cm.partition_id = b;
+    cm.codec = KITE_CODEC_DVLE;
+    cm.row_count = m.rows;
+    cm.raw_bytes = m.bytes;
+    cm.key_min_lo[0] = m.kmin_lo;
+    cm.key_min_lo[1] = m.kmin_hi;
+    cm.key_max_lo[0] = m.kmax_lo;
+    cm.key_max_lo[1] = m.kmax_hi;
+    if (emit(user, &cm, ctx->h_out.as<uint8_t>() + m.byte_off, (size_t)m.bytes) != 0)
+      return fail(ctx, KITE_ERR_CALLBACK, "emit callback aborted");
+  }
+  return KITE_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+int kite_gpu_abi_version(void) { return KITE_GPU_ABI_VERSION; }
+
+int kite_gpu_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+  return n;
+}
+
+const char* kite_gpu_last_error(const kite_gpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void* kite_gpu_alloc_pinned(size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) return nullptr;
+  return p;
+}
+void kite_gpu_free_pinned(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+int kite_gpu_open(const kite_gpu_cfg* cfg, kite_gpu_ctx** out) {
+  if (!cfg || !out) return KITE_ERR_BAD_INPUT;
+  *out = nullptr;
+  if (cfg->k < 1 || cfg->k > 64) return KITE_ERR_UNSUPPORTED;
+  if (cfg->partitions < 2 || (cfg->partitions & (cfg->partitions - 1)) || cfg->partitions > 65536)
+    return KITE_ERR_BAD_INPUT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || cfg->device < 0 || cfg->device >= ndev)
+    return KITE_ERR_CUDA;
+  if (cudaSetDevice(cfg->device) != cudaSuccess) return KITE_ERR_CUDA;
+  kite_gpu_ctx* ctx = new kite_gpu_ctx();
+  ctx->cfg = *cfg;
+  if (ctx->cfg.timeout_ms == 0) ctx->cfg.timeout_ms = 600000;
+  if (ctx->cfg.imbalance_bound <= 0) ctx->cfg.imbalance_bound = 1.10;
+  if (cfg->stream) {
+    ctx->stream = (cudaStream_t)cfg->stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete ctx;
+      return KITE_ERR_CUDA;
+    }
+    ctx->own_stream = true;
+  }
+  if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return KITE_ERR_CUDA;
+  }
+  ctx->ev.resize(9);
+  for (auto& e : ctx->ev) cudaEventCreate(&e);
+  if (ctx->cfg.arena_bytes == 0) {
+    size_t fr = 0, to = 0;
+    cudaMemGetInfo(&fr, &to);
+    ctx->cfg.arena_bytes = std::max<uint64_t>(fr / 8, 64ull << 20);
+  }
+  ctx->mlp = mlp_create();
+  *out = ctx;
+  return KITE_OK;
+}
+
+void kite_gpu_close(kite_gpu_ctx* ctx) {
+  if (!ctx) return;
+  cudaStreamSynchronize(ctx->stream);
+  cudaStreamSynchronize(ctx->copy_stream);
+  for (auto e : ctx->ticket_events) cudaEventDestroy(e);
+  for (auto e : ctx->ev) cudaEventDestroy(e);
+  DevBuf* bufs[] = {&ctx->arena, &ctx->blocks, &ctx->nl, &ctx->scan_tmp, &ctx->bucket_count, &ctx->bucket_off,
+                    &ctx->bucket_fill, &ctx->totals, &ctx->status, &ctx->keys_a, &ctx->keys_b, &ctx->counts,
+                    &ctx->sample, &ctx->sample_count, &ctx->splitters, &ctx->hist16, &ctx->slices,
+                    &ctx->tile_count, &ctx->tile_off, &ctx->tile_fill, &ctx->tiles, &ctx->big_ids,
+                    &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out};
+  for (DevBuf* b : bufs) b->release();
+  ctx->h_blocks.release();
+  ctx->h_small.release();
+  ctx->h_tiles.release();
+  ctx->h_out.release();
+  mlp_destroy(ctx->mlp);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  cudaStreamDestroy(ctx->copy_stream);
+  delete ctx;
+}
+
+int64_t kite_gpu_count_submit(kite_gpu_ctx* ctx, const uint8_t* fastq, size_t len) {
+  if (!ctx || (!fastq && len)) return KITE_ERR_BAD_INPUT;
+  if (ctx->ext_mode) return fail(ctx, KITE_ERR_STATE, "host and device submissions cannot mix in one segment");
+  if (len == 0) return ctx->next_ticket++;
+  const uint64_t off = (ctx->arena_used + 15) & ~15ull;
+  if (off + len + 16 > ctx->cfg.arena_bytes) {
+    if (ctx->chunks.empty() && len + 16 > ctx->cfg.arena_bytes)
+      return fail(ctx, KITE_ERR_BAD_INPUT, "chunk larger than the device arena");
+    return fail(ctx, KITE_ERR_STATE, "device arena full: finish the segment first");
+  }
+  // the copy stream waits for earlier compute on the arena (a finish may be in flight)
+  cudaEvent_t dep;
+  KCU(cudaEventCreateWithFlags(&dep, cudaEventDisableTiming));
+  KCU(cudaEventRecord(dep, ctx->stream));
+  KCU(cudaStreamWaitEvent(ctx->copy_stream, dep, 0));
+  cudaEventDestroy(dep);
+  if (off + len + 16 > ctx->arena.cap) {
+    // grow geometrically up to arena_bytes, keeping the bytes already queued
+    uint64_t want = std::max<uint64_t>(off + len + 16, std::max<uint64_t>(ctx->arena.cap * 2, 64ull << 20));
+    want = std::min<uint64_t>(want, ctx->cfg.arena_bytes);
+    void* np = nullptr;
+    KCU(cudaMalloc(&np, want));
+    if (ctx->arena_used) {
+      KCU(cudaMemcpyAsync(np, ctx->arena.p, ctx->arena_used, cudaMemcpyDeviceToDevice, ctx->copy_stream));
+      KCU(cudaStreamSynchronize(ctx->copy_stream));
+    }
+    if (ctx->arena.p) cudaFree(ctx->arena.p);
+    ctx->arena.p = np;
+    ctx->arena.cap = want;
+  }
+  KCU(cudaMemcpyAsync(ctx->arena.as<uint8_t>() + off, fastq, len, cudaMemcpyHostToDevice, ctx->copy_stream));
+  // zero the 16 pad bytes after the chunk (vector loads may read them)
+  KCU(cudaMemsetAsync(ctx->arena.as<uint8_t>() + off + len, 0, 16, ctx->copy_stream));
+  cudaEvent_t e;
+  KCU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  KCU(cudaEventRecord(e, ctx->copy_stream));
+  ctx->ticket_events.push_back(e);
+  ctx->chunks.push_back(Chunk{off, len});
+  ctx->arena_used = off + len;
+  ctx->stats.h2d_bytes += len;
+  return ctx->next_ticket++;
+}
+
+int kite_gpu_wait_ticket(kite_gpu_ctx* ctx, int64_t ticket) {
+  if (!ctx) return KITE_ERR_BAD_INPUT;
+  // tickets complete in order on the copy stream; waiting for the stream is
+  // a superset of waiting for this ticket
+  (void)ticket;
+  return wait_stream(ctx, ctx->copy_stream);
+}
+
+int kite_gpu_count_submit_device(kite_gpu_ctx* ctx, const uint8_t* d_fastq, size_t len) {
+  if (!ctx || (!d_fastq && len)) return KITE_ERR_BAD_INPUT;
+  if (!ctx->ext_mode && !ctx->chunks.empty())
+    return fail(ctx, KITE_ERR_STATE, "host and device submissions cannot mix in one segment");
+  if (((uintptr_t)d_fastq) & 15) return fail(ctx, KITE_ERR_BAD_INPUT, "device chunk must be 16-byte aligned");
+  if (len == 0) return KITE_OK;
+  if (!ctx->ext_mode) {
+    ctx->ext_mode = true;
+    ctx->ext_base = d_fastq;
+  }
+  if (d_fastq < ctx->ext_base) return fail(ctx, KITE_ERR_BAD_INPUT, "device chunks must not precede the first one");
+  ctx->chunks.push_back(Chunk{(uint64_t)(d_fastq - ctx->ext_base), len});
+  return KITE_OK;
+}
+
+int kite_gpu_count_finish(kite_gpu_ctx* ctx, kite_gpu_emit_fn emit, void* user) {
+  if (!ctx) return KITE_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->cfg.device);
+  // compute waits for all queued copies
+  cudaEvent_t dep;
+  KCU(cudaEventCreateWithFlags(&dep, cudaEventDisableTiming));
+  KCU(cudaEventRecord(dep, ctx->copy_stream));
+  KCU(cudaStreamWaitEvent(ctx->stream, dep, 0));
+  cudaEventDestroy(dep);
+  int rc = ctx->cfg.k <= 31 ? run_count<uint64_t>(ctx) : run_count<u128>(ctx);
+  if (rc == KITE_OK) rc = emit_results(ctx, emit, user);
+  for (auto e : ctx->ticket_events) cudaEventDestroy(e);
+  ctx->ticket_events.clear();
+  reset_segment(ctx);
+  return rc;
+}
+
+int kite_gpu_result_partition(kite_gpu_ctx* ctx, uint32_t partition, kite_chunk_meta* meta,
+                              const uint8_t** device_payload, size_t* len) {
+  if (!ctx || partition >= ctx->res_meta.size()) return KITE_ERR_BAD_INPUT;
+  const BucketMeta& m = ctx->res_meta[partition];
+  if (meta) {
+    std::memset(meta, 0, sizeof *meta);
+    meta->partition_id = partition;
+    meta->codec = KITE_CODEC_DVLE;
+    meta->row_count = m.rows;
+    meta->raw_bytes = m.bytes;
+    meta->key_min_lo[0] = m.kmin_lo;
+    meta->key_min_lo[1] = m.kmin_hi;
+    meta->key_max_lo[0] = m.kmax_lo;
+    meta->key_max_lo[1] = m.kmax_hi;
+  }
+  if (device_payload) *device_payload = ctx->out.as<uint8_t>() + m.byte_off;
+  if (len) *len = (size_t)m.bytes;
+  return KITE_OK;
+}
+
+int kite_gpu_get_stats(kite_gpu_ctx* ctx, kite_gpu_stats* out) {
+  if (!ctx || !out) return KITE_ERR_BAD_INPUT;
+  *out = ctx->stats;
+  return KITE_OK;
+}
+
+int kite_gpu_synchronize(kite_gpu_ctx* ctx) {
+  if (!ctx) return KITE_ERR_BAD_INPUT;
+  int rc = wait_stream(ctx, ctx->copy_stream);
+  if (rc) return rc;
+  return wait_stream(ctx, ctx->stream);
+}
+
+int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n, kite_gpu_emit_fn emit, void* user) {
+  if (!ctx || !inputs || n <= 0) return KITE_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->cfg.device);
+  std::string msg;
+  int rc = merge_run(ctx->cfg.k <= 31 ? 8 : 16, ctx->cfg.partitions, inputs, n, ctx->stream, ctx->cfg.timeout_ms,
+                     emit, user, &msg, &ctx->stats);
+  if (rc) ctx->err = msg;
+  return rc;
+}
+
+}  // extern "C"

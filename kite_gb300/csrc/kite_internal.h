@@ -1,0 +1,137 @@
+// Internal launch interface between the C-ABI orchestration (kite_gpu.cu) and
+// the kernel translation units.  Not part of the public ABI.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "kite_common.cuh"
+
+namespace kite {
+
+// One extraction work block: a byte range of one submitted chunk.
+struct BlockDesc {
+  uint64_t start;        // first byte (arena offset), 16-byte aligned
+  uint64_t end;          // one past the last byte
+  uint64_t chunk_start;  // arena offset of the chunk's first byte
+  uint32_t first_block;  // index of the chunk's first block
+  uint32_t flags;        // bit 1: block of the segment's first chunk (key sample source)
+};
+
+// A contiguous slice of one hash bucket's keys (level-2 tiling work unit).
+struct SliceDesc {
+  uint64_t start;   // key index
+  uint32_t len;     // keys
+  uint32_t bucket;
+};
+
+// A key-range tile: the on-chip sort unit.
+struct TileDesc {
+  uint64_t start;   // key index of the tile's first key
+  uint32_t len;     // keys in the tile
+  uint32_t bucket;
+};
+
+// Per-tile results of the sort + run-length reduction.
+template <class T>
+struct TileOut {
+  T first_key, last_key;
+  uint32_t rows;        // unique keys
+  uint32_t first_count;
+  uint64_t rest_bytes;  // DVLE bytes of rows 1..rows-1 (deltas inside the tile)
+};
+
+struct CountTotals {
+  unsigned long long reads, bases, kmers, samples;
+};
+
+template <class T>
+struct ExtractParams {
+  const uint8_t* arena;
+  const BlockDesc* blocks;
+  const unsigned long long* block_nl_excl;  // exclusive newline prefix per block (global order)
+  uint32_t k;
+  uint32_t canonical;
+  uint32_t shift;        // 64 - log2(partitions)
+  uint32_t partitions;
+  uint32_t blk_bytes;
+  // histogram pass
+  unsigned long long* bucket_count;  // [partitions]
+  CountTotals* totals;
+  T* sample;                         // may be null
+  unsigned int* sample_count;
+  uint32_t sample_cap;
+  uint32_t sample_mask;              // keep positions whose mixed hash & mask == 0
+  // scatter pass
+  const unsigned long long* bucket_off;  // [partitions] region start (key index)
+  unsigned long long* bucket_fill;       // [partitions]
+  T* keys_out;
+  DevStatus* status;
+};
+
+template <class T>
+struct TileSplitParams {
+  const T* keys_in;
+  T* keys_out;
+  const SliceDesc* slices;
+  const T* splitters;     // S-1 ascending keys
+  uint32_t S;             // tiles per bucket (power of two)
+  unsigned long long* tile_count;       // [P*S]
+  const unsigned long long* tile_off;   // [P*S]
+  unsigned long long* tile_fill;        // [P*S]
+  DevStatus* status;
+};
+
+// ---- launchers (count_kernels.cu) ----
+void launch_newline_count(const uint8_t* arena, const BlockDesc* blocks, uint32_t nblocks,
+                          unsigned long long* nl_out, cudaStream_t s);
+template <class T>
+void launch_extract_hist(const ExtractParams<T>& p, uint32_t nblocks, cudaStream_t s);
+template <class T>
+void launch_extract_scatter(const ExtractParams<T>& p, uint32_t nblocks, cudaStream_t s);
+template <class T>
+void launch_tile_hist(const TileSplitParams<T>& p, uint32_t nslices, uint32_t slice_keys, cudaStream_t s);
+template <class T>
+void launch_tile_scatter(const TileSplitParams<T>& p, uint32_t nslices, uint32_t slice_keys, cudaStream_t s);
+size_t extract_smem_bytes(int key_bytes, uint32_t blk_bytes, uint32_t partitions, bool scatter);
+uint32_t split_slice_keys(int key_bytes);
+
+// ---- scan.cu ----
+// Exclusive scan of n u64 values (in may equal out).  `tmp` needs
+// scan_tmp_elems(n) entries.
+size_t scan_tmp_elems(size_t n);
+void exclusive_scan_u64(const unsigned long long* in, unsigned long long* out, size_t n,
+                        unsigned long long* tmp, cudaStream_t s);
+
+// ---- sort_kernels.cu ----
+constexpr int kTileThreads = 512;
+template <class T> __host__ __device__ constexpr int tile_items() { return sizeof(T) == 8 ? 16 : 8; }
+template <class T> __host__ __device__ constexpr uint32_t tile_capacity() { return (uint32_t)(kTileThreads * tile_items<T>()); }
+
+template <class T>
+void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
+                      DevStatus* st, cudaStream_t s);
+// Oversized tiles (more keys than tile_capacity): one CTA per tile, LSD
+// passes through global memory with `scratch` (>= largest tile keys).
+template <class T>
+void launch_big_tile_sort(T* keys, uint32_t* counts, T* scratch, const TileDesc* tiles, const uint32_t* big_ids,
+                          uint32_t nbig, TileOut<T>* out, DevStatus* st, cudaStream_t s);
+
+// ---- encode_kernels.cu ----
+struct BucketMeta {
+  unsigned long long rows;
+  unsigned long long bytes;
+  unsigned long long byte_off;
+  unsigned long long kmin_lo, kmin_hi, kmax_lo, kmax_hi;
+};
+template <class T>
+void launch_tile_link(const TileOut<T>* tout, uint32_t P, uint32_t S, unsigned long long* tile_boff, T* tile_prev,
+                      BucketMeta* meta, cudaStream_t s);
+template <class T>
+void launch_encode(const T* keys, const uint32_t* counts, const TileDesc* tiles, const TileOut<T>* tout,
+                   const unsigned long long* tile_boff, const T* tile_prev, const BucketMeta* meta, uint32_t ntiles,
+                   uint8_t* out, unsigned long long out_cap, DevStatus* st, cudaStream_t s);
+void launch_bucket_offsets(BucketMeta* meta, uint32_t P, unsigned long long* tmp, cudaStream_t s);
+
+}  // namespace kite

@@ -1,0 +1,15 @@
+// GPU k-way merge of .kite inputs (kite merge).  Internal.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <cuda_runtime.h>
+
+#include "kite_gpu.h"
+
+namespace kite {
+
+int merge_run(int key_bytes, uint32_t partitions, const kite_gpu_merge_input* inputs, int n, cudaStream_t s,
+              uint32_t timeout_ms, kite_gpu_emit_fn emit, void* user, std::string* msg, kite_gpu_stats* st);
+
+}  // namespace kite

@@ -1,0 +1,67 @@
+// Device-wide exclusive prefix sum over u64 (reduce-then-scan, no inter-CTA
+// waiting).  Used for bucket/tile region offsets and newline prefixes.
+#include "kite_internal.h"
+
+namespace kite {
+
+static constexpr int kScanThreads = 256;
+static constexpr int kScanItems = 16;
+static constexpr size_t kScanTile = (size_t)kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const unsigned long long* __restrict__ in, size_t n,
+                                                              unsigned long long* __restrict__ sums) {
+  __shared__ unsigned long long sm[34];
+  const size_t base = blockIdx.x * kScanTile;
+  unsigned long long acc = 0;
+  for (int i = 0; i < kScanItems; ++i) {
+    const size_t idx = base + (size_t)i * kScanThreads + threadIdx.x;
+    if (idx < n) acc += in[idx];
+  }
+  unsigned long long total;
+  block_exclusive_scan<kScanThreads, unsigned long long>(acc, sm, &total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// Scans one tile per CTA in blocked order and adds the tile offset.
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile(const unsigned long long* __restrict__ in,
+                                                            unsigned long long* __restrict__ out, size_t n,
+                                                            const unsigned long long* __restrict__ offs) {
+  __shared__ unsigned long long sm[34];
+  const size_t base = blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+  unsigned long long v[kScanItems];
+  unsigned long long acc = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = (base + i < n) ? in[base + i] : 0ull;
+    acc += v[i];
+  }
+  unsigned long long total;
+  unsigned long long pre = block_exclusive_scan<kScanThreads, unsigned long long>(acc, sm, &total);
+  if (offs) pre += offs[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i < n) out[base + i] = pre;
+    pre += v[i];
+  }
+}
+
+size_t scan_tmp_elems(size_t n) {
+  size_t tiles = (n + kScanTile - 1) / kScanTile;
+  if (tiles <= 1) return 1;
+  return tiles + scan_tmp_elems(tiles);
+}
+
+void exclusive_scan_u64(const unsigned long long* in, unsigned long long* out, size_t n, unsigned long long* tmp,
+                        cudaStream_t s) {
+  if (n == 0) return;
+  const size_t tiles = (n + kScanTile - 1) / kScanTile;
+  if (tiles == 1) {
+    k_scan_tile<<<1, kScanThreads, 0, s>>>(in, out, n, nullptr);
+    return;
+  }
+  k_scan_reduce<<<(unsigned)tiles, kScanThreads, 0, s>>>(in, n, tmp);
+  exclusive_scan_u64(tmp, tmp, tiles, tmp + tiles, s);
+  k_scan_tile<<<(unsigned)tiles, kScanThreads, 0, s>>>(in, out, n, tmp);
+}
+
+}  // namespace kite

@@ -1,0 +1,376 @@
+// On-chip tile sort + run-length reduction (the sort/RLE of a flushed bucket:
+// radix_sort_u64_kmer / radix_sort_u128_kmer src/count/sorter.rs:67-93,
+// :388-437, then rle_compress_typed :514-530 with u32 saturation).
+//
+// A tile is a key range of one hash bucket.  One CTA loads the whole tile into
+// shared memory, sorts only the bits that vary inside it (LSD, 8-bit digits,
+// stable warp-match ranking), then emits unique (key, count) rows in place
+// and the tile's DVLE size for every row but the first.
+#include "kite_internal.h"
+
+namespace kite {
+
+template <class T>
+__device__ __forceinline__ T warp_min(T v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const T w = shfl_xor_key(v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+template <class T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const T w = shfl_xor_key(v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+
+// Block-wide min and max of the thread values (smem needs 2*NW keys).
+template <int NT, class T>
+__device__ __forceinline__ void block_minmax(T& mn, T& mx, T* red) {
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  mn = warp_min(mn);
+  mx = warp_max(mx);
+  if (lane == 0) {
+    red[wid] = mn;
+    red[NW + wid] = mx;
+  }
+  __syncthreads();
+  mn = red[0];
+  mx = red[NW];
+  for (int w = 1; w < NW; ++w) {
+    mn = red[w] < mn ? red[w] : mn;
+    mx = red[NW + w] > mx ? red[NW + w] : mx;
+  }
+  __syncthreads();
+}
+
+template <class T>
+__device__ __forceinline__ int varying_bits(T mn, T mx) {
+  const T x = mn ^ mx;
+  return x == T(0) ? 0 : KeyTraits<T>::kBits - clz_key(x);
+}
+
+template <class T>
+struct TileSmem {
+  static constexpr int NT = kTileThreads;
+  static constexpr int ITEMS = tile_items<T>();
+  static constexpr int CAP = NT * ITEMS;
+  static constexpr int NW = NT / 32;
+  static constexpr size_t buf_bytes = (size_t)CAP * sizeof(T);
+  static constexpr size_t hist_bytes = (size_t)256 * NW * 4;
+  static constexpr size_t head_bytes = ((size_t)(CAP + 1) * 2 + 15) & ~(size_t)15;
+  static constexpr size_t misc_bytes = 64 * 8 + 2 * NW * sizeof(T) + 256 * 8;
+  static constexpr size_t total = buf_bytes + hist_bytes + head_bytes + misc_bytes;
+};
+
+// Sort the n keys in buf (shared memory) over bits [0, nbits).
+template <class T>
+__device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, unsigned* warp_hist,
+                                                unsigned* scan_sm) {
+  constexpr int NT = kTileThreads, ITEMS = tile_items<T>();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned pos0 = (unsigned)wid * 32u * ITEMS + lane;
+  for (int shift = 0; shift < nbits; shift += 8) {
+    T key[ITEMS];
+    unsigned dig[ITEMS], dest[ITEMS];
+    bool valid[ITEMS];
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r) {
+      const unsigned pos = pos0 + r * 32u;
+      valid[r] = pos < n;
+      key[r] = valid[r] ? buf[pos] : T(0);
+      dig[r] = digit_of(key[r], shift);
+    }
+    block_rank<NT, ITEMS, 256>(dig, valid, dest, warp_hist, scan_sm, nullptr, nullptr);
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r)
+      if (valid[r]) buf[dest[r]] = key[r];
+    __syncthreads();
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kTileThreads, 1)
+    k_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, const TileDesc* __restrict__ tiles,
+                TileOut<T>* __restrict__ tout, DevStatus* st) {
+  using L = TileSmem<T>;
+  constexpr int NT = L::NT, ITEMS = L::ITEMS, NW = L::NW;
+  extern __shared__ __align__(16) uint8_t sm[];
+  T* buf = reinterpret_cast<T*>(sm);
+  unsigned* warp_hist = reinterpret_cast<unsigned*>(sm + L::buf_bytes);
+  unsigned short* head = reinterpret_cast<unsigned short*>(sm + L::buf_bytes + L::hist_bytes);
+  unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(sm + L::buf_bytes + L::hist_bytes + L::head_bytes);
+  unsigned* scan_sm = reinterpret_cast<unsigned*>(scan64);
+  T* red = reinterpret_cast<T*>(scan64 + 64);
+
+  const TileDesc td = tiles[blockIdx.x];
+  const unsigned n = td.len;
+  if (n > (unsigned)L::CAP) return;  // oversized tiles take the global-memory path
+  if (n == 0) {
+    if (threadIdx.x == 0) {
+      TileOut<T> o;
+      o.first_key = o.last_key = T(0);
+      o.rows = 0;
+      o.first_count = 0;
+      o.rest_bytes = 0;
+      tout[blockIdx.x] = o;
+    }
+    return;
+  }
+  T* g = keys + td.start;
+  T mn = ~T(0), mx = T(0);
+  for (unsigned i = threadIdx.x; i < n; i += NT) {
+    const T v = g[i];
+    buf[i] = v;
+    mn = v < mn ? v : mn;
+    mx = v > mx ? v : mx;
+  }
+  block_minmax<NT>(mn, mx, red);
+  smem_radix_sort<T>(buf, n, varying_bits(mn, mx), warp_hist, scan_sm);
+
+  // Run-length reduction: heads in blocked order.
+  const unsigned b0 = threadIdx.x * ITEMS;
+  unsigned nh = 0;
+#pragma unroll
+  for (int r = 0; r < ITEMS; ++r) {
+    const unsigned i = b0 + r;
+    if (i < n && (i == 0 || buf[i] != buf[i - 1])) nh++;
+  }
+  unsigned U;
+  unsigned u = block_exclusive_scan<NT, unsigned>(nh, scan_sm, &U);
+#pragma unroll
+  for (int r = 0; r < ITEMS; ++r) {
+    const unsigned i = b0 + r;
+    if (i < n && (i == 0 || buf[i] != buf[i - 1])) head[u++] = (unsigned short)i;
+  }
+  if (threadIdx.x == 0) head[U] = (unsigned short)n;
+  __syncthreads();
+  // n <= CAP <= 65535 fits the u16 head positions; head[U] = n may equal 65536
+  // only if CAP were 65536, which it is not.
+  unsigned long long rest = 0;
+  uint32_t* gc = counts + td.start;
+  for (unsigned v = threadIdx.x; v < U; v += NT) {
+    const unsigned i = head[v];
+    const unsigned c = (unsigned)head[v + 1] - i;
+    const T key = buf[i];
+    g[v] = key;
+    gc[v] = c;
+    if (v > 0) rest += (unsigned long long)(varint_len(key - buf[head[v - 1]]) + varint_len((uint64_t)c));
+  }
+  unsigned long long rest_total;
+  block_exclusive_scan<NT, unsigned long long>(rest, scan64, &rest_total);
+  if (threadIdx.x == 0) {
+    TileOut<T> o;
+    o.first_key = buf[head[0]];
+    o.first_count = (unsigned)head[1] - head[0];
+    o.last_key = buf[head[U - 1]];
+    o.rows = U;
+    o.rest_bytes = rest_total;
+    tout[blockIdx.x] = o;
+  }
+  (void)st;
+  (void)NW;
+}
+
+template <class T>
+void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
+                      DevStatus* st, cudaStream_t s) {
+  const size_t smem = TileSmem<T>::total;
+  cudaFuncSetAttribute(k_tile_sort<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (ntiles) k_tile_sort<T><<<ntiles, kTileThreads, smem, s>>>(keys, counts, tiles, out, st);
+}
+template void launch_tile_sort<uint64_t>(uint64_t*, uint32_t*, const TileDesc*, uint32_t, TileOut<uint64_t>*,
+                                         DevStatus*, cudaStream_t);
+template void launch_tile_sort<u128>(u128*, uint32_t*, const TileDesc*, uint32_t, TileOut<u128>*, DevStatus*,
+                                     cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Oversized tiles: one CTA, LSD passes through global memory.  Each pass
+// histograms the digit, then walks the tile in CAP-key chunks, ranks each
+// chunk stably on chip and appends every digit group at its running offset.
+// Then a chunked run-length reduction with carries between chunks.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(kTileThreads, 1)
+    k_big_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, T* __restrict__ scratch,
+                    const TileDesc* __restrict__ tiles, const uint32_t* __restrict__ big_ids,
+                    TileOut<T>* __restrict__ tout, DevStatus* st) {
+  using L = TileSmem<T>;
+  constexpr int NT = L::NT, ITEMS = L::ITEMS, CAP = L::CAP;
+  extern __shared__ __align__(16) uint8_t sm[];
+  T* buf = reinterpret_cast<T*>(sm);
+  unsigned* warp_hist = reinterpret_cast<unsigned*>(sm + L::buf_bytes);
+  unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(sm + L::buf_bytes + L::hist_bytes + L::head_bytes);
+  unsigned* scan_sm = reinterpret_cast<unsigned*>(scan64);
+  T* red = reinterpret_cast<T*>(scan64 + 64);
+  unsigned long long* run_off = reinterpret_cast<unsigned long long*>(red + 2 * L::NW);  // 256
+  unsigned* dtot = reinterpret_cast<unsigned*>(sm + L::buf_bytes + L::hist_bytes);        // 256 (head area)
+  unsigned* dstart = dtot + 256;                                                          // 256
+
+  const uint32_t tid = big_ids[blockIdx.x];
+  const TileDesc td = tiles[tid];
+  const unsigned long long n = td.len;
+  T* src = keys + td.start;
+  T* dst = scratch + td.start;
+
+  T mn = ~T(0), mx = T(0);
+  for (unsigned long long i = threadIdx.x; i < n; i += NT) {
+    const T v = src[i];
+    mn = v < mn ? v : mn;
+    mx = v > mx ? v : mx;
+  }
+  block_minmax<NT>(mn, mx, red);
+  if (mn == mx) {  // one key fills the tile: a single row
+    if (threadIdx.x == 0) {
+      keys[td.start] = mn;
+      counts[td.start] = n > 0xffffffffull ? 0xffffffffu : (uint32_t)n;
+      TileOut<T> o;
+      o.first_key = o.last_key = mn;
+      o.rows = 1;
+      o.first_count = counts[td.start];
+      o.rest_bytes = 0;
+      tout[tid] = o;
+    }
+    return;
+  }
+  const int nbits = varying_bits(mn, mx);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned pos0 = (unsigned)wid * 32u * ITEMS + lane;
+  for (int shift = 0; shift < nbits; shift += 8) {
+    // digit histogram
+    for (int d = threadIdx.x; d < 256; d += NT) warp_hist[d] = 0;
+    __syncthreads();
+    for (unsigned long long i = threadIdx.x; i < n; i += NT) atomicAdd(&warp_hist[digit_of(src[i], shift)], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long acc = 0;
+      for (int d = 0; d < 256; ++d) {
+        run_off[d] = acc;
+        acc += warp_hist[d];
+      }
+    }
+    __syncthreads();
+    for (unsigned long long c0 = 0; c0 < n; c0 += CAP) {
+      const unsigned cn = (unsigned)((n - c0) < (unsigned long long)CAP ? (n - c0) : CAP);
+      T key[ITEMS];
+      unsigned dig[ITEMS], dest[ITEMS];
+      bool valid[ITEMS];
+#pragma unroll
+      for (int r = 0; r < ITEMS; ++r) {
+        const unsigned pos = pos0 + r * 32u;
+        valid[r] = pos < cn;
+        key[r] = valid[r] ? src[c0 + pos] : T(0);
+        dig[r] = digit_of(key[r], shift);
+      }
+      block_rank<NT, ITEMS, 256>(dig, valid, dest, warp_hist, scan_sm, dtot, dstart);
+#pragma unroll
+      for (int r = 0; r < ITEMS; ++r)
+        if (valid[r]) dst[run_off[dig[r]] + (dest[r] - dstart[dig[r]])] = key[r];
+      __syncthreads();
+      for (int d = threadIdx.x; d < 256; d += NT) run_off[d] += dtot[d];
+      __syncthreads();
+    }
+    T* t = src;
+    src = dst;
+    dst = t;
+  }
+  // Run-length reduction of the sorted keys in src (keys or scratch).
+  // Pass A: unique keys to keys[start+u], head positions to counts[start+u].
+  T* ok = keys + td.start;
+  uint32_t* oc = counts + td.start;
+  unsigned long long U = 0;
+  for (unsigned long long c0 = 0; c0 < n; c0 += CAP) {
+    const unsigned cn = (unsigned)((n - c0) < (unsigned long long)CAP ? (n - c0) : CAP);
+    const unsigned b0 = threadIdx.x * ITEMS;
+    T kv[ITEMS];
+    bool hd[ITEMS];
+    unsigned nh = 0;
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r) {
+      const unsigned i = b0 + r;
+      hd[r] = false;
+      if (i < cn) {
+        const unsigned long long gi = c0 + i;
+        kv[r] = src[gi];
+        hd[r] = gi == 0 || kv[r] != src[gi - 1];
+        nh += hd[r];
+      }
+    }
+    unsigned tot;
+    unsigned long long u = U + block_exclusive_scan<NT, unsigned>(nh, scan_sm, &tot);
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r)
+      if (hd[r]) {
+        ok[u] = kv[r];
+        oc[u] = (uint32_t)(c0 + b0 + r);
+        u++;
+      }
+    U += tot;
+    __syncthreads();
+  }
+  // Pass B: head positions -> counts (saturating u32), DVLE rest bytes.
+  unsigned long long rest = 0;
+  for (unsigned long long c0 = 0; c0 < U; c0 += CAP) {
+    const unsigned cn = (unsigned)((U - c0) < (unsigned long long)CAP ? (U - c0) : CAP);
+    unsigned long long cnt[ITEMS];
+    T kv[ITEMS], kp[ITEMS];
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r) {
+      const unsigned i = threadIdx.x + r * NT;
+      cnt[r] = 0;
+      if (i < cn) {
+        const unsigned long long v = c0 + i;
+        const unsigned long long h0 = oc[v];
+        const unsigned long long h1 = (v + 1 < U) ? (unsigned long long)oc[v + 1] : n;
+        cnt[r] = h1 - h0;
+        kv[r] = ok[v];
+        kp[r] = v > 0 ? ok[v - 1] : T(0);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r) {
+      const unsigned i = threadIdx.x + r * NT;
+      if (i < cn) {
+        const unsigned long long v = c0 + i;
+        const uint32_t c = cnt[r] > 0xffffffffull ? 0xffffffffu : (uint32_t)cnt[r];
+        oc[v] = c;
+        if (v > 0) rest += (unsigned long long)(varint_len(kv[r] - kp[r]) + varint_len((uint64_t)c));
+      }
+    }
+    __syncthreads();
+  }
+  unsigned long long rest_total;
+  block_exclusive_scan<NT, unsigned long long>(rest, scan64, &rest_total);
+  if (threadIdx.x == 0) {
+    TileOut<T> o;
+    o.first_key = ok[0];
+    o.first_count = oc[0];
+    o.last_key = ok[U - 1];
+    o.rows = (uint32_t)U;
+    o.rest_bytes = rest_total;
+    tout[tid] = o;
+  }
+  (void)st;
+}
+
+template <class T>
+void launch_big_tile_sort(T* keys, uint32_t* counts, T* scratch, const TileDesc* tiles, const uint32_t* big_ids,
+                          uint32_t nbig, TileOut<T>* out, DevStatus* st, cudaStream_t s) {
+  const size_t smem = TileSmem<T>::total;
+  cudaFuncSetAttribute(k_big_tile_sort<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (nbig) k_big_tile_sort<T><<<nbig, kTileThreads, smem, s>>>(keys, counts, scratch, tiles, big_ids, out, st);
+}
+template void launch_big_tile_sort<uint64_t>(uint64_t*, uint32_t*, uint64_t*, const TileDesc*, const uint32_t*,
+                                             uint32_t, TileOut<uint64_t>*, DevStatus*, cudaStream_t);
+template void launch_big_tile_sort<u128>(u128*, uint32_t*, u128*, const TileDesc*, const uint32_t*, uint32_t,
+                                         TileOut<u128>*, DevStatus*, cudaStream_t);
+
+}  // namespace kite

@@ -1,0 +1,942 @@
+// libkite_host.so: .kite writer/reader, planner, FASTQ ingest, TSV dump and
+// the synthetic-input generator.  See include/kite_host.h for the contract and
+// the reference functions each part restates.
+#include "kite_host.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cerrno>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fcntl.h>
+#include <memory>
+#include <mutex>
+#include <queue>
+#include <string>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <thread>
+#include <unistd.h>
+#include <vector>
+
+#if KITE_HAVE_ZLIB
+#include <zlib.h>
+#endif
+
+typedef unsigned __int128 u128;
+
+namespace {
+
+constexpr uint64_t MiB = 1024ull * 1024ull;
+constexpr uint64_t GiB = 1024ull * MiB;
+
+thread_local std::string g_err;
+
+int set_err(const std::string& m, int code = -1) {
+  g_err = m;
+  return code;
+}
+
+inline void le(std::vector<uint8_t>& o, uint64_t v, int n) {
+  for (int i = 0; i < n; ++i) o.push_back((uint8_t)(v >> (8 * i)));
+}
+inline uint64_t rd(const uint8_t* p, int n) {
+  uint64_t v = 0;
+  for (int i = 0; i < n; ++i) v |= (uint64_t)p[i] << (8 * i);
+  return v;
+}
+
+// KiteHeader::write_to (src/format/header.rs:62-92): 128 bytes, LE.
+void header_image(const kite_header_info& h, uint64_t cio, uint64_t pto, uint64_t fo, uint64_t tc, uint64_t tr,
+                  uint8_t* out) {
+  std::vector<uint8_t> o;
+  o.reserve(128);
+  o.insert(o.end(), {'K', 'X', '2', '!'});
+  le(o, 1, 2);
+  o.push_back((uint8_t)h.k);
+  o.push_back(h.canonical ? 1 : 0);
+  le(o, h.partitions, 4);
+  le(o, h.key_width, 2);
+  le(o, h.codec_mask, 2);
+  le(o, 0, 4);
+  le(o, cio, 8);
+  le(o, pto, 8);
+  le(o, fo, 8);
+  le(o, tc, 8);
+  le(o, tr, 8);
+  uint8_t res[68] = {0};
+  if (h.has_min || h.has_max) {
+    memcpy(res, "KMT1", 4);
+    uint32_t flags = (h.has_min ? 1u : 0u) | (h.has_max ? 2u : 0u);
+    uint32_t mn = h.has_min ? h.min_count : 0, mx = h.has_max ? h.max_count : 0;
+    memcpy(res + 4, &flags, 4);
+    memcpy(res + 8, &mn, 4);
+    memcpy(res + 12, &mx, 4);
+  }
+  o.insert(o.end(), res, res + 68);
+  memcpy(out, o.data(), 128);
+}
+
+}  // namespace
+
+// ============================================================================
+// Writer: ConcurrentKiteWriter's layout for a single appending thread.
+// ============================================================================
+struct kite_writer {
+  struct Meta {
+    uint64_t off, rows, enc, raw;
+    uint32_t codec;
+    uint64_t kmin[4], kmax[4];
+  };
+  struct Pending {
+    uint64_t rel;
+    Meta m;
+  };
+  struct Part {
+    std::vector<uint8_t> buf;
+    std::vector<Pending> pending;
+    std::vector<Meta> committed;
+  };
+  kite_header_info h{};
+  uint64_t staging = 0, high = 0, low = 0, next_off = 128, staged = 0;
+  std::vector<Part> parts;
+  FILE* f = nullptr;
+  std::vector<uint8_t> image;  // in-memory mode
+  bool in_memory = false;
+  bool finalized = false;
+
+  int put(const uint8_t* p, size_t n, uint64_t* off) {
+    *off = next_off;
+    next_off += n;
+    if (in_memory) {
+      image.insert(image.end(), p, p + n);
+    } else if (n && fwrite(p, 1, n, f) != n) {
+      return set_err(std::string("write failed: ") + strerror(errno));
+    }
+    return 0;
+  }
+  int flush_part(size_t pid) {
+    Part& s = parts[pid];
+    if (s.buf.empty()) return 0;
+    uint64_t off;
+    if (put(s.buf.data(), s.buf.size(), &off)) return -1;
+    staged -= s.buf.size();
+    for (auto& pd : s.pending) {
+      Meta m = pd.m;
+      m.off = off + pd.rel;
+      s.committed.push_back(m);
+    }
+    s.pending.clear();
+    s.buf.clear();
+    return 0;
+  }
+  bool needs_drain() const { return staged >= high; }
+  int drain_one(bool* did) {
+    size_t best = SIZE_MAX, bytes = 0;
+    for (size_t p = 0; p < parts.size(); ++p)
+      if (parts[p].buf.size() > bytes) {
+        bytes = parts[p].buf.size();
+        best = p;
+      }
+    *did = best != SIZE_MAX;
+    return *did ? flush_part(best) : 0;
+  }
+  int drain_excess() {
+    for (int attempts = 0; staged > low && attempts < 4; ++attempts) {
+      bool did;
+      if (drain_one(&did)) return -1;
+      if (!did) break;
+    }
+    return 0;
+  }
+};
+
+extern "C" {
+
+const char* kite_host_last_error(void) { return g_err.c_str(); }
+
+uint64_t kite_suggest_write_lanes(uint64_t workers) {
+  return std::min<uint64_t>(std::max<uint64_t>((workers + 7) / 8, 2), 6);
+}
+
+kite_writer* kite_writer_open(const char* path, const kite_header_info* h, uint64_t staging_bytes,
+                              uint64_t write_lanes) {
+  if (!h || h->partitions == 0) {
+    set_err("bad writer arguments");
+    return nullptr;
+  }
+  auto* w = new kite_writer();
+  w->h = *h;
+  w->staging = staging_bytes;
+  w->high = std::max<uint64_t>(staging_bytes * write_lanes * 4, staging_bytes);
+  w->low = w->high / 2;
+  w->parts.resize(h->partitions);
+  uint8_t hdr[128];
+  header_image(*h, 0, 0, 0, 0, 0, hdr);
+  if (!path) {
+    w->in_memory = true;
+    w->image.assign(hdr, hdr + 128);
+  } else {
+    w->f = fopen(path, "wb+");
+    if (!w->f) {
+      set_err(std::string("failed to create ") + path + ": " + strerror(errno));
+      delete w;
+      return nullptr;
+    }
+    if (fwrite(hdr, 1, 128, w->f) != 128) {
+      set_err("header write failed");
+      fclose(w->f);
+      delete w;
+      return nullptr;
+    }
+  }
+  return w;
+}
+
+// append_chunk src/count/writer.rs:285-348
+int kite_writer_append(kite_writer* w, const kite_chunk_meta* m, const uint8_t* data, size_t n) {
+  if (!w || !m || m->partition_id >= w->parts.size()) return set_err("bad append");
+  auto& s = w->parts[m->partition_id];
+  if (!s.buf.empty() && s.buf.size() + n > w->staging)
+    if (w->flush_part(m->partition_id)) return -1;
+  kite_writer::Meta mm{};
+  mm.rows = m->row_count;
+  mm.enc = n;
+  mm.raw = m->raw_bytes;
+  mm.codec = m->codec;
+  memcpy(mm.kmin, m->key_min_lo, 16);
+  memcpy(mm.kmin + 2, m->key_min_hi, 16);
+  memcpy(mm.kmax, m->key_max_lo, 16);
+  memcpy(mm.kmax + 2, m->key_max_hi, 16);
+  if (n >= w->staging) {
+    if (w->put(data, n, &mm.off)) return -1;
+    s.committed.push_back(mm);
+  } else {
+    kite_writer::Pending pd{s.buf.size(), mm};
+    s.buf.insert(s.buf.end(), data, data + n);
+    s.pending.push_back(pd);
+    w->staged += n;
+    if (s.buf.size() >= w->staging)
+      if (w->flush_part(m->partition_id)) return -1;
+  }
+  if (w->needs_drain()) return w->drain_excess();
+  return 0;
+}
+
+int kite_writer_emit(void* w, const kite_chunk_meta* meta, const uint8_t* data, size_t len) {
+  return kite_writer_append(static_cast<kite_writer*>(w), meta, data, len) ? 1 : 0;
+}
+
+// CountWorker::flush_all's trailing loop (src/count/worker.rs:286-290)
+int kite_writer_worker_drain(kite_writer* w) {
+  while (w->needs_drain()) {
+    bool did;
+    if (w->drain_one(&did)) return -1;
+    if (!did) break;
+  }
+  return 0;
+}
+
+// finalize src/count/writer.rs:350-494
+int kite_writer_finalize(kite_writer* w, uint64_t* total_chunks, uint64_t* total_rows) {
+  if (!w || w->finalized) return set_err("writer already finalized");
+  std::vector<std::vector<kite_writer::Meta>> all(w->parts.size());
+  for (size_t p = 0; p < w->parts.size(); ++p) {
+    if (w->flush_part(p)) return -1;
+    all[p] = w->parts[p].committed;
+    std::sort(all[p].begin(), all[p].end(),
+              [](const kite_writer::Meta& a, const kite_writer::Meta& b) { return a.off < b.off; });
+  }
+  uint64_t data_end = w->next_off, tc = 0, tr = 0;
+  for (auto& v : all)
+    for (auto& c : v) {
+      tc++;
+      tr += c.rows;
+    }
+  const uint64_t cio = data_end, pto = cio + tc * 128, fo = pto + w->parts.size() * 40;
+  std::vector<uint8_t> t;
+  t.reserve(tc * 128 + w->parts.size() * 40 + 24);
+  for (size_t p = 0; p < all.size(); ++p)
+    for (auto& c : all[p]) {
+      le(t, p, 4);
+      le(t, c.codec, 4);
+      le(t, c.off, 8);
+      le(t, c.enc, 8);
+      le(t, c.raw, 8);
+      le(t, c.rows, 8);
+      for (int i = 0; i < 4; ++i) le(t, c.kmin[i], 8);
+      for (int i = 0; i < 4; ++i) le(t, c.kmax[i], 8);
+      for (int i = 0; i < 24; ++i) t.push_back(0);
+    }
+  uint64_t first = 0;
+  for (auto& v : all) {
+    uint64_t rows = 0, bytes = 0, minoff = UINT64_MAX;
+    for (auto& c : v) {
+      rows += c.rows;
+      bytes += c.enc;
+      minoff = std::min(minoff, c.off);
+    }
+    le(t, first, 8);
+    le(t, v.size(), 8);
+    le(t, rows, 8);
+    le(t, v.empty() ? 0 : minoff, 8);
+    le(t, bytes, 8);
+    first += v.size();
+  }
+  le(t, tc, 8);
+  le(t, tr, 8);
+  t.insert(t.end(), {'K', 'X', '2', 'F', 'O', 'O', 'T', '!'});
+  uint8_t hdr[128];
+  header_image(w->h, cio, pto, fo, tc, tr, hdr);
+  if (w->in_memory) {
+    w->image.insert(w->image.end(), t.begin(), t.end());
+    memcpy(w->image.data(), hdr, 128);
+  } else {
+    if (fseeko(w->f, (off_t)data_end, SEEK_SET) || fwrite(t.data(), 1, t.size(), w->f) != t.size() ||
+        fseeko(w->f, 0, SEEK_SET) || fwrite(hdr, 1, 128, w->f) != 128 || fflush(w->f))
+      return set_err(std::string("finalize write failed: ") + strerror(errno));
+    if (ftruncate(fileno(w->f), (off_t)(fo + 24))) return set_err("set_len failed");
+  }
+  w->finalized = true;
+  if (total_chunks) *total_chunks = tc;
+  if (total_rows) *total_rows = tr;
+  return 0;
+}
+
+const uint8_t* kite_writer_image(kite_writer* w, size_t* len) {
+  if (!w || !w->in_memory) return nullptr;
+  if (len) *len = w->image.size();
+  return w->image.data();
+}
+
+void kite_writer_close(kite_writer* w) {
+  if (!w) return;
+  if (w->f) fclose(w->f);
+  delete w;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Reader
+// ============================================================================
+struct kite_reader {
+  const uint8_t* data = nullptr;
+  size_t len = 0;
+  void* map = nullptr;
+  std::vector<uint8_t> own;
+  kite_header_info h{};
+  uint64_t cio = 0, pto = 0, fo = 0, total_chunks = 0, total_rows = 0;
+  std::vector<uint64_t> c_off, c_len, c_rows, p_first, p_count;
+  std::vector<uint32_t> c_codec;
+};
+
+namespace {
+
+int reader_parse(kite_reader* r) {
+  const uint8_t* p = r->data;
+  const size_t n = r->len;
+  if (n < 128 + 24) return set_err("file too small");
+  if (memcmp(p, "KX2!", 4)) return set_err("invalid magic: expected KITE");
+  if (rd(p + 4, 2) != 1) return set_err("unsupported version: " + std::to_string(rd(p + 4, 2)));
+  r->h.k = p[6];
+  r->h.canonical = p[7];
+  r->h.partitions = (uint32_t)rd(p + 8, 4);
+  r->h.key_width = (uint16_t)rd(p + 12, 2);
+  r->h.codec_mask = (uint16_t)rd(p + 14, 2);
+  r->cio = rd(p + 20, 8);
+  r->pto = rd(p + 28, 8);
+  r->fo = rd(p + 36, 8);
+  r->total_rows = rd(p + 52, 8);
+  if (!memcmp(p + 60, "KMT1", 4)) {
+    uint32_t flags = (uint32_t)rd(p + 64, 4);
+    r->h.has_min = (flags & 1) != 0;
+    r->h.has_max = (flags & 2) != 0;
+    r->h.min_count = (uint32_t)rd(p + 68, 4);
+    r->h.max_count = (uint32_t)rd(p + 72, 4);
+  }
+  if (r->fo + 24 > n) return set_err("footer out of bounds");
+  if (memcmp(p + r->fo + 16, "KX2FOOT!", 8)) return set_err("invalid footer magic");
+  r->total_chunks = rd(p + r->fo, 8);
+  const uint64_t P = r->h.partitions;
+  if (r->pto + P * 40 > n) return set_err("partition table out of bounds");
+  if (r->pto < r->cio) return set_err("invalid chunk index offsets");
+  if ((r->pto - r->cio) % 128) return set_err("chunk index size misaligned");
+  const uint64_t nc = (r->pto - r->cio) / 128;
+  for (uint64_t c = 0; c < nc; ++c) {
+    const uint8_t* e = p + r->cio + c * 128;
+    r->c_codec.push_back((uint32_t)rd(e + 4, 4));
+    r->c_off.push_back(rd(e + 8, 8));
+    r->c_len.push_back(rd(e + 16, 8));
+    r->c_rows.push_back(rd(e + 32, 8));
+  }
+  for (uint64_t b = 0; b < P; ++b) {
+    const uint8_t* e = p + r->pto + b * 40;
+    uint64_t first = rd(e, 8), cnt = rd(e + 8, 8);
+    if (first + cnt > nc) return set_err("partition " + std::to_string(b) + " chunk range out of bounds");
+    for (uint64_t c = first; c < first + cnt; ++c) {
+      if (r->c_len[c] == 0 || r->c_off[c] + r->c_len[c] > n)
+        return set_err("partition " + std::to_string(b) + " chunk out of bounds");
+      if (r->c_codec[c] & ~7u) return set_err("partition " + std::to_string(b) + " chunk uses unsupported codec mask");
+    }
+    r->p_first.push_back(first);
+    r->p_count.push_back(cnt);
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+kite_reader* kite_reader_open(const char* path) {
+  int fd = open(path, O_RDONLY);
+  if (fd < 0) {
+    set_err(std::string("failed to open ") + path + ": " + strerror(errno));
+    return nullptr;
+  }
+  struct stat st;
+  fstat(fd, &st);
+  auto* r = new kite_reader();
+  r->len = (size_t)st.st_size;
+  if (r->len) {
+    r->map = mmap(nullptr, r->len, PROT_READ, MAP_PRIVATE, fd, 0);
+    if (r->map == MAP_FAILED) {
+      close(fd);
+      set_err("mmap failed");
+      delete r;
+      return nullptr;
+    }
+    r->data = static_cast<const uint8_t*>(r->map);
+  }
+  close(fd);
+  if (reader_parse(r)) {
+    kite_reader_close(r);
+    return nullptr;
+  }
+  return r;
+}
+
+kite_reader* kite_reader_open_image(const uint8_t* data, size_t len) {
+  auto* r = new kite_reader();
+  r->own.assign(data, data + len);
+  r->data = r->own.data();
+  r->len = len;
+  if (reader_parse(r)) {
+    delete r;
+    return nullptr;
+  }
+  return r;
+}
+
+void kite_reader_close(kite_reader* r) {
+  if (!r) return;
+  if (r->map && r->map != MAP_FAILED) munmap(r->map, r->len);
+  delete r;
+}
+
+int kite_reader_header(const kite_reader* r, kite_header_info* h, uint64_t* tc, uint64_t* tr) {
+  if (!r) return -1;
+  if (h) *h = r->h;
+  if (tc) *tc = r->total_chunks;
+  if (tr) *tr = r->total_rows;
+  return 0;
+}
+
+int kite_reader_merge_input(const kite_reader* r, kite_gpu_merge_input* mi) {
+  if (!r || !mi) return -1;
+  mi->base = r->data;
+  mi->base_len = r->len;
+  mi->chunk_offset = r->c_off.data();
+  mi->chunk_len = r->c_len.data();
+  mi->chunk_rows = r->c_rows.data();
+  mi->chunk_codec = r->c_codec.data();
+  mi->part_first = r->p_first.data();
+  mi->part_count = r->p_count.data();
+  mi->has_min = r->h.has_min;
+  mi->has_max = r->h.has_max;
+  mi->min_count = r->h.min_count;
+  mi->max_count = r->h.max_count;
+  return 0;
+}
+
+int kite_count_passes_filter(uint64_t count, int has_min, uint32_t mn, int has_max, uint32_t mx) {
+  if (has_min && count < mn) return 0;
+  if (has_max && count > mx) return 0;
+  return 1;
+}
+
+// Segment streams of one partition merged by key with saturating u32 sums
+// (LoserTreeMerger src/dump/loser_tree.rs:141-175), header filter on the
+// summed count, 2-bit -> ACGT MSB first (decode_kmer_any src/dump/decoder.rs:27-50).
+int64_t kite_dump_partition(const kite_reader* r, uint32_t p, char** buf, size_t* cap, size_t* len) {
+  if (!r || p >= r->h.partitions) return set_err("bad partition");
+  const bool wide = r->h.key_width == 128;
+  if (r->h.key_width != 64 && r->h.key_width != 128) return set_err("unsupported key width for dump");
+  struct Stream {
+    const uint8_t* d;
+    size_t n, pos;
+    uint64_t left;
+    u128 prev;
+    bool dvle;
+    size_t es;
+    bool next(u128& k, uint32_t& c) {
+      if (!left) return false;
+      left--;
+      if (!dvle) {
+        if (pos + es > n) return false;
+        k = es == 12 ? (u128)rd(d + pos, 8) : ((u128)rd(d + pos + 8, 8) << 64) | rd(d + pos, 8);
+        c = (uint32_t)rd(d + pos + es - 4, 4);
+        pos += es;
+        return true;
+      }
+      if (pos == 0) {
+        const size_t kb = es - 4;
+        if (n < es) return false;
+        k = kb == 8 ? (u128)rd(d, 8) : ((u128)rd(d + 8, 8) << 64) | rd(d, 8);
+        c = (uint32_t)rd(d + kb, 4);
+        pos = es;
+        prev = k;
+        return true;
+      }
+      u128 delta = 0;
+      unsigned sh = 0;
+      for (size_t i = 0; pos < n && i < (es == 12 ? 10u : 19u); ++i) {
+        uint8_t b = d[pos++];
+        delta |= (u128)(b & 0x7f) << sh;
+        sh += 7;
+        if (!(b & 0x80)) break;
+      }
+      uint64_t cc = 0;
+      sh = 0;
+      for (size_t i = 0; pos < n && i < 10; ++i) {
+        uint8_t b = d[pos++];
+        cc |= (uint64_t)(b & 0x7f) << sh;
+        sh += 7;
+        if (!(b & 0x80)) break;
+      }
+      k = prev + delta;
+      prev = k;
+      c = (uint32_t)cc;
+      return true;
+    }
+  };
+  std::vector<Stream> ss;
+  for (uint64_t c = r->p_first[p]; c < r->p_first[p] + r->p_count[p]; ++c) {
+    if (r->c_codec[c] & 4u) return set_err("zstd chunks are not supported");
+    ss.push_back(Stream{r->data + r->c_off[c], (size_t)r->c_len[c], 0, r->c_rows[c], 0,
+                        (r->c_codec[c] & 2u) != 0, (size_t)(wide ? 20 : 12)});
+  }
+  struct Head {
+    u128 k;
+    uint32_t c;
+    size_t s;
+  };
+  auto cmp = [](const Head& a, const Head& b) { return a.k != b.k ? a.k > b.k : a.s > b.s; };
+  std::priority_queue<Head, std::vector<Head>, decltype(cmp)> pq(cmp);
+  for (size_t i = 0; i < ss.size(); ++i) {
+    Head h{0, 0, i};
+    if (ss[i].next(h.k, h.c)) pq.push(h);
+  }
+  const unsigned k = (unsigned)r->h.k;
+  static const char dna[4] = {'A', 'C', 'G', 'T'};
+  size_t start = *len;
+  while (!pq.empty()) {
+    const u128 key = pq.top().k;
+    uint32_t tot = 0;
+    while (!pq.empty() && pq.top().k == key) {
+      Head h = pq.top();
+      pq.pop();
+      tot = (tot > 0xffffffffu - h.c) ? 0xffffffffu : tot + h.c;
+      if (ss[h.s].next(h.k, h.c)) pq.push(h);
+    }
+    if (!kite_count_passes_filter(tot, r->h.has_min, r->h.min_count, r->h.has_max, r->h.max_count)) continue;
+    if (*len + k + 16 > *cap) {
+      size_t nc = std::max<size_t>(*cap * 2, *len + k + (1 << 20));
+      char* nb = static_cast<char*>(realloc(*buf, nc));
+      if (!nb) return set_err("out of memory");
+      *buf = nb;
+      *cap = nc;
+    }
+    char* o = *buf + *len;
+    for (unsigned i = 0; i < k; ++i) o[i] = dna[(unsigned)(key >> (2 * (k - 1 - i))) & 3];
+    o[k] = '\t';
+    int nn = snprintf(o + k + 1, 12, "%u", tot);
+    o[k + 1 + nn] = '\n';
+    *len += k + 2 + nn;
+  }
+  return (int64_t)(*len - start);
+}
+
+// ============================================================================
+// Memory spec, planner
+// ============================================================================
+int64_t kite_parse_memory_spec(const char* spec) {
+  const std::string s = spec ? spec : "";
+  auto bad = [&](const std::string& why) { return set_err("invalid memory size '" + s + "': " + why); };
+  bool digits = !s.empty() && std::all_of(s.begin(), s.end(), [](char c) { return c >= '0' && c <= '9'; });
+  if (digits) {
+    errno = 0;
+    unsigned long long v = strtoull(s.c_str(), nullptr, 10);
+    if (errno) return bad("expected formats like 512M, 64G, 1T, or raw bytes");
+    if (v == 0) return bad("value must be greater than zero");
+    return (int64_t)v;
+  }
+  if (s.size() < 2) return bad("expected formats like 512M, 64G, 1T, or raw bytes");
+  const char suf = s.back();
+  uint64_t mul = suf == 'M' ? MiB : suf == 'G' ? GiB : suf == 'T' ? 1024 * GiB : 0;
+  if (!mul) return bad("suffix must be M, G, or T");
+  const std::string num = s.substr(0, s.size() - 1);
+  if (num.empty() || !std::all_of(num.begin(), num.end(), [](char c) { return c >= '0' && c <= '9'; }))
+    return bad("numeric part must be a positive integer");
+  unsigned long long v = strtoull(num.c_str(), nullptr, 10);
+  if (v == 0) return bad("value must be greater than zero");
+  if (v > (unsigned long long)INT64_MAX / mul) return set_err("memory size '" + s + "' exceeds supported range");
+  return (int64_t)(v * mul);
+}
+
+// resolve_memory_limit_bytes src/runtime.rs:56-71: explicit spec, else 2/3 of
+// MemAvailable, else physical memory minus headroom.
+int64_t kite_resolve_memory_limit(const char* spec) {
+  if (spec && *spec) return kite_parse_memory_spec(spec);
+  FILE* f = fopen("/proc/meminfo", "r");
+  if (f) {
+    char line[256];
+    while (fgets(line, sizeof line, f)) {
+      unsigned long long kib;
+      if (sscanf(line, "MemAvailable: %llu", &kib) == 1) {
+        fclose(f);
+        uint64_t v = (uint64_t)kib * 1024 * 2 / 3;
+        if (v) return (int64_t)v;
+        f = nullptr;
+        break;
+      }
+    }
+    if (f) fclose(f);
+  }
+  long pages = sysconf(_SC_PHYS_PAGES), ps = sysconf(_SC_PAGESIZE);
+  if (pages <= 0 || ps <= 0) return set_err("sysconf(_SC_PHYS_PAGES/_SC_PAGESIZE) failed");
+  uint64_t total = (uint64_t)pages * (uint64_t)ps;
+  uint64_t head = std::min(std::max(total / 100, 512 * MiB), 2 * GiB);
+  return (int64_t)(total - head);
+}
+
+int kite_derive_plan(uint64_t input_bytes, double avg_read_len, int comp, int k, uint64_t req_partitions,
+                     uint64_t total_threads, uint64_t mem, int64_t buffer_mb, uint64_t chunk_kmers, kite_plan* out) {
+  const bool u64keys = k <= 31;
+  const uint64_t E = u64keys ? 1 : 2;
+  // target_partition_bytes_for src/count/mod.rs:961-974
+  const uint64_t base_mb = u64keys ? 640 : (k <= 64 ? 448 : 320);
+  uint64_t tmb;
+  if (u64keys && k >= 22) tmb = 192;
+  else if (k <= 21) tmb = base_mb + 64;
+  else if (k >= 52) tmb = base_mb - 64;
+  else tmb = base_mb;
+  const uint64_t target = tmb * MiB;
+  // target_worker_budget_bytes :883-890
+  uint64_t min_wb = u64keys ? 1250 * MiB : (k <= 64 ? 2 * GiB : 3 * GiB);
+  min_wb = std::min(min_wb, std::max(mem / 2, 512 * MiB));
+  uint64_t decomp = 1;
+  if (comp == KITE_INPUT_BGZF) {
+    uint64_t maxd = std::max<uint64_t>(total_threads / 2, 1);
+    uint64_t div = k <= 31 ? 4 : k <= 51 ? 5 : k <= 75 ? 6 : 8;
+    decomp = std::min(std::max<uint64_t>(total_threads / div, 1), maxd);
+  }
+  const uint64_t mmap_res = comp == KITE_INPUT_BGZF ? input_bytes : 0;
+  uint64_t untracked = mem / 6 + (total_threads + 3) * 8 * MiB + decomp * 32 * MiB;
+  untracked = std::min(std::max(untracked, 2 * GiB), 12 * GiB);
+  untracked = std::min(untracked, mem / 3) + mmap_res;
+  uint64_t workers = total_threads > decomp + 1 ? total_threads - decomp - 1 : 0;
+  workers = std::max<uint64_t>(workers, 1);
+  const bool auto_p = req_partitions == 0;
+  uint64_t P = req_partitions;
+  if (auto_p) {
+    // derive_partition_count :998-1016 then memory_thread_capped_partitions :923-942
+    double expansion = std::min(std::max(avg_read_len / 10.0, 4.0), 24.0);
+    uint64_t est = (uint64_t)((double)input_bytes * expansion * (double)E);
+    uint64_t raw = std::max<uint64_t>((est + target - 1) / target, 1);
+    uint64_t rp = 1;
+    while (rp < raw) rp <<= 1;
+    uint64_t derived = std::min<uint64_t>(std::max<uint64_t>(rp, 256), 2048);
+    uint64_t plan_mb = std::max<int64_t>(buffer_mb >= 0 ? buffer_mb : 8, 1);
+    uint64_t per = plan_mb * MiB + workers * 5 * 1024;
+    uint64_t capped = std::max<uint64_t>((mem / 4) / std::max<uint64_t>(per, 1), 256);
+    uint64_t fp = 1;
+    while ((fp << 1) <= capped) fp <<= 1;
+    P = std::min<uint64_t>(std::max<uint64_t>(std::min(derived, fp), 256), 2048);
+  }
+  std::vector<uint64_t> cands;
+  if (buffer_mb >= 0) {
+    uint64_t req = std::max<int64_t>(buffer_mb, 1);
+    for (uint64_t v : {req, (uint64_t)16, (uint64_t)8, (uint64_t)4, (uint64_t)2, (uint64_t)1})
+      if (v <= req) cands.push_back(v);
+  } else {
+    cands = {16, 8, 4, 2};
+  }
+  std::sort(cands.rbegin(), cands.rend());
+  cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
+  size_t si = 0;
+  for (;;) {
+    const uint64_t staging = cands[si] * MiB;
+    uint64_t chunk = chunk_kmers ? std::min(std::max(chunk_kmers * 2, 8 * MiB), 64 * MiB)
+                                 : std::min(std::max(mem / (workers * 96), 8 * MiB), 64 * MiB);
+    uint64_t qbase = comp == KITE_INPUT_PLAIN ? 8 : std::min<uint64_t>(std::max<uint64_t>(decomp * 2, 8), 64);
+    uint64_t queue = std::min(qbase, std::min<uint64_t>(std::max<uint64_t>(mem / GiB, 8), 64));
+    uint64_t dbud = chunk * queue;
+    uint64_t reserved = dbud + P * staging + workers * 48 * MiB + untracked;
+    uint64_t tracked = mem > untracked + dbud ? mem - untracked - dbud : 0;
+    uint64_t wb = (mem > reserved ? mem - reserved : 0) / workers;
+    uint64_t lf = std::max(wb * 45 / 100, std::max(chunk * 2, staging * 4));
+    if (reserved < mem && tracked > 0 && wb >= min_wb) {
+      out->partitions = P;
+      out->chunk_size_bytes = chunk;
+      out->staging_bytes = staging;
+      out->worker_threads = workers;
+      out->local_flush_bytes = lf;
+      out->decomp_threads = decomp;
+      out->writer_lanes = kite_suggest_write_lanes(workers);
+      out->queue_depth = queue;
+      out->avg_read_len = avg_read_len;
+      return 0;
+    }
+    if (si + 1 < cands.size()) {
+      si++;
+      continue;
+    }
+    if (workers > 1) {
+      workers--;
+      si = 0;
+      continue;
+    }
+    if (auto_p && P > 256) {
+      P /= 2;
+      si = 0;
+      continue;
+    }
+    return set_err("unable to derive count heuristic plan within memory budget " + std::to_string(mem) + " bytes");
+  }
+}
+
+// ============================================================================
+// Input: sniffing and chunked readers
+// ============================================================================
+int kite_detect_compression(const char* path) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return set_err(std::string("failed to inspect input FASTQ compression.\nInput: ") + path);
+  uint8_t h[18];
+  size_t n = fread(h, 1, 18, f);
+  fclose(f);
+  if (n < 2 || h[0] != 0x1f || h[1] != 0x8b) return KITE_INPUT_PLAIN;
+  if (n >= 18 && (h[3] & 0x04)) {
+    size_t xlen = (size_t)h[10] | ((size_t)h[11] << 8);
+    if (xlen >= 6 && h[12] == 0x42 && h[13] == 0x43) return KITE_INPUT_BGZF;
+  }
+  return KITE_INPUT_GZIP;
+}
+
+}  // extern "C"
+
+struct kite_input {
+  FILE* f = nullptr;
+#if KITE_HAVE_ZLIB
+  gzFile gz = nullptr;
+#endif
+  uint64_t chunk = 0;
+  std::vector<uint8_t> carry;
+  bool eof = false;
+  size_t read_raw(uint8_t* dst, size_t want) {
+    size_t total = 0;
+#if KITE_HAVE_ZLIB
+    if (gz) {
+      while (total < want) {
+        int r = gzread(gz, dst + total, (unsigned)std::min<size_t>(want - total, 1u << 30));
+        if (r <= 0) {
+          if (r < 0) {
+            int e;
+            g_err = std::string("decompress_error: ") + gzerror(gz, &e);
+          }
+          break;
+        }
+        total += (size_t)r;
+      }
+      return total;
+    }
+#endif
+    while (total < want) {
+      size_t r = fread(dst + total, 1, want - total, f);
+      if (r == 0) break;
+      total += r;
+    }
+    return total;
+  }
+};
+
+extern "C" {
+
+kite_input* kite_input_open(const char* path, uint64_t chunk_size) {
+  int comp = kite_detect_compression(path);
+  if (comp < 0) return nullptr;
+  auto* in = new kite_input();
+  in->chunk = chunk_size;
+  if (comp == KITE_INPUT_PLAIN) {
+    in->f = fopen(path, "rb");
+    if (!in->f) {
+      set_err(std::string("failed to open input FASTQ.\nInput: ") + path);
+      delete in;
+      return nullptr;
+    }
+    setvbuf(in->f, nullptr, _IOFBF, 2 << 20);
+  } else {
+#if KITE_HAVE_ZLIB
+    in->gz = gzopen(path, "rb");
+    if (!in->gz) {
+      set_err(std::string("failed to open input FASTQ.\nInput: ") + path);
+      delete in;
+      return nullptr;
+    }
+    gzbuffer(in->gz, 1 << 20);
+#else
+    set_err("gzip input needs zlib, which this build lacks");
+    delete in;
+    return nullptr;
+#endif
+  }
+  return in;
+}
+
+uint64_t kite_input_max_chunk(const kite_input* in) { return in->chunk + in->chunk; }
+
+// next_chunk: carry + chunk_size new bytes; on a full read cut after the last
+// 4k-th newline and carry the rest (src/count/decompress.rs:36-81).
+int64_t kite_input_next(kite_input* in, uint8_t* dst, size_t cap) {
+  const size_t c = in->carry.size();
+  if (cap < c + in->chunk) return set_err("input buffer too small");
+  if (c) memcpy(dst, in->carry.data(), c);
+  in->carry.clear();
+  const size_t got = in->eof ? 0 : in->read_raw(dst + c, in->chunk);
+  if (!g_err.empty() && got < in->chunk && g_err.rfind("decompress_error", 0) == 0) {
+    // the reference logs the error and stops reading (src/count/mod.rs:471-474)
+    fprintf(stderr, "[kite count] %s\n", g_err.c_str());
+    g_err.clear();
+  }
+  const size_t len = c + got;
+  if (len == 0) return 0;
+  if (got < in->chunk) {
+    in->eof = true;
+    return (int64_t)len;
+  }
+  size_t nl = 0, last = 0;
+  for (size_t i = 0; i < len; ++i)
+    if (dst[i] == '\n' && (++nl & 3) == 0) last = i + 1;
+  if (last == 0 || last >= len) return (int64_t)len;
+  in->carry.assign(dst + last, dst + len);
+  return (int64_t)last;
+}
+
+void kite_input_close(kite_input* in) {
+  if (!in) return;
+  if (in->f) fclose(in->f);
+#if KITE_HAVE_ZLIB
+  if (in->gz) gzclose(in->gz);
+#endif
+  delete in;
+}
+
+// sample_input src/count/mod.rs:1018-1079 (plain/gzip): 8 MiB chunks until
+// >= 200,000 reads or >= 32 MiB decompressed; mean sequence-line length.
+double kite_sample_avg_read_len(const char* path, int comp) {
+  (void)comp;
+  kite_input* in = kite_input_open(path, 8 * MiB);
+  if (!in) return 150.0;
+  std::vector<uint8_t> buf(16 * MiB + 64);
+  uint64_t reads = 0, bases = 0, decomp = 0;
+  while (reads < 200000 && decomp < 32 * MiB) {
+    int64_t n = kite_input_next(in, buf.data(), buf.size());
+    if (n <= 0) break;
+    decomp += (uint64_t)n;
+    if (buf[0] != '@') continue;
+    int state = 0;
+    size_t seq_start = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      if (buf[i] != '\n') continue;
+      if (state == 0) {
+        state = 1;
+        seq_start = (size_t)i + 1;
+      } else if (state == 1) {
+        if ((size_t)i > seq_start) {
+          reads++;
+          bases += (size_t)i - seq_start;
+        }
+        state = 2;
+      } else {
+        state = state == 2 ? 3 : 0;
+      }
+    }
+    if (state == 1 && seq_start < (size_t)n) {
+      reads++;
+      bases += (size_t)n - seq_start;
+    }
+  }
+  kite_input_close(in);
+  return reads ? (double)bases / (double)reads : 150.0;
+}
+
+// ============================================================================
+// Synthetic reads
+// ============================================================================
+int64_t kite_synth_reads(const uint8_t* genome, uint64_t glen, uint64_t n_reads, uint32_t L, double sub_rate,
+                         double n_rate, double rc_frac, uint64_t seed, uint64_t first_index, uint8_t* out,
+                         uint64_t cap, int threads) {
+  const uint64_t rec = 11 + 1 + L + 1 + 2 + L + 1;
+  if (glen < L || n_reads * rec > cap) return set_err("synth: bad sizes");
+  const int nt = std::max(1, threads);
+  auto work = [&](uint64_t r0, uint64_t r1) {
+    for (uint64_t r = r0; r < r1; ++r) {
+      // splitmix64 stream per read: deterministic regardless of thread count
+      uint64_t st = seed * 0x9E3779B97F4A7C15ull + (first_index + r) * 0xD1B54A32D192ED03ull;
+      auto next = [&]() {
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+      };
+      auto unif = [&]() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); };
+      uint8_t* o = out + r * rec;
+      const uint64_t idx = first_index + r;
+      o[0] = '@';
+      o[1] = 'r';
+      for (int d = 0; d < 9; ++d) {
+        uint64_t p = 1;
+        for (int e = 0; e < 8 - d; ++e) p *= 10;
+        o[2 + d] = (uint8_t)('0' + (idx / p) % 10);
+      }
+      o[11] = '\n';
+      const uint64_t start = next() % (glen - L + 1);
+      const bool minus = unif() < rc_frac;
+      uint8_t* s = o + 12;
+      static const char dna[4] = {'A', 'C', 'G', 'T'};
+      for (uint32_t i = 0; i < L; ++i) {
+        uint8_t c = minus ? (uint8_t)(3 - genome[start + L - 1 - i]) : genome[start + i];
+        if (sub_rate > 0 && unif() < sub_rate) c = (uint8_t)((c + 1 + next() % 3) & 3);
+        s[i] = (uint8_t)dna[c];
+        if (n_rate > 0 && unif() < n_rate) s[i] = 'N';
+      }
+      o[12 + L] = '\n';
+      o[13 + L] = '+';
+      o[14 + L] = '\n';
+      memset(o + 15 + L, 'I', L);
+      o[15 + 2 * L] = '\n';
+    }
+  };
+  std::vector<std::thread> th;
+  const uint64_t per = (n_reads + nt - 1) / nt;
+  for (int t = 0; t < nt; ++t) {
+    uint64_t a = t * per, b = std::min<uint64_t>(n_reads, a + per);
+    if (a < b) th.emplace_back(work, a, b);
+  }
+  for (auto& x : th) x.join();
+  return (int64_t)(n_reads * rec);
+}
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+"""GPU count path vs the CPU oracle: bit-exact partition payloads (DVLE
+bytes), row counts, key ranges and the reads/bases/kmers summary.  Integer
+work: the bar is byte equality."""
+import numpy as np
+import pytest
+
+from kite_gb300 import synth
+from gpu_helpers import assert_parity, gpu_count
+
+pytestmark = pytest.mark.gpu
+
+
+EDGE = [
+    b"",
+    b"@r\nACGT\n+\nIIII\n",
+    b"@r\nACGTNACGTTGCA\n+\nIIIIIIIIIIIII\n@s\n\n+\n\n@t\nacgtacgtACGTtt\n+\nIIIIIIIIIIIIII\n",
+    b"@r\r\nACGTACGTAC\r\n+\r\nIIIIIIIIII\r\n",
+    b"@r\nACGTACGTACGGATTACA\n+\nIIIIIIIIIIIIIIIIII\n@u\nGGGATTACAGATTACACC",  # unterminated seq line
+    b"NOTFASTQ\nACGTACGT\n+\nIIIIIIII\n",  # chunk not starting with '@' is ignored
+    b"@q\nACGTACGTAC\n+\n@IIIIIIIII\n@r\nTTTTGGGGCCCCAAAA\n+\nIIIIIIIIIIIIIIII\n",  # '@' in quality
+]
+
+
+@pytest.mark.parametrize("k,canonical", [(1, False), (3, True), (21, False), (31, True), (32, True), (33, False),
+                                         (63, True), (64, False), (64, True)])
+@pytest.mark.parametrize("case", range(len(EDGE)))
+def test_edge_inputs(gpu, orc, case, k, canonical):
+    assert_parity(gpu, orc, EDGE[case], k, canonical, 4)
+
+
+@pytest.mark.parametrize("P", [2, 16, 256, 2048])
+def test_partitions(gpu, orc, P):
+    fq = synth.small_workload(seed=11, n_reads=3000, genome_len=20_000)
+    assert_parity(gpu, orc, fq, 21, False, P)
+
+
+@pytest.mark.parametrize("k,canonical", [(21, False), (31, True), (47, True), (63, True)])
+def test_small_workload(gpu, orc, k, canonical):
+    fq = synth.small_workload(seed=7, n_reads=20_000, genome_len=200_000)
+    assert_parity(gpu, orc, fq, k, canonical, 16, chunk_size=300_000)
+
+
+def test_tiled_buckets_u64(gpu, orc):
+    # enough k-mers per bucket to need key-range tiles (and several chunks)
+    fq = synth.small_workload(seed=1, n_reads=60_000, genome_len=1_000_000)
+    st = assert_parity(gpu, orc, fq, 21, False, 2, chunk_size=1 << 20)
+    assert st["tiles_per_bucket"] > 1
+
+
+def test_tiled_buckets_u128(gpu, orc):
+    fq = synth.small_workload(seed=2, n_reads=40_000, genome_len=500_000)
+    st = assert_parity(gpu, orc, fq, 63, True, 2, chunk_size=1 << 20)
+    assert st["tiles_per_bucket"] > 1
+
+
+def test_heavy_hitter_oversized_tile(gpu, orc):
+    # poly-A reads: one key with a huge count fills a tile beyond on-chip capacity
+    rng = np.random.default_rng(3)
+    g = synth.genome_iid(rng, 50_000)
+    fq = synth.reads_fixed(rng, g, 4000, 150, 0.0) + (b"@a\n" + b"A" * 150 + b"\n+\n" + b"I" * 150 + b"\n") * 3000
+    st = assert_parity(gpu, orc, fq, 21, True, 2)
+    assert st["big_tiles"] >= 1
+
+
+def test_heavy_mixed_big_tile(gpu, orc):
+    # a low-complexity region: few distinct keys, many copies, in a tiled bucket
+    rng = np.random.default_rng(9)
+    g = synth.genome_iid(rng, 400_000)
+    g[:2000] = np.tile(np.array([0, 1], dtype=np.uint8), 1000)
+    fq = synth.reads_fixed(rng, g, 40_000, 150, 0.0)
+    fq += synth.reads_fixed(rng, g[:2200], 20_000, 150, 0.0)
+    assert_parity(gpu, orc, fq, 31, False, 2)
+
+
+def test_segments_flush(gpu, orc):
+    # a small arena forces several segments: partitions then hold several
+    # chunks; compare through dump TSV equality (counts summed across chunks)
+    fq = synth.small_workload(seed=5, n_reads=5000, genome_len=30_000)
+    from kite_gb300 import ingest
+    chunks = ingest.split_chunks(fq, 100_000)
+    rows = {}
+    with gpu.Counter(21, False, 8, arena_bytes=256 * 1024) as c:
+        for o, l in chunks:
+            try:
+                c.submit(fq[o:o + l])
+            except gpu.KiteGpuError as e:
+                assert e.code == -9
+                for m, p in c.finish():
+                    rows.setdefault(m["partition_id"], []).append(p)
+                c.submit(fq[o:o + l])
+        for m, p in c.finish():
+            rows.setdefault(m["partition_id"], []).append(p)
+        assert c.stats()["segments"] >= 2
+    assert max(len(v) for v in rows.values()) >= 2
