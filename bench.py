@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""Benchmark: exact k-mer counting throughput on one GB300 (k-mers/s).
+
+Workload (the 10M-read k=31 configuration): seeded 50 Mbp genome (80% i.i.d.
+ACGT, 20% copies of 100 distinct 2 kbp repeat elements at 1% per-copy
+divergence), 10,000,000 reads of 150 bp, strand 50/50, 1% substitutions,
+0.1% N; k=31 canonical, 256 partitions (the planner's choice for this input),
+sampled-histogram splitters.  One step = one full count of the whole input:
+FASTQ bytes -> per-partition DVLE payloads of sorted (k-mer, count) rows.
+
+  value  input already resident in HBM (kite_gpu_count_submit_device),
+         device time of K steps from CUDA events on the counting stream.
+  e2e    the same count through the C ABI from pinned host memory: H2D of
+         the FASTQ and D2H of every partition payload inside the timed region.
+
+--impl reference times the CPU restatement of the reference's count (the
+oracle port: per-thread hash-bucket workers, sort, RLE, DVLE) on the host
+cores on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+K = 31
+CANONICAL = True
+PARTITIONS = 256
+READ_LEN = 150
+CHUNK = 64 << 20
+METRIC = "exact k-mers/s at k=31 (canonical, 10M x 150 bp reads)"
+UNIT = "k-mers/s"
+
+
+def gen_workload(n_reads: int, seed: int = 2):
+    from kite_gb300 import host, synth
+    rng = np.random.default_rng(seed)
+    genome = synth.genome_with_repeats(rng, 50_000_000)
+    data = host.synth_reads(genome, n_reads, READ_LEN, 0.01, 0.001, 0.5, seed=seed,
+                            threads=max(1, os.cpu_count() or 1))
+    return data
+
+
+def chunk_layout(data) -> list:
+    from kite_gb300 import ingest
+    return ingest.split_chunks(data, CHUNK)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks() -> tuple:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json, copy burst)"
+    return 6800.0, "fallback"
+
+
+def stage_bytes(st: dict, fastq_bytes: int) -> dict:
+    """Algorithmic bytes per stage for one step (w = 8-byte keys)."""
+    w = 8
+    N = st["kmers"]
+    d = st["rows"]
+    E = st["payload_bytes"]
+    return {
+        0: ("k_newline_count", fastq_bytes),
+        1: ("k_extract<hist>", fastq_bytes),
+        2: ("k_extract<scatter>", fastq_bytes + N * w),
+        3: ("k_tile_hist+k_tile_scatter", 3 * N * w),
+        4: ("k_tile_sort", N * w + d * (w + 4)),
+        5: ("k_big_tile_sort", 0),
+        6: ("k_encode", d * (w + 4) + E),
+    }
+
+
+def ncu_traffic(kernel_family: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/ncu_count_kernels.json), scaled to this workload."""
+    p = ROOT / "profiles" / "ncu_count_kernels.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        ent = d["kernels"].get(kernel_family)
+        return ent
+    except Exception:
+        return None
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("KITE_BENCH_GLOO") is None else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v: float) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(world, v: float) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_baseline(data, layout, reads_sample: int, threads: int) -> dict:
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.lib()
+    # the first reads_sample records (fixed-length records)
+    rec_len = 11 + 1 + READ_LEN + 1 + 2 + READ_LEN + 1
+    n = min(len(data), reads_sample * rec_len)
+    sample = bytes(memoryview(data)[:n])
+    workers = max(1, threads - 2)  # reader + writer threads as in the reference plan
+    r = oracle.count_buffer(sample, K, CANONICAL, PARTITIONS, workers)
+    secs = r["ns"] / 1e9
+    return {"value": r["kmers"] / secs, "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": f"first {reads_sample:,} reads ({n / 1e6:.0f} MB) of the workload, {workers} worker threads",
+            "seconds": secs, "kmers": r["kmers"]}
+
+
+def run_reference(args):
+    world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    reads_sample = args.ref_reads
+    data = gen_workload(reads_sample)
+    layout = None
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(data, layout, reads_sample, threads)
+        if i >= args.warmup:
+            vals.append(cb)
+    v = statistics.median(c["value"] for c in vals)
+    ms = statistics.median(c["seconds"] for c in vals) * 1e3
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": f"same shape as the GPU arm, bounded sample of {reads_sample:,} reads",
+                       "k": K, "canonical": CANONICAL, "partitions": PARTITIONS},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--reads", type=int, default=10_000_000)
+    ap.add_argument("--ref-reads", type=int, default=2_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-splitter-compare", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    world, rank, local = dist_setup()
+    import torch
+    torch.cuda.set_device(local)
+    from kite_gb300 import gpu
+
+    data = gen_workload(args.reads, seed=2 + rank)  # each rank counts its own replica (weak scaling)
+    layout = chunk_layout(data)
+    total = len(data)
+    # device-resident copy, every chunk at a 16-byte aligned offset, 16 pad bytes after each
+    offs = []
+    pos = 0
+    for o, l in layout:
+        offs.append(pos)
+        pos = (pos + l + 16 + 15) & ~15
+    dev = torch.zeros(pos + 64, dtype=torch.uint8, device="cuda")
+    host_t = torch.frombuffer(data, dtype=torch.uint8)
+    for (o, l), d in zip(layout, offs):
+        dev[d:d + l].copy_(host_t[o:o + l])
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    base = dev.data_ptr()
+
+    def device_step(c):
+        for (o, l), d in zip(layout, offs):
+            c.submit_device(base + d, l)
+        c.finish(collect=False)
+
+    c = gpu.Counter(K, CANONICAL, PARTITIONS, device=local, splitter_mode=gpu.SPLIT_SAMPLED,
+                    stream=stream.cuda_stream)
+    for _ in range(args.warmup):
+        device_step(c)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    stage_sum = [0.0] * 12
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        device_step(c)
+        st = c.stats()
+        launches += st["kernel_launches"]
+        for i in range(12):
+            stage_sum[i] += st["stage_ms"][i]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ms_total = e0.elapsed_time(e1)
+    ms_total = max_over_ranks(world, ms_total)
+    kmers = st["kmers"]
+    value = sum_over_ranks(world, kmers * args.steps) / (ms_total / 1e3)
+
+    # ---- roofline of the dominant kernel ----
+    stages = stage_bytes(st, total)
+    avg_ms = {i: stage_sum[i] / args.steps for i in stages}
+    dom = max(stages, key=lambda i: avg_ms[i])
+    name, algo_bytes = stages[dom]
+    peak, peak_src = peaks()
+    achieved = algo_bytes / (avg_ms[dom] / 1e3) / 1e9
+    tr = ncu_traffic(name)
+    traffic = None
+    if tr and tr.get("dram_bytes_per_key") is not None:
+        traffic = tr["dram_bytes_per_key"] * kmers
+    sort_ms = avg_ms[3] + avg_ms[4] + avg_ms[5]
+    sort_bytes = stages[3][1] + stages[4][1]
+    roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                "algorithmic_bytes": algo_bytes, "kernel_ms": avg_ms[dom],
+                "sort_gbs": sort_bytes / (sort_ms / 1e3) / 1e9 if sort_ms > 0 else None,
+                "sort_frac": (sort_bytes / (sort_ms / 1e3) / 1e9) / peak if sort_ms > 0 else None,
+                "stage_ms": {stages[i][0]: round(avg_ms[i], 4) for i in stages}}
+
+    # ---- learned vs sampled splitters on the same input (identical output) ----
+    splitters = None
+    if not args.no_splitter_compare:
+        cl = gpu.Counter(K, CANONICAL, PARTITIONS, device=local, splitter_mode=gpu.SPLIT_LEARNED,
+                         imbalance_bound=10.0, stream=stream.cuda_stream)
+        device_step(cl)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 2
+        for _ in range(reps):
+            device_step(cl)
+        torch.cuda.synchronize()
+        tl = (time.perf_counter() - t0) / reps
+        stl = cl.stats()
+        cl.close()
+        splitters = {"sampled": {"kmers_per_s": value / world, "tile_imbalance": st["tile_imbalance"],
+                                 "big_tiles": st["big_tiles"]},
+                     "learned": {"kmers_per_s": kmers / tl, "tile_imbalance": stl["tile_imbalance"],
+                                 "big_tiles": stl["big_tiles"], "mlp_loss": stl["mlp_loss"],
+                                 "predicted_imbalance": stl["mlp_pred_imbalance"],
+                                 "used": stl["splitter_used"] == gpu.SPLIT_LEARNED}}
+
+    # ---- e2e through the C ABI from pinned host memory ----
+    pinned = torch.empty(total, dtype=torch.uint8).pin_memory()
+    pinned.copy_(host_t)
+    pbase = pinned.data_ptr()
+    d2h = [0]
+
+    def e2e_step(cc):
+        for o, l in layout:
+            cc.submit((pbase + o, l))
+        out_bytes = 0
+
+        def cb(meta, payload):
+            nonlocal out_bytes
+            out_bytes += len(payload)
+        cc.finish(collect=True, callback=cb)
+        d2h[0] = out_bytes
+
+    ce = gpu.Counter(K, CANONICAL, PARTITIONS, device=local, splitter_mode=gpu.SPLIT_SAMPLED)
+    e2e_step(ce)
+    ce.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step(ce)
+    ce.synchronize()
+    barrier(world)
+    te = max_over_ranks(world, time.perf_counter() - t0)
+    e2e_val = sum_over_ranks(world, kmers * args.steps) / te
+    ce.close()
+    c.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(data, layout, args.ref_reads, os.cpu_count() or 1)
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded)",
+                "config": {"workload": f"{args.reads:,} x {READ_LEN} bp reads, 50 Mbp genome with 20% repeats, "
+                                       f"1% subs, 0.1% N, strand 50/50; k={K} canonical; {PARTITIONS} partitions; "
+                                       "sampled-histogram splitters",
+                           "reads": args.reads, "k": K, "canonical": CANONICAL, "partitions": PARTITIONS,
+                           "fastq_bytes": total, "kmers_per_step": kmers, "rows_per_step": st["rows"],
+                           "payload_bytes_per_step": st["payload_bytes"],
+                           "l2": "inputs larger than L2 (FASTQ and keys are GBs; no flush needed)",
+                           "parallelism": f"replicas x{world}"},
+                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": total, "d2h_bytes_per_step": d2h[0]},
+                "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+                "splitters": splitters,
+                "tiles": {"tiles": st["tiles"], "per_bucket": st["tiles_per_bucket"], "big": st["big_tiles"],
+                          "imbalance": st["tile_imbalance"]}}
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -96,6 +96,8 @@ typedef struct {
   int splitter_used;                 /* KITE_SPLIT_SAMPLED or KITE_SPLIT_LEARNED */
   double stage_ms[12];               /* per-stage device time of the last finish (events) */
   uint64_t h2d_bytes, d2h_bytes;
+  uint64_t kernel_launches;          /* kernels this library launched in the last finish */
+  double mlp_loss, mlp_pred_imbalance, hist_pred_imbalance; /* learned-splitter diagnostics */
 } kite_gpu_stats;
 
 /* Merge input: one .kite file's partition table, with payloads in host memory

@@ -14,11 +14,14 @@ namespace kite {
 // tile byte offsets, row totals and the bucket's min/max key.
 template <class T>
 __global__ void k_tile_link(const TileOut<T>* __restrict__ tout, uint32_t P, uint32_t S,
-                            unsigned long long* __restrict__ tile_boff, T* __restrict__ tile_prev,
-                            BucketMeta* __restrict__ meta) {
+                            const uint32_t* __restrict__ tile_first, unsigned long long* __restrict__ tile_boff,
+                            T* __restrict__ tile_prev, BucketMeta* __restrict__ meta) {
   const int lane = threadIdx.x & 31;
   const uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (b >= P) return;
+  // tiles of bucket b: [t0, t0 + S) (fixed S) or [tile_first[b], tile_first[b+1])
+  const size_t t0 = tile_first ? tile_first[b] : (size_t)b * S;
+  if (tile_first) S = tile_first[b + 1] - tile_first[b];
   bool have_prev = false;
   T prev = T(0), kmin = T(0);
   unsigned long long boff = 0, rows = 0;
@@ -30,7 +33,7 @@ __global__ void k_tile_link(const TileOut<T>* __restrict__ tout, uint32_t P, uin
     o.rows = 0;
     o.first_count = 0;
     o.rest_bytes = 0;
-    if (j < S) o = tout[(size_t)b * S + j];
+    if (j < S) o = tout[t0 + j];
     const bool ne = o.rows > 0;
     const unsigned ball = __ballot_sync(0xffffffffu, ne);
     // previous non-empty lane's last key
@@ -57,8 +60,8 @@ __global__ void k_tile_link(const TileOut<T>* __restrict__ tout, uint32_t P, uin
       }
     }
     if (j < S) {
-      tile_boff[(size_t)b * S + j] = boff + inc - bytes;
-      tile_prev[(size_t)b * S + j] = p;
+      tile_boff[t0 + j] = boff + inc - bytes;
+      tile_prev[t0 + j] = p;
     }
     // first non-empty tile overall gives kmin
     if (!have_prev && ball) {
@@ -91,8 +94,20 @@ void launch_tile_link(const TileOut<T>* tout, uint32_t P, uint32_t S, unsigned l
                       BucketMeta* meta, cudaStream_t s) {
   const unsigned threads = 256;
   const unsigned blocks = (unsigned)(((size_t)P * 32 + threads - 1) / threads);
-  k_tile_link<T><<<blocks, threads, 0, s>>>(tout, P, S, tile_boff, tile_prev, meta);
+  k_tile_link<T><<<blocks, threads, 0, s>>>(tout, P, S, nullptr, tile_boff, tile_prev, meta);
 }
+
+template <class T>
+void launch_tile_link_ranges(const TileOut<T>* tout, uint32_t P, const uint32_t* tile_first,
+                             unsigned long long* tile_boff, T* tile_prev, BucketMeta* meta, cudaStream_t s) {
+  const unsigned threads = 256;
+  const unsigned blocks = (unsigned)(((size_t)P * 32 + threads - 1) / threads);
+  k_tile_link<T><<<blocks, threads, 0, s>>>(tout, P, 0, tile_first, tile_boff, tile_prev, meta);
+}
+template void launch_tile_link_ranges<uint64_t>(const TileOut<uint64_t>*, uint32_t, const uint32_t*,
+                                                unsigned long long*, uint64_t*, BucketMeta*, cudaStream_t);
+template void launch_tile_link_ranges<u128>(const TileOut<u128>*, uint32_t, const uint32_t*, unsigned long long*,
+                                            u128*, BucketMeta*, cudaStream_t);
 template void launch_tile_link<uint64_t>(const TileOut<uint64_t>*, uint32_t, uint32_t, unsigned long long*,
                                          uint64_t*, BucketMeta*, cudaStream_t);
 template void launch_tile_link<u128>(const TileOut<u128>*, uint32_t, uint32_t, unsigned long long*, u128*,

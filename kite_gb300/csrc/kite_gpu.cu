@@ -105,7 +105,7 @@ struct kite_gpu_ctx {
 
   // scratch
   DevBuf blocks, nl, scan_tmp, bucket_count, bucket_off, bucket_fill, totals, status;
-  DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, hist16;
+  DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, splitters2, hist16;
   DevBuf slices, tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
   HostBuf h_blocks, h_small, h_tiles, h_out;
   std::vector<cudaEvent_t> ev;  // stage events
@@ -196,6 +196,7 @@ int run_count(kite_gpu_ctx* ctx) {
   const uint64_t prev_h2d = st.h2d_bytes, prev_d2h = st.d2h_bytes;
   const uint32_t prev_segments = st.segments;
   std::memset(&st, 0, sizeof st);
+  st.hist_pred_imbalance = -1.0;
   st.h2d_bytes = prev_h2d;
   st.d2h_bytes = prev_d2h;
   st.segments = prev_segments + 1;
@@ -240,8 +241,8 @@ int run_count(kite_gpu_ctx* ctx) {
   KCU(cudaMemsetAsync(ctx->status.p, 0, sizeof(DevStatus), s));
   const uint8_t* base = arena_base(ctx);
   launch_newline_count(base, ctx->blocks.as<BlockDesc>(), nblocks, ctx->nl.as<unsigned long long>(), s);
-  exclusive_scan_u64(ctx->nl.as<unsigned long long>(), ctx->nl.as<unsigned long long>(), nblocks,
-                     ctx->scan_tmp.as<unsigned long long>(), s);
+  st.kernel_launches += 1 + exclusive_scan_u64(ctx->nl.as<unsigned long long>(), ctx->nl.as<unsigned long long>(),
+                                               nblocks, ctx->scan_tmp.as<unsigned long long>(), s);
   KCU(cudaEventRecord(ctx->ev[1], s));
 
   // ---- K2 histogram pass --------------------------------------------------
@@ -274,6 +275,7 @@ int run_count(kite_gpu_ctx* ctx) {
   ep.sample_mask = mask;
   ep.status = ctx->status.as<DevStatus>();
   launch_extract_hist<T>(ep, nblocks, s);
+  st.kernel_launches += 1;
   KCU(cudaGetLastError());
   KCU(cudaEventRecord(ctx->ev[2], s));
 
@@ -323,6 +325,7 @@ int run_count(kite_gpu_ctx* ctx) {
   ep.bucket_fill = ctx->bucket_fill.as<unsigned long long>();
   ep.keys_out = ctx->keys_a.as<T>();
   launch_extract_scatter<T>(ep, nblocks, s);
+  st.kernel_launches += 1;
   KCU(cudaGetLastError());
   KCU(cudaEventRecord(ctx->ev[3], s));
 
@@ -337,19 +340,44 @@ int run_count(kite_gpu_ctx* ctx) {
   if (S == 1) {
     for (uint32_t b = 0; b < P; ++b) ht.push_back(TileDesc{boff[b], (uint32_t)bcount[b], b});
   } else {
+    // Splitters: SAMPLED = histogram only; LEARNED = train the CDF, keep it
+    // unless its predicted max/mean tile load exceeds imbalance_bound (then the
+    // histogram); AUTO = histogram unless its own prediction exceeds the
+    // bound, then as LEARNED.
     KCU(ctx->splitters.ensure((size_t)S * sizeof(T)));
+    KCU(ctx->splitters2.ensure((size_t)S * sizeof(T)));
     KCU(ctx->hist16.ensure((size_t)65536 * 4));
-    bool learned = false;
     const int mode = ctx->cfg.splitter_mode;
-    if (mode == KITE_SPLIT_LEARNED || mode == KITE_SPLIT_AUTO) {
-      int lrc = mlp_splitters<T>(ctx->mlp, ctx->sample.as<T>(), nsample, 2 * k, S, ctx->splitters.as<T>(),
-                                 ctx->cfg.imbalance_bound, s, &learned);
-      if (lrc) return fail(ctx, KITE_ERR_CUDA, "learned splitter training failed");
+    const double bound = ctx->cfg.imbalance_bound;
+    T* hist_spl = ctx->splitters.as<T>();
+    T* mlp_spl = ctx->splitters2.as<T>();
+    double hist_imb = -1.0;
+    if (mode != KITE_SPLIT_LEARNED) {
+      st.kernel_launches +=
+          compute_hist_splitters<T>(ctx->sample.as<T>(), nsample, 2 * k, S, hist_spl, ctx->hist16.as<unsigned>(), s);
+      if (mode == KITE_SPLIT_AUTO) {
+        if (predict_imbalance<T>(ctx->mlp, ctx->sample.as<T>(), nsample, hist_spl, S, s, ctx->cfg.timeout_ms,
+                                 &hist_imb))
+          return fail(ctx, KITE_ERR_TIMEOUT, "splitter evaluation did not finish");
+        st.kernel_launches += 1;
+      }
     }
-    if (!learned)
-      compute_hist_splitters<T>(ctx->sample.as<T>(), nsample, 2 * k, S, ctx->splitters.as<T>(),
-                                ctx->hist16.as<unsigned>(), s);
+    bool learned = false;
+    if (mode == KITE_SPLIT_LEARNED || (mode == KITE_SPLIT_AUTO && hist_imb > bound)) {
+      MlpReport rep;
+      if (mlp_splitters<T>(ctx->mlp, ctx->sample.as<T>(), nsample, 2 * k, S, mlp_spl, s, ctx->cfg.timeout_ms, &rep))
+        return fail(ctx, KITE_ERR_CUDA, "learned splitter training failed");
+      st.kernel_launches += rep.launches;
+      st.mlp_loss = rep.loss;
+      st.mlp_pred_imbalance = rep.pred_imbalance;
+      learned = rep.pred_imbalance <= bound;
+      if (!learned && mode == KITE_SPLIT_LEARNED)
+        st.kernel_launches += compute_hist_splitters<T>(ctx->sample.as<T>(), nsample, 2 * k, S, hist_spl,
+                                                        ctx->hist16.as<unsigned>(), s);
+    }
+    st.hist_pred_imbalance = hist_imb;
     st.splitter_used = learned ? KITE_SPLIT_LEARNED : KITE_SPLIT_SAMPLED;
+    const T* chosen = learned ? mlp_spl : hist_spl;
     const uint32_t sk = split_slice_keys(sizeof(T));
     std::vector<SliceDesc> hsl;
     for (uint32_t b = 0; b < P; ++b)
@@ -370,15 +398,15 @@ int run_count(kite_gpu_ctx* ctx) {
     tp.keys_in = ctx->keys_a.as<T>();
     tp.keys_out = ctx->keys_b.as<T>();
     tp.slices = ctx->slices.as<SliceDesc>();
-    tp.splitters = ctx->splitters.as<T>();
+    tp.splitters = chosen;
     tp.S = S;
     tp.tile_count = ctx->tile_count.as<unsigned long long>();
     tp.tile_off = ctx->tile_off.as<unsigned long long>();
     tp.tile_fill = ctx->tile_fill.as<unsigned long long>();
     tp.status = ctx->status.as<DevStatus>();
     launch_tile_hist<T>(tp, (uint32_t)hsl.size(), sk, s);
-    exclusive_scan_u64(tp.tile_count, ctx->tile_off.as<unsigned long long>(), nt,
-                       ctx->scan_tmp.as<unsigned long long>(), s);
+    st.kernel_launches += 2 + exclusive_scan_u64(tp.tile_count, ctx->tile_off.as<unsigned long long>(), nt,
+                                                 ctx->scan_tmp.as<unsigned long long>(), s);
     launch_tile_scatter<T>(tp, (uint32_t)hsl.size(), sk, s);
     KCU(cudaGetLastError());
     // tile counts/offsets to host to build the tile list
@@ -424,6 +452,7 @@ int run_count(kite_gpu_ctx* ctx) {
   // ---- K4 tile sort + RLE ---------------------------------------------------
   launch_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ntiles,
                       ctx->tile_out.as<TileOut<T>>(), ctx->status.as<DevStatus>(), s);
+  st.kernel_launches += 1 + (big.empty() ? 0 : 1) + 4;  // tile sort, big tiles, link, offsets, encode
   KCU(cudaGetLastError());
   KCU(cudaEventRecord(ctx->ev[5], s));
   launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(),
@@ -583,7 +612,7 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
   for (auto e : ctx->ev) cudaEventDestroy(e);
   DevBuf* bufs[] = {&ctx->arena, &ctx->blocks, &ctx->nl, &ctx->scan_tmp, &ctx->bucket_count, &ctx->bucket_off,
                     &ctx->bucket_fill, &ctx->totals, &ctx->status, &ctx->keys_a, &ctx->keys_b, &ctx->counts,
-                    &ctx->sample, &ctx->sample_count, &ctx->splitters, &ctx->hist16, &ctx->slices,
+                    &ctx->sample, &ctx->sample_count, &ctx->splitters, &ctx->splitters2, &ctx->hist16, &ctx->slices,
                     &ctx->tile_count, &ctx->tile_off, &ctx->tile_fill, &ctx->tiles, &ctx->big_ids,
                     &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out};
   for (DevBuf* b : bufs) b->release();
@@ -717,7 +746,7 @@ int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n,
   if (!ctx || !inputs || n <= 0) return KITE_ERR_BAD_INPUT;
   cudaSetDevice(ctx->cfg.device);
   std::string msg;
-  int rc = merge_run(ctx->cfg.k <= 31 ? 8 : 16, ctx->cfg.partitions, inputs, n, ctx->stream, ctx->cfg.timeout_ms,
+  int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, inputs, n, ctx->stream, ctx->cfg.timeout_ms,
                      emit, user, &msg, &ctx->stats);
   if (rc) ctx->err = msg;
   return rc;

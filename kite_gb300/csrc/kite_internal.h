@@ -101,8 +101,12 @@ uint32_t split_slice_keys(int key_bytes);
 // Exclusive scan of n u64 values (in may equal out).  `tmp` needs
 // scan_tmp_elems(n) entries.
 size_t scan_tmp_elems(size_t n);
-void exclusive_scan_u64(const unsigned long long* in, unsigned long long* out, size_t n,
-                        unsigned long long* tmp, cudaStream_t s);
+// Returns the number of kernels launched.
+int exclusive_scan_u64(const unsigned long long* in, unsigned long long* out, size_t n,
+                       unsigned long long* tmp, cudaStream_t s);
+// Waits for the work queued on s, polling with a deadline: 0 ok, -1 CUDA
+// error, -3 timeout.
+int bounded_sync(cudaStream_t s, uint32_t timeout_ms);
 
 // ---- sort_kernels.cu ----
 constexpr int kTileThreads = 512;
@@ -132,6 +136,10 @@ template <class T>
 void launch_encode(const T* keys, const uint32_t* counts, const TileDesc* tiles, const TileOut<T>* tout,
                    const unsigned long long* tile_boff, const T* tile_prev, const BucketMeta* meta, uint32_t ntiles,
                    uint8_t* out, unsigned long long out_cap, DevStatus* st, cudaStream_t s);
+// Same, with variable tile ranges per bucket: tiles of b are [tile_first[b], tile_first[b+1]).
+template <class T>
+void launch_tile_link_ranges(const TileOut<T>* tout, uint32_t P, const uint32_t* tile_first,
+                             unsigned long long* tile_boff, T* tile_prev, BucketMeta* meta, cudaStream_t s);
 void launch_bucket_offsets(BucketMeta* meta, uint32_t P, unsigned long long* tmp, cudaStream_t s);
 
 }  // namespace kite

@@ -1,12 +1,824 @@
-// GPU merge (placeholder until the merge kernels land).
+// GPU `kite merge`: decode every input chunk, k-way merge per partition with
+// exact count summation, DVLE re-encode.
+//
+// Reference semantics restated (src/merge/mod.rs:198-214 and
+// src/kiteops/mod.rs:433-859):
+//   load_partition_counts   every chunk of one input's partition decoded
+//                           (DVLE or RAW), equal keys summed in u64 (saturating)
+//   apply_reader_filter     that input's header min/max, on the per-input sum
+//   merge_vectors_total     union over inputs, u64 saturating sums
+//   serialize_partition_chunk  a total above u32::MAX is an error naming the key;
+//                           otherwise one DVLE chunk per non-empty partition.
+//
+// GPU structure:
+//   decode    payload bytes cut into 2 KiB segments; per-segment varint
+//             terminator counts and delta sums, per-stream scans, then a decode
+//             pass that writes (key, u64 count) rows.  A "stream" is one chunk.
+//   tiles     key-range tiles per partition from global splitters, refined by
+//             bisection until every tile fits on chip; each stream is
+//             binary-searched for the tile edges.
+//   merge     one CTA per tile: rows of all its streams into shared memory,
+//             merged ranks by binary search (ties broken by stream order),
+//             per-input sums, filter, cross-input sums, overflow check.
+//   encode    the count path's DVLE link + encode kernels.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
 #include "merge.h"
+#include "kite_internal.h"
+#include "splitters.h"
 
 namespace kite {
 
-int merge_run(int, uint32_t, const kite_gpu_merge_input*, int, cudaStream_t, uint32_t, kite_gpu_emit_fn, void*,
-              std::string* msg, kite_gpu_stats*) {
-  *msg = "merge not built yet";
-  return KITE_ERR_UNSUPPORTED;
+namespace {
+
+constexpr uint32_t kSeg = 2048;          // decode segment bytes
+constexpr int kMergeThreads = 512;
+constexpr uint32_t kMergeCap = 4096;      // rows per merge tile
+constexpr uint32_t kMaxTileStreams = 256; // streams per tile (inputs x chunks)
+
+struct StreamDesc {
+  uint64_t byte_off;   // payload offset in the device byte buffer
+  uint64_t byte_len;
+  uint64_t row_off;    // first row in the decoded arrays
+  uint64_t rows;
+  uint32_t codec;
+  uint32_t input;
+  uint32_t partition;
+  uint32_t head;       // raw head bytes (12 or 20) for DVLE, 0 for RAW
+};
+
+struct SegDesc {
+  uint64_t start, end;  // byte range (device buffer offsets) inside the stream's varint area
+  uint32_t stream;
+  uint32_t first;       // 1 if first segment of the stream
+};
+
+struct InputFilter {
+  uint32_t has_min, has_max, min_count, max_count;
+};
+
+// One entry of a tile's stream list.
+struct TileStream {
+  uint64_t lo, hi;      // row range [lo, hi) (absolute row indices)
+  uint32_t input;
+  uint32_t pad;
+};
+
+struct MergeTile {
+  uint64_t out_off;     // output row base (reserved = rows in)
+  uint32_t first_ts;    // index into TileStream list
+  uint32_t nts;
+  uint32_t rows_in;
+  uint32_t partition;
+};
+
+__device__ __forceinline__ bool is_term(uint8_t b) { return (b & 0x80u) == 0; }
+
+__global__ void k_seg_terms(const uint8_t* __restrict__ bytes, const SegDesc* __restrict__ segs, uint32_t nseg,
+                            uint32_t* __restrict__ terms) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const SegDesc d = segs[s];
+  uint32_t c = 0;
+  for (uint64_t p = d.start; p < d.end; ++p) c += is_term(bytes[p]);
+  terms[s] = c;
+}
+
+// Decodes the varints whose terminator lies in the segment.  varint index v
+// (within the stream's varint area): even = key delta of row v/2+1, odd =
+// count of row (v-1)/2+1.  MODE 0 sums the deltas, MODE 1 writes rows.
+template <class T, int MODE>
+__global__ void k_seg_decode(const uint8_t* __restrict__ bytes, const SegDesc* __restrict__ segs, uint32_t nseg,
+                             const StreamDesc* __restrict__ streams, const unsigned long long* __restrict__ vstart,
+                             T* __restrict__ dsum, const T* __restrict__ kstart, T* __restrict__ keys,
+                             unsigned long long* __restrict__ counts, DevStatus* st) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const SegDesc d = segs[s];
+  const StreamDesc sd = streams[d.stream];
+  const uint64_t area = sd.byte_off + sd.head;
+  // start of the first varint owned by this segment
+  uint64_t p = d.start;
+  while (p > area && !is_term(bytes[p - 1])) --p;
+  unsigned long long v = vstart[s];
+  T acc = MODE == 1 ? kstart[s] : T(0);
+  const uint64_t nvar = sd.rows ? 2 * (sd.rows - 1) : 0;
+  while (p < d.end) {
+    // decode one varint (delta up to 19 bytes for u128, 10 for u64)
+    T val = 0;
+    unsigned sh = 0;
+    uint64_t q = p;
+    const uint64_t lim = sd.byte_off + sd.byte_len;
+    while (q < lim) {
+      const uint8_t b = bytes[q++];
+      if (sh < (unsigned)KeyTraits<T>::kBits) val |= (T)(b & 0x7f) << sh;
+      sh += 7;
+      if (is_term(b)) break;
+    }
+    if (v >= nvar) break;  // bytes after the last row are ignored, as the reference decodes row_count rows
+    if ((v & 1ull) == 0) {
+      acc += val;  // wrapping add, as the reference's wrapping_add
+      if (MODE == 1) keys[sd.row_off + v / 2 + 1] = acc;
+    } else if (MODE == 1) {
+      counts[sd.row_off + (v - 1) / 2 + 1] = (unsigned long long)(uint64_t)val;
+    }
+    ++v;
+    p = q;
+  }
+  if (MODE == 0) dsum[s] = acc;
+}
+
+// Head row of every DVLE stream and all rows of RAW streams.
+template <class T>
+__global__ void k_stream_heads(const uint8_t* __restrict__ bytes, const StreamDesc* __restrict__ streams,
+                               uint32_t nstreams, T* __restrict__ keys, unsigned long long* __restrict__ counts,
+                               T* __restrict__ first_keys) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nstreams) return;
+  const StreamDesc sd = streams[i];
+  if (sd.rows == 0 || sd.head == 0) return;
+  const uint8_t* p = bytes + sd.byte_off;
+  T k = 0;
+  for (int b = 0; b < (int)sizeof(T); ++b) k |= (T)p[b] << (8 * b);
+  uint32_t c = 0;
+  for (int b = 0; b < 4; ++b) c |= (uint32_t)p[sizeof(T) + b] << (8 * b);
+  keys[sd.row_off] = k;
+  counts[sd.row_off] = c;
+  first_keys[i] = k;
+}
+
+template <class T>
+__global__ void k_raw_rows(const uint8_t* __restrict__ bytes, const StreamDesc* __restrict__ streams,
+                           const uint32_t* __restrict__ raw_ids, uint32_t nraw, T* __restrict__ keys,
+                           unsigned long long* __restrict__ counts) {
+  // one CTA per RAW stream
+  if (blockIdx.x >= nraw) return;
+  const StreamDesc sd = streams[raw_ids[blockIdx.x]];
+  const uint32_t es = sizeof(T) + 4;
+  for (uint64_t r = threadIdx.x; r < sd.rows; r += blockDim.x) {
+    const uint8_t* p = bytes + sd.byte_off + r * es;
+    T k = 0;
+    for (int b = 0; b < (int)sizeof(T); ++b) k |= (T)p[b] << (8 * b);
+    uint32_t c = 0;
+    for (int b = 0; b < 4; ++b) c |= (uint32_t)p[sizeof(T) + b] << (8 * b);
+    keys[sd.row_off + r] = k;
+    counts[sd.row_off + r] = c;
+  }
+}
+
+// lower_bound of `key` in the sorted rows [lo, hi) of the decoded key array.
+template <class T>
+__global__ void k_lower_bound(const T* __restrict__ keys, const uint64_t* __restrict__ qlo,
+                              const uint64_t* __restrict__ qhi, const T* __restrict__ qkey, uint32_t nq,
+                              uint64_t* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  uint64_t lo = qlo[i], hi = qhi[i];
+  const T key = qkey[i];
+  while (lo < hi) {
+    const uint64_t mid = lo + (hi - lo) / 2;
+    if (keys[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  out[i] = lo;
+}
+
+template <class T>
+__global__ void k_sample_rows(const T* __restrict__ keys, uint64_t nrows, uint32_t nsample, T* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsample) return;
+  out[i] = keys[(uint64_t)((unsigned __int128)i * nrows / nsample)];
+}
+
+template <class T>
+struct MergeSmem {
+  static constexpr size_t keys = (size_t)kMergeCap * sizeof(T);
+  static constexpr size_t cnts = (size_t)kMergeCap * 8;
+  static constexpr size_t tag = (size_t)kMergeCap * 2;
+  static constexpr size_t perm = (size_t)kMergeCap * 2;
+  static constexpr size_t head = (size_t)(kMergeCap + 1) * 2;
+  static constexpr size_t seg = (size_t)(kMaxTileStreams + 1) * 4 + kMaxTileStreams * 4;
+  static constexpr size_t misc = 64 * 8;
+  static constexpr size_t total = keys + cnts + tag + perm + ((head + 15) & ~(size_t)15) + seg + misc;
+};
+
+template <class T>
+__global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
+    const T* __restrict__ keys, const unsigned long long* __restrict__ counts, const MergeTile* __restrict__ tiles,
+    const TileStream* __restrict__ ts, const InputFilter* __restrict__ filt, T* __restrict__ out_keys,
+    uint32_t* __restrict__ out_counts, TileOut<T>* __restrict__ tout, unsigned long long* __restrict__ overflow,
+    DevStatus* st) {
+  using L = MergeSmem<T>;
+  constexpr int NT = kMergeThreads;
+  extern __shared__ __align__(16) uint8_t sm[];
+  T* sk = reinterpret_cast<T*>(sm);
+  unsigned long long* sc = reinterpret_cast<unsigned long long*>(sm + L::keys);
+  uint16_t* stag = reinterpret_cast<uint16_t*>(sm + L::keys + L::cnts);
+  uint16_t* perm = reinterpret_cast<uint16_t*>(sm + L::keys + L::cnts + L::tag);
+  uint16_t* head = reinterpret_cast<uint16_t*>(sm + L::keys + L::cnts + L::tag + L::perm);
+  uint32_t* sstart = reinterpret_cast<uint32_t*>(sm + L::keys + L::cnts + L::tag + L::perm +
+                                                 ((L::head + 15) & ~(size_t)15));
+  uint32_t* sinput = sstart + kMaxTileStreams + 1;
+  unsigned long long* misc = reinterpret_cast<unsigned long long*>(sinput + kMaxTileStreams);
+
+  const MergeTile mt = tiles[blockIdx.x];
+  const uint32_t nts = mt.nts, n = mt.rows_in;
+  if (n == 0 || nts == 0) {
+    if (threadIdx.x == 0) {
+      TileOut<T> o{};
+      tout[blockIdx.x] = o;
+    }
+    return;
+  }
+  if (n > kMergeCap || nts > kMaxTileStreams) {
+    dev_fail(st, KITE_DEV_TILE_OVERFLOW, blockIdx.x, n, nts);
+    return;
+  }
+  if (threadIdx.x == 0) {
+    uint32_t a = 0;
+    for (uint32_t i = 0; i < nts; ++i) {
+      sstart[i] = a;
+      sinput[i] = ts[mt.first_ts + i].input;
+      a += (uint32_t)(ts[mt.first_ts + i].hi - ts[mt.first_ts + i].lo);
+    }
+    sstart[nts] = a;
+  }
+  __syncthreads();
+  // load rows of every stream
+  for (uint32_t i = 0; i < nts; ++i) {
+    const TileStream t = ts[mt.first_ts + i];
+    const uint32_t b0 = sstart[i], len = (uint32_t)(t.hi - t.lo);
+    for (uint32_t r = threadIdx.x; r < len; r += NT) {
+      sk[b0 + r] = keys[t.lo + r];
+      sc[b0 + r] = counts[t.lo + r];
+      stag[b0 + r] = (uint16_t)i;
+    }
+  }
+  __syncthreads();
+  // merged rank of every row: own index + rows of other streams before it
+  for (uint32_t r = threadIdx.x; r < n; r += NT) {
+    const uint32_t a = stag[r];
+    const T key = sk[r];
+    uint32_t rank = r - sstart[a];
+    for (uint32_t b = 0; b < nts; ++b) {
+      if (b == a) continue;
+      uint32_t lo = sstart[b], hi = sstart[b + 1];
+      // streams before a: count keys <= key; after a: keys < key
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        const bool before = b < a ? sk[mid] <= key : sk[mid] < key;
+        if (before) lo = mid + 1;
+        else hi = mid;
+      }
+      rank += lo - sstart[b];
+    }
+    perm[rank] = (uint16_t)r;
+  }
+  __syncthreads();
+  // key-group heads in merged order
+  constexpr int PER = kMergeCap / NT;
+  const uint32_t q0 = threadIdx.x * PER;
+  uint32_t nh = 0;
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const uint32_t q = q0 + i;
+    if (q < n && (q == 0 || sk[perm[q]] != sk[perm[q - 1]])) nh++;
+  }
+  unsigned G;
+  unsigned* scan32 = reinterpret_cast<unsigned*>(misc);
+  unsigned g = block_exclusive_scan<NT, unsigned>(nh, scan32, &G);
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const uint32_t q = q0 + i;
+    if (q < n && (q == 0 || sk[perm[q]] != sk[perm[q - 1]])) head[g++] = (uint16_t)q;
+  }
+  if (threadIdx.x == 0) head[G] = (uint16_t)n;
+  __syncthreads();
+  // per group: per-input sums (u64 saturating), input filter, total.
+  // Outputs are compacted in group order; groups are handled in rounds of NT.
+  unsigned long long out_base = 0;
+  T prev_last = T(0);
+  bool have_prev = false;
+  unsigned long long rest = 0;
+  T first_key = T(0), last_key = T(0);
+  uint32_t first_count = 0;
+  unsigned* scan_b = scan32 + 40;
+  for (uint32_t g0 = 0; g0 < G; g0 += NT) {
+    const uint32_t gi = g0 + threadIdx.x;
+    bool present = false;
+    unsigned long long total = 0;
+    T key = T(0);
+    if (gi < G) {
+      const uint32_t a = head[gi], b = head[gi + 1];
+      key = sk[perm[a]];
+      uint32_t cur_in = 0xffffffffu;
+      unsigned long long part = 0;
+      for (uint32_t q = a; q <= b; ++q) {
+        const uint32_t in = q < b ? sinput[stag[perm[q]]] : 0xfffffffeu;
+        if (in != cur_in) {
+          if (cur_in != 0xffffffffu) {
+            const InputFilter f = filt[cur_in];
+            const bool ok = !(f.has_min && part < f.min_count) && !(f.has_max && part > f.max_count);
+            if (ok) {
+              total = (total > ~0ull - part) ? ~0ull : total + part;
+              present = true;
+            }
+          }
+          cur_in = in;
+          part = 0;
+        }
+        if (q < b) {
+          const unsigned long long c = sc[perm[q]];
+          part = (part > ~0ull - c) ? ~0ull : part + c;
+        }
+      }
+    }
+    unsigned tot;
+    const unsigned idx = block_exclusive_scan<NT, unsigned>(present ? 1u : 0u, scan_b, &tot);
+    if (present) {
+      const unsigned long long o = out_base + idx;
+      if (total > 0xffffffffull) atomicMin(overflow, ((unsigned long long)blockIdx.x << 32) | (o & 0xffffffffull));
+      const uint32_t c32 = total > 0xffffffffull ? 0xffffffffu : (uint32_t)total;
+      out_keys[mt.out_off + o] = key;
+      out_counts[mt.out_off + o] = c32;
+    }
+    __syncthreads();
+    // DVLE sizes of the rows after the tile's first (the previous row may come
+    // from the previous round; both are already in global memory and visible
+    // to the whole CTA after the barrier).
+    for (unsigned u = threadIdx.x; u < tot; u += NT) {
+      const unsigned long long o = out_base + u;
+      const T kk = out_keys[mt.out_off + o];
+      const uint32_t cc = out_counts[mt.out_off + o];
+      if (o > 0) {
+        const T pk = out_keys[mt.out_off + o - 1];
+        rest += (unsigned long long)(varint_len((T)(kk - pk)) + varint_len((uint64_t)cc));
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && tot) {
+      if (!have_prev) {
+        first_key = out_keys[mt.out_off + out_base];
+        first_count = out_counts[mt.out_off + out_base];
+      }
+      last_key = out_keys[mt.out_off + out_base + tot - 1];
+      have_prev = true;
+    }
+    out_base += tot;
+    __syncthreads();
+  }
+  (void)prev_last;
+  unsigned long long rest_total;
+  block_exclusive_scan<NT, unsigned long long>(rest, misc + 8, &rest_total);
+  if (threadIdx.x == 0) {
+    TileOut<T> o;
+    o.first_key = first_key;
+    o.last_key = last_key;
+    o.rows = (uint32_t)out_base;
+    o.first_count = first_count;
+    o.rest_bytes = rest_total;
+    tout[blockIdx.x] = o;
+  }
+}
+
+template <class T>
+struct Key128 {
+  static unsigned __int128 to(T v) { return (unsigned __int128)v; }
+};
+
+// ---- host side -----------------------------------------------------------------
+struct Dev {
+  void* p = nullptr;
+  size_t cap = 0;
+  bool ensure(size_t b) {
+    if (b <= cap) return true;
+    cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMalloc(&p, b + 256) != cudaSuccess) return false;
+    cap = b + 256;
+    return true;
+  }
+  ~Dev() { cudaFree(p); }
+  template <class U> U* as() { return static_cast<U*>(p); }
+};
+
+template <class T>
+int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, int n, cudaStream_t s,
+                uint32_t timeout_ms,
+                kite_gpu_emit_fn emit, void* user, std::string* msg, kite_gpu_stats* stat) {
+  auto fail = [&](int code, const std::string& m) {
+    *msg = m;
+    return code;
+  };
+#define MCU(call)                                                                      \
+  do {                                                                                 \
+    cudaError_t _e = (call);                                                           \
+    if (_e != cudaSuccess) return fail(KITE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+  auto sync = [&]() { return bounded_sync(s, timeout_ms); };
+  const uint32_t head_bytes = sizeof(T) + 4;
+  // ---- streams (one per input chunk), bytes to the device ----
+  std::vector<StreamDesc> streams;
+  std::vector<uint64_t> in_base(n);
+  uint64_t total_bytes = 0, total_rows = 0;
+  std::vector<std::pair<uint64_t, uint64_t>> in_span(n);  // file [lo, hi) of payload bytes
+  for (int i = 0; i < n; ++i) {
+    uint64_t lo = UINT64_MAX, hi = 0;
+    uint64_t nch = 0;
+    for (uint32_t p = 0; p < P; ++p) nch = std::max<uint64_t>(nch, in[i].part_first[p] + in[i].part_count[p]);
+    for (uint64_t c = 0; c < nch; ++c) {
+      lo = std::min(lo, in[i].chunk_offset[c]);
+      hi = std::max(hi, in[i].chunk_offset[c] + in[i].chunk_len[c]);
+    }
+    if (nch == 0) lo = hi = 0;
+    if (hi > in[i].base_len) return fail(KITE_ERR_BAD_INPUT, "chunk out of bounds in input #" + std::to_string(i + 1));
+    in_span[i] = {lo, hi};
+    in_base[i] = total_bytes;
+    total_bytes += (hi - lo + 15) & ~15ull;
+  }
+  for (uint32_t p = 0; p < P; ++p)
+    for (int i = 0; i < n; ++i)
+      for (uint64_t c = in[i].part_first[p]; c < in[i].part_first[p] + in[i].part_count[p]; ++c) {
+        const uint32_t codec = in[i].chunk_codec[c];
+        if (codec & KITE_CODEC_ZSTD) return fail(KITE_ERR_UNSUPPORTED, "zstd chunks are not supported by the GPU merge");
+        StreamDesc sd{};
+        sd.byte_off = in_base[i] + in[i].chunk_offset[c] - in_span[i].first;
+        sd.byte_len = in[i].chunk_len[c];
+        sd.rows = in[i].chunk_rows[c];
+        sd.row_off = total_rows;
+        sd.codec = codec;
+        sd.input = (uint32_t)i;
+        sd.partition = p;
+        sd.head = (codec & KITE_CODEC_DVLE) ? head_bytes : 0;
+        if (sd.rows && (codec & KITE_CODEC_DVLE) && sd.byte_len < head_bytes)
+          return fail(KITE_ERR_BAD_INPUT, sizeof(T) == 8 ? "u64 DVLE payload too small" : "u128 DVLE payload too small");
+        if (sd.rows && !(codec & KITE_CODEC_DVLE) && sd.byte_len < sd.rows * head_bytes)
+          return fail(KITE_ERR_BAD_INPUT, "raw row payload truncated");
+        total_rows += sd.rows;
+        streams.push_back(sd);
+      }
+  stat->h2d_bytes += total_bytes;
+  Dev d_bytes, d_streams, d_segs, d_terms, d_vstart, d_dsum, d_kstart, d_keys, d_counts, d_first, d_raw;
+  if (!d_bytes.ensure(total_bytes + 64)) return fail(KITE_ERR_OOM, "device bytes");
+  for (int i = 0; i < n; ++i)
+    if (in_span[i].second > in_span[i].first)
+      MCU(cudaMemcpyAsync(d_bytes.as<uint8_t>() + in_base[i], in[i].base + in_span[i].first,
+                          in_span[i].second - in_span[i].first, cudaMemcpyHostToDevice, s));
+  // ---- decode segments ----
+  std::vector<SegDesc> segs;
+  std::vector<uint32_t> raw_ids;
+  std::vector<uint32_t> seg_first(streams.size() + 1);
+  for (uint32_t si = 0; si < streams.size(); ++si) {
+    seg_first[si] = (uint32_t)segs.size();
+    const StreamDesc& sd = streams[si];
+    if (sd.rows == 0) continue;
+    if (sd.head == 0) {
+      raw_ids.push_back(si);
+      continue;
+    }
+    const uint64_t a = sd.byte_off + sd.head, e = sd.byte_off + sd.byte_len;
+    for (uint64_t o = a; o < e; o += kSeg) segs.push_back(SegDesc{o, std::min(o + kSeg, e), si, o == a ? 1u : 0u});
+  }
+  seg_first[streams.size()] = (uint32_t)segs.size();
+  const uint32_t nseg = (uint32_t)segs.size(), nst = (uint32_t)streams.size();
+  if (!d_streams.ensure(nst * sizeof(StreamDesc) + 8) || !d_segs.ensure(nseg * sizeof(SegDesc) + 8) ||
+      !d_terms.ensure(nseg * 4 + 8) || !d_vstart.ensure(nseg * 8 + 8) || !d_dsum.ensure(nseg * sizeof(T) + 16) ||
+      !d_kstart.ensure(nseg * sizeof(T) + 16) || !d_keys.ensure(total_rows * sizeof(T) + 16) ||
+      !d_counts.ensure(total_rows * 8 + 16) || !d_first.ensure(nst * sizeof(T) + 16) || !d_raw.ensure(raw_ids.size() * 4 + 8))
+    return fail(KITE_ERR_OOM, "merge decode buffers");
+  MCU(cudaMemcpyAsync(d_streams.p, streams.data(), nst * sizeof(StreamDesc), cudaMemcpyHostToDevice, s));
+  if (nseg) MCU(cudaMemcpyAsync(d_segs.p, segs.data(), nseg * sizeof(SegDesc), cudaMemcpyHostToDevice, s));
+  if (!raw_ids.empty())
+    MCU(cudaMemcpyAsync(d_raw.p, raw_ids.data(), raw_ids.size() * 4, cudaMemcpyHostToDevice, s));
+  int launches = 0;
+  if (nseg) {
+    k_seg_terms<<<(nseg + 255) / 256, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_segs.as<SegDesc>(), nseg,
+                                                    d_terms.as<uint32_t>());
+    launches++;
+  }
+  std::vector<uint32_t> terms(nseg);
+  if (nseg) MCU(cudaMemcpyAsync(terms.data(), d_terms.p, nseg * 4, cudaMemcpyDeviceToHost, s));
+  if (sync()) return fail(KITE_ERR_TIMEOUT, "merge decode wait");
+  // per-stream varint starts; the varint count must be 2*(rows-1)
+  std::vector<unsigned long long> vstart(nseg);
+  for (uint32_t si = 0; si < nst; ++si) {
+    unsigned long long v = 0;
+    for (uint32_t g = seg_first[si]; g < seg_first[si + 1]; ++g) {
+      vstart[g] = v;
+      v += terms[g];
+    }
+    const StreamDesc& sd = streams[si];
+    if (sd.head && sd.rows && v < 2 * (sd.rows - 1))
+      return fail(KITE_ERR_BAD_INPUT, sizeof(T) == 8 ? "invalid u64 DVLE delta" : "invalid u128 DVLE delta");
+  }
+  DevStatus* dst = nullptr;
+  MCU(cudaMallocAsync(&dst, sizeof(DevStatus), s));
+  MCU(cudaMemsetAsync(dst, 0, sizeof(DevStatus), s));
+  if (nseg) {
+    MCU(cudaMemcpyAsync(d_vstart.p, vstart.data(), nseg * 8, cudaMemcpyHostToDevice, s));
+    k_seg_decode<T, 0><<<(nseg + 255) / 256, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_segs.as<SegDesc>(), nseg,
+                                                          d_streams.as<StreamDesc>(),
+                                                          d_vstart.as<unsigned long long>(), d_dsum.as<T>(), nullptr,
+                                                          nullptr, nullptr, dst);
+    launches++;
+  }
+  k_stream_heads<T><<<(nst + 255) / 256, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_streams.as<StreamDesc>(), nst,
+                                                      d_keys.as<T>(), d_counts.as<unsigned long long>(),
+                                                      d_first.as<T>());
+  launches++;
+  if (!raw_ids.empty()) {
+    k_raw_rows<T><<<(unsigned)raw_ids.size(), 256, 0, s>>>(d_bytes.as<uint8_t>(), d_streams.as<StreamDesc>(),
+                                                           d_raw.as<uint32_t>(), (uint32_t)raw_ids.size(),
+                                                           d_keys.as<T>(), d_counts.as<unsigned long long>());
+    launches++;
+  }
+  std::vector<T> dsum(nseg), first(nst);
+  if (nseg) MCU(cudaMemcpyAsync(dsum.data(), d_dsum.p, nseg * sizeof(T), cudaMemcpyDeviceToHost, s));
+  MCU(cudaMemcpyAsync(first.data(), d_first.p, nst * sizeof(T), cudaMemcpyDeviceToHost, s));
+  if (sync()) return fail(KITE_ERR_TIMEOUT, "merge decode wait");
+  std::vector<T> kstart(nseg);
+  for (uint32_t si = 0; si < nst; ++si) {
+    T acc = first[si];
+    for (uint32_t g = seg_first[si]; g < seg_first[si + 1]; ++g) {
+      kstart[g] = acc;
+      acc += dsum[g];
+    }
+  }
+  if (nseg) {
+    MCU(cudaMemcpyAsync(d_kstart.p, kstart.data(), nseg * sizeof(T), cudaMemcpyHostToDevice, s));
+    k_seg_decode<T, 1><<<(nseg + 255) / 256, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_segs.as<SegDesc>(), nseg,
+                                                          d_streams.as<StreamDesc>(),
+                                                          d_vstart.as<unsigned long long>(), nullptr, d_kstart.as<T>(),
+                                                          d_keys.as<T>(), d_counts.as<unsigned long long>(), dst);
+    launches++;
+  }
+  // ---- tiles: global splitters from a row sample, refined by bisection ----
+  std::vector<uint32_t> part_first_stream(P + 1, 0);
+  {
+    uint32_t si = 0;
+    for (uint32_t p = 0; p < P; ++p) {
+      part_first_stream[p] = si;
+      while (si < nst && streams[si].partition == p) si++;
+    }
+    part_first_stream[P] = nst;
+  }
+  uint32_t S = 1;
+  while ((double)total_rows / ((double)P * S) > 0.25 * kMergeCap && S < 4096) S <<= 1;
+  std::vector<T> spl;
+  if (S > 1 && total_rows) {
+    const uint32_t ns = (uint32_t)std::min<uint64_t>(total_rows, 1u << 20);
+    Dev d_sample, d_spl, d_hist;
+    if (!d_sample.ensure(ns * sizeof(T)) || !d_spl.ensure(S * sizeof(T)) || !d_hist.ensure(65536 * 4))
+      return fail(KITE_ERR_OOM, "merge splitters");
+    k_sample_rows<T><<<(ns + 255) / 256, 256, 0, s>>>(d_keys.as<T>(), total_rows, ns, d_sample.as<T>());
+    // sampling every m-th row of the concatenated streams is a uniform sample
+    // of the key multiset; key bits from the input k
+    launches += 1 + compute_hist_splitters<T>(d_sample.as<T>(), ns, key_bits, S, d_spl.as<T>(),
+                                              d_hist.as<unsigned>(), s);
+    spl.resize(S - 1);
+    MCU(cudaMemcpyAsync(spl.data(), d_spl.p, (S - 1) * sizeof(T), cudaMemcpyDeviceToHost, s));
+    if (sync()) return fail(KITE_ERR_TIMEOUT, "merge splitter wait");
+  }
+  // ranges per partition: [lo_key, hi_key) with an "unbounded" flag for the top
+  struct Range {
+    uint32_t p;
+    T lo, hi;
+    bool open_hi;
+    std::vector<uint64_t> lo_pos, hi_pos;  // per stream of p
+  };
+  std::vector<Range> work, done;
+  for (uint32_t p = 0; p < P; ++p) {
+    if (part_first_stream[p] == part_first_stream[p + 1]) continue;
+    T lo = 0;
+    for (uint32_t j = 0; j < S; ++j) {
+      Range r;
+      r.p = p;
+      r.lo = lo;
+      r.open_hi = j + 1 == S;
+      r.hi = r.open_hi ? T(0) : spl[j];
+      if (!r.open_hi && r.hi <= r.lo) continue;  // empty (repeated splitter)
+      work.push_back(r);
+      if (!r.open_hi) lo = r.hi;
+    }
+  }
+  Dev d_qlo, d_qhi, d_qkey, d_qout;
+  for (int round = 0; !work.empty() && round < 200; ++round) {
+    // queries: for every range and stream, lower_bound(lo) and lower_bound(hi)
+    std::vector<uint64_t> qlo, qhi;
+    std::vector<T> qkey;
+    for (auto& r : work)
+      for (uint32_t si = part_first_stream[r.p]; si < part_first_stream[r.p + 1]; ++si) {
+        const uint64_t a = streams[si].row_off, b = a + streams[si].rows;
+        qlo.push_back(a);
+        qhi.push_back(b);
+        qkey.push_back(r.lo);
+        qlo.push_back(a);
+        qhi.push_back(b);
+        qkey.push_back(r.open_hi ? T(0) : r.hi);
+      }
+    const uint32_t nq = (uint32_t)qlo.size();
+    if (!d_qlo.ensure(nq * 8) || !d_qhi.ensure(nq * 8) || !d_qkey.ensure(nq * sizeof(T)) || !d_qout.ensure(nq * 8))
+      return fail(KITE_ERR_OOM, "merge tile queries");
+    MCU(cudaMemcpyAsync(d_qlo.p, qlo.data(), nq * 8, cudaMemcpyHostToDevice, s));
+    MCU(cudaMemcpyAsync(d_qhi.p, qhi.data(), nq * 8, cudaMemcpyHostToDevice, s));
+    MCU(cudaMemcpyAsync(d_qkey.p, qkey.data(), nq * sizeof(T), cudaMemcpyHostToDevice, s));
+    k_lower_bound<T><<<(nq + 255) / 256, 256, 0, s>>>(d_keys.as<T>(), d_qlo.as<uint64_t>(), d_qhi.as<uint64_t>(),
+                                                      d_qkey.as<T>(), nq, d_qout.as<uint64_t>());
+    launches++;
+    std::vector<uint64_t> qout(nq);
+    MCU(cudaMemcpyAsync(qout.data(), d_qout.p, nq * 8, cudaMemcpyDeviceToHost, s));
+    if (sync()) return fail(KITE_ERR_TIMEOUT, "merge tile wait");
+    std::vector<Range> next;
+    size_t q = 0;
+    for (auto& r : work) {
+      uint64_t rows = 0;
+      r.lo_pos.clear();
+      r.hi_pos.clear();
+      for (uint32_t si = part_first_stream[r.p]; si < part_first_stream[r.p + 1]; ++si) {
+        const uint64_t a = qout[q++], b0 = qout[q++];
+        const uint64_t b = r.open_hi ? streams[si].row_off + streams[si].rows : b0;
+        r.lo_pos.push_back(a);
+        r.hi_pos.push_back(b);
+        rows += b - a;
+      }
+      const uint32_t nstr = part_first_stream[r.p + 1] - part_first_stream[r.p];
+      const T hi_eff = r.open_hi ? (sizeof(T) == 8 ? (T)~0ull : ~T(0)) : r.hi;
+      if (rows > kMergeCap && hi_eff - r.lo > T(1)) {
+        const T mid = r.lo + (hi_eff - r.lo) / 2;
+        Range a = r, b = r;
+        a.hi = mid;
+        a.open_hi = false;
+        b.lo = mid;
+        next.push_back(a);
+        next.push_back(b);
+      } else {
+        if (rows > kMergeCap || nstr > kMaxTileStreams)
+          return fail(KITE_ERR_UNSUPPORTED, "merge tile cannot be split below the on-chip capacity");
+        done.push_back(std::move(r));
+      }
+    }
+    work.swap(next);
+  }
+  if (!work.empty()) return fail(KITE_ERR_UNSUPPORTED, "merge tile refinement did not converge");
+  std::sort(done.begin(), done.end(), [](const Range& a, const Range& b) { return a.p != b.p ? a.p < b.p : a.lo < b.lo; });
+  // ---- tile lists ----
+  std::vector<MergeTile> mts;
+  std::vector<TileStream> tss;
+  std::vector<TileDesc> tds;
+  std::vector<uint32_t> tile_first(P + 1, 0);
+  uint64_t out_off = 0;
+  {
+    size_t di = 0;
+    for (uint32_t p = 0; p < P; ++p) {
+      tile_first[p] = (uint32_t)mts.size();
+      while (di < done.size() && done[di].p == p) {
+        const Range& r = done[di++];
+        MergeTile mt{};
+        mt.out_off = out_off;
+        mt.first_ts = (uint32_t)tss.size();
+        mt.partition = p;
+        uint64_t rows = 0;
+        for (size_t k2 = 0; k2 < r.lo_pos.size(); ++k2) {
+          if (r.hi_pos[k2] == r.lo_pos[k2]) continue;
+          tss.push_back(TileStream{r.lo_pos[k2], r.hi_pos[k2], streams[part_first_stream[p] + k2].input, 0});
+          rows += r.hi_pos[k2] - r.lo_pos[k2];
+        }
+        mt.nts = (uint32_t)(tss.size() - mt.first_ts);
+        mt.rows_in = (uint32_t)rows;
+        tds.push_back(TileDesc{out_off, 0, p});
+        out_off += rows;
+        mts.push_back(mt);
+      }
+    }
+    tile_first[P] = (uint32_t)mts.size();
+  }
+  const uint32_t ntiles = (uint32_t)mts.size();
+  std::vector<InputFilter> filt(n);
+  for (int i = 0; i < n; ++i)
+    filt[i] = InputFilter{(uint32_t)in[i].has_min, (uint32_t)in[i].has_max, in[i].min_count, in[i].max_count};
+  Dev d_mt, d_ts, d_filt, d_okeys, d_ocounts, d_tout, d_over, d_tds, d_tf, d_boff, d_prev, d_meta, d_out;
+  if (!d_mt.ensure(ntiles * sizeof(MergeTile) + 8) || !d_ts.ensure(tss.size() * sizeof(TileStream) + 8) ||
+      !d_filt.ensure(n * sizeof(InputFilter)) || !d_okeys.ensure(out_off * sizeof(T) + 16) ||
+      !d_ocounts.ensure(out_off * 4 + 16) || !d_tout.ensure(ntiles * sizeof(TileOut<T>) + 16) ||
+      !d_over.ensure(8) || !d_tds.ensure(ntiles * sizeof(TileDesc) + 8) || !d_tf.ensure((P + 1) * 4) ||
+      !d_boff.ensure(ntiles * 8 + 8) || !d_prev.ensure(ntiles * sizeof(T) + 16) || !d_meta.ensure(P * sizeof(BucketMeta)))
+    return fail(KITE_ERR_OOM, "merge tile buffers");
+  if (ntiles) {
+    MCU(cudaMemcpyAsync(d_mt.p, mts.data(), ntiles * sizeof(MergeTile), cudaMemcpyHostToDevice, s));
+    MCU(cudaMemcpyAsync(d_ts.p, tss.data(), tss.size() * sizeof(TileStream), cudaMemcpyHostToDevice, s));
+  }
+  MCU(cudaMemcpyAsync(d_filt.p, filt.data(), n * sizeof(InputFilter), cudaMemcpyHostToDevice, s));
+  MCU(cudaMemsetAsync(d_over.p, 0xff, 8, s));
+  const size_t smem = MergeSmem<T>::total;
+  cudaFuncSetAttribute(k_merge_tiles<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (ntiles) {
+    k_merge_tiles<T><<<ntiles, kMergeThreads, smem, s>>>(d_keys.as<T>(), d_counts.as<unsigned long long>(),
+                                                         d_mt.as<MergeTile>(), d_ts.as<TileStream>(),
+                                                         d_filt.as<InputFilter>(), d_okeys.as<T>(),
+                                                         d_ocounts.as<uint32_t>(), d_tout.as<TileOut<T>>(),
+                                                         d_over.as<unsigned long long>(), dst);
+    launches++;
+  }
+  DevStatus hst{};
+  unsigned long long over = 0;
+  std::vector<TileOut<T>> htout(ntiles);
+  MCU(cudaMemcpyAsync(&hst, dst, sizeof hst, cudaMemcpyDeviceToHost, s));
+  MCU(cudaMemcpyAsync(&over, d_over.p, 8, cudaMemcpyDeviceToHost, s));
+  if (ntiles) MCU(cudaMemcpyAsync(htout.data(), d_tout.p, ntiles * sizeof(TileOut<T>), cudaMemcpyDeviceToHost, s));
+  if (sync()) return fail(KITE_ERR_TIMEOUT, "merge wait");
+  cudaFreeAsync(dst, s);
+  if (hst.code) {
+    char b[160];
+    snprintf(b, sizeof b, "merge: device status %u (%u, %u, %u)", hst.code, hst.a, hst.b, hst.c);
+    return fail(hst.code == KITE_DEV_BAD_INPUT ? KITE_ERR_BAD_INPUT : KITE_ERR_DEVICE, b);
+  }
+  if (over != ~0ull) {
+    // first overflowing row in (partition, key) order: name its key like the reference
+    const uint32_t t = (uint32_t)(over >> 32), r = (uint32_t)(over & 0xffffffffu);
+    T key{};
+    MCU(cudaMemcpyAsync(&key, d_okeys.as<T>() + mts[t].out_off + r, sizeof(T), cudaMemcpyDeviceToHost, s));
+    if (sync()) return fail(KITE_ERR_TIMEOUT, "merge wait");
+    unsigned __int128 v = (unsigned __int128)key;
+    std::string ks;
+    if (v == 0) ks = "0";
+    while (v) {
+      ks.insert(ks.begin(), (char)('0' + (int)(v % 10)));
+      v /= 10;
+    }
+    return fail(KITE_ERR_COUNT_OVERFLOW, "merged count exceeds u32 for key " + ks);
+  }
+  // ---- encode: per partition, tiles in key order ----
+  for (uint32_t t = 0; t < ntiles; ++t) tds[t].len = htout[t].rows;
+  if (ntiles) MCU(cudaMemcpyAsync(d_tds.p, tds.data(), ntiles * sizeof(TileDesc), cudaMemcpyHostToDevice, s));
+  MCU(cudaMemcpyAsync(d_tf.p, tile_first.data(), (P + 1) * 4, cudaMemcpyHostToDevice, s));
+  launch_tile_link_ranges<T>(d_tout.as<TileOut<T>>(), P, d_tf.as<uint32_t>(), d_boff.as<unsigned long long>(),
+                             d_prev.as<T>(), d_meta.as<BucketMeta>(), s);
+  launch_bucket_offsets(d_meta.as<BucketMeta>(), P, nullptr, s);
+  launches += 2;
+  std::vector<BucketMeta> meta(P);
+  MCU(cudaMemcpyAsync(meta.data(), d_meta.p, P * sizeof(BucketMeta), cudaMemcpyDeviceToHost, s));
+  if (sync()) return fail(KITE_ERR_TIMEOUT, "merge wait");
+  uint64_t out_bytes = 0, out_rows = 0;
+  for (auto& m : meta) {
+    out_bytes += m.bytes;
+    out_rows += m.rows;
+  }
+  if (!d_out.ensure(out_bytes + 16)) return fail(KITE_ERR_OOM, "merge output");
+  DevStatus* est = nullptr;
+  MCU(cudaMallocAsync(&est, sizeof(DevStatus), s));
+  MCU(cudaMemsetAsync(est, 0, sizeof(DevStatus), s));
+  launch_encode<T>(d_okeys.as<T>(), d_ocounts.as<uint32_t>(), d_tds.as<TileDesc>(), d_tout.as<TileOut<T>>(),
+                   d_boff.as<unsigned long long>(), d_prev.as<T>(), d_meta.as<BucketMeta>(), ntiles,
+                   d_out.as<uint8_t>(), out_bytes, est, s);
+  launches++;
+  std::vector<uint8_t> hout(out_bytes);
+  if (out_bytes) MCU(cudaMemcpyAsync(hout.data(), d_out.p, out_bytes, cudaMemcpyDeviceToHost, s));
+  MCU(cudaMemcpyAsync(&hst, est, sizeof hst, cudaMemcpyDeviceToHost, s));
+  if (sync()) return fail(KITE_ERR_TIMEOUT, "merge wait");
+  cudaFreeAsync(est, s);
+  if (hst.code) return fail(KITE_ERR_DEVICE, "merge encode failed");
+  stat->d2h_bytes += out_bytes;
+  stat->rows = out_rows;
+  stat->payload_bytes = out_bytes;
+  stat->tiles = ntiles;
+  stat->kernel_launches = launches;
+  uint64_t tmax = 0, tsum = 0, tne = 0;
+  for (auto& m : mts)
+    if (m.rows_in) {
+      tmax = std::max<uint64_t>(tmax, m.rows_in);
+      tsum += m.rows_in;
+      tne++;
+    }
+  stat->tile_imbalance = tne ? (double)tmax / ((double)tsum / tne) : 0.0;
+  if (!emit) return KITE_OK;
+  for (uint32_t p = 0; p < P; ++p) {
+    const BucketMeta& m = meta[p];
+    if (!m.rows) continue;
+    kite_chunk_meta cm{};
+    cm.partition_id = p;
+    cm.codec = KITE_CODEC_DVLE;
+    cm.row_count = m.rows;
+    cm.raw_bytes = m.bytes;
+    cm.key_min_lo[0] = m.kmin_lo;
+    cm.key_min_lo[1] = m.kmin_hi;
+    cm.key_max_lo[0] = m.kmax_lo;
+    cm.key_max_lo[1] = m.kmax_hi;
+    if (emit(user, &cm, hout.data() + m.byte_off, (size_t)m.bytes)) return fail(KITE_ERR_CALLBACK, "emit callback aborted");
+  }
+  return KITE_OK;
+#undef MCU
+}
+
+}  // namespace
+
+int merge_run(int k, uint32_t partitions, const kite_gpu_merge_input* inputs, int n, cudaStream_t s,
+              uint32_t timeout_ms, kite_gpu_emit_fn emit, void* user, std::string* msg, kite_gpu_stats* st) {
+  if (k <= 31) return merge_typed<uint64_t>(partitions, 2 * k, inputs, n, s, timeout_ms, emit, user, msg, st);
+  return merge_typed<u128>(partitions, 2 * k, inputs, n, s, timeout_ms, emit, user, msg, st);
 }
 
 }  // namespace kite

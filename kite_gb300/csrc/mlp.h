@@ -13,12 +13,23 @@ struct MlpModel;
 MlpModel* mlp_create();
 void mlp_destroy(MlpModel* m);
 
-// Trains the CDF on the sampled keys and writes S-1 splitters.  *used is set
-// to false (and nothing is written) when the predicted max/mean tile load on
-// the sample exceeds `bound`: the caller then falls back to the sampled
-// histogram splitters.
+struct MlpReport {
+  int launches = 0;
+  float loss = 0.f;
+  double pred_imbalance = 0.0;  // max/mean tile load of the sample under the learned splitters
+};
+
+// Trains the CDF on the sampled keys and writes S-1 ascending splitters to
+// d_spl.  Returns 0 on success (report filled), non-zero on a CUDA failure or
+// timeout.  Fewer than 1024 samples (or 4 per tile): nothing is trained and
+// report->pred_imbalance is +inf.
 template <class T>
-int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits, uint32_t S, T* d_spl, double bound,
-                  cudaStream_t s, bool* used);
+int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits, uint32_t S, T* d_spl,
+                  cudaStream_t s, uint32_t timeout_ms, MlpReport* report);
+
+// max/mean tile load of `n` sample keys under S-1 splitters (bounded wait).
+template <class T>
+int predict_imbalance(MlpModel* m, const T* d_sample, uint32_t n, const T* d_spl, uint32_t S, cudaStream_t s,
+                      uint32_t timeout_ms, double* out);
 
 }  // namespace kite

@@ -1,5 +1,8 @@
 // Device-wide exclusive prefix sum over u64 (reduce-then-scan, no inter-CTA
 // waiting).  Used for bucket/tile region offsets and newline prefixes.
+#include <chrono>
+#include <thread>
+
 #include "kite_internal.h"
 
 namespace kite {
@@ -51,17 +54,44 @@ size_t scan_tmp_elems(size_t n) {
   return tiles + scan_tmp_elems(tiles);
 }
 
-void exclusive_scan_u64(const unsigned long long* in, unsigned long long* out, size_t n, unsigned long long* tmp,
-                        cudaStream_t s) {
-  if (n == 0) return;
+int exclusive_scan_u64(const unsigned long long* in, unsigned long long* out, size_t n, unsigned long long* tmp,
+                       cudaStream_t s) {
+  if (n == 0) return 0;
   const size_t tiles = (n + kScanTile - 1) / kScanTile;
   if (tiles == 1) {
     k_scan_tile<<<1, kScanThreads, 0, s>>>(in, out, n, nullptr);
-    return;
+    return 1;
   }
   k_scan_reduce<<<(unsigned)tiles, kScanThreads, 0, s>>>(in, n, tmp);
-  exclusive_scan_u64(tmp, tmp, tiles, tmp + tiles, s);
+  const int inner = exclusive_scan_u64(tmp, tmp, tiles, tmp + tiles, s);
   k_scan_tile<<<(unsigned)tiles, kScanThreads, 0, s>>>(in, out, n, tmp);
+  return inner + 2;
+}
+
+int bounded_sync(cudaStream_t s, uint32_t timeout_ms) {
+  cudaEvent_t e;
+  if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return -1;
+  if (cudaEventRecord(e, s) != cudaSuccess) {
+    cudaEventDestroy(e);
+    return -1;
+  }
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
+  int rc = 0;
+  for (int spins = 0;; ++spins) {
+    const cudaError_t q = cudaEventQuery(e);
+    if (q == cudaSuccess) break;
+    if (q != cudaErrorNotReady) {
+      rc = -1;
+      break;
+    }
+    if (std::chrono::steady_clock::now() > deadline) {
+      rc = -3;
+      break;
+    }
+    if (spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  cudaEventDestroy(e);
+  return rc;
 }
 
 }  // namespace kite

@@ -62,16 +62,17 @@ __global__ void __launch_bounds__(1024) k_hist_splitters(unsigned* __restrict__ 
 }
 
 template <class T>
-void compute_hist_splitters(const T* d_sample, uint32_t nsample, uint32_t key_bits, uint32_t S, T* d_spl,
-                            unsigned* d_hist /* 65536 */, cudaStream_t s) {
+int compute_hist_splitters(const T* d_sample, uint32_t nsample, uint32_t key_bits, uint32_t S, T* d_spl,
+                           unsigned* d_hist /* 65536 */, cudaStream_t s) {
   const uint32_t hbits = key_bits < 16 ? key_bits : 16;
   cudaMemsetAsync(d_hist, 0, sizeof(unsigned) << hbits, s);
   if (nsample) k_sample_hist<T><<<256, 256, 0, s>>>(d_sample, nsample, key_bits, hbits, d_hist);
   k_hist_splitters<T><<<1, 1024, 0, s>>>(d_hist, hbits, key_bits, S, d_spl);
+  return nsample ? 2 : 1;
 }
-template void compute_hist_splitters<uint64_t>(const uint64_t*, uint32_t, uint32_t, uint32_t, uint64_t*, unsigned*,
-                                               cudaStream_t);
-template void compute_hist_splitters<u128>(const u128*, uint32_t, uint32_t, uint32_t, u128*, unsigned*,
-                                           cudaStream_t);
+template int compute_hist_splitters<uint64_t>(const uint64_t*, uint32_t, uint32_t, uint32_t, uint64_t*, unsigned*,
+                                              cudaStream_t);
+template int compute_hist_splitters<u128>(const u128*, uint32_t, uint32_t, uint32_t, u128*, unsigned*,
+                                          cudaStream_t);
 
 }  // namespace kite

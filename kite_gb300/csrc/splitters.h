@@ -11,8 +11,9 @@ namespace kite {
 // S-1 ascending splitters from a 2^16-bin histogram of the sampled keys'
 // top bits (key_bits = 2k).  With no sample, splitters cut [0, 2^key_bits)
 // uniformly.
+// Returns the number of kernels launched.
 template <class T>
-void compute_hist_splitters(const T* d_sample, uint32_t nsample, uint32_t key_bits, uint32_t S, T* d_spl,
-                            unsigned* d_hist, cudaStream_t s);
+int compute_hist_splitters(const T* d_sample, uint32_t nsample, uint32_t key_bits, uint32_t S, T* d_spl,
+                           unsigned* d_hist, cudaStream_t s);
 
 }  // namespace kite
