@@ -98,6 +98,7 @@ typedef struct {
   uint64_t h2d_bytes, d2h_bytes;
   uint64_t kernel_launches;          /* kernels this library launched in the last finish */
   double mlp_loss, mlp_pred_imbalance, hist_pred_imbalance; /* learned-splitter diagnostics */
+  double range_imbalance;            /* max / mean keys per key range (summed over partitions) */
 } kite_gpu_stats;
 
 /* Merge input: one .kite file's partition table, with payloads in host memory

@@ -45,21 +45,29 @@ void launch_newline_count(const uint8_t* arena, const BlockDesc* blocks, uint32_
 }
 
 // ---------------------------------------------------------------------------
-// Rolling extraction over one thread's byte range.  `sb` is indexed by
-// (pos + kHalo - blk_start).  Warm-up bytes before `ts` only seed the window;
-// a newline resets it, so bytes of earlier lines never leak into a k-mer.
+// Shared-memory byte layout of a block: block-relative byte rel = pos + kHalo
+// - blk_start lives in segment rel >> pts (one thread's range of PT = 1 << pts
+// bytes) at a stride of PT + 4 bytes, so the 32 lanes of a warp, each walking
+// its own range, read 32 different banks.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pidx(uint32_t rel, uint32_t pts) {
+  return (rel >> pts) * ((1u << pts) + 4u) + (rel & ((1u << pts) - 1u));
+}
+
+// Rolling extraction over one thread's byte range.  Warm-up bytes before `ts`
+// only seed the window; a newline resets it, so bytes of earlier lines never
+// leak into a k-mer.
 template <class T, class F>
-__device__ __forceinline__ void roll_range(const uint8_t* sb, uint64_t blk_start, uint64_t ws, uint64_t ts,
-                                           uint64_t te, unsigned phase, bool chunk_ok, const uint8_t* table,
-                                           uint32_t k, bool canonical, F&& emit) {
+__device__ __forceinline__ void roll_range(const uint8_t* sb, uint32_t pts, uint64_t blk_start, uint64_t ws,
+                                           uint64_t ts, uint64_t te, unsigned phase, bool chunk_ok,
+                                           const uint8_t* table, uint32_t k, bool canonical, F&& emit) {
   const T mask = (2 * k == (uint32_t)KeyTraits<T>::kBits) ? ~T(0) : ((T(1) << (2 * k)) - T(1));
   const unsigned rsh = 2 * (k - 1);
   T fwd = 0, rev = 0;
   uint32_t run = 0;
   unsigned ph = phase;
   for (uint64_t pos = ws; pos < te; ++pos) {
-    const uint8_t b = sb[pos + kHalo - blk_start];
+    const uint8_t b = sb[pidx((uint32_t)(pos + kHalo - blk_start), pts)];
     if (b == '\n') {
       fwd = 0;
       rev = 0;
@@ -89,9 +97,15 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   return x;
 }
 
+__host__ __device__ __forceinline__ size_t padded_bytes(uint32_t blk_bytes) {
+  const size_t pt = blk_bytes / kExtractThreads;
+  const size_t segs = ((size_t)kHalo + blk_bytes + 16 + pt - 1) / pt;
+  return (segs * (pt + 4) + 15) & ~(size_t)15;
+}
+
 size_t extract_smem_bytes(int key_bytes, uint32_t blk_bytes, uint32_t partitions, bool scatter) {
   (void)key_bytes;
-  size_t o = ((size_t)kHalo + blk_bytes + 16 + 15) & ~(size_t)15;
+  size_t o = padded_bytes(blk_bytes);
   if (scatter) o += (size_t)partitions * 8;  // reservation base (u64)
   o += (size_t)partitions * 4;               // histogram / cursor
   o += 34 * 4 + 256;                         // scan scratch + base table
@@ -106,7 +120,7 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract(ExtractParams<T> p)
   extern __shared__ __align__(16) uint8_t sm[];
   const uint32_t P = p.partitions;
   uint8_t* sb = sm;
-  size_t o = ((size_t)kHalo + p.blk_bytes + 16 + 15) & ~(size_t)15;
+  size_t o = padded_bytes(p.blk_bytes);
   unsigned long long* base = reinterpret_cast<unsigned long long*>(sm + o);
   if (MODE == 1) o += (size_t)P * 8;
   unsigned* hist = reinterpret_cast<unsigned*>(sm + o);
@@ -118,8 +132,18 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract(ExtractParams<T> p)
   const BlockDesc d = p.blocks[blockIdx.x];
   const uint64_t s = d.start, e = d.end;
   const uint64_t hs = (s - d.chunk_start >= (uint64_t)kHalo) ? s - kHalo : d.chunk_start;
-  for (uint64_t w = (hs >> 4) + threadIdx.x; w < ((e + 15) >> 4); w += NT)
-    *reinterpret_cast<uint4*>(sb + (w * 16 + kHalo - s)) = reinterpret_cast<const uint4*>(p.arena)[w];
+  const uint32_t PT = p.blk_bytes / NT;
+  const uint32_t pts = 31 - __clz(PT);
+  // coalesced 16-byte loads, stored as four 4-byte words (PT >= 4, so a word
+  // never straddles a segment and its padded address stays 4-byte aligned)
+  for (uint64_t w = (hs >> 4) + threadIdx.x; w < ((e + 15) >> 4); w += NT) {
+    const uint4 v = reinterpret_cast<const uint4*>(p.arena)[w];
+    const uint32_t rel = (uint32_t)(w * 16 + kHalo - s);
+    *reinterpret_cast<uint32_t*>(sb + pidx(rel, pts)) = v.x;
+    *reinterpret_cast<uint32_t*>(sb + pidx(rel + 4, pts)) = v.y;
+    *reinterpret_cast<uint32_t*>(sb + pidx(rel + 8, pts)) = v.z;
+    *reinterpret_cast<uint32_t*>(sb + pidx(rel + 12, pts)) = v.w;
+  }
   for (int i = threadIdx.x; i < 256; i += NT) {
     uint8_t v = 255;
     if (i == 'A' || i == 'a') v = 0;
@@ -131,11 +155,10 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract(ExtractParams<T> p)
   for (uint32_t b = threadIdx.x; b < P; b += NT) hist[b] = 0;
   __syncthreads();
 
-  const uint32_t PT = p.blk_bytes / NT;
   const uint64_t ts = s + (uint64_t)threadIdx.x * PT;
   const uint64_t te = ts < e ? (ts + PT < e ? ts + PT : e) : ts;
   unsigned nl = 0;
-  for (uint64_t pos = ts; pos < te; ++pos) nl += sb[pos + kHalo - s] == '\n';
+  for (uint64_t pos = ts; pos < te; ++pos) nl += sb[pidx((uint32_t)(pos + kHalo - s), pts)] == '\n';
   unsigned nl_total;
   const unsigned nl_before = block_exclusive_scan<NT, unsigned>(nl, scan_sm, &nl_total);
   const unsigned long long line0 = p.block_nl_excl[blockIdx.x] - p.block_nl_excl[d.first_block];
@@ -148,7 +171,7 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract(ExtractParams<T> p)
   if (MODE == 0) {
     unsigned long long kmers = 0;
     const bool sampling = p.sample != nullptr && (d.flags & 2u);
-    roll_range<T>(sb, s, ws, ts, te, phase, chunk_ok, table, p.k, canon, [&](T key, uint64_t pos) {
+    roll_range<T>(sb, pts, s, ws, ts, te, phase, chunk_ok, table, p.k, canon, [&](T key, uint64_t pos) {
       kmers++;
       atomicAdd(&hist[bucket_of(key, shift)], 1u);
       if (sampling && (mix64(pos) & p.sample_mask) == 0) {
@@ -160,9 +183,9 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract(ExtractParams<T> p)
     unsigned long long reads = 0, bases = 0;
     if (chunk_ok) {
       unsigned ph = phase;
-      uint8_t prev = ts > d.chunk_start ? sb[ts - 1 + kHalo - s] : (uint8_t)'\n';
+      uint8_t prev = ts > d.chunk_start ? sb[pidx((uint32_t)(ts - 1 + kHalo - s), pts)] : (uint8_t)'\n';
       for (uint64_t pos = ts; pos < te; ++pos) {
-        const uint8_t b = sb[pos + kHalo - s];
+        const uint8_t b = sb[pidx((uint32_t)(pos + kHalo - s), pts)];
         if (b == '\n') {
           ph = (ph + 1) & 3;
         } else if (ph == 1) {
@@ -187,7 +210,7 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract(ExtractParams<T> p)
       if (bases) atomicAdd(&p.totals->bases, bases);
     }
   } else {
-    roll_range<T>(sb, s, ws, ts, te, phase, chunk_ok, table, p.k, canon,
+    roll_range<T>(sb, pts, s, ws, ts, te, phase, chunk_ok, table, p.k, canon,
                   [&](T key, uint64_t) { atomicAdd(&hist[bucket_of(key, shift)], 1u); });
     __syncthreads();
     for (uint32_t b = threadIdx.x; b < P; b += NT) {
@@ -204,7 +227,7 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract(ExtractParams<T> p)
       hist[b] = 0;
     }
     __syncthreads();
-    roll_range<T>(sb, s, ws, ts, te, phase, chunk_ok, table, p.k, canon, [&](T key, uint64_t) {
+    roll_range<T>(sb, pts, s, ws, ts, te, phase, chunk_ok, table, p.k, canon, [&](T key, uint64_t) {
       const uint32_t b = bucket_of(key, shift);
       const unsigned slot = atomicAdd(&hist[b], 1u);
       const unsigned long long r = base[b];
@@ -234,109 +257,143 @@ template void launch_extract_scatter<u128>(const ExtractParams<u128>&, uint32_t,
 // Level-2 split: inside every hash bucket, route keys to S key-range tiles by
 // the splitters (upper bound = number of splitters <= key).  Tiles are laid
 // out bucket-major, so each bucket's tiles stay contiguous and in key order.
+// Each bucket is cut into G parts; part (b, g) owns the sub-range
+// [off[(b*S+j)*G+g], +cnt) of tile (b, j), so no two CTAs share a cursor and
+// the only atomics are shared-memory ones.
 // ---------------------------------------------------------------------------
+// Tile of a key = number of splitters <= key.  A lookup table over the top
+// kLutBits of the key gives the number of splitters below the key's bin; a
+// short forward scan covers the splitters inside the bin (exact for any
+// ascending splitters).
+static constexpr int kLutBits = 12;
+
 template <class T>
-__device__ __forceinline__ uint32_t tile_of(const T* spl, uint32_t S, T key) {
-  uint32_t j = 0;
-  for (uint32_t step = S >> 1; step; step >>= 1)
-    if (spl[j + step - 1] <= key) j += step;
+__device__ __forceinline__ uint32_t tile_of(const T* spl, const uint16_t* lut, uint32_t lut_shift, uint32_t S,
+                                            T key) {
+  uint32_t j = lut[(uint32_t)(uint64_t)(key >> lut_shift)];
+  while (j + 1 < S && spl[j] <= key) ++j;
   return j;
 }
 
-static constexpr int kSplitThreads = 256;
+// Loads the splitters and builds the table (block-wide; ends with a barrier).
+template <class T>
+__device__ __forceinline__ void load_splitters(const T* g_spl, uint32_t S, uint32_t key_bits, T* spl, uint16_t* lut,
+                                               uint32_t* lut_shift) {
+  for (uint32_t i = threadIdx.x; i + 1 < S; i += blockDim.x) spl[i] = g_spl[i];
+  __syncthreads();
+  const uint32_t L = key_bits < (uint32_t)kLutBits ? key_bits : (uint32_t)kLutBits;
+  *lut_shift = key_bits - L;
+  for (uint32_t bin = threadIdx.x; bin < (1u << L); bin += blockDim.x) {
+    const T start = (T)bin << *lut_shift;
+    uint32_t lo = 0, hi = S - 1;  // lower_bound over S-1 splitters
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (spl[mid] < start) lo = mid + 1;
+      else hi = mid;
+    }
+    lut[bin] = (uint16_t)lo;
+  }
+  __syncthreads();
+}
+
+static constexpr size_t kLutBytes = ((size_t)(1u << kLutBits) * 2 + 15) & ~(size_t)15;
+
+static constexpr int kSplitThreads = 512;
+
+__device__ __forceinline__ void part_range(const unsigned long long* boff, const unsigned long long* bcnt,
+                                           uint32_t b, uint32_t g, uint32_t G, uint64_t* lo, uint64_t* hi) {
+  const uint64_t n = bcnt[b], base = boff[b];
+  *lo = base + n * g / G;
+  *hi = base + n * (g + 1) / G;
+}
 
 template <class T>
 __global__ void __launch_bounds__(kSplitThreads) k_tile_hist(TileSplitParams<T> p) {
   extern __shared__ __align__(16) uint8_t sm[];
-  const uint32_t S = p.S;
+  const uint32_t S = p.S, G = p.G;
   T* spl = reinterpret_cast<T*>(sm);
-  unsigned* hist = reinterpret_cast<unsigned*>(spl + S);
-  const SliceDesc sl = p.slices[blockIdx.x];
-  for (uint32_t i = threadIdx.x; i + 1 < S; i += blockDim.x) spl[i] = p.splitters[i];
+  uint16_t* lut = reinterpret_cast<uint16_t*>(sm + (size_t)S * sizeof(T));
+  unsigned* hist = reinterpret_cast<unsigned*>(sm + (size_t)S * sizeof(T) + kLutBytes);
+  const uint32_t b = blockIdx.x / G, g = blockIdx.x % G;
   for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) hist[i] = 0;
+  uint32_t lsh;
+  load_splitters(p.splitters, S, p.key_bits, spl, lut, &lsh);
+  uint64_t lo, hi;
+  part_range(p.bucket_off, p.bucket_count, b, g, G, &lo, &hi);
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+    atomicAdd(&hist[tile_of(spl, lut, lsh, S, p.keys_in[i])], 1u);
   __syncthreads();
-  const T* src = p.keys_in + sl.start;
-  for (uint32_t i = threadIdx.x; i < sl.len; i += blockDim.x) atomicAdd(&hist[tile_of(spl, S, src[i])], 1u);
-  __syncthreads();
-  unsigned long long* tc = p.tile_count + (size_t)sl.bucket * S;
   for (uint32_t j = threadIdx.x; j < S; j += blockDim.x)
-    if (hist[j]) atomicAdd(&tc[j], (unsigned long long)hist[j]);
+    p.tile_count[((size_t)b * S + j) * G + g] = hist[j];
 }
 
-template <class T, int ITEMS>
+template <class T>
 __global__ void __launch_bounds__(kSplitThreads) k_tile_scatter(TileSplitParams<T> p) {
   extern __shared__ __align__(16) uint8_t sm[];
-  const uint32_t S = p.S;
+  const uint32_t S = p.S, G = p.G;
   unsigned long long* base = reinterpret_cast<unsigned long long*>(sm);
   T* spl = reinterpret_cast<T*>(base + S);
-  unsigned* hist = reinterpret_cast<unsigned*>(spl + S);
-  const SliceDesc sl = p.slices[blockIdx.x];
-  for (uint32_t i = threadIdx.x; i + 1 < S; i += blockDim.x) spl[i] = p.splitters[i];
-  for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) hist[i] = 0;
-  __syncthreads();
-  const T* src = p.keys_in + sl.start;
-  T key[ITEMS];
-  uint32_t tj[ITEMS];
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    const uint32_t i = r * kSplitThreads + threadIdx.x;
-    tj[r] = 0xffffffffu;
-    if (i < sl.len) {
-      key[r] = src[i];
-      tj[r] = tile_of(spl, S, key[r]);
-      atomicAdd(&hist[tj[r]], 1u);
-    }
-  }
-  __syncthreads();
-  const size_t tb = (size_t)sl.bucket * S;
+  uint16_t* lut = reinterpret_cast<uint16_t*>(sm + (size_t)S * 8 + (size_t)S * sizeof(T));
+  unsigned* cur = reinterpret_cast<unsigned*>(sm + (size_t)S * 8 + (size_t)S * sizeof(T) + kLutBytes);
+  const uint32_t b = blockIdx.x / G, g = blockIdx.x % G;
   for (uint32_t j = threadIdx.x; j < S; j += blockDim.x) {
-    const unsigned h = hist[j];
-    unsigned long long r = 0;
-    if (h) {
-      r = atomicAdd(&p.tile_fill[tb + j], (unsigned long long)h);
-      if (r + h > p.tile_count[tb + j]) {
-        dev_fail(p.status, KITE_DEV_REGION_OVERFLOW, (unsigned)(tb + j), (unsigned)r, h);
-        r = ~0ull;
-      } else {
-        r += p.tile_off[tb + j];
-      }
-    }
-    base[j] = r;
-    hist[j] = 0;
+    base[j] = p.tile_off[((size_t)b * S + j) * G + g];
+    cur[j] = 0;
   }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    if (tj[r] != 0xffffffffu) {
-      const unsigned slot = atomicAdd(&hist[tj[r]], 1u);
-      const unsigned long long b0 = base[tj[r]];
-      if (b0 != ~0ull) p.keys_out[b0 + slot] = key[r];
-    }
+  uint32_t lsh;
+  load_splitters(p.splitters, S, p.key_bits, spl, lut, &lsh);
+  uint64_t lo, hi;
+  part_range(p.bucket_off, p.bucket_count, b, g, G, &lo, &hi);
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const T key = p.keys_in[i];
+    const uint32_t j = tile_of(spl, lut, lsh, S, key);
+    const unsigned slot = atomicAdd(&cur[j], 1u);
+    p.keys_out[base[j] + slot] = key;
   }
 }
 
+// Tile list from the scanned part offsets: tile t = (b, j) starts at
+// off[t*G] and ends where tile t+1 starts (the last at n_keys).
+__global__ void k_make_tiles(const unsigned long long* __restrict__ off, uint32_t ntiles, uint32_t S, uint32_t G,
+                             unsigned long long n_keys, TileDesc* __restrict__ tiles, uint32_t* __restrict__ lens) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const unsigned long long a = off[(size_t)t * G];
+  const unsigned long long e = t + 1 < ntiles ? off[(size_t)(t + 1) * G] : n_keys;
+  TileDesc d;
+  d.start = a;
+  d.len = (uint32_t)(e - a);
+  d.bucket = t / S;
+  tiles[t] = d;
+  lens[t] = d.len;
+}
+
+size_t tile_split_smem(int key_bytes, uint32_t S, bool scatter) {
+  return (scatter ? (size_t)S * 8 : 0) + (size_t)S * key_bytes + kLutBytes + (size_t)S * 4;
+}
+
 template <class T>
-void launch_tile_hist(const TileSplitParams<T>& p, uint32_t nslices, uint32_t, cudaStream_t s) {
-  const size_t smem = (size_t)p.S * sizeof(T) + (size_t)p.S * 4;
+void launch_tile_hist(const TileSplitParams<T>& p, cudaStream_t s) {
+  const size_t smem = tile_split_smem(sizeof(T), p.S, false);
   cudaFuncSetAttribute(k_tile_hist<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (nslices) k_tile_hist<T><<<nslices, kSplitThreads, smem, s>>>(p);
+  k_tile_hist<T><<<p.P * p.G, kSplitThreads, smem, s>>>(p);
 }
 
 template <class T>
-constexpr int split_items() { return sizeof(T) == 8 ? 16 : 8; }
-
-uint32_t split_slice_keys(int key_bytes) { return kSplitThreads * (key_bytes == 8 ? 16 : 8); }
-
-template <class T>
-void launch_tile_scatter(const TileSplitParams<T>& p, uint32_t nslices, uint32_t, cudaStream_t s) {
-  const size_t smem = (size_t)p.S * 8 + (size_t)p.S * sizeof(T) + (size_t)p.S * 4;
-  cudaFuncSetAttribute(k_tile_scatter<T, split_items<T>()>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
-  if (nslices) k_tile_scatter<T, split_items<T>()><<<nslices, kSplitThreads, smem, s>>>(p);
+void launch_tile_scatter(const TileSplitParams<T>& p, cudaStream_t s) {
+  const size_t smem = tile_split_smem(sizeof(T), p.S, true);
+  cudaFuncSetAttribute(k_tile_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_tile_scatter<T><<<p.P * p.G, kSplitThreads, smem, s>>>(p);
 }
-template void launch_tile_hist<uint64_t>(const TileSplitParams<uint64_t>&, uint32_t, uint32_t, cudaStream_t);
-template void launch_tile_hist<u128>(const TileSplitParams<u128>&, uint32_t, uint32_t, cudaStream_t);
-template void launch_tile_scatter<uint64_t>(const TileSplitParams<uint64_t>&, uint32_t, uint32_t, cudaStream_t);
-template void launch_tile_scatter<u128>(const TileSplitParams<u128>&, uint32_t, uint32_t, cudaStream_t);
+
+void launch_make_tiles(const unsigned long long* off, uint32_t ntiles, uint32_t S, uint32_t G,
+                       unsigned long long n_keys, TileDesc* tiles, uint32_t* lens, cudaStream_t s) {
+  if (ntiles) k_make_tiles<<<(ntiles + 255) / 256, 256, 0, s>>>(off, ntiles, S, G, n_keys, tiles, lens);
+}
+
+template void launch_tile_hist<uint64_t>(const TileSplitParams<uint64_t>&, cudaStream_t);
+template void launch_tile_hist<u128>(const TileSplitParams<u128>&, cudaStream_t);
+template void launch_tile_scatter<uint64_t>(const TileSplitParams<uint64_t>&, cudaStream_t);
+template void launch_tile_scatter<u128>(const TileSplitParams<u128>&, cudaStream_t);
 
 }  // namespace kite

@@ -155,7 +155,8 @@ template <int NT, int ITEMS, int RADIX>
 __device__ __forceinline__ void block_rank(const unsigned (&digit)[ITEMS], const bool (&valid)[ITEMS],
                                            unsigned (&dest)[ITEMS], unsigned* warp_hist, unsigned* scan_smem,
                                            unsigned* digit_total /* RADIX entries or nullptr */,
-                                           unsigned* digit_start /* RADIX entries or nullptr */) {
+                                           unsigned* digit_start /* RADIX entries or nullptr */,
+                                           int items = ITEMS /* rounds in use (block-uniform) */) {
   constexpr int NW = NT / 32;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
@@ -164,6 +165,7 @@ __device__ __forceinline__ void block_rank(const unsigned (&digit)[ITEMS], const
   __syncwarp();
 #pragma unroll
   for (int r = 0; r < ITEMS; ++r) {
+    if (r >= items) break;
     const unsigned d = valid[r] ? digit[r] : (unsigned)RADIX;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const unsigned before = __popc(peers & lt);

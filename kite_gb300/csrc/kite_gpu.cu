@@ -106,7 +106,7 @@ struct kite_gpu_ctx {
   // scratch
   DevBuf blocks, nl, scan_tmp, bucket_count, bucket_off, bucket_fill, totals, status;
   DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, splitters2, hist16;
-  DevBuf slices, tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
+  DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
   HostBuf h_blocks, h_small, h_tiles, h_out;
   std::vector<cudaEvent_t> ev;  // stage events
 
@@ -378,57 +378,53 @@ int run_count(kite_gpu_ctx* ctx) {
     st.hist_pred_imbalance = hist_imb;
     st.splitter_used = learned ? KITE_SPLIT_LEARNED : KITE_SPLIT_SAMPLED;
     const T* chosen = learned ? mlp_spl : hist_spl;
-    const uint32_t sk = split_slice_keys(sizeof(T));
-    std::vector<SliceDesc> hsl;
-    for (uint32_t b = 0; b < P; ++b)
-      for (uint64_t o = 0; o < bcount[b]; o += sk)
-        hsl.push_back(SliceDesc{boff[b] + o, (uint32_t)std::min<uint64_t>(sk, bcount[b] - o), b});
-    const size_t nt = (size_t)P * S;
-    KCU(ctx->slices.ensure(hsl.size() * sizeof(SliceDesc)));
-    KCU(ctx->h_tiles.ensure(std::max(hsl.size() * sizeof(SliceDesc), nt * (sizeof(TileDesc) + 8))));
-    std::memcpy(ctx->h_tiles.p, hsl.data(), hsl.size() * sizeof(SliceDesc));
-    KCU(cudaMemcpyAsync(ctx->slices.p, ctx->h_tiles.p, hsl.size() * sizeof(SliceDesc), cudaMemcpyHostToDevice, s));
-    KCU(ctx->tile_count.ensure(nt * 8));
-    KCU(ctx->tile_off.ensure(nt * 8));
-    KCU(ctx->tile_fill.ensure(nt * 8));
-    KCU(ctx->scan_tmp.ensure(scan_tmp_elems(nt) * 8 + 64));
-    KCU(cudaMemsetAsync(ctx->tile_count.p, 0, nt * 8, s));
-    KCU(cudaMemsetAsync(ctx->tile_fill.p, 0, nt * 8, s));
+    // G parts per bucket: enough CTAs to fill the GPU twice, parts of >= 32K keys
+    uint32_t G = (uint32_t)std::max<uint64_t>(1, (2ull * 152 + P - 1) / P);
+    G = (uint32_t)std::min<uint64_t>(G, std::max<uint64_t>(1, maxb / 32768));
+    G = std::min<uint32_t>(G, 64);
+    const size_t nt = (size_t)P * S, ntg = nt * G;
+    KCU(ctx->tile_count.ensure(ntg * 8));
+    KCU(ctx->tile_off.ensure(ntg * 8));
+    KCU(ctx->scan_tmp.ensure(scan_tmp_elems(ntg) * 8 + 64));
     TileSplitParams<T> tp{};
     tp.keys_in = ctx->keys_a.as<T>();
     tp.keys_out = ctx->keys_b.as<T>();
-    tp.slices = ctx->slices.as<SliceDesc>();
+    tp.bucket_off = ctx->bucket_off.as<unsigned long long>();
+    tp.bucket_count = ctx->bucket_count.as<unsigned long long>();
     tp.splitters = chosen;
+    tp.P = P;
     tp.S = S;
+    tp.G = G;
+    tp.key_bits = 2 * k;
     tp.tile_count = ctx->tile_count.as<unsigned long long>();
     tp.tile_off = ctx->tile_off.as<unsigned long long>();
-    tp.tile_fill = ctx->tile_fill.as<unsigned long long>();
-    tp.status = ctx->status.as<DevStatus>();
-    launch_tile_hist<T>(tp, (uint32_t)hsl.size(), sk, s);
-    st.kernel_launches += 2 + exclusive_scan_u64(tp.tile_count, ctx->tile_off.as<unsigned long long>(), nt,
+    launch_tile_hist<T>(tp, s);
+    st.kernel_launches += 3 + exclusive_scan_u64(tp.tile_count, ctx->tile_off.as<unsigned long long>(), ntg,
                                                  ctx->scan_tmp.as<unsigned long long>(), s);
-    launch_tile_scatter<T>(tp, (uint32_t)hsl.size(), sk, s);
+    launch_tile_scatter<T>(tp, s);
+    KCU(ctx->tiles.ensure(nt * sizeof(TileDesc)));
+    KCU(ctx->tile_fill.ensure(nt * 4));
+    launch_make_tiles(ctx->tile_off.as<unsigned long long>(), (uint32_t)nt, S, G, N, ctx->tiles.as<TileDesc>(),
+                      ctx->tile_fill.as<uint32_t>(), s);
     KCU(cudaGetLastError());
-    // tile counts/offsets to host to build the tile list
-    uint64_t* htc = reinterpret_cast<uint64_t*>(ctx->h_tiles.as<uint8_t>() + nt * sizeof(TileDesc));
-    KCU(cudaMemcpyAsync(htc, ctx->tile_count.p, nt * 8, cudaMemcpyDeviceToHost, s));
+    KCU(ctx->h_tiles.ensure(nt * 4 + 64));
+    KCU(cudaMemcpyAsync(ctx->h_tiles.p, ctx->tile_fill.p, nt * 4, cudaMemcpyDeviceToHost, s));
     rc = wait_stream(ctx, s);
     if (rc) return rc;
+    const uint32_t* lens = ctx->h_tiles.as<uint32_t>();
     ht.resize(nt);
-    uint64_t a2 = 0;
-    for (size_t t = 0; t < nt; ++t) {
-      ht[t] = TileDesc{a2, (uint32_t)htc[t], (uint32_t)(t / S)};
-      a2 += htc[t];
-    }
+    for (size_t t = 0; t < nt; ++t) ht[t] = TileDesc{0, lens[t], (uint32_t)(t / S)};
     sorted = ctx->keys_b.as<T>();
     scratch = ctx->keys_a.as<T>();
   }
   KCU(cudaEventRecord(ctx->ev[4], s));
   const uint32_t ntiles = (uint32_t)ht.size();
   std::vector<uint32_t> big;
+  std::vector<uint64_t> range(S, 0);
   uint64_t tmax = 0, tsum = 0, tne = 0;
   for (uint32_t t = 0; t < ntiles; ++t) {
     if (ht[t].len > CAP) big.push_back(t);
+    range[t % S] += ht[t].len;
     if (ht[t].len) {
       tmax = std::max<uint64_t>(tmax, ht[t].len);
       tsum += ht[t].len;
@@ -438,15 +434,19 @@ int run_count(kite_gpu_ctx* ctx) {
   st.tiles = ntiles;
   st.big_tiles = (uint32_t)big.size();
   st.tile_imbalance = tne ? (double)tmax / ((double)tsum / (double)tne) : 0.0;
-  KCU(ctx->h_tiles.ensure(ht.size() * sizeof(TileDesc) + big.size() * 4 + 64));
-  std::memcpy(ctx->h_tiles.p, ht.data(), ht.size() * sizeof(TileDesc));
-  std::memcpy(ctx->h_tiles.as<uint8_t>() + ht.size() * sizeof(TileDesc), big.data(), big.size() * 4);
-  KCU(ctx->tiles.ensure(ht.size() * sizeof(TileDesc)));
+  st.range_imbalance = (double)*std::max_element(range.begin(), range.end()) / ((double)N / S);
+  KCU(ctx->h_tiles.ensure(std::max(ht.size() * sizeof(TileDesc), ht.size() * 4) + big.size() * 4 + 64));
+  if (S == 1) {
+    std::memcpy(ctx->h_tiles.p, ht.data(), ht.size() * sizeof(TileDesc));
+    KCU(ctx->tiles.ensure(ht.size() * sizeof(TileDesc)));
+    KCU(cudaMemcpyAsync(ctx->tiles.p, ctx->h_tiles.p, ht.size() * sizeof(TileDesc), cudaMemcpyHostToDevice, s));
+  }
   KCU(ctx->big_ids.ensure(big.size() * 4 + 4));
-  KCU(cudaMemcpyAsync(ctx->tiles.p, ctx->h_tiles.p, ht.size() * sizeof(TileDesc), cudaMemcpyHostToDevice, s));
-  if (!big.empty())
-    KCU(cudaMemcpyAsync(ctx->big_ids.p, ctx->h_tiles.as<uint8_t>() + ht.size() * sizeof(TileDesc), big.size() * 4,
-                        cudaMemcpyHostToDevice, s));
+  if (!big.empty()) {
+    uint8_t* hb2 = ctx->h_tiles.as<uint8_t>() + std::max(ht.size() * sizeof(TileDesc), ht.size() * 4);
+    std::memcpy(hb2, big.data(), big.size() * 4);
+    KCU(cudaMemcpyAsync(ctx->big_ids.p, hb2, big.size() * 4, cudaMemcpyHostToDevice, s));
+  }
   KCU(ctx->tile_out.ensure((size_t)ntiles * sizeof(TileOut<T>)));
 
   // ---- K4 tile sort + RLE ---------------------------------------------------
@@ -612,7 +612,7 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
   for (auto e : ctx->ev) cudaEventDestroy(e);
   DevBuf* bufs[] = {&ctx->arena, &ctx->blocks, &ctx->nl, &ctx->scan_tmp, &ctx->bucket_count, &ctx->bucket_off,
                     &ctx->bucket_fill, &ctx->totals, &ctx->status, &ctx->keys_a, &ctx->keys_b, &ctx->counts,
-                    &ctx->sample, &ctx->sample_count, &ctx->splitters, &ctx->splitters2, &ctx->hist16, &ctx->slices,
+                    &ctx->sample, &ctx->sample_count, &ctx->splitters, &ctx->splitters2, &ctx->hist16,
                     &ctx->tile_count, &ctx->tile_off, &ctx->tile_fill, &ctx->tiles, &ctx->big_ids,
                     &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out};
   for (DevBuf* b : bufs) b->release();

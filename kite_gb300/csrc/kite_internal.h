@@ -19,13 +19,6 @@ struct BlockDesc {
   uint32_t flags;        // bit 1: block of the segment's first chunk (key sample source)
 };
 
-// A contiguous slice of one hash bucket's keys (level-2 tiling work unit).
-struct SliceDesc {
-  uint64_t start;   // key index
-  uint32_t len;     // keys
-  uint32_t bucket;
-};
-
 // A key-range tile: the on-chip sort unit.
 struct TileDesc {
   uint64_t start;   // key index of the tile's first key
@@ -72,15 +65,17 @@ struct ExtractParams {
 
 template <class T>
 struct TileSplitParams {
-  const T* keys_in;
-  T* keys_out;
-  const SliceDesc* slices;
+  const T* keys_in;       // bucket-grouped keys
+  T* keys_out;            // tile-grouped keys
+  const unsigned long long* bucket_off;    // [P]
+  const unsigned long long* bucket_count;  // [P]
   const T* splitters;     // S-1 ascending keys
+  uint32_t P;
   uint32_t S;             // tiles per bucket (power of two)
-  unsigned long long* tile_count;       // [P*S]
-  const unsigned long long* tile_off;   // [P*S]
-  unsigned long long* tile_fill;        // [P*S]
-  DevStatus* status;
+  uint32_t G;             // parts per bucket
+  uint32_t key_bits;      // 2k: significant key bits (splitter lookup table)
+  unsigned long long* tile_count;       // [P*S*G] (tile-major, part-minor)
+  const unsigned long long* tile_off;   // exclusive scan of tile_count
 };
 
 // ---- launchers (count_kernels.cu) ----
@@ -91,11 +86,13 @@ void launch_extract_hist(const ExtractParams<T>& p, uint32_t nblocks, cudaStream
 template <class T>
 void launch_extract_scatter(const ExtractParams<T>& p, uint32_t nblocks, cudaStream_t s);
 template <class T>
-void launch_tile_hist(const TileSplitParams<T>& p, uint32_t nslices, uint32_t slice_keys, cudaStream_t s);
+void launch_tile_hist(const TileSplitParams<T>& p, cudaStream_t s);
 template <class T>
-void launch_tile_scatter(const TileSplitParams<T>& p, uint32_t nslices, uint32_t slice_keys, cudaStream_t s);
+void launch_tile_scatter(const TileSplitParams<T>& p, cudaStream_t s);
+void launch_make_tiles(const unsigned long long* off, uint32_t ntiles, uint32_t S, uint32_t G,
+                       unsigned long long n_keys, TileDesc* tiles, uint32_t* lens, cudaStream_t s);
+size_t tile_split_smem(int key_bytes, uint32_t S, bool scatter);
 size_t extract_smem_bytes(int key_bytes, uint32_t blk_bytes, uint32_t partitions, bool scatter);
-uint32_t split_slice_keys(int key_bytes);
 
 // ---- scan.cu ----
 // Exclusive scan of n u64 values (in may equal out).  `tmp` needs

@@ -118,6 +118,7 @@ __global__ void k_seg_decode(const uint8_t* __restrict__ bytes, const SegDesc* _
       sh += 7;
       if (is_term(b)) break;
     }
+    if (q > d.end) break;  // terminator in the next segment: that segment owns this varint
     if (v >= nvar) break;  // bytes after the last row are ignored, as the reference decodes row_count rows
     if ((v & 1ull) == 0) {
       acc += val;  // wrapping add, as the reference's wrapping_add
@@ -200,7 +201,8 @@ struct MergeSmem {
   static constexpr size_t tag = (size_t)kMergeCap * 2;
   static constexpr size_t perm = (size_t)kMergeCap * 2;
   static constexpr size_t head = (size_t)(kMergeCap + 1) * 2;
-  static constexpr size_t seg = (size_t)(kMaxTileStreams + 1) * 4 + kMaxTileStreams * 4;
+  // every region starts 16-byte aligned (misc holds 8-byte scan values)
+  static constexpr size_t seg = ((size_t)(kMaxTileStreams + 1) * 4 + kMaxTileStreams * 4 + 15) & ~(size_t)15;
   static constexpr size_t misc = 64 * 8;
   static constexpr size_t total = keys + cnts + tag + perm + ((head + 15) & ~(size_t)15) + seg + misc;
 };
@@ -222,7 +224,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
   uint32_t* sstart = reinterpret_cast<uint32_t*>(sm + L::keys + L::cnts + L::tag + L::perm +
                                                  ((L::head + 15) & ~(size_t)15));
   uint32_t* sinput = sstart + kMaxTileStreams + 1;
-  unsigned long long* misc = reinterpret_cast<unsigned long long*>(sinput + kMaxTileStreams);
+  unsigned long long* misc = reinterpret_cast<unsigned long long*>(reinterpret_cast<uint8_t*>(sstart) + L::seg);
 
   const MergeTile mt = tiles[blockIdx.x];
   const uint32_t nts = mt.nts, n = mt.rows_in;

@@ -3,16 +3,24 @@
 // tile splitters.  No counterpart in the reference: it only moves tile
 // boundaries, so counts stay exact whatever it predicts.
 //
-// Model: x = the top 32 bits of the 2k-bit key (below the fixed zero bits),
-// as 32 features in {0,1};  h1 = relu(W1 x + b1) (64);  h2 = relu(W2 h1 + b2)
-// (64);  y = w3 . h2 + b3  ~  CDF(key) in [0,1].  Loss = mean (y - rank/n)^2
-// over the sampled keys (ranks from a sort of the sample).  The CDF is
-// inverted by a bit-by-bit search per splitter, which only needs y to be
-// non-decreasing to be exact and stays well defined otherwise; splitters are
-// sorted afterwards.  The predicted max/mean tile load on the sample decides
-// between these splitters and the histogram fallback.
+// Model.  Let V(key) be the top 48 of the 2k key bits; its top 16 bits are the
+// key's bin b, the next 32 bits its place inside the bin.  With C(b) and m(b)
+// the sample counts below and inside bin b (from the sample histogram),
+//     F(key) = ( C(b) + m(b) * g(V(key)) ) / n
+// where g is the MLP: 48 features in {0,1} -> 64 ReLU -> 64 ReLU -> 1.  The
+// histogram places the mass of every bin; the network learns how that mass is
+// spread inside a bin, which is what a histogram cannot resolve when one bin
+// holds more than a tile's share of keys (low-complexity, AT-rich k-mers).
+// Loss = mean over the sample of (F_hat - rank/n)^2, i.e. the global CDF
+// error, so heavy bins dominate training.
+//
+// Splitter j: the bin holding quantile j/S from the histogram, then a
+// bit-by-bit search of g inside the bin for the within-bin target.  The
+// predicted max/mean tile load of the sample decides between these splitters
+// and the histogram ones.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -21,8 +29,9 @@
 
 namespace kite {
 
-static constexpr int kIn = 32, kH = 64;
-static constexpr int kParams = kIn * kH + kH + kH * kH + kH + kH + 1;  // 6337
+static constexpr int kIn = 48, kH = 64;
+static constexpr int kBinBits = 16, kSubBits = 32;
+static constexpr int kParams = kIn * kH + kH + kH * kH + kH + kH + 1;
 
 // parameter offsets
 static constexpr int oW1 = 0, oB1 = oW1 + kIn * kH, oW2 = oB1 + kH, oB2 = oW2 + kH * kH, oW3 = oB2 + kH,
@@ -34,7 +43,8 @@ struct MlpModel {
   float* m = nullptr;
   float* v = nullptr;
   float* feats = nullptr;   // [n, kIn]
-  float* target = nullptr;  // [n]
+  float* target = nullptr;  // [n] within-bin fraction
+  float* scale = nullptr;   // [n] m(b)/n
   float* loss = nullptr;    // [1]
   uint32_t cap = 0;
   void* keys_sorted = nullptr;
@@ -42,9 +52,9 @@ struct MlpModel {
   unsigned* tile_hits = nullptr;
   uint32_t tile_cap = 0;
   uint32_t* batch_idx = nullptr;
+  unsigned* hist = nullptr;  // [65536] sample histogram, then inclusive cumulative
   float last_loss = 0;
   double last_pred_imbalance = 0;
-  double last_hist_imbalance = 0;
 };
 
 MlpModel* mlp_create() { return new MlpModel(); }
@@ -57,30 +67,55 @@ void mlp_destroy(MlpModel* m) {
   cudaFree(m->v);
   cudaFree(m->feats);
   cudaFree(m->target);
+  cudaFree(m->scale);
   cudaFree(m->loss);
   cudaFree(m->keys_sorted);
   cudaFree(m->tile_hits);
   cudaFree(m->batch_idx);
+  cudaFree(m->hist);
   delete m;
 }
 
-// ---- features ---------------------------------------------------------------
+// ---- 48-bit view of a key ---------------------------------------------------
 template <class T>
-__device__ __forceinline__ void key_features(T key, uint32_t key_bits, float* f) {
-  // top 32 bits of the key_bits-wide value
-  const int sh = (int)key_bits - kIn;
-  const uint32_t top = sh >= 0 ? (uint32_t)(uint64_t)(key >> sh) : (uint32_t)(uint64_t)(key << (-sh));
-#pragma unroll
-  for (int i = 0; i < kIn; ++i) f[i] = (float)((top >> (kIn - 1 - i)) & 1u);
+__device__ __forceinline__ uint64_t view48(T key, uint32_t key_bits) {
+  return key_bits >= 48 ? (uint64_t)(key >> (key_bits - 48)) : ((uint64_t)key << (48 - key_bits));
 }
 
 template <class T>
-__global__ void k_make_features(const T* __restrict__ sorted, uint32_t n, uint32_t key_bits, float* __restrict__ feats,
-                                float* __restrict__ target) {
+__global__ void k_bin_hist(const T* __restrict__ keys, uint32_t n, uint32_t key_bits, unsigned* __restrict__ hist) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(&hist[(uint32_t)(view48(keys[i], key_bits) >> kSubBits)], 1u);
+}
+
+// inclusive cumulative counts, one CTA
+__global__ void __launch_bounds__(1024) k_cum(unsigned* __restrict__ h) {
+  __shared__ unsigned sm[34];
+  unsigned carry = 0;
+  for (uint32_t b0 = 0; b0 < (1u << kBinBits); b0 += 1024) {
+    const unsigned v = h[b0 + threadIdx.x];
+    unsigned tot;
+    const unsigned ex = block_exclusive_scan<1024, unsigned>(v, sm, &tot);
+    h[b0 + threadIdx.x] = carry + ex + v;
+    carry += tot;
+  }
+}
+
+template <class T>
+__global__ void k_make_features(const T* __restrict__ sorted, uint32_t n, uint32_t key_bits,
+                                const unsigned* __restrict__ cum, float* __restrict__ feats,
+                                float* __restrict__ target, float* __restrict__ scale) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  key_features(sorted[i], key_bits, feats + (size_t)i * kIn);
-  target[i] = ((float)i + 0.5f) / (float)n;
+  const uint64_t v = view48(sorted[i], key_bits);
+  const uint32_t b = (uint32_t)(v >> kSubBits);
+  const unsigned hi = cum[b], lo = b ? cum[b - 1] : 0u;
+  const float m = (float)(hi - lo);
+  float* f = feats + (size_t)i * kIn;
+#pragma unroll
+  for (int q = 0; q < kIn; ++q) f[q] = (float)((v >> (kIn - 1 - q)) & 1ull);
+  target[i] = ((float)(i - lo) + 0.5f) / m;
+  scale[i] = m / (float)n;
 }
 
 // ---- forward + backward ------------------------------------------------------
@@ -88,13 +123,15 @@ __global__ void k_make_features(const T* __restrict__ sorted, uint32_t n, uint32
 // memory, feature-major with a padded stride so lanes hit distinct banks),
 // then weight-parallel gradient sums over the CTA's samples (no atomics
 // inside the CTA), one global atomicAdd per parameter per CTA.
+// Per-sample loss: (scale * (y - target))^2 / batch (scale = 1 without array).
 static constexpr int kB = 128;        // samples per CTA (== threads)
 static constexpr int kLd = kB + 1;    // padded row stride
 static constexpr size_t kFbSmem = (size_t)(kParams + kIn * kLd + 3 * kH * kLd + kB) * sizeof(float);
 
 __global__ void __launch_bounds__(kB) k_fwd_bwd(const float* __restrict__ params, const float* __restrict__ feats,
-                                                const float* __restrict__ target, const uint32_t* __restrict__ idx,
-                                                uint32_t batch, float* __restrict__ grads, float* __restrict__ loss) {
+                                                const float* __restrict__ target, const float* __restrict__ scale,
+                                                const uint32_t* __restrict__ idx, uint32_t batch,
+                                                float* __restrict__ grads, float* __restrict__ loss) {
   extern __shared__ float sm[];
   float* P = sm;                       // parameters
   float* X = P + kParams;              // [kIn][kLd]
@@ -109,7 +146,6 @@ __global__ void __launch_bounds__(kB) k_fwd_bwd(const float* __restrict__ params
   const uint32_t s = live ? idx[b] : 0;
   for (int i = 0; i < kIn; ++i) X[i * kLd + t] = live ? feats[(size_t)s * kIn + i] : 0.f;
   __syncthreads();
-  // forward
   for (int j = 0; j < kH; ++j) {
     float a = P[oB1 + j];
     for (int i = 0; i < kIn; ++i) a += P[oW1 + j * kIn + i] * X[i * kLd + t];
@@ -123,13 +159,12 @@ __global__ void __launch_bounds__(kB) k_fwd_bwd(const float* __restrict__ params
     H2[j * kLd + t] = h;
     y += P[oW3 + j] * h;
   }
-  const float e = live ? y - target[s] : 0.f;
-  const float dy = live ? 2.f * e / (float)batch : 0.f;
+  const float sc = live ? (scale ? scale[s] : 1.f) : 0.f;
+  const float e = live ? sc * (y - target[s]) : 0.f;
+  const float dy = live ? 2.f * e * sc / (float)batch : 0.f;
   DY[t] = dy;
-  // d2 = dy * w3 masked by relu
   for (int j = 0; j < kH; ++j) D[j * kLd + t] = H2[j * kLd + t] > 0.f ? dy * P[oW3 + j] : 0.f;
   __syncthreads();
-  // grads of layer 3 and layer 2 (weight-parallel over the CTA's samples)
   for (int w = t; w < kH * kH + kH + kH + 1; w += kB) {
     float g = 0.f;
     if (w < kH * kH) {
@@ -149,7 +184,6 @@ __global__ void __launch_bounds__(kB) k_fwd_bwd(const float* __restrict__ params
       atomicAdd(&grads[oB3], g);
     }
   }
-  // d1 = W2^T d2 masked by relu (per sample)
   float d1[kH];
   for (int i = 0; i < kH; ++i) d1[i] = 0.f;
   for (int j = 0; j < kH; ++j) {
@@ -160,7 +194,6 @@ __global__ void __launch_bounds__(kB) k_fwd_bwd(const float* __restrict__ params
   __syncthreads();
   for (int i = 0; i < kH; ++i) D[i * kLd + t] = H1[i * kLd + t] > 0.f ? d1[i] : 0.f;
   __syncthreads();
-  // grads of layer 1
   for (int w = t; w < kIn * kH + kH; w += kB) {
     float g = 0.f;
     if (w < kIn * kH) {
@@ -173,7 +206,6 @@ __global__ void __launch_bounds__(kB) k_fwd_bwd(const float* __restrict__ params
       atomicAdd(&grads[oB1 + j], g);
     }
   }
-  // loss
   float l = e * e / (float)batch;
   for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
   if ((t & 31) == 0 && l != 0.f) atomicAdd(loss, l);
@@ -192,14 +224,12 @@ __global__ void k_adam(float* __restrict__ p, float* __restrict__ g, float* __re
   g[i] = 0.f;
 }
 
-// Batch index generator: a fixed-stride walk through a permutation-free
-// shuffle (i * stride + offset mod n with stride coprime to n).
+// Batch indices: a strided walk (stride coprime to n) over the sample.
 __global__ void k_batch_idx(uint32_t* idx, uint32_t batch, uint32_t n, uint32_t start, uint32_t stride) {
   const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b < batch) idx[b] = (uint32_t)(((uint64_t)(start + b) * stride) % n);
 }
 
-// ---- inference: forward one key ---------------------------------------------
 __device__ float mlp_eval(const float* __restrict__ P, const float* x) {
   float h1[kH];
   for (int j = 0; j < kH; ++j) {
@@ -217,34 +247,47 @@ __device__ float mlp_eval(const float* __restrict__ P, const float* x) {
   return y;
 }
 
-// One thread per splitter: bit-by-bit search for the largest key whose
-// predicted CDF stays below j/S (the model sees the top 32 bits; lower bits
-// of the splitter stay 0).
+// One thread per splitter j: bin from the cumulative histogram, then the
+// largest 32-bit sub-position whose predicted within-bin fraction stays below
+// the target; the splitter is the first key of the next 48-bit cell.
 template <class T>
-__global__ void k_invert(const float* __restrict__ params, uint32_t S, uint32_t key_bits, T* __restrict__ spl) {
+__global__ void k_invert(const float* __restrict__ params, const unsigned* __restrict__ cum, uint32_t n, uint32_t S,
+                         uint32_t key_bits, T* __restrict__ spl) {
   extern __shared__ float P[];
   for (int i = threadIdx.x; i < kParams; i += blockDim.x) P[i] = params[i];
   __syncthreads();
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (j >= S) return;
-  const float q = (float)j / (float)S;
-  uint32_t top = 0;
-  float x[kIn];
-  for (int bit = kIn - 1; bit >= 0; --bit) {
-    const uint32_t cand = top | (1u << bit);
-#pragma unroll
-    for (int i = 0; i < kIn; ++i) x[i] = (float)((cand >> (kIn - 1 - i)) & 1u);
-    if (mlp_eval(P, x) <= q) top = cand;
+  const double q = (double)n * j / S;  // sample rank at the cut
+  uint32_t lo = 0, hi = (1u << kBinBits) - 1;
+  while (lo < hi) {  // first bin whose inclusive cumulative count exceeds q
+    const uint32_t mid = (lo + hi) >> 1;
+    if ((double)cum[mid] > q) hi = mid;
+    else lo = mid + 1;
   }
-  // splitter = first key of the next 32-bit cell
-  const int sh = (int)key_bits - kIn;
+  const uint32_t b = lo;
+  const double below = b ? cum[b - 1] : 0.0, mass = (double)cum[b] - below;
+  const float u = mass > 0 ? (float)((q - below) / mass) : 1.f;
+  uint32_t sub = 0;
+  float x[kIn];
+  for (int bit = kSubBits - 1; bit >= 0; --bit) {
+    const uint32_t cand = sub | (1u << bit);
+    const uint64_t v = ((uint64_t)b << kSubBits) | cand;
+#pragma unroll
+    for (int i = 0; i < kIn; ++i) x[i] = (float)((v >> (kIn - 1 - i)) & 1ull);
+    if (mlp_eval(P, x) <= u) sub = cand;
+  }
+  const uint64_t cell = (((uint64_t)b << kSubBits) | sub) + 1;  // first cell above
   T s;
-  if (top == 0xffffffffu) s = sh >= 0 ? ((T)1 << key_bits) - T(1) : (T)top;
-  else s = sh >= 0 ? ((T)(top + 1u) << sh) : (T)((top + 1u) >> (-sh));
+  if (key_bits >= 48) {
+    s = cell >= (1ull << 48) ? ((key_bits == (uint32_t)KeyTraits<T>::kBits) ? ~T(0) : (T(1) << key_bits) - T(1))
+                             : (T)cell << (key_bits - 48);
+  } else {
+    s = (T)((cell + ((1ull << (48 - key_bits)) - 1)) >> (48 - key_bits));
+  }
   spl[j - 1] = s;
 }
 
-// Predicted per-tile load on the sample (sorted) for given splitters.
 template <class T>
 __global__ void k_tile_hits(const T* __restrict__ sample, uint32_t n, const T* __restrict__ spl, uint32_t S,
                             unsigned* __restrict__ hits) {
@@ -271,9 +314,6 @@ __global__ void k_sort_splitters(T* spl, uint32_t n) {
   }
 }
 
-// ---- host driver ----------------------------------------------------------------
-namespace {
-
 // Bitonic sort of the sample in device memory (padded to a power of two
 // with the all-ones key, which sorts last and is dropped).
 template <class T>
@@ -296,22 +336,28 @@ __global__ void k_bitonic_step(T* keys, uint32_t np2, uint32_t j, uint32_t k) {
   }
 }
 
+namespace {
+
 template <class T>
-void sort_sample(MlpModel* m, const T* d_sample, uint32_t n, cudaStream_t s, T** out) {
-  uint32_t np2 = 1;
+int sort_sample(MlpModel* m, const T* d_sample, uint32_t n, cudaStream_t s, T** out) {
+  uint32_t np2 = 1, launches = 1;
   while (np2 < n) np2 <<= 1;
   const size_t bytes = (size_t)np2 * sizeof(T);
   if (m->keys_cap < bytes) {
     cudaFree(m->keys_sorted);
-    cudaMalloc(&m->keys_sorted, bytes);
+    if (cudaMalloc(&m->keys_sorted, bytes) != cudaSuccess) return -1;
     m->keys_cap = bytes;
   }
   T* keys = static_cast<T*>(m->keys_sorted);
   const uint32_t blocks = (np2 + 255) / 256;
   k_pad<T><<<blocks, 256, 0, s>>>(keys, d_sample, n, np2);
   for (uint32_t k = 2; k <= np2; k <<= 1)
-    for (uint32_t j = k >> 1; j > 0; j >>= 1) k_bitonic_step<T><<<blocks, 256, 0, s>>>(keys, np2, j, k);
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      k_bitonic_step<T><<<blocks, 256, 0, s>>>(keys, np2, j, k);
+      launches++;
+    }
   *out = keys;
+  return (int)launches;
 }
 
 }  // namespace
@@ -351,30 +397,32 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
   rep->pred_imbalance = 1e30;
   if (!m || n < 4 * S || n < 1024) return 0;  // too few samples to learn from
   T* sorted = nullptr;
-  sort_sample<T>(m, d_sample, n, s, &sorted);
-  uint32_t np2 = 1, lg = 0;
-  while (np2 < n) {
-    np2 <<= 1;
-    lg++;
-  }
-  rep->launches += 1 + (int)(lg * (lg + 1) / 2);
+  const int sl = sort_sample<T>(m, d_sample, n, s, &sorted);
+  if (sl < 0) return 1;
+  rep->launches += sl;
   if (m->cap < n) {
     cudaFree(m->feats);
     cudaFree(m->target);
+    cudaFree(m->scale);
     if (cudaMalloc(&m->feats, (size_t)n * kIn * sizeof(float)) != cudaSuccess) return 1;
     if (cudaMalloc(&m->target, (size_t)n * sizeof(float)) != cudaSuccess) return 1;
+    if (cudaMalloc(&m->scale, (size_t)n * sizeof(float)) != cudaSuccess) return 1;
     m->cap = n;
   }
-  k_make_features<T><<<(n + 255) / 256, 256, 0, s>>>(sorted, n, key_bits, m->feats, m->target);
-  rep->launches += 1;
+  if (!m->hist && cudaMalloc(&m->hist, sizeof(unsigned) << kBinBits) != cudaSuccess) return 1;
+  cudaMemsetAsync(m->hist, 0, sizeof(unsigned) << kBinBits, s);
+  k_bin_hist<T><<<(n + 255) / 256, 256, 0, s>>>(sorted, n, key_bits, m->hist);
+  k_cum<<<1, 1024, 0, s>>>(m->hist);
+  k_make_features<T><<<(n + 255) / 256, 256, 0, s>>>(sorted, n, key_bits, m->hist, m->feats, m->target, m->scale);
+  rep->launches += 3;
   int steps = 400;
   if (const char* e = getenv("KITE_MLP_STEPS")) steps = std::max(1, atoi(e));
   int tl = 0;
-  if (mlp_train(m, n, steps, 8192, 3e-3f, s, timeout_ms, &rep->loss, &tl)) return 1;
+  if (mlp_train(m, n, steps, 8192, 2e-3f, s, timeout_ms, &rep->loss, &tl)) return 1;
   rep->launches += tl;
   const size_t smem = kParams * sizeof(float);
   cudaFuncSetAttribute(k_invert<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_invert<T><<<(S + 127) / 128, 128, smem, s>>>(m->params, S, key_bits, d_spl);
+  k_invert<T><<<(S + 127) / 128, 128, smem, s>>>(m->params, m->hist, n, S, key_bits, d_spl);
   k_sort_splitters<T><<<1, 1024, 0, s>>>(d_spl, S - 1);
   rep->launches += 2;
   if (predict_imbalance<T>(m, sorted, n, d_spl, S, s, timeout_ms, &rep->pred_imbalance)) return 1;
@@ -388,7 +436,7 @@ template int mlp_splitters<uint64_t>(MlpModel*, const uint64_t*, uint32_t, uint3
 template int mlp_splitters<u128>(MlpModel*, const u128*, uint32_t, uint32_t, uint32_t, u128*, cudaStream_t, uint32_t,
                                  MlpReport*);
 
-// Trains on m->feats / m->target (n samples) with Adam; deterministic init.
+// Trains on m->feats / m->target / m->scale (n samples) with Adam; fixed init.
 int mlp_train(MlpModel* m, uint32_t n, int steps, uint32_t batch, float lr, cudaStream_t s, uint32_t timeout_ms,
               float* final_loss, int* launches) {
   if (!m->params) {
@@ -399,7 +447,6 @@ int mlp_train(MlpModel* m, uint32_t n, int steps, uint32_t batch, float lr, cuda
     cudaMalloc(&m->loss, sizeof(float) * 2);
     cudaMalloc(&m->batch_idx, (size_t)65536 * 4);
   }
-  // He-style init from a fixed LCG; output bias 0.5
   std::vector<float> p(kParams, 0.f);
   uint64_t st = 0x2545F4914F6CDD1Dull;
   auto rnd = [&]() {
@@ -417,8 +464,6 @@ int mlp_train(MlpModel* m, uint32_t n, int steps, uint32_t batch, float lr, cuda
   cudaMemsetAsync(m->m, 0, kParams * sizeof(float), s);
   cudaMemsetAsync(m->v, 0, kParams * sizeof(float), s);
   batch = std::min(std::min(batch, n), 65536u);
-  uint32_t* idx = m->batch_idx;
-  // stride coprime with n
   auto gcd = [](uint32_t a, uint32_t b) {
     while (b) {
       uint32_t t = a % b;
@@ -434,13 +479,14 @@ int mlp_train(MlpModel* m, uint32_t n, int steps, uint32_t batch, float lr, cuda
   const float b1 = 0.9f, b2 = 0.999f;
   double c1 = 1, c2 = 1;
   for (int t = 0; t < steps; ++t) {
-    k_batch_idx<<<(batch + 255) / 256, 256, 0, s>>>(idx, batch, n, (uint32_t)((uint64_t)t * batch % n), stride);
+    k_batch_idx<<<(batch + 255) / 256, 256, 0, s>>>(m->batch_idx, batch, n, (uint32_t)((uint64_t)t * batch % n),
+                                                    stride);
     cudaMemsetAsync(m->loss, 0, sizeof(float), s);
-    k_fwd_bwd<<<(batch + kB - 1) / kB, kB, kFbSmem, s>>>(m->params, m->feats, m->target, idx, batch, m->grads,
-                                                        m->loss);
+    k_fwd_bwd<<<(batch + kB - 1) / kB, kB, kFbSmem, s>>>(m->params, m->feats, m->target, m->scale, m->batch_idx,
+                                                        batch, m->grads, m->loss);
     c1 *= b1;
     c2 *= b2;
-    const float decay = t > steps / 2 ? 0.3f : 1.0f;
+    const float decay = t > steps * 3 / 4 ? 0.2f : (t > steps / 2 ? 0.5f : 1.0f);
     k_adam<<<(kParams + 255) / 256, 256, 0, s>>>(m->params, m->grads, m->m, m->v, lr * decay, b1, b2, 1e-8f,
                                                  (float)(1 - c1), (float)(1 - c2));
   }
@@ -455,8 +501,9 @@ int mlp_train(MlpModel* m, uint32_t n, int steps, uint32_t batch, float lr, cuda
 }  // namespace kite
 
 // ---- test hooks (C ABI, no counterpart in the reference) -------------------------
-// Forward + backward of one batch against a given parameter vector, so tests can
-// check the hand-written gradients against a CPU float64 reference.
+// One forward + backward of the learned-CDF network over n samples (unit
+// scale) against a given parameter vector, so tests can check the
+// hand-written gradients against a CPU float64 reference.
 extern "C" int kite_mlp_grad_check(const float* params, const float* feats, const float* target, uint32_t n,
                                    float* grads_out, float* loss_out) {
   using namespace kite;
@@ -477,7 +524,7 @@ extern "C" int kite_mlp_grad_check(const float* params, const float* feats, cons
   cudaMemset(dg, 0, kParams * 4);
   cudaMemset(dl, 0, 4);
   cudaFuncSetAttribute(k_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFbSmem);
-  k_fwd_bwd<<<(n + kB - 1) / kB, kB, kFbSmem>>>(dp, df, dt, di, n, dg, dl);
+  k_fwd_bwd<<<(n + kB - 1) / kB, kB, kFbSmem>>>(dp, df, dt, nullptr, di, n, dg, dl);
   cudaError_t e = cudaDeviceSynchronize();
   cudaMemcpy(grads_out, dg, kParams * 4, cudaMemcpyDeviceToHost);
   cudaMemcpy(loss_out, dl, 4, cudaMemcpyDeviceToHost);
@@ -491,3 +538,4 @@ extern "C" int kite_mlp_grad_check(const float* params, const float* feats, cons
 }
 
 extern "C" int kite_mlp_param_count(void) { return kite::kParams; }
+extern "C" int kite_mlp_input_count(void) { return kite::kIn; }

@@ -69,30 +69,116 @@ struct TileSmem {
   static constexpr size_t total = buf_bytes + hist_bytes + head_bytes + misc_bytes;
 };
 
-// Sort the n keys in buf (shared memory) over bits [0, nbits).
+// Stable LSD passes over bits [lo_bit, nbits) of the n keys in buf (shared
+// memory), 8-bit digits.
 template <class T>
 __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, unsigned* warp_hist,
-                                                unsigned* scan_sm) {
+                                                unsigned* scan_sm, int lo_bit = 0) {
   constexpr int NT = kTileThreads, ITEMS = tile_items<T>();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const unsigned pos0 = (unsigned)wid * 32u * ITEMS + lane;
-  for (int shift = 0; shift < nbits; shift += 8) {
+  // spread the n keys over every warp: `items` rounds of 32 per warp
+  const int items = (int)((n + NT - 1) / NT);
+  const unsigned pos0 = (unsigned)wid * 32u * (unsigned)items + lane;
+  for (int shift = lo_bit; shift < nbits; shift += 8) {
     T key[ITEMS];
     unsigned dig[ITEMS], dest[ITEMS];
     bool valid[ITEMS];
 #pragma unroll
     for (int r = 0; r < ITEMS; ++r) {
       const unsigned pos = pos0 + r * 32u;
-      valid[r] = pos < n;
+      valid[r] = r < items && pos < n;
       key[r] = valid[r] ? buf[pos] : T(0);
       dig[r] = digit_of(key[r], shift);
     }
-    block_rank<NT, ITEMS, 256>(dig, valid, dest, warp_hist, scan_sm, nullptr, nullptr);
+    block_rank<NT, ITEMS, 256>(dig, valid, dest, warp_hist, scan_sm, nullptr, nullptr, items);
 #pragma unroll
     for (int r = 0; r < ITEMS; ++r)
       if (valid[r]) buf[dest[r]] = key[r];
     __syncthreads();
   }
+}
+
+// Sorts buf (n keys with `nbits` varying low bits).  Two stable 8-bit passes
+// order the keys by their top 16 varying bits; a "run" is then a maximal
+// stretch of equal 16-bit prefix.  A run whose keys are all equal (the usual
+// case: copies of one k-mer) is already in place.  In the others every key
+// counts the smaller keys (and equal keys before it) in its run to find its
+// final slot.  If such a run is longer than kMaxRun the tile takes the full
+// LSD instead.  `runs` needs n+1 u16, `mixed` n bytes.  Ends with a barrier.
+constexpr unsigned kMaxRun = 512;
+
+template <class T>
+__device__ __forceinline__ void smem_sort_prefix_runs(T* buf, unsigned n, int nbits, unsigned* warp_hist,
+                                                      unsigned* scan_sm, unsigned short* runs, uint8_t* mixed,
+                                                      unsigned* flag) {
+  constexpr int NT = kTileThreads, ITEMS = tile_items<T>();
+  const int lo = nbits > 16 ? nbits - 16 : 0;
+  smem_radix_sort<T>(buf, n, nbits, warp_hist, scan_sm, lo);
+  if (lo == 0) return;
+  // run ids (blocked arrangement), run starts, mixed-run flags
+  const unsigned b0 = threadIdx.x * ITEMS;
+  unsigned nh = 0;
+#pragma unroll
+  for (int r = 0; r < ITEMS; ++r) {
+    const unsigned i = b0 + r;
+    if (i < n && (i == 0 || (buf[i] >> lo) != (buf[i - 1] >> lo))) nh++;
+  }
+  unsigned R;
+  unsigned rid0 = block_exclusive_scan<NT, unsigned>(nh, scan_sm, &R);
+  unsigned rid = rid0;
+  unsigned myrid[ITEMS];
+#pragma unroll
+  for (int r = 0; r < ITEMS; ++r) {
+    const unsigned i = b0 + r;
+    if (i < n && (i == 0 || (buf[i] >> lo) != (buf[i - 1] >> lo))) runs[rid++] = (unsigned short)i;
+    myrid[r] = rid - 1;  // run of element i
+  }
+  for (unsigned q = threadIdx.x; q < R; q += NT) mixed[q] = 0;
+  if (threadIdx.x == 0) {
+    runs[R] = (unsigned short)n;
+    *flag = 0;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < ITEMS; ++r) {
+    const unsigned i = b0 + r;
+    if (i < n && i > 0 && (buf[i] >> lo) == (buf[i - 1] >> lo) && buf[i] != buf[i - 1]) mixed[myrid[r]] = 1;
+  }
+  __syncthreads();
+  T key[ITEMS];
+  unsigned npos[ITEMS];
+#pragma unroll
+  for (int r = 0; r < ITEMS; ++r) {
+    const unsigned i = b0 + r;
+    npos[r] = i;
+    if (i >= n || !mixed[myrid[r]]) continue;
+    const unsigned a = runs[myrid[r]], e = runs[myrid[r] + 1];
+    if (e - a > kMaxRun) {
+      *flag = 1;
+      continue;
+    }
+    const T k0 = buf[i];
+    key[r] = k0;
+    unsigned less = 0, eq_before = 0;
+    for (unsigned j = a; j < e; ++j) {
+      const T v = buf[j];
+      less += v < k0;
+      eq_before += (v == k0) & (j < i);
+    }
+    npos[r] = a + less + eq_before;
+  }
+  __syncthreads();
+  if (*flag) {
+    smem_radix_sort<T>(buf, n, lo, warp_hist, scan_sm, 0);  // low bits, then the top 16 again (stable LSD)
+    smem_radix_sort<T>(buf, n, nbits, warp_hist, scan_sm, lo);
+    return;
+  }
+#pragma unroll
+  for (int r = 0; r < ITEMS; ++r) {
+    const unsigned i = b0 + r;
+    if (i < n && npos[r] != i) buf[npos[r]] = key[r];
+  }
+  __syncthreads();
 }
 
 template <class T>
@@ -132,7 +218,8 @@ __global__ void __launch_bounds__(kTileThreads, 1)
     mx = v > mx ? v : mx;
   }
   block_minmax<NT>(mn, mx, red);
-  smem_radix_sort<T>(buf, n, varying_bits(mn, mx), warp_hist, scan_sm);
+  smem_sort_prefix_runs<T>(buf, n, varying_bits(mn, mx), warp_hist, scan_sm, head,
+                           reinterpret_cast<uint8_t*>(warp_hist), reinterpret_cast<unsigned*>(red + 2 * NW));
 
   // Run-length reduction: heads in blocked order.
   const unsigned b0 = threadIdx.x * ITEMS;

@@ -60,7 +60,8 @@ class Stats(C.Structure):
                 ("tiles_per_bucket", C.c_uint32), ("segments", C.c_uint32), ("tile_imbalance", C.c_double),
                 ("splitter_used", C.c_int), ("stage_ms", C.c_double * 12), ("h2d_bytes", C.c_uint64),
                 ("d2h_bytes", C.c_uint64), ("kernel_launches", C.c_uint64), ("mlp_loss", C.c_double),
-                ("mlp_pred_imbalance", C.c_double), ("hist_pred_imbalance", C.c_double)]
+                ("mlp_pred_imbalance", C.c_double), ("hist_pred_imbalance", C.c_double),
+                ("range_imbalance", C.c_double)]
 
     def as_dict(self) -> dict:
         d = {f: getattr(self, f) for f, _ in self._fields_ if f != "stage_ms"}
