@@ -162,6 +162,41 @@ int kite_gpu_get_stats(kite_gpu_ctx* ctx, kite_gpu_stats* out);
 /* Device-side timing of the last count/merge, summed per kernel family. */
 int kite_gpu_synchronize(kite_gpu_ctx* ctx);
 
+/* Largest FASTQ chunk kite_gpu_count_rows_noalloc accepts. */
+#define KITE_NOALLOC_MAX_BYTES (512u * 1024u)
+
+/* Counts one small FASTQ chunk that already lives in device memory, without
+ * allocating anything: no context, no cudaMalloc / cudaFree, no pinned host
+ * buffer.  It has no counterpart in the reference.  It is meant for callers
+ * that cannot allocate device memory at the moment they count: a process
+ * whose framework already reserved the device's memory for its own pool, or
+ * a loop counting small read batches between other GPU work that must not
+ * take the device-wide synchronisation of cudaMalloc / cudaFree.
+ *
+ * Same counting rules as kite_gpu_count_submit + kite_gpu_count_finish on one
+ * chunk (a chunk not starting with '@' counts nothing).  Results go to the
+ * caller's device arrays, grouped by partition in ascending order, keys
+ * ascending inside a partition: d_keys gets the keys (8-byte little-endian
+ * words for k <= 31, 16-byte words for k >= 32; aligned to the word size),
+ * d_counts their counts, d_partition_rows[partitions] the rows of each
+ * partition; totals[4] (host) gets reads, bases, k-mers and rows.
+ *
+ * Working memory is one fixed array of about 21 MiB in this library's device
+ * data, one per device, which every call on that device shares: calls that
+ * overlap on the GPU race and corrupt each other's results, so serialise them
+ * (and after KITE_ERR_TIMEOUT, wait for `stream` before the next call).  The
+ * first call on a device looks the array up (cudaGetSymbolAddress, with that
+ * device current); make it before any stream capture starts.  Runs on
+ * `stream` (NULL = the default stream) of `device`, restores the caller's
+ * current device, and returns when the work is done (at most timeout_ms;
+ * 0 = 600000).  Errors: KITE_ERR_UNSUPPORTED when len exceeds
+ * KITE_NOALLOC_MAX_BYTES (nothing runs); KITE_ERR_BAD_INPUT for invalid
+ * arguments, or when the rows exceed max_rows (totals[3] then gives the rows
+ * needed). */
+int kite_gpu_count_rows_noalloc(int device, int k, int canonical, uint32_t partitions, const uint8_t* d_fastq,
+                                size_t len, void* d_keys, uint32_t* d_counts, uint64_t max_rows,
+                                uint32_t* d_partition_rows, uint64_t* totals, void* stream, uint32_t timeout_ms);
+
 #ifdef __cplusplus
 }
 #endif
