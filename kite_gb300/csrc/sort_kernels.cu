@@ -3,9 +3,10 @@
 // :388-437, then rle_compress_typed :514-530 with u32 saturation).
 //
 // A tile is a key range of one hash bucket.  One CTA loads the whole tile into
-// shared memory, sorts only the bits that vary inside it (LSD, 8-bit digits,
-// stable warp-match ranking), then emits unique (key, count) rows in place
-// and the tile's DVLE size for every row but the first.
+// shared memory, orders it by a 4096-bin counting pass over its key span (bins
+// holding several distinct keys are finished by counting, rare large ones by
+// LSD passes), then emits unique (key, count) rows in place and the tile's
+// DVLE size for every row but the first.
 #include "kite_internal.h"
 
 namespace kite {
@@ -98,102 +99,64 @@ __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, u
   }
 }
 
-// Sorts buf (n keys with `nbits` varying low bits).  Two stable 8-bit passes
-// order the keys by their top 16 varying bits; a "run" is then a maximal
-// stretch of equal 16-bit prefix.  A run whose keys are all equal (the usual
-// case: copies of one k-mer) is already in place.  In the others every key
-// counts the smaller keys (and equal keys before it) in its run to find its
-// final slot.  If such a run is longer than kMaxRun the tile takes the full
-// LSD instead.  `runs` needs n+1 u16, `mixed` n bytes.  Ends with a barrier.
-constexpr unsigned kMaxRun = 512;
+// ---------------------------------------------------------------------------
+// Tile sort by binning.  One CTA per tile of n <= CAP keys:
+//  1. load the tile into shared memory; block min / max;
+//  2. bin = (key - min) >> s with 4096 bins spanning [min, max]: histogram by
+//     shared atomics, exclusive scan, then the key INDICES (u16) are scattered
+//     into bin order.  Bins are key-ordered; order inside a bin is arbitrary;
+//  3. a bin holding more than one distinct key is ordered by counting: each
+//     key counts the smaller keys, and the equal keys placed before it, in its
+//     bin.  A bin of one repeated k-mer (the usual case) costs nothing.  A
+//     mixed bin larger than kMaxMixed sends the tile to a full LSD sort;
+//  4. run-length reduction over the sorted order: head flags by warp ballots,
+//     rows written to global memory over the tile's keys (u32 counts; a tile
+//     holds fewer than 2^32 keys, so no count saturates here).
+// Keys never sit in register arrays on the main path, so the kernel fits 64
+// registers and two CTAs share an SM.
+// ---------------------------------------------------------------------------
+constexpr int kBinBits = 12, kBins = 1 << kBinBits;
+constexpr unsigned kMaxMixed = 256;
 
 template <class T>
-__device__ __forceinline__ void smem_sort_prefix_runs(T* buf, unsigned n, int nbits, unsigned* warp_hist,
-                                                      unsigned* scan_sm, unsigned short* runs, uint8_t* mixed,
-                                                      unsigned* flag) {
-  constexpr int NT = kTileThreads, ITEMS = tile_items<T>();
-  const int lo = nbits > 16 ? nbits - 16 : 0;
-  smem_radix_sort<T>(buf, n, nbits, warp_hist, scan_sm, lo);
-  if (lo == 0) return;
-  // run ids (blocked arrangement), run starts, mixed-run flags
-  const unsigned b0 = threadIdx.x * ITEMS;
-  unsigned nh = 0;
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    const unsigned i = b0 + r;
-    if (i < n && (i == 0 || (buf[i] >> lo) != (buf[i - 1] >> lo))) nh++;
-  }
-  unsigned R;
-  unsigned rid0 = block_exclusive_scan<NT, unsigned>(nh, scan_sm, &R);
-  unsigned rid = rid0;
-  unsigned myrid[ITEMS];
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    const unsigned i = b0 + r;
-    if (i < n && (i == 0 || (buf[i] >> lo) != (buf[i - 1] >> lo))) runs[rid++] = (unsigned short)i;
-    myrid[r] = rid - 1;  // run of element i
-  }
-  for (unsigned q = threadIdx.x; q < R; q += NT) mixed[q] = 0;
-  if (threadIdx.x == 0) {
-    runs[R] = (unsigned short)n;
-    *flag = 0;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    const unsigned i = b0 + r;
-    if (i < n && i > 0 && (buf[i] >> lo) == (buf[i - 1] >> lo) && buf[i] != buf[i - 1]) mixed[myrid[r]] = 1;
-  }
-  __syncthreads();
-  T key[ITEMS];
-  unsigned npos[ITEMS];
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    const unsigned i = b0 + r;
-    npos[r] = i;
-    if (i >= n || !mixed[myrid[r]]) continue;
-    const unsigned a = runs[myrid[r]], e = runs[myrid[r] + 1];
-    if (e - a > kMaxRun) {
-      *flag = 1;
-      continue;
-    }
-    const T k0 = buf[i];
-    key[r] = k0;
-    unsigned less = 0, eq_before = 0;
-    for (unsigned j = a; j < e; ++j) {
-      const T v = buf[j];
-      less += v < k0;
-      eq_before += (v == k0) & (j < i);
-    }
-    npos[r] = a + less + eq_before;
-  }
-  __syncthreads();
-  if (*flag) {
-    smem_radix_sort<T>(buf, n, lo, warp_hist, scan_sm, 0);  // low bits, then the top 16 again (stable LSD)
-    smem_radix_sort<T>(buf, n, nbits, warp_hist, scan_sm, lo);
-    return;
-  }
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    const unsigned i = b0 + r;
-    if (i < n && npos[r] != i) buf[npos[r]] = key[r];
-  }
-  __syncthreads();
+struct BinSmem {
+  static constexpr int NT = kTileThreads;
+  static constexpr int ITEMS = tile_items<T>();
+  static constexpr int CAP = NT * ITEMS;  // 8192 u64 / 4096 u128 keys
+  static constexpr int NW = NT / 32;
+  static constexpr size_t buf_bytes = (size_t)CAP * sizeof(T);
+  static constexpr size_t perm_bytes = (size_t)CAP * 2;
+  // bin counters; later the u16 run heads (CAP + 1 entries), or the LSD
+  // fallback's per-warp digit histograms (256 * NW counters)
+  static constexpr size_t bin_bytes = (size_t)kBins * 4 + 16;
+  static constexpr size_t flag_bytes = kBins;
+  static constexpr size_t misc_bytes = 64 * 8 + 2 * NW * sizeof(T) + 16;
+  static constexpr size_t total = buf_bytes + perm_bytes + bin_bytes + flag_bytes + misc_bytes;
+  static_assert((size_t)(CAP + 1) * 2 <= bin_bytes, "run heads must fit the bin area");
+  static_assert((size_t)256 * NW * 4 <= bin_bytes, "LSD histograms must fit the bin area");
+  static_assert(kBins % (4 * NT) == 0, "bin scan takes whole uint4 groups");
+};
+
+template <class T>
+__device__ __forceinline__ unsigned bin_of(T key, T mn, int s) {
+  return (unsigned)(uint64_t)((key - mn) >> s);
 }
 
 template <class T>
-__global__ void __launch_bounds__(kTileThreads, 1)
+__global__ void __launch_bounds__(kTileThreads, 2)
     k_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, const TileDesc* __restrict__ tiles,
                 TileOut<T>* __restrict__ tout, DevStatus* st) {
-  using L = TileSmem<T>;
-  constexpr int NT = L::NT, ITEMS = L::ITEMS, NW = L::NW;
+  using L = BinSmem<T>;
+  constexpr int NT = L::NT, NW = L::NW, ITEMS = L::ITEMS;
   extern __shared__ __align__(16) uint8_t sm[];
   T* buf = reinterpret_cast<T*>(sm);
-  unsigned* warp_hist = reinterpret_cast<unsigned*>(sm + L::buf_bytes);
-  unsigned short* head = reinterpret_cast<unsigned short*>(sm + L::buf_bytes + L::hist_bytes);
-  unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(sm + L::buf_bytes + L::hist_bytes + L::head_bytes);
+  unsigned short* perm = reinterpret_cast<unsigned short*>(sm + L::buf_bytes);
+  unsigned* bins = reinterpret_cast<unsigned*>(sm + L::buf_bytes + L::perm_bytes);
+  uint8_t* flag = sm + L::buf_bytes + L::perm_bytes + L::bin_bytes;
+  unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(flag + L::flag_bytes);
   unsigned* scan_sm = reinterpret_cast<unsigned*>(scan64);
   T* red = reinterpret_cast<T*>(scan64 + 64);
+  unsigned* misc = reinterpret_cast<unsigned*>(red + 2 * NW);
 
   const TileDesc td = tiles[blockIdx.x];
   const unsigned n = td.len;
@@ -210,6 +173,7 @@ __global__ void __launch_bounds__(kTileThreads, 1)
     return;
   }
   T* g = keys + td.start;
+  uint32_t* gc = counts + td.start;
   T mn = ~T(0), mx = T(0);
   for (unsigned i = threadIdx.x; i < n; i += NT) {
     const T v = g[i];
@@ -218,58 +182,161 @@ __global__ void __launch_bounds__(kTileThreads, 1)
     mx = v > mx ? v : mx;
   }
   block_minmax<NT>(mn, mx, red);
-  smem_sort_prefix_runs<T>(buf, n, varying_bits(mn, mx), warp_hist, scan_sm, head,
-                           reinterpret_cast<uint8_t*>(warp_hist), reinterpret_cast<unsigned*>(red + 2 * NW));
+  if (mn == mx) {  // one key fills the tile
+    if (threadIdx.x == 0) {
+      g[0] = mn;
+      gc[0] = n;
+      TileOut<T> o;
+      o.first_key = o.last_key = mn;
+      o.rows = 1;
+      o.first_count = n;
+      o.rest_bytes = 0;
+      tout[blockIdx.x] = o;
+    }
+    return;
+  }
+  const int rb = KeyTraits<T>::kBits - clz_key(T(mx - mn));
+  const int s = rb > kBinBits ? rb - kBinBits : 0;
 
-  // Run-length reduction: heads in blocked order.
-  const unsigned b0 = threadIdx.x * ITEMS;
-  unsigned nh = 0;
+  // ---- 2. bin histogram, scan, index scatter ----
+  for (int b = threadIdx.x; b < kBins; b += NT) bins[b] = 0;
+  for (int b = threadIdx.x; b < kBins / 4; b += NT) reinterpret_cast<unsigned*>(flag)[b] = 0;
+  if (threadIdx.x == 0) misc[0] = 0;
+  __syncthreads();
+  for (unsigned i = threadIdx.x; i < n; i += NT) atomicAdd(&bins[bin_of(buf[i], mn, s)], 1u);
+  __syncthreads();
+  {
+    constexpr int G = kBins / (4 * NT);  // uint4 groups per thread
+    uint4* b4 = reinterpret_cast<uint4*>(bins) + threadIdx.x * G;
+    uint4 x[G];
+    unsigned sum = 0;
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      x[j] = b4[j];
+      sum += x[j].x + x[j].y + x[j].z + x[j].w;
+    }
+    unsigned tot;
+    unsigned pre = block_exclusive_scan<NT, unsigned>(sum, scan_sm, &tot);
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      uint4 y;
+      y.x = pre;
+      pre += x[j].x;
+      y.y = pre;
+      pre += x[j].y;
+      y.z = pre;
+      pre += x[j].z;
+      y.w = pre;
+      pre += x[j].w;
+      b4[j] = y;
+    }
+  }
+  __syncthreads();
+  for (unsigned i = threadIdx.x; i < n; i += NT) {
+    const unsigned p = atomicAdd(&bins[bin_of(buf[i], mn, s)], 1u);
+    perm[p] = (unsigned short)i;
+  }
+  __syncthreads();
+  // bins[b] is now the end of bin b; its start is bins[b - 1] (0 for b = 0)
+
+  // ---- 3. bins holding more than one distinct key ----
+  for (unsigned p = threadIdx.x + 1; p < n; p += NT) {
+    const T a = buf[perm[p]], b = buf[perm[p - 1]];
+    if (a != b) {
+      const unsigned ba = bin_of(a, mn, s);
+      if (bin_of(b, mn, s) == ba) flag[ba] = 1;
+    }
+  }
+  __syncthreads();
+  unsigned pend[ITEMS];  // (new position << 16) | key index, or ~0
 #pragma unroll
   for (int r = 0; r < ITEMS; ++r) {
-    const unsigned i = b0 + r;
-    if (i < n && (i == 0 || buf[i] != buf[i - 1])) nh++;
+    pend[r] = ~0u;
+    const unsigned p = threadIdx.x + r * NT;
+    if (p >= n) continue;
+    const unsigned idx = perm[p];
+    const T k0 = buf[idx];
+    const unsigned bb = bin_of(k0, mn, s);
+    if (!flag[bb]) continue;
+    const unsigned a = bb ? bins[bb - 1] : 0u, e = bins[bb];
+    if (e - a > kMaxMixed) {
+      misc[0] = 1;
+      continue;
+    }
+    unsigned less = 0, eqb = 0;
+    for (unsigned j = a; j < e; ++j) {
+      const T v = buf[perm[j]];
+      less += v < k0;
+      eqb += (v == k0) & (j < p);
+    }
+    pend[r] = ((a + less + eqb) << 16) | idx;
+  }
+  __syncthreads();
+  if (misc[0]) {
+    // a large bin of distinct keys: full LSD over the varying bits, in place
+    smem_radix_sort<T>(buf, n, varying_bits(mn, mx), bins, scan_sm, 0);
+    for (unsigned p = threadIdx.x; p < n; p += NT) perm[p] = (unsigned short)p;
+  } else {
+#pragma unroll
+    for (int r = 0; r < ITEMS; ++r)
+      if (pend[r] != ~0u) perm[pend[r] >> 16] = (unsigned short)(pend[r] & 0xffffu);
+  }
+  __syncthreads();
+
+  // ---- 4. run-length reduction in sorted order (position p holds buf[perm[p]]) ----
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned rounds = (n + NT - 1) / NT;
+  const unsigned w0 = (unsigned)wid * 32u * rounds;
+  unsigned hmask = 0, cnt = 0;
+  for (unsigned r = 0; r < rounds; ++r) {
+    const unsigned p = w0 + r * 32u + lane;
+    bool h = false;
+    if (p < n) h = p == 0 || buf[perm[p]] != buf[perm[p - 1]];
+    hmask |= (unsigned)h << r;
+    cnt += __popc(__ballot_sync(0xffffffffu, h));
   }
   unsigned U;
-  unsigned u = block_exclusive_scan<NT, unsigned>(nh, scan_sm, &U);
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    const unsigned i = b0 + r;
-    if (i < n && (i == 0 || buf[i] != buf[i - 1])) head[u++] = (unsigned short)i;
+  unsigned u = block_exclusive_scan<NT, unsigned>(lane == 0 ? cnt : 0u, scan_sm, &U);
+  u = __shfl_sync(0xffffffffu, u, 0);
+  unsigned short* head = reinterpret_cast<unsigned short*>(bins);
+  const unsigned lt = (1u << lane) - 1u;
+  for (unsigned r = 0; r < rounds; ++r) {
+    const bool h = (hmask >> r) & 1u;
+    const unsigned bal = __ballot_sync(0xffffffffu, h);
+    if (h) head[u + __popc(bal & lt)] = (unsigned short)(w0 + r * 32u + lane);
+    u += __popc(bal);
   }
   if (threadIdx.x == 0) head[U] = (unsigned short)n;
   __syncthreads();
-  // n <= CAP <= 65535 fits the u16 head positions; head[U] = n may equal 65536
-  // only if CAP were 65536, which it is not.
   unsigned long long rest = 0;
-  uint32_t* gc = counts + td.start;
   for (unsigned v = threadIdx.x; v < U; v += NT) {
     const unsigned i = head[v];
     const unsigned c = (unsigned)head[v + 1] - i;
-    const T key = buf[i];
+    const T key = buf[perm[i]];
     g[v] = key;
     gc[v] = c;
-    if (v > 0) rest += (unsigned long long)(varint_len(key - buf[head[v - 1]]) + varint_len((uint64_t)c));
+    if (v > 0) rest += (unsigned long long)(varint_len(T(key - buf[perm[head[v - 1]]])) + varint_len((uint64_t)c));
   }
   unsigned long long rest_total;
   block_exclusive_scan<NT, unsigned long long>(rest, scan64, &rest_total);
   if (threadIdx.x == 0) {
     TileOut<T> o;
-    o.first_key = buf[head[0]];
+    o.first_key = buf[perm[head[0]]];
     o.first_count = (unsigned)head[1] - head[0];
-    o.last_key = buf[head[U - 1]];
+    o.last_key = buf[perm[head[U - 1]]];
     o.rows = U;
     o.rest_bytes = rest_total;
     tout[blockIdx.x] = o;
   }
   (void)st;
-  (void)NW;
 }
 
 template <class T>
 void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
                       DevStatus* st, cudaStream_t s) {
-  const size_t smem = TileSmem<T>::total;
+  const size_t smem = BinSmem<T>::total;
   cudaFuncSetAttribute(k_tile_sort<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_tile_sort<T>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (ntiles) k_tile_sort<T><<<ntiles, kTileThreads, smem, s>>>(keys, counts, tiles, out, st);
 }
 template void launch_tile_sort<uint64_t>(uint64_t*, uint32_t*, const TileDesc*, uint32_t, TileOut<uint64_t>*,

@@ -72,6 +72,20 @@ def test_heavy_mixed_big_tile(gpu, orc):
     assert_parity(gpu, orc, fq, 31, False, 2)
 
 
+@pytest.mark.parametrize("copies", [100, 300])
+def test_mixed_bin(gpu, orc, copies):
+    # Two distinct repeated keys that sit close together in one tile (k=21
+    # forward keys 0 = A*21 and 2 = A*20+G share partition 0 of 2, and G*21
+    # widens the tile's span so both fall in its first bin): 100 copies each
+    # are ordered by counting inside the bin, 300 each take the LSD fallback.
+    def rec(s):
+        return b"@m\n" + s + b"\n+\n" + b"I" * len(s) + b"\n"
+    fq = rec(b"A" * 21) * copies + rec(b"A" * 20 + b"G") * copies + rec(b"G" * 21)
+    rng = np.random.default_rng(11)
+    fq += synth.reads_fixed(rng, synth.genome_iid(rng, 5000), 40, 60, 0.0)
+    assert_parity(gpu, orc, fq, 21, False, 2)
+
+
 def test_segments_flush(gpu, orc):
     # a small arena forces several segments: partitions then hold several
     # chunks; compare through dump TSV equality (counts summed across chunks)
