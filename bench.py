@@ -229,6 +229,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--reads", type=int, default=10_000_000)
     ap.add_argument("--ref-reads", type=int, default=2_000_000)
+    ap.add_argument("--partitions", type=int, default=PARTITIONS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-splitter-compare", action="store_true")
     args = ap.parse_args()
@@ -262,7 +263,7 @@ def main():
             c.submit_device(base + d, l)
         c.finish(collect=False)
 
-    c = gpu.Counter(K, CANONICAL, PARTITIONS, device=local, splitter_mode=gpu.SPLIT_SAMPLED,
+    c = gpu.Counter(K, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED,
                     stream=stream.cuda_stream)
     for _ in range(args.warmup):
         device_step(c)
@@ -314,7 +315,7 @@ def main():
     # ---- learned vs sampled splitters on the same input (identical output) ----
     splitters = None
     if not args.no_splitter_compare:
-        cl = gpu.Counter(K, CANONICAL, PARTITIONS, device=local, splitter_mode=gpu.SPLIT_LEARNED,
+        cl = gpu.Counter(K, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_LEARNED,
                          imbalance_bound=10.0, stream=stream.cuda_stream)
         device_step(cl)
         torch.cuda.synchronize()
@@ -339,20 +340,29 @@ def main():
     pbase = pinned.data_ptr()
     d2h = [0]
 
+    e2e_parts = {"submit_s": 0.0, "finish_s": 0.0, "d2h_ms": 0.0}
+
     def e2e_step(cc):
+        t_a = time.perf_counter()
         for o, l in layout:
             cc.submit((pbase + o, l))
+        t_b = time.perf_counter()
+        e2e_parts["submit_s"] += t_b - t_a
         out_bytes = 0
 
-        def cb(meta, payload):
+        def cb(meta, addr, n):
             nonlocal out_bytes
-            out_bytes += len(payload)
-        cc.finish(collect=True, callback=cb)
+            out_bytes += n
+        cc.finish(collect=True, callback=cb, raw=True)
+        e2e_parts["finish_s"] += time.perf_counter() - t_b
+        e2e_parts["d2h_ms"] += cc.stats()["stage_ms"][7]
         d2h[0] = out_bytes
 
-    ce = gpu.Counter(K, CANONICAL, PARTITIONS, device=local, splitter_mode=gpu.SPLIT_SAMPLED)
+    ce = gpu.Counter(K, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED)
     e2e_step(ce)
     ce.synchronize()
+    for key in e2e_parts:
+        e2e_parts[key] = 0.0
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -374,14 +384,18 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded)",
                 "config": {"workload": f"{args.reads:,} x {READ_LEN} bp reads, 50 Mbp genome with 20% repeats, "
-                                       f"1% subs, 0.1% N, strand 50/50; k={K} canonical; {PARTITIONS} partitions; "
+                                       f"1% subs, 0.1% N, strand 50/50; k={K} canonical; {args.partitions} partitions; "
                                        "sampled-histogram splitters",
-                           "reads": args.reads, "k": K, "canonical": CANONICAL, "partitions": PARTITIONS,
+                           "reads": args.reads, "k": K, "canonical": CANONICAL, "partitions": args.partitions,
                            "fastq_bytes": total, "kmers_per_step": kmers, "rows_per_step": st["rows"],
                            "payload_bytes_per_step": st["payload_bytes"],
                            "l2": "inputs larger than L2 (FASTQ and keys are GBs; no flush needed)",
                            "parallelism": f"replicas x{world}"},
-                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": total, "d2h_bytes_per_step": d2h[0]},
+                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": total, "d2h_bytes_per_step": d2h[0],
+                        "ms_per_step": te / args.steps * 1e3,
+                        "submit_ms": e2e_parts["submit_s"] / args.steps * 1e3,
+                        "finish_ms": e2e_parts["finish_s"] / args.steps * 1e3,
+                        "d2h_ms": e2e_parts["d2h_ms"] / args.steps},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "splitters": splitters,
                 "tiles": {"tiles": st["tiles"], "per_bucket": st["tiles_per_bucket"], "big": st["big_tiles"],

@@ -299,6 +299,7 @@ __device__ __forceinline__ void load_splitters(const T* g_spl, uint32_t S, uint3
 static constexpr size_t kLutBytes = ((size_t)(1u << kLutBits) * 2 + 15) & ~(size_t)15;
 
 static constexpr int kSplitThreads = 512;
+static constexpr int kSplitUnroll = 8;
 
 __device__ __forceinline__ void part_range(const unsigned long long* boff, const unsigned long long* bcnt,
                                            uint32_t b, uint32_t g, uint32_t G, uint64_t* lo, uint64_t* hi) {
@@ -320,8 +321,18 @@ __global__ void __launch_bounds__(kSplitThreads) k_tile_hist(TileSplitParams<T> 
   load_splitters(p.splitters, S, p.key_bits, spl, lut, &lsh);
   uint64_t lo, hi;
   part_range(p.bucket_off, p.bucket_count, b, g, G, &lo, &hi);
-  for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-    atomicAdd(&hist[tile_of(spl, lut, lsh, S, p.keys_in[i])], 1u);
+  // kSplitUnroll independent loads in flight per thread before any use
+  for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += (uint64_t)kSplitThreads * kSplitUnroll) {
+    T key[kSplitUnroll];
+#pragma unroll
+    for (int u = 0; u < kSplitUnroll; ++u) {
+      const uint64_t i = i0 + (uint64_t)u * kSplitThreads;
+      key[u] = i < hi ? p.keys_in[i] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kSplitUnroll; ++u)
+      if (i0 + (uint64_t)u * kSplitThreads < hi) atomicAdd(&hist[tile_of(spl, lut, lsh, S, key[u])], 1u);
+  }
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < S; j += blockDim.x)
     p.tile_count[((size_t)b * S + j) * G + g] = hist[j];
@@ -344,11 +355,20 @@ __global__ void __launch_bounds__(kSplitThreads) k_tile_scatter(TileSplitParams<
   load_splitters(p.splitters, S, p.key_bits, spl, lut, &lsh);
   uint64_t lo, hi;
   part_range(p.bucket_off, p.bucket_count, b, g, G, &lo, &hi);
-  for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    const T key = p.keys_in[i];
-    const uint32_t j = tile_of(spl, lut, lsh, S, key);
-    const unsigned slot = atomicAdd(&cur[j], 1u);
-    p.keys_out[base[j] + slot] = key;
+  for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += (uint64_t)kSplitThreads * kSplitUnroll) {
+    T key[kSplitUnroll];
+#pragma unroll
+    for (int u = 0; u < kSplitUnroll; ++u) {
+      const uint64_t i = i0 + (uint64_t)u * kSplitThreads;
+      key[u] = i < hi ? p.keys_in[i] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kSplitUnroll; ++u) {
+      if (i0 + (uint64_t)u * kSplitThreads >= hi) break;
+      const uint32_t j = tile_of(spl, lut, lsh, S, key[u]);
+      const unsigned slot = atomicAdd(&cur[j], 1u);
+      p.keys_out[base[j] + slot] = key[u];
+    }
   }
 }
 

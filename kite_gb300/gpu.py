@@ -154,14 +154,20 @@ class Counter:
     def submit_device(self, ptr: int, n: int) -> None:
         self._check(self._L.kite_gpu_count_submit_device(self._h, C.c_void_p(ptr), n))
 
-    def finish(self, collect: bool = True, callback=None) -> list:
+    def finish(self, collect: bool = True, callback=None, raw: bool = False) -> list:
         """Count the segment; returns [(meta dict, payload bytes)] per non-empty
-        partition when collect, else keeps results on the device."""
+        partition when collect, else keeps results on the device.  With raw and
+        a callback, the callback gets (meta, host address, length) of the
+        payload in the library's host buffer (valid during the call) instead of
+        a copy."""
         out = []
 
         def _emit(user, meta, data, n):
             try:
                 m = meta.contents.as_dict()
+                if raw and callback is not None:
+                    callback(m, C.cast(data, C.c_void_p).value, n)
+                    return 0
                 payload = C.string_at(data, n)
                 if callback is not None:
                     callback(m, payload)
