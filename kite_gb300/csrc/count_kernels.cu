@@ -254,121 +254,187 @@ template void launch_extract_scatter<uint64_t>(const ExtractParams<uint64_t>&, u
 template void launch_extract_scatter<u128>(const ExtractParams<u128>&, uint32_t, cudaStream_t);
 
 // ---------------------------------------------------------------------------
-// Level-2 split: inside every hash bucket, route keys to S key-range tiles by
-// the splitters (upper bound = number of splitters <= key).  Tiles are laid
-// out bucket-major, so each bucket's tiles stay contiguous and in key order.
-// Each bucket is cut into G parts; part (b, g) owns the sub-range
-// [off[(b*S+j)*G+g], +cnt) of tile (b, j), so no two CTAs share a cursor and
+// Key-range split: inside every hash bucket, route keys to S key-range tiles
+// by the global splitters (tile of a key = number of splitters <= key).
+// Tiles are laid out bucket-major, so each bucket's tiles stay contiguous and
+// in key order.  One level handles D <= 256 sub-ranges ("digits") per region;
+// S > 256 tiles take two levels (coarse ranges, then tiles inside each coarse
+// range), so that every scatter writes to at most 256 destinations.
+// Each region is processed in G parts; part (r, g) owns the sub-range
+// [off[(r*D+d)*G+g], +count) of digit d, so no two CTAs share a cursor and
 // the only atomics are shared-memory ones.
 // ---------------------------------------------------------------------------
-// Tile of a key = number of splitters <= key.  A lookup table over the top
-// kLutBits of the key gives the number of splitters below the key's bin; a
-// short forward scan covers the splitters inside the bin (exact for any
-// ascending splitters).
-static constexpr int kLutBits = 12;
-
-template <class T>
-__device__ __forceinline__ uint32_t tile_of(const T* spl, const uint16_t* lut, uint32_t lut_shift, uint32_t S,
-                                            T key) {
-  uint32_t j = lut[(uint32_t)(uint64_t)(key >> lut_shift)];
-  while (j + 1 < S && spl[j] <= key) ++j;
-  return j;
-}
-
-// Loads the splitters and builds the table (block-wide; ends with a barrier).
-template <class T>
-__device__ __forceinline__ void load_splitters(const T* g_spl, uint32_t S, uint32_t key_bits, T* spl, uint16_t* lut,
-                                               uint32_t* lut_shift) {
-  for (uint32_t i = threadIdx.x; i + 1 < S; i += blockDim.x) spl[i] = g_spl[i];
-  __syncthreads();
-  const uint32_t L = key_bits < (uint32_t)kLutBits ? key_bits : (uint32_t)kLutBits;
-  *lut_shift = key_bits - L;
-  for (uint32_t bin = threadIdx.x; bin < (1u << L); bin += blockDim.x) {
-    const T start = (T)bin << *lut_shift;
-    uint32_t lo = 0, hi = S - 1;  // lower_bound over S-1 splitters
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (spl[mid] < start) lo = mid + 1;
-      else hi = mid;
-    }
-    lut[bin] = (uint16_t)lo;
-  }
-  __syncthreads();
-}
-
-static constexpr size_t kLutBytes = ((size_t)(1u << kLutBits) * 2 + 15) & ~(size_t)15;
-
+static constexpr int kLutBits = 12, kLutSize = 1 << kLutBits;
+static constexpr size_t kLutBytes = ((size_t)(kLutSize + 1) * 2 + 15) & ~(size_t)15;
 static constexpr int kSplitThreads = 512;
 static constexpr int kSplitUnroll = 8;
+static constexpr uint32_t kMaxDigits = 256;
 
-__device__ __forceinline__ void part_range(const unsigned long long* boff, const unsigned long long* bcnt,
-                                           uint32_t b, uint32_t g, uint32_t G, uint64_t* lo, uint64_t* hi) {
-  const uint64_t n = bcnt[b], base = boff[b];
+// Loads region r's D-1 digit splitters and builds a table over the region's
+// key range [lo, hi] (the splitters just outside it): lut[bin] = number of the
+// region's splitters below the bin's first key.  Block-wide; ends with a barrier.
+template <class T>
+__device__ void load_digits(const TileSplitParams<T>& p, uint32_t r, T* spl, uint16_t* lut, T* lo_out,
+                            uint32_t* shift_out) {
+  const uint32_t nspl = p.D - 1;
+  const long long base = (long long)p.spl_first + (long long)(r % p.spl_mod) * p.spl_region_stride;
+  for (uint32_t i = threadIdx.x; i < nspl; i += blockDim.x) spl[i] = p.splitters[base + (long long)i * p.spl_step];
+  const long long lo_i = base - (long long)p.spl_step, hi_i = base + (long long)nspl * p.spl_step;
+  const T kmax = p.key_bits >= (uint32_t)KeyTraits<T>::kBits ? ~T(0) : ((T(1) << p.key_bits) - T(1));
+  const T lo = lo_i >= 0 ? p.splitters[lo_i] : T(0);
+  const T hi = hi_i < (long long)p.spl_total ? p.splitters[hi_i] : kmax;
+  const T range = hi > lo ? T(hi - lo) : T(0);
+  const int rb = range == T(0) ? 0 : KeyTraits<T>::kBits - clz_key(range);
+  const uint32_t shift = rb > kLutBits ? (uint32_t)(rb - kLutBits) : 0u;
+  __syncthreads();
+  for (uint32_t bin = threadIdx.x; bin <= (uint32_t)kLutSize; bin += blockDim.x) {
+    uint32_t v = nspl;
+    if (bin < (uint32_t)kLutSize) {
+      const T off = (T)bin << shift;
+      if (off <= T(~T(0) - lo)) {
+        const T start = lo + off;
+        uint32_t a = 0, e = nspl;  // lower bound: splitters below start
+        while (a < e) {
+          const uint32_t m = (a + e) >> 1;
+          if (spl[m] < start) a = m + 1;
+          else e = m;
+        }
+        v = a;
+      }
+    }
+    lut[bin] = (uint16_t)v;
+  }
+  __syncthreads();
+  *lo_out = lo;
+  *shift_out = shift;
+}
+
+// Digit of a key (>= lo): number of the region's splitters <= key, searched
+// between the table entries of its bin and the next.
+template <class T>
+__device__ __forceinline__ uint32_t digit_of_key(const T* spl, const uint16_t* lut, T lo, uint32_t shift, T key) {
+  const T rel = key > lo ? T(key - lo) : T(0);
+  const T b = rel >> shift;
+  const uint32_t bin = b >= (T)kLutSize ? (uint32_t)kLutSize - 1u : (uint32_t)(uint64_t)b;
+  uint32_t a = lut[bin], e = lut[bin + 1];
+  while (a < e) {
+    const uint32_t m = (a + e) >> 1;
+    if (spl[m] <= key) a = m + 1;
+    else e = m;
+  }
+  return a;
+}
+
+__device__ __forceinline__ void part_range(const unsigned long long* roff, const unsigned long long* rcnt,
+                                           uint32_t r, uint32_t g, uint32_t G, uint64_t* lo, uint64_t* hi) {
+  const uint64_t n = rcnt[r], base = roff[r];
   *lo = base + n * g / G;
   *hi = base + n * (g + 1) / G;
 }
 
+// Digit histogram of one part (shared-memory counters).
 template <class T>
-__global__ void __launch_bounds__(kSplitThreads) k_tile_hist(TileSplitParams<T> p) {
-  extern __shared__ __align__(16) uint8_t sm[];
-  const uint32_t S = p.S, G = p.G;
-  T* spl = reinterpret_cast<T*>(sm);
-  uint16_t* lut = reinterpret_cast<uint16_t*>(sm + (size_t)S * sizeof(T));
-  unsigned* hist = reinterpret_cast<unsigned*>(sm + (size_t)S * sizeof(T) + kLutBytes);
-  const uint32_t b = blockIdx.x / G, g = blockIdx.x % G;
-  for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) hist[i] = 0;
-  uint32_t lsh;
-  load_splitters(p.splitters, S, p.key_bits, spl, lut, &lsh);
-  uint64_t lo, hi;
-  part_range(p.bucket_off, p.bucket_count, b, g, G, &lo, &hi);
+__global__ void __launch_bounds__(kSplitThreads) k_split_hist(TileSplitParams<T> p) {
+  __shared__ T spl[kMaxDigits];
+  __shared__ __align__(16) uint16_t lut[kLutBytes / 2];
+  __shared__ unsigned hist[kMaxDigits];
+  const uint32_t D = p.D, G = p.G;
+  const uint32_t r = blockIdx.x / G, g = blockIdx.x % G;
+  for (uint32_t i = threadIdx.x; i < D; i += kSplitThreads) hist[i] = 0;
+  T lo;
+  uint32_t sh;
+  load_digits(p, r, spl, lut, &lo, &sh);
+  uint64_t a, e;
+  part_range(p.region_off, p.region_count, r, g, G, &a, &e);
   // kSplitUnroll independent loads in flight per thread before any use
-  for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += (uint64_t)kSplitThreads * kSplitUnroll) {
+  for (uint64_t i0 = a + threadIdx.x; i0 < e; i0 += (uint64_t)kSplitThreads * kSplitUnroll) {
     T key[kSplitUnroll];
 #pragma unroll
     for (int u = 0; u < kSplitUnroll; ++u) {
       const uint64_t i = i0 + (uint64_t)u * kSplitThreads;
-      key[u] = i < hi ? p.keys_in[i] : T(0);
+      key[u] = i < e ? p.keys_in[i] : T(0);
     }
 #pragma unroll
     for (int u = 0; u < kSplitUnroll; ++u)
-      if (i0 + (uint64_t)u * kSplitThreads < hi) atomicAdd(&hist[tile_of(spl, lut, lsh, S, key[u])], 1u);
+      if (i0 + (uint64_t)u * kSplitThreads < e) atomicAdd(&hist[digit_of_key(spl, lut, lo, sh, key[u])], 1u);
   }
   __syncthreads();
-  for (uint32_t j = threadIdx.x; j < S; j += blockDim.x)
-    p.tile_count[((size_t)b * S + j) * G + g] = hist[j];
+  for (uint32_t d = threadIdx.x; d < D; d += kSplitThreads) p.tile_count[((size_t)r * D + d) * G + g] = hist[d];
 }
 
+// Scatter of one part, a batch of BATCH keys at a time: the batch is ranked on
+// chip by digit (stable warp-match ranking), staged in digit order, and each
+// digit's run is written to its destination with consecutive threads on
+// consecutive addresses, so global writes go out as whole sectors.
 template <class T>
-__global__ void __launch_bounds__(kSplitThreads) k_tile_scatter(TileSplitParams<T> p) {
+struct ScatterSmem {
+  static constexpr int NT = kSplitThreads, NW = NT / 32;
+  static constexpr int IT = sizeof(T) == 8 ? 8 : 4;
+  static constexpr int BATCH = NT * IT;
+  static constexpr size_t o_stage = 0;
+  static constexpr size_t o_dig = o_stage + (size_t)BATCH * sizeof(T);
+  static constexpr size_t o_whist = o_dig + (size_t)BATCH;
+  static constexpr size_t o_cur = o_whist + (size_t)kMaxDigits * NW * 4;
+  static constexpr size_t o_dtot = o_cur + (size_t)kMaxDigits * 8;
+  static constexpr size_t o_dstart = o_dtot + (size_t)kMaxDigits * 4;
+  static constexpr size_t o_spl = o_dstart + (size_t)kMaxDigits * 4;
+  static constexpr size_t o_lut = o_spl + (size_t)kMaxDigits * sizeof(T);
+  static constexpr size_t o_scan = o_lut + kLutBytes;
+  static constexpr size_t total = o_scan + 64 * 4;
+};
+
+template <class T>
+__global__ void __launch_bounds__(kSplitThreads, 2) k_split_scatter(TileSplitParams<T> p) {
+  using L = ScatterSmem<T>;
+  constexpr int NT = L::NT, IT = L::IT, BATCH = L::BATCH;
   extern __shared__ __align__(16) uint8_t sm[];
-  const uint32_t S = p.S, G = p.G;
-  unsigned long long* base = reinterpret_cast<unsigned long long*>(sm);
-  T* spl = reinterpret_cast<T*>(base + S);
-  uint16_t* lut = reinterpret_cast<uint16_t*>(sm + (size_t)S * 8 + (size_t)S * sizeof(T));
-  unsigned* cur = reinterpret_cast<unsigned*>(sm + (size_t)S * 8 + (size_t)S * sizeof(T) + kLutBytes);
-  const uint32_t b = blockIdx.x / G, g = blockIdx.x % G;
-  for (uint32_t j = threadIdx.x; j < S; j += blockDim.x) {
-    base[j] = p.tile_off[((size_t)b * S + j) * G + g];
-    cur[j] = 0;
-  }
-  uint32_t lsh;
-  load_splitters(p.splitters, S, p.key_bits, spl, lut, &lsh);
-  uint64_t lo, hi;
-  part_range(p.bucket_off, p.bucket_count, b, g, G, &lo, &hi);
-  for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += (uint64_t)kSplitThreads * kSplitUnroll) {
-    T key[kSplitUnroll];
+  T* stage = reinterpret_cast<T*>(sm + L::o_stage);
+  uint8_t* dig8 = sm + L::o_dig;
+  unsigned* whist = reinterpret_cast<unsigned*>(sm + L::o_whist);
+  unsigned long long* cur = reinterpret_cast<unsigned long long*>(sm + L::o_cur);
+  unsigned* dtot = reinterpret_cast<unsigned*>(sm + L::o_dtot);
+  unsigned* dstart = reinterpret_cast<unsigned*>(sm + L::o_dstart);
+  T* spl = reinterpret_cast<T*>(sm + L::o_spl);
+  uint16_t* lut = reinterpret_cast<uint16_t*>(sm + L::o_lut);
+  unsigned* scan_sm = reinterpret_cast<unsigned*>(sm + L::o_scan);
+  const uint32_t D = p.D, G = p.G;
+  const uint32_t r = blockIdx.x / G, g = blockIdx.x % G;
+  for (uint32_t d = threadIdx.x; d < D; d += NT) cur[d] = p.tile_off[((size_t)r * D + d) * G + g];
+  T lo;
+  uint32_t sh;
+  load_digits(p, r, spl, lut, &lo, &sh);
+  uint64_t a, e;
+  part_range(p.region_off, p.region_count, r, g, G, &a, &e);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned pos0 = (unsigned)wid * 32u * IT + lane;
+  for (uint64_t c0 = a; c0 < e; c0 += BATCH) {
+    const unsigned cn = (unsigned)((e - c0) < (uint64_t)BATCH ? (e - c0) : (uint64_t)BATCH);
+    T key[IT];
+    unsigned dg[IT], dest[IT];
+    bool valid[IT];
 #pragma unroll
-    for (int u = 0; u < kSplitUnroll; ++u) {
-      const uint64_t i = i0 + (uint64_t)u * kSplitThreads;
-      key[u] = i < hi ? p.keys_in[i] : T(0);
+    for (int q = 0; q < IT; ++q) {
+      const unsigned pos = pos0 + q * 32u;
+      valid[q] = pos < cn;
+      key[q] = valid[q] ? p.keys_in[c0 + pos] : T(0);
     }
 #pragma unroll
-    for (int u = 0; u < kSplitUnroll; ++u) {
-      if (i0 + (uint64_t)u * kSplitThreads >= hi) break;
-      const uint32_t j = tile_of(spl, lut, lsh, S, key[u]);
-      const unsigned slot = atomicAdd(&cur[j], 1u);
-      p.keys_out[base[j] + slot] = key[u];
+    for (int q = 0; q < IT; ++q) dg[q] = valid[q] ? digit_of_key(spl, lut, lo, sh, key[q]) : 0u;
+    block_rank<NT, IT, (int)kMaxDigits>(dg, valid, dest, whist, scan_sm, dtot, dstart);
+#pragma unroll
+    for (int q = 0; q < IT; ++q)
+      if (valid[q]) {
+        stage[dest[q]] = key[q];
+        dig8[dest[q]] = (uint8_t)dg[q];
+      }
+    __syncthreads();
+    for (unsigned i = threadIdx.x; i < cn; i += NT) {
+      const unsigned d = dig8[i];
+      p.keys_out[cur[d] + (i - dstart[d])] = stage[i];
     }
+    __syncthreads();
+    for (uint32_t d = threadIdx.x; d < D; d += NT) cur[d] += dtot[d];
+    __syncthreads();
   }
 }
 
@@ -388,22 +454,28 @@ __global__ void k_make_tiles(const unsigned long long* __restrict__ off, uint32_
   lens[t] = d.len;
 }
 
-size_t tile_split_smem(int key_bytes, uint32_t S, bool scatter) {
-  return (scatter ? (size_t)S * 8 : 0) + (size_t)S * key_bytes + kLutBytes + (size_t)S * 4;
+// Region bounds of the next level from a level's scanned part offsets.
+__global__ void k_region_bounds(const unsigned long long* __restrict__ off, uint32_t nreg, uint32_t G,
+                                unsigned long long n_keys, unsigned long long* __restrict__ roff,
+                                unsigned long long* __restrict__ rcnt) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nreg) return;
+  const unsigned long long a = off[(size_t)t * G];
+  const unsigned long long e = t + 1 < nreg ? off[(size_t)(t + 1) * G] : n_keys;
+  roff[t] = a;
+  rcnt[t] = e - a;
 }
 
 template <class T>
-void launch_tile_hist(const TileSplitParams<T>& p, cudaStream_t s) {
-  const size_t smem = tile_split_smem(sizeof(T), p.S, false);
-  cudaFuncSetAttribute(k_tile_hist<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_tile_hist<T><<<p.P * p.G, kSplitThreads, smem, s>>>(p);
+void launch_split_hist(const TileSplitParams<T>& p, cudaStream_t s) {
+  if (p.R * p.G) k_split_hist<T><<<p.R * p.G, kSplitThreads, 0, s>>>(p);
 }
 
 template <class T>
-void launch_tile_scatter(const TileSplitParams<T>& p, cudaStream_t s) {
-  const size_t smem = tile_split_smem(sizeof(T), p.S, true);
-  cudaFuncSetAttribute(k_tile_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_tile_scatter<T><<<p.P * p.G, kSplitThreads, smem, s>>>(p);
+void launch_split_scatter(const TileSplitParams<T>& p, cudaStream_t s) {
+  const size_t smem = ScatterSmem<T>::total;
+  cudaFuncSetAttribute(k_split_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (p.R * p.G) k_split_scatter<T><<<p.R * p.G, kSplitThreads, smem, s>>>(p);
 }
 
 void launch_make_tiles(const unsigned long long* off, uint32_t ntiles, uint32_t S, uint32_t G,
@@ -411,9 +483,14 @@ void launch_make_tiles(const unsigned long long* off, uint32_t ntiles, uint32_t 
   if (ntiles) k_make_tiles<<<(ntiles + 255) / 256, 256, 0, s>>>(off, ntiles, S, G, n_keys, tiles, lens);
 }
 
-template void launch_tile_hist<uint64_t>(const TileSplitParams<uint64_t>&, cudaStream_t);
-template void launch_tile_hist<u128>(const TileSplitParams<u128>&, cudaStream_t);
-template void launch_tile_scatter<uint64_t>(const TileSplitParams<uint64_t>&, cudaStream_t);
-template void launch_tile_scatter<u128>(const TileSplitParams<u128>&, cudaStream_t);
+void launch_region_bounds(const unsigned long long* off, uint32_t nreg, uint32_t G, unsigned long long n_keys,
+                          unsigned long long* roff, unsigned long long* rcnt, cudaStream_t s) {
+  if (nreg) k_region_bounds<<<(nreg + 255) / 256, 256, 0, s>>>(off, nreg, G, n_keys, roff, rcnt);
+}
+
+template void launch_split_hist<uint64_t>(const TileSplitParams<uint64_t>&, cudaStream_t);
+template void launch_split_hist<u128>(const TileSplitParams<u128>&, cudaStream_t);
+template void launch_split_scatter<uint64_t>(const TileSplitParams<uint64_t>&, cudaStream_t);
+template void launch_split_scatter<u128>(const TileSplitParams<u128>&, cudaStream_t);
 
 }  // namespace kite

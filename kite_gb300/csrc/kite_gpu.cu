@@ -107,6 +107,7 @@ struct kite_gpu_ctx {
   DevBuf blocks, nl, scan_tmp, bucket_count, bucket_off, bucket_fill, totals, status;
   DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, splitters2, hist16;
   DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
+  DevBuf lvl_count, lvl_off, reg_off, reg_cnt;
   HostBuf h_blocks, h_small, h_tiles, h_out;
   std::vector<cudaEvent_t> ev;  // stage events
 
@@ -378,30 +379,84 @@ int run_count(kite_gpu_ctx* ctx) {
     st.hist_pred_imbalance = hist_imb;
     st.splitter_used = learned ? KITE_SPLIT_LEARNED : KITE_SPLIT_SAMPLED;
     const T* chosen = learned ? mlp_spl : hist_spl;
-    // G parts per bucket: enough CTAs to fill the GPU twice, parts of >= 32K keys
-    uint32_t G = (uint32_t)std::max<uint64_t>(1, (2ull * 152 + P - 1) / P);
-    G = (uint32_t)std::min<uint64_t>(G, std::max<uint64_t>(1, maxb / 32768));
-    G = std::min<uint32_t>(G, 64);
-    const size_t nt = (size_t)P * S, ntg = nt * G;
+    // Split into tiles: one level of S digits when S <= 256, else coarse
+    // ranges of 256 tiles first, then the tiles inside each coarse range.
+    // G parts per region: enough CTAs to fill the GPU twice, parts of >= 32K keys.
+    auto parts = [&](uint64_t regions, uint64_t max_region) {
+      uint64_t g = std::max<uint64_t>(1, (2ull * 152 + regions - 1) / regions);
+      g = std::min<uint64_t>(g, std::max<uint64_t>(1, max_region / 32768));
+      return (uint32_t)std::min<uint64_t>(g, 64);
+    };
+    const uint32_t D2 = std::min<uint32_t>(S, 256), D1 = S / D2;
+    const size_t nt = (size_t)P * S;
+    TileSplitParams<T> tp{};
+    tp.splitters = chosen;
+    tp.spl_total = S - 1;
+    tp.key_bits = 2 * k;
+    tp.spl_step = 1;
+    tp.spl_mod = 1;
+    uint32_t G = 1;
+    T* level_in = ctx->keys_a.as<T>();
+    T* level_out = ctx->keys_b.as<T>();
+    if (D1 > 1) {
+      // level 1: buckets -> (bucket, coarse range); coarse splitter c is tile splitter (c+1)*D2-1
+      const uint32_t G1 = parts(P, maxb);
+      const size_t n1 = (size_t)P * D1 * G1;
+      KCU(ctx->lvl_count.ensure(n1 * 8));
+      KCU(ctx->lvl_off.ensure(n1 * 8));
+      KCU(ctx->reg_off.ensure((size_t)P * D1 * 8));
+      KCU(ctx->reg_cnt.ensure((size_t)P * D1 * 8));
+      KCU(ctx->scan_tmp.ensure(scan_tmp_elems(n1) * 8 + 64));
+      TileSplitParams<T> t1 = tp;
+      t1.keys_in = level_in;
+      t1.keys_out = level_out;
+      t1.region_off = ctx->bucket_off.as<unsigned long long>();
+      t1.region_count = ctx->bucket_count.as<unsigned long long>();
+      t1.R = P;
+      t1.D = D1;
+      t1.G = G1;
+      t1.spl_first = D2 - 1;
+      t1.spl_step = D2;
+      t1.spl_region_stride = 0;
+      t1.tile_count = ctx->lvl_count.as<unsigned long long>();
+      t1.tile_off = ctx->lvl_off.as<unsigned long long>();
+      launch_split_hist<T>(t1, s);
+      st.kernel_launches += 3 + exclusive_scan_u64(t1.tile_count, ctx->lvl_off.as<unsigned long long>(), n1,
+                                                   ctx->scan_tmp.as<unsigned long long>(), s);
+      launch_split_scatter<T>(t1, s);
+      launch_region_bounds(t1.tile_off, P * D1, G1, N, ctx->reg_off.as<unsigned long long>(),
+                           ctx->reg_cnt.as<unsigned long long>(), s);
+      // level 2: (bucket, coarse c) -> tiles c*D2 .. c*D2+D2-1
+      G = parts((uint64_t)P * D1, (maxb + D1 - 1) / D1 * 2);
+      tp.region_off = ctx->reg_off.as<unsigned long long>();
+      tp.region_count = ctx->reg_cnt.as<unsigned long long>();
+      tp.R = P * D1;
+      tp.spl_first = 0;
+      tp.spl_mod = D1;
+      tp.spl_region_stride = D2;
+      std::swap(level_in, level_out);
+    } else {
+      G = parts(P, maxb);
+      tp.region_off = ctx->bucket_off.as<unsigned long long>();
+      tp.region_count = ctx->bucket_count.as<unsigned long long>();
+      tp.R = P;
+      tp.spl_first = 0;
+      tp.spl_region_stride = 0;
+    }
+    const size_t ntg = nt * G;
     KCU(ctx->tile_count.ensure(ntg * 8));
     KCU(ctx->tile_off.ensure(ntg * 8));
     KCU(ctx->scan_tmp.ensure(scan_tmp_elems(ntg) * 8 + 64));
-    TileSplitParams<T> tp{};
-    tp.keys_in = ctx->keys_a.as<T>();
-    tp.keys_out = ctx->keys_b.as<T>();
-    tp.bucket_off = ctx->bucket_off.as<unsigned long long>();
-    tp.bucket_count = ctx->bucket_count.as<unsigned long long>();
-    tp.splitters = chosen;
-    tp.P = P;
-    tp.S = S;
+    tp.keys_in = level_in;
+    tp.keys_out = level_out;
+    tp.D = D2;
     tp.G = G;
-    tp.key_bits = 2 * k;
     tp.tile_count = ctx->tile_count.as<unsigned long long>();
     tp.tile_off = ctx->tile_off.as<unsigned long long>();
-    launch_tile_hist<T>(tp, s);
+    launch_split_hist<T>(tp, s);
     st.kernel_launches += 3 + exclusive_scan_u64(tp.tile_count, ctx->tile_off.as<unsigned long long>(), ntg,
                                                  ctx->scan_tmp.as<unsigned long long>(), s);
-    launch_tile_scatter<T>(tp, s);
+    launch_split_scatter<T>(tp, s);
     KCU(ctx->tiles.ensure(nt * sizeof(TileDesc)));
     KCU(ctx->tile_fill.ensure(nt * 4));
     launch_make_tiles(ctx->tile_off.as<unsigned long long>(), (uint32_t)nt, S, G, N, ctx->tiles.as<TileDesc>(),
@@ -414,8 +469,8 @@ int run_count(kite_gpu_ctx* ctx) {
     const uint32_t* lens = ctx->h_tiles.as<uint32_t>();
     ht.resize(nt);
     for (size_t t = 0; t < nt; ++t) ht[t] = TileDesc{0, lens[t], (uint32_t)(t / S)};
-    sorted = ctx->keys_b.as<T>();
-    scratch = ctx->keys_a.as<T>();
+    sorted = level_out;
+    scratch = level_in;
   }
   KCU(cudaEventRecord(ctx->ev[4], s));
   const uint32_t ntiles = (uint32_t)ht.size();
@@ -614,7 +669,8 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
                     &ctx->bucket_fill, &ctx->totals, &ctx->status, &ctx->keys_a, &ctx->keys_b, &ctx->counts,
                     &ctx->sample, &ctx->sample_count, &ctx->splitters, &ctx->splitters2, &ctx->hist16,
                     &ctx->tile_count, &ctx->tile_off, &ctx->tile_fill, &ctx->tiles, &ctx->big_ids,
-                    &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out};
+                    &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out,
+                    &ctx->lvl_count, &ctx->lvl_off, &ctx->reg_off, &ctx->reg_cnt};
   for (DevBuf* b : bufs) b->release();
   ctx->h_blocks.release();
   ctx->h_small.release();

@@ -63,18 +63,25 @@ struct ExtractParams {
   DevStatus* status;
 };
 
+// One level of the key-range split.  Region r (a hash bucket, or one coarse
+// key range of a bucket) is cut into D <= 256 digits by D-1 of the global
+// splitters: spl[spl_first + (r % spl_mod) * spl_region_stride + i * spl_step]
+// for i < D-1 (spl_total splitters in all).  Each region is processed in G
+// parts.
 template <class T>
 struct TileSplitParams {
-  const T* keys_in;       // bucket-grouped keys
-  T* keys_out;            // tile-grouped keys
-  const unsigned long long* bucket_off;    // [P]
-  const unsigned long long* bucket_count;  // [P]
-  const T* splitters;     // S-1 ascending keys
-  uint32_t P;
-  uint32_t S;             // tiles per bucket (power of two)
-  uint32_t G;             // parts per bucket
-  uint32_t key_bits;      // 2k: significant key bits (splitter lookup table)
-  unsigned long long* tile_count;       // [P*S*G] (tile-major, part-minor)
+  const T* keys_in;
+  T* keys_out;
+  const unsigned long long* region_off;    // [R] first key of each region
+  const unsigned long long* region_count;  // [R]
+  const T* splitters;     // spl_total ascending keys
+  uint32_t spl_total;
+  uint32_t R;             // regions
+  uint32_t D;             // digits per region (2..256)
+  uint32_t G;             // parts per region
+  uint32_t spl_first, spl_step, spl_mod, spl_region_stride;
+  uint32_t key_bits;      // 2k: significant key bits
+  unsigned long long* tile_count;       // [R*D*G] (digit-major, part-minor)
   const unsigned long long* tile_off;   // exclusive scan of tile_count
 };
 
@@ -86,12 +93,13 @@ void launch_extract_hist(const ExtractParams<T>& p, uint32_t nblocks, cudaStream
 template <class T>
 void launch_extract_scatter(const ExtractParams<T>& p, uint32_t nblocks, cudaStream_t s);
 template <class T>
-void launch_tile_hist(const TileSplitParams<T>& p, cudaStream_t s);
+void launch_split_hist(const TileSplitParams<T>& p, cudaStream_t s);
 template <class T>
-void launch_tile_scatter(const TileSplitParams<T>& p, cudaStream_t s);
+void launch_split_scatter(const TileSplitParams<T>& p, cudaStream_t s);
 void launch_make_tiles(const unsigned long long* off, uint32_t ntiles, uint32_t S, uint32_t G,
                        unsigned long long n_keys, TileDesc* tiles, uint32_t* lens, cudaStream_t s);
-size_t tile_split_smem(int key_bytes, uint32_t S, bool scatter);
+void launch_region_bounds(const unsigned long long* off, uint32_t nreg, uint32_t G, unsigned long long n_keys,
+                          unsigned long long* roff, unsigned long long* rcnt, cudaStream_t s);
 size_t extract_smem_bytes(int key_bytes, uint32_t blk_bytes, uint32_t partitions, bool scatter);
 
 // ---- scan.cu ----

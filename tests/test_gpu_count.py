@@ -47,6 +47,13 @@ def test_tiled_buckets_u64(gpu, orc):
     assert st["tiles_per_bucket"] > 1
 
 
+def test_tiled_single_level(gpu, orc):
+    # up to 256 tiles per bucket: the split runs as one level
+    fq = synth.small_workload(seed=3, n_reads=20_000, genome_len=400_000)
+    st = assert_parity(gpu, orc, fq, 25, True, 8)
+    assert 1 < st["tiles_per_bucket"] <= 256
+
+
 def test_tiled_buckets_u128(gpu, orc):
     fq = synth.small_workload(seed=2, n_reads=40_000, genome_len=500_000)
     st = assert_parity(gpu, orc, fq, 63, True, 2, chunk_size=1 << 20)
