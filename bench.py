@@ -399,7 +399,7 @@ def main():
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "splitters": splitters,
                 "tiles": {"tiles": st["tiles"], "per_bucket": st["tiles_per_bucket"], "big": st["big_tiles"],
-                          "imbalance": st["tile_imbalance"]}}
+                          "imbalance": st["tile_imbalance"], "sort_fallbacks": st["sort_fallbacks"]}}
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

@@ -99,6 +99,7 @@ typedef struct {
   uint64_t kernel_launches;          /* kernels this library launched in the last finish */
   double mlp_loss, mlp_pred_imbalance, hist_pred_imbalance; /* learned-splitter diagnostics */
   double range_imbalance;            /* max / mean keys per key range (summed over partitions) */
+  uint64_t sort_fallbacks;           /* tiles whose on-chip sort fell back to LSD passes (a large bin of distinct keys) */
 } kite_gpu_stats;
 
 /* Merge input: one .kite file's partition table, with payloads in host memory

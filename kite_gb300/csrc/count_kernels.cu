@@ -103,8 +103,10 @@ __host__ __device__ __forceinline__ size_t padded_bytes(uint32_t blk_bytes) {
   return (segs * (pt + 4) + 15) & ~(size_t)15;
 }
 
+size_t extract64_smem_bytes(uint32_t partitions, bool scatter);
+
 size_t extract_smem_bytes(int key_bytes, uint32_t blk_bytes, uint32_t partitions, bool scatter) {
-  (void)key_bytes;
+  if (key_bytes == 8) return extract64_smem_bytes(partitions, scatter);
   size_t o = padded_bytes(blk_bytes);
   if (scatter) o += (size_t)partitions * 8;  // reservation base (u64)
   o += (size_t)partitions * 4;               // histogram / cursor
@@ -236,17 +238,246 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract(ExtractParams<T> p)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Bit-parallel extraction for k <= 31 (u64 keys).  Each thread owns 64 bytes
+// of the block as two 32-byte words and also encodes the word before them.
+// Per word, with byte-wise SIMD compares: 2-bit codes packed with the first
+// byte in the top bits, the reverse-complement stream (field-reversed ~code),
+// and bit masks of newlines and A/C/G/T bytes.  Line phase gives the
+// sequence-line mask; a k-mer ending at byte e is valid when the k mask bits
+// ending at e are all set, and its forward and reverse-complement values are
+// two funnel shifts of the (previous word, word) pair.  Only valid ends are
+// visited, so the cost is per k-mer, not per byte.
+// ---------------------------------------------------------------------------
+struct Word32 {
+  uint64_t code;   // 2-bit codes, byte 0 in bits 63..62
+  uint64_t rcode;  // complement codes in reverse byte order (byte 31 in bits 63..62)
+  uint32_t nl;     // bit i: byte i is '\n'
+  uint32_t vb;     // bit i: byte i is A/C/G/T in either case
+};
+
+// one bit per byte from a byte-wise 0x00/0xFF mask (byte j -> bit j)
+__device__ __forceinline__ uint32_t byte_bits(uint32_t m) { return ((m & 0x01010101u) * 0x10204080u) >> 28; }
+
+__device__ __forceinline__ Word32 encode_word(const uint4 a, const uint4 b) {
+  const uint32_t x[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+  Word32 w;
+  w.code = 0;
+  w.nl = 0;
+  w.vb = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const uint32_t v = x[q];
+    const uint32_t u = v & 0xDFDFDFDFu;  // fold lower case
+    const uint32_t valid = __vcmpeq4(u, 0x41414141u) | __vcmpeq4(u, 0x43434343u) | __vcmpeq4(u, 0x47474747u) |
+                           __vcmpeq4(u, 0x54545454u);
+    // A/a=0 C/c=1 G/g=2 T/t=3 from ASCII bits 1 and 2
+    const uint32_t c4 = ((v >> 1) ^ (v >> 2)) & 0x03030303u;
+    const uint32_t p8 = (c4 * 0x40100401u) >> 24;  // byte 0's code in bits 7..6
+    w.code |= (uint64_t)p8 << (56 - 8 * q);
+    w.nl |= byte_bits(__vcmpeq4(v, 0x0a0a0a0au)) << (4 * q);
+    w.vb |= byte_bits(valid) << (4 * q);
+  }
+  uint64_t r = __brevll(~w.code);
+  w.rcode = ((r >> 1) & 0x5555555555555555ull) | ((r & 0x5555555555555555ull) << 1);
+  return w;
+}
+
+// Sequence-line bytes of a word given the line phase at its first byte;
+// advances the phase past the word.
+__device__ __forceinline__ uint32_t seq_mask(uint32_t nl, unsigned& ph) {
+  uint32_t seq = 0, m = nl;
+  unsigned start = 0, p = ph;
+  while (m) {
+    const unsigned q = __ffs(m) - 1;
+    if (p == 1) seq |= (uint32_t)((1ull << q) - (1ull << start));
+    p = (p + 1) & 3u;
+    start = q + 1;
+    m &= m - 1;
+  }
+  if (p == 1) seq |= (uint32_t)((1ull << 32) - (1ull << start));
+  ph = p;
+  return seq;
+}
+
+// bit j set iff bits j .. j+k-1 of a are all set
+__device__ __forceinline__ uint64_t runs_of(uint64_t a, uint32_t k) {
+  uint64_t r = a;
+  uint32_t len = 1;
+  while (2 * len <= k) {
+    r &= r >> len;
+    len *= 2;
+  }
+  if (len < k) r &= r >> (k - len);
+  return r;
+}
+
+// Visits every valid k-mer ending in word w (previous word pw): f(key, e).
+template <class F>
+__device__ __forceinline__ void word_kmers(uint32_t V, const Word32& pw, const Word32& w, uint32_t k, uint64_t mask,
+                                           bool canonical, F&& f) {
+  while (V) {
+    const uint32_t e = __ffs(V) - 1;
+    V &= V - 1;
+    const uint32_t s = 2 * (31 - e);
+    const uint64_t fwd = (s ? ((w.code >> s) | (pw.code << (64 - s))) : w.code) & mask;
+    uint64_t key = fwd;
+    if (canonical) {
+      const uint32_t t = 2 * (33 + e - k);  // 4 .. 126
+      const uint64_t rc = (t < 64 ? ((pw.rcode >> t) | (w.rcode << (64 - t))) : (w.rcode >> (t - 64))) & mask;
+      key = rc < fwd ? rc : fwd;
+    }
+    f(key, e);
+  }
+}
+
+__device__ __forceinline__ void load_word(const uint8_t* arena, uint64_t pos, uint64_t end, Word32& w,
+                                          uint32_t& in_range) {
+  uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
+  // only 16-byte halves that start inside the block: at most 15 bytes past
+  // its end, which the 16 pad bytes after every chunk cover
+  if (pos < end) a = *reinterpret_cast<const uint4*>(arena + pos);
+  if (pos + 16 < end) b = *reinterpret_cast<const uint4*>(arena + pos + 16);
+  w = encode_word(a, b);
+  in_range = pos >= end ? 0u : (end - pos >= 32 ? 0xFFFFFFFFu : (uint32_t)((1ull << (end - pos)) - 1));
+}
+
+size_t extract64_smem_bytes(uint32_t partitions, bool scatter) {
+  return (scatter ? (size_t)partitions * 8 : 0) + (size_t)partitions * 4 + 64 * 4;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uint64_t> p) {
+  constexpr int NT = kExtractThreads;
+  extern __shared__ __align__(16) uint8_t sm[];
+  const uint32_t P = p.partitions;
+  unsigned long long* base = reinterpret_cast<unsigned long long*>(sm);
+  unsigned* hist = reinterpret_cast<unsigned*>(sm + (MODE == 1 ? (size_t)P * 8 : 0));
+  unsigned* scan_sm = hist + P;
+  for (uint32_t b = threadIdx.x; b < P; b += NT) hist[b] = 0;
+
+  const BlockDesc d = p.blocks[blockIdx.x];
+  const uint64_t e = d.end;
+  const uint64_t ts = d.start + (uint64_t)threadIdx.x * 64;
+  const bool chunk_ok = p.arena[d.chunk_start] == '@';  // src/count/parser.rs:27-29
+  const uint32_t k = p.k;
+  const uint64_t mask = (1ull << (2 * k)) - 1;
+  const bool canon = p.canonical != 0;
+  const uint32_t shift = p.shift;
+
+  Word32 wp, w0, w1;
+  uint32_t r0, r1, rp;
+  // ts - chunk_start is a multiple of 64: the word before is wholly inside
+  // the chunk, or the thread starts the chunk
+  const bool has_prev = ts > d.chunk_start && ts < e;
+  load_word(p.arena, has_prev ? ts - 32 : ts, has_prev ? ts : ts, wp, rp);
+  if (!has_prev) {
+    wp.nl = 0;
+    wp.vb = 0;
+  }
+  load_word(p.arena, ts, e, w0, r0);
+  load_word(p.arena, ts + 32, e, w1, r1);
+  w0.nl &= r0;
+  w1.nl &= r1;
+  unsigned nl_total;
+  const unsigned nl_before = block_exclusive_scan<NT, unsigned>(__popc(w0.nl) + __popc(w1.nl), scan_sm, &nl_total);
+  const unsigned long long line0 = p.block_nl_excl[blockIdx.x] - p.block_nl_excl[d.first_block];
+  unsigned ph = (unsigned)((line0 + nl_before) & 3ull);  // line phase at ts
+  unsigned php = (ph - (unsigned)__popc(wp.nl)) & 3u;     // at ts - 32
+  const uint32_t seqp = has_prev ? seq_mask(wp.nl, php) : 0u;
+  const uint32_t seq0 = seq_mask(w0.nl, ph) & r0;
+  const uint32_t seq1 = seq_mask(w1.nl, ph) & r1;
+  const uint32_t okp = chunk_ok ? (seqp & wp.vb) : 0u;
+  const uint32_t ok0 = chunk_ok ? (seq0 & w0.vb) : 0u;
+  const uint32_t ok1 = chunk_ok ? (seq1 & w1.vb) : 0u;
+  const uint32_t V0 = (uint32_t)(runs_of((uint64_t)okp | ((uint64_t)ok0 << 32), k) >> (33 - k));
+  const uint32_t V1 = (uint32_t)(runs_of((uint64_t)ok0 | ((uint64_t)ok1 << 32), k) >> (33 - k));
+  __syncthreads();  // hist zeroed
+
+  if (MODE == 0) {
+    unsigned long long kmers = __popc(V0) + __popc(V1);
+    const bool sampling = p.sample != nullptr && (d.flags & 2u);
+    auto emit = [&](uint64_t key, uint64_t pos) {
+      atomicAdd(&hist[bucket_of(key, shift)], 1u);
+      if (sampling && (mix64(pos) & p.sample_mask) == 0) {
+        const unsigned idx = atomicAdd(p.sample_count, 1u);
+        if (idx < p.sample_cap) p.sample[idx] = key;
+      }
+    };
+    word_kmers(V0, wp, w0, k, mask, canon, [&](uint64_t key, uint32_t b) { emit(key, ts + b); });
+    word_kmers(V1, w0, w1, k, mask, canon, [&](uint64_t key, uint32_t b) { emit(key, ts + 32 + b); });
+    // reads = starts of non-empty sequence-line runs; bases = sequence-line bytes
+    unsigned long long reads = 0, bases = 0;
+    if (chunk_ok) {
+      bases = __popc(seq0) + __popc(seq1);
+      reads = __popc(seq0 & ~((seq0 << 1) | (seqp >> 31))) + __popc(seq1 & ~((seq1 << 1) | (seq0 >> 31)));
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < P; b += NT)
+      if (hist[b]) atomicAdd(&p.bucket_count[b], (unsigned long long)hist[b]);
+    for (int o2 = 16; o2; o2 >>= 1) {
+      kmers += __shfl_xor_sync(0xffffffffu, kmers, o2);
+      reads += __shfl_xor_sync(0xffffffffu, reads, o2);
+      bases += __shfl_xor_sync(0xffffffffu, bases, o2);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (kmers) atomicAdd(&p.totals->kmers, kmers);
+      if (reads) atomicAdd(&p.totals->reads, reads);
+      if (bases) atomicAdd(&p.totals->bases, bases);
+    }
+  } else {
+    auto count = [&](uint64_t key, uint32_t) { atomicAdd(&hist[bucket_of(key, shift)], 1u); };
+    word_kmers(V0, wp, w0, k, mask, canon, count);
+    word_kmers(V1, w0, w1, k, mask, canon, count);
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < P; b += NT) {
+      const unsigned h = hist[b];
+      unsigned long long r = 0;
+      if (h) {
+        r = atomicAdd(&p.bucket_fill[b], (unsigned long long)h);
+        if (r + h > p.bucket_count[b]) {
+          dev_fail(p.status, KITE_DEV_REGION_OVERFLOW, b, (unsigned)r, h);
+          r = ~0ull;
+        }
+      }
+      base[b] = r;
+      hist[b] = 0;
+    }
+    __syncthreads();
+    auto write = [&](uint64_t key, uint32_t) {
+      const uint32_t b = bucket_of(key, shift);
+      const unsigned slot = atomicAdd(&hist[b], 1u);
+      const unsigned long long r = base[b];
+      if (r != ~0ull) p.keys_out[p.bucket_off[b] + r + slot] = key;
+    };
+    word_kmers(V0, wp, w0, k, mask, canon, write);
+    word_kmers(V1, w0, w1, k, mask, canon, write);
+  }
+}
+
 template <class T>
 void launch_extract_hist(const ExtractParams<T>& p, uint32_t nblocks, cudaStream_t s) {
   const size_t smem = extract_smem_bytes(sizeof(T), p.blk_bytes, p.partitions, false);
-  cudaFuncSetAttribute(k_extract<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (nblocks) k_extract<T, 0><<<nblocks, kExtractThreads, smem, s>>>(p);
+  if constexpr (sizeof(T) == 8) {
+    cudaFuncSetAttribute(k_extract64<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nblocks)
+      k_extract64<0><<<nblocks, kExtractThreads, smem, s>>>(reinterpret_cast<const ExtractParams<uint64_t>&>(p));
+  } else {
+    cudaFuncSetAttribute(k_extract<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nblocks) k_extract<T, 0><<<nblocks, kExtractThreads, smem, s>>>(p);
+  }
 }
 template <class T>
 void launch_extract_scatter(const ExtractParams<T>& p, uint32_t nblocks, cudaStream_t s) {
   const size_t smem = extract_smem_bytes(sizeof(T), p.blk_bytes, p.partitions, true);
-  cudaFuncSetAttribute(k_extract<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (nblocks) k_extract<T, 1><<<nblocks, kExtractThreads, smem, s>>>(p);
+  if constexpr (sizeof(T) == 8) {
+    cudaFuncSetAttribute(k_extract64<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nblocks)
+      k_extract64<1><<<nblocks, kExtractThreads, smem, s>>>(reinterpret_cast<const ExtractParams<uint64_t>&>(p));
+  } else {
+    cudaFuncSetAttribute(k_extract<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nblocks) k_extract<T, 1><<<nblocks, kExtractThreads, smem, s>>>(p);
+  }
 }
 template void launch_extract_hist<uint64_t>(const ExtractParams<uint64_t>&, uint32_t, cudaStream_t);
 template void launch_extract_hist<u128>(const ExtractParams<u128>&, uint32_t, cudaStream_t);

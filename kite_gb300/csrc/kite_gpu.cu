@@ -107,7 +107,7 @@ struct kite_gpu_ctx {
   DevBuf blocks, nl, scan_tmp, bucket_count, bucket_off, bucket_fill, totals, status;
   DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, splitters2, hist16;
   DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
-  DevBuf lvl_count, lvl_off, reg_off, reg_cnt;
+  DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats;
   HostBuf h_blocks, h_small, h_tiles, h_out;
   std::vector<cudaEvent_t> ev;  // stage events
 
@@ -505,8 +505,10 @@ int run_count(kite_gpu_ctx* ctx) {
   KCU(ctx->tile_out.ensure((size_t)ntiles * sizeof(TileOut<T>)));
 
   // ---- K4 tile sort + RLE ---------------------------------------------------
+  KCU(ctx->sort_stats.ensure(8));
+  KCU(cudaMemsetAsync(ctx->sort_stats.p, 0, 8, s));
   launch_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ntiles,
-                      ctx->tile_out.as<TileOut<T>>(), ctx->status.as<DevStatus>(), s);
+                      ctx->tile_out.as<TileOut<T>>(), ctx->sort_stats.as<unsigned long long>(), s);
   st.kernel_launches += 1 + (big.empty() ? 0 : 1) + 4;  // tile sort, big tiles, link, offsets, encode
   KCU(cudaGetLastError());
   KCU(cudaEventRecord(ctx->ev[5], s));
@@ -526,7 +528,10 @@ int run_count(kite_gpu_ctx* ctx) {
   launch_bucket_offsets(ctx->meta.as<BucketMeta>(), P, nullptr, s);
   ctx->res_meta.resize(P);
   KCU(cudaMemcpyAsync(ctx->res_meta.data(), ctx->meta.p, (size_t)P * sizeof(BucketMeta), cudaMemcpyDeviceToHost, s));
+  KCU(cudaMemcpyAsync(ctx->h_small.p, ctx->sort_stats.p, 8, cudaMemcpyDeviceToHost, s));
   rc = wait_stream(ctx, s);
+  if (rc) return rc;
+  std::memcpy(&st.sort_fallbacks, ctx->h_small.p, 8);
   if (rc) return rc;
   rc = check_status(ctx, "count");
   if (rc) return rc;
@@ -670,7 +675,7 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
                     &ctx->sample, &ctx->sample_count, &ctx->splitters, &ctx->splitters2, &ctx->hist16,
                     &ctx->tile_count, &ctx->tile_off, &ctx->tile_fill, &ctx->tiles, &ctx->big_ids,
                     &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out,
-                    &ctx->lvl_count, &ctx->lvl_off, &ctx->reg_off, &ctx->reg_cnt};
+                    &ctx->lvl_count, &ctx->lvl_off, &ctx->reg_off, &ctx->reg_cnt, &ctx->sort_stats};
   for (DevBuf* b : bufs) b->release();
   ctx->h_blocks.release();
   ctx->h_small.release();

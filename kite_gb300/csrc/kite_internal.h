@@ -118,9 +118,10 @@ constexpr int kTileThreads = 512;
 template <class T> __host__ __device__ constexpr int tile_items() { return sizeof(T) == 8 ? 16 : 8; }
 template <class T> __host__ __device__ constexpr uint32_t tile_capacity() { return (uint32_t)(kTileThreads * tile_items<T>()); }
 
+// `fallbacks` (device counter) counts tiles that took the LSD fallback.
 template <class T>
 void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
-                      DevStatus* st, cudaStream_t s);
+                      unsigned long long* fallbacks, cudaStream_t s);
 // Oversized tiles (more keys than tile_capacity): one CTA per tile, LSD
 // passes through global memory with `scratch` (>= largest tile keys).
 template <class T>

@@ -145,7 +145,7 @@ __device__ __forceinline__ unsigned bin_of(T key, T mn, int s) {
 template <class T>
 __global__ void __launch_bounds__(kTileThreads, 2)
     k_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, const TileDesc* __restrict__ tiles,
-                TileOut<T>* __restrict__ tout, DevStatus* st) {
+                TileOut<T>* __restrict__ tout, unsigned long long* fallbacks) {
   using L = BinSmem<T>;
   constexpr int NT = L::NT, NW = L::NW, ITEMS = L::ITEMS;
   extern __shared__ __align__(16) uint8_t sm[];
@@ -274,6 +274,7 @@ __global__ void __launch_bounds__(kTileThreads, 2)
   __syncthreads();
   if (misc[0]) {
     // a large bin of distinct keys: full LSD over the varying bits, in place
+    if (threadIdx.x == 0 && fallbacks) atomicAdd(fallbacks, 1ull);
     smem_radix_sort<T>(buf, n, varying_bits(mn, mx), bins, scan_sm, 0);
     for (unsigned p = threadIdx.x; p < n; p += NT) perm[p] = (unsigned short)p;
   } else {
@@ -328,20 +329,19 @@ __global__ void __launch_bounds__(kTileThreads, 2)
     o.rest_bytes = rest_total;
     tout[blockIdx.x] = o;
   }
-  (void)st;
 }
 
 template <class T>
 void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
-                      DevStatus* st, cudaStream_t s) {
+                      unsigned long long* fallbacks, cudaStream_t s) {
   const size_t smem = BinSmem<T>::total;
   cudaFuncSetAttribute(k_tile_sort<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(k_tile_sort<T>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  if (ntiles) k_tile_sort<T><<<ntiles, kTileThreads, smem, s>>>(keys, counts, tiles, out, st);
+  if (ntiles) k_tile_sort<T><<<ntiles, kTileThreads, smem, s>>>(keys, counts, tiles, out, fallbacks);
 }
 template void launch_tile_sort<uint64_t>(uint64_t*, uint32_t*, const TileDesc*, uint32_t, TileOut<uint64_t>*,
-                                         DevStatus*, cudaStream_t);
-template void launch_tile_sort<u128>(u128*, uint32_t*, const TileDesc*, uint32_t, TileOut<u128>*, DevStatus*,
+                                         unsigned long long*, cudaStream_t);
+template void launch_tile_sort<u128>(u128*, uint32_t*, const TileDesc*, uint32_t, TileOut<u128>*, unsigned long long*,
                                      cudaStream_t);
 
 // ---------------------------------------------------------------------------
