@@ -108,7 +108,11 @@ __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, u
 //  3. a bin holding more than one distinct key is ordered by counting: each
 //     key counts the smaller keys, and the equal keys placed before it, in its
 //     bin.  A bin of one repeated k-mer (the usual case) costs nothing.  A
-//     mixed bin larger than kMaxMixed sends the tile to a full LSD sort;
+//     mixed bin larger than kMaxMixed (typically a heavily repeated k-mer next
+//     to a few others) is sorted by one warp: it extracts the bin's distinct
+//     keys in ascending order with their counts and rewrites the bin's slots
+//     with them in order (equal keys are interchangeable).  Only a large bin
+//     with more than kMaxDistinct distinct keys sends the tile to LSD passes;
 //  4. run-length reduction over the sorted order: head flags by warp ballots,
 //     rows written to global memory over the tile's keys (u32 counts; a tile
 //     holds fewer than 2^32 keys, so no count saturates here).
@@ -117,6 +121,8 @@ __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, u
 // ---------------------------------------------------------------------------
 constexpr int kBinBits = 12, kBins = 1 << kBinBits;
 constexpr unsigned kMaxMixed = 256;
+constexpr unsigned kMaxLarge = 32;     // large mixed bins per tile (n / (kMaxMixed + 1) < 32)
+constexpr unsigned kMaxDistinct = 32;  // distinct keys a warp extracts from one large bin
 
 template <class T>
 struct BinSmem {
@@ -130,7 +136,7 @@ struct BinSmem {
   // fallback's per-warp digit histograms (256 * NW counters)
   static constexpr size_t bin_bytes = (size_t)kBins * 4 + 16;
   static constexpr size_t flag_bytes = kBins;
-  static constexpr size_t misc_bytes = 64 * 8 + 2 * NW * sizeof(T) + 16;
+  static constexpr size_t misc_bytes = 64 * 8 + 2 * NW * sizeof(T) + 16 + kMaxLarge * 2;
   static constexpr size_t total = buf_bytes + perm_bytes + bin_bytes + flag_bytes + misc_bytes;
   static_assert((size_t)(CAP + 1) * 2 <= bin_bytes, "run heads must fit the bin area");
   static_assert((size_t)256 * NW * 4 <= bin_bytes, "LSD histograms must fit the bin area");
@@ -156,7 +162,8 @@ __global__ void __launch_bounds__(kTileThreads, 2)
   unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(flag + L::flag_bytes);
   unsigned* scan_sm = reinterpret_cast<unsigned*>(scan64);
   T* red = reinterpret_cast<T*>(scan64 + 64);
-  unsigned* misc = reinterpret_cast<unsigned*>(red + 2 * NW);
+  unsigned* misc = reinterpret_cast<unsigned*>(red + 2 * NW);  // [0] LSD fallback, [1] large bins
+  unsigned short* large = reinterpret_cast<unsigned short*>(misc + 4);
 
   const TileDesc td = tiles[blockIdx.x];
   const unsigned n = td.len;
@@ -201,7 +208,10 @@ __global__ void __launch_bounds__(kTileThreads, 2)
   // ---- 2. bin histogram, scan, index scatter ----
   for (int b = threadIdx.x; b < kBins; b += NT) bins[b] = 0;
   for (int b = threadIdx.x; b < kBins / 4; b += NT) reinterpret_cast<unsigned*>(flag)[b] = 0;
-  if (threadIdx.x == 0) misc[0] = 0;
+  if (threadIdx.x == 0) {
+    misc[0] = 0;
+    misc[1] = 0;
+  }
   __syncthreads();
   for (unsigned i = threadIdx.x; i < n; i += NT) atomicAdd(&bins[bin_of(buf[i], mn, s)], 1u);
   __syncthreads();
@@ -260,7 +270,11 @@ __global__ void __launch_bounds__(kTileThreads, 2)
     if (!flag[bb]) continue;
     const unsigned a = bb ? bins[bb - 1] : 0u, e = bins[bb];
     if (e - a > kMaxMixed) {
-      misc[0] = 1;
+      if (p == a) {  // the bin's first position registers it
+        const unsigned q = atomicAdd(&misc[1], 1u);
+        if (q < kMaxLarge) large[q] = (unsigned short)bb;
+        else misc[0] = 1;
+      }
       continue;
     }
     unsigned less = 0, eqb = 0;
@@ -270,6 +284,67 @@ __global__ void __launch_bounds__(kTileThreads, 2)
       eqb += (v == k0) & (j < p);
     }
     pend[r] = ((a + less + eqb) << 16) | idx;
+  }
+  __syncthreads();
+  {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned nlarge = misc[1] < kMaxLarge ? misc[1] : kMaxLarge;
+    for (unsigned li = wid; li < nlarge; li += NW) {
+      const unsigned bb = large[li];
+      const unsigned a = bb ? bins[bb - 1] : 0u, e = bins[bb];
+      T myv = T(0), cur = T(0);
+      unsigned myc = 0, U = 0;
+      bool have = false, overflow = false;
+      for (;;) {
+        // smallest key above `cur` in the bin, and its number of copies
+        T best = T(0);
+        unsigned cnt = 0;
+        for (unsigned j = a + lane; j < e; j += 32) {
+          const T v = buf[perm[j]];
+          if (have && !(cur < v)) continue;
+          if (cnt == 0 || v < best) {
+            best = v;
+            cnt = 1;
+          } else if (v == best) {
+            ++cnt;
+          }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+          const T ob = shfl_xor_key(best, o);
+          const unsigned oc = __shfl_xor_sync(0xffffffffu, cnt, o);
+          if (oc && (cnt == 0 || ob < best)) {
+            best = ob;
+            cnt = oc;
+          } else if (oc && ob == best) {
+            cnt += oc;
+          }
+        }
+        if (cnt == 0) break;
+        if (U == kMaxDistinct) {
+          overflow = true;
+          break;
+        }
+        if (lane == (int)U) {
+          myv = best;
+          myc = cnt;
+        }
+        ++U;
+        cur = best;
+        have = true;
+      }
+      if (overflow) {
+        if (lane == 0) misc[0] = 1;
+        continue;
+      }
+      unsigned off = a;
+      for (unsigned u = 0; u < U; ++u) {
+        const T v = shfl_key(myv, (int)u);
+        const unsigned c = __shfl_sync(0xffffffffu, myc, (int)u);
+        for (unsigned t = lane; t < c; t += 32) buf[perm[off + t]] = v;
+        off += c;
+      }
+    }
   }
   __syncthreads();
   if (misc[0]) {

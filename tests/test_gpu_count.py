@@ -79,18 +79,37 @@ def test_heavy_mixed_big_tile(gpu, orc):
     assert_parity(gpu, orc, fq, 31, False, 2)
 
 
+def _rec(s: bytes) -> bytes:
+    return b"@m\n" + s + b"\n+\n" + b"I" * len(s) + b"\n"
+
+
+def _kmer(v: int, k: int) -> bytes:
+    return bytes(b"ACGT"[(v >> (2 * (k - 1 - i))) & 3] for i in range(k))
+
+
 @pytest.mark.parametrize("copies", [100, 300])
 def test_mixed_bin(gpu, orc, copies):
     # Two distinct repeated keys that sit close together in one tile (k=21
     # forward keys 0 = A*21 and 2 = A*20+G share partition 0 of 2, and G*21
     # widens the tile's span so both fall in its first bin): 100 copies each
-    # are ordered by counting inside the bin, 300 each take the LSD fallback.
-    def rec(s):
-        return b"@m\n" + s + b"\n+\n" + b"I" * len(s) + b"\n"
-    fq = rec(b"A" * 21) * copies + rec(b"A" * 20 + b"G") * copies + rec(b"G" * 21)
+    # are ordered by counting inside the bin; 300 each make a large bin that
+    # one warp sorts by extracting its distinct keys.
+    fq = _rec(b"A" * 21) * copies + _rec(b"A" * 20 + b"G") * copies + _rec(b"G" * 21)
     rng = np.random.default_rng(11)
     fq += synth.reads_fixed(rng, synth.genome_iid(rng, 5000), 40, 60, 0.0)
-    assert_parity(gpu, orc, fq, 21, False, 2)
+    st = assert_parity(gpu, orc, fq, 21, False, 2)
+    assert st["sort_fallbacks"] == 0
+
+
+def test_large_bin_many_distinct(gpu, orc):
+    # 40 distinct small keys of partition 0 (of 2), 10 copies each, share the
+    # first bin of a tile widened by G*21: more distinct keys than one warp
+    # extracts, so the tile takes the LSD fallback.
+    from kite_build import bucket
+    vals = [v for v in range(400) if bucket(v, 2, False) == 0][:40]
+    fq = b"".join(_rec(_kmer(v, 21)) * 10 for v in vals) + _rec(b"G" * 21)
+    st = assert_parity(gpu, orc, fq, 21, False, 2)
+    assert st["sort_fallbacks"] >= 1
 
 
 def test_segments_flush(gpu, orc):
