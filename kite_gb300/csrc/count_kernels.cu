@@ -97,6 +97,65 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   return x;
 }
 
+// Per-block bucket counts: one row of the block x bucket count matrix when
+// the host provides it (no atomics), else global atomics.
+template <int NT, class T>
+__device__ __forceinline__ void flush_hist(const ExtractParams<T>& p, const unsigned* hist, uint32_t P) {
+  if (p.blk_counts) {
+    unsigned* row = p.blk_counts + (size_t)blockIdx.x * P;
+    for (uint32_t b = threadIdx.x; b < P; b += NT) row[b] = hist[b];
+  } else {
+    for (uint32_t b = threadIdx.x; b < P; b += NT)
+      if (hist[b]) atomicAdd(&p.bucket_count[b], (unsigned long long)hist[b]);
+  }
+}
+
+// Reads / bases / k-mers of the CTA: one atomic per total per CTA.
+// `red` holds 3 * NT / 32 values; ends with a barrier.
+template <int NT>
+__device__ __forceinline__ void flush_totals(CountTotals* tot, unsigned long long kmers, unsigned long long reads,
+                                             unsigned long long bases, unsigned long long* red) {
+  constexpr int NW = NT / 32;
+  for (int o2 = 16; o2; o2 >>= 1) {
+    kmers += __shfl_xor_sync(0xffffffffu, kmers, o2);
+    reads += __shfl_xor_sync(0xffffffffu, reads, o2);
+    bases += __shfl_xor_sync(0xffffffffu, bases, o2);
+  }
+  const int wid = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[wid] = kmers;
+    red[NW + wid] = reads;
+    red[2 * NW + wid] = bases;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    unsigned long long v = 0;
+    for (int w = 0; w < NW; ++w) v += red[threadIdx.x * NW + w];
+    if (v) atomicAdd(threadIdx.x == 0 ? &tot->kmers : threadIdx.x == 1 ? &tot->reads : &tot->bases, v);
+  }
+  __syncthreads();
+}
+
+// Write offsets of the CTA inside every bucket region: from the scanned
+// count matrix when there is one, else by global atomic reservation.
+// Leaves base[b] = offset (~0 after an overflow) and hist[] zeroed.
+template <int NT, class T>
+__device__ __forceinline__ void reserve_ranges(const ExtractParams<T>& p, unsigned* hist, unsigned long long* base,
+                                               uint32_t P) {
+  for (uint32_t b = threadIdx.x; b < P; b += NT) {
+    const unsigned h = hist[b];
+    unsigned long long r = 0;
+    if (p.blk_offs) r = p.blk_offs[(size_t)blockIdx.x * P + b];
+    else if (h) r = atomicAdd(&p.bucket_fill[b], (unsigned long long)h);
+    if (h && r + h > p.bucket_count[b]) {
+      dev_fail(p.status, KITE_DEV_REGION_OVERFLOW, b, (unsigned)r, h);
+      r = ~0ull;
+    }
+    base[b] = r;
+    hist[b] = 0;
+  }
+}
+
 __host__ __device__ __forceinline__ size_t padded_bytes(uint32_t blk_bytes) {
   const size_t pt = blk_bytes / kExtractThreads;
   const size_t segs = ((size_t)kHalo + blk_bytes + 16 + pt - 1) / pt;
@@ -110,7 +169,7 @@ size_t extract_smem_bytes(int key_bytes, uint32_t blk_bytes, uint32_t partitions
   size_t o = padded_bytes(blk_bytes);
   if (scatter) o += (size_t)partitions * 8;  // reservation base (u64)
   o += (size_t)partitions * 4;               // histogram / cursor
-  o += 34 * 4 + 256;                         // scan scratch + base table
+  o += 64 * 4 + 256;                         // scan / reduction scratch + base table
   return o;
 }
 
@@ -128,7 +187,7 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract(ExtractParams<T> p)
   unsigned* hist = reinterpret_cast<unsigned*>(sm + o);
   o += (size_t)P * 4;
   unsigned* scan_sm = reinterpret_cast<unsigned*>(sm + o);
-  o += 34 * 4;
+  o += 64 * 4;
   uint8_t* table = sm + o;
 
   const BlockDesc d = p.blocks[blockIdx.x];
@@ -198,36 +257,13 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract(ExtractParams<T> p)
       }
     }
     __syncthreads();
-    for (uint32_t b = threadIdx.x; b < P; b += NT)
-      if (hist[b]) atomicAdd(&p.bucket_count[b], (unsigned long long)hist[b]);
-    // warp-aggregated totals
-    for (int o2 = 16; o2; o2 >>= 1) {
-      kmers += __shfl_xor_sync(0xffffffffu, kmers, o2);
-      reads += __shfl_xor_sync(0xffffffffu, reads, o2);
-      bases += __shfl_xor_sync(0xffffffffu, bases, o2);
-    }
-    if ((threadIdx.x & 31) == 0) {
-      if (kmers) atomicAdd(&p.totals->kmers, kmers);
-      if (reads) atomicAdd(&p.totals->reads, reads);
-      if (bases) atomicAdd(&p.totals->bases, bases);
-    }
+    flush_hist<NT>(p, hist, P);
+    flush_totals<NT>(p.totals, kmers, reads, bases, reinterpret_cast<unsigned long long*>(scan_sm));
   } else {
     roll_range<T>(sb, pts, s, ws, ts, te, phase, chunk_ok, table, p.k, canon,
                   [&](T key, uint64_t) { atomicAdd(&hist[bucket_of(key, shift)], 1u); });
     __syncthreads();
-    for (uint32_t b = threadIdx.x; b < P; b += NT) {
-      const unsigned h = hist[b];
-      unsigned long long r = 0;
-      if (h) {
-        r = atomicAdd(&p.bucket_fill[b], (unsigned long long)h);
-        if (r + h > p.bucket_count[b]) {
-          dev_fail(p.status, KITE_DEV_REGION_OVERFLOW, b, (unsigned)r, h);
-          r = ~0ull;
-        }
-      }
-      base[b] = r;
-      hist[b] = 0;
-    }
+    reserve_ranges<NT>(p, hist, base, P);
     __syncthreads();
     roll_range<T>(sb, pts, s, ws, ts, te, phase, chunk_ok, table, p.k, canon, [&](T key, uint64_t) {
       const uint32_t b = bucket_of(key, shift);
@@ -413,36 +449,14 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
       reads = __popc(seq0 & ~((seq0 << 1) | (seqp >> 31))) + __popc(seq1 & ~((seq1 << 1) | (seq0 >> 31)));
     }
     __syncthreads();
-    for (uint32_t b = threadIdx.x; b < P; b += NT)
-      if (hist[b]) atomicAdd(&p.bucket_count[b], (unsigned long long)hist[b]);
-    for (int o2 = 16; o2; o2 >>= 1) {
-      kmers += __shfl_xor_sync(0xffffffffu, kmers, o2);
-      reads += __shfl_xor_sync(0xffffffffu, reads, o2);
-      bases += __shfl_xor_sync(0xffffffffu, bases, o2);
-    }
-    if ((threadIdx.x & 31) == 0) {
-      if (kmers) atomicAdd(&p.totals->kmers, kmers);
-      if (reads) atomicAdd(&p.totals->reads, reads);
-      if (bases) atomicAdd(&p.totals->bases, bases);
-    }
+    flush_hist<NT>(p, hist, P);
+    flush_totals<NT>(p.totals, kmers, reads, bases, reinterpret_cast<unsigned long long*>(scan_sm));
   } else {
     auto count = [&](uint64_t key, uint32_t) { atomicAdd(&hist[bucket_of(key, shift)], 1u); };
     word_kmers(V0, wp, w0, k, mask, canon, count);
     word_kmers(V1, w0, w1, k, mask, canon, count);
     __syncthreads();
-    for (uint32_t b = threadIdx.x; b < P; b += NT) {
-      const unsigned h = hist[b];
-      unsigned long long r = 0;
-      if (h) {
-        r = atomicAdd(&p.bucket_fill[b], (unsigned long long)h);
-        if (r + h > p.bucket_count[b]) {
-          dev_fail(p.status, KITE_DEV_REGION_OVERFLOW, b, (unsigned)r, h);
-          r = ~0ull;
-        }
-      }
-      base[b] = r;
-      hist[b] = 0;
-    }
+    reserve_ranges<NT>(p, hist, base, P);
     __syncthreads();
     auto write = [&](uint64_t key, uint32_t) {
       const uint32_t b = bucket_of(key, shift);

@@ -107,7 +107,7 @@ struct kite_gpu_ctx {
   DevBuf blocks, nl, scan_tmp, bucket_count, bucket_off, bucket_fill, totals, status;
   DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, splitters2, hist16;
   DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
-  DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats;
+  DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats, blk_mat, blk_gsum;
   HostBuf h_blocks, h_small, h_tiles, h_out;
   std::vector<cudaEvent_t> ev;  // stage events
 
@@ -275,8 +275,21 @@ int run_count(kite_gpu_ctx* ctx) {
   ep.sample_cap = sample_cap;
   ep.sample_mask = mask;
   ep.status = ctx->status.as<DevStatus>();
+  // per-block bucket counts in a blocks x buckets matrix (no contended
+  // atomics), scanned per bucket into each block's write offsets
+  const uint64_t groups = ((uint64_t)nblocks + 255) / 256;
+  const bool use_matrix = (uint64_t)nblocks * P * 4 <= (2ull << 30) && groups <= 65535;
+  if (use_matrix) {
+    KCU(ctx->blk_mat.ensure((size_t)nblocks * P * 4));
+    KCU(ctx->blk_gsum.ensure((size_t)groups * P * 8));
+    ep.blk_counts = ctx->blk_mat.as<unsigned>();
+  }
   launch_extract_hist<T>(ep, nblocks, s);
   st.kernel_launches += 1;
+  if (use_matrix)
+    st.kernel_launches += count_matrix_offsets(ctx->blk_mat.as<unsigned>(), nblocks, P,
+                                               ctx->blk_gsum.as<unsigned long long>(),
+                                               ctx->bucket_count.as<unsigned long long>(), s);
   KCU(cudaGetLastError());
   KCU(cudaEventRecord(ctx->ev[2], s));
 
@@ -325,6 +338,8 @@ int run_count(kite_gpu_ctx* ctx) {
   ep.bucket_off = ctx->bucket_off.as<unsigned long long>();
   ep.bucket_fill = ctx->bucket_fill.as<unsigned long long>();
   ep.keys_out = ctx->keys_a.as<T>();
+  ep.blk_counts = nullptr;
+  ep.blk_offs = (use_matrix && maxb < (1ull << 32)) ? ctx->blk_mat.as<unsigned>() : nullptr;
   launch_extract_scatter<T>(ep, nblocks, s);
   st.kernel_launches += 1;
   KCU(cudaGetLastError());
@@ -675,7 +690,8 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
                     &ctx->sample, &ctx->sample_count, &ctx->splitters, &ctx->splitters2, &ctx->hist16,
                     &ctx->tile_count, &ctx->tile_off, &ctx->tile_fill, &ctx->tiles, &ctx->big_ids,
                     &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out,
-                    &ctx->lvl_count, &ctx->lvl_off, &ctx->reg_off, &ctx->reg_cnt, &ctx->sort_stats};
+                    &ctx->lvl_count, &ctx->lvl_off, &ctx->reg_off, &ctx->reg_cnt, &ctx->sort_stats,
+                    &ctx->blk_mat, &ctx->blk_gsum};
   for (DevBuf* b : bufs) b->release();
   ctx->h_blocks.release();
   ctx->h_small.release();

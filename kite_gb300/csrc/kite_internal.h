@@ -56,6 +56,11 @@ struct ExtractParams {
   unsigned int* sample_count;
   uint32_t sample_cap;
   uint32_t sample_mask;              // keep positions whose mixed hash & mask == 0
+  // per-block bucket counts [blocks][partitions]: the histogram pass writes
+  // them (instead of atomics on bucket_count) and, scanned per bucket, they
+  // become each block's write offsets inside the bucket regions; null = atomics
+  unsigned* blk_counts;
+  const unsigned* blk_offs;
   // scatter pass
   const unsigned long long* bucket_off;  // [partitions] region start (key index)
   unsigned long long* bucket_fill;       // [partitions]
@@ -109,6 +114,12 @@ size_t scan_tmp_elems(size_t n);
 // Returns the number of kernels launched.
 int exclusive_scan_u64(const unsigned long long* in, unsigned long long* out, size_t n,
                        unsigned long long* tmp, cudaStream_t s);
+// Column sums / offsets of a rows x cols u32 count matrix (row-major):
+// after count_matrix_offsets, m[r][c] = sum of m[0..r)[c] (in place) and
+// col_total[c] = the column sum.  `gsum` needs ceil(rows/256)*cols u64.
+// Column totals must stay below 2^32.  Returns the number of launches.
+int count_matrix_offsets(unsigned* m, uint32_t rows, uint32_t cols, unsigned long long* gsum,
+                         unsigned long long* col_total, cudaStream_t s);
 // Waits for the work queued on s, polling with a deadline: 0 ok, -1 CUDA
 // error, -3 timeout.
 int bounded_sync(cudaStream_t s, uint32_t timeout_ms);

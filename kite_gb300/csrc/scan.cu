@@ -48,6 +48,61 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tile(const unsigned long 
   }
 }
 
+// ---- column offsets of a row-major u32 count matrix (rows = blocks) ----
+static constexpr uint32_t kColRows = 256;  // rows per group
+
+// Column sums of each group of kColRows rows.
+__global__ void __launch_bounds__(256) k_col_group_sums(const unsigned* __restrict__ m, uint32_t rows, uint32_t cols,
+                                                        unsigned long long* __restrict__ gsum) {
+  const uint32_t g = blockIdx.y;
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  const uint32_t r0 = g * kColRows, r1 = min(rows, r0 + kColRows);
+  unsigned long long acc = 0;
+  for (uint32_t r = r0; r < r1; ++r) acc += m[(size_t)r * cols + c];
+  gsum[(size_t)g * cols + c] = acc;
+}
+
+// Exclusive scan of the group sums down each column; column totals.
+__global__ void __launch_bounds__(256) k_col_group_scan(unsigned long long* __restrict__ gsum, uint32_t groups,
+                                                        uint32_t cols, unsigned long long* __restrict__ total) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  unsigned long long acc = 0;
+  for (uint32_t g = 0; g < groups; ++g) {
+    const unsigned long long v = gsum[(size_t)g * cols + c];
+    gsum[(size_t)g * cols + c] = acc;
+    acc += v;
+  }
+  total[c] = acc;
+}
+
+// Rows of each group turned into running column offsets, in place.
+__global__ void __launch_bounds__(256) k_col_offsets(unsigned* __restrict__ m, uint32_t rows, uint32_t cols,
+                                                     const unsigned long long* __restrict__ gsum) {
+  const uint32_t g = blockIdx.y;
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  const uint32_t r0 = g * kColRows, r1 = min(rows, r0 + kColRows);
+  unsigned acc = (unsigned)gsum[(size_t)g * cols + c];
+  for (uint32_t r = r0; r < r1; ++r) {
+    const unsigned v = m[(size_t)r * cols + c];
+    m[(size_t)r * cols + c] = acc;
+    acc += v;
+  }
+}
+
+int count_matrix_offsets(unsigned* m, uint32_t rows, uint32_t cols, unsigned long long* gsum,
+                         unsigned long long* col_total, cudaStream_t s) {
+  if (rows == 0 || cols == 0) return 0;
+  const uint32_t groups = (rows + kColRows - 1) / kColRows;
+  const dim3 grid((cols + 255) / 256, groups);
+  k_col_group_sums<<<grid, 256, 0, s>>>(m, rows, cols, gsum);
+  k_col_group_scan<<<(cols + 255) / 256, 256, 0, s>>>(gsum, groups, cols, col_total);
+  k_col_offsets<<<grid, 256, 0, s>>>(m, rows, cols, gsum);
+  return 3;
+}
+
 size_t scan_tmp_elems(size_t n) {
   size_t tiles = (n + kScanTile - 1) / kScanTile;
   if (tiles <= 1) return 1;
