@@ -9,6 +9,8 @@
 //   KmerWord::to_bucket      src/count/kmer.rs:67-71, :111-116
 //   CountWorker::push_kmer   src/count/worker.rs:164-175 (replaced by a two-pass
 //                            histogram + reservation scatter into bucket regions)
+#include <cstdlib>
+
 #include "kite_internal.h"
 
 namespace kite {
@@ -608,30 +610,30 @@ __global__ void __launch_bounds__(kSplitThreads) k_split_hist(TileSplitParams<T>
 }
 
 // Scatter of one part, a batch of BATCH keys at a time: the batch is ranked on
-// chip by digit (stable warp-match ranking), staged in digit order, and each
-// digit's run is written to its destination with consecutive threads on
-// consecutive addresses, so global writes go out as whole sectors.
-template <class T>
+// chip by digit (stable warp-match ranking over RADIX >= D digits), staged in
+// digit order, and each digit's run is written to its destination with
+// consecutive threads on consecutive addresses, so global writes go out as
+// whole sectors.
+template <class T, int NT_, int IT_, int RADIX_>
 struct ScatterSmem {
-  static constexpr int NT = kSplitThreads, NW = NT / 32;
-  static constexpr int IT = sizeof(T) == 8 ? 8 : 4;
+  static constexpr int NT = NT_, NW = NT / 32, IT = IT_, RADIX = RADIX_;
   static constexpr int BATCH = NT * IT;
   static constexpr size_t o_stage = 0;
   static constexpr size_t o_dig = o_stage + (size_t)BATCH * sizeof(T);
-  static constexpr size_t o_whist = o_dig + (size_t)BATCH;
-  static constexpr size_t o_cur = o_whist + (size_t)kMaxDigits * NW * 4;
+  static constexpr size_t o_whist = (o_dig + (size_t)BATCH + 15) & ~(size_t)15;
+  static constexpr size_t o_cur = o_whist + (size_t)RADIX * NW * 4;
   static constexpr size_t o_dtot = o_cur + (size_t)kMaxDigits * 8;
-  static constexpr size_t o_dstart = o_dtot + (size_t)kMaxDigits * 4;
-  static constexpr size_t o_spl = o_dstart + (size_t)kMaxDigits * 4;
+  static constexpr size_t o_dstart = o_dtot + (size_t)RADIX * 4;
+  static constexpr size_t o_spl = o_dstart + (size_t)RADIX * 4;
   static constexpr size_t o_lut = o_spl + (size_t)kMaxDigits * sizeof(T);
   static constexpr size_t o_scan = o_lut + kLutBytes;
   static constexpr size_t total = o_scan + 64 * 4;
 };
 
-template <class T>
-__global__ void __launch_bounds__(kSplitThreads, 2) k_split_scatter(TileSplitParams<T> p) {
-  using L = ScatterSmem<T>;
-  constexpr int NT = L::NT, IT = L::IT, BATCH = L::BATCH;
+template <class T, int NT, int IT, int RADIX>
+__global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k_split_scatter(TileSplitParams<T> p) {
+  using L = ScatterSmem<T, NT, IT, RADIX>;
+  constexpr int BATCH = L::BATCH;
   extern __shared__ __align__(16) uint8_t sm[];
   T* stage = reinterpret_cast<T*>(sm + L::o_stage);
   uint8_t* dig8 = sm + L::o_dig;
@@ -665,7 +667,7 @@ __global__ void __launch_bounds__(kSplitThreads, 2) k_split_scatter(TileSplitPar
     }
 #pragma unroll
     for (int q = 0; q < IT; ++q) dg[q] = valid[q] ? digit_of_key(spl, lut, lo, sh, key[q]) : 0u;
-    block_rank<NT, IT, (int)kMaxDigits>(dg, valid, dest, whist, scan_sm, dtot, dstart);
+    block_rank<NT, IT, RADIX>(dg, valid, dest, whist, scan_sm, dtot, dstart);
 #pragma unroll
     for (int q = 0; q < IT; ++q)
       if (valid[q]) {
@@ -716,11 +718,34 @@ void launch_split_hist(const TileSplitParams<T>& p, cudaStream_t s) {
   if (p.R * p.G) k_split_hist<T><<<p.R * p.G, kSplitThreads, 0, s>>>(p);
 }
 
+template <class T, int NT, int IT, int RADIX>
+static void scatter_with(const TileSplitParams<T>& p, cudaStream_t s) {
+  const size_t smem = ScatterSmem<T, NT, IT, RADIX>::total;
+  cudaFuncSetAttribute(k_split_scatter<T, NT, IT, RADIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (p.R * p.G) k_split_scatter<T, NT, IT, RADIX><<<p.R * p.G, NT, smem, s>>>(p);
+}
+
+template <class T, int NT, int IT>
+static void scatter_shape(const TileSplitParams<T>& p, cudaStream_t s) {
+  if (p.D <= 16) scatter_with<T, NT, IT, 16>(p, s);
+  else scatter_with<T, NT, IT, 256>(p, s);
+}
+
+// Launch shape of the scatter (threads x keys per thread); KITE_SCATTER_SHAPE
+// = 0..3 overrides it for tuning.
 template <class T>
 void launch_split_scatter(const TileSplitParams<T>& p, cudaStream_t s) {
-  const size_t smem = ScatterSmem<T>::total;
-  cudaFuncSetAttribute(k_split_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (p.R * p.G) k_split_scatter<T><<<p.R * p.G, kSplitThreads, smem, s>>>(p);
+  static const int shape = [] {
+    const char* e = getenv("KITE_SCATTER_SHAPE");
+    return e ? atoi(e) : 0;
+  }();
+  constexpr int W = sizeof(T) == 8 ? 1 : 2;  // u128 keys: half the keys per thread
+  switch (shape) {
+    case 1: scatter_shape<T, 256, 16 / W>(p, s); break;
+    case 2: scatter_shape<T, 512, 8 / W>(p, s); break;
+    case 3: scatter_shape<T, 512, 16 / W>(p, s); break;
+    default: scatter_shape<T, 256, 8 / W>(p, s); break;
+  }
 }
 
 void launch_make_tiles(const unsigned long long* off, uint32_t ntiles, uint32_t S, uint32_t G,

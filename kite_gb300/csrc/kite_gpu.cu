@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -346,7 +347,13 @@ int run_count(kite_gpu_ctx* ctx) {
   KCU(cudaEventRecord(ctx->ev[3], s));
 
   // ---- K3b tile split -----------------------------------------------------
-  const double fill = 0.5;  // target mean tile load as a fraction of capacity
+  // target mean tile load as a fraction of on-chip capacity; KITE_TILE_FILL
+  // overrides it for tuning
+  static const double fill = [] {
+    const char* e = getenv("KITE_TILE_FILL");
+    const double v = e ? atof(e) : 0.0;
+    return v > 0.05 && v <= 4.0 ? v : 1.0;
+  }();
   uint32_t S = 1;
   while ((double)maxb / S > fill * CAP && S < 4096) S <<= 1;
   st.tiles_per_bucket = S;
@@ -492,8 +499,13 @@ int run_count(kite_gpu_ctx* ctx) {
   std::vector<uint32_t> big;
   std::vector<uint64_t> range(S, 0);
   uint64_t tmax = 0, tsum = 0, tne = 0;
+  size_t nlarge = 0;  // big[0 .. nlarge): on chip at twice the capacity; the rest: global memory
   for (uint32_t t = 0; t < ntiles; ++t) {
-    if (ht[t].len > CAP) big.push_back(t);
+    if (ht[t].len > CAP && ht[t].len <= 2 * CAP) big.push_back(t);
+  }
+  nlarge = big.size();
+  for (uint32_t t = 0; t < ntiles; ++t) {
+    if (ht[t].len > 2 * CAP) big.push_back(t);
     range[t % S] += ht[t].len;
     if (ht[t].len) {
       tmax = std::max<uint64_t>(tmax, ht[t].len);
@@ -524,11 +536,15 @@ int run_count(kite_gpu_ctx* ctx) {
   KCU(cudaMemsetAsync(ctx->sort_stats.p, 0, 8, s));
   launch_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ntiles,
                       ctx->tile_out.as<TileOut<T>>(), ctx->sort_stats.as<unsigned long long>(), s);
-  st.kernel_launches += 1 + (big.empty() ? 0 : 1) + 4;  // tile sort, big tiles, link, offsets, encode
+  const size_t nhuge = big.size() - nlarge;
+  st.kernel_launches += 1 + (nlarge ? 1 : 0) + (nhuge ? 1 : 0) + 4;  // sorts, link, offsets, encode
   KCU(cudaGetLastError());
   KCU(cudaEventRecord(ctx->ev[5], s));
+  launch_tile_sort_large<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ctx->big_ids.as<uint32_t>(),
+                            (uint32_t)nlarge, ctx->tile_out.as<TileOut<T>>(),
+                            ctx->sort_stats.as<unsigned long long>(), s);
   launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(),
-                          ctx->big_ids.as<uint32_t>(), (uint32_t)big.size(), ctx->tile_out.as<TileOut<T>>(),
+                          ctx->big_ids.as<uint32_t>() + nlarge, (uint32_t)nhuge, ctx->tile_out.as<TileOut<T>>(),
                           ctx->status.as<DevStatus>(), s);
   KCU(cudaGetLastError());
   KCU(cudaEventRecord(ctx->ev[6], s));

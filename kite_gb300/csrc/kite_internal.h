@@ -133,7 +133,12 @@ template <class T> __host__ __device__ constexpr uint32_t tile_capacity() { retu
 template <class T>
 void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
                       unsigned long long* fallbacks, cudaStream_t s);
-// Oversized tiles (more keys than tile_capacity): one CTA per tile, LSD
+// Tiles of tile_capacity < len <= 2 * tile_capacity, listed in ids: the same
+// on-chip sort with twice the shared memory (one CTA per SM).
+template <class T>
+void launch_tile_sort_large(T* keys, uint32_t* counts, const TileDesc* tiles, const uint32_t* ids, uint32_t nids,
+                            TileOut<T>* out, unsigned long long* fallbacks, cudaStream_t s);
+// Oversized tiles (more keys than 2 * tile_capacity): one CTA per tile, LSD
 // passes through global memory with `scratch` (>= largest tile keys).
 template <class T>
 void launch_big_tile_sort(T* keys, uint32_t* counts, T* scratch, const TileDesc* tiles, const uint32_t* big_ids,

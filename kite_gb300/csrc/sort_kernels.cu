@@ -72,10 +72,10 @@ struct TileSmem {
 
 // Stable LSD passes over bits [lo_bit, nbits) of the n keys in buf (shared
 // memory), 8-bit digits.
-template <class T>
+template <class T, int ITEMS = tile_items<T>()>
 __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, unsigned* warp_hist,
                                                 unsigned* scan_sm, int lo_bit = 0) {
-  constexpr int NT = kTileThreads, ITEMS = tile_items<T>();
+  constexpr int NT = kTileThreads;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   // spread the n keys over every warp: `items` rounds of 32 per warp
   const int items = (int)((n + NT - 1) / NT);
@@ -121,22 +121,25 @@ __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, u
 // ---------------------------------------------------------------------------
 constexpr int kBinBits = 12, kBins = 1 << kBinBits;
 constexpr unsigned kMaxMixed = 256;
-constexpr unsigned kMaxLarge = 32;     // large mixed bins per tile (n / (kMaxMixed + 1) < 32)
 constexpr unsigned kMaxDistinct = 32;  // distinct keys a warp extracts from one large bin
 
-template <class T>
+// MULT = 1: the regular tile (8192 u64 / 4096 u128 keys, two CTAs per SM);
+// MULT = 2: twice that for the few oversized tiles (one CTA per SM).
+template <class T, int MULT>
 struct BinSmem {
   static constexpr int NT = kTileThreads;
-  static constexpr int ITEMS = tile_items<T>();
-  static constexpr int CAP = NT * ITEMS;  // 8192 u64 / 4096 u128 keys
+  static constexpr int ITEMS = tile_items<T>() * MULT;
+  static constexpr int CAP = NT * ITEMS;
   static constexpr int NW = NT / 32;
+  static constexpr unsigned MAXLARGE = CAP / (kMaxMixed + 1) + 1;  // large mixed bins per tile
   static constexpr size_t buf_bytes = (size_t)CAP * sizeof(T);
   static constexpr size_t perm_bytes = (size_t)CAP * 2;
   // bin counters; later the u16 run heads (CAP + 1 entries), or the LSD
   // fallback's per-warp digit histograms (256 * NW counters)
-  static constexpr size_t bin_bytes = (size_t)kBins * 4 + 16;
+  static constexpr size_t head_need = ((size_t)(CAP + 1) * 2 + 15) & ~(size_t)15;
+  static constexpr size_t bin_bytes = ((size_t)kBins * 4 > head_need ? (size_t)kBins * 4 : head_need) + 16;
   static constexpr size_t flag_bytes = kBins;
-  static constexpr size_t misc_bytes = 64 * 8 + 2 * NW * sizeof(T) + 16 + kMaxLarge * 2;
+  static constexpr size_t misc_bytes = 64 * 8 + 2 * NW * sizeof(T) + 16 + MAXLARGE * 2;
   static constexpr size_t total = buf_bytes + perm_bytes + bin_bytes + flag_bytes + misc_bytes;
   static_assert((size_t)(CAP + 1) * 2 <= bin_bytes, "run heads must fit the bin area");
   static_assert((size_t)256 * NW * 4 <= bin_bytes, "LSD histograms must fit the bin area");
@@ -148,11 +151,12 @@ __device__ __forceinline__ unsigned bin_of(T key, T mn, int s) {
   return (unsigned)(uint64_t)((key - mn) >> s);
 }
 
-template <class T>
-__global__ void __launch_bounds__(kTileThreads, 2)
+template <class T, int MULT>
+__global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
     k_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, const TileDesc* __restrict__ tiles,
-                TileOut<T>* __restrict__ tout, unsigned long long* fallbacks) {
-  using L = BinSmem<T>;
+                const uint32_t* __restrict__ ids, TileOut<T>* __restrict__ tout, unsigned long long* fallbacks) {
+  using L = BinSmem<T, MULT>;
+  constexpr unsigned kMaxLarge = L::MAXLARGE;
   constexpr int NT = L::NT, NW = L::NW, ITEMS = L::ITEMS;
   extern __shared__ __align__(16) uint8_t sm[];
   T* buf = reinterpret_cast<T*>(sm);
@@ -165,9 +169,10 @@ __global__ void __launch_bounds__(kTileThreads, 2)
   unsigned* misc = reinterpret_cast<unsigned*>(red + 2 * NW);  // [0] LSD fallback, [1] large bins
   unsigned short* large = reinterpret_cast<unsigned short*>(misc + 4);
 
-  const TileDesc td = tiles[blockIdx.x];
+  const uint32_t tid = ids ? ids[blockIdx.x] : blockIdx.x;
+  const TileDesc td = tiles[tid];
   const unsigned n = td.len;
-  if (n > (unsigned)L::CAP) return;  // oversized tiles take the global-memory path
+  if (n > (unsigned)L::CAP) return;  // oversized tiles take a larger path
   if (n == 0) {
     if (threadIdx.x == 0) {
       TileOut<T> o;
@@ -175,7 +180,7 @@ __global__ void __launch_bounds__(kTileThreads, 2)
       o.rows = 0;
       o.first_count = 0;
       o.rest_bytes = 0;
-      tout[blockIdx.x] = o;
+      tout[tid] = o;
     }
     return;
   }
@@ -198,7 +203,7 @@ __global__ void __launch_bounds__(kTileThreads, 2)
       o.rows = 1;
       o.first_count = n;
       o.rest_bytes = 0;
-      tout[blockIdx.x] = o;
+      tout[tid] = o;
     }
     return;
   }
@@ -350,7 +355,7 @@ __global__ void __launch_bounds__(kTileThreads, 2)
   if (misc[0]) {
     // a large bin of distinct keys: full LSD over the varying bits, in place
     if (threadIdx.x == 0 && fallbacks) atomicAdd(fallbacks, 1ull);
-    smem_radix_sort<T>(buf, n, varying_bits(mn, mx), bins, scan_sm, 0);
+    smem_radix_sort<T, ITEMS>(buf, n, varying_bits(mn, mx), bins, scan_sm, 0);
     for (unsigned p = threadIdx.x; p < n; p += NT) perm[p] = (unsigned short)p;
   } else {
 #pragma unroll
@@ -402,22 +407,37 @@ __global__ void __launch_bounds__(kTileThreads, 2)
     o.last_key = buf[perm[head[U - 1]]];
     o.rows = U;
     o.rest_bytes = rest_total;
-    tout[blockIdx.x] = o;
+    tout[tid] = o;
   }
+}
+
+template <class T, int MULT>
+static void tile_sort_with(T* keys, uint32_t* counts, const TileDesc* tiles, const uint32_t* ids, uint32_t n,
+                           TileOut<T>* out, unsigned long long* fallbacks, cudaStream_t s) {
+  const size_t smem = BinSmem<T, MULT>::total;
+  cudaFuncSetAttribute(k_tile_sort<T, MULT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_tile_sort<T, MULT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (n) k_tile_sort<T, MULT><<<n, kTileThreads, smem, s>>>(keys, counts, tiles, ids, out, fallbacks);
 }
 
 template <class T>
 void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
                       unsigned long long* fallbacks, cudaStream_t s) {
-  const size_t smem = BinSmem<T>::total;
-  cudaFuncSetAttribute(k_tile_sort<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaFuncSetAttribute(k_tile_sort<T>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  if (ntiles) k_tile_sort<T><<<ntiles, kTileThreads, smem, s>>>(keys, counts, tiles, out, fallbacks);
+  tile_sort_with<T, 1>(keys, counts, tiles, nullptr, ntiles, out, fallbacks, s);
+}
+template <class T>
+void launch_tile_sort_large(T* keys, uint32_t* counts, const TileDesc* tiles, const uint32_t* ids, uint32_t nids,
+                            TileOut<T>* out, unsigned long long* fallbacks, cudaStream_t s) {
+  tile_sort_with<T, 2>(keys, counts, tiles, ids, nids, out, fallbacks, s);
 }
 template void launch_tile_sort<uint64_t>(uint64_t*, uint32_t*, const TileDesc*, uint32_t, TileOut<uint64_t>*,
                                          unsigned long long*, cudaStream_t);
 template void launch_tile_sort<u128>(u128*, uint32_t*, const TileDesc*, uint32_t, TileOut<u128>*, unsigned long long*,
                                      cudaStream_t);
+template void launch_tile_sort_large<uint64_t>(uint64_t*, uint32_t*, const TileDesc*, const uint32_t*, uint32_t,
+                                               TileOut<uint64_t>*, unsigned long long*, cudaStream_t);
+template void launch_tile_sort_large<u128>(u128*, uint32_t*, const TileDesc*, const uint32_t*, uint32_t,
+                                           TileOut<u128>*, unsigned long long*, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Oversized tiles: one CTA, LSD passes through global memory.  Each pass

@@ -101,6 +101,15 @@ def test_mixed_bin(gpu, orc, copies):
     assert st["sort_fallbacks"] == 0
 
 
+def test_large_tile_on_chip(gpu, orc):
+    # 12,001 keys in partition 0: the tile holding the two repeated keys is
+    # over the regular on-chip capacity (8192) but within twice it, so it
+    # takes the double-capacity on-chip sort.
+    fq = _rec(b"A" * 21) * 6000 + _rec(b"A" * 20 + b"G") * 6000 + _rec(b"G" * 21)
+    st = assert_parity(gpu, orc, fq, 21, False, 2)
+    assert st["big_tiles"] >= 1
+
+
 def test_large_bin_many_distinct(gpu, orc):
     # 40 distinct small keys of partition 0 (of 2), 10 copies each, share the
     # first bin of a tile widened by G*21: more distinct keys than one warp
