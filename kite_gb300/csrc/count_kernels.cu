@@ -381,7 +381,7 @@ __device__ __forceinline__ void load_word(const uint8_t* arena, uint64_t pos, ui
 }
 
 size_t extract64_smem_bytes(uint32_t partitions, bool scatter) {
-  return (scatter ? (size_t)partitions * 8 : 0) + (size_t)partitions * 4 + 64 * 4;
+  return (scatter ? (size_t)partitions * 8 : 0) + (size_t)partitions * 4 + 96 * 4;
 }
 
 template <int MODE>
@@ -435,8 +435,25 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
   if (MODE == 0) {
     unsigned long long kmers = __popc(V0) + __popc(V1);
     const bool sampling = p.sample != nullptr && (d.flags & 2u);
+    // staged keys: this thread's run inside the block's reserved range
+    uint64_t* out = nullptr;
+    if (p.keys_stage) {
+      unsigned tot;
+      const unsigned before = block_exclusive_scan<NT, unsigned>((unsigned)kmers, scan_sm, &tot);
+      unsigned long long* bb = reinterpret_cast<unsigned long long*>(scan_sm) + 40;
+      if (threadIdx.x == 0) {
+        unsigned long long at = tot ? atomicAdd(p.stage_counter, (unsigned long long)tot) : 0ull;
+        if (at + tot > p.stage_cap) at = ~0ull;  // over capacity: the host takes the other scatter path
+        *bb = at;
+        p.blk_keys[2 * (size_t)blockIdx.x] = at;
+        p.blk_keys[2 * (size_t)blockIdx.x + 1] = tot;
+      }
+      __syncthreads();
+      if (*bb != ~0ull) out = p.keys_stage + *bb + before;
+    }
     auto emit = [&](uint64_t key, uint64_t pos) {
       atomicAdd(&hist[bucket_of(key, shift)], 1u);
+      if (out) *out++ = key;
       if (sampling && (mix64(pos) & p.sample_mask) == 0) {
         const unsigned idx = atomicAdd(p.sample_count, 1u);
         if (idx < p.sample_cap) p.sample[idx] = key;
@@ -683,6 +700,82 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
     for (uint32_t d = threadIdx.x; d < D; d += NT) cur[d] += dtot[d];
     __syncthreads();
   }
+}
+
+// Bucket scatter of staged keys, one CTA per extraction block: batches of
+// BATCH keys ranked on chip by partition (stable warp-match ranking), staged in
+// partition order and written as runs at the block's offsets.
+constexpr int kBsThreads = 256, kBsItems = 8, kBsBatch = kBsThreads * kBsItems;
+struct BsSmem {
+  static constexpr int NW = kBsThreads / 32;
+  static constexpr size_t o_stage = 0;
+  static constexpr size_t o_dig = o_stage + (size_t)kBsBatch * 8;
+  static constexpr size_t o_whist = (o_dig + (size_t)kBsBatch + 15) & ~(size_t)15;
+  static constexpr size_t o_cur = o_whist + (size_t)256 * NW * 4;
+  static constexpr size_t o_dtot = o_cur + (size_t)256 * 8;
+  static constexpr size_t o_dstart = o_dtot + (size_t)256 * 4;
+  static constexpr size_t o_scan = o_dstart + (size_t)256 * 4;
+  static constexpr size_t total = o_scan + 64 * 4;
+};
+
+__global__ void __launch_bounds__(kBsThreads, 4)
+    k_bucket_scatter(const uint64_t* __restrict__ keys_stage, const unsigned long long* __restrict__ blk_keys,
+                     const unsigned* __restrict__ blk_offs, const unsigned long long* __restrict__ bucket_off,
+                     uint32_t P, uint32_t shift, uint64_t* __restrict__ keys_out) {
+  using L = BsSmem;
+  constexpr int NT = kBsThreads, IT = kBsItems;
+  __shared__ __align__(16) uint8_t sm[L::total];
+  uint64_t* stage = reinterpret_cast<uint64_t*>(sm + L::o_stage);
+  uint8_t* dig8 = sm + L::o_dig;
+  unsigned* whist = reinterpret_cast<unsigned*>(sm + L::o_whist);
+  unsigned long long* cur = reinterpret_cast<unsigned long long*>(sm + L::o_cur);
+  unsigned* dtot = reinterpret_cast<unsigned*>(sm + L::o_dtot);
+  unsigned* dstart = reinterpret_cast<unsigned*>(sm + L::o_dstart);
+  unsigned* scan_sm = reinterpret_cast<unsigned*>(sm + L::o_scan);
+  const uint64_t a = blk_keys[2 * (size_t)blockIdx.x];
+  const uint64_t n = blk_keys[2 * (size_t)blockIdx.x + 1];
+  if (n == 0) return;
+  const unsigned* row = blk_offs + (size_t)blockIdx.x * P;
+  for (uint32_t b = threadIdx.x; b < P; b += NT) cur[b] = bucket_off[b] + row[b];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned pos0 = (unsigned)wid * 32u * IT + lane;
+  for (uint64_t c0 = 0; c0 < n; c0 += kBsBatch) {
+    const unsigned cn = (unsigned)((n - c0) < (uint64_t)kBsBatch ? (n - c0) : (uint64_t)kBsBatch);
+    uint64_t key[IT];
+    unsigned dg[IT], dest[IT];
+    bool valid[IT];
+#pragma unroll
+    for (int q = 0; q < IT; ++q) {
+      const unsigned pos = pos0 + q * 32u;
+      valid[q] = pos < cn;
+      key[q] = valid[q] ? keys_stage[a + c0 + pos] : 0ull;
+      dg[q] = valid[q] ? bucket_of(key[q], shift) : 0u;
+    }
+    block_rank<NT, IT, 256>(dg, valid, dest, whist, scan_sm, dtot, dstart);
+#pragma unroll
+    for (int q = 0; q < IT; ++q)
+      if (valid[q]) {
+        stage[dest[q]] = key[q];
+        dig8[dest[q]] = (uint8_t)dg[q];
+      }
+    __syncthreads();
+    for (unsigned i = threadIdx.x; i < cn; i += NT) {
+      const unsigned d = dig8[i];
+      keys_out[cur[d] + (i - dstart[d])] = stage[i];
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < P; b += NT) cur[b] += dtot[b];
+    __syncthreads();
+  }
+}
+
+void launch_bucket_scatter(const uint64_t* keys_stage, const unsigned long long* blk_keys, const unsigned* blk_offs,
+                           const unsigned long long* bucket_off, uint32_t partitions, uint32_t shift, uint32_t nblocks,
+                           uint64_t* keys_out, cudaStream_t s) {
+  if (nblocks)
+    k_bucket_scatter<<<nblocks, kBsThreads, 0, s>>>(keys_stage, blk_keys, blk_offs, bucket_off, partitions, shift,
+                                                    keys_out);
 }
 
 // Tile list from the scanned part offsets: tile t = (b, j) starts at

@@ -108,7 +108,7 @@ struct kite_gpu_ctx {
   DevBuf blocks, nl, scan_tmp, bucket_count, bucket_off, bucket_fill, totals, status;
   DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, splitters2, hist16;
   DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
-  DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats, blk_mat, blk_gsum;
+  DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats, blk_mat, blk_gsum, blk_keys, stage_ctr;
   HostBuf h_blocks, h_small, h_tiles, h_out;
   std::vector<cudaEvent_t> ev;  // stage events
 
@@ -285,6 +285,25 @@ int run_count(kite_gpu_ctx* ctx) {
     KCU(ctx->blk_gsum.ensure((size_t)groups * P * 8));
     ep.blk_counts = ctx->blk_mat.as<unsigned>();
   }
+  // u64 keys and at most 256 partitions: the histogram pass also stages every
+  // block's keys (capacity: half a key per FASTQ byte; more than that and the
+  // extraction scatter runs instead), then an on-chip ranked scatter moves
+  // them to the bucket regions
+  uint64_t fastq_bytes = 0;
+  for (const Chunk& ch : ctx->chunks) fastq_bytes += ch.len;
+  const bool stage_keys = sizeof(T) == 8 && use_matrix && P <= 256;
+  const uint64_t stage_cap = fastq_bytes / 2 + 1024;
+  if (stage_keys) {
+    const uint64_t cap = stage_cap;
+    KCU(ctx->keys_b.ensure(cap * sizeof(T)));
+    KCU(ctx->blk_keys.ensure((size_t)nblocks * 16));
+    KCU(ctx->stage_ctr.ensure(8));
+    KCU(cudaMemsetAsync(ctx->stage_ctr.p, 0, 8, s));
+    ep.keys_stage = ctx->keys_b.as<T>();
+    ep.stage_cap = cap;
+    ep.stage_counter = ctx->stage_ctr.as<unsigned long long>();
+    ep.blk_keys = ctx->blk_keys.as<unsigned long long>();
+  }
   launch_extract_hist<T>(ep, nblocks, s);
   st.kernel_launches += 1;
   if (use_matrix)
@@ -296,13 +315,17 @@ int run_count(kite_gpu_ctx* ctx) {
 
   // bring bucket counts, totals and the sample count to the host
   const size_t small_bytes = (size_t)P * 8 + sizeof(CountTotals) + 8;
-  KCU(ctx->h_small.ensure(small_bytes + (size_t)P * 8));
+  KCU(ctx->h_small.ensure(small_bytes + 8 + (size_t)P * 8));
   uint8_t* hs = ctx->h_small.as<uint8_t>();
   KCU(cudaMemcpyAsync(hs, ctx->bucket_count.p, (size_t)P * 8, cudaMemcpyDeviceToHost, s));
   KCU(cudaMemcpyAsync(hs + (size_t)P * 8, ctx->totals.p, sizeof(CountTotals), cudaMemcpyDeviceToHost, s));
   KCU(cudaMemcpyAsync(hs + (size_t)P * 8 + sizeof(CountTotals), ctx->sample_count.p, 4, cudaMemcpyDeviceToHost, s));
+  if (stage_keys)
+    KCU(cudaMemcpyAsync(hs + (size_t)P * 8 + sizeof(CountTotals) + 8, ctx->stage_ctr.p, 8, cudaMemcpyDeviceToHost, s));
   int rc = wait_stream(ctx, s);
   if (rc) return rc;
+  uint64_t staged = ~0ull;
+  if (stage_keys) std::memcpy(&staged, hs + (size_t)P * 8 + sizeof(CountTotals) + 8, 8);
   std::vector<uint64_t> bcount(P);
   std::memcpy(bcount.data(), hs, (size_t)P * 8);
   CountTotals tot;
@@ -341,7 +364,14 @@ int run_count(kite_gpu_ctx* ctx) {
   ep.keys_out = ctx->keys_a.as<T>();
   ep.blk_counts = nullptr;
   ep.blk_offs = (use_matrix && maxb < (1ull << 32)) ? ctx->blk_mat.as<unsigned>() : nullptr;
-  launch_extract_scatter<T>(ep, nblocks, s);
+  if (stage_keys && ep.blk_offs && staged == N && N <= stage_cap) {
+    launch_bucket_scatter(reinterpret_cast<const uint64_t*>(ctx->keys_b.p), ctx->blk_keys.as<unsigned long long>(),
+                          ep.blk_offs, ctx->bucket_off.as<unsigned long long>(), P, ep.shift, nblocks,
+                          reinterpret_cast<uint64_t*>(ctx->keys_a.p), s);
+  } else {
+    ep.keys_stage = nullptr;
+    launch_extract_scatter<T>(ep, nblocks, s);
+  }
   st.kernel_launches += 1;
   KCU(cudaGetLastError());
   KCU(cudaEventRecord(ctx->ev[3], s));
@@ -707,7 +737,7 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
                     &ctx->tile_count, &ctx->tile_off, &ctx->tile_fill, &ctx->tiles, &ctx->big_ids,
                     &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out,
                     &ctx->lvl_count, &ctx->lvl_off, &ctx->reg_off, &ctx->reg_cnt, &ctx->sort_stats,
-                    &ctx->blk_mat, &ctx->blk_gsum};
+                    &ctx->blk_mat, &ctx->blk_gsum, &ctx->blk_keys, &ctx->stage_ctr};
   for (DevBuf* b : bufs) b->release();
   ctx->h_blocks.release();
   ctx->h_small.release();

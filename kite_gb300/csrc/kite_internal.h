@@ -61,6 +61,13 @@ struct ExtractParams {
   // become each block's write offsets inside the bucket regions; null = atomics
   unsigned* blk_counts;
   const unsigned* blk_offs;
+  // histogram pass, optional: every block's keys, in block-local order, to
+  // keys_stage at a position reserved on stage_counter; blk_keys[2*b] = that
+  // position, blk_keys[2*b+1] = the block's key count (null = not written)
+  T* keys_stage;
+  unsigned long long stage_cap;          // keys keys_stage holds; a block past it writes nothing
+  unsigned long long* stage_counter;
+  unsigned long long* blk_keys;
   // scatter pass
   const unsigned long long* bucket_off;  // [partitions] region start (key index)
   unsigned long long* bucket_fill;       // [partitions]
@@ -97,6 +104,12 @@ template <class T>
 void launch_extract_hist(const ExtractParams<T>& p, uint32_t nblocks, cudaStream_t s);
 template <class T>
 void launch_extract_scatter(const ExtractParams<T>& p, uint32_t nblocks, cudaStream_t s);
+// Scatter of the staged keys of every block into the bucket regions
+// (partitions <= 256): keys of block b go to bucket_off[k] + blk_offs[b][k]
+// onwards, ranked on chip so that writes are coalesced.
+void launch_bucket_scatter(const uint64_t* keys_stage, const unsigned long long* blk_keys, const unsigned* blk_offs,
+                           const unsigned long long* bucket_off, uint32_t partitions, uint32_t shift, uint32_t nblocks,
+                           uint64_t* keys_out, cudaStream_t s);
 template <class T>
 void launch_split_hist(const TileSplitParams<T>& p, cudaStream_t s);
 template <class T>

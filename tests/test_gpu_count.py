@@ -121,6 +121,15 @@ def test_large_bin_many_distinct(gpu, orc):
     assert st["sort_fallbacks"] >= 1
 
 
+def test_dense_sequence_fallback(gpu, orc):
+    # sequence lines with empty quality lines: close to one k-mer per FASTQ
+    # byte, more than the staged-key capacity, so the extraction scatter runs
+    rng = np.random.default_rng(12)
+    seqs = [bytes(b"ACGT"[x] for x in rng.integers(0, 4, 2000)) for _ in range(50)]
+    fq = b"".join(b"@d\n" + q + b"\n+\n\n" for q in seqs)
+    assert_parity(gpu, orc, fq, 21, True, 16)
+
+
 def test_segments_flush(gpu, orc):
     # a small arena forces several segments: partitions then hold several
     # chunks; compare through dump TSV equality (counts summed across chunks)
