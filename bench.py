@@ -112,16 +112,19 @@ def peaks() -> tuple:
 
 
 def stage_bytes(st: dict, fastq_bytes: int) -> dict:
-    """Algorithmic bytes per stage for one step (w = 8-byte keys)."""
+    """Algorithmic bytes per stage for one step (w = 8-byte keys): the bytes
+    each stage must read and write at minimum, per the kernels that ran."""
     w = 8
     N = st["kmers"]
     d = st["rows"]
     E = st["payload_bytes"]
+    staged = st.get("staged_scatter", 0) == 1
+    levels = st.get("split_levels", 1)
     return {
         0: ("k_newline_count", fastq_bytes),
-        1: ("k_extract<hist>", fastq_bytes),
-        2: ("k_extract<scatter>", fastq_bytes + N * w),
-        3: ("k_tile_hist+k_tile_scatter", 3 * N * w),
+        1: ("k_extract<hist>", fastq_bytes + (N * w if staged else 0)),
+        2: ("k_bucket_scatter" if staged else "k_extract<scatter>", 2 * N * w if staged else fastq_bytes + N * w),
+        3: ("k_split_hist+k_split_scatter", 3 * N * w * levels),
         4: ("k_tile_sort", N * w + d * (w + 4)),
         5: ("k_big_tile_sort", 0),
         6: ("k_encode", d * (w + 4) + E),
@@ -302,11 +305,14 @@ def main():
     tr = ncu_traffic(name)
     traffic = None
     if tr and tr.get("dram_bytes_per_key") is not None:
-        traffic = tr["dram_bytes_per_key"] * kmers
+        # ncu DRAM bytes per k-mer from the committed 1M-read capture, scaled
+        # to this step's k-mers (the split's figure is per level)
+        traffic = tr["dram_bytes_per_key"] * kmers * (st.get("split_levels", 1) if tr.get("per_level") else 1)
     sort_ms = avg_ms[3] + avg_ms[4] + avg_ms[5]
     sort_bytes = stages[3][1] + stages[4][1]
     roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                "traffic_source": "profiles/count_kernels_1M_full.md (ncu, 1M reads) scaled per k-mer",
                 "algorithmic_bytes": algo_bytes, "kernel_ms": avg_ms[dom],
                 "sort_gbs": sort_bytes / (sort_ms / 1e3) / 1e9 if sort_ms > 0 else None,
                 "sort_frac": (sort_bytes / (sort_ms / 1e3) / 1e9) / peak if sort_ms > 0 else None,

@@ -100,6 +100,8 @@ typedef struct {
   double mlp_loss, mlp_pred_imbalance, hist_pred_imbalance; /* learned-splitter diagnostics */
   double range_imbalance;            /* max / mean keys per key range (summed over partitions) */
   uint64_t sort_fallbacks;           /* tiles whose on-chip sort fell back to LSD passes (a large bin of distinct keys) */
+  uint32_t split_levels;             /* key-range split passes over the keys (0, 1 or 2) */
+  uint32_t staged_scatter;           /* 1: keys staged by the histogram pass, then a ranked bucket scatter */
 } kite_gpu_stats;
 
 /* Merge input: one .kite file's partition table, with payloads in host memory

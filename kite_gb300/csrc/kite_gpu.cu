@@ -365,6 +365,7 @@ int run_count(kite_gpu_ctx* ctx) {
   ep.blk_counts = nullptr;
   ep.blk_offs = (use_matrix && maxb < (1ull << 32)) ? ctx->blk_mat.as<unsigned>() : nullptr;
   if (stage_keys && ep.blk_offs && staged == N && N <= stage_cap) {
+    st.staged_scatter = 1;
     launch_bucket_scatter(reinterpret_cast<const uint64_t*>(ctx->keys_b.p), ctx->blk_keys.as<unsigned long long>(),
                           ep.blk_offs, ctx->bucket_off.as<unsigned long long>(), P, ep.shift, nblocks,
                           reinterpret_cast<uint64_t*>(ctx->keys_a.p), s);
@@ -440,6 +441,7 @@ int run_count(kite_gpu_ctx* ctx) {
       return (uint32_t)std::min<uint64_t>(g, 64);
     };
     const uint32_t D2 = std::min<uint32_t>(S, 256), D1 = S / D2;
+    st.split_levels = D1 > 1 ? 2 : 1;
     const size_t nt = (size_t)P * S;
     TileSplitParams<T> tp{};
     tp.splitters = chosen;
