@@ -52,6 +52,20 @@ def gen_workload(n_reads: int, seed: int = 2):
     return data
 
 
+# --workload skewed: learned vs sampled splitters on skewed u128 keys: 20 Mbp
+# genome whose first 30% is an AT-rich Markov chain (P(A)=P(T)=0.4), the rest
+# uniform; 4M reads of 250 bp, 1% substitutions; k=63 canonical.
+SKEWED = {"k": 63, "reads": 4_000_000, "read_len": 250,
+          "metric": "exact k-mers/s at k=63 (canonical, 4M x 250 bp skewed reads)",
+          "text": "4,000,000 x 250 bp reads, 20 Mbp genome (first 30% AT-rich Markov chain P(A)=P(T)=0.4, "
+                  "rest uniform), 1% subs; k=63 canonical"}
+
+
+def gen_skewed(n_reads: int, seed: int = 4):
+    from kite_gb300 import synth
+    return synth.skewed_workload(seed=seed, n_reads=n_reads)
+
+
 def chunk_layout(data) -> list:
     from kite_gb300 import ingest
     return ingest.split_chunks(data, CHUNK)
@@ -181,16 +195,16 @@ def sum_over_ranks(world, v: float) -> float:
     return float(t.item())
 
 
-def cpu_baseline(data, layout, reads_sample: int, threads: int) -> dict:
+def cpu_baseline(data, layout, reads_sample: int, threads: int, k: int = K, read_len: int = READ_LEN) -> dict:
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
     oracle.lib()
     # the first reads_sample records (fixed-length records)
-    rec_len = 11 + 1 + READ_LEN + 1 + 2 + READ_LEN + 1
+    rec_len = 11 + 1 + read_len + 1 + 2 + read_len + 1
     n = min(len(data), reads_sample * rec_len)
     sample = bytes(memoryview(data)[:n])
     workers = max(1, threads - 2)  # reader + writer threads as in the reference plan
-    r = oracle.count_buffer(sample, K, CANONICAL, PARTITIONS, workers)
+    r = oracle.count_buffer(sample, k, CANONICAL, PARTITIONS, workers)
     secs = r["ns"] / 1e9
     return {"value": r["kmers"] / secs, "unit": UNIT, "cores": workers, "kind": "port",
             "sample": f"first {reads_sample:,} reads ({n / 1e6:.0f} MB) of the workload, {workers} worker threads",
@@ -235,6 +249,7 @@ def main():
     ap.add_argument("--partitions", type=int, default=PARTITIONS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-splitter-compare", action="store_true")
+    ap.add_argument("--workload", default="repeats", choices=["repeats", "skewed"])
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -244,7 +259,15 @@ def main():
     torch.cuda.set_device(local)
     from kite_gb300 import gpu
 
-    data = gen_workload(args.reads, seed=2 + rank)  # each rank counts its own replica (weak scaling)
+    skewed = args.workload == "skewed"
+    kk = SKEWED["k"] if skewed else K
+    metric = SKEWED["metric"] if skewed else METRIC
+    if skewed and args.reads == 10_000_000:
+        args.reads = SKEWED["reads"]
+    if skewed:
+        data = gen_skewed(args.reads, seed=4 + rank)
+    else:
+        data = gen_workload(args.reads, seed=2 + rank)  # each rank counts its own replica (weak scaling)
     layout = chunk_layout(data)
     total = len(data)
     # device-resident copy, every chunk at a 16-byte aligned offset, 16 pad bytes after each
@@ -266,7 +289,7 @@ def main():
             c.submit_device(base + d, l)
         c.finish(collect=False)
 
-    c = gpu.Counter(K, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED,
+    c = gpu.Counter(kk, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED,
                     stream=stream.cuda_stream)
     for _ in range(args.warmup):
         device_step(c)
@@ -321,7 +344,7 @@ def main():
     # ---- learned vs sampled splitters on the same input (identical output) ----
     splitters = None
     if not args.no_splitter_compare:
-        cl = gpu.Counter(K, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_LEARNED,
+        cl = gpu.Counter(kk, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_LEARNED,
                          imbalance_bound=10.0, stream=stream.cuda_stream)
         device_step(cl)
         torch.cuda.synchronize()
@@ -334,8 +357,10 @@ def main():
         stl = cl.stats()
         cl.close()
         splitters = {"sampled": {"kmers_per_s": value / world, "tile_imbalance": st["tile_imbalance"],
+                                 "range_imbalance": st["range_imbalance"],
                                  "big_tiles": st["big_tiles"]},
                      "learned": {"kmers_per_s": kmers / tl, "tile_imbalance": stl["tile_imbalance"],
+                                 "range_imbalance": stl["range_imbalance"], "model_reused": stl["mlp_reused"] == 1,
                                  "big_tiles": stl["big_tiles"], "mlp_loss": stl["mlp_loss"],
                                  "predicted_imbalance": stl["mlp_pred_imbalance"],
                                  "used": stl["splitter_used"] == gpu.SPLIT_LEARNED}}
@@ -364,7 +389,7 @@ def main():
         e2e_parts["d2h_ms"] += cc.stats()["stage_ms"][7]
         d2h[0] = out_bytes
 
-    ce = gpu.Counter(K, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED)
+    ce = gpu.Counter(kk, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED)
     e2e_step(ce)
     ce.synchronize()
     for key in e2e_parts:
@@ -382,17 +407,21 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cb = cpu_baseline(data, layout, args.ref_reads, os.cpu_count() or 1)
+        cb = cpu_baseline(data, layout, args.ref_reads // (4 if skewed else 1), os.cpu_count() or 1, kk,
+                          SKEWED["read_len"] if skewed else READ_LEN)
         cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded)",
-                "config": {"workload": f"{args.reads:,} x {READ_LEN} bp reads, 50 Mbp genome with 20% repeats, "
-                                       f"1% subs, 0.1% N, strand 50/50; k={K} canonical; {args.partitions} partitions; "
+                "scaling": "weak", "vs_baseline": None, "dtype": "u128" if kk > 31 else "u64",
+                "data": "synthetic (seeded)",
+                "config": {"workload": (SKEWED["text"] if skewed else
+                                        f"{args.reads:,} x {READ_LEN} bp reads, 50 Mbp genome with 20% repeats, "
+                                        f"1% subs, 0.1% N, strand 50/50; k={K} canonical") +
+                                       f"; {args.partitions} partitions; "
                                        "sampled-histogram splitters",
-                           "reads": args.reads, "k": K, "canonical": CANONICAL, "partitions": args.partitions,
+                           "reads": args.reads, "k": kk, "canonical": CANONICAL, "partitions": args.partitions,
                            "fastq_bytes": total, "kmers_per_step": kmers, "rows_per_step": st["rows"],
                            "payload_bytes_per_step": st["payload_bytes"],
                            "l2": "inputs larger than L2 (FASTQ and keys are GBs; no flush needed)",

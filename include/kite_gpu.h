@@ -102,6 +102,7 @@ typedef struct {
   uint64_t sort_fallbacks;           /* tiles whose on-chip sort fell back to LSD passes (a large bin of distinct keys) */
   uint32_t split_levels;             /* key-range split passes over the keys (0, 1 or 2) */
   uint32_t staged_scatter;           /* 1: keys staged by the histogram pass, then a ranked bucket scatter */
+  uint32_t mlp_reused;               /* 1: the learned CDF of an earlier segment was kept (no training) */
 } kite_gpu_stats;
 
 /* Merge input: one .kite file's partition table, with payloads in host memory

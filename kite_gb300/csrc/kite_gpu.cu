@@ -424,6 +424,7 @@ int run_count(kite_gpu_ctx* ctx) {
       st.kernel_launches += rep.launches;
       st.mlp_loss = rep.loss;
       st.mlp_pred_imbalance = rep.pred_imbalance;
+      st.mlp_reused = rep.reused ? 1u : 0u;
       learned = rep.pred_imbalance <= bound;
       if (!learned && mode == KITE_SPLIT_LEARNED)
         st.kernel_launches += compute_hist_splitters<T>(ctx->sample.as<T>(), nsample, 2 * k, S, hist_spl,

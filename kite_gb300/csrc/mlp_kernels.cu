@@ -55,6 +55,8 @@ struct MlpModel {
   unsigned* hist = nullptr;  // [65536] sample histogram, then inclusive cumulative
   float last_loss = 0;
   double last_pred_imbalance = 0;
+  bool trained = false;
+  uint32_t trained_key_bits = 0;
 };
 
 MlpModel* mlp_create() { return new MlpModel(); }
@@ -413,15 +415,30 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
   cudaMemsetAsync(m->hist, 0, sizeof(unsigned) << kBinBits, s);
   k_bin_hist<T><<<(n + 255) / 256, 256, 0, s>>>(sorted, n, key_bits, m->hist);
   k_cum<<<1, 1024, 0, s>>>(m->hist);
+  rep->launches += 2;
+  const size_t smem = kParams * sizeof(float);
+  cudaFuncSetAttribute(k_invert<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (m->trained && m->trained_key_bits == key_bits) {
+    // the within-bin shape learned on an earlier segment, over this sample's histogram
+    k_invert<T><<<(S + 127) / 128, 128, smem, s>>>(m->params, m->hist, n, S, key_bits, d_spl);
+    k_sort_splitters<T><<<1, 1024, 0, s>>>(d_spl, S - 1);
+    rep->launches += 3;
+    double pred = 0;
+    if (predict_imbalance<T>(m, sorted, n, d_spl, S, s, timeout_ms, &pred)) return 1;
+    if (pred <= m->last_pred_imbalance * 1.05) {
+      rep->pred_imbalance = pred;
+      rep->loss = m->last_loss;
+      rep->reused = true;
+      return cudaGetLastError() == cudaSuccess ? 0 : 1;
+    }
+  }
   k_make_features<T><<<(n + 255) / 256, 256, 0, s>>>(sorted, n, key_bits, m->hist, m->feats, m->target, m->scale);
-  rep->launches += 3;
+  rep->launches += 1;
   int steps = 400;
   if (const char* e = getenv("KITE_MLP_STEPS")) steps = std::max(1, atoi(e));
   int tl = 0;
   if (mlp_train(m, n, steps, 8192, 2e-3f, s, timeout_ms, &rep->loss, &tl)) return 1;
   rep->launches += tl;
-  const size_t smem = kParams * sizeof(float);
-  cudaFuncSetAttribute(k_invert<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_invert<T><<<(S + 127) / 128, 128, smem, s>>>(m->params, m->hist, n, S, key_bits, d_spl);
   k_sort_splitters<T><<<1, 1024, 0, s>>>(d_spl, S - 1);
   rep->launches += 2;
@@ -429,6 +446,8 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
   rep->launches += 1;
   m->last_loss = rep->loss;
   m->last_pred_imbalance = rep->pred_imbalance;
+  m->trained = true;
+  m->trained_key_bits = key_bits;
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 template int mlp_splitters<uint64_t>(MlpModel*, const uint64_t*, uint32_t, uint32_t, uint32_t, uint64_t*,

@@ -62,7 +62,8 @@ class Stats(C.Structure):
                 ("d2h_bytes", C.c_uint64), ("kernel_launches", C.c_uint64), ("mlp_loss", C.c_double),
                 ("mlp_pred_imbalance", C.c_double), ("hist_pred_imbalance", C.c_double),
                 ("range_imbalance", C.c_double), ("sort_fallbacks", C.c_uint64),
-                ("split_levels", C.c_uint32), ("staged_scatter", C.c_uint32)]
+                ("split_levels", C.c_uint32), ("staged_scatter", C.c_uint32),
+                ("mlp_reused", C.c_uint32)]
 
     def as_dict(self) -> dict:
         d = {f: getattr(self, f) for f, _ in self._fields_ if f != "stage_ms"}
