@@ -1,4 +1,4 @@
-// Count-path kernels: FASTQ line indexing, rolling k-mer extraction with
+// Count-path kernels: FASTQ line indexing, bit-parallel k-mer extraction with
 // canonical min and N-splitting, hash-partition (bucket) scatter, and the
 // key-range tile split that feeds the on-chip sort.
 //
@@ -15,7 +15,6 @@
 
 namespace kite {
 
-static constexpr int kHalo = 64;        // >= k-1 for every k <= 64
 static constexpr int kExtractThreads = 256;
 
 // ---------------------------------------------------------------------------
@@ -44,50 +43,6 @@ __global__ void __launch_bounds__(256) k_newline_count(const uint8_t* __restrict
 void launch_newline_count(const uint8_t* arena, const BlockDesc* blocks, uint32_t nblocks,
                           unsigned long long* nl_out, cudaStream_t s) {
   if (nblocks) k_newline_count<<<nblocks, 256, 0, s>>>(arena, blocks, nl_out);
-}
-
-// ---------------------------------------------------------------------------
-// Shared-memory byte layout of a block: block-relative byte rel = pos + kHalo
-// - blk_start lives in segment rel >> pts (one thread's range of PT = 1 << pts
-// bytes) at a stride of PT + 4 bytes, so the 32 lanes of a warp, each walking
-// its own range, read 32 different banks.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t pidx(uint32_t rel, uint32_t pts) {
-  return (rel >> pts) * ((1u << pts) + 4u) + (rel & ((1u << pts) - 1u));
-}
-
-// Rolling extraction over one thread's byte range.  Warm-up bytes before `ts`
-// only seed the window; a newline resets it, so bytes of earlier lines never
-// leak into a k-mer.
-template <class T, class F>
-__device__ __forceinline__ void roll_range(const uint8_t* sb, uint32_t pts, uint64_t blk_start, uint64_t ws,
-                                           uint64_t ts, uint64_t te, unsigned phase, bool chunk_ok,
-                                           const uint8_t* table, uint32_t k, bool canonical, F&& emit) {
-  const T mask = (2 * k == (uint32_t)KeyTraits<T>::kBits) ? ~T(0) : ((T(1) << (2 * k)) - T(1));
-  const unsigned rsh = 2 * (k - 1);
-  T fwd = 0, rev = 0;
-  uint32_t run = 0;
-  unsigned ph = phase;
-  for (uint64_t pos = ws; pos < te; ++pos) {
-    const uint8_t b = sb[pidx((uint32_t)(pos + kHalo - blk_start), pts)];
-    if (b == '\n') {
-      fwd = 0;
-      rev = 0;
-      run = 0;
-      if (pos >= ts) ph = (ph + 1) & 3;
-      continue;
-    }
-    const uint8_t c = table[b];
-    if (!chunk_ok || ph != 1 || c > 3) {
-      fwd = 0;
-      rev = 0;
-      run = 0;
-      continue;
-    }
-    fwd = ((fwd << 2) | T(c)) & mask;
-    rev = (rev >> 2) | (T(c ^ 3) << rsh);
-    if (++run >= k && pos >= ts) emit(canonical ? (fwd < rev ? fwd : rev) : fwd, pos);
-  }
 }
 
 __device__ __forceinline__ uint64_t mix64(uint64_t x) {
@@ -158,122 +113,12 @@ __device__ __forceinline__ void reserve_ranges(const ExtractParams<T>& p, unsign
   }
 }
 
-__host__ __device__ __forceinline__ size_t padded_bytes(uint32_t blk_bytes) {
-  const size_t pt = blk_bytes / kExtractThreads;
-  const size_t segs = ((size_t)kHalo + blk_bytes + 16 + pt - 1) / pt;
-  return (segs * (pt + 4) + 15) & ~(size_t)15;
-}
-
 size_t extract64_smem_bytes(uint32_t partitions, bool scatter);
 
 size_t extract_smem_bytes(int key_bytes, uint32_t blk_bytes, uint32_t partitions, bool scatter) {
-  if (key_bytes == 8) return extract64_smem_bytes(partitions, scatter);
-  size_t o = padded_bytes(blk_bytes);
-  if (scatter) o += (size_t)partitions * 8;  // reservation base (u64)
-  o += (size_t)partitions * 4;               // histogram / cursor
-  o += 64 * 4 + 256;                         // scan / reduction scratch + base table
-  return o;
-}
-
-// MODE 0: histogram pass (bucket counts, totals, sampling).
-// MODE 1: scatter pass (reserve bucket ranges, write keys).
-template <class T, int MODE>
-__global__ void __launch_bounds__(kExtractThreads) k_extract(ExtractParams<T> p) {
-  constexpr int NT = kExtractThreads;
-  extern __shared__ __align__(16) uint8_t sm[];
-  const uint32_t P = p.partitions;
-  uint8_t* sb = sm;
-  size_t o = padded_bytes(p.blk_bytes);
-  unsigned long long* base = reinterpret_cast<unsigned long long*>(sm + o);
-  if (MODE == 1) o += (size_t)P * 8;
-  unsigned* hist = reinterpret_cast<unsigned*>(sm + o);
-  o += (size_t)P * 4;
-  unsigned* scan_sm = reinterpret_cast<unsigned*>(sm + o);
-  o += 64 * 4;
-  uint8_t* table = sm + o;
-
-  const BlockDesc d = p.blocks[blockIdx.x];
-  const uint64_t s = d.start, e = d.end;
-  const uint64_t hs = (s - d.chunk_start >= (uint64_t)kHalo) ? s - kHalo : d.chunk_start;
-  const uint32_t PT = p.blk_bytes / NT;
-  const uint32_t pts = 31 - __clz(PT);
-  // coalesced 16-byte loads, stored as four 4-byte words (PT >= 4, so a word
-  // never straddles a segment and its padded address stays 4-byte aligned)
-  for (uint64_t w = (hs >> 4) + threadIdx.x; w < ((e + 15) >> 4); w += NT) {
-    const uint4 v = reinterpret_cast<const uint4*>(p.arena)[w];
-    const uint32_t rel = (uint32_t)(w * 16 + kHalo - s);
-    *reinterpret_cast<uint32_t*>(sb + pidx(rel, pts)) = v.x;
-    *reinterpret_cast<uint32_t*>(sb + pidx(rel + 4, pts)) = v.y;
-    *reinterpret_cast<uint32_t*>(sb + pidx(rel + 8, pts)) = v.z;
-    *reinterpret_cast<uint32_t*>(sb + pidx(rel + 12, pts)) = v.w;
-  }
-  for (int i = threadIdx.x; i < 256; i += NT) {
-    uint8_t v = 255;
-    if (i == 'A' || i == 'a') v = 0;
-    else if (i == 'C' || i == 'c') v = 1;
-    else if (i == 'G' || i == 'g') v = 2;
-    else if (i == 'T' || i == 't') v = 3;
-    table[i] = v;
-  }
-  for (uint32_t b = threadIdx.x; b < P; b += NT) hist[b] = 0;
-  __syncthreads();
-
-  const uint64_t ts = s + (uint64_t)threadIdx.x * PT;
-  const uint64_t te = ts < e ? (ts + PT < e ? ts + PT : e) : ts;
-  unsigned nl = 0;
-  for (uint64_t pos = ts; pos < te; ++pos) nl += sb[pidx((uint32_t)(pos + kHalo - s), pts)] == '\n';
-  unsigned nl_total;
-  const unsigned nl_before = block_exclusive_scan<NT, unsigned>(nl, scan_sm, &nl_total);
-  const unsigned long long line0 = p.block_nl_excl[blockIdx.x] - p.block_nl_excl[d.first_block];
-  const unsigned phase = (unsigned)((line0 + nl_before) & 3ull);
-  const bool chunk_ok = p.arena[d.chunk_start] == '@';  // src/count/parser.rs:27-29
-  const uint64_t ws = (ts - hs >= p.k - 1) ? ts - (p.k - 1) : hs;
-  const bool canon = p.canonical != 0;
-  const uint32_t shift = p.shift;
-
-  if (MODE == 0) {
-    unsigned long long kmers = 0;
-    const bool sampling = p.sample != nullptr && (d.flags & 2u);
-    roll_range<T>(sb, pts, s, ws, ts, te, phase, chunk_ok, table, p.k, canon, [&](T key, uint64_t pos) {
-      kmers++;
-      atomicAdd(&hist[bucket_of(key, shift)], 1u);
-      if (sampling && (mix64(pos) & p.sample_mask) == 0) {
-        const unsigned idx = atomicAdd(p.sample_count, 1u);
-        if (idx < p.sample_cap) p.sample[idx] = key;
-      }
-    });
-    // reads / bases of this thread's range
-    unsigned long long reads = 0, bases = 0;
-    if (chunk_ok) {
-      unsigned ph = phase;
-      uint8_t prev = ts > d.chunk_start ? sb[pidx((uint32_t)(ts - 1 + kHalo - s), pts)] : (uint8_t)'\n';
-      for (uint64_t pos = ts; pos < te; ++pos) {
-        const uint8_t b = sb[pidx((uint32_t)(pos + kHalo - s), pts)];
-        if (b == '\n') {
-          ph = (ph + 1) & 3;
-        } else if (ph == 1) {
-          bases++;
-          reads += prev == '\n';
-        }
-        prev = b;
-      }
-    }
-    __syncthreads();
-    flush_hist<NT>(p, hist, P);
-    flush_totals<NT>(p.totals, kmers, reads, bases, reinterpret_cast<unsigned long long*>(scan_sm));
-  } else {
-    roll_range<T>(sb, pts, s, ws, ts, te, phase, chunk_ok, table, p.k, canon,
-                  [&](T key, uint64_t) { atomicAdd(&hist[bucket_of(key, shift)], 1u); });
-    __syncthreads();
-    reserve_ranges<NT>(p, hist, base, P);
-    __syncthreads();
-    roll_range<T>(sb, pts, s, ws, ts, te, phase, chunk_ok, table, p.k, canon, [&](T key, uint64_t) {
-      const uint32_t b = bucket_of(key, shift);
-      const unsigned slot = atomicAdd(&hist[b], 1u);
-      const unsigned long long r = base[b];
-      if (r != ~0ull) p.keys_out[p.bucket_off[b] + r + slot] = key;
-    });
-  }
+  (void)key_bytes;
+  (void)blk_bytes;
+  return extract64_smem_bytes(partitions, scatter);
 }
 
 // ---------------------------------------------------------------------------
@@ -488,6 +333,156 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same for 32 <= k <= 64 (u128 keys): a k-mer ending in a word reaches up
+// to two words back, so each thread also encodes the two words before its
+// own; windows are funnel shifts of three packed words.
+// ---------------------------------------------------------------------------
+// bit j set iff bits j .. j+k-1 of a are all set
+__device__ __forceinline__ u128 runs_of128(u128 a, uint32_t k) {
+  u128 r = a;
+  uint32_t len = 1;
+  while (2 * len <= k) {
+    r &= r >> len;
+    len *= 2;
+  }
+  if (len < k) r &= r >> (k - len);
+  return r;
+}
+
+// Visits every valid k-mer ending in word w (previous words p1, p2): f(key, e).
+template <class F>
+__device__ __forceinline__ void word_kmers128(uint32_t V, const Word32& p2, const Word32& p1, const Word32& w,
+                                              uint32_t k, u128 mask, bool canonical, F&& f) {
+  const u128 X = ((u128)p1.code << 64) | w.code;       // forward stream p1 | w (p2 above it)
+  const u128 RL = ((u128)p1.rcode << 64) | p2.rcode;   // reverse stream R(w) | R(p1) | R(p2), low part
+  const u128 RH = ((u128)w.rcode << 64) | p1.rcode;    // high part
+  while (V) {
+    const uint32_t e = __ffs(V) - 1;
+    V &= V - 1;
+    const uint32_t sft = 2 * (31 - e);  // 0 .. 62
+    const u128 fwd = (sft ? ((X >> sft) | ((u128)p2.code << (128 - sft))) : X) & mask;
+    u128 key = fwd;
+    if (canonical) {
+      const uint32_t t = 2 * (65 + e - k);  // 2 .. 128 for 32 <= k <= 64
+      u128 rc;
+      if (t < 64) rc = (RL >> t) | ((u128)w.rcode << (128 - t));
+      else if (t < 128) rc = RH >> (t - 64);
+      else rc = (u128)w.rcode;
+      rc &= mask;
+      key = rc < fwd ? rc : fwd;
+    }
+    f(key, e);
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kExtractThreads) k_extract128(ExtractParams<u128> p) {
+  constexpr int NT = kExtractThreads;
+  extern __shared__ __align__(16) uint8_t sm[];
+  const uint32_t P = p.partitions;
+  unsigned long long* base = reinterpret_cast<unsigned long long*>(sm);
+  unsigned* hist = reinterpret_cast<unsigned*>(sm + (MODE == 1 ? (size_t)P * 8 : 0));
+  unsigned* scan_sm = hist + P;
+  for (uint32_t b = threadIdx.x; b < P; b += NT) hist[b] = 0;
+
+  const BlockDesc d = p.blocks[blockIdx.x];
+  const uint64_t e = d.end;
+  const uint64_t ts = d.start + (uint64_t)threadIdx.x * 64;
+  const bool chunk_ok = p.arena[d.chunk_start] == '@';  // src/count/parser.rs:27-29
+  const uint32_t k = p.k;
+  const u128 mask = 2 * k == 128 ? ~u128(0) : ((u128(1) << (2 * k)) - u128(1));
+  const bool canon = p.canonical != 0;
+  const uint32_t shift = p.shift;
+
+  Word32 wq, wp, w0, w1;
+  uint32_t r0, r1, rp;
+  // ts - chunk_start is a multiple of 64: the two words before are wholly
+  // inside the chunk, or the thread starts the chunk
+  const bool has_prev = ts > d.chunk_start && ts < e;
+  load_word(p.arena, has_prev ? ts - 64 : ts, has_prev ? ts : ts, wq, rp);
+  load_word(p.arena, has_prev ? ts - 32 : ts, has_prev ? ts : ts, wp, rp);
+  if (!has_prev) {
+    wq.nl = wq.vb = 0;
+    wp.nl = wp.vb = 0;
+  }
+  load_word(p.arena, ts, e, w0, r0);
+  load_word(p.arena, ts + 32, e, w1, r1);
+  w0.nl &= r0;
+  w1.nl &= r1;
+  unsigned nl_total;
+  const unsigned nl_before = block_exclusive_scan<NT, unsigned>(__popc(w0.nl) + __popc(w1.nl), scan_sm, &nl_total);
+  const unsigned long long line0 = p.block_nl_excl[blockIdx.x] - p.block_nl_excl[d.first_block];
+  unsigned ph = (unsigned)((line0 + nl_before) & 3ull);                       // line phase at ts
+  unsigned phq = (ph - (unsigned)__popc(wp.nl) - (unsigned)__popc(wq.nl)) & 3u;  // at ts - 64
+  const uint32_t seqq = has_prev ? seq_mask(wq.nl, phq) : 0u;
+  const uint32_t seqp = has_prev ? seq_mask(wp.nl, phq) : 0u;
+  const uint32_t seq0 = seq_mask(w0.nl, ph) & r0;
+  const uint32_t seq1 = seq_mask(w1.nl, ph) & r1;
+  const uint32_t okq = chunk_ok ? (seqq & wq.vb) : 0u;
+  const uint32_t okp = chunk_ok ? (seqp & wp.vb) : 0u;
+  const uint32_t ok0 = chunk_ok ? (seq0 & w0.vb) : 0u;
+  const uint32_t ok1 = chunk_ok ? (seq1 & w1.vb) : 0u;
+  const uint32_t V0 =
+      (uint32_t)(uint64_t)(runs_of128((u128)okq | ((u128)okp << 32) | ((u128)ok0 << 64), k) >> (65 - k));
+  const uint32_t V1 =
+      (uint32_t)(uint64_t)(runs_of128((u128)okp | ((u128)ok0 << 32) | ((u128)ok1 << 64), k) >> (65 - k));
+  __syncthreads();  // hist zeroed
+
+  if (MODE == 0) {
+    unsigned long long kmers = __popc(V0) + __popc(V1);
+    const bool sampling = p.sample != nullptr && (d.flags & 2u);
+    u128* out = nullptr;
+    if (p.keys_stage) {
+      unsigned tot;
+      const unsigned before = block_exclusive_scan<NT, unsigned>((unsigned)kmers, scan_sm, &tot);
+      unsigned long long* bb = reinterpret_cast<unsigned long long*>(scan_sm) + 40;
+      if (threadIdx.x == 0) {
+        unsigned long long at = tot ? atomicAdd(p.stage_counter, (unsigned long long)tot) : 0ull;
+        if (at + tot > p.stage_cap) at = ~0ull;  // over capacity: the host takes the other scatter path
+        *bb = at;
+        p.blk_keys[2 * (size_t)blockIdx.x] = at;
+        p.blk_keys[2 * (size_t)blockIdx.x + 1] = tot;
+      }
+      __syncthreads();
+      if (*bb != ~0ull) out = p.keys_stage + *bb + before;
+    }
+    auto emit = [&](u128 key, uint64_t pos) {
+      atomicAdd(&hist[bucket_of(key, shift)], 1u);
+      if (out) *out++ = key;
+      if (sampling && (mix64(pos) & p.sample_mask) == 0) {
+        const unsigned idx = atomicAdd(p.sample_count, 1u);
+        if (idx < p.sample_cap) p.sample[idx] = key;
+      }
+    };
+    word_kmers128(V0, wq, wp, w0, k, mask, canon, [&](u128 key, uint32_t b) { emit(key, ts + b); });
+    word_kmers128(V1, wp, w0, w1, k, mask, canon, [&](u128 key, uint32_t b) { emit(key, ts + 32 + b); });
+    unsigned long long reads = 0, bases = 0;
+    if (chunk_ok) {
+      bases = __popc(seq0) + __popc(seq1);
+      reads = __popc(seq0 & ~((seq0 << 1) | (seqp >> 31))) + __popc(seq1 & ~((seq1 << 1) | (seq0 >> 31)));
+    }
+    __syncthreads();
+    flush_hist<NT>(p, hist, P);
+    flush_totals<NT>(p.totals, kmers, reads, bases, reinterpret_cast<unsigned long long*>(scan_sm));
+  } else {
+    auto count = [&](u128 key, uint32_t) { atomicAdd(&hist[bucket_of(key, shift)], 1u); };
+    word_kmers128(V0, wq, wp, w0, k, mask, canon, count);
+    word_kmers128(V1, wp, w0, w1, k, mask, canon, count);
+    __syncthreads();
+    reserve_ranges<NT>(p, hist, base, P);
+    __syncthreads();
+    auto write = [&](u128 key, uint32_t) {
+      const uint32_t b = bucket_of(key, shift);
+      const unsigned slot = atomicAdd(&hist[b], 1u);
+      const unsigned long long r = base[b];
+      if (r != ~0ull) p.keys_out[p.bucket_off[b] + r + slot] = key;
+    };
+    word_kmers128(V0, wq, wp, w0, k, mask, canon, write);
+    word_kmers128(V1, wp, w0, w1, k, mask, canon, write);
+  }
+}
+
 template <class T>
 void launch_extract_hist(const ExtractParams<T>& p, uint32_t nblocks, cudaStream_t s) {
   const size_t smem = extract_smem_bytes(sizeof(T), p.blk_bytes, p.partitions, false);
@@ -496,8 +491,8 @@ void launch_extract_hist(const ExtractParams<T>& p, uint32_t nblocks, cudaStream
     if (nblocks)
       k_extract64<0><<<nblocks, kExtractThreads, smem, s>>>(reinterpret_cast<const ExtractParams<uint64_t>&>(p));
   } else {
-    cudaFuncSetAttribute(k_extract<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (nblocks) k_extract<T, 0><<<nblocks, kExtractThreads, smem, s>>>(p);
+    cudaFuncSetAttribute(k_extract128<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nblocks) k_extract128<0><<<nblocks, kExtractThreads, smem, s>>>(p);
   }
 }
 template <class T>
@@ -508,8 +503,8 @@ void launch_extract_scatter(const ExtractParams<T>& p, uint32_t nblocks, cudaStr
     if (nblocks)
       k_extract64<1><<<nblocks, kExtractThreads, smem, s>>>(reinterpret_cast<const ExtractParams<uint64_t>&>(p));
   } else {
-    cudaFuncSetAttribute(k_extract<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (nblocks) k_extract<T, 1><<<nblocks, kExtractThreads, smem, s>>>(p);
+    cudaFuncSetAttribute(k_extract128<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nblocks) k_extract128<1><<<nblocks, kExtractThreads, smem, s>>>(p);
   }
 }
 template void launch_extract_hist<uint64_t>(const ExtractParams<uint64_t>&, uint32_t, cudaStream_t);
@@ -706,10 +701,11 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
 // BATCH keys ranked on chip by partition (stable warp-match ranking), staged in
 // partition order and written as runs at the block's offsets.
 constexpr int kBsThreads = 256, kBsItems = 8, kBsBatch = kBsThreads * kBsItems;
+template <class T>
 struct BsSmem {
   static constexpr int NW = kBsThreads / 32;
   static constexpr size_t o_stage = 0;
-  static constexpr size_t o_dig = o_stage + (size_t)kBsBatch * 8;
+  static constexpr size_t o_dig = o_stage + (size_t)kBsBatch * sizeof(T);
   static constexpr size_t o_whist = (o_dig + (size_t)kBsBatch + 15) & ~(size_t)15;
   static constexpr size_t o_cur = o_whist + (size_t)256 * NW * 4;
   static constexpr size_t o_dtot = o_cur + (size_t)256 * 8;
@@ -718,14 +714,15 @@ struct BsSmem {
   static constexpr size_t total = o_scan + 64 * 4;
 };
 
+template <class T>
 __global__ void __launch_bounds__(kBsThreads, 4)
-    k_bucket_scatter(const uint64_t* __restrict__ keys_stage, const unsigned long long* __restrict__ blk_keys,
+    k_bucket_scatter(const T* __restrict__ keys_stage, const unsigned long long* __restrict__ blk_keys,
                      const unsigned* __restrict__ blk_offs, const unsigned long long* __restrict__ bucket_off,
-                     uint32_t P, uint32_t shift, uint64_t* __restrict__ keys_out) {
-  using L = BsSmem;
+                     uint32_t P, uint32_t shift, T* __restrict__ keys_out) {
+  using L = BsSmem<T>;
   constexpr int NT = kBsThreads, IT = kBsItems;
-  __shared__ __align__(16) uint8_t sm[L::total];
-  uint64_t* stage = reinterpret_cast<uint64_t*>(sm + L::o_stage);
+  extern __shared__ __align__(16) uint8_t sm[];
+  T* stage = reinterpret_cast<T*>(sm + L::o_stage);
   uint8_t* dig8 = sm + L::o_dig;
   unsigned* whist = reinterpret_cast<unsigned*>(sm + L::o_whist);
   unsigned long long* cur = reinterpret_cast<unsigned long long*>(sm + L::o_cur);
@@ -742,14 +739,14 @@ __global__ void __launch_bounds__(kBsThreads, 4)
   const unsigned pos0 = (unsigned)wid * 32u * IT + lane;
   for (uint64_t c0 = 0; c0 < n; c0 += kBsBatch) {
     const unsigned cn = (unsigned)((n - c0) < (uint64_t)kBsBatch ? (n - c0) : (uint64_t)kBsBatch);
-    uint64_t key[IT];
+    T key[IT];
     unsigned dg[IT], dest[IT];
     bool valid[IT];
 #pragma unroll
     for (int q = 0; q < IT; ++q) {
       const unsigned pos = pos0 + q * 32u;
       valid[q] = pos < cn;
-      key[q] = valid[q] ? keys_stage[a + c0 + pos] : 0ull;
+      key[q] = valid[q] ? keys_stage[a + c0 + pos] : T(0);
       dg[q] = valid[q] ? bucket_of(key[q], shift) : 0u;
     }
     block_rank<NT, IT, 256>(dg, valid, dest, whist, scan_sm, dtot, dstart);
@@ -770,13 +767,21 @@ __global__ void __launch_bounds__(kBsThreads, 4)
   }
 }
 
-void launch_bucket_scatter(const uint64_t* keys_stage, const unsigned long long* blk_keys, const unsigned* blk_offs,
+template <class T>
+void launch_bucket_scatter(const T* keys_stage, const unsigned long long* blk_keys, const unsigned* blk_offs,
                            const unsigned long long* bucket_off, uint32_t partitions, uint32_t shift, uint32_t nblocks,
-                           uint64_t* keys_out, cudaStream_t s) {
+                           T* keys_out, cudaStream_t s) {
+  const size_t smem = BsSmem<T>::total;
+  cudaFuncSetAttribute(k_bucket_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (nblocks)
-    k_bucket_scatter<<<nblocks, kBsThreads, 0, s>>>(keys_stage, blk_keys, blk_offs, bucket_off, partitions, shift,
-                                                    keys_out);
+    k_bucket_scatter<T><<<nblocks, kBsThreads, smem, s>>>(keys_stage, blk_keys, blk_offs, bucket_off, partitions,
+                                                          shift, keys_out);
 }
+template void launch_bucket_scatter<uint64_t>(const uint64_t*, const unsigned long long*, const unsigned*,
+                                              const unsigned long long*, uint32_t, uint32_t, uint32_t, uint64_t*,
+                                              cudaStream_t);
+template void launch_bucket_scatter<u128>(const u128*, const unsigned long long*, const unsigned*,
+                                          const unsigned long long*, uint32_t, uint32_t, uint32_t, u128*, cudaStream_t);
 
 // Tile list from the scanned part offsets: tile t = (b, j) starts at
 // off[t*G] and ends where tile t+1 starts (the last at n_keys).

@@ -206,7 +206,7 @@ int run_count(kite_gpu_ctx* ctx) {
   KCU(cudaEventRecord(ctx->ev[0], s));
 
   // ---- blocks -------------------------------------------------------------
-  uint32_t blk = sizeof(T) == 8 ? 16384 : 8192;
+  uint32_t blk = 16384;  // 256 threads x 64 bytes
   while (blk > 1024 && extract_smem_bytes(sizeof(T), blk, P, true) > 200 * 1024) blk >>= 1;
   if (extract_smem_bytes(sizeof(T), blk, P, true) > 220 * 1024)
     return fail(ctx, KITE_ERR_UNSUPPORTED, "partition count too large for the extraction kernel");
@@ -291,7 +291,7 @@ int run_count(kite_gpu_ctx* ctx) {
   // them to the bucket regions
   uint64_t fastq_bytes = 0;
   for (const Chunk& ch : ctx->chunks) fastq_bytes += ch.len;
-  const bool stage_keys = sizeof(T) == 8 && use_matrix && P <= 256;
+  const bool stage_keys = use_matrix && P <= 256;
   const uint64_t stage_cap = fastq_bytes / 2 + 1024;
   if (stage_keys) {
     const uint64_t cap = stage_cap;
@@ -366,9 +366,8 @@ int run_count(kite_gpu_ctx* ctx) {
   ep.blk_offs = (use_matrix && maxb < (1ull << 32)) ? ctx->blk_mat.as<unsigned>() : nullptr;
   if (stage_keys && ep.blk_offs && staged == N && N <= stage_cap) {
     st.staged_scatter = 1;
-    launch_bucket_scatter(reinterpret_cast<const uint64_t*>(ctx->keys_b.p), ctx->blk_keys.as<unsigned long long>(),
-                          ep.blk_offs, ctx->bucket_off.as<unsigned long long>(), P, ep.shift, nblocks,
-                          reinterpret_cast<uint64_t*>(ctx->keys_a.p), s);
+    launch_bucket_scatter<T>(ctx->keys_b.as<T>(), ctx->blk_keys.as<unsigned long long>(), ep.blk_offs,
+                             ctx->bucket_off.as<unsigned long long>(), P, ep.shift, nblocks, ctx->keys_a.as<T>(), s);
   } else {
     ep.keys_stage = nullptr;
     launch_extract_scatter<T>(ep, nblocks, s);

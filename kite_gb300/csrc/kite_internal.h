@@ -107,9 +107,10 @@ void launch_extract_scatter(const ExtractParams<T>& p, uint32_t nblocks, cudaStr
 // Scatter of the staged keys of every block into the bucket regions
 // (partitions <= 256): keys of block b go to bucket_off[k] + blk_offs[b][k]
 // onwards, ranked on chip so that writes are coalesced.
-void launch_bucket_scatter(const uint64_t* keys_stage, const unsigned long long* blk_keys, const unsigned* blk_offs,
+template <class T>
+void launch_bucket_scatter(const T* keys_stage, const unsigned long long* blk_keys, const unsigned* blk_offs,
                            const unsigned long long* bucket_off, uint32_t partitions, uint32_t shift, uint32_t nblocks,
-                           uint64_t* keys_out, cudaStream_t s);
+                           T* keys_out, cudaStream_t s);
 template <class T>
 void launch_split_hist(const TileSplitParams<T>& p, cudaStream_t s);
 template <class T>
