@@ -43,11 +43,18 @@ METRIC = "exact k-mers/s at k=31 (canonical, 10M x 150 bp reads)"
 UNIT = "k-mers/s"
 
 
-def gen_workload(n_reads: int, seed: int = 2):
+_GENOMES = {}
+
+
+def gen_workload(n_reads: int, seed: int = 2, genome_seed: int | None = None):
+    """Reads of the 10M-read workload's shape; the genome comes from
+    genome_seed (default: seed), the reads from seed."""
     from kite_gb300 import host, synth
-    rng = np.random.default_rng(seed)
-    genome = synth.genome_with_repeats(rng, 50_000_000)
-    data = host.synth_reads(genome, n_reads, READ_LEN, 0.01, 0.001, 0.5, seed=seed,
+    gs = seed if genome_seed is None else genome_seed
+    if gs not in _GENOMES:
+        _GENOMES.clear()
+        _GENOMES[gs] = synth.genome_with_repeats(np.random.default_rng(gs), 50_000_000)
+    data = host.synth_reads(_GENOMES[gs], n_reads, READ_LEN, 0.01, 0.001, 0.5, seed=seed,
                             threads=max(1, os.cpu_count() or 1))
     return data
 
@@ -238,6 +245,88 @@ def run_reference(args):
     return 0
 
 
+MERGE_METRIC = "merged input rows/s (8 .kite databases, k=31 canonical, 256 partitions)"
+
+
+def run_merge_bench(args, world, rank, local):
+    """8 .kite databases, each counted (on this GPU) from its own seeded
+    sample of the 10M-read workload's shape with 2M-10M reads, merged by
+    kite_gpu_merge: inputs in pinned host memory, outputs read in place.  One
+    step = one full merge (H2D, decode, k-way merge with exact u32 summation,
+    encode, D2H)."""
+    import torch
+    from kite_gb300 import gpu, host
+    from kite_gb300.kitefile import KiteImage
+    rng = np.random.default_rng(5)
+    reads = [max(1000, int(x * args.merge_scale)) for x in rng.integers(2_000_000, 10_000_001, size=8)]
+    images = []
+    for i, nr in enumerate(reads):
+        data = gen_workload(nr, seed=100 + i + 8 * rank, genome_seed=2)  # one genome, own reads
+        layout = chunk_layout(data)
+        pinned = torch.frombuffer(bytearray(data), dtype=torch.uint8).pin_memory()
+        base = pinned.data_ptr()
+        w = host.Writer(None, K, CANONICAL, PARTITIONS, 8, 7, 16 << 20, 2)
+        with gpu.Counter(K, CANONICAL, PARTITIONS, device=local, arena_bytes=len(data) + (64 << 20)) as c:
+            for o, l in layout:
+                c.submit((base + o, l))
+            for m, p in c.finish():
+                w.append(m, p)
+        w.finalize()
+        images.append(w.image())
+        w.close()
+        del pinned, data
+    kis = [KiteImage.parse(img) for img in images]
+    pins = []
+    for img in images:
+        t = torch.empty(len(img), dtype=torch.uint8).pin_memory()
+        t.numpy()[:] = np.frombuffer(img, dtype=np.uint8)
+        pins.append(t)
+    bases = [t.data_ptr() for t in pins]
+    rows_in = sum(ki.total_rows for ki in kis)
+    bytes_in = sum(len(img) for img in images)
+    out_stats = {"rows": 0, "bytes": 0}
+
+    def cb(meta, addr, n):
+        out_stats["rows"] += meta["row_count"]
+        out_stats["bytes"] += n
+
+    c = gpu.Counter(K, CANONICAL, PARTITIONS, device=local)
+    for _ in range(args.warmup):
+        out_stats["rows"] = out_stats["bytes"] = 0
+        c.merge(kis, callback=cb, bases=bases)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out_stats["rows"] = out_stats["bytes"] = 0
+        c.merge(kis, callback=cb, bases=bases)
+    c.synchronize()
+    barrier(world)
+    dt = max_over_ranks(world, (time.perf_counter() - t0) / args.steps)
+    c.close()
+    value = sum_over_ranks(world, rows_in) / dt
+    peak, peak_src = peaks()
+    algo = rows_in * 12 + out_stats["rows"] * 12  # decoded rows in + merged rows out, (key, count) as 8+4 B
+    if rank == 0:
+        line = {"metric": MERGE_METRIC, "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded)",
+                "config": {"workload": "8 .kite databases, each counted from its own seeded read sample "
+                                       f"({min(reads):,}-{max(reads):,} reads) of the 10M-read workload's genome "
+                                       "and read shape; k=31 canonical; "
+                                       "256 partitions; merge with exact u32 summation",
+                           "reads_per_db": reads, "rows_in": rows_in, "rows_out": out_stats["rows"],
+                           "input_bytes": bytes_in, "output_bytes": out_stats["bytes"],
+                           "parallelism": f"replicas x{world}"},
+                "e2e": {"value": value, "unit": "rows/s", "h2d_bytes_per_step": bytes_in,
+                        "d2h_bytes_per_step": out_stats["bytes"]},
+                "roofline": {"bound": "hbm", "kernel": "merge (whole call)", "achieved": algo / dt / 1e9,
+                             "peak": peak, "unit": "GB/s", "frac": algo / dt / 1e9 / peak, "traffic": None,
+                             "peak_source": peak_src, "algorithmic_bytes": algo}}
+        print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -249,7 +338,8 @@ def main():
     ap.add_argument("--partitions", type=int, default=PARTITIONS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-splitter-compare", action="store_true")
-    ap.add_argument("--workload", default="repeats", choices=["repeats", "skewed"])
+    ap.add_argument("--workload", default="repeats", choices=["repeats", "skewed", "merge"])
+    ap.add_argument("--merge-scale", type=float, default=1.0, help="read-count scale of the merge databases")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -258,6 +348,8 @@ def main():
     import torch
     torch.cuda.set_device(local)
     from kite_gb300 import gpu
+    if args.workload == "merge":
+        return run_merge_bench(args, world, rank, local)
 
     skewed = args.workload == "skewed"
     kk = SKEWED["k"] if skewed else K

@@ -198,19 +198,28 @@ class Counter:
     def synchronize(self) -> None:
         self._check(self._L.kite_gpu_synchronize(self._h))
 
-    def merge(self, inputs: list, collect: bool = True) -> list:
-        """inputs: list of kitefile.KiteImage; returns [(meta, payload)]."""
+    def merge(self, inputs: list, collect: bool = True, callback=None, bases: list | None = None) -> list:
+        """inputs: list of kitefile.KiteImage; returns [(meta, payload)].
+        With a callback, it gets (meta, host address, length) of each output
+        chunk (valid during the call) and nothing is collected.  `bases`:
+        optional host addresses holding each image's bytes (no copy)."""
         arr = (MergeInput * len(inputs))()
         keep = []
         for i, img in enumerate(inputs):
-            mi, k = img.merge_input()
+            mi, k = img.merge_input(bases[i] if bases else None)
             arr[i] = mi
             keep.append(k)
         out = []
 
         def _emit(user, meta, data, n):
-            out.append((meta.contents.as_dict(), C.string_at(data, n)))
-            return 0
+            try:
+                if callback is not None:
+                    callback(meta.contents.as_dict(), C.cast(data, C.c_void_p).value, n)
+                elif collect:
+                    out.append((meta.contents.as_dict(), C.string_at(data, n)))
+                return 0
+            except Exception:  # pragma: no cover - surfaced as KITE_ERR_CALLBACK
+                return 1
 
         cb = EMIT(_emit)
         self._check(self._L.kite_gpu_merge(self._h, arr, len(inputs), cb, None))

@@ -74,8 +74,10 @@ class KiteImage:
     def payload(self, c: Chunk) -> bytes:
         return self.data[c.file_offset:c.file_offset + c.encoded_bytes]
 
-    def merge_input(self):
-        """A kite_gpu_merge_input over this image (keeps the arrays alive)."""
+    def merge_input(self, base_address: int | None = None):
+        """A kite_gpu_merge_input over this image (keeps the arrays alive).
+        With base_address, the image bytes are read from that host address
+        (e.g. a pinned copy of the image) instead of a private copy."""
         from .gpu import MergeInput
         n = len(self.chunks)
         arrs = {
@@ -86,9 +88,12 @@ class KiteImage:
             "first": np.array(self.part_first, dtype=np.uint64),
             "count": np.array(self.part_count, dtype=np.uint64),
         }
-        buf = (C.c_uint8 * len(self.data)).from_buffer_copy(self.data)
+        buf = None
+        if base_address is None:
+            buf = (C.c_uint8 * len(self.data)).from_buffer_copy(self.data)
+            base_address = C.addressof(buf)
         p64 = lambda a: a.ctypes.data_as(C.POINTER(C.c_uint64))  # noqa: E731
-        mi = MergeInput(C.addressof(buf), len(self.data), p64(arrs["off"]), p64(arrs["len"]), p64(arrs["rows"]),
+        mi = MergeInput(base_address, len(self.data), p64(arrs["off"]), p64(arrs["len"]), p64(arrs["rows"]),
                         arrs["codec"].ctypes.data_as(C.POINTER(C.c_uint32)), p64(arrs["first"]),
                         p64(arrs["count"]), 1 if self.min_count is not None else 0,
                         1 if self.max_count is not None else 0, self.min_count or 0, self.max_count or 0)
