@@ -69,6 +69,9 @@ typedef struct {
   uint64_t arena_bytes;      /* FASTQ bytes held on device before a flush (0 = auto) */
   uint32_t timeout_ms;       /* bound on every host-side wait (0 = 600000) */
   void* stream;              /* optional cudaStream_t to run on (NULL = own stream) */
+  uint32_t samples;          /* batched count: samples per segment (0 = 1); see kite_gpu_count_submit_sample */
+  double tile_fill;          /* mean tile load as a fraction of on-chip capacity (0 = 1.0) */
+  int scatter_shape;         /* key-range split scatter launch shape 0..3 (0 = 256 threads x 8 keys) */
 } kite_gpu_cfg;
 
 /* One emitted chunk: the arguments of ConcurrentKiteWriter::append_chunk. */
@@ -143,6 +146,18 @@ int kite_gpu_wait_ticket(kite_gpu_ctx* ctx, int64_t ticket);
  * start must be 16-byte aligned and 16 readable bytes must follow the last
  * chunk.  Used by benchmarks that time the kernels on HBM-resident input. */
 int kite_gpu_count_submit_device(kite_gpu_ctx* ctx, const uint8_t* d_fastq, size_t len);
+
+/* Batched count (no counterpart in the reference, which runs one input per
+ * process): with cfg.samples = S > 1, chunks are queued for sample s < S and
+ * every sample of the segment is counted by one launch sequence.  Keys of
+ * sample s fall in partitions s*cfg.partitions + p (p = the reference's
+ * partition of the key), so the finish emits each sample's partitions as one
+ * contiguous range, ascending; kite_gpu_sample_totals gives each sample's
+ * reads, bases and k-mers of the last finish.  The plain submit calls queue
+ * for sample 0. */
+int64_t kite_gpu_count_submit_sample(kite_gpu_ctx* ctx, uint32_t sample, const uint8_t* fastq, size_t len);
+int kite_gpu_count_submit_device_sample(kite_gpu_ctx* ctx, uint32_t sample, const uint8_t* d_fastq, size_t len);
+int kite_gpu_sample_totals(kite_gpu_ctx* ctx, uint32_t sample, uint64_t totals[3]);
 
 /* Count everything submitted since the last finish: emit one DVLE chunk per
  * non-empty partition (ascending), then reset for the next segment.  With

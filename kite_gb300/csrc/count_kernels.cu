@@ -57,13 +57,15 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
 // Per-block bucket counts: one row of the block x bucket count matrix when
 // the host provides it (no atomics), else global atomics.
 template <int NT, class T>
-__device__ __forceinline__ void flush_hist(const ExtractParams<T>& p, const unsigned* hist, uint32_t P) {
+__device__ __forceinline__ void flush_hist(const ExtractParams<T>& p, const unsigned* hist, uint32_t P,
+                                           uint32_t sample) {
   if (p.blk_counts) {
     unsigned* row = p.blk_counts + (size_t)blockIdx.x * P;
     for (uint32_t b = threadIdx.x; b < P; b += NT) row[b] = hist[b];
   } else {
+    unsigned long long* cnt = p.bucket_count + (size_t)sample * P;
     for (uint32_t b = threadIdx.x; b < P; b += NT)
-      if (hist[b]) atomicAdd(&p.bucket_count[b], (unsigned long long)hist[b]);
+      if (hist[b]) atomicAdd(&cnt[b], (unsigned long long)hist[b]);
   }
 }
 
@@ -98,13 +100,15 @@ __device__ __forceinline__ void flush_totals(CountTotals* tot, unsigned long lon
 // Leaves base[b] = offset (~0 after an overflow) and hist[] zeroed.
 template <int NT, class T>
 __device__ __forceinline__ void reserve_ranges(const ExtractParams<T>& p, unsigned* hist, unsigned long long* base,
-                                               uint32_t P) {
+                                               uint32_t P, const BlockDesc& d) {
+  const size_t g0 = (size_t)d.sample * P;  // this sample's first global bucket
   for (uint32_t b = threadIdx.x; b < P; b += NT) {
     const unsigned h = hist[b];
     unsigned long long r = 0;
-    if (p.blk_offs) r = p.blk_offs[(size_t)blockIdx.x * P + b];
-    else if (h) r = atomicAdd(&p.bucket_fill[b], (unsigned long long)h);
-    if (h && r + h > p.bucket_count[b]) {
+    if (p.blk_offs)  // offset inside the sample's bucket region: this row minus the sample's first row
+      r = p.blk_offs[(size_t)blockIdx.x * P + b] - p.blk_offs[(size_t)d.sample_first * P + b];
+    else if (h) r = atomicAdd(&p.bucket_fill[g0 + b], (unsigned long long)h);
+    if (h && r + h > p.bucket_count[g0 + b]) {
       dev_fail(p.status, KITE_DEV_REGION_OVERFLOW, b, (unsigned)r, h);
       r = ~0ull;
     }
@@ -313,20 +317,20 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
       reads = __popc(seq0 & ~((seq0 << 1) | (seqp >> 31))) + __popc(seq1 & ~((seq1 << 1) | (seq0 >> 31)));
     }
     __syncthreads();
-    flush_hist<NT>(p, hist, P);
-    flush_totals<NT>(p.totals, kmers, reads, bases, reinterpret_cast<unsigned long long*>(scan_sm));
+    flush_hist<NT>(p, hist, P, d.sample);
+    flush_totals<NT>(p.totals + d.sample, kmers, reads, bases, reinterpret_cast<unsigned long long*>(scan_sm));
   } else {
     auto count = [&](uint64_t key, uint32_t) { atomicAdd(&hist[bucket_of(key, shift)], 1u); };
     word_kmers(V0, wp, w0, k, mask, canon, count);
     word_kmers(V1, w0, w1, k, mask, canon, count);
     __syncthreads();
-    reserve_ranges<NT>(p, hist, base, P);
+    reserve_ranges<NT>(p, hist, base, P, d);
     __syncthreads();
     auto write = [&](uint64_t key, uint32_t) {
       const uint32_t b = bucket_of(key, shift);
       const unsigned slot = atomicAdd(&hist[b], 1u);
       const unsigned long long r = base[b];
-      if (r != ~0ull) p.keys_out[p.bucket_off[b] + r + slot] = key;
+      if (r != ~0ull) p.keys_out[p.bucket_off[(size_t)d.sample * P + b] + r + slot] = key;
     };
     word_kmers(V0, wp, w0, k, mask, canon, write);
     word_kmers(V1, w0, w1, k, mask, canon, write);
@@ -463,20 +467,20 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract128(ExtractParams<u1
       reads = __popc(seq0 & ~((seq0 << 1) | (seqp >> 31))) + __popc(seq1 & ~((seq1 << 1) | (seq0 >> 31)));
     }
     __syncthreads();
-    flush_hist<NT>(p, hist, P);
-    flush_totals<NT>(p.totals, kmers, reads, bases, reinterpret_cast<unsigned long long*>(scan_sm));
+    flush_hist<NT>(p, hist, P, d.sample);
+    flush_totals<NT>(p.totals + d.sample, kmers, reads, bases, reinterpret_cast<unsigned long long*>(scan_sm));
   } else {
     auto count = [&](u128 key, uint32_t) { atomicAdd(&hist[bucket_of(key, shift)], 1u); };
     word_kmers128(V0, wq, wp, w0, k, mask, canon, count);
     word_kmers128(V1, wp, w0, w1, k, mask, canon, count);
     __syncthreads();
-    reserve_ranges<NT>(p, hist, base, P);
+    reserve_ranges<NT>(p, hist, base, P, d);
     __syncthreads();
     auto write = [&](u128 key, uint32_t) {
       const uint32_t b = bucket_of(key, shift);
       const unsigned slot = atomicAdd(&hist[b], 1u);
       const unsigned long long r = base[b];
-      if (r != ~0ull) p.keys_out[p.bucket_off[b] + r + slot] = key;
+      if (r != ~0ull) p.keys_out[p.bucket_off[(size_t)d.sample * P + b] + r + slot] = key;
     };
     word_kmers128(V0, wq, wp, w0, k, mask, canon, write);
     word_kmers128(V1, wp, w0, w1, k, mask, canon, write);
@@ -717,8 +721,9 @@ struct BsSmem {
 template <class T>
 __global__ void __launch_bounds__(kBsThreads, 4)
     k_bucket_scatter(const T* __restrict__ keys_stage, const unsigned long long* __restrict__ blk_keys,
-                     const unsigned* __restrict__ blk_offs, const unsigned long long* __restrict__ bucket_off,
-                     uint32_t P, uint32_t shift, T* __restrict__ keys_out) {
+                     const unsigned* __restrict__ blk_offs, const BlockDesc* __restrict__ blocks,
+                     const unsigned long long* __restrict__ bucket_off, uint32_t P, uint32_t shift,
+                     T* __restrict__ keys_out) {
   using L = BsSmem<T>;
   constexpr int NT = kBsThreads, IT = kBsItems;
   extern __shared__ __align__(16) uint8_t sm[];
@@ -732,8 +737,11 @@ __global__ void __launch_bounds__(kBsThreads, 4)
   const uint64_t a = blk_keys[2 * (size_t)blockIdx.x];
   const uint64_t n = blk_keys[2 * (size_t)blockIdx.x + 1];
   if (n == 0) return;
+  const BlockDesc d = blocks[blockIdx.x];
   const unsigned* row = blk_offs + (size_t)blockIdx.x * P;
-  for (uint32_t b = threadIdx.x; b < P; b += NT) cur[b] = bucket_off[b] + row[b];
+  const unsigned* first = blk_offs + (size_t)d.sample_first * P;  // the sample's first block
+  const unsigned long long* boff = bucket_off + (size_t)d.sample * P;
+  for (uint32_t b = threadIdx.x; b < P; b += NT) cur[b] = boff[b] + (row[b] - first[b]);
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned pos0 = (unsigned)wid * 32u * IT + lane;
@@ -769,19 +777,42 @@ __global__ void __launch_bounds__(kBsThreads, 4)
 
 template <class T>
 void launch_bucket_scatter(const T* keys_stage, const unsigned long long* blk_keys, const unsigned* blk_offs,
-                           const unsigned long long* bucket_off, uint32_t partitions, uint32_t shift, uint32_t nblocks,
-                           T* keys_out, cudaStream_t s) {
+                           const BlockDesc* blocks, const unsigned long long* bucket_off, uint32_t partitions,
+                           uint32_t shift, uint32_t nblocks, T* keys_out, cudaStream_t s) {
   const size_t smem = BsSmem<T>::total;
   cudaFuncSetAttribute(k_bucket_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (nblocks)
-    k_bucket_scatter<T><<<nblocks, kBsThreads, smem, s>>>(keys_stage, blk_keys, blk_offs, bucket_off, partitions,
-                                                          shift, keys_out);
+    k_bucket_scatter<T><<<nblocks, kBsThreads, smem, s>>>(keys_stage, blk_keys, blk_offs, blocks, bucket_off,
+                                                          partitions, shift, keys_out);
 }
 template void launch_bucket_scatter<uint64_t>(const uint64_t*, const unsigned long long*, const unsigned*,
-                                              const unsigned long long*, uint32_t, uint32_t, uint32_t, uint64_t*,
-                                              cudaStream_t);
-template void launch_bucket_scatter<u128>(const u128*, const unsigned long long*, const unsigned*,
-                                          const unsigned long long*, uint32_t, uint32_t, uint32_t, u128*, cudaStream_t);
+                                              const BlockDesc*, const unsigned long long*, uint32_t, uint32_t,
+                                              uint32_t, uint64_t*, cudaStream_t);
+template void launch_bucket_scatter<u128>(const u128*, const unsigned long long*, const unsigned*, const BlockDesc*,
+                                          const unsigned long long*, uint32_t, uint32_t, uint32_t, u128*,
+                                          cudaStream_t);
+
+// Batched count: total of bucket b of sample t = the scanned matrix at the
+// next sample's first block (or the column total) minus it at this sample's.
+__global__ void k_sample_bucket_counts(const unsigned* __restrict__ m, const unsigned long long* __restrict__ col_total,
+                                       const uint32_t* __restrict__ sample_first, uint32_t samples, uint32_t P,
+                                       uint32_t nblocks, unsigned long long* __restrict__ bucket_count) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= samples * P) return;
+  const uint32_t t = i / P, b = i % P;
+  const uint32_t f = sample_first[t], nf = sample_first[t + 1];
+  const unsigned long long lo = f < nblocks ? m[(size_t)f * P + b] : col_total[b];
+  const unsigned long long hi = nf < nblocks ? m[(size_t)nf * P + b] : col_total[b];
+  bucket_count[i] = hi - lo;
+}
+
+void launch_sample_bucket_counts(const unsigned* m, const unsigned long long* col_total, const uint32_t* sample_first,
+                                 uint32_t samples, uint32_t partitions, uint32_t nblocks,
+                                 unsigned long long* bucket_count, cudaStream_t s) {
+  const uint32_t n = samples * partitions;
+  if (n) k_sample_bucket_counts<<<(n + 255) / 256, 256, 0, s>>>(m, col_total, sample_first, samples, partitions, nblocks,
+                                                              bucket_count);
+}
 
 // Tile list from the scanned part offsets: tile t = (b, j) starts at
 // off[t*G] and ends where tile t+1 starts (the last at n_keys).
@@ -829,14 +860,9 @@ static void scatter_shape(const TileSplitParams<T>& p, cudaStream_t s) {
   else scatter_with<T, NT, IT, 256>(p, s);
 }
 
-// Launch shape of the scatter (threads x keys per thread); KITE_SCATTER_SHAPE
-// = 0..3 overrides it for tuning.
+// Launch shape of the scatter (threads x keys per thread), 0..3.
 template <class T>
-void launch_split_scatter(const TileSplitParams<T>& p, cudaStream_t s) {
-  static const int shape = [] {
-    const char* e = getenv("KITE_SCATTER_SHAPE");
-    return e ? atoi(e) : 0;
-  }();
+void launch_split_scatter(const TileSplitParams<T>& p, int shape, cudaStream_t s) {
   constexpr int W = sizeof(T) == 8 ? 1 : 2;  // u128 keys: half the keys per thread
   switch (shape) {
     case 1: scatter_shape<T, 256, 16 / W>(p, s); break;
@@ -858,7 +884,7 @@ void launch_region_bounds(const unsigned long long* off, uint32_t nreg, uint32_t
 
 template void launch_split_hist<uint64_t>(const TileSplitParams<uint64_t>&, cudaStream_t);
 template void launch_split_hist<u128>(const TileSplitParams<u128>&, cudaStream_t);
-template void launch_split_scatter<uint64_t>(const TileSplitParams<uint64_t>&, cudaStream_t);
-template void launch_split_scatter<u128>(const TileSplitParams<u128>&, cudaStream_t);
+template void launch_split_scatter<uint64_t>(const TileSplitParams<uint64_t>&, int, cudaStream_t);
+template void launch_split_scatter<u128>(const TileSplitParams<u128>&, int, cudaStream_t);
 
 }  // namespace kite

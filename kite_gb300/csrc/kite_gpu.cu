@@ -82,6 +82,7 @@ struct HostBuf {
 struct Chunk {
   uint64_t off;  // offset from the arena base
   uint64_t len;
+  uint32_t sample;  // batched count: the sample it belongs to
 };
 
 enum Stage { ST_LINES = 0, ST_HIST, ST_SCATTER, ST_SPLIT, ST_SORT, ST_BIG, ST_ENCODE, ST_D2H, ST_COUNT };
@@ -109,12 +110,14 @@ struct kite_gpu_ctx {
   DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, splitters2, hist16;
   DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
   DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats, blk_mat, blk_gsum, blk_keys, stage_ctr;
+  DevBuf col_total, sample_first;
   HostBuf h_blocks, h_small, h_tiles, h_out;
   std::vector<cudaEvent_t> ev;  // stage events
 
   // results of the last finish
   std::vector<BucketMeta> res_meta;
   uint64_t res_bytes = 0;
+  std::vector<uint64_t> sample_totals;  // reads, bases, k-mers per sample of the last finish
   kite_gpu_stats stats{};
   MlpModel* mlp = nullptr;
 };
@@ -191,7 +194,9 @@ void reset_segment(kite_gpu_ctx* ctx) {
 template <class T>
 int run_count(kite_gpu_ctx* ctx) {
   cudaStream_t s = ctx->stream;
-  const uint32_t P = ctx->cfg.partitions;
+  const uint32_t P = ctx->cfg.partitions;                  // per sample
+  const uint32_t NS = ctx->cfg.samples ? ctx->cfg.samples : 1;
+  const uint32_t PT = P * NS;                               // buckets of the segment (sample-major)
   const uint32_t k = (uint32_t)ctx->cfg.k;
   const uint32_t CAP = tile_capacity<T>();
   auto& st = ctx->stats;
@@ -210,13 +215,20 @@ int run_count(kite_gpu_ctx* ctx) {
   while (blk > 1024 && extract_smem_bytes(sizeof(T), blk, P, true) > 200 * 1024) blk >>= 1;
   if (extract_smem_bytes(sizeof(T), blk, P, true) > 220 * 1024)
     return fail(ctx, KITE_ERR_UNSUPPORTED, "partition count too large for the extraction kernel");
+  // blocks in sample order (chunks of one sample keep their submission order)
+  std::vector<size_t> order(ctx->chunks.size());
+  for (size_t c = 0; c < order.size(); ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t a, size_t b) { return ctx->chunks[a].sample < ctx->chunks[b].sample; });
   std::vector<BlockDesc> hb;
+  std::vector<uint32_t> sample_first(NS + 1, 0xFFFFFFFFu);
   uint64_t chunk0_len = 0;
-  for (size_t c = 0; c < ctx->chunks.size(); ++c) {
+  for (size_t c : order) {
     const Chunk& ch = ctx->chunks[c];
     if (ch.len == 0) continue;
     const uint32_t first = (uint32_t)hb.size();
     if (hb.empty()) chunk0_len = ch.len;
+    if (sample_first[ch.sample] == 0xFFFFFFFFu) sample_first[ch.sample] = first;
     for (uint64_t o = 0; o < ch.len; o += blk) {
       BlockDesc d;
       d.start = ch.off + o;
@@ -224,12 +236,19 @@ int run_count(kite_gpu_ctx* ctx) {
       d.chunk_start = ch.off;
       d.first_block = first;
       d.flags = (first == 0) ? 2u : 0u;
+      d.sample = ch.sample;
+      d.sample_first = sample_first[ch.sample];
       hb.push_back(d);
     }
   }
   const uint32_t nblocks = (uint32_t)hb.size();
+  // samples without blocks start where the next one does
+  sample_first[NS] = nblocks;
+  for (int t = (int)NS - 1; t >= 0; --t)
+    if (sample_first[t] == 0xFFFFFFFFu) sample_first[t] = sample_first[t + 1];
+  ctx->sample_totals.assign((size_t)NS * 3, 0);
   if (nblocks == 0) {
-    ctx->res_meta.assign(P, BucketMeta{});
+    ctx->res_meta.assign(PT, BucketMeta{});
     ctx->res_bytes = 0;
     return KITE_OK;
   }
@@ -238,7 +257,7 @@ int run_count(kite_gpu_ctx* ctx) {
   KCU(ctx->blocks.ensure(hb.size() * sizeof(BlockDesc)));
   KCU(cudaMemcpyAsync(ctx->blocks.p, ctx->h_blocks.p, hb.size() * sizeof(BlockDesc), cudaMemcpyHostToDevice, s));
   KCU(ctx->nl.ensure((size_t)nblocks * 8));
-  KCU(ctx->scan_tmp.ensure(scan_tmp_elems(std::max<size_t>((size_t)nblocks, (size_t)P * 4096)) * 8 + 64));
+  KCU(ctx->scan_tmp.ensure(scan_tmp_elems(std::max<size_t>((size_t)nblocks, (size_t)PT * 4096)) * 8 + 64));
   KCU(ctx->status.ensure(sizeof(DevStatus)));
   KCU(cudaMemsetAsync(ctx->status.p, 0, sizeof(DevStatus), s));
   const uint8_t* base = arena_base(ctx);
@@ -249,12 +268,12 @@ int run_count(kite_gpu_ctx* ctx) {
 
   // ---- K2 histogram pass --------------------------------------------------
   const uint32_t sample_cap = 1u << 20;
-  KCU(ctx->bucket_count.ensure((size_t)P * 8));
-  KCU(ctx->totals.ensure(sizeof(CountTotals)));
+  KCU(ctx->bucket_count.ensure((size_t)PT * 8));
+  KCU(ctx->totals.ensure(NS * sizeof(CountTotals)));
   KCU(ctx->sample.ensure((size_t)sample_cap * sizeof(T)));
   KCU(ctx->sample_count.ensure(8));
-  KCU(cudaMemsetAsync(ctx->bucket_count.p, 0, (size_t)P * 8, s));
-  KCU(cudaMemsetAsync(ctx->totals.p, 0, sizeof(CountTotals), s));
+  KCU(cudaMemsetAsync(ctx->bucket_count.p, 0, (size_t)PT * 8, s));
+  KCU(cudaMemsetAsync(ctx->totals.p, 0, NS * sizeof(CountTotals), s));
   KCU(cudaMemsetAsync(ctx->sample_count.p, 0, 8, s));
   // keep ~2^20 of the first chunk's k-mer positions (about one k-mer per 2.5 bytes)
   uint64_t est = std::max<uint64_t>(chunk0_len * 2 / 5, 1);
@@ -306,56 +325,75 @@ int run_count(kite_gpu_ctx* ctx) {
   }
   launch_extract_hist<T>(ep, nblocks, s);
   st.kernel_launches += 1;
-  if (use_matrix)
+  if (use_matrix) {
+    // column totals straight into the bucket counts for one sample; per
+    // (sample, bucket) totals from the sample boundaries for a batch
+    KCU(ctx->col_total.ensure((size_t)P * 8));
     st.kernel_launches += count_matrix_offsets(ctx->blk_mat.as<unsigned>(), nblocks, P,
                                                ctx->blk_gsum.as<unsigned long long>(),
-                                               ctx->bucket_count.as<unsigned long long>(), s);
+                                               NS == 1 ? ctx->bucket_count.as<unsigned long long>()
+                                                       : ctx->col_total.as<unsigned long long>(), s);
+    if (NS > 1) {
+      KCU(ctx->sample_first.ensure((NS + 1) * 4));
+      KCU(cudaMemcpyAsync(ctx->sample_first.p, sample_first.data(), (NS + 1) * 4, cudaMemcpyHostToDevice, s));
+      launch_sample_bucket_counts(ctx->blk_mat.as<unsigned>(), ctx->col_total.as<unsigned long long>(),
+                                  ctx->sample_first.as<uint32_t>(), NS, P, nblocks,
+                                  ctx->bucket_count.as<unsigned long long>(), s);
+      st.kernel_launches += 1;
+    }
+  }
   KCU(cudaGetLastError());
   KCU(cudaEventRecord(ctx->ev[2], s));
 
   // bring bucket counts, totals and the sample count to the host
-  const size_t small_bytes = (size_t)P * 8 + sizeof(CountTotals) + 8;
-  KCU(ctx->h_small.ensure(small_bytes + 8 + (size_t)P * 8));
+  // host copies: bucket counts, per-sample totals, sample count, staged keys
+  const size_t o_tot = (size_t)PT * 8, o_ns = o_tot + NS * sizeof(CountTotals), o_stg = o_ns + 8;
+  const size_t small_bytes = o_stg + 8;
+  KCU(ctx->h_small.ensure(small_bytes + (size_t)PT * 8));
   uint8_t* hs = ctx->h_small.as<uint8_t>();
-  KCU(cudaMemcpyAsync(hs, ctx->bucket_count.p, (size_t)P * 8, cudaMemcpyDeviceToHost, s));
-  KCU(cudaMemcpyAsync(hs + (size_t)P * 8, ctx->totals.p, sizeof(CountTotals), cudaMemcpyDeviceToHost, s));
-  KCU(cudaMemcpyAsync(hs + (size_t)P * 8 + sizeof(CountTotals), ctx->sample_count.p, 4, cudaMemcpyDeviceToHost, s));
-  if (stage_keys)
-    KCU(cudaMemcpyAsync(hs + (size_t)P * 8 + sizeof(CountTotals) + 8, ctx->stage_ctr.p, 8, cudaMemcpyDeviceToHost, s));
+  KCU(cudaMemcpyAsync(hs, ctx->bucket_count.p, (size_t)PT * 8, cudaMemcpyDeviceToHost, s));
+  KCU(cudaMemcpyAsync(hs + o_tot, ctx->totals.p, NS * sizeof(CountTotals), cudaMemcpyDeviceToHost, s));
+  KCU(cudaMemcpyAsync(hs + o_ns, ctx->sample_count.p, 4, cudaMemcpyDeviceToHost, s));
+  if (stage_keys) KCU(cudaMemcpyAsync(hs + o_stg, ctx->stage_ctr.p, 8, cudaMemcpyDeviceToHost, s));
   int rc = wait_stream(ctx, s);
   if (rc) return rc;
   uint64_t staged = ~0ull;
-  if (stage_keys) std::memcpy(&staged, hs + (size_t)P * 8 + sizeof(CountTotals) + 8, 8);
-  std::vector<uint64_t> bcount(P);
-  std::memcpy(bcount.data(), hs, (size_t)P * 8);
-  CountTotals tot;
-  std::memcpy(&tot, hs + (size_t)P * 8, sizeof tot);
+  if (stage_keys) std::memcpy(&staged, hs + o_stg, 8);
+  std::vector<uint64_t> bcount(PT);
+  std::memcpy(bcount.data(), hs, (size_t)PT * 8);
+  std::vector<CountTotals> tot(NS);
+  std::memcpy(tot.data(), hs + o_tot, NS * sizeof(CountTotals));
   uint32_t nsample = 0;
-  std::memcpy(&nsample, hs + (size_t)P * 8 + sizeof(CountTotals), 4);
+  std::memcpy(&nsample, hs + o_ns, 4);
   nsample = std::min(nsample, sample_cap);
-  st.reads = tot.reads;
-  st.bases = tot.bases;
-  st.kmers = tot.kmers;
-  const uint64_t N = tot.kmers;
+  for (uint32_t t = 0; t < NS; ++t) {
+    st.reads += tot[t].reads;
+    st.bases += tot[t].bases;
+    st.kmers += tot[t].kmers;
+    ctx->sample_totals[3 * t] = tot[t].reads;
+    ctx->sample_totals[3 * t + 1] = tot[t].bases;
+    ctx->sample_totals[3 * t + 2] = tot[t].kmers;
+  }
+  const uint64_t N = st.kmers;
   if (N == 0) {
-    ctx->res_meta.assign(P, BucketMeta{});
+    ctx->res_meta.assign(PT, BucketMeta{});
     ctx->res_bytes = 0;
     return KITE_OK;
   }
 
   // ---- K3 scatter pass ----------------------------------------------------
-  std::vector<uint64_t> boff(P);
+  std::vector<uint64_t> boff(PT);
   uint64_t acc = 0, maxb = 0;
-  for (uint32_t b = 0; b < P; ++b) {
+  for (uint32_t b = 0; b < PT; ++b) {
     boff[b] = acc;
     acc += bcount[b];
     maxb = std::max(maxb, bcount[b]);
   }
-  std::memcpy(hs + small_bytes, boff.data(), (size_t)P * 8);
-  KCU(ctx->bucket_off.ensure((size_t)P * 8));
-  KCU(ctx->bucket_fill.ensure((size_t)P * 8));
-  KCU(cudaMemcpyAsync(ctx->bucket_off.p, hs + small_bytes, (size_t)P * 8, cudaMemcpyHostToDevice, s));
-  KCU(cudaMemsetAsync(ctx->bucket_fill.p, 0, (size_t)P * 8, s));
+  std::memcpy(hs + small_bytes, boff.data(), (size_t)PT * 8);
+  KCU(ctx->bucket_off.ensure((size_t)PT * 8));
+  KCU(ctx->bucket_fill.ensure((size_t)PT * 8));
+  KCU(cudaMemcpyAsync(ctx->bucket_off.p, hs + small_bytes, (size_t)PT * 8, cudaMemcpyHostToDevice, s));
+  KCU(cudaMemsetAsync(ctx->bucket_fill.p, 0, (size_t)PT * 8, s));
   KCU(ctx->keys_a.ensure(N * sizeof(T)));
   KCU(ctx->keys_b.ensure(N * sizeof(T)));
   KCU(ctx->counts.ensure(N * 4));
@@ -367,7 +405,8 @@ int run_count(kite_gpu_ctx* ctx) {
   if (stage_keys && ep.blk_offs && staged == N && N <= stage_cap) {
     st.staged_scatter = 1;
     launch_bucket_scatter<T>(ctx->keys_b.as<T>(), ctx->blk_keys.as<unsigned long long>(), ep.blk_offs,
-                             ctx->bucket_off.as<unsigned long long>(), P, ep.shift, nblocks, ctx->keys_a.as<T>(), s);
+                             ctx->blocks.as<BlockDesc>(), ctx->bucket_off.as<unsigned long long>(), P, ep.shift,
+                             nblocks, ctx->keys_a.as<T>(), s);
   } else {
     ep.keys_stage = nullptr;
     launch_extract_scatter<T>(ep, nblocks, s);
@@ -377,13 +416,8 @@ int run_count(kite_gpu_ctx* ctx) {
   KCU(cudaEventRecord(ctx->ev[3], s));
 
   // ---- K3b tile split -----------------------------------------------------
-  // target mean tile load as a fraction of on-chip capacity; KITE_TILE_FILL
-  // overrides it for tuning
-  static const double fill = [] {
-    const char* e = getenv("KITE_TILE_FILL");
-    const double v = e ? atof(e) : 0.0;
-    return v > 0.05 && v <= 4.0 ? v : 1.0;
-  }();
+  // target mean tile load as a fraction of on-chip capacity (cfg.tile_fill)
+  const double fill = std::min(4.0, std::max(0.05, ctx->cfg.tile_fill));
   uint32_t S = 1;
   while ((double)maxb / S > fill * CAP && S < 4096) S <<= 1;
   st.tiles_per_bucket = S;
@@ -391,7 +425,7 @@ int run_count(kite_gpu_ctx* ctx) {
   T* scratch = ctx->keys_b.as<T>();
   std::vector<TileDesc> ht;
   if (S == 1) {
-    for (uint32_t b = 0; b < P; ++b) ht.push_back(TileDesc{boff[b], (uint32_t)bcount[b], b});
+    for (uint32_t b = 0; b < PT; ++b) ht.push_back(TileDesc{boff[b], (uint32_t)bcount[b], b});
   } else {
     // Splitters: SAMPLED = histogram only; LEARNED = train the CDF, keep it
     // unless its predicted max/mean tile load exceeds imbalance_bound (then the
@@ -442,7 +476,7 @@ int run_count(kite_gpu_ctx* ctx) {
     };
     const uint32_t D2 = std::min<uint32_t>(S, 256), D1 = S / D2;
     st.split_levels = D1 > 1 ? 2 : 1;
-    const size_t nt = (size_t)P * S;
+    const size_t nt = (size_t)PT * S;
     TileSplitParams<T> tp{};
     tp.splitters = chosen;
     tp.spl_total = S - 1;
@@ -454,19 +488,19 @@ int run_count(kite_gpu_ctx* ctx) {
     T* level_out = ctx->keys_b.as<T>();
     if (D1 > 1) {
       // level 1: buckets -> (bucket, coarse range); coarse splitter c is tile splitter (c+1)*D2-1
-      const uint32_t G1 = parts(P, maxb);
-      const size_t n1 = (size_t)P * D1 * G1;
+      const uint32_t G1 = parts(PT, maxb);
+      const size_t n1 = (size_t)PT * D1 * G1;
       KCU(ctx->lvl_count.ensure(n1 * 8));
       KCU(ctx->lvl_off.ensure(n1 * 8));
-      KCU(ctx->reg_off.ensure((size_t)P * D1 * 8));
-      KCU(ctx->reg_cnt.ensure((size_t)P * D1 * 8));
+      KCU(ctx->reg_off.ensure((size_t)PT * D1 * 8));
+      KCU(ctx->reg_cnt.ensure((size_t)PT * D1 * 8));
       KCU(ctx->scan_tmp.ensure(scan_tmp_elems(n1) * 8 + 64));
       TileSplitParams<T> t1 = tp;
       t1.keys_in = level_in;
       t1.keys_out = level_out;
       t1.region_off = ctx->bucket_off.as<unsigned long long>();
       t1.region_count = ctx->bucket_count.as<unsigned long long>();
-      t1.R = P;
+      t1.R = PT;
       t1.D = D1;
       t1.G = G1;
       t1.spl_first = D2 - 1;
@@ -477,23 +511,23 @@ int run_count(kite_gpu_ctx* ctx) {
       launch_split_hist<T>(t1, s);
       st.kernel_launches += 3 + exclusive_scan_u64(t1.tile_count, ctx->lvl_off.as<unsigned long long>(), n1,
                                                    ctx->scan_tmp.as<unsigned long long>(), s);
-      launch_split_scatter<T>(t1, s);
-      launch_region_bounds(t1.tile_off, P * D1, G1, N, ctx->reg_off.as<unsigned long long>(),
+      launch_split_scatter<T>(t1, ctx->cfg.scatter_shape, s);
+      launch_region_bounds(t1.tile_off, PT * D1, G1, N, ctx->reg_off.as<unsigned long long>(),
                            ctx->reg_cnt.as<unsigned long long>(), s);
       // level 2: (bucket, coarse c) -> tiles c*D2 .. c*D2+D2-1
-      G = parts((uint64_t)P * D1, (maxb + D1 - 1) / D1 * 2);
+      G = parts((uint64_t)PT * D1, (maxb + D1 - 1) / D1 * 2);
       tp.region_off = ctx->reg_off.as<unsigned long long>();
       tp.region_count = ctx->reg_cnt.as<unsigned long long>();
-      tp.R = P * D1;
+      tp.R = PT * D1;
       tp.spl_first = 0;
       tp.spl_mod = D1;
       tp.spl_region_stride = D2;
       std::swap(level_in, level_out);
     } else {
-      G = parts(P, maxb);
+      G = parts(PT, maxb);
       tp.region_off = ctx->bucket_off.as<unsigned long long>();
       tp.region_count = ctx->bucket_count.as<unsigned long long>();
-      tp.R = P;
+      tp.R = PT;
       tp.spl_first = 0;
       tp.spl_region_stride = 0;
     }
@@ -510,7 +544,7 @@ int run_count(kite_gpu_ctx* ctx) {
     launch_split_hist<T>(tp, s);
     st.kernel_launches += 3 + exclusive_scan_u64(tp.tile_count, ctx->tile_off.as<unsigned long long>(), ntg,
                                                  ctx->scan_tmp.as<unsigned long long>(), s);
-    launch_split_scatter<T>(tp, s);
+    launch_split_scatter<T>(tp, ctx->cfg.scatter_shape, s);
     KCU(ctx->tiles.ensure(nt * sizeof(TileDesc)));
     KCU(ctx->tile_fill.ensure(nt * 4));
     launch_make_tiles(ctx->tile_off.as<unsigned long long>(), (uint32_t)nt, S, G, N, ctx->tiles.as<TileDesc>(),
@@ -582,15 +616,15 @@ int run_count(kite_gpu_ctx* ctx) {
   KCU(cudaEventRecord(ctx->ev[6], s));
 
   // ---- K7 DVLE encode -------------------------------------------------------
-  const uint32_t Sl = ntiles / P;
+  const uint32_t Sl = ntiles / PT;
   KCU(ctx->tile_boff.ensure((size_t)ntiles * 8));
   KCU(ctx->tile_prev.ensure((size_t)ntiles * sizeof(T)));
-  KCU(ctx->meta.ensure((size_t)P * sizeof(BucketMeta)));
-  launch_tile_link<T>(ctx->tile_out.as<TileOut<T>>(), P, Sl, ctx->tile_boff.as<unsigned long long>(),
+  KCU(ctx->meta.ensure((size_t)PT * sizeof(BucketMeta)));
+  launch_tile_link<T>(ctx->tile_out.as<TileOut<T>>(), PT, Sl, ctx->tile_boff.as<unsigned long long>(),
                       ctx->tile_prev.as<T>(), ctx->meta.as<BucketMeta>(), s);
-  launch_bucket_offsets(ctx->meta.as<BucketMeta>(), P, nullptr, s);
-  ctx->res_meta.resize(P);
-  KCU(cudaMemcpyAsync(ctx->res_meta.data(), ctx->meta.p, (size_t)P * sizeof(BucketMeta), cudaMemcpyDeviceToHost, s));
+  launch_bucket_offsets(ctx->meta.as<BucketMeta>(), PT, nullptr, s);
+  ctx->res_meta.resize(PT);
+  KCU(cudaMemcpyAsync(ctx->res_meta.data(), ctx->meta.p, (size_t)PT * sizeof(BucketMeta), cudaMemcpyDeviceToHost, s));
   KCU(cudaMemcpyAsync(ctx->h_small.p, ctx->sort_stats.p, 8, cudaMemcpyDeviceToHost, s));
   rc = wait_stream(ctx, s);
   if (rc) return rc;
@@ -599,7 +633,7 @@ int run_count(kite_gpu_ctx* ctx) {
   rc = check_status(ctx, "count");
   if (rc) return rc;
   uint64_t total_bytes = 0, rows = 0;
-  for (uint32_t b = 0; b < P; ++b) {
+  for (uint32_t b = 0; b < PT; ++b) {
     total_bytes += ctx->res_meta[b].bytes;
     rows += ctx->res_meta[b].rows;
   }
@@ -702,6 +736,12 @@ int kite_gpu_open(const kite_gpu_cfg* cfg, kite_gpu_ctx** out) {
   ctx->cfg = *cfg;
   if (ctx->cfg.timeout_ms == 0) ctx->cfg.timeout_ms = 600000;
   if (ctx->cfg.imbalance_bound <= 0) ctx->cfg.imbalance_bound = 1.10;
+  if (ctx->cfg.samples == 0) ctx->cfg.samples = 1;
+  if ((uint64_t)ctx->cfg.samples * ctx->cfg.partitions > (1u << 20)) {
+    delete ctx;
+    return KITE_ERR_BAD_INPUT;
+  }
+  if (ctx->cfg.tile_fill <= 0) ctx->cfg.tile_fill = 1.0;
   if (cfg->stream) {
     ctx->stream = (cudaStream_t)cfg->stream;
   } else {
@@ -739,7 +779,8 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
                     &ctx->tile_count, &ctx->tile_off, &ctx->tile_fill, &ctx->tiles, &ctx->big_ids,
                     &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out,
                     &ctx->lvl_count, &ctx->lvl_off, &ctx->reg_off, &ctx->reg_cnt, &ctx->sort_stats,
-                    &ctx->blk_mat, &ctx->blk_gsum, &ctx->blk_keys, &ctx->stage_ctr};
+                    &ctx->blk_mat, &ctx->blk_gsum, &ctx->blk_keys, &ctx->stage_ctr,
+                    &ctx->col_total, &ctx->sample_first};
   for (DevBuf* b : bufs) b->release();
   ctx->h_blocks.release();
   ctx->h_small.release();
@@ -751,8 +792,10 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
   delete ctx;
 }
 
-int64_t kite_gpu_count_submit(kite_gpu_ctx* ctx, const uint8_t* fastq, size_t len) {
+int64_t kite_gpu_count_submit_sample(kite_gpu_ctx* ctx, uint32_t sample, const uint8_t* fastq, size_t len) {
   if (!ctx || (!fastq && len)) return KITE_ERR_BAD_INPUT;
+  if (sample >= (ctx->cfg.samples ? ctx->cfg.samples : 1u))
+    return fail(ctx, KITE_ERR_BAD_INPUT, "sample index beyond cfg.samples");
   if (ctx->ext_mode) return fail(ctx, KITE_ERR_STATE, "host and device submissions cannot mix in one segment");
   if (len == 0) return ctx->next_ticket++;
   const uint64_t off = (ctx->arena_used + 15) & ~15ull;
@@ -788,7 +831,7 @@ int64_t kite_gpu_count_submit(kite_gpu_ctx* ctx, const uint8_t* fastq, size_t le
   KCU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   KCU(cudaEventRecord(e, ctx->copy_stream));
   ctx->ticket_events.push_back(e);
-  ctx->chunks.push_back(Chunk{off, len});
+  ctx->chunks.push_back(Chunk{off, len, sample});
   ctx->arena_used = off + len;
   ctx->stats.h2d_bytes += len;
   return ctx->next_ticket++;
@@ -802,8 +845,14 @@ int kite_gpu_wait_ticket(kite_gpu_ctx* ctx, int64_t ticket) {
   return wait_stream(ctx, ctx->copy_stream);
 }
 
-int kite_gpu_count_submit_device(kite_gpu_ctx* ctx, const uint8_t* d_fastq, size_t len) {
+int64_t kite_gpu_count_submit(kite_gpu_ctx* ctx, const uint8_t* fastq, size_t len) {
+  return kite_gpu_count_submit_sample(ctx, 0, fastq, len);
+}
+
+int kite_gpu_count_submit_device_sample(kite_gpu_ctx* ctx, uint32_t sample, const uint8_t* d_fastq, size_t len) {
   if (!ctx || (!d_fastq && len)) return KITE_ERR_BAD_INPUT;
+  if (sample >= (ctx->cfg.samples ? ctx->cfg.samples : 1u))
+    return fail(ctx, KITE_ERR_BAD_INPUT, "sample index beyond cfg.samples");
   if (!ctx->ext_mode && !ctx->chunks.empty())
     return fail(ctx, KITE_ERR_STATE, "host and device submissions cannot mix in one segment");
   if (((uintptr_t)d_fastq) & 15) return fail(ctx, KITE_ERR_BAD_INPUT, "device chunk must be 16-byte aligned");
@@ -813,7 +862,18 @@ int kite_gpu_count_submit_device(kite_gpu_ctx* ctx, const uint8_t* d_fastq, size
     ctx->ext_base = d_fastq;
   }
   if (d_fastq < ctx->ext_base) return fail(ctx, KITE_ERR_BAD_INPUT, "device chunks must not precede the first one");
-  ctx->chunks.push_back(Chunk{(uint64_t)(d_fastq - ctx->ext_base), len});
+  ctx->chunks.push_back(Chunk{(uint64_t)(d_fastq - ctx->ext_base), len, sample});
+  return KITE_OK;
+}
+
+int kite_gpu_count_submit_device(kite_gpu_ctx* ctx, const uint8_t* d_fastq, size_t len) {
+  return kite_gpu_count_submit_device_sample(ctx, 0, d_fastq, len);
+}
+
+int kite_gpu_sample_totals(kite_gpu_ctx* ctx, uint32_t sample, uint64_t* totals) {
+  if (!ctx || !totals) return KITE_ERR_BAD_INPUT;
+  if ((size_t)sample * 3 + 3 > ctx->sample_totals.size()) return fail(ctx, KITE_ERR_BAD_INPUT, "no such sample in the last finish");
+  for (int i = 0; i < 3; ++i) totals[i] = ctx->sample_totals[(size_t)sample * 3 + i];
   return KITE_OK;
 }
 

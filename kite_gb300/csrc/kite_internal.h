@@ -12,11 +12,13 @@ namespace kite {
 
 // One extraction work block: a byte range of one submitted chunk.
 struct BlockDesc {
-  uint64_t start;        // first byte (arena offset), 16-byte aligned
-  uint64_t end;          // one past the last byte
-  uint64_t chunk_start;  // arena offset of the chunk's first byte
-  uint32_t first_block;  // index of the chunk's first block
-  uint32_t flags;        // bit 1: block of the segment's first chunk (key sample source)
+  uint64_t start;         // first byte (arena offset), 16-byte aligned
+  uint64_t end;           // one past the last byte
+  uint64_t chunk_start;   // arena offset of the chunk's first byte
+  uint32_t first_block;   // index of the chunk's first block
+  uint32_t flags;         // bit 1: block of the segment's first chunk (key sample source)
+  uint32_t sample;        // sample of a batched count (0 otherwise): its buckets are sample*P .. sample*P+P-1
+  uint32_t sample_first;  // index of the sample's first block (blocks of a sample are contiguous)
 };
 
 // A key-range tile: the on-chip sort unit.
@@ -47,11 +49,11 @@ struct ExtractParams {
   uint32_t k;
   uint32_t canonical;
   uint32_t shift;        // 64 - log2(partitions)
-  uint32_t partitions;
+  uint32_t partitions;   // per sample; global bucket arrays hold samples * partitions entries
   uint32_t blk_bytes;
   // histogram pass
-  unsigned long long* bucket_count;  // [partitions]
-  CountTotals* totals;
+  unsigned long long* bucket_count;  // [samples * partitions]
+  CountTotals* totals;               // [samples]
   T* sample;                         // may be null
   unsigned int* sample_count;
   uint32_t sample_cap;
@@ -109,12 +111,17 @@ void launch_extract_scatter(const ExtractParams<T>& p, uint32_t nblocks, cudaStr
 // onwards, ranked on chip so that writes are coalesced.
 template <class T>
 void launch_bucket_scatter(const T* keys_stage, const unsigned long long* blk_keys, const unsigned* blk_offs,
-                           const unsigned long long* bucket_off, uint32_t partitions, uint32_t shift, uint32_t nblocks,
-                           T* keys_out, cudaStream_t s);
+                           const BlockDesc* blocks, const unsigned long long* bucket_off, uint32_t partitions,
+                           uint32_t shift, uint32_t nblocks, T* keys_out, cudaStream_t s);
+// Batched count: bucket totals of every (sample, bucket) from the scanned
+// count matrix m (rows = blocks, cols = partitions), col_total = column sums.
+void launch_sample_bucket_counts(const unsigned* m, const unsigned long long* col_total, const uint32_t* sample_first,
+                                 uint32_t samples, uint32_t partitions, uint32_t nblocks,
+                                 unsigned long long* bucket_count, cudaStream_t s);
 template <class T>
 void launch_split_hist(const TileSplitParams<T>& p, cudaStream_t s);
 template <class T>
-void launch_split_scatter(const TileSplitParams<T>& p, cudaStream_t s);
+void launch_split_scatter(const TileSplitParams<T>& p, int shape, cudaStream_t s);  // shape 0..3: threads x keys
 void launch_make_tiles(const unsigned long long* off, uint32_t ntiles, uint32_t S, uint32_t G,
                        unsigned long long n_keys, TileDesc* tiles, uint32_t* lens, cudaStream_t s);
 void launch_region_bounds(const unsigned long long* off, uint32_t nreg, uint32_t G, unsigned long long n_keys,

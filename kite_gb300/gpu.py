@@ -27,7 +27,8 @@ EXPORTED = [
     "kite_gpu_abi_version", "kite_gpu_device_count", "kite_gpu_open", "kite_gpu_close", "kite_gpu_last_error",
     "kite_gpu_alloc_pinned", "kite_gpu_free_pinned", "kite_gpu_count_submit", "kite_gpu_wait_ticket",
     "kite_gpu_count_submit_device", "kite_gpu_count_finish", "kite_gpu_result_partition", "kite_gpu_merge",
-    "kite_gpu_get_stats", "kite_gpu_synchronize",
+    "kite_gpu_get_stats", "kite_gpu_synchronize", "kite_gpu_count_submit_sample",
+    "kite_gpu_count_submit_device_sample", "kite_gpu_sample_totals",
 ]
 
 
@@ -40,7 +41,8 @@ class KiteGpuError(RuntimeError):
 class Cfg(C.Structure):
     _fields_ = [("device", C.c_int), ("k", C.c_int), ("canonical", C.c_int), ("partitions", C.c_uint32),
                 ("splitter_mode", C.c_int), ("imbalance_bound", C.c_double), ("arena_bytes", C.c_uint64),
-                ("timeout_ms", C.c_uint32), ("stream", C.c_void_p)]
+                ("timeout_ms", C.c_uint32), ("stream", C.c_void_p), ("samples", C.c_uint32),
+                ("tile_fill", C.c_double), ("scatter_shape", C.c_int)]
 
 
 class ChunkMeta(C.Structure):
@@ -100,6 +102,10 @@ def lib() -> C.CDLL:
         L.kite_gpu_wait_ticket.argtypes = [C.c_void_p, C.c_int64]
         L.kite_gpu_count_submit_device.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
         L.kite_gpu_count_finish.argtypes = [C.c_void_p, EMIT, C.c_void_p]
+        L.kite_gpu_count_submit_sample.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t]
+        L.kite_gpu_count_submit_sample.restype = C.c_int64
+        L.kite_gpu_count_submit_device_sample.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t]
+        L.kite_gpu_sample_totals.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64)]
         L.kite_gpu_result_partition.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(ChunkMeta),
                                                 C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
         L.kite_gpu_merge.argtypes = [C.c_void_p, C.POINTER(MergeInput), C.c_int, EMIT, C.c_void_p]
@@ -118,10 +124,11 @@ class Counter:
 
     def __init__(self, k: int, canonical: bool, partitions: int, device: int = 0,
                  splitter_mode: int = SPLIT_AUTO, imbalance_bound: float = 1.10, arena_bytes: int = 0,
-                 timeout_ms: int = 0, stream: int | None = None):
+                 timeout_ms: int = 0, stream: int | None = None, samples: int = 1, tile_fill: float = 0.0,
+                 scatter_shape: int = 0):
         self._L = lib()
         cfg = Cfg(device, k, 1 if canonical else 0, partitions, splitter_mode, imbalance_bound, arena_bytes,
-                  timeout_ms, C.c_void_p(stream) if stream else None)
+                  timeout_ms, C.c_void_p(stream) if stream else None, samples, tile_fill, scatter_shape)
         h = C.c_void_p()
         rc = self._L.kite_gpu_open(C.byref(cfg), C.byref(h))
         if rc != KITE_OK:
@@ -153,8 +160,18 @@ class Counter:
     def wait(self, ticket: int) -> None:
         self._check(self._L.kite_gpu_wait_ticket(self._h, ticket))
 
-    def submit_device(self, ptr: int, n: int) -> None:
-        self._check(self._L.kite_gpu_count_submit_device(self._h, C.c_void_p(ptr), n))
+    def submit_device(self, ptr: int, n: int, sample: int = 0) -> None:
+        self._check(self._L.kite_gpu_count_submit_device_sample(self._h, sample, C.c_void_p(ptr), n))
+
+    def submit_sample(self, sample: int, ptr: int, n: int) -> int:
+        """Queue n bytes at host address ptr for `sample` of a batched count."""
+        return self._check(self._L.kite_gpu_count_submit_sample(self._h, sample, C.c_void_p(ptr), n))
+
+    def sample_totals(self, sample: int) -> tuple:
+        """(reads, bases, k-mers) of `sample` in the last finish."""
+        out = (C.c_uint64 * 3)()
+        self._check(self._L.kite_gpu_sample_totals(self._h, sample, out))
+        return tuple(int(x) for x in out)
 
     def finish(self, collect: bool = True, callback=None, raw: bool = False) -> list:
         """Count the segment; returns [(meta dict, payload bytes)] per non-empty
