@@ -626,10 +626,10 @@ __global__ void __launch_bounds__(kSplitThreads) k_split_hist(TileSplitParams<T>
 }
 
 // Scatter of one part, a batch of BATCH keys at a time: the batch is ranked on
-// chip by digit (stable warp-match ranking over RADIX >= D digits), staged in
-// digit order, and each digit's run is written to its destination with
-// consecutive threads on consecutive addresses, so global writes go out as
-// whole sectors.
+// chip by digit (shared-memory atomics over RADIX >= D digits; key order inside
+// a tile does not matter), staged in digit order, and each digit's run is
+// written to its destination with consecutive threads on consecutive
+// addresses, so global writes go out as whole sectors.
 template <class T, int NT_, int IT_, int RADIX_>
 struct ScatterSmem {
   static constexpr int NT = NT_, NW = NT / 32, IT = IT_, RADIX = RADIX_;
@@ -663,6 +663,7 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
   const uint32_t D = p.D, G = p.G;
   const uint32_t r = blockIdx.x / G, g = blockIdx.x % G;
   for (uint32_t d = threadIdx.x; d < D; d += NT) cur[d] = p.tile_off[((size_t)r * D + d) * G + g];
+  for (int d = threadIdx.x; d < RADIX; d += NT) whist[d] = 0;  // rank counters
   T lo;
   uint32_t sh;
   load_digits(p, r, spl, lut, &lo, &sh);
@@ -683,7 +684,7 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
     }
 #pragma unroll
     for (int q = 0; q < IT; ++q) dg[q] = valid[q] ? digit_of_key(spl, lut, lo, sh, key[q]) : 0u;
-    block_rank<NT, IT, RADIX>(dg, valid, dest, whist, scan_sm, dtot, dstart);
+    atomic_rank<NT, IT, RADIX>(dg, valid, dest, whist, scan_sm, dtot, dstart);
 #pragma unroll
     for (int q = 0; q < IT; ++q)
       if (valid[q]) {
@@ -702,8 +703,9 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
 }
 
 // Bucket scatter of staged keys, one CTA per extraction block: batches of
-// BATCH keys ranked on chip by partition (stable warp-match ranking), staged in
-// partition order and written as runs at the block's offsets.
+// BATCH keys ranked on chip by partition (shared-memory atomics; order inside a
+// partition does not matter), staged in partition order and written as runs at
+// the block's offsets.
 constexpr int kBsThreads = 256, kBsItems = 8, kBsBatch = kBsThreads * kBsItems;
 template <class T>
 struct BsSmem {
@@ -742,6 +744,7 @@ __global__ void __launch_bounds__(kBsThreads, 4)
   const unsigned* first = blk_offs + (size_t)d.sample_first * P;  // the sample's first block
   const unsigned long long* boff = bucket_off + (size_t)d.sample * P;
   for (uint32_t b = threadIdx.x; b < P; b += NT) cur[b] = boff[b] + (row[b] - first[b]);
+  for (int b = threadIdx.x; b < 256; b += NT) whist[b] = 0;  // rank counters
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned pos0 = (unsigned)wid * 32u * IT + lane;
@@ -757,7 +760,7 @@ __global__ void __launch_bounds__(kBsThreads, 4)
       key[q] = valid[q] ? keys_stage[a + c0 + pos] : T(0);
       dg[q] = valid[q] ? bucket_of(key[q], shift) : 0u;
     }
-    block_rank<NT, IT, 256>(dg, valid, dest, whist, scan_sm, dtot, dstart);
+    atomic_rank<NT, IT, 256>(dg, valid, dest, whist, scan_sm, dtot, dstart);
 #pragma unroll
     for (int q = 0; q < IT; ++q)
       if (valid[q]) {

@@ -141,6 +141,35 @@ __device__ __forceinline__ V block_exclusive_scan(V x, V* smem, V* total) {
 }
 
 // ---------------------------------------------------------------------------
+// Block-wide digit ranking by shared-memory atomics (not stable: order inside
+// a digit is arbitrary).  `cnt` holds RADIX zeroed counters and is left
+// zeroed; digit_total / digit_start get the batch's per-digit counts and
+// exclusive starts; dest[r] = position of item r in digit-major order.
+// ---------------------------------------------------------------------------
+template <int NT, int ITEMS, int RADIX>
+__device__ __forceinline__ void atomic_rank(const unsigned (&digit)[ITEMS], const bool (&valid)[ITEMS],
+                                            unsigned (&dest)[ITEMS], unsigned* cnt, unsigned* scan_smem,
+                                            unsigned* digit_total, unsigned* digit_start) {
+  static_assert(RADIX <= NT, "one counter per thread");
+#pragma unroll
+  for (int r = 0; r < ITEMS; ++r) dest[r] = valid[r] ? atomicAdd(&cnt[digit[r]], 1u) : 0u;
+  __syncthreads();
+  const int d = threadIdx.x;
+  const unsigned v = d < RADIX ? cnt[d] : 0u;
+  unsigned total;
+  const unsigned ex = block_exclusive_scan<NT, unsigned>(v, scan_smem, &total);
+  if (d < RADIX) {
+    digit_start[d] = ex;
+    digit_total[d] = v;
+    cnt[d] = 0;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < ITEMS; ++r)
+    if (valid[r]) dest[r] += digit_start[digit[r]];
+}
+
+// ---------------------------------------------------------------------------
 // Stable block-wide digit ranking (the LSD radix step used on chip).
 //
 // Items are owned in "warp-striped" order: warp w owns the contiguous
