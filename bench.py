@@ -460,6 +460,9 @@ def main():
     ap.add_argument("--batch-scale", type=float, default=0.25, help="read-count scale of the batch samples")
     ap.add_argument("--autotune-out", default=None, help="write the batch autotuner's table here (JSON)")
     ap.add_argument("--merge-scale", type=float, default=1.0, help="read-count scale of the merge databases")
+    ap.add_argument("--scatter-shape", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="key-range split scatter launch shape (0 = by digit count)")
+    ap.add_argument("--tile-fill", type=float, default=1.0, help="target mean tile load / on-chip capacity")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -504,7 +507,7 @@ def main():
         c.finish(collect=False)
 
     c = gpu.Counter(kk, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED,
-                    stream=stream.cuda_stream)
+                    stream=stream.cuda_stream, scatter_shape=args.scatter_shape, tile_fill=args.tile_fill)
     for _ in range(args.warmup):
         device_step(c)
     torch.cuda.synchronize()
@@ -603,7 +606,8 @@ def main():
         e2e_parts["d2h_ms"] += cc.stats()["stage_ms"][7]
         d2h[0] = out_bytes
 
-    ce = gpu.Counter(kk, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED)
+    ce = gpu.Counter(kk, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED,
+                     scatter_shape=args.scatter_shape, tile_fill=args.tile_fill)
     e2e_step(ce)
     ce.synchronize()
     for key in e2e_parts:

@@ -60,7 +60,7 @@ template <int NT, class T>
 __device__ __forceinline__ void flush_hist(const ExtractParams<T>& p, const unsigned* hist, uint32_t P,
                                            uint32_t sample) {
   if (p.blk_counts) {
-    unsigned* row = p.blk_counts + (size_t)blockIdx.x * P;
+    unsigned* row = p.blk_counts + (size_t)(blockIdx.x + p.block_base) * P;
     for (uint32_t b = threadIdx.x; b < P; b += NT) row[b] = hist[b];
   } else {
     unsigned long long* cnt = p.bucket_count + (size_t)sample * P;
@@ -106,7 +106,7 @@ __device__ __forceinline__ void reserve_ranges(const ExtractParams<T>& p, unsign
     const unsigned h = hist[b];
     unsigned long long r = 0;
     if (p.blk_offs)  // offset inside the sample's bucket region: this row minus the sample's first row
-      r = p.blk_offs[(size_t)blockIdx.x * P + b] - p.blk_offs[(size_t)d.sample_first * P + b];
+      r = p.blk_offs[(size_t)(blockIdx.x + p.block_base) * P + b] - p.blk_offs[(size_t)d.sample_first * P + b];
     else if (h) r = atomicAdd(&p.bucket_fill[g0 + b], (unsigned long long)h);
     if (h && r + h > p.bucket_count[g0 + b]) {
       dev_fail(p.status, KITE_DEV_REGION_OVERFLOW, b, (unsigned)r, h);
@@ -243,7 +243,8 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
   unsigned* scan_sm = hist + P;
   for (uint32_t b = threadIdx.x; b < P; b += NT) hist[b] = 0;
 
-  const BlockDesc d = p.blocks[blockIdx.x];
+  const uint32_t bi = blockIdx.x + p.block_base;  // global block index
+  const BlockDesc d = p.blocks[bi];
   const uint64_t e = d.end;
   const uint64_t ts = d.start + (uint64_t)threadIdx.x * 64;
   const bool chunk_ok = p.arena[d.chunk_start] == '@';  // src/count/parser.rs:27-29
@@ -268,7 +269,7 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
   w1.nl &= r1;
   unsigned nl_total;
   const unsigned nl_before = block_exclusive_scan<NT, unsigned>(__popc(w0.nl) + __popc(w1.nl), scan_sm, &nl_total);
-  const unsigned long long line0 = p.block_nl_excl[blockIdx.x] - p.block_nl_excl[d.first_block];
+  const unsigned long long line0 = p.block_nl_excl[bi] - p.block_nl_excl[d.first_block];
   unsigned ph = (unsigned)((line0 + nl_before) & 3ull);  // line phase at ts
   unsigned php = (ph - (unsigned)__popc(wp.nl)) & 3u;     // at ts - 32
   const uint32_t seqp = has_prev ? seq_mask(wp.nl, php) : 0u;
@@ -294,8 +295,8 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
         unsigned long long at = tot ? atomicAdd(p.stage_counter, (unsigned long long)tot) : 0ull;
         if (at + tot > p.stage_cap) at = ~0ull;  // over capacity: the host takes the other scatter path
         *bb = at;
-        p.blk_keys[2 * (size_t)blockIdx.x] = at;
-        p.blk_keys[2 * (size_t)blockIdx.x + 1] = tot;
+        p.blk_keys[2 * (size_t)bi] = at;
+        p.blk_keys[2 * (size_t)bi + 1] = tot;
       }
       __syncthreads();
       if (*bb != ~0ull) out = p.keys_stage + *bb + before;
@@ -390,7 +391,8 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract128(ExtractParams<u1
   unsigned* scan_sm = hist + P;
   for (uint32_t b = threadIdx.x; b < P; b += NT) hist[b] = 0;
 
-  const BlockDesc d = p.blocks[blockIdx.x];
+  const uint32_t bi = blockIdx.x + p.block_base;  // global block index
+  const BlockDesc d = p.blocks[bi];
   const uint64_t e = d.end;
   const uint64_t ts = d.start + (uint64_t)threadIdx.x * 64;
   const bool chunk_ok = p.arena[d.chunk_start] == '@';  // src/count/parser.rs:27-29
@@ -416,7 +418,7 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract128(ExtractParams<u1
   w1.nl &= r1;
   unsigned nl_total;
   const unsigned nl_before = block_exclusive_scan<NT, unsigned>(__popc(w0.nl) + __popc(w1.nl), scan_sm, &nl_total);
-  const unsigned long long line0 = p.block_nl_excl[blockIdx.x] - p.block_nl_excl[d.first_block];
+  const unsigned long long line0 = p.block_nl_excl[bi] - p.block_nl_excl[d.first_block];
   unsigned ph = (unsigned)((line0 + nl_before) & 3ull);                       // line phase at ts
   unsigned phq = (ph - (unsigned)__popc(wp.nl) - (unsigned)__popc(wq.nl)) & 3u;  // at ts - 64
   const uint32_t seqq = has_prev ? seq_mask(wq.nl, phq) : 0u;
@@ -445,8 +447,8 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract128(ExtractParams<u1
         unsigned long long at = tot ? atomicAdd(p.stage_counter, (unsigned long long)tot) : 0ull;
         if (at + tot > p.stage_cap) at = ~0ull;  // over capacity: the host takes the other scatter path
         *bb = at;
-        p.blk_keys[2 * (size_t)blockIdx.x] = at;
-        p.blk_keys[2 * (size_t)blockIdx.x + 1] = tot;
+        p.blk_keys[2 * (size_t)bi] = at;
+        p.blk_keys[2 * (size_t)bi + 1] = tot;
       }
       __syncthreads();
       if (*bb != ~0ull) out = p.keys_stage + *bb + before;
@@ -520,9 +522,12 @@ template void launch_extract_scatter<u128>(const ExtractParams<u128>&, uint32_t,
 // Key-range split: inside every hash bucket, route keys to S key-range tiles
 // by the global splitters (tile of a key = number of splitters <= key).
 // Tiles are laid out bucket-major, so each bucket's tiles stay contiguous and
-// in key order.  One level handles D <= 256 sub-ranges ("digits") per region;
-// S > 256 tiles take two levels (coarse ranges, then tiles inside each coarse
-// range), so that every scatter writes to at most 256 destinations.
+// in key order.  One level handles D <= 1024 sub-ranges ("digits") per
+// region; S > 1024 tiles take two levels (coarse ranges, then tiles inside
+// each coarse range), so that every scatter writes to at most 1024
+// destinations.  A digit's runs from consecutive batches of one part are
+// adjacent, so partial sectors written by one batch are completed in L2 by the
+// next before they reach DRAM.
 // Each region is processed in G parts; part (r, g) owns the sub-range
 // [off[(r*D+d)*G+g], +count) of digit d, so no two CTAs share a cursor and
 // the only atomics are shared-memory ones.
@@ -531,7 +536,7 @@ static constexpr int kLutBits = 12, kLutSize = 1 << kLutBits;
 static constexpr size_t kLutBytes = ((size_t)(kLutSize + 1) * 2 + 15) & ~(size_t)15;
 static constexpr int kSplitThreads = 512;
 static constexpr int kSplitUnroll = 8;
-static constexpr uint32_t kMaxDigits = 256;
+static constexpr uint32_t kMaxDigits = 1024;
 
 // Loads region r's D-1 digit splitters and builds a table over the region's
 // key range [lo, hi] (the splitters just outside it): lut[bin] = number of the
@@ -636,12 +641,12 @@ struct ScatterSmem {
   static constexpr int BATCH = NT * IT;
   static constexpr size_t o_stage = 0;
   static constexpr size_t o_dig = o_stage + (size_t)BATCH * sizeof(T);
-  static constexpr size_t o_whist = (o_dig + (size_t)BATCH + 15) & ~(size_t)15;
-  static constexpr size_t o_cur = o_whist + (size_t)RADIX * NW * 4;
-  static constexpr size_t o_dtot = o_cur + (size_t)kMaxDigits * 8;
+  static constexpr size_t o_whist = (o_dig + (size_t)BATCH * 2 + 15) & ~(size_t)15;
+  static constexpr size_t o_cur = o_whist + (size_t)RADIX * 4;
+  static constexpr size_t o_dtot = o_cur + (size_t)RADIX * 8;
   static constexpr size_t o_dstart = o_dtot + (size_t)RADIX * 4;
   static constexpr size_t o_spl = o_dstart + (size_t)RADIX * 4;
-  static constexpr size_t o_lut = o_spl + (size_t)kMaxDigits * sizeof(T);
+  static constexpr size_t o_lut = o_spl + (size_t)RADIX * sizeof(T);
   static constexpr size_t o_scan = o_lut + kLutBytes;
   static constexpr size_t total = o_scan + 64 * 4;
 };
@@ -652,7 +657,7 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
   constexpr int BATCH = L::BATCH;
   extern __shared__ __align__(16) uint8_t sm[];
   T* stage = reinterpret_cast<T*>(sm + L::o_stage);
-  uint8_t* dig8 = sm + L::o_dig;
+  uint16_t* dig16 = reinterpret_cast<uint16_t*>(sm + L::o_dig);
   unsigned* whist = reinterpret_cast<unsigned*>(sm + L::o_whist);
   unsigned long long* cur = reinterpret_cast<unsigned long long*>(sm + L::o_cur);
   unsigned* dtot = reinterpret_cast<unsigned*>(sm + L::o_dtot);
@@ -689,11 +694,11 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
     for (int q = 0; q < IT; ++q)
       if (valid[q]) {
         stage[dest[q]] = key[q];
-        dig8[dest[q]] = (uint8_t)dg[q];
+        dig16[dest[q]] = (uint16_t)dg[q];
       }
     __syncthreads();
     for (unsigned i = threadIdx.x; i < cn; i += NT) {
-      const unsigned d = dig8[i];
+      const unsigned d = dig16[i];
       p.keys_out[cur[d] + (i - dstart[d])] = stage[i];
     }
     __syncthreads();
@@ -850,29 +855,58 @@ void launch_split_hist(const TileSplitParams<T>& p, cudaStream_t s) {
   if (p.R * p.G) k_split_hist<T><<<p.R * p.G, kSplitThreads, 0, s>>>(p);
 }
 
-template <class T, int NT, int IT, int RADIX>
-static void scatter_with(const TileSplitParams<T>& p, cudaStream_t s) {
-  const size_t smem = ScatterSmem<T, NT, IT, RADIX>::total;
-  cudaFuncSetAttribute(k_split_scatter<T, NT, IT, RADIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (p.R * p.G) k_split_scatter<T, NT, IT, RADIX><<<p.R * p.G, NT, smem, s>>>(p);
+template <class T, int NT_, int IT_, int RADIX_>
+struct ScatterCfg {
+  static constexpr int NT = NT_, IT = IT_, RADIX = RADIX_;
+};
+
+// Calls f(ScatterCfg<...>{}) for the scatter instance of D digits and launch
+// shape 0..3 (threads x keys per thread; 0 picks 256 x 8 for up to 256 digits
+// and 512 x 8 above: twice the keys per batch for four times the destinations).
+template <class T, class F>
+static void with_scatter_cfg(uint32_t D, int shape, F&& f) {
+  constexpr int W = sizeof(T) == 8 ? 1 : 2;  // u128 keys: half the keys per thread
+  auto by_radix = [&](auto cfg) {
+    using C = decltype(cfg);
+    if (D <= 16) f(ScatterCfg<T, C::NT, C::IT, 16>{});
+    else if (D <= 256) f(ScatterCfg<T, C::NT, C::IT, 256>{});
+    else f(ScatterCfg<T, C::NT, C::IT, 1024>{});
+  };
+  switch (shape) {
+    case 1: by_radix(ScatterCfg<T, 256, 16 / W, 0>{}); break;
+    case 2: by_radix(ScatterCfg<T, 512, 8 / W, 0>{}); break;
+    case 3: by_radix(ScatterCfg<T, 512, 16 / W, 0>{}); break;
+    default:
+      if (D > 256) by_radix(ScatterCfg<T, 512, 8 / W, 0>{});
+      else by_radix(ScatterCfg<T, 256, 8 / W, 0>{});
+      break;
+  }
 }
 
-template <class T, int NT, int IT>
-static void scatter_shape(const TileSplitParams<T>& p, cudaStream_t s) {
-  if (p.D <= 16) scatter_with<T, NT, IT, 16>(p, s);
-  else scatter_with<T, NT, IT, 256>(p, s);
-}
-
-// Launch shape of the scatter (threads x keys per thread), 0..3.
 template <class T>
 void launch_split_scatter(const TileSplitParams<T>& p, int shape, cudaStream_t s) {
-  constexpr int W = sizeof(T) == 8 ? 1 : 2;  // u128 keys: half the keys per thread
-  switch (shape) {
-    case 1: scatter_shape<T, 256, 16 / W>(p, s); break;
-    case 2: scatter_shape<T, 512, 8 / W>(p, s); break;
-    case 3: scatter_shape<T, 512, 16 / W>(p, s); break;
-    default: scatter_shape<T, 256, 8 / W>(p, s); break;
-  }
+  with_scatter_cfg<T>(p.D, shape, [&](auto cfg) {
+    using C = decltype(cfg);
+    auto kern = k_split_scatter<T, C::NT, C::IT, C::RADIX>;
+    const size_t smem = ScatterSmem<T, C::NT, C::IT, C::RADIX>::total;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (p.R * p.G) kern<<<p.R * p.G, C::NT, smem, s>>>(p);
+  });
+}
+
+template <class T>
+uint32_t split_scatter_slots(uint32_t D, int shape) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  with_scatter_cfg<T>(D, shape, [&](auto cfg) {
+    using C = decltype(cfg);
+    auto kern = k_split_scatter<T, C::NT, C::IT, C::RADIX>;
+    const size_t smem = ScatterSmem<T, C::NT, C::IT, C::RADIX>::total;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::NT, smem);
+  });
+  return (uint32_t)std::max(1, sms) * (uint32_t)std::max(1, per_sm);
 }
 
 void launch_make_tiles(const unsigned long long* off, uint32_t ntiles, uint32_t S, uint32_t G,
@@ -889,5 +923,7 @@ template void launch_split_hist<uint64_t>(const TileSplitParams<uint64_t>&, cuda
 template void launch_split_hist<u128>(const TileSplitParams<u128>&, cudaStream_t);
 template void launch_split_scatter<uint64_t>(const TileSplitParams<uint64_t>&, int, cudaStream_t);
 template void launch_split_scatter<u128>(const TileSplitParams<u128>&, int, cudaStream_t);
+template uint32_t split_scatter_slots<uint64_t>(uint32_t, int);
+template uint32_t split_scatter_slots<u128>(uint32_t, int);
 
 }  // namespace kite

@@ -144,25 +144,35 @@ __device__ __forceinline__ V block_exclusive_scan(V x, V* smem, V* total) {
 // Block-wide digit ranking by shared-memory atomics (not stable: order inside
 // a digit is arbitrary).  `cnt` holds RADIX zeroed counters and is left
 // zeroed; digit_total / digit_start get the batch's per-digit counts and
-// exclusive starts; dest[r] = position of item r in digit-major order.
+// exclusive starts; dest[r] = position of item r in digit-major order.  With
+// RADIX > NT each thread scans RADIX / NT consecutive counters.
 // ---------------------------------------------------------------------------
 template <int NT, int ITEMS, int RADIX>
 __device__ __forceinline__ void atomic_rank(const unsigned (&digit)[ITEMS], const bool (&valid)[ITEMS],
                                             unsigned (&dest)[ITEMS], unsigned* cnt, unsigned* scan_smem,
                                             unsigned* digit_total, unsigned* digit_start) {
-  static_assert(RADIX <= NT, "one counter per thread");
+  static_assert(RADIX <= NT || RADIX % NT == 0, "counters split evenly over the threads");
+  constexpr int PER = RADIX > NT ? RADIX / NT : 1;
 #pragma unroll
   for (int r = 0; r < ITEMS; ++r) dest[r] = valid[r] ? atomicAdd(&cnt[digit[r]], 1u) : 0u;
   __syncthreads();
-  const int d = threadIdx.x;
-  const unsigned v = d < RADIX ? cnt[d] : 0u;
-  unsigned total;
-  const unsigned ex = block_exclusive_scan<NT, unsigned>(v, scan_smem, &total);
-  if (d < RADIX) {
-    digit_start[d] = ex;
-    digit_total[d] = v;
-    cnt[d] = 0;
+  const int d0 = threadIdx.x * PER;
+  unsigned v[PER], sum = 0;
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    v[j] = d0 + j < RADIX ? cnt[d0 + j] : 0u;
+    sum += v[j];
   }
+  unsigned total;
+  unsigned ex = block_exclusive_scan<NT, unsigned>(sum, scan_smem, &total);
+#pragma unroll
+  for (int j = 0; j < PER; ++j)
+    if (d0 + j < RADIX) {
+      digit_start[d0 + j] = ex;
+      digit_total[d0 + j] = v[j];
+      cnt[d0 + j] = 0;
+      ex += v[j];
+    }
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < ITEMS; ++r)

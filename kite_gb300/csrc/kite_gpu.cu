@@ -87,6 +87,9 @@ struct Chunk {
 
 enum Stage { ST_LINES = 0, ST_HIST, ST_SCATTER, ST_SPLIT, ST_SORT, ST_BIG, ST_ENCODE, ST_D2H, ST_COUNT };
 
+// Bucket groups of the sort / encode / copy-out pipeline.
+constexpr uint32_t kSortGroups = 4;
+
 }  // namespace
 
 struct kite_gpu_ctx {
@@ -111,12 +114,14 @@ struct kite_gpu_ctx {
   DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
   DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats, blk_mat, blk_gsum, blk_keys, stage_ctr;
   DevBuf col_total, sample_first;
-  HostBuf h_blocks, h_small, h_tiles, h_out;
-  std::vector<cudaEvent_t> ev;  // stage events
+  HostBuf h_blocks, h_small, h_tiles, h_out, h_meta;
+  std::vector<cudaEvent_t> ev;   // stage events
+  std::vector<cudaEvent_t> gev;  // sort / encode / copy-out events, 8 per bucket group
 
   // results of the last finish
   std::vector<BucketMeta> res_meta;
   uint64_t res_bytes = 0;
+  bool res_on_host = false;  // the payload was copied to h_out while encoding
   std::vector<uint64_t> sample_totals;  // reads, bases, k-mers per sample of the last finish
   kite_gpu_stats stats{};
   MlpModel* mlp = nullptr;
@@ -138,27 +143,27 @@ int fail(kite_gpu_ctx* c, int code, const std::string& msg) {
   } while (0)
 
 // Bounded wait for all work queued on `s`.
-int wait_stream(kite_gpu_ctx* ctx, cudaStream_t s) {
-  cudaEvent_t e;
-  KCU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  KCU(cudaEventRecord(e, s));
+// Waits (bounded by cfg.timeout_ms) for a recorded event.
+int wait_event(kite_gpu_ctx* ctx, cudaEvent_t e) {
   const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(ctx->cfg.timeout_ms);
   int spins = 0;
   for (;;) {
     cudaError_t q = cudaEventQuery(e);
-    if (q == cudaSuccess) break;
-    if (q != cudaErrorNotReady) {
-      cudaEventDestroy(e);
-      return fail(ctx, KITE_ERR_CUDA, std::string("stream wait: ") + cudaGetErrorString(q));
-    }
-    if (std::chrono::steady_clock::now() > deadline) {
-      cudaEventDestroy(e);
+    if (q == cudaSuccess) return KITE_OK;
+    if (q != cudaErrorNotReady) return fail(ctx, KITE_ERR_CUDA, std::string("stream wait: ") + cudaGetErrorString(q));
+    if (std::chrono::steady_clock::now() > deadline)
       return fail(ctx, KITE_ERR_TIMEOUT, "device work did not finish within timeout_ms");
-    }
     if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
+}
+
+int wait_stream(kite_gpu_ctx* ctx, cudaStream_t s) {
+  cudaEvent_t e;
+  KCU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  KCU(cudaEventRecord(e, s));
+  const int rc = wait_event(ctx, e);
   cudaEventDestroy(e);
-  return KITE_OK;
+  return rc;
 }
 
 int check_status(kite_gpu_ctx* ctx, const char* where) {
@@ -191,8 +196,10 @@ void reset_segment(kite_gpu_ctx* ctx) {
   ctx->ext_base = nullptr;
 }
 
+// to_host: copy each bucket group's payload to the pinned host buffer as soon
+// as it is encoded.
 template <class T>
-int run_count(kite_gpu_ctx* ctx) {
+int run_count(kite_gpu_ctx* ctx, bool to_host) {
   cudaStream_t s = ctx->stream;
   const uint32_t P = ctx->cfg.partitions;                  // per sample
   const uint32_t NS = ctx->cfg.samples ? ctx->cfg.samples : 1;
@@ -222,6 +229,11 @@ int run_count(kite_gpu_ctx* ctx) {
                    [&](size_t a, size_t b) { return ctx->chunks[a].sample < ctx->chunks[b].sample; });
   std::vector<BlockDesc> hb;
   std::vector<uint32_t> sample_first(NS + 1, 0xFFFFFFFFu);
+  struct Span {
+    size_t chunk;
+    uint32_t first, n;
+  };
+  std::vector<Span> spans;  // each chunk's blocks, in block order
   uint64_t chunk0_len = 0;
   for (size_t c : order) {
     const Chunk& ch = ctx->chunks[c];
@@ -240,6 +252,7 @@ int run_count(kite_gpu_ctx* ctx) {
       d.sample_first = sample_first[ch.sample];
       hb.push_back(d);
     }
+    spans.push_back(Span{c, first, (uint32_t)hb.size() - first});
   }
   const uint32_t nblocks = (uint32_t)hb.size();
   // samples without blocks start where the next one does
@@ -261,12 +274,8 @@ int run_count(kite_gpu_ctx* ctx) {
   KCU(ctx->status.ensure(sizeof(DevStatus)));
   KCU(cudaMemsetAsync(ctx->status.p, 0, sizeof(DevStatus), s));
   const uint8_t* base = arena_base(ctx);
-  launch_newline_count(base, ctx->blocks.as<BlockDesc>(), nblocks, ctx->nl.as<unsigned long long>(), s);
-  st.kernel_launches += 1 + exclusive_scan_u64(ctx->nl.as<unsigned long long>(), ctx->nl.as<unsigned long long>(),
-                                               nblocks, ctx->scan_tmp.as<unsigned long long>(), s);
-  KCU(cudaEventRecord(ctx->ev[1], s));
 
-  // ---- K2 histogram pass --------------------------------------------------
+  // ---- K1 newline count + K2 histogram pass -------------------------------
   const uint32_t sample_cap = 1u << 20;
   KCU(ctx->bucket_count.ensure((size_t)PT * 8));
   KCU(ctx->totals.ensure(NS * sizeof(CountTotals)));
@@ -323,8 +332,41 @@ int run_count(kite_gpu_ctx* ctx) {
     ep.stage_counter = ctx->stage_ctr.as<unsigned long long>();
     ep.blk_keys = ctx->blk_keys.as<unsigned long long>();
   }
-  launch_extract_hist<T>(ep, nblocks, s);
-  st.kernel_launches += 1;
+  // Host chunks: each chunk's newline count, scan and histogram pass start
+  // as soon as that chunk's copy has landed, so the copies of later chunks
+  // overlap the extraction of earlier ones.  Newline prefixes are counted
+  // from each chunk's start, which is all the extraction reads of them.
+  const bool overlap = !ctx->ext_mode && spans.size() > 1 && ctx->ticket_events.size() == ctx->chunks.size();
+  unsigned long long* nl = ctx->nl.as<unsigned long long>();
+  auto wait_all_copies = [&]() -> cudaError_t {
+    cudaEvent_t dep;
+    cudaError_t e = cudaEventCreateWithFlags(&dep, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(dep, ctx->copy_stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, dep, 0);
+    cudaEventDestroy(dep);
+    return e;
+  };
+  if (overlap) {
+    KCU(cudaEventRecord(ctx->ev[1], s));  // the newline stage folds into the histogram stage
+    for (const Span& sp : spans) {
+      KCU(cudaStreamWaitEvent(s, ctx->ticket_events[sp.chunk], 0));
+      launch_newline_count(base, ctx->blocks.as<BlockDesc>() + sp.first, sp.n, nl + sp.first, s);
+      st.kernel_launches += 1 + exclusive_scan_u64(nl + sp.first, nl + sp.first, sp.n,
+                                                   ctx->scan_tmp.as<unsigned long long>(), s);
+      ep.block_base = sp.first;
+      launch_extract_hist<T>(ep, sp.n, s);
+      st.kernel_launches += 1;
+    }
+    ep.block_base = 0;
+    KCU(wait_all_copies());
+  } else {
+    KCU(wait_all_copies());
+    launch_newline_count(base, ctx->blocks.as<BlockDesc>(), nblocks, nl, s);
+    st.kernel_launches += 1 + exclusive_scan_u64(nl, nl, nblocks, ctx->scan_tmp.as<unsigned long long>(), s);
+    KCU(cudaEventRecord(ctx->ev[1], s));
+    launch_extract_hist<T>(ep, nblocks, s);
+    st.kernel_launches += 1;
+  }
   if (use_matrix) {
     // column totals straight into the bucket counts for one sample; per
     // (sample, bucket) totals from the sample boundaries for a batch
@@ -466,15 +508,27 @@ int run_count(kite_gpu_ctx* ctx) {
     st.hist_pred_imbalance = hist_imb;
     st.splitter_used = learned ? KITE_SPLIT_LEARNED : KITE_SPLIT_SAMPLED;
     const T* chosen = learned ? mlp_spl : hist_spl;
-    // Split into tiles: one level of S digits when S <= 256, else coarse
-    // ranges of 256 tiles first, then the tiles inside each coarse range.
-    // G parts per region: enough CTAs to fill the GPU twice, parts of >= 32K keys.
-    auto parts = [&](uint64_t regions, uint64_t max_region) {
-      uint64_t g = std::max<uint64_t>(1, (2ull * 152 + regions - 1) / regions);
-      g = std::min<uint64_t>(g, std::max<uint64_t>(1, max_region / 32768));
-      return (uint32_t)std::min<uint64_t>(g, 64);
+    // Split into tiles: one level of S digits when S <= 1024, else coarse
+    // ranges of 1024 tiles first, then the tiles inside each coarse range.
+    // G parts per region (parts of >= 32K keys, G <= 64): the fewest parts
+    // whose CTAs fill the scatter's resident slots in whole waves, as far as
+    // a 2% gain in the used fraction of the last wave goes.
+    auto parts = [&](uint64_t regions, uint64_t max_region, uint32_t D) {
+      const uint64_t slots = split_scatter_slots<T>(D, ctx->cfg.scatter_shape);
+      const uint64_t gmax = std::min<uint64_t>(64, std::max<uint64_t>(1, max_region / 32768));
+      uint64_t best = 1;
+      double best_used = 0.0;
+      for (uint64_t g = 1; g <= gmax; ++g) {
+        const uint64_t ctas = regions * g;
+        const double used = (double)ctas / (double)(((ctas + slots - 1) / slots) * slots);
+        if (used > best_used + 0.02) {
+          best = g;
+          best_used = used;
+        }
+      }
+      return (uint32_t)best;
     };
-    const uint32_t D2 = std::min<uint32_t>(S, 256), D1 = S / D2;
+    const uint32_t D2 = std::min<uint32_t>(S, 1024), D1 = S / D2;
     st.split_levels = D1 > 1 ? 2 : 1;
     const size_t nt = (size_t)PT * S;
     TileSplitParams<T> tp{};
@@ -488,7 +542,7 @@ int run_count(kite_gpu_ctx* ctx) {
     T* level_out = ctx->keys_b.as<T>();
     if (D1 > 1) {
       // level 1: buckets -> (bucket, coarse range); coarse splitter c is tile splitter (c+1)*D2-1
-      const uint32_t G1 = parts(PT, maxb);
+      const uint32_t G1 = parts(PT, maxb, D1);
       const size_t n1 = (size_t)PT * D1 * G1;
       KCU(ctx->lvl_count.ensure(n1 * 8));
       KCU(ctx->lvl_off.ensure(n1 * 8));
@@ -515,7 +569,7 @@ int run_count(kite_gpu_ctx* ctx) {
       launch_region_bounds(t1.tile_off, PT * D1, G1, N, ctx->reg_off.as<unsigned long long>(),
                            ctx->reg_cnt.as<unsigned long long>(), s);
       // level 2: (bucket, coarse c) -> tiles c*D2 .. c*D2+D2-1
-      G = parts((uint64_t)PT * D1, (maxb + D1 - 1) / D1 * 2);
+      G = parts((uint64_t)PT * D1, (maxb + D1 - 1) / D1 * 2, D2);
       tp.region_off = ctx->reg_off.as<unsigned long long>();
       tp.region_count = ctx->reg_cnt.as<unsigned long long>();
       tp.R = PT * D1;
@@ -524,7 +578,7 @@ int run_count(kite_gpu_ctx* ctx) {
       tp.spl_region_stride = D2;
       std::swap(level_in, level_out);
     } else {
-      G = parts(PT, maxb);
+      G = parts(PT, maxb, D2);
       tp.region_off = ctx->bucket_off.as<unsigned long long>();
       tp.region_count = ctx->bucket_count.as<unsigned long long>();
       tp.R = PT;
@@ -562,16 +616,27 @@ int run_count(kite_gpu_ctx* ctx) {
   }
   KCU(cudaEventRecord(ctx->ev[4], s));
   const uint32_t ntiles = (uint32_t)ht.size();
-  std::vector<uint32_t> big;
+  const uint32_t Sl = ntiles / PT;  // tiles per bucket
+  // Bucket groups: each group's tiles are sorted, linked and encoded in turn,
+  // so one group's payload copies to the host while the next one sorts.
+  const uint32_t NG = std::min<uint32_t>(kSortGroups, PT);
+  std::vector<uint32_t> gb(NG + 1);  // first bucket of each group
+  for (uint32_t g = 0; g <= NG; ++g) gb[g] = (uint32_t)((uint64_t)PT * g / NG);
+  // oversized tiles, group by group: first those sorted on chip at twice the
+  // capacity, then those sorted through global memory
+  std::vector<uint32_t> big, gbig(NG + 1, 0), glarge(NG, 0);
+  for (uint32_t g = 0; g < NG; ++g) {
+    gbig[g] = (uint32_t)big.size();
+    for (uint32_t t = gb[g] * Sl; t < gb[g + 1] * Sl; ++t)
+      if (ht[t].len > CAP && ht[t].len <= 2 * CAP) big.push_back(t);
+    glarge[g] = (uint32_t)big.size() - gbig[g];
+    for (uint32_t t = gb[g] * Sl; t < gb[g + 1] * Sl; ++t)
+      if (ht[t].len > 2 * CAP) big.push_back(t);
+  }
+  gbig[NG] = (uint32_t)big.size();
   std::vector<uint64_t> range(S, 0);
   uint64_t tmax = 0, tsum = 0, tne = 0;
-  size_t nlarge = 0;  // big[0 .. nlarge): on chip at twice the capacity; the rest: global memory
   for (uint32_t t = 0; t < ntiles; ++t) {
-    if (ht[t].len > CAP && ht[t].len <= 2 * CAP) big.push_back(t);
-  }
-  nlarge = big.size();
-  for (uint32_t t = 0; t < ntiles; ++t) {
-    if (ht[t].len > 2 * CAP) big.push_back(t);
     range[t % S] += ht[t].len;
     if (ht[t].len) {
       tmax = std::max<uint64_t>(tmax, ht[t].len);
@@ -596,72 +661,153 @@ int run_count(kite_gpu_ctx* ctx) {
     KCU(cudaMemcpyAsync(ctx->big_ids.p, hb2, big.size() * 4, cudaMemcpyHostToDevice, s));
   }
   KCU(ctx->tile_out.ensure((size_t)ntiles * sizeof(TileOut<T>)));
-
-  // ---- K4 tile sort + RLE ---------------------------------------------------
   KCU(ctx->sort_stats.ensure(8));
   KCU(cudaMemsetAsync(ctx->sort_stats.p, 0, 8, s));
-  launch_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ntiles,
-                      ctx->tile_out.as<TileOut<T>>(), ctx->sort_stats.as<unsigned long long>(), s);
-  const size_t nhuge = big.size() - nlarge;
-  st.kernel_launches += 1 + (nlarge ? 1 : 0) + (nhuge ? 1 : 0) + 4;  // sorts, link, offsets, encode
-  KCU(cudaGetLastError());
-  KCU(cudaEventRecord(ctx->ev[5], s));
-  launch_tile_sort_large<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ctx->big_ids.as<uint32_t>(),
-                            (uint32_t)nlarge, ctx->tile_out.as<TileOut<T>>(),
-                            ctx->sort_stats.as<unsigned long long>(), s);
-  launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(),
-                          ctx->big_ids.as<uint32_t>() + nlarge, (uint32_t)nhuge, ctx->tile_out.as<TileOut<T>>(),
-                          ctx->status.as<DevStatus>(), s);
-  KCU(cudaGetLastError());
-  KCU(cudaEventRecord(ctx->ev[6], s));
-
-  // ---- K7 DVLE encode -------------------------------------------------------
-  const uint32_t Sl = ntiles / PT;
   KCU(ctx->tile_boff.ensure((size_t)ntiles * 8));
   KCU(ctx->tile_prev.ensure((size_t)ntiles * sizeof(T)));
   KCU(ctx->meta.ensure((size_t)PT * sizeof(BucketMeta)));
-  launch_tile_link<T>(ctx->tile_out.as<TileOut<T>>(), PT, Sl, ctx->tile_boff.as<unsigned long long>(),
-                      ctx->tile_prev.as<T>(), ctx->meta.as<BucketMeta>(), s);
-  launch_bucket_offsets(ctx->meta.as<BucketMeta>(), PT, nullptr, s);
-  ctx->res_meta.resize(PT);
-  KCU(cudaMemcpyAsync(ctx->res_meta.data(), ctx->meta.p, (size_t)PT * sizeof(BucketMeta), cudaMemcpyDeviceToHost, s));
+  KCU(ctx->h_meta.ensure((size_t)PT * sizeof(BucketMeta)));
+  // payload buffers: the previous payload size or 2.25 bytes per k-mer to
+  // start with; grown, keeping what is written, when a group needs more
+  KCU(ctx->out.ensure(std::max<uint64_t>(ctx->res_bytes, N * 9 / 4) + 16));
+  if (to_host) KCU(ctx->h_out.ensure(std::max<uint64_t>(ctx->res_bytes, N * 9 / 4) + 16));
+  ctx->res_on_host = false;
+  ctx->res_meta.assign(PT, BucketMeta{});
+  st.kernel_launches += 1 + (uint64_t)NG * 3 + (uint64_t)NG * 3;  // memset, per group: sort, link, offsets, encode
+  for (uint32_t g = 0; g < NG; ++g) st.kernel_launches += (glarge[g] ? 1 : 0) + (gbig[g + 1] - gbig[g] > glarge[g] ? 1 : 0);
+  cudaEvent_t* gev = ctx->gev.data();  // per group: sort, large, link | encode | copy start/end
+  TileOut<T>* tout = ctx->tile_out.as<TileOut<T>>();
+  BucketMeta* meta = ctx->meta.as<BucketMeta>();
+  BucketMeta* hmeta = ctx->h_meta.as<BucketMeta>();
+
+  // ---- K4 tile sort + RLE, K5 link and byte offsets (one group) --------------
+  auto queue_sort = [&](uint32_t g) -> cudaError_t {
+    const uint32_t t0 = gb[g] * Sl, nt = (gb[g + 1] - gb[g]) * Sl, nb = gb[g + 1] - gb[g];
+    cudaEventRecord(gev[8 * g], s);
+    launch_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>() + t0, nt, tout + t0,
+                        ctx->sort_stats.as<unsigned long long>(), s);
+    cudaEventRecord(gev[8 * g + 1], s);
+    launch_tile_sort_large<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(),
+                              ctx->big_ids.as<uint32_t>() + gbig[g], glarge[g], tout,
+                              ctx->sort_stats.as<unsigned long long>(), s);
+    launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(),
+                            ctx->big_ids.as<uint32_t>() + gbig[g] + glarge[g], gbig[g + 1] - gbig[g] - glarge[g], tout,
+                            ctx->status.as<DevStatus>(), s);
+    cudaEventRecord(gev[8 * g + 2], s);
+    // ---- K5: per-bucket tile links, byte offsets from the group's start
+    launch_tile_link<T>(tout + t0, nb, Sl, ctx->tile_boff.as<unsigned long long>() + t0, ctx->tile_prev.as<T>() + t0,
+                        meta + gb[g], s);
+    launch_bucket_offsets(meta + gb[g], nb, nullptr, s);
+    cudaMemcpyAsync(hmeta + gb[g], meta + gb[g], (size_t)nb * sizeof(BucketMeta), cudaMemcpyDeviceToHost, s);
+    cudaEventRecord(gev[8 * g + 3], s);
+    return cudaGetLastError();
+  };
+  // Grows a payload buffer to `need` bytes keeping its first `keep` bytes
+  // (after every queued encode and copy has finished).
+  auto grow_out = [&](uint64_t need, uint64_t keep) -> int {
+    int r = wait_stream(ctx, s);
+    if (!r) r = wait_stream(ctx, ctx->copy_stream);
+    if (r) return r;
+    if (need > ctx->out.cap) {
+      DevBuf nb;
+      KCU(nb.ensure(need));
+      if (keep) KCU(cudaMemcpy(nb.p, ctx->out.p, keep, cudaMemcpyDeviceToDevice));
+      ctx->out.release();
+      ctx->out = nb;
+    }
+    if (to_host && need > ctx->h_out.cap) {
+      HostBuf nb;
+      KCU(nb.ensure(need));
+      if (keep) std::memcpy(nb.p, ctx->h_out.p, keep);
+      ctx->h_out.release();
+      ctx->h_out = nb;
+    }
+    return KITE_OK;
+  };
+
+  uint64_t total_bytes = 0, rows = 0;
+  float ms_sort = 0, ms_big = 0, ms_enc = 0, ms_d2h = 0;
+  KCU(queue_sort(0));
+  for (uint32_t g = 0; g < NG; ++g) {
+    if (g + 1 < NG) KCU(queue_sort(g + 1));
+    rc = wait_event(ctx, gev[8 * g + 3]);
+    if (rc) return rc;
+    const uint32_t t0 = gb[g] * Sl, nt = (gb[g + 1] - gb[g]) * Sl;
+    uint64_t gbytes = 0;
+    for (uint32_t b = gb[g]; b < gb[g + 1]; ++b) {
+      BucketMeta m = hmeta[b];
+      gbytes += m.bytes;
+      rows += m.rows;
+      m.byte_off += total_bytes;
+      ctx->res_meta[b] = m;
+    }
+    if (total_bytes + gbytes + 16 > ctx->out.cap || (to_host && total_bytes + gbytes + 16 > ctx->h_out.cap)) {
+      rc = grow_out(total_bytes + gbytes + 16 + (total_bytes + gbytes) / 4, total_bytes);
+      if (rc) return rc;
+    }
+    // ---- K7 DVLE encode of the group, then its copy to the host
+    cudaEventRecord(gev[8 * g + 4], s);
+    launch_encode<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>() + t0, tout + t0,
+                     ctx->tile_boff.as<unsigned long long>() + t0, ctx->tile_prev.as<T>() + t0, meta, nt,
+                     ctx->out.as<uint8_t>() + total_bytes, gbytes, ctx->status.as<DevStatus>(), s);
+    cudaEventRecord(gev[8 * g + 5], s);
+    KCU(cudaGetLastError());
+    if (to_host) {
+      KCU(cudaStreamWaitEvent(ctx->copy_stream, gev[8 * g + 5], 0));
+      cudaEventRecord(gev[8 * g + 6], ctx->copy_stream);
+      if (gbytes)
+        KCU(cudaMemcpyAsync(ctx->h_out.as<uint8_t>() + total_bytes, ctx->out.as<uint8_t>() + total_bytes, gbytes,
+                            cudaMemcpyDeviceToHost, ctx->copy_stream));
+      cudaEventRecord(gev[8 * g + 7], ctx->copy_stream);
+    }
+    total_bytes += gbytes;
+  }
+  KCU(cudaEventRecord(ctx->ev[7], s));
   KCU(cudaMemcpyAsync(ctx->h_small.p, ctx->sort_stats.p, 8, cudaMemcpyDeviceToHost, s));
   rc = wait_stream(ctx, s);
+  if (!rc && to_host) rc = wait_stream(ctx, ctx->copy_stream);
   if (rc) return rc;
   std::memcpy(&st.sort_fallbacks, ctx->h_small.p, 8);
-  if (rc) return rc;
   rc = check_status(ctx, "count");
   if (rc) return rc;
-  uint64_t total_bytes = 0, rows = 0;
-  for (uint32_t b = 0; b < PT; ++b) {
-    total_bytes += ctx->res_meta[b].bytes;
-    rows += ctx->res_meta[b].rows;
+  for (uint32_t g = 0; g < NG; ++g) {
+    float a = 0, b = 0, c = 0, d = 0;
+    cudaEventElapsedTime(&a, gev[8 * g], gev[8 * g + 1]);
+    cudaEventElapsedTime(&b, gev[8 * g + 1], gev[8 * g + 2]);
+    cudaEventElapsedTime(&c, gev[8 * g + 2], gev[8 * g + 3]);
+    cudaEventElapsedTime(&d, gev[8 * g + 4], gev[8 * g + 5]);
+    ms_sort += a;
+    ms_big += b;
+    ms_enc += c + d;
+    if (to_host) {
+      float e = 0;
+      cudaEventElapsedTime(&e, gev[8 * g + 6], gev[8 * g + 7]);
+      ms_d2h += e;
+    }
   }
-  KCU(ctx->out.ensure(total_bytes + 16));
-  launch_encode<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ctx->tile_out.as<TileOut<T>>(),
-                   ctx->tile_boff.as<unsigned long long>(), ctx->tile_prev.as<T>(), ctx->meta.as<BucketMeta>(), ntiles,
-                   ctx->out.as<uint8_t>(), total_bytes, ctx->status.as<DevStatus>(), s);
-  KCU(cudaGetLastError());
-  KCU(cudaEventRecord(ctx->ev[7], s));
-  rc = check_status(ctx, "encode");
-  if (rc) return rc;
   ctx->res_bytes = total_bytes;
+  ctx->res_on_host = to_host;
+  if (to_host) st.d2h_bytes += total_bytes;
   st.rows = rows;
   st.payload_bytes = total_bytes;
   // stage times
-  static const int map[7] = {ST_LINES, ST_HIST, ST_SCATTER, ST_SPLIT, ST_SORT, ST_BIG, ST_ENCODE};
-  for (int i = 0; i < 7; ++i) {
+  static const int map[4] = {ST_LINES, ST_HIST, ST_SCATTER, ST_SPLIT};
+  for (int i = 0; i < 4; ++i) {
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
     st.stage_ms[map[i]] = ms;
   }
+  st.stage_ms[ST_SORT] = ms_sort;
+  st.stage_ms[ST_BIG] = ms_big;
+  st.stage_ms[ST_ENCODE] = ms_enc;
+  st.stage_ms[ST_D2H] = ms_d2h;
   return KITE_OK;
 }
 
 int emit_results(kite_gpu_ctx* ctx, kite_gpu_emit_fn emit, void* user) {
   if (!emit) return KITE_OK;
   const uint32_t P = (uint32_t)ctx->res_meta.size();
-  if (ctx->res_bytes) {
+  if (ctx->res_bytes && !ctx->res_on_host) {
     KCU(ctx->h_out.ensure(ctx->res_bytes));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -757,6 +903,8 @@ int kite_gpu_open(const kite_gpu_cfg* cfg, kite_gpu_ctx** out) {
   }
   ctx->ev.resize(9);
   for (auto& e : ctx->ev) cudaEventCreate(&e);
+  ctx->gev.resize(8 * kSortGroups);
+  for (auto& e : ctx->gev) cudaEventCreate(&e);
   if (ctx->cfg.arena_bytes == 0) {
     size_t fr = 0, to = 0;
     cudaMemGetInfo(&fr, &to);
@@ -773,6 +921,7 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
   cudaStreamSynchronize(ctx->copy_stream);
   for (auto e : ctx->ticket_events) cudaEventDestroy(e);
   for (auto e : ctx->ev) cudaEventDestroy(e);
+  for (auto e : ctx->gev) cudaEventDestroy(e);
   DevBuf* bufs[] = {&ctx->arena, &ctx->blocks, &ctx->nl, &ctx->scan_tmp, &ctx->bucket_count, &ctx->bucket_off,
                     &ctx->bucket_fill, &ctx->totals, &ctx->status, &ctx->keys_a, &ctx->keys_b, &ctx->counts,
                     &ctx->sample, &ctx->sample_count, &ctx->splitters, &ctx->splitters2, &ctx->hist16,
@@ -786,6 +935,7 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
   ctx->h_small.release();
   ctx->h_tiles.release();
   ctx->h_out.release();
+  ctx->h_meta.release();
   mlp_destroy(ctx->mlp);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   cudaStreamDestroy(ctx->copy_stream);
@@ -880,13 +1030,7 @@ int kite_gpu_sample_totals(kite_gpu_ctx* ctx, uint32_t sample, uint64_t* totals)
 int kite_gpu_count_finish(kite_gpu_ctx* ctx, kite_gpu_emit_fn emit, void* user) {
   if (!ctx) return KITE_ERR_BAD_INPUT;
   cudaSetDevice(ctx->cfg.device);
-  // compute waits for all queued copies
-  cudaEvent_t dep;
-  KCU(cudaEventCreateWithFlags(&dep, cudaEventDisableTiming));
-  KCU(cudaEventRecord(dep, ctx->copy_stream));
-  KCU(cudaStreamWaitEvent(ctx->stream, dep, 0));
-  cudaEventDestroy(dep);
-  int rc = ctx->cfg.k <= 31 ? run_count<uint64_t>(ctx) : run_count<u128>(ctx);
+  int rc = ctx->cfg.k <= 31 ? run_count<uint64_t>(ctx, emit != nullptr) : run_count<u128>(ctx, emit != nullptr);
   if (rc == KITE_OK) rc = emit_results(ctx, emit, user);
   for (auto e : ctx->ticket_events) cudaEventDestroy(e);
   ctx->ticket_events.clear();

@@ -45,7 +45,8 @@ template <class T>
 struct ExtractParams {
   const uint8_t* arena;
   const BlockDesc* blocks;
-  const unsigned long long* block_nl_excl;  // exclusive newline prefix per block (global order)
+  const unsigned long long* block_nl_excl;  // newlines before each block, counted from its chunk's start
+  uint32_t block_base;   // the launch's first block: block index = blockIdx.x + block_base
   uint32_t k;
   uint32_t canonical;
   uint32_t shift;        // 64 - log2(partitions)
@@ -122,6 +123,8 @@ template <class T>
 void launch_split_hist(const TileSplitParams<T>& p, cudaStream_t s);
 template <class T>
 void launch_split_scatter(const TileSplitParams<T>& p, int shape, cudaStream_t s);  // shape 0..3: threads x keys
+template <class T>
+uint32_t split_scatter_slots(uint32_t D, int shape);  // resident scatter CTAs on the device
 void launch_make_tiles(const unsigned long long* off, uint32_t ntiles, uint32_t S, uint32_t G,
                        unsigned long long n_keys, TileDesc* tiles, uint32_t* lens, cudaStream_t s);
 void launch_region_bounds(const unsigned long long* off, uint32_t nreg, uint32_t G, unsigned long long n_keys,

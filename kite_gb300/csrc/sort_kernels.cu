@@ -4,9 +4,9 @@
 //
 // A tile is a key range of one hash bucket.  One CTA loads the whole tile into
 // shared memory, orders it by a 4096-bin counting pass over its key span (bins
-// holding several distinct keys are finished by counting, rare large ones by
-// LSD passes), then emits unique (key, count) rows in place and the tile's
-// DVLE size for every row but the first.
+// holding several distinct keys are finished by a thread or a warp, rare
+// pathological ones by LSD passes), then emits unique (key, count) rows in
+// place and the tile's DVLE size for every row but the first.
 #include "kite_internal.h"
 
 namespace kite {
@@ -103,24 +103,27 @@ __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, u
 // Tile sort by binning.  One CTA per tile of n <= CAP keys:
 //  1. load the tile into shared memory; block min / max;
 //  2. bin = (key - min) >> s with 4096 bins spanning [min, max]: histogram by
-//     shared atomics, exclusive scan, then the key INDICES (u16) are scattered
-//     into bin order.  Bins are key-ordered; order inside a bin is arbitrary;
-//  3. a bin holding more than one distinct key is ordered by counting: each
-//     key counts the smaller keys, and the equal keys placed before it, in its
-//     bin.  A bin of one repeated k-mer (the usual case) costs nothing.  A
-//     mixed bin larger than kMaxMixed (typically a heavily repeated k-mer next
-//     to a few others) is sorted by one warp: it extracts the bin's distinct
-//     keys in ascending order with their counts and rewrites the bin's slots
-//     with them in order (equal keys are interchangeable).  Only a large bin
-//     with more than kMaxDistinct distinct keys sends the tile to LSD passes;
-//  4. run-length reduction over the sorted order: head flags by warp ballots,
+//     shared atomics and an exclusive scan; then the keys themselves are
+//     scattered into bin order (re-read from global memory, where the tile
+//     still sits in L2).  Bins are key-ordered; order inside a bin is
+//     arbitrary, so every later pass reads shared memory directly;
+//  3. a bin holding more than one distinct key is found where two different
+//     neighbours share it, and listed once (a shared bit per bin);
+//  4. a small listed bin (<= kSmallBin keys, typically two colliding k-mers)
+//     is insertion-sorted in place by one thread.  A larger one (typically a
+//     heavily repeated k-mer next to a few others) belongs to one warp: up to
+//     32 keys are ranked by counting across the lanes; beyond that the warp
+//     extracts the bin's distinct keys in ascending order with their counts
+//     and rewrites the bin with them (equal keys are interchangeable).  A bin
+//     of more than kMaxDistinct distinct keys is ranked by counting when it
+//     holds at most kMaxMixed keys and otherwise sends the tile to LSD passes;
+//  5. run-length reduction over the sorted keys: head flags by warp ballots,
 //     rows written to global memory over the tile's keys (u32 counts; a tile
 //     holds fewer than 2^32 keys, so no count saturates here).
-// Keys never sit in register arrays on the main path, so the kernel fits 64
-// registers and two CTAs share an SM.
 // ---------------------------------------------------------------------------
 constexpr int kBinBits = 12, kBins = 1 << kBinBits;
-constexpr unsigned kMaxMixed = 256;
+constexpr unsigned kSmallBin = 16;     // mixed bins a single thread sorts
+constexpr unsigned kMaxMixed = 256;    // largest bin ranked by counting when it has many distinct keys
 constexpr unsigned kMaxDistinct = 32;  // distinct keys a warp extracts from one large bin
 
 // MULT = 1: the regular tile (8192 u64 / 4096 u128 keys, two CTAs per SM);
@@ -131,16 +134,17 @@ struct BinSmem {
   static constexpr int ITEMS = tile_items<T>() * MULT;
   static constexpr int CAP = NT * ITEMS;
   static constexpr int NW = NT / 32;
-  static constexpr unsigned MAXLARGE = CAP / (kMaxMixed + 1) + 1;  // large mixed bins per tile
+  static constexpr unsigned MAXSMALL = CAP / 2;                   // a mixed bin holds >= 2 keys
+  static constexpr unsigned MAXLARGE = CAP / (kSmallBin + 1) + 1;  // ... a large one > kSmallBin
   static constexpr size_t buf_bytes = (size_t)CAP * sizeof(T);
-  static constexpr size_t perm_bytes = (size_t)CAP * 2;
   // bin counters; later the u16 run heads (CAP + 1 entries), or the LSD
   // fallback's per-warp digit histograms (256 * NW counters)
   static constexpr size_t head_need = ((size_t)(CAP + 1) * 2 + 15) & ~(size_t)15;
   static constexpr size_t bin_bytes = ((size_t)kBins * 4 > head_need ? (size_t)kBins * 4 : head_need) + 16;
-  static constexpr size_t flag_bytes = kBins;
-  static constexpr size_t misc_bytes = 64 * 8 + 2 * NW * sizeof(T) + 16 + MAXLARGE * 2;
-  static constexpr size_t total = buf_bytes + perm_bytes + bin_bytes + flag_bytes + misc_bytes;
+  static constexpr size_t fbit_bytes = kBins / 8;
+  static constexpr size_t list_bytes = ((size_t)(MAXSMALL + MAXLARGE) * 2 + 15) & ~(size_t)15;
+  static constexpr size_t misc_bytes = 64 * 8 + 2 * NW * sizeof(T) + 16;
+  static constexpr size_t total = buf_bytes + bin_bytes + fbit_bytes + list_bytes + misc_bytes;
   static_assert((size_t)(CAP + 1) * 2 <= bin_bytes, "run heads must fit the bin area");
   static_assert((size_t)256 * NW * 4 <= bin_bytes, "LSD histograms must fit the bin area");
   static_assert(kBins % (4 * NT) == 0, "bin scan takes whole uint4 groups");
@@ -151,23 +155,104 @@ __device__ __forceinline__ unsigned bin_of(T key, T mn, int s) {
   return (unsigned)(uint64_t)((key - mn) >> s);
 }
 
+// One warp orders buf[a, a + m), m <= kMaxMixed, by counting: each key's new
+// position is the number of smaller keys plus the equal keys before it.
+template <class T>
+__device__ __forceinline__ void warp_count_sort(T* buf, unsigned a, unsigned m, unsigned lane) {
+  constexpr int R = kMaxMixed / 32;
+  T key[R];
+  unsigned rk[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const unsigned q = lane + 32u * i;
+    key[i] = q < m ? buf[a + q] : T(0);
+    rk[i] = 0;
+  }
+  for (unsigned t = 0; t < m; ++t) {
+    const T v = buf[a + t];
+#pragma unroll
+    for (int i = 0; i < R; ++i) rk[i] += (unsigned)(v < key[i]) | ((unsigned)(v == key[i]) & (unsigned)(t < lane + 32u * i));
+  }
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < R; ++i)
+    if (lane + 32u * i < m) buf[a + rk[i]] = key[i];
+  __syncwarp();
+}
+
+// One warp orders buf[a, a + m) by extracting its distinct keys in ascending
+// order with their counts and rewriting the range with them.  False (range
+// untouched) when the range holds more than kMaxDistinct distinct keys.
+template <class T>
+__device__ __forceinline__ bool warp_distinct_sort(T* buf, unsigned a, unsigned m, unsigned lane) {
+  const unsigned e = a + m;
+  T myv = T(0), cur = T(0);
+  unsigned myc = 0, U = 0;
+  bool have = false;
+  for (;;) {
+    // smallest key above `cur` in the range, and its number of copies
+    T best = T(0);
+    unsigned cnt = 0;
+    for (unsigned j = a + lane; j < e; j += 32) {
+      const T v = buf[j];
+      if (have && !(cur < v)) continue;
+      if (cnt == 0 || v < best) {
+        best = v;
+        cnt = 1;
+      } else if (v == best) {
+        ++cnt;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const T ob = shfl_xor_key(best, o);
+      const unsigned oc = __shfl_xor_sync(0xffffffffu, cnt, o);
+      if (oc && (cnt == 0 || ob < best)) {
+        best = ob;
+        cnt = oc;
+      } else if (oc && ob == best) {
+        cnt += oc;
+      }
+    }
+    if (cnt == 0) break;
+    if (U == kMaxDistinct) return false;
+    if (lane == U) {
+      myv = best;
+      myc = cnt;
+    }
+    ++U;
+    cur = best;
+    have = true;
+  }
+  __syncwarp();
+  unsigned off = a;
+  for (unsigned u = 0; u < U; ++u) {
+    const T v = shfl_key(myv, (int)u);
+    const unsigned c = __shfl_sync(0xffffffffu, myc, (int)u);
+    for (unsigned t = lane; t < c; t += 32) buf[off + t] = v;
+    off += c;
+  }
+  __syncwarp();
+  return true;
+}
+
 template <class T, int MULT>
 __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
     k_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, const TileDesc* __restrict__ tiles,
                 const uint32_t* __restrict__ ids, TileOut<T>* __restrict__ tout, unsigned long long* fallbacks) {
   using L = BinSmem<T, MULT>;
-  constexpr unsigned kMaxLarge = L::MAXLARGE;
   constexpr int NT = L::NT, NW = L::NW, ITEMS = L::ITEMS;
   extern __shared__ __align__(16) uint8_t sm[];
   T* buf = reinterpret_cast<T*>(sm);
-  unsigned short* perm = reinterpret_cast<unsigned short*>(sm + L::buf_bytes);
-  unsigned* bins = reinterpret_cast<unsigned*>(sm + L::buf_bytes + L::perm_bytes);
-  uint8_t* flag = sm + L::buf_bytes + L::perm_bytes + L::bin_bytes;
-  unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(flag + L::flag_bytes);
+  unsigned* bins = reinterpret_cast<unsigned*>(sm + L::buf_bytes);
+  unsigned* fbits = reinterpret_cast<unsigned*>(sm + L::buf_bytes + L::bin_bytes);
+  unsigned short* small_list = reinterpret_cast<unsigned short*>(sm + L::buf_bytes + L::bin_bytes + L::fbit_bytes);
+  unsigned short* large_list = small_list + L::MAXSMALL;
+  unsigned long long* scan64 =
+      reinterpret_cast<unsigned long long*>(sm + L::buf_bytes + L::bin_bytes + L::fbit_bytes + L::list_bytes);
   unsigned* scan_sm = reinterpret_cast<unsigned*>(scan64);
   T* red = reinterpret_cast<T*>(scan64 + 64);
-  unsigned* misc = reinterpret_cast<unsigned*>(red + 2 * NW);  // [0] LSD fallback, [1] large bins
-  unsigned short* large = reinterpret_cast<unsigned short*>(misc + 4);
+  unsigned* misc = reinterpret_cast<unsigned*>(red + 2 * NW);  // [0] LSD fallback, [1] small bins, [2] large bins
 
   const uint32_t tid = ids ? ids[blockIdx.x] : blockIdx.x;
   const TileDesc td = tiles[tid];
@@ -210,13 +295,10 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
   const int rb = KeyTraits<T>::kBits - clz_key(T(mx - mn));
   const int s = rb > kBinBits ? rb - kBinBits : 0;
 
-  // ---- 2. bin histogram, scan, index scatter ----
+  // ---- 2. bin histogram, scan, key scatter into bin order ----
   for (int b = threadIdx.x; b < kBins; b += NT) bins[b] = 0;
-  for (int b = threadIdx.x; b < kBins / 4; b += NT) reinterpret_cast<unsigned*>(flag)[b] = 0;
-  if (threadIdx.x == 0) {
-    misc[0] = 0;
-    misc[1] = 0;
-  }
+  for (int b = threadIdx.x; b < kBins / 32; b += NT) fbits[b] = 0;
+  if (threadIdx.x < 4) misc[threadIdx.x] = 0;
   __syncthreads();
   for (unsigned i = threadIdx.x; i < n; i += NT) atomicAdd(&bins[bin_of(buf[i], mn, s)], 1u);
   __syncthreads();
@@ -247,124 +329,79 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
     }
   }
   __syncthreads();
+#pragma unroll 4
   for (unsigned i = threadIdx.x; i < n; i += NT) {
-    const unsigned p = atomicAdd(&bins[bin_of(buf[i], mn, s)], 1u);
-    perm[p] = (unsigned short)i;
+    const T v = g[i];
+    buf[atomicAdd(&bins[bin_of(v, mn, s)], 1u)] = v;
   }
   __syncthreads();
   // bins[b] is now the end of bin b; its start is bins[b - 1] (0 for b = 0)
 
-  // ---- 3. bins holding more than one distinct key ----
+  // ---- 3. list the bins holding more than one distinct key ----
   for (unsigned p = threadIdx.x + 1; p < n; p += NT) {
-    const T a = buf[perm[p]], b = buf[perm[p - 1]];
+    const T a = buf[p], b = buf[p - 1];
     if (a != b) {
       const unsigned ba = bin_of(a, mn, s);
-      if (bin_of(b, mn, s) == ba) flag[ba] = 1;
-    }
-  }
-  __syncthreads();
-  unsigned pend[ITEMS];  // (new position << 16) | key index, or ~0
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    pend[r] = ~0u;
-    const unsigned p = threadIdx.x + r * NT;
-    if (p >= n) continue;
-    const unsigned idx = perm[p];
-    const T k0 = buf[idx];
-    const unsigned bb = bin_of(k0, mn, s);
-    if (!flag[bb]) continue;
-    const unsigned a = bb ? bins[bb - 1] : 0u, e = bins[bb];
-    if (e - a > kMaxMixed) {
-      if (p == a) {  // the bin's first position registers it
-        const unsigned q = atomicAdd(&misc[1], 1u);
-        if (q < kMaxLarge) large[q] = (unsigned short)bb;
-        else misc[0] = 1;
+      if (bin_of(b, mn, s) == ba) {
+        const unsigned bit = 1u << (ba & 31);
+        if (!(atomicOr(&fbits[ba >> 5], bit) & bit)) {
+          const unsigned m = bins[ba] - (ba ? bins[ba - 1] : 0u);
+          if (m <= kSmallBin) small_list[atomicAdd(&misc[1], 1u)] = (unsigned short)ba;
+          else large_list[atomicAdd(&misc[2], 1u)] = (unsigned short)ba;
+        }
       }
-      continue;
     }
-    unsigned less = 0, eqb = 0;
-    for (unsigned j = a; j < e; ++j) {
-      const T v = buf[perm[j]];
-      less += v < k0;
-      eqb += (v == k0) & (j < p);
-    }
-    pend[r] = ((a + less + eqb) << 16) | idx;
   }
   __syncthreads();
+
+  // ---- 4. order the listed bins ----
   {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const unsigned nlarge = misc[1] < kMaxLarge ? misc[1] : kMaxLarge;
+    const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned nlarge = misc[2];
     for (unsigned li = wid; li < nlarge; li += NW) {
-      const unsigned bb = large[li];
+      const unsigned bb = large_list[li];
+      const unsigned a = bb ? bins[bb - 1] : 0u, m = bins[bb] - a;
+      if (m <= 32) {
+        // rank by counting across the lanes
+        const T mine = lane < m ? buf[a + lane] : T(0);
+        unsigned r = 0;
+        for (unsigned t = 0; t < m; ++t) {
+          const T v = shfl_key(mine, (int)t);
+          r += (unsigned)(v < mine) | ((unsigned)(v == mine) & (unsigned)(t < lane));
+        }
+        __syncwarp();
+        if (lane < m) buf[a + r] = mine;
+        __syncwarp();
+      } else if (!warp_distinct_sort(buf, a, m, lane)) {
+        if (m <= kMaxMixed) warp_count_sort(buf, a, m, lane);
+        else if (lane == 0) misc[0] = 1;
+      }
+    }
+    const unsigned nsmall = misc[1];
+    for (unsigned i = threadIdx.x; i < nsmall; i += NT) {
+      const unsigned bb = small_list[i];
       const unsigned a = bb ? bins[bb - 1] : 0u, e = bins[bb];
-      T myv = T(0), cur = T(0);
-      unsigned myc = 0, U = 0;
-      bool have = false, overflow = false;
-      for (;;) {
-        // smallest key above `cur` in the bin, and its number of copies
-        T best = T(0);
-        unsigned cnt = 0;
-        for (unsigned j = a + lane; j < e; j += 32) {
-          const T v = buf[perm[j]];
-          if (have && !(cur < v)) continue;
-          if (cnt == 0 || v < best) {
-            best = v;
-            cnt = 1;
-          } else if (v == best) {
-            ++cnt;
-          }
+      for (unsigned j = a + 1; j < e; ++j) {
+        const T v = buf[j];
+        unsigned q = j;
+        while (q > a) {
+          const T w = buf[q - 1];
+          if (!(v < w)) break;
+          buf[q] = w;
+          --q;
         }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-          const T ob = shfl_xor_key(best, o);
-          const unsigned oc = __shfl_xor_sync(0xffffffffu, cnt, o);
-          if (oc && (cnt == 0 || ob < best)) {
-            best = ob;
-            cnt = oc;
-          } else if (oc && ob == best) {
-            cnt += oc;
-          }
-        }
-        if (cnt == 0) break;
-        if (U == kMaxDistinct) {
-          overflow = true;
-          break;
-        }
-        if (lane == (int)U) {
-          myv = best;
-          myc = cnt;
-        }
-        ++U;
-        cur = best;
-        have = true;
-      }
-      if (overflow) {
-        if (lane == 0) misc[0] = 1;
-        continue;
-      }
-      unsigned off = a;
-      for (unsigned u = 0; u < U; ++u) {
-        const T v = shfl_key(myv, (int)u);
-        const unsigned c = __shfl_sync(0xffffffffu, myc, (int)u);
-        for (unsigned t = lane; t < c; t += 32) buf[perm[off + t]] = v;
-        off += c;
+        buf[q] = v;
       }
     }
   }
   __syncthreads();
   if (misc[0]) {
-    // a large bin of distinct keys: full LSD over the varying bits, in place
+    // a large bin of many distinct keys: full LSD over the varying bits, in place
     if (threadIdx.x == 0 && fallbacks) atomicAdd(fallbacks, 1ull);
     smem_radix_sort<T, ITEMS>(buf, n, varying_bits(mn, mx), bins, scan_sm, 0);
-    for (unsigned p = threadIdx.x; p < n; p += NT) perm[p] = (unsigned short)p;
-  } else {
-#pragma unroll
-    for (int r = 0; r < ITEMS; ++r)
-      if (pend[r] != ~0u) perm[pend[r] >> 16] = (unsigned short)(pend[r] & 0xffffu);
   }
-  __syncthreads();
 
-  // ---- 4. run-length reduction in sorted order (position p holds buf[perm[p]]) ----
+  // ---- 5. run-length reduction over the sorted keys ----
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned rounds = (n + NT - 1) / NT;
   const unsigned w0 = (unsigned)wid * 32u * rounds;
@@ -372,7 +409,7 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
   for (unsigned r = 0; r < rounds; ++r) {
     const unsigned p = w0 + r * 32u + lane;
     bool h = false;
-    if (p < n) h = p == 0 || buf[perm[p]] != buf[perm[p - 1]];
+    if (p < n) h = p == 0 || buf[p] != buf[p - 1];
     hmask |= (unsigned)h << r;
     cnt += __popc(__ballot_sync(0xffffffffu, h));
   }
@@ -393,18 +430,18 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
   for (unsigned v = threadIdx.x; v < U; v += NT) {
     const unsigned i = head[v];
     const unsigned c = (unsigned)head[v + 1] - i;
-    const T key = buf[perm[i]];
+    const T key = buf[i];
     g[v] = key;
     gc[v] = c;
-    if (v > 0) rest += (unsigned long long)(varint_len(T(key - buf[perm[head[v - 1]]])) + varint_len((uint64_t)c));
+    if (v > 0) rest += (unsigned long long)(varint_len(T(key - buf[head[v - 1]])) + varint_len((uint64_t)c));
   }
   unsigned long long rest_total;
   block_exclusive_scan<NT, unsigned long long>(rest, scan64, &rest_total);
   if (threadIdx.x == 0) {
     TileOut<T> o;
-    o.first_key = buf[perm[head[0]]];
+    o.first_key = buf[head[0]];
     o.first_count = (unsigned)head[1] - head[0];
-    o.last_key = buf[perm[head[U - 1]]];
+    o.last_key = buf[head[U - 1]];
     o.rows = U;
     o.rest_bytes = rest_total;
     tout[tid] = o;
@@ -453,7 +490,6 @@ __global__ void __launch_bounds__(kTileThreads, 1)
   using L = TileSmem<T>;
   constexpr int NT = L::NT, ITEMS = L::ITEMS, CAP = L::CAP;
   extern __shared__ __align__(16) uint8_t sm[];
-  T* buf = reinterpret_cast<T*>(sm);
   unsigned* warp_hist = reinterpret_cast<unsigned*>(sm + L::buf_bytes);
   unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(sm + L::buf_bytes + L::hist_bytes + L::head_bytes);
   unsigned* scan_sm = reinterpret_cast<unsigned*>(scan64);
