@@ -45,6 +45,36 @@ void launch_newline_count(const uint8_t* arena, const BlockDesc* blocks, uint32_
   if (nblocks) k_newline_count<<<nblocks, 256, 0, s>>>(arena, blocks, nl_out);
 }
 
+// Block descriptors from the chunk spans: one thread per block, its chunk by
+// binary search over the spans' first blocks.
+__global__ void k_make_blocks(const ChunkSpan* __restrict__ spans, uint32_t nspans, uint32_t blk, uint32_t nblocks,
+                              BlockDesc* __restrict__ out) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nblocks) return;
+  uint32_t lo = 0, hi = nspans;
+  while (hi - lo > 1) {
+    const uint32_t m = (lo + hi) >> 1;
+    if (spans[m].first_block <= b) lo = m;
+    else hi = m;
+  }
+  const ChunkSpan c = spans[lo];
+  const uint64_t o = (uint64_t)(b - c.first_block) * blk;
+  BlockDesc d;
+  d.start = c.off + o;
+  d.end = c.off + (o + blk < c.len ? o + blk : c.len);
+  d.chunk_start = c.off;
+  d.first_block = c.first_block;
+  d.flags = c.flags;
+  d.sample = c.sample;
+  d.sample_first = c.sample_first;
+  out[b] = d;
+}
+
+void launch_make_blocks(const ChunkSpan* spans, uint32_t nspans, uint32_t blk, uint32_t nblocks, BlockDesc* out,
+                        cudaStream_t s) {
+  if (nblocks) k_make_blocks<<<(nblocks + 255) / 256, 256, 0, s>>>(spans, nspans, blk, nblocks, out);
+}
+
 __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   x ^= x >> 30;
   x *= 0xbf58476d1ce4e5b9ull;
@@ -119,10 +149,16 @@ __device__ __forceinline__ void reserve_ranges(const ExtractParams<T>& p, unsign
 
 size_t extract64_smem_bytes(uint32_t partitions, bool scatter);
 
+// A word's forward and reverse-complement code streams, shared with the warp.
+struct CodeWords {
+  uint64_t code, rcode;
+};
+
 size_t extract_smem_bytes(int key_bytes, uint32_t blk_bytes, uint32_t partitions, bool scatter) {
-  (void)key_bytes;
   (void)blk_bytes;
-  return extract64_smem_bytes(partitions, scatter);
+  const size_t b = extract64_smem_bytes(partitions, scatter);
+  // the u64 histogram pass also shares every thread's three encoded words with its warp
+  return key_bytes == 8 && !scatter ? ((b + 15) & ~(size_t)15) + (size_t)kExtractThreads * 3 * sizeof(CodeWords) : b;
 }
 
 // ---------------------------------------------------------------------------
@@ -301,16 +337,56 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
       __syncthreads();
       if (*bb != ~0ull) out = p.keys_stage + *bb + before;
     }
-    auto emit = [&](uint64_t key, uint64_t pos) {
-      atomicAdd(&hist[bucket_of(key, shift)], 1u);
-      if (out) *out++ = key;
-      if (sampling && (mix64(pos) & p.sample_mask) == 0) {
-        const unsigned idx = atomicAdd(p.sample_count, 1u);
-        if (idx < p.sample_cap) p.sample[idx] = key;
+    // The warp walks its words in thread order, one lane per end byte, so the
+    // lanes share every sequence word's k-mers (a thread's own bytes may be
+    // a quality line) and a word's keys go out as one coalesced run.
+    const unsigned lane = threadIdx.x & 31;
+    CodeWords* ws = reinterpret_cast<CodeWords*>(sm + ((((size_t)P * 4 + 96 * 4) + 15) & ~(size_t)15)) +
+                    (size_t)(threadIdx.x & ~31u) * 3;
+    ws[3 * lane] = CodeWords{wp.code, wp.rcode};
+    ws[3 * lane + 1] = CodeWords{w0.code, w0.rcode};
+    ws[3 * lane + 2] = CodeWords{w1.code, w1.rcode};
+    __syncwarp();
+    const unsigned lt = (1u << lane) - 1u;
+    const uint64_t wts = ts - (uint64_t)lane * 64;  // the warp's first byte
+    uint64_t* wbase = nullptr;
+    {
+      const unsigned long long ob = out ? (unsigned long long)(out - p.keys_stage) : 0ull;
+      const unsigned long long o0 = __shfl_sync(0xffffffffu, ob, 0);
+      if (__shfl_sync(0xffffffffu, out ? 1u : 0u, 0)) wbase = p.keys_stage + o0;
+    }
+    unsigned run = 0;
+    for (unsigned ls = __ballot_sync(0xffffffffu, (V0 | V1) != 0u); ls; ls &= ls - 1) {
+      const int l = __ffs(ls) - 1;
+      const unsigned lv[2] = {__shfl_sync(0xffffffffu, V0, l), __shfl_sync(0xffffffffu, V1, l)};
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const unsigned V = lv[h];
+        if (V == 0u) continue;
+        if ((V >> lane) & 1u) {
+          const CodeWords pw = ws[3 * l + h], cw = ws[3 * l + h + 1];
+          const uint32_t sft = 2 * (31 - lane);
+          const uint64_t fwd = (sft ? ((cw.code >> sft) | (pw.code << (64 - sft))) : cw.code) & mask;
+          uint64_t key = fwd;
+          if (canon) {
+            const uint32_t t = 2 * (33 + lane - k);  // 4 .. 126
+            const uint64_t rc =
+                (t < 64 ? ((pw.rcode >> t) | (cw.rcode << (64 - t))) : (cw.rcode >> (t - 64))) & mask;
+            key = rc < fwd ? rc : fwd;
+          }
+          atomicAdd(&hist[bucket_of(key, shift)], 1u);
+          if (wbase) wbase[run + __popc(V & lt)] = key;
+          if (sampling) {
+            const uint64_t pos = wts + (uint64_t)l * 64 + 32 * h + lane;
+            if ((mix64(pos) & p.sample_mask) == 0) {
+              const unsigned idx = atomicAdd(p.sample_count, 1u);
+              if (idx < p.sample_cap) p.sample[idx] = key;
+            }
+          }
+        }
+        run += __popc(V);
       }
-    };
-    word_kmers(V0, wp, w0, k, mask, canon, [&](uint64_t key, uint32_t b) { emit(key, ts + b); });
-    word_kmers(V1, w0, w1, k, mask, canon, [&](uint64_t key, uint32_t b) { emit(key, ts + 32 + b); });
+    }
     // reads = starts of non-empty sequence-line runs; bases = sequence-line bytes
     unsigned long long reads = 0, bases = 0;
     if (chunk_ok) {
@@ -632,54 +708,73 @@ __global__ void __launch_bounds__(kSplitThreads) k_split_hist(TileSplitParams<T>
 
 // Scatter of one part, a batch of BATCH keys at a time: the batch is ranked on
 // chip by digit (shared-memory atomics over RADIX >= D digits; key order inside
-// a tile does not matter), staged in digit order, and each digit's run is
-// written to its destination with consecutive threads on consecutive
-// addresses, so global writes go out as whole sectors.
+// a tile does not matter) and staged in digit order behind each digit's keys
+// held back from the previous batch.  Each digit's run is written up to its
+// last 32-byte sector boundary with consecutive threads on consecutive
+// addresses; the keys past the boundary (fewer than a sector) wait for the
+// next batch.  Global writes therefore go out as whole sectors, except the
+// first and last one of each digit in the part, even when a batch holds only a
+// few keys per digit.
 template <class T, int NT_, int IT_, int RADIX_>
 struct ScatterSmem {
   static constexpr int NT = NT_, NW = NT / 32, IT = IT_, RADIX = RADIX_;
   static constexpr int BATCH = NT * IT;
+  static constexpr int KPS = 32 / (int)sizeof(T);            // keys per sector
+  static constexpr int STAGE = BATCH + RADIX * (KPS - 1);    // a batch and every digit's held-back keys
   static constexpr size_t o_stage = 0;
-  static constexpr size_t o_dig = o_stage + (size_t)BATCH * sizeof(T);
-  static constexpr size_t o_whist = (o_dig + (size_t)BATCH * 2 + 15) & ~(size_t)15;
+  static constexpr size_t o_dig = o_stage + (size_t)STAGE * sizeof(T);
+  static constexpr size_t o_whist = (o_dig + (size_t)STAGE * 2 + 15) & ~(size_t)15;
   static constexpr size_t o_cur = o_whist + (size_t)RADIX * 4;
   static constexpr size_t o_dtot = o_cur + (size_t)RADIX * 8;
   static constexpr size_t o_dstart = o_dtot + (size_t)RADIX * 4;
-  static constexpr size_t o_spl = o_dstart + (size_t)RADIX * 4;
+  static constexpr size_t o_wr = o_dstart + (size_t)RADIX * 4;
+  static constexpr size_t o_held = o_wr + (size_t)RADIX * 2;
+  static constexpr size_t o_spl = (o_held + (size_t)RADIX + 15) & ~(size_t)15;
   static constexpr size_t o_lut = o_spl + (size_t)RADIX * sizeof(T);
   static constexpr size_t o_scan = o_lut + kLutBytes;
   static constexpr size_t total = o_scan + 64 * 4;
+  static_assert(STAGE < 65536, "write counts are 16-bit");
 };
 
 template <class T, int NT, int IT, int RADIX>
 __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k_split_scatter(TileSplitParams<T> p) {
   using L = ScatterSmem<T, NT, IT, RADIX>;
-  constexpr int BATCH = L::BATCH;
+  constexpr int BATCH = L::BATCH, KPS = L::KPS;
+  constexpr int PER = RADIX > NT ? RADIX / NT : 1;  // digits owned by each thread
+  static_assert(RADIX <= NT || RADIX % NT == 0, "digits split evenly over the threads");
   extern __shared__ __align__(16) uint8_t sm[];
   T* stage = reinterpret_cast<T*>(sm + L::o_stage);
   uint16_t* dig16 = reinterpret_cast<uint16_t*>(sm + L::o_dig);
   unsigned* whist = reinterpret_cast<unsigned*>(sm + L::o_whist);
   unsigned long long* cur = reinterpret_cast<unsigned long long*>(sm + L::o_cur);
-  unsigned* dtot = reinterpret_cast<unsigned*>(sm + L::o_dtot);
-  unsigned* dstart = reinterpret_cast<unsigned*>(sm + L::o_dstart);
+  unsigned* dtot = reinterpret_cast<unsigned*>(sm + L::o_dtot);      // held + new keys of the batch
+  unsigned* dstart = reinterpret_cast<unsigned*>(sm + L::o_dstart);  // the digit's first stage slot
+  uint16_t* wr = reinterpret_cast<uint16_t*>(sm + L::o_wr);          // keys written this batch
+  uint8_t* held = sm + L::o_held;                                    // held-back keys ahead of the new ones
   T* spl = reinterpret_cast<T*>(sm + L::o_spl);
   uint16_t* lut = reinterpret_cast<uint16_t*>(sm + L::o_lut);
   unsigned* scan_sm = reinterpret_cast<unsigned*>(sm + L::o_scan);
   const uint32_t D = p.D, G = p.G;
   const uint32_t r = blockIdx.x / G, g = blockIdx.x % G;
-  for (uint32_t d = threadIdx.x; d < D; d += NT) cur[d] = p.tile_off[((size_t)r * D + d) * G + g];
-  for (int d = threadIdx.x; d < RADIX; d += NT) whist[d] = 0;  // rank counters
+  for (uint32_t d = threadIdx.x; d < (uint32_t)RADIX; d += NT) {
+    cur[d] = d < D ? p.tile_off[((size_t)r * D + d) * G + g] : 0ull;
+    whist[d] = 0;  // rank counters
+    dtot[d] = 0;
+    dstart[d] = 0;
+    wr[d] = 0;
+  }
   T lo;
   uint32_t sh;
-  load_digits(p, r, spl, lut, &lo, &sh);
+  load_digits(p, r, spl, lut, &lo, &sh);  // ends with a barrier
   uint64_t a, e;
   part_range(p.region_off, p.region_count, r, g, G, &a, &e);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned pos0 = (unsigned)wid * 32u * IT + lane;
+  const unsigned d0 = threadIdx.x * PER;
   for (uint64_t c0 = a; c0 < e; c0 += BATCH) {
     const unsigned cn = (unsigned)((e - c0) < (uint64_t)BATCH ? (e - c0) : (uint64_t)BATCH);
     T key[IT];
-    unsigned dg[IT], dest[IT];
+    unsigned dg[IT], rank[IT];
     bool valid[IT];
 #pragma unroll
     for (int q = 0; q < IT; ++q) {
@@ -689,21 +784,78 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
     }
 #pragma unroll
     for (int q = 0; q < IT; ++q) dg[q] = valid[q] ? digit_of_key(spl, lut, lo, sh, key[q]) : 0u;
-    atomic_rank<NT, IT, RADIX>(dg, valid, dest, whist, scan_sm, dtot, dstart);
+#pragma unroll
+    for (int q = 0; q < IT; ++q) rank[q] = valid[q] ? atomicAdd(&whist[dg[q]], 1u) : 0u;
+    __syncthreads();
+    // owned digits: the keys held back by the last batch (to registers), the
+    // new totals and stage starts, and how many keys reach a sector boundary
+    T hk[PER][KPS - 1];
+    unsigned nh[PER], nt[PER], sum = 0;
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const unsigned d = d0 + j;
+      nh[j] = nt[j] = 0;
+      if (d < (unsigned)RADIX) {
+        const unsigned w = wr[d];
+        nh[j] = dtot[d] - w;
+        const unsigned hs = dstart[d] + w;
+#pragma unroll
+        for (int k = 0; k < KPS - 1; ++k)
+          if ((unsigned)k < nh[j]) hk[j][k] = stage[hs + k];
+        cur[d] += w;
+        nt[j] = nh[j] + whist[d];
+        whist[d] = 0;
+      }
+      sum += nt[j];
+    }
+    unsigned total;
+    unsigned ex = block_exclusive_scan<NT, unsigned>(sum, scan_sm, &total);
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const unsigned d = d0 + j;
+      if (d < (unsigned)RADIX) {
+        dstart[d] = ex;
+        dtot[d] = nt[j];
+        held[d] = (uint8_t)nh[j];
+        const unsigned long long cb = cur[d];
+        const unsigned long long B = (cb + nt[j]) & ~(unsigned long long)(KPS - 1);
+        wr[d] = (uint16_t)(B > cb ? B - cb : 0ull);
+        ex += nt[j];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const unsigned d = d0 + j;
+#pragma unroll
+      for (int k = 0; k < KPS - 1; ++k)
+        if ((unsigned)k < nh[j]) {
+          stage[dstart[d] + k] = hk[j][k];
+          dig16[dstart[d] + k] = (uint16_t)d;
+        }
+    }
 #pragma unroll
     for (int q = 0; q < IT; ++q)
       if (valid[q]) {
-        stage[dest[q]] = key[q];
-        dig16[dest[q]] = (uint16_t)dg[q];
+        const unsigned at = dstart[dg[q]] + held[dg[q]] + rank[q];
+        stage[at] = key[q];
+        dig16[at] = (uint16_t)dg[q];
       }
     __syncthreads();
-    for (unsigned i = threadIdx.x; i < cn; i += NT) {
-      const unsigned d = dig16[i];
-      p.keys_out[cur[d] + (i - dstart[d])] = stage[i];
+    for (unsigned i = threadIdx.x; i < total; i += NT) {
+      const unsigned d = dig16[i], v = i - dstart[d];
+      if (v < wr[d]) p.keys_out[cur[d] + v] = stage[i];
     }
-    __syncthreads();
-    for (uint32_t d = threadIdx.x; d < D; d += NT) cur[d] += dtot[d];
-    __syncthreads();
+    // no barrier: the next batch changes the stage and the digit state only
+    // after its first barrier, which every thread reaches after this loop
+  }
+  __syncthreads();
+  // the part's last keys of every digit (a partial sector)
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const unsigned d = d0 + j;
+    if (d < (unsigned)RADIX)
+      for (unsigned k = wr[d]; k < dtot[d]; ++k) p.keys_out[cur[d] + k] = stage[dstart[d] + k];
   }
 }
 

@@ -113,7 +113,7 @@ struct kite_gpu_ctx {
   DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, splitters2, hist16;
   DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
   DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats, blk_mat, blk_gsum, blk_keys, stage_ctr;
-  DevBuf col_total, sample_first;
+  DevBuf col_total, sample_first, spans;
   HostBuf h_blocks, h_small, h_tiles, h_out, h_meta;
   std::vector<cudaEvent_t> ev;   // stage events
   std::vector<cudaEvent_t> gev;  // sort / encode / copy-out events, 8 per bucket group
@@ -227,34 +227,26 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   for (size_t c = 0; c < order.size(); ++c) order[c] = c;
   std::stable_sort(order.begin(), order.end(),
                    [&](size_t a, size_t b) { return ctx->chunks[a].sample < ctx->chunks[b].sample; });
-  std::vector<BlockDesc> hb;
   std::vector<uint32_t> sample_first(NS + 1, 0xFFFFFFFFu);
   struct Span {
     size_t chunk;
     uint32_t first, n;
   };
   std::vector<Span> spans;  // each chunk's blocks, in block order
+  std::vector<ChunkSpan> cspans;
   uint64_t chunk0_len = 0;
+  uint32_t nblocks = 0;
   for (size_t c : order) {
     const Chunk& ch = ctx->chunks[c];
     if (ch.len == 0) continue;
-    const uint32_t first = (uint32_t)hb.size();
-    if (hb.empty()) chunk0_len = ch.len;
+    const uint32_t first = nblocks;
+    if (first == 0) chunk0_len = ch.len;
     if (sample_first[ch.sample] == 0xFFFFFFFFu) sample_first[ch.sample] = first;
-    for (uint64_t o = 0; o < ch.len; o += blk) {
-      BlockDesc d;
-      d.start = ch.off + o;
-      d.end = ch.off + std::min<uint64_t>(o + blk, ch.len);
-      d.chunk_start = ch.off;
-      d.first_block = first;
-      d.flags = (first == 0) ? 2u : 0u;
-      d.sample = ch.sample;
-      d.sample_first = sample_first[ch.sample];
-      hb.push_back(d);
-    }
-    spans.push_back(Span{c, first, (uint32_t)hb.size() - first});
+    const uint32_t nb = (uint32_t)((ch.len + blk - 1) / blk);
+    cspans.push_back(ChunkSpan{ch.off, ch.len, first, first == 0 ? 2u : 0u, ch.sample, sample_first[ch.sample]});
+    spans.push_back(Span{c, first, nb});
+    nblocks += nb;
   }
-  const uint32_t nblocks = (uint32_t)hb.size();
   // samples without blocks start where the next one does
   sample_first[NS] = nblocks;
   for (int t = (int)NS - 1; t >= 0; --t)
@@ -265,10 +257,13 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     ctx->res_bytes = 0;
     return KITE_OK;
   }
-  KCU(ctx->h_blocks.ensure(hb.size() * sizeof(BlockDesc)));
-  std::memcpy(ctx->h_blocks.p, hb.data(), hb.size() * sizeof(BlockDesc));
-  KCU(ctx->blocks.ensure(hb.size() * sizeof(BlockDesc)));
-  KCU(cudaMemcpyAsync(ctx->blocks.p, ctx->h_blocks.p, hb.size() * sizeof(BlockDesc), cudaMemcpyHostToDevice, s));
+  KCU(ctx->h_blocks.ensure(cspans.size() * sizeof(ChunkSpan)));
+  std::memcpy(ctx->h_blocks.p, cspans.data(), cspans.size() * sizeof(ChunkSpan));
+  KCU(ctx->spans.ensure(cspans.size() * sizeof(ChunkSpan)));
+  KCU(cudaMemcpyAsync(ctx->spans.p, ctx->h_blocks.p, cspans.size() * sizeof(ChunkSpan), cudaMemcpyHostToDevice, s));
+  KCU(ctx->blocks.ensure((size_t)nblocks * sizeof(BlockDesc)));
+  launch_make_blocks(ctx->spans.as<ChunkSpan>(), (uint32_t)cspans.size(), blk, nblocks, ctx->blocks.as<BlockDesc>(), s);
+  st.kernel_launches += 1;
   KCU(ctx->nl.ensure((size_t)nblocks * 8));
   KCU(ctx->scan_tmp.ensure(scan_tmp_elems(std::max<size_t>((size_t)nblocks, (size_t)PT * 4096)) * 8 + 64));
   KCU(ctx->status.ensure(sizeof(DevStatus)));
@@ -929,7 +924,7 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
                     &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out,
                     &ctx->lvl_count, &ctx->lvl_off, &ctx->reg_off, &ctx->reg_cnt, &ctx->sort_stats,
                     &ctx->blk_mat, &ctx->blk_gsum, &ctx->blk_keys, &ctx->stage_ctr,
-                    &ctx->col_total, &ctx->sample_first};
+                    &ctx->col_total, &ctx->sample_first, &ctx->spans};
   for (DevBuf* b : bufs) b->release();
   ctx->h_blocks.release();
   ctx->h_small.release();

@@ -21,6 +21,16 @@ struct BlockDesc {
   uint32_t sample_first;  // index of the sample's first block (blocks of a sample are contiguous)
 };
 
+// One chunk's run of extraction blocks (the block descriptors are made on
+// the device from these).
+struct ChunkSpan {
+  uint64_t off, len;      // arena offset and length of the chunk
+  uint32_t first_block;   // index of its first block
+  uint32_t flags;         // copied to its blocks
+  uint32_t sample;        // sample of a batched count
+  uint32_t sample_first;  // index of the sample's first block
+};
+
 // A key-range tile: the on-chip sort unit.
 struct TileDesc {
   uint64_t start;   // key index of the tile's first key
@@ -101,6 +111,8 @@ struct TileSplitParams {
 };
 
 // ---- launchers (count_kernels.cu) ----
+void launch_make_blocks(const ChunkSpan* spans, uint32_t nspans, uint32_t blk, uint32_t nblocks, BlockDesc* out,
+                        cudaStream_t s);
 void launch_newline_count(const uint8_t* arena, const BlockDesc* blocks, uint32_t nblocks,
                           unsigned long long* nl_out, cudaStream_t s);
 template <class T>

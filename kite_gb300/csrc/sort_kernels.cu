@@ -108,23 +108,26 @@ __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, u
 //     still sits in L2).  Bins are key-ordered; order inside a bin is
 //     arbitrary, so every later pass reads shared memory directly;
 //  3. a bin holding more than one distinct key is found where two different
-//     neighbours share it, and listed once (a shared bit per bin);
-//  4. a small listed bin (<= kSmallBin keys, typically two colliding k-mers)
-//     is insertion-sorted in place by one thread.  A larger one (typically a
-//     heavily repeated k-mer next to a few others) belongs to one warp: up to
-//     32 keys are ranked by counting across the lanes; beyond that the warp
-//     extracts the bin's distinct keys in ascending order with their counts
-//     and rewrites the bin with them (equal keys are interchangeable).  A bin
-//     of more than kMaxDistinct distinct keys is ranked by counting when it
+//     neighbours share it, and marked (a shared bit per bin);
+//  4. a marked bin of at most kSmallBin keys (typically two colliding
+//     k-mers) is insertion-sorted by the thread owning its bit; a larger one
+//     (typically a repeated k-mer and a colliding one) by the warp owning its
+//     bit word.  Up to 32 keys sit one per lane: lanes with equal keys find
+//     each other by a match, and each key's new position is the copies of
+//     the smaller distinct keys plus its equal predecessors.  A larger bin
+//     has its distinct keys extracted in ascending order with their counts
+//     and is rewritten with them (equal keys are interchangeable).  A bin of
+//     more than kMaxDistinct distinct keys is ranked by counting when it
 //     holds at most kMaxMixed keys and otherwise sends the tile to LSD passes;
 //  5. run-length reduction over the sorted keys: head flags by warp ballots,
 //     rows written to global memory over the tile's keys (u32 counts; a tile
 //     holds fewer than 2^32 keys, so no count saturates here).
 // ---------------------------------------------------------------------------
 constexpr int kBinBits = 12, kBins = 1 << kBinBits;
-constexpr unsigned kSmallBin = 16;     // mixed bins a single thread sorts
+constexpr unsigned kSmallBin = 16;     // marked bins a single thread sorts
 constexpr unsigned kMaxMixed = 256;    // largest bin ranked by counting when it has many distinct keys
 constexpr unsigned kMaxDistinct = 32;  // distinct keys a warp extracts from one large bin
+constexpr int kLoadBatch = 8;          // global loads a thread keeps in flight
 
 // MULT = 1: the regular tile (8192 u64 / 4096 u128 keys, two CTAs per SM);
 // MULT = 2: twice that for the few oversized tiles (one CTA per SM).
@@ -134,25 +137,55 @@ struct BinSmem {
   static constexpr int ITEMS = tile_items<T>() * MULT;
   static constexpr int CAP = NT * ITEMS;
   static constexpr int NW = NT / 32;
-  static constexpr unsigned MAXSMALL = CAP / 2;                   // a mixed bin holds >= 2 keys
-  static constexpr unsigned MAXLARGE = CAP / (kSmallBin + 1) + 1;  // ... a large one > kSmallBin
   static constexpr size_t buf_bytes = (size_t)CAP * sizeof(T);
   // bin counters; later the u16 run heads (CAP + 1 entries), or the LSD
   // fallback's per-warp digit histograms (256 * NW counters)
   static constexpr size_t head_need = ((size_t)(CAP + 1) * 2 + 15) & ~(size_t)15;
   static constexpr size_t bin_bytes = ((size_t)kBins * 4 > head_need ? (size_t)kBins * 4 : head_need) + 16;
   static constexpr size_t fbit_bytes = kBins / 8;
-  static constexpr size_t list_bytes = ((size_t)(MAXSMALL + MAXLARGE) * 2 + 15) & ~(size_t)15;
   static constexpr size_t misc_bytes = 64 * 8 + 2 * NW * sizeof(T) + 16;
-  static constexpr size_t total = buf_bytes + bin_bytes + fbit_bytes + list_bytes + misc_bytes;
+  static constexpr size_t total = buf_bytes + bin_bytes + fbit_bytes + misc_bytes;
   static_assert((size_t)(CAP + 1) * 2 <= bin_bytes, "run heads must fit the bin area");
   static_assert((size_t)256 * NW * 4 <= bin_bytes, "LSD histograms must fit the bin area");
   static_assert(kBins % (4 * NT) == 0, "bin scan takes whole uint4 groups");
+  static_assert(kBins % (32 * NW) == 0, "every warp owns whole words of bin marks");
+  static_assert(kBins % NT == 0 && kBins / NT <= 32 && 32 % (kBins / NT) == 0, "every thread owns bin marks in one word");
 };
 
 template <class T>
 __device__ __forceinline__ unsigned bin_of(T key, T mn, int s) {
   return (unsigned)(uint64_t)((key - mn) >> s);
+}
+
+template <class T>
+__device__ __forceinline__ unsigned match_key(T v) {
+  unsigned eq = __match_any_sync(0xffffffffu, (unsigned long long)(uint64_t)v);
+  if (sizeof(T) > 8) eq &= __match_any_sync(0xffffffffu, (unsigned long long)hi64(v));
+  return eq;
+}
+
+// One warp orders buf[a, a + m), m <= 32, one key per lane: a key's new
+// position is the copies of the smaller distinct keys (one shuffle per
+// distinct key, from its lowest lane) plus its equal predecessors.
+template <class T>
+__device__ __forceinline__ void warp_match_sort(T* buf, unsigned a, unsigned m, unsigned lane) {
+  const bool act = lane < m;
+  const T mine = act ? buf[a + lane] : T(0);
+  const unsigned amask = m >= 32 ? 0xffffffffu : ((1u << m) - 1u);
+  const unsigned eq = match_key(mine) & amask;
+  const unsigned leaders = __ballot_sync(0xffffffffu, act && (unsigned)(__ffs(eq) - 1) == lane);
+  const unsigned cnt = __popc(eq);
+  unsigned less = 0;
+  for (unsigned L = leaders; L; L &= L - 1) {
+    const int l = __ffs(L) - 1;
+    const T kl = shfl_key(mine, l);
+    const unsigned cl = __shfl_sync(0xffffffffu, cnt, l);
+    less += kl < mine ? cl : 0u;
+  }
+  const unsigned pos = a + less + __popc(eq & ((1u << lane) - 1u));
+  __syncwarp();
+  if (act) buf[pos] = mine;
+  __syncwarp();
 }
 
 // One warp orders buf[a, a + m), m <= kMaxMixed, by counting: each key's new
@@ -246,13 +279,10 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
   T* buf = reinterpret_cast<T*>(sm);
   unsigned* bins = reinterpret_cast<unsigned*>(sm + L::buf_bytes);
   unsigned* fbits = reinterpret_cast<unsigned*>(sm + L::buf_bytes + L::bin_bytes);
-  unsigned short* small_list = reinterpret_cast<unsigned short*>(sm + L::buf_bytes + L::bin_bytes + L::fbit_bytes);
-  unsigned short* large_list = small_list + L::MAXSMALL;
-  unsigned long long* scan64 =
-      reinterpret_cast<unsigned long long*>(sm + L::buf_bytes + L::bin_bytes + L::fbit_bytes + L::list_bytes);
+  unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(sm + L::buf_bytes + L::bin_bytes + L::fbit_bytes);
   unsigned* scan_sm = reinterpret_cast<unsigned*>(scan64);
   T* red = reinterpret_cast<T*>(scan64 + 64);
-  unsigned* misc = reinterpret_cast<unsigned*>(red + 2 * NW);  // [0] LSD fallback, [1] small bins, [2] large bins
+  unsigned* misc = reinterpret_cast<unsigned*>(red + 2 * NW);  // [0] LSD fallback
 
   const uint32_t tid = ids ? ids[blockIdx.x] : blockIdx.x;
   const TileDesc td = tiles[tid];
@@ -272,11 +302,23 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
   T* g = keys + td.start;
   uint32_t* gc = counts + td.start;
   T mn = ~T(0), mx = T(0);
-  for (unsigned i = threadIdx.x; i < n; i += NT) {
-    const T v = g[i];
-    buf[i] = v;
-    mn = v < mn ? v : mn;
-    mx = v > mx ? v : mx;
+  // kLoadBatch independent loads in flight per thread
+  for (unsigned i0 = threadIdx.x; i0 < n; i0 += NT * kLoadBatch) {
+    T v[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const unsigned i = i0 + u * NT;
+      v[u] = i < n ? g[i] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const unsigned i = i0 + u * NT;
+      if (i < n) {
+        buf[i] = v[u];
+        mn = v[u] < mn ? v[u] : mn;
+        mx = v[u] > mx ? v[u] : mx;
+      }
+    }
   }
   block_minmax<NT>(mn, mx, red);
   if (mn == mx) {  // one key fills the tile
@@ -329,58 +371,41 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
     }
   }
   __syncthreads();
-#pragma unroll 4
-  for (unsigned i = threadIdx.x; i < n; i += NT) {
-    const T v = g[i];
-    buf[atomicAdd(&bins[bin_of(v, mn, s)], 1u)] = v;
+  for (unsigned i0 = threadIdx.x; i0 < n; i0 += NT * kLoadBatch) {
+    T v[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const unsigned i = i0 + u * NT;
+      v[u] = i < n ? g[i] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u)
+      if (i0 + u * NT < n) buf[atomicAdd(&bins[bin_of(v[u], mn, s)], 1u)] = v[u];
   }
   __syncthreads();
   // bins[b] is now the end of bin b; its start is bins[b - 1] (0 for b = 0)
 
-  // ---- 3. list the bins holding more than one distinct key ----
+  // ---- 3. mark the bins holding more than one distinct key ----
   for (unsigned p = threadIdx.x + 1; p < n; p += NT) {
     const T a = buf[p], b = buf[p - 1];
     if (a != b) {
       const unsigned ba = bin_of(a, mn, s);
-      if (bin_of(b, mn, s) == ba) {
-        const unsigned bit = 1u << (ba & 31);
-        if (!(atomicOr(&fbits[ba >> 5], bit) & bit)) {
-          const unsigned m = bins[ba] - (ba ? bins[ba - 1] : 0u);
-          if (m <= kSmallBin) small_list[atomicAdd(&misc[1], 1u)] = (unsigned short)ba;
-          else large_list[atomicAdd(&misc[2], 1u)] = (unsigned short)ba;
-        }
-      }
+      if (bin_of(b, mn, s) == ba) atomicOr(&fbits[ba >> 5], 1u << (ba & 31));
     }
   }
   __syncthreads();
 
-  // ---- 4. order the listed bins ----
+  // ---- 4. order the marked bins: small ones by the thread owning their
+  // bits, larger ones by the warp owning their bit words ----
   {
+    constexpr int BPT = kBins / NT, WORDS = kBins / 32 / NW;
     const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const unsigned nlarge = misc[2];
-    for (unsigned li = wid; li < nlarge; li += NW) {
-      const unsigned bb = large_list[li];
-      const unsigned a = bb ? bins[bb - 1] : 0u, m = bins[bb] - a;
-      if (m <= 32) {
-        // rank by counting across the lanes
-        const T mine = lane < m ? buf[a + lane] : T(0);
-        unsigned r = 0;
-        for (unsigned t = 0; t < m; ++t) {
-          const T v = shfl_key(mine, (int)t);
-          r += (unsigned)(v < mine) | ((unsigned)(v == mine) & (unsigned)(t < lane));
-        }
-        __syncwarp();
-        if (lane < m) buf[a + r] = mine;
-        __syncwarp();
-      } else if (!warp_distinct_sort(buf, a, m, lane)) {
-        if (m <= kMaxMixed) warp_count_sort(buf, a, m, lane);
-        else if (lane == 0) misc[0] = 1;
-      }
-    }
-    const unsigned nsmall = misc[1];
-    for (unsigned i = threadIdx.x; i < nsmall; i += NT) {
-      const unsigned bb = small_list[i];
+    const unsigned b0 = threadIdx.x * BPT;
+    for (unsigned bits = (fbits[b0 >> 5] >> (b0 & 31)) & (BPT == 32 ? 0xffffffffu : ((1u << BPT) - 1u)); bits;
+         bits &= bits - 1) {
+      const unsigned bb = b0 + (__ffs(bits) - 1);
       const unsigned a = bb ? bins[bb - 1] : 0u, e = bins[bb];
+      if (e - a > kSmallBin) continue;
       for (unsigned j = a + 1; j < e; ++j) {
         const T v = buf[j];
         unsigned q = j;
@@ -391,6 +416,19 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
           --q;
         }
         buf[q] = v;
+      }
+    }
+    for (int wi = 0; wi < WORDS; ++wi) {
+      const unsigned word = wid * WORDS + wi;
+      for (unsigned bits = fbits[word]; bits; bits &= bits - 1) {
+        const unsigned bb = word * 32 + (__ffs(bits) - 1);
+        const unsigned a = bb ? bins[bb - 1] : 0u, m = bins[bb] - a;
+        if (m <= kSmallBin) continue;
+        if (m <= 32) warp_match_sort(buf, a, m, lane);
+        else if (!warp_distinct_sort(buf, a, m, lane)) {
+          if (m <= kMaxMixed) warp_count_sort(buf, a, m, lane);
+          else if (lane == 0) misc[0] = 1;
+        }
       }
     }
   }
