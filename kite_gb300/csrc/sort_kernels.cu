@@ -3,7 +3,7 @@
 // :388-437, then rle_compress_typed :514-530 with u32 saturation).
 //
 // A tile is a key range of one hash bucket.  One CTA loads the whole tile into
-// shared memory, orders it by a 4096-bin counting pass over its key span (bins
+// shared memory, orders it by a 16384-bin counting pass over its key span (bins
 // holding several distinct keys are finished by a thread or a warp, rare
 // pathological ones by LSD passes), then emits unique (key, count) rows in
 // place and the tile's DVLE size for every row but the first.
@@ -102,7 +102,7 @@ __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, u
 // ---------------------------------------------------------------------------
 // Tile sort by binning.  One CTA per tile of n <= CAP keys:
 //  1. load the tile into shared memory; block min / max;
-//  2. bin = (key - min) >> s with 4096 bins spanning [min, max]: histogram by
+//  2. bin = (key - min) >> s with 16384 bins spanning [min, max]: histogram by
 //     shared atomics and an exclusive scan; then the keys themselves are
 //     scattered into bin order (re-read from global memory, where the tile
 //     still sits in L2).  Bins are key-ordered; order inside a bin is
@@ -123,7 +123,9 @@ __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, u
 //     rows written to global memory over the tile's keys (u32 counts; a tile
 //     holds fewer than 2^32 keys, so no count saturates here).
 // ---------------------------------------------------------------------------
-constexpr int kBinBits = 12, kBins = 1 << kBinBits;
+// 16384 bins with 16-bit counters packed two to a word (a tile holds at most
+// 16384 keys, so no half carries into the other)
+constexpr int kBinBits = 14, kBins = 1 << kBinBits;
 constexpr unsigned kSmallBin = 16;     // marked bins a single thread sorts
 constexpr unsigned kMaxMixed = 256;    // largest bin ranked by counting when it has many distinct keys
 constexpr unsigned kMaxDistinct = 32;  // distinct keys a warp extracts from one large bin
@@ -141,13 +143,14 @@ struct BinSmem {
   // bin counters; later the u16 run heads (CAP + 1 entries), or the LSD
   // fallback's per-warp digit histograms (256 * NW counters)
   static constexpr size_t head_need = ((size_t)(CAP + 1) * 2 + 15) & ~(size_t)15;
-  static constexpr size_t bin_bytes = ((size_t)kBins * 4 > head_need ? (size_t)kBins * 4 : head_need) + 16;
+  static constexpr size_t bin_bytes = ((size_t)kBins * 2 > head_need ? (size_t)kBins * 2 : head_need) + 16;
   static constexpr size_t fbit_bytes = kBins / 8;
   static constexpr size_t misc_bytes = 64 * 8 + 2 * NW * sizeof(T) + 16;
   static constexpr size_t total = buf_bytes + bin_bytes + fbit_bytes + misc_bytes;
   static_assert((size_t)(CAP + 1) * 2 <= bin_bytes, "run heads must fit the bin area");
   static_assert((size_t)256 * NW * 4 <= bin_bytes, "LSD histograms must fit the bin area");
-  static_assert(kBins % (4 * NT) == 0, "bin scan takes whole uint4 groups");
+  static_assert(kBins / 2 % (4 * NT) == 0, "bin scan takes whole uint4 groups");
+  static_assert(CAP <= 65535, "bin offsets fit 16 bits");
   static_assert(kBins % (32 * NW) == 0, "every warp owns whole words of bin marks");
   static_assert(kBins % NT == 0 && kBins / NT <= 32 && 32 % (kBins / NT) == 0, "every thread owns bin marks in one word");
 };
@@ -155,6 +158,15 @@ struct BinSmem {
 template <class T>
 __device__ __forceinline__ unsigned bin_of(T key, T mn, int s) {
   return (unsigned)(uint64_t)((key - mn) >> s);
+}
+
+// Packed 16-bit bin counters: bin b is half (b & 1) of word b >> 1.
+__device__ __forceinline__ unsigned bin_add(unsigned* bins, unsigned b) {
+  const unsigned sh = (b & 1u) << 4;
+  return (atomicAdd(&bins[b >> 1], 1u << sh) >> sh) & 0xffffu;
+}
+__device__ __forceinline__ unsigned bin_get(const unsigned* bins, unsigned b) {
+  return (bins[b >> 1] >> ((b & 1u) << 4)) & 0xffffu;
 }
 
 template <class T>
@@ -338,35 +350,38 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
   const int s = rb > kBinBits ? rb - kBinBits : 0;
 
   // ---- 2. bin histogram, scan, key scatter into bin order ----
-  for (int b = threadIdx.x; b < kBins; b += NT) bins[b] = 0;
+  for (int b = threadIdx.x; b < kBins / 2; b += NT) bins[b] = 0;
   for (int b = threadIdx.x; b < kBins / 32; b += NT) fbits[b] = 0;
   if (threadIdx.x < 4) misc[threadIdx.x] = 0;
   __syncthreads();
-  for (unsigned i = threadIdx.x; i < n; i += NT) atomicAdd(&bins[bin_of(buf[i], mn, s)], 1u);
+  for (unsigned i = threadIdx.x; i < n; i += NT) bin_add(bins, bin_of(buf[i], mn, s));
   __syncthreads();
   {
-    constexpr int G = kBins / (4 * NT);  // uint4 groups per thread
+    constexpr int G = kBins / 2 / (4 * NT);  // uint4 groups (8 bins each) per thread
     uint4* b4 = reinterpret_cast<uint4*>(bins) + threadIdx.x * G;
     uint4 x[G];
     unsigned sum = 0;
 #pragma unroll
     for (int j = 0; j < G; ++j) {
       x[j] = b4[j];
-      sum += x[j].x + x[j].y + x[j].z + x[j].w;
+      const unsigned w2 = x[j].x + x[j].y + x[j].z + x[j].w;  // both halves, no carry across
+      sum += (w2 & 0xffffu) + (w2 >> 16);
     }
     unsigned tot;
     unsigned pre = block_exclusive_scan<NT, unsigned>(sum, scan_sm, &tot);
+    // each word becomes (start of its even bin) | (start of its odd bin) << 16
+    auto put = [&](unsigned w) {
+      const unsigned r = pre | ((pre + (w & 0xffffu)) << 16);
+      pre += (w & 0xffffu) + (w >> 16);
+      return r;
+    };
 #pragma unroll
     for (int j = 0; j < G; ++j) {
       uint4 y;
-      y.x = pre;
-      pre += x[j].x;
-      y.y = pre;
-      pre += x[j].y;
-      y.z = pre;
-      pre += x[j].z;
-      y.w = pre;
-      pre += x[j].w;
+      y.x = put(x[j].x);
+      y.y = put(x[j].y);
+      y.z = put(x[j].z);
+      y.w = put(x[j].w);
       b4[j] = y;
     }
   }
@@ -380,10 +395,10 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
     }
 #pragma unroll
     for (int u = 0; u < kLoadBatch; ++u)
-      if (i0 + u * NT < n) buf[atomicAdd(&bins[bin_of(v[u], mn, s)], 1u)] = v[u];
+      if (i0 + u * NT < n) buf[bin_add(bins, bin_of(v[u], mn, s))] = v[u];
   }
   __syncthreads();
-  // bins[b] is now the end of bin b; its start is bins[b - 1] (0 for b = 0)
+  // bin_get(b) is now the end of bin b; its start is the end of bin b - 1 (0 for b = 0)
 
   // ---- 3. mark the bins holding more than one distinct key ----
   for (unsigned p = threadIdx.x + 1; p < n; p += NT) {
@@ -404,7 +419,7 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
     for (unsigned bits = (fbits[b0 >> 5] >> (b0 & 31)) & (BPT == 32 ? 0xffffffffu : ((1u << BPT) - 1u)); bits;
          bits &= bits - 1) {
       const unsigned bb = b0 + (__ffs(bits) - 1);
-      const unsigned a = bb ? bins[bb - 1] : 0u, e = bins[bb];
+      const unsigned a = bb ? bin_get(bins, bb - 1) : 0u, e = bin_get(bins, bb);
       if (e - a > kSmallBin) continue;
       for (unsigned j = a + 1; j < e; ++j) {
         const T v = buf[j];
@@ -422,7 +437,7 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
       const unsigned word = wid * WORDS + wi;
       for (unsigned bits = fbits[word]; bits; bits &= bits - 1) {
         const unsigned bb = word * 32 + (__ffs(bits) - 1);
-        const unsigned a = bb ? bins[bb - 1] : 0u, m = bins[bb] - a;
+        const unsigned a = bb ? bin_get(bins, bb - 1) : 0u, m = bin_get(bins, bb) - a;
         if (m <= kSmallBin) continue;
         if (m <= 32) warp_match_sort(buf, a, m, lane);
         else if (!warp_distinct_sort(buf, a, m, lane)) {
