@@ -460,6 +460,7 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   st.tiles_per_bucket = S;
   T* sorted = ctx->keys_a.as<T>();
   T* scratch = ctx->keys_b.as<T>();
+  const T* tile_spl = nullptr;  // the splitters that cut every bucket into its S tiles
   std::vector<TileDesc> ht;
   if (S == 1) {
     for (uint32_t b = 0; b < PT; ++b) ht.push_back(TileDesc{boff[b], (uint32_t)bcount[b], b});
@@ -503,6 +504,7 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     st.hist_pred_imbalance = hist_imb;
     st.splitter_used = learned ? KITE_SPLIT_LEARNED : KITE_SPLIT_SAMPLED;
     const T* chosen = learned ? mlp_spl : hist_spl;
+    tile_spl = chosen;
     // Split into tiles: one level of S digits when S <= 1024, else coarse
     // ranges of 1024 tiles first, then the tiles inside each coarse range.
     // G parts per region (parts of >= 32K keys, G <= 64): the fewest parts
@@ -612,6 +614,7 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   KCU(cudaEventRecord(ctx->ev[4], s));
   const uint32_t ntiles = (uint32_t)ht.size();
   const uint32_t Sl = ntiles / PT;  // tiles per bucket
+  const T kmax = 2 * k >= (uint32_t)KeyTraits<T>::kBits ? ~T(0) : ((T(1) << (2 * k)) - T(1));
   // Bucket groups: each group's tiles are sorted, linked and encoded in turn,
   // so one group's payload copies to the host while the next one sorts.
   const uint32_t NG = std::min<uint32_t>(kSortGroups, PT);
@@ -680,11 +683,11 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     const uint32_t t0 = gb[g] * Sl, nt = (gb[g + 1] - gb[g]) * Sl, nb = gb[g + 1] - gb[g];
     cudaEventRecord(gev[8 * g], s);
     launch_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>() + t0, nt, tout + t0,
-                        ctx->sort_stats.as<unsigned long long>(), s);
+                        ctx->sort_stats.as<unsigned long long>(), TileRanges<T>{tile_spl, Sl, t0, kmax}, s);
     cudaEventRecord(gev[8 * g + 1], s);
     launch_tile_sort_large<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(),
                               ctx->big_ids.as<uint32_t>() + gbig[g], glarge[g], tout,
-                              ctx->sort_stats.as<unsigned long long>(), s);
+                              ctx->sort_stats.as<unsigned long long>(), TileRanges<T>{tile_spl, Sl, 0, kmax}, s);
     launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(),
                             ctx->big_ids.as<uint32_t>() + gbig[g] + glarge[g], gbig[g + 1] - gbig[g] - glarge[g], tout,
                             ctx->status.as<DevStatus>(), s);

@@ -165,15 +165,26 @@ constexpr int kTileThreads = 512;
 template <class T> __host__ __device__ constexpr int tile_items() { return sizeof(T) == 8 ? 16 : 8; }
 template <class T> __host__ __device__ constexpr uint32_t tile_capacity() { return (uint32_t)(kTileThreads * tile_items<T>()); }
 
+// Key range of every tile: tile t of a bucket holds the keys in
+// [spl[t-1], spl[t]) (0 and kmax close the ends), S tiles per bucket; tile
+// index of a launch's tile i = tile0 + i.
+template <class T>
+struct TileRanges {
+  const T* spl;
+  uint32_t S;
+  uint32_t tile0;
+  T kmax;
+};
+
 // `fallbacks` (device counter) counts tiles that took the LSD fallback.
 template <class T>
 void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
-                      unsigned long long* fallbacks, cudaStream_t s);
+                      unsigned long long* fallbacks, TileRanges<T> rg, cudaStream_t s);
 // Tiles of tile_capacity < len <= 2 * tile_capacity, listed in ids: the same
 // on-chip sort with twice the shared memory (one CTA per SM).
 template <class T>
 void launch_tile_sort_large(T* keys, uint32_t* counts, const TileDesc* tiles, const uint32_t* ids, uint32_t nids,
-                            TileOut<T>* out, unsigned long long* fallbacks, cudaStream_t s);
+                            TileOut<T>* out, unsigned long long* fallbacks, TileRanges<T> rg, cudaStream_t s);
 // Oversized tiles (more keys than 2 * tile_capacity): one CTA per tile, LSD
 // passes through global memory with `scratch` (>= largest tile keys).
 template <class T>

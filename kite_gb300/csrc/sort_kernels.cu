@@ -101,9 +101,10 @@ __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, u
 
 // ---------------------------------------------------------------------------
 // Tile sort by binning.  One CTA per tile of n <= CAP keys:
-//  1. load the tile into shared memory; block min / max;
-//  2. bin = (key - min) >> s with 16384 bins spanning [min, max]: histogram by
-//     shared atomics and an exclusive scan; then the keys themselves are
+//  1. load the tile into shared memory, counting the keys per bin on the way:
+//     bin = (key - lo) >> s with 16384 bins spanning the tile's key range
+//     [lo, hi] (its splitters);
+//  2. an exclusive scan of the bin counts; then the keys themselves are
 //     scattered into bin order (re-read from global memory, where the tile
 //     still sits in L2).  Bins are key-ordered; order inside a bin is
 //     arbitrary, so every later pass reads shared memory directly;
@@ -145,7 +146,8 @@ struct BinSmem {
   static constexpr size_t head_need = ((size_t)(CAP + 1) * 2 + 15) & ~(size_t)15;
   static constexpr size_t bin_bytes = ((size_t)kBins * 2 > head_need ? (size_t)kBins * 2 : head_need) + 16;
   static constexpr size_t fbit_bytes = kBins / 8;
-  static constexpr size_t misc_bytes = 64 * 8 + 2 * NW * sizeof(T) + 16;
+  static constexpr unsigned MAXLARGE = CAP / (kSmallBin + 1) + 1;  // marked bins above kSmallBin keys
+  static constexpr size_t misc_bytes = 64 * 8 + 16 + ((MAXLARGE * 2 + 15) & ~(size_t)15);
   static constexpr size_t total = buf_bytes + bin_bytes + fbit_bytes + misc_bytes;
   static_assert((size_t)(CAP + 1) * 2 <= bin_bytes, "run heads must fit the bin area");
   static_assert((size_t)256 * NW * 4 <= bin_bytes, "LSD histograms must fit the bin area");
@@ -284,7 +286,8 @@ __device__ __forceinline__ bool warp_distinct_sort(T* buf, unsigned a, unsigned 
 template <class T, int MULT>
 __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
     k_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, const TileDesc* __restrict__ tiles,
-                const uint32_t* __restrict__ ids, TileOut<T>* __restrict__ tout, unsigned long long* fallbacks) {
+                const uint32_t* __restrict__ ids, TileOut<T>* __restrict__ tout, unsigned long long* fallbacks,
+                TileRanges<T> rg) {
   using L = BinSmem<T, MULT>;
   constexpr int NT = L::NT, NW = L::NW, ITEMS = L::ITEMS;
   extern __shared__ __align__(16) uint8_t sm[];
@@ -293,8 +296,8 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
   unsigned* fbits = reinterpret_cast<unsigned*>(sm + L::buf_bytes + L::bin_bytes);
   unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(sm + L::buf_bytes + L::bin_bytes + L::fbit_bytes);
   unsigned* scan_sm = reinterpret_cast<unsigned*>(scan64);
-  T* red = reinterpret_cast<T*>(scan64 + 64);
-  unsigned* misc = reinterpret_cast<unsigned*>(red + 2 * NW);  // [0] LSD fallback
+  unsigned* misc = reinterpret_cast<unsigned*>(scan64 + 64);  // [0] LSD fallback, [1] large bins
+  unsigned short* large = reinterpret_cast<unsigned short*>(misc + 4);
 
   const uint32_t tid = ids ? ids[blockIdx.x] : blockIdx.x;
   const TileDesc td = tiles[tid];
@@ -313,7 +316,26 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
   }
   T* g = keys + td.start;
   uint32_t* gc = counts + td.start;
-  T mn = ~T(0), mx = T(0);
+  // the tile's key range from its splitters
+  const uint32_t tl = rg.S > 1 ? (rg.tile0 + tid) % rg.S : 0u;
+  const T mn = tl > 0 ? rg.spl[tl - 1] : T(0);
+  T mx = rg.kmax;
+  if (tl + 1 < rg.S) {
+    const T e = rg.spl[tl];
+    mx = e > mn ? T(e - T(1)) : mn;
+  }
+  const int rb = mx == mn ? 0 : KeyTraits<T>::kBits - clz_key(T(mx - mn));
+  const int s = rb > kBinBits ? rb - kBinBits : 0;
+  auto bin_at = [&](T key) -> unsigned {  // clamped: a key outside the range cannot leave the table
+    const unsigned b = key < mn ? 0u : bin_of(key, mn, s);
+    return b < (unsigned)kBins ? b : (unsigned)kBins - 1u;
+  };
+
+  // ---- 1. load with the bin histogram; 2. scan, key scatter into bin order ----
+  for (int b = threadIdx.x; b < kBins / 2; b += NT) bins[b] = 0;
+  for (int b = threadIdx.x; b < kBins / 32; b += NT) fbits[b] = 0;
+  if (threadIdx.x < 4) misc[threadIdx.x] = 0;
+  __syncthreads();
   // kLoadBatch independent loads in flight per thread
   for (unsigned i0 = threadIdx.x; i0 < n; i0 += NT * kLoadBatch) {
     T v[kLoadBatch];
@@ -327,34 +349,10 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
       const unsigned i = i0 + u * NT;
       if (i < n) {
         buf[i] = v[u];
-        mn = v[u] < mn ? v[u] : mn;
-        mx = v[u] > mx ? v[u] : mx;
+        bin_add(bins, bin_at(v[u]));
       }
     }
   }
-  block_minmax<NT>(mn, mx, red);
-  if (mn == mx) {  // one key fills the tile
-    if (threadIdx.x == 0) {
-      g[0] = mn;
-      gc[0] = n;
-      TileOut<T> o;
-      o.first_key = o.last_key = mn;
-      o.rows = 1;
-      o.first_count = n;
-      o.rest_bytes = 0;
-      tout[tid] = o;
-    }
-    return;
-  }
-  const int rb = KeyTraits<T>::kBits - clz_key(T(mx - mn));
-  const int s = rb > kBinBits ? rb - kBinBits : 0;
-
-  // ---- 2. bin histogram, scan, key scatter into bin order ----
-  for (int b = threadIdx.x; b < kBins / 2; b += NT) bins[b] = 0;
-  for (int b = threadIdx.x; b < kBins / 32; b += NT) fbits[b] = 0;
-  if (threadIdx.x < 4) misc[threadIdx.x] = 0;
-  __syncthreads();
-  for (unsigned i = threadIdx.x; i < n; i += NT) bin_add(bins, bin_of(buf[i], mn, s));
   __syncthreads();
   {
     constexpr int G = kBins / 2 / (4 * NT);  // uint4 groups (8 bins each) per thread
@@ -395,7 +393,7 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
     }
 #pragma unroll
     for (int u = 0; u < kLoadBatch; ++u)
-      if (i0 + u * NT < n) buf[bin_add(bins, bin_of(v[u], mn, s))] = v[u];
+      if (i0 + u * NT < n) buf[bin_add(bins, bin_at(v[u]))] = v[u];
   }
   __syncthreads();
   // bin_get(b) is now the end of bin b; its start is the end of bin b - 1 (0 for b = 0)
@@ -404,16 +402,22 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
   for (unsigned p = threadIdx.x + 1; p < n; p += NT) {
     const T a = buf[p], b = buf[p - 1];
     if (a != b) {
-      const unsigned ba = bin_of(a, mn, s);
-      if (bin_of(b, mn, s) == ba) atomicOr(&fbits[ba >> 5], 1u << (ba & 31));
+      const unsigned ba = bin_at(a);
+      if (bin_at(b) == ba) {
+        const unsigned bit = 1u << (ba & 31);
+        if (!(atomicOr(&fbits[ba >> 5], bit) & bit)) {
+          const unsigned m = bin_get(bins, ba) - (ba ? bin_get(bins, ba - 1) : 0u);
+          if (m > kSmallBin) large[atomicAdd(&misc[1], 1u)] = (unsigned short)ba;
+        }
+      }
     }
   }
   __syncthreads();
 
   // ---- 4. order the marked bins: small ones by the thread owning their
-  // bits, larger ones by the warp owning their bit words ----
+  // bits, the listed larger ones by the warps in turn ----
   {
-    constexpr int BPT = kBins / NT, WORDS = kBins / 32 / NW;
+    constexpr int BPT = kBins / NT;
     const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const unsigned b0 = threadIdx.x * BPT;
     for (unsigned bits = (fbits[b0 >> 5] >> (b0 & 31)) & (BPT == 32 ? 0xffffffffu : ((1u << BPT) - 1u)); bits;
@@ -433,17 +437,14 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
         buf[q] = v;
       }
     }
-    for (int wi = 0; wi < WORDS; ++wi) {
-      const unsigned word = wid * WORDS + wi;
-      for (unsigned bits = fbits[word]; bits; bits &= bits - 1) {
-        const unsigned bb = word * 32 + (__ffs(bits) - 1);
-        const unsigned a = bb ? bin_get(bins, bb - 1) : 0u, m = bin_get(bins, bb) - a;
-        if (m <= kSmallBin) continue;
-        if (m <= 32) warp_match_sort(buf, a, m, lane);
-        else if (!warp_distinct_sort(buf, a, m, lane)) {
-          if (m <= kMaxMixed) warp_count_sort(buf, a, m, lane);
-          else if (lane == 0) misc[0] = 1;
-        }
+    const unsigned nlarge = misc[1];
+    for (unsigned li = wid; li < nlarge; li += NW) {
+      const unsigned bb = large[li];
+      const unsigned a = bb ? bin_get(bins, bb - 1) : 0u, m = bin_get(bins, bb) - a;
+      if (m <= 32) warp_match_sort(buf, a, m, lane);
+      else if (!warp_distinct_sort(buf, a, m, lane)) {
+        if (m <= kMaxMixed) warp_count_sort(buf, a, m, lane);
+        else if (lane == 0) misc[0] = 1;
       }
     }
   }
@@ -503,31 +504,32 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
 
 template <class T, int MULT>
 static void tile_sort_with(T* keys, uint32_t* counts, const TileDesc* tiles, const uint32_t* ids, uint32_t n,
-                           TileOut<T>* out, unsigned long long* fallbacks, cudaStream_t s) {
+                           TileOut<T>* out, unsigned long long* fallbacks, TileRanges<T> rg, cudaStream_t s) {
   const size_t smem = BinSmem<T, MULT>::total;
   cudaFuncSetAttribute(k_tile_sort<T, MULT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(k_tile_sort<T, MULT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  if (n) k_tile_sort<T, MULT><<<n, kTileThreads, smem, s>>>(keys, counts, tiles, ids, out, fallbacks);
+  if (n) k_tile_sort<T, MULT><<<n, kTileThreads, smem, s>>>(keys, counts, tiles, ids, out, fallbacks, rg);
 }
 
 template <class T>
 void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
-                      unsigned long long* fallbacks, cudaStream_t s) {
-  tile_sort_with<T, 1>(keys, counts, tiles, nullptr, ntiles, out, fallbacks, s);
+                      unsigned long long* fallbacks, TileRanges<T> rg, cudaStream_t s) {
+  tile_sort_with<T, 1>(keys, counts, tiles, nullptr, ntiles, out, fallbacks, rg, s);
 }
 template <class T>
 void launch_tile_sort_large(T* keys, uint32_t* counts, const TileDesc* tiles, const uint32_t* ids, uint32_t nids,
-                            TileOut<T>* out, unsigned long long* fallbacks, cudaStream_t s) {
-  tile_sort_with<T, 2>(keys, counts, tiles, ids, nids, out, fallbacks, s);
+                            TileOut<T>* out, unsigned long long* fallbacks, TileRanges<T> rg, cudaStream_t s) {
+  tile_sort_with<T, 2>(keys, counts, tiles, ids, nids, out, fallbacks, rg, s);
 }
 template void launch_tile_sort<uint64_t>(uint64_t*, uint32_t*, const TileDesc*, uint32_t, TileOut<uint64_t>*,
-                                         unsigned long long*, cudaStream_t);
+                                         unsigned long long*, TileRanges<uint64_t>, cudaStream_t);
 template void launch_tile_sort<u128>(u128*, uint32_t*, const TileDesc*, uint32_t, TileOut<u128>*, unsigned long long*,
-                                     cudaStream_t);
+                                     TileRanges<u128>, cudaStream_t);
 template void launch_tile_sort_large<uint64_t>(uint64_t*, uint32_t*, const TileDesc*, const uint32_t*, uint32_t,
-                                               TileOut<uint64_t>*, unsigned long long*, cudaStream_t);
+                                               TileOut<uint64_t>*, unsigned long long*, TileRanges<uint64_t>,
+                                               cudaStream_t);
 template void launch_tile_sort_large<u128>(u128*, uint32_t*, const TileDesc*, const uint32_t*, uint32_t,
-                                           TileOut<u128>*, unsigned long long*, cudaStream_t);
+                                           TileOut<u128>*, unsigned long long*, TileRanges<u128>, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Oversized tiles: one CTA, LSD passes through global memory.  Each pass
