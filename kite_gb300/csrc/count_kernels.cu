@@ -147,7 +147,7 @@ __device__ __forceinline__ void reserve_ranges(const ExtractParams<T>& p, unsign
   }
 }
 
-size_t extract64_smem_bytes(uint32_t partitions, bool scatter);
+__host__ __device__ size_t extract64_smem_bytes(uint32_t partitions, bool scatter);
 
 // A word's forward and reverse-complement code streams, shared with the warp.
 struct CodeWords {
@@ -191,11 +191,13 @@ __device__ __forceinline__ Word32 encode_word(const uint4 a, const uint4 b) {
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const uint32_t v = x[q];
-    const uint32_t u = v & 0xDFDFDFDFu;  // fold lower case
-    const uint32_t valid = __vcmpeq4(u, 0x41414141u) | __vcmpeq4(u, 0x43434343u) | __vcmpeq4(u, 0x47474747u) |
-                           __vcmpeq4(u, 0x54545454u);
     // A/a=0 C/c=1 G/g=2 T/t=3 from ASCII bits 1 and 2
     const uint32_t c4 = ((v >> 1) ^ (v >> 2)) & 0x03030303u;
+    // a byte is a base when, case folded, it is the letter its code stands
+    // for: a byte permute of "ACGT" with the codes as selectors
+    const uint32_t x = c4 | (c4 >> 4);
+    const uint32_t y = x & 0x00FF00FFu;
+    const uint32_t valid = __vcmpeq4(v & 0xDFDFDFDFu, __byte_perm(0x54474341u, 0u, (y | (y >> 8)) & 0xFFFFu));
     const uint32_t p8 = (c4 * 0x40100401u) >> 24;  // byte 0's code in bits 7..6
     w.code |= (uint64_t)p8 << (56 - 8 * q);
     w.nl |= byte_bits(__vcmpeq4(v, 0x0a0a0a0au)) << (4 * q);
@@ -265,12 +267,18 @@ __device__ __forceinline__ void load_word(const uint8_t* arena, uint64_t pos, ui
   in_range = pos >= end ? 0u : (end - pos >= 32 ? 0xFFFFFFFFu : (uint32_t)((1ull << (end - pos)) - 1));
 }
 
-size_t extract64_smem_bytes(uint32_t partitions, bool scatter) {
-  return (scatter ? (size_t)partitions * 8 : 0) + (size_t)partitions * 4 + 96 * 4;
+// Extraction shared memory: [scatter bases P x 8] | histogram P x 4 | scan
+// area 96 x 4 | (16-aligned) every warp's last word (8 x Word32) | (u64
+// histogram pass) the threads' encoded words.
+__host__ __device__ static size_t extract_xw_offset(uint32_t partitions, bool scatter) {
+  return ((scatter ? (size_t)partitions * 8 : 0) + (size_t)partitions * 4 + 96 * 4 + 15) & ~(size_t)15;
+}
+__host__ __device__ size_t extract64_smem_bytes(uint32_t partitions, bool scatter) {
+  return extract_xw_offset(partitions, scatter) + (size_t)(kExtractThreads / 32) * sizeof(Word32);
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uint64_t> p) {
+__global__ void __launch_bounds__(kExtractThreads, 6) k_extract64(ExtractParams<uint64_t> p) {
   constexpr int NT = kExtractThreads;
   extern __shared__ __align__(16) uint8_t sm[];
   const uint32_t P = p.partitions;
@@ -290,21 +298,37 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
   const uint32_t shift = p.shift;
 
   Word32 wp, w0, w1;
-  uint32_t r0, r1, rp;
-  // ts - chunk_start is a multiple of 64: the word before is wholly inside
-  // the chunk, or the thread starts the chunk
-  const bool has_prev = ts > d.chunk_start && ts < e;
-  load_word(p.arena, has_prev ? ts - 32 : ts, has_prev ? ts : ts, wp, rp);
-  if (!has_prev) {
-    wp.nl = 0;
-    wp.vb = 0;
-  }
+  uint32_t r0, r1;
   load_word(p.arena, ts, e, w0, r0);
   load_word(p.arena, ts + 32, e, w1, r1);
   w0.nl &= r0;
   w1.nl &= r1;
+  // The word before ts is lane - 1's second word, the previous warp's last
+  // one for lane 0; only the block's first thread encodes it itself.  (ts -
+  // chunk_start is a multiple of 64: the word before is wholly inside the
+  // chunk, or the thread starts the chunk.)
+  const unsigned xlane = threadIdx.x & 31, xwid = threadIdx.x >> 5;
+  Word32* xw = reinterpret_cast<Word32*>(sm + extract_xw_offset(P, MODE == 1));
+  if (xlane == 31) xw[xwid] = w1;
+  wp.code = __shfl_up_sync(0xffffffffu, w1.code, 1);
+  wp.rcode = __shfl_up_sync(0xffffffffu, w1.rcode, 1);
+  wp.nl = __shfl_up_sync(0xffffffffu, w1.nl, 1);
+  wp.vb = __shfl_up_sync(0xffffffffu, w1.vb, 1);
   unsigned nl_total;
   const unsigned nl_before = block_exclusive_scan<NT, unsigned>(__popc(w0.nl) + __popc(w1.nl), scan_sm, &nl_total);
+  const bool has_prev = ts > d.chunk_start && ts < e;
+  if (xlane == 0) {
+    if (xwid > 0) {
+      wp = xw[xwid - 1];
+    } else if (has_prev) {
+      uint32_t rp;
+      load_word(p.arena, ts - 32, ts, wp, rp);
+    }
+  }
+  if (!has_prev) {
+    wp.nl = 0;
+    wp.vb = 0;
+  }
   const unsigned long long line0 = p.block_nl_excl[bi] - p.block_nl_excl[d.first_block];
   unsigned ph = (unsigned)((line0 + nl_before) & 3ull);  // line phase at ts
   unsigned php = (ph - (unsigned)__popc(wp.nl)) & 3u;     // at ts - 32
@@ -341,7 +365,7 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
     // lanes share every sequence word's k-mers (a thread's own bytes may be
     // a quality line) and a word's keys go out as one coalesced run.
     const unsigned lane = threadIdx.x & 31;
-    CodeWords* ws = reinterpret_cast<CodeWords*>(sm + ((((size_t)P * 4 + 96 * 4) + 15) & ~(size_t)15)) +
+    CodeWords* ws = reinterpret_cast<CodeWords*>(sm + ((extract64_smem_bytes(P, false) + 15) & ~(size_t)15)) +
                     (size_t)(threadIdx.x & ~31u) * 3;
     ws[3 * lane] = CodeWords{wp.code, wp.rcode};
     ws[3 * lane + 1] = CodeWords{w0.code, w0.rcode};
@@ -363,11 +387,13 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
       for (int h = 0; h < 2; ++h) {
         const unsigned V = lv[h];
         if (V == 0u) continue;
-        if ((V >> lane) & 1u) {
+        const bool act = (V >> lane) & 1u;
+        uint64_t key = 0;
+        if (act) {
           const CodeWords pw = ws[3 * l + h], cw = ws[3 * l + h + 1];
           const uint32_t sft = 2 * (31 - lane);
           const uint64_t fwd = (sft ? ((cw.code >> sft) | (pw.code << (64 - sft))) : cw.code) & mask;
-          uint64_t key = fwd;
+          key = fwd;
           if (canon) {
             const uint32_t t = 2 * (33 + lane - k);  // 4 .. 126
             const uint64_t rc =
@@ -376,12 +402,19 @@ __global__ void __launch_bounds__(kExtractThreads) k_extract64(ExtractParams<uin
           }
           atomicAdd(&hist[bucket_of(key, shift)], 1u);
           if (wbase) wbase[run + __popc(V & lt)] = key;
-          if (sampling) {
-            const uint64_t pos = wts + (uint64_t)l * 64 + 32 * h + lane;
-            if ((mix64(pos) & p.sample_mask) == 0) {
-              const unsigned idx = atomicAdd(p.sample_count, 1u);
-              if (idx < p.sample_cap) p.sample[idx] = key;
-            }
+        }
+        if (sampling) {
+          // the k-mers whose end position hashes into the sample: one
+          // reservation per word
+          const uint64_t pos = wts + (uint64_t)l * 64 + 32 * h + lane;
+          const bool take = act && (mix64(pos) & p.sample_mask) == 0;
+          const unsigned tb = __ballot_sync(0xffffffffu, take);
+          if (tb) {
+            const int ld = __ffs(tb) - 1;
+            unsigned at = 0;
+            if ((int)lane == ld) at = atomicAdd(p.sample_count, (unsigned)__popc(tb));
+            at = __shfl_sync(0xffffffffu, at, ld) + __popc(tb & lt);
+            if (take && at < p.sample_cap) p.sample[at] = key;
           }
         }
         run += __popc(V);

@@ -271,7 +271,7 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   const uint8_t* base = arena_base(ctx);
 
   // ---- K1 newline count + K2 histogram pass -------------------------------
-  const uint32_t sample_cap = 1u << 20;
+  const uint32_t sample_cap = 1u << 22;
   KCU(ctx->bucket_count.ensure((size_t)PT * 8));
   KCU(ctx->totals.ensure(NS * sizeof(CountTotals)));
   KCU(ctx->sample.ensure((size_t)sample_cap * sizeof(T)));
@@ -279,7 +279,7 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   KCU(cudaMemsetAsync(ctx->bucket_count.p, 0, (size_t)PT * 8, s));
   KCU(cudaMemsetAsync(ctx->totals.p, 0, NS * sizeof(CountTotals), s));
   KCU(cudaMemsetAsync(ctx->sample_count.p, 0, 8, s));
-  // keep ~2^20 of the first chunk's k-mer positions (about one k-mer per 2.5 bytes)
+  // keep ~2^22 of the first chunk's k-mer positions (about one k-mer per 2.5 bytes)
   uint64_t est = std::max<uint64_t>(chunk0_len * 2 / 5, 1);
   uint32_t mask = 0;
   while ((est >> log2u((uint64_t)mask + 1)) > sample_cap && mask < (1u << 30)) mask = mask * 2 + 1;

@@ -31,6 +31,7 @@ namespace kite {
 
 static constexpr int kIn = 48, kH = 64;
 static constexpr int kBinBits = 16, kSubBits = 32;
+static constexpr uint32_t kTrainRows = 1u << 20;  // training rows taken from the sorted key sample
 static constexpr int kParams = kIn * kH + kH + kH * kH + kH + kH + 1;
 
 // parameter offsets
@@ -52,7 +53,8 @@ struct MlpModel {
   unsigned* tile_hits = nullptr;
   uint32_t tile_cap = 0;
   uint32_t* batch_idx = nullptr;
-  unsigned* hist = nullptr;  // [65536] sample histogram, then inclusive cumulative
+  unsigned* hist = nullptr;   // [65536] sample histogram, then inclusive cumulative
+  unsigned* hist2 = nullptr;  // [65536] the same over the sorted training subset
   float last_loss = 0;
   double last_pred_imbalance = 0;
   bool trained = false;
@@ -75,6 +77,7 @@ void mlp_destroy(MlpModel* m) {
   cudaFree(m->tile_hits);
   cudaFree(m->batch_idx);
   cudaFree(m->hist);
+  cudaFree(m->hist2);
   delete m;
 }
 
@@ -103,21 +106,24 @@ __global__ void __launch_bounds__(1024) k_cum(unsigned* __restrict__ h) {
   }
 }
 
+// Training rows from every `stride`-th key of the sorted sample of n keys:
+// row j describes key i = j * stride (its rank among the n keys).
 template <class T>
-__global__ void k_make_features(const T* __restrict__ sorted, uint32_t n, uint32_t key_bits,
-                                const unsigned* __restrict__ cum, float* __restrict__ feats,
+__global__ void k_make_features(const T* __restrict__ sorted, uint32_t n, uint32_t rows, uint32_t stride,
+                                uint32_t key_bits, const unsigned* __restrict__ cum, float* __restrict__ feats,
                                 float* __restrict__ target, float* __restrict__ scale) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= rows) return;
+  const uint32_t i = j * stride;
   const uint64_t v = view48(sorted[i], key_bits);
   const uint32_t b = (uint32_t)(v >> kSubBits);
   const unsigned hi = cum[b], lo = b ? cum[b - 1] : 0u;
   const float m = (float)(hi - lo);
-  float* f = feats + (size_t)i * kIn;
+  float* f = feats + (size_t)j * kIn;
 #pragma unroll
   for (int q = 0; q < kIn; ++q) f[q] = (float)((v >> (kIn - 1 - q)) & 1ull);
-  target[i] = ((float)(i - lo) + 0.5f) / m;
-  scale[i] = m / (float)n;
+  target[j] = ((float)(i - lo) + 0.5f) / m;
+  scale[j] = m / (float)n;
 }
 
 // ---- forward + backward ------------------------------------------------------
@@ -398,22 +404,11 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
   *rep = MlpReport{};
   rep->pred_imbalance = 1e30;
   if (!m || n < 4 * S || n < 1024) return 0;  // too few samples to learn from
-  T* sorted = nullptr;
-  const int sl = sort_sample<T>(m, d_sample, n, s, &sorted);
-  if (sl < 0) return 1;
-  rep->launches += sl;
-  if (m->cap < n) {
-    cudaFree(m->feats);
-    cudaFree(m->target);
-    cudaFree(m->scale);
-    if (cudaMalloc(&m->feats, (size_t)n * kIn * sizeof(float)) != cudaSuccess) return 1;
-    if (cudaMalloc(&m->target, (size_t)n * sizeof(float)) != cudaSuccess) return 1;
-    if (cudaMalloc(&m->scale, (size_t)n * sizeof(float)) != cudaSuccess) return 1;
-    m->cap = n;
-  }
   if (!m->hist && cudaMalloc(&m->hist, sizeof(unsigned) << kBinBits) != cudaSuccess) return 1;
+  if (!m->hist2 && cudaMalloc(&m->hist2, sizeof(unsigned) << kBinBits) != cudaSuccess) return 1;
+  // cumulative bin histogram of the whole sample (its order does not matter)
   cudaMemsetAsync(m->hist, 0, sizeof(unsigned) << kBinBits, s);
-  k_bin_hist<T><<<(n + 255) / 256, 256, 0, s>>>(sorted, n, key_bits, m->hist);
+  k_bin_hist<T><<<(n + 255) / 256, 256, 0, s>>>(d_sample, n, key_bits, m->hist);
   k_cum<<<1, 1024, 0, s>>>(m->hist);
   rep->launches += 2;
   const size_t smem = kParams * sizeof(float);
@@ -424,7 +419,7 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
     k_sort_splitters<T><<<1, 1024, 0, s>>>(d_spl, S - 1);
     rep->launches += 3;
     double pred = 0;
-    if (predict_imbalance<T>(m, sorted, n, d_spl, S, s, timeout_ms, &pred)) return 1;
+    if (predict_imbalance<T>(m, d_sample, n, d_spl, S, s, timeout_ms, &pred)) return 1;
     if (pred <= m->last_pred_imbalance * 1.05) {
       rep->pred_imbalance = pred;
       rep->loss = m->last_loss;
@@ -432,17 +427,37 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
       return cudaGetLastError() == cudaSuccess ? 0 : 1;
     }
   }
-  k_make_features<T><<<(n + 255) / 256, 256, 0, s>>>(sorted, n, key_bits, m->hist, m->feats, m->target, m->scale);
-  rep->launches += 1;
+  // training rows: the within-bin ranks of a sorted subset of at most
+  // kTrainRows keys (the sample fills in no particular order)
+  const uint32_t rows = n < kTrainRows ? n : kTrainRows;
+  T* sorted = nullptr;
+  const int sl = sort_sample<T>(m, d_sample, rows, s, &sorted);
+  if (sl < 0) return 1;
+  rep->launches += sl;
+  if (m->cap < rows) {
+    cudaFree(m->feats);
+    cudaFree(m->target);
+    cudaFree(m->scale);
+    if (cudaMalloc(&m->feats, (size_t)rows * kIn * sizeof(float)) != cudaSuccess) return 1;
+    if (cudaMalloc(&m->target, (size_t)rows * sizeof(float)) != cudaSuccess) return 1;
+    if (cudaMalloc(&m->scale, (size_t)rows * sizeof(float)) != cudaSuccess) return 1;
+    m->cap = rows;
+  }
+  cudaMemsetAsync(m->hist2, 0, sizeof(unsigned) << kBinBits, s);
+  k_bin_hist<T><<<(rows + 255) / 256, 256, 0, s>>>(sorted, rows, key_bits, m->hist2);
+  k_cum<<<1, 1024, 0, s>>>(m->hist2);
+  k_make_features<T><<<(rows + 255) / 256, 256, 0, s>>>(sorted, rows, rows, 1, key_bits, m->hist2, m->feats,
+                                                         m->target, m->scale);
+  rep->launches += 3;
   int steps = 400;
   if (const char* e = getenv("KITE_MLP_STEPS")) steps = std::max(1, atoi(e));
   int tl = 0;
-  if (mlp_train(m, n, steps, 8192, 2e-3f, s, timeout_ms, &rep->loss, &tl)) return 1;
+  if (mlp_train(m, rows, steps, 8192, 2e-3f, s, timeout_ms, &rep->loss, &tl)) return 1;
   rep->launches += tl;
   k_invert<T><<<(S + 127) / 128, 128, smem, s>>>(m->params, m->hist, n, S, key_bits, d_spl);
   k_sort_splitters<T><<<1, 1024, 0, s>>>(d_spl, S - 1);
   rep->launches += 2;
-  if (predict_imbalance<T>(m, sorted, n, d_spl, S, s, timeout_ms, &rep->pred_imbalance)) return 1;
+  if (predict_imbalance<T>(m, d_sample, n, d_spl, S, s, timeout_ms, &rep->pred_imbalance)) return 1;
   rep->launches += 1;
   m->last_loss = rep->loss;
   m->last_pred_imbalance = rep->pred_imbalance;
