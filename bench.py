@@ -462,7 +462,8 @@ def main():
     ap.add_argument("--merge-scale", type=float, default=1.0, help="read-count scale of the merge databases")
     ap.add_argument("--scatter-shape", type=int, default=0, choices=[0, 1, 2, 3],
                     help="key-range split scatter launch shape (0 = by digit count)")
-    ap.add_argument("--tile-fill", type=float, default=1.0, help="target mean tile load / on-chip capacity")
+    ap.add_argument("--tile-fill", type=float, default=0.0,
+                    help="target tile load / on-chip capacity (0 = the library default)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

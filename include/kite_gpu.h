@@ -70,7 +70,7 @@ typedef struct {
   uint32_t timeout_ms;       /* bound on every host-side wait (0 = 600000) */
   void* stream;              /* optional cudaStream_t to run on (NULL = own stream) */
   uint32_t samples;          /* batched count: samples per segment (0 = 1); see kite_gpu_count_submit_sample */
-  double tile_fill;          /* mean tile load as a fraction of on-chip capacity (0 = 1.0) */
+  double tile_fill;          /* target tile load as a fraction of on-chip capacity (0 = 0.85) */
   int scatter_shape;         /* key-range split scatter launch shape 0..3 (0 = 256 threads x 8 keys) */
 } kite_gpu_cfg;
 

@@ -1,10 +1,11 @@
 """Autotuner for the count's launch shapes.
 
 Two knobs decide how the key-range sort is cut and launched:
-  tile_fill      mean tile load as a fraction of the on-chip tile capacity
+  tile_fill      target tile load as a fraction of the on-chip tile capacity
                  (tile shape: more, smaller tiles vs fewer, fuller ones);
   scatter_shape  launch shape of the key-range split scatter, threads x keys
-                 per thread: 0 = 256x8, 1 = 256x16, 2 = 512x8, 3 = 512x16.
+                 per thread: 0 = 256x8 up to 256 digits and 512x8 above,
+                 1 = 256x16, 2 = 512x8, 3 = 512x16.
 `tune` times a caller-supplied count of the real workload for every pair and
 keeps the fastest; `record` writes the choice and the whole table as JSON so a
 run can be reproduced with the same shapes.
@@ -14,9 +15,9 @@ from __future__ import annotations
 import json
 import time
 
-FILLS = (0.5, 0.75, 1.0)
+FILLS = (0.7, 0.85, 1.0)
 SHAPES = (0, 1, 2, 3)
-SHAPE_NAMES = {0: "256x8", 1: "256x16", 2: "512x8", 3: "512x16"}
+SHAPE_NAMES = {0: "by digits", 1: "256x16", 2: "512x8", 3: "512x16"}
 
 
 def tune(run_once, fills=FILLS, shapes=SHAPES, reps: int = 2) -> tuple[dict, list]:

@@ -17,6 +17,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <cmath>
 #include <vector>
 
 #include "kite_gpu.h"
@@ -453,10 +454,21 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   KCU(cudaEventRecord(ctx->ev[3], s));
 
   // ---- K3b tile split -----------------------------------------------------
-  // target mean tile load as a fraction of on-chip capacity (cfg.tile_fill)
+  // Tiles per bucket: the largest bucket's keys over the target tile load
+  // (cfg.tile_fill of the on-chip capacity), rounded up to a multiple of 32
+  // for one split level (up to 1024 tiles); beyond that a power of two, so
+  // that the two levels divide it evenly.
   const double fill = std::min(4.0, std::max(0.05, ctx->cfg.tile_fill));
   uint32_t S = 1;
-  while ((double)maxb / S > fill * CAP && S < 4096) S <<= 1;
+  if ((double)maxb > fill * CAP) {
+    const double want = std::ceil((double)maxb / (fill * CAP));
+    if (want <= 1024.0) {
+      S = std::min<uint32_t>(1024, ((uint32_t)want + 31) & ~31u);
+    } else {
+      S = 2048;
+      while ((double)S < want && S < 4096) S <<= 1;
+    }
+  }
   st.tiles_per_bucket = S;
   T* sorted = ctx->keys_a.as<T>();
   T* scratch = ctx->keys_b.as<T>();
@@ -885,7 +897,7 @@ int kite_gpu_open(const kite_gpu_cfg* cfg, kite_gpu_ctx** out) {
     delete ctx;
     return KITE_ERR_BAD_INPUT;
   }
-  if (ctx->cfg.tile_fill <= 0) ctx->cfg.tile_fill = 1.0;
+  if (ctx->cfg.tile_fill <= 0) ctx->cfg.tile_fill = 0.85;
   if (cfg->stream) {
     ctx->stream = (cudaStream_t)cfg->stream;
   } else {

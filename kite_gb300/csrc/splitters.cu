@@ -40,12 +40,12 @@ __global__ void __launch_bounds__(1024) k_hist_splitters(unsigned* __restrict__ 
   __syncthreads();
   const unsigned long long total = carry;
   const uint32_t sh = key_bits - hbits;
-  const int sbits = 31 - __clz((int)S);
   for (uint32_t j = threadIdx.x + 1; j < S; j += blockDim.x) {
     T s;
     if (total == 0) {
-      // no sample: uniform cut of [0, 2^key_bits)
-      s = key_bits >= (uint32_t)sbits ? ((T)j << (key_bits - sbits)) : (T)(j >> (sbits - key_bits));
+      // no sample: uniform cut of [0, 2^key_bits): j/S as a 32-bit fraction, scaled
+      const unsigned long long f = ((unsigned long long)j << 32) / S;
+      s = key_bits >= 32 ? ((T)f << (key_bits - 32)) : (T)(f >> (32 - key_bits));
     } else {
       const unsigned long long target = (total * (unsigned long long)j + S - 1) / S;
       uint32_t lo = 0, hi = nb - 1;
