@@ -72,10 +72,9 @@ struct TileSmem {
 
 // Stable LSD passes over bits [lo_bit, nbits) of the n keys in buf (shared
 // memory), 8-bit digits.
-template <class T, int ITEMS = tile_items<T>()>
+template <class T, int NT, int ITEMS>
 __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, unsigned* warp_hist,
                                                 unsigned* scan_sm, int lo_bit = 0) {
-  constexpr int NT = kTileThreads;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   // spread the n keys over every warp: `items` rounds of 32 per warp
   const int items = (int)((n + NT - 1) / NT);
@@ -133,11 +132,12 @@ constexpr unsigned kMaxDistinct = 32;  // distinct keys a warp extracts from one
 constexpr int kLoadBatch = 8;          // global loads a thread keeps in flight
 
 // MULT = 1: the regular tile (8192 u64 / 4096 u128 keys, two CTAs per SM);
-// MULT = 2: twice that for the few oversized tiles (one CTA per SM).
+// MULT = 2: twice that, with twice the threads, for the oversized tiles (one
+// CTA per SM).
 template <class T, int MULT>
 struct BinSmem {
-  static constexpr int NT = kTileThreads;
-  static constexpr int ITEMS = tile_items<T>() * MULT;
+  static constexpr int NT = kTileThreads * MULT;
+  static constexpr int ITEMS = tile_items<T>();
   static constexpr int CAP = NT * ITEMS;
   static constexpr int NW = NT / 32;
   static constexpr size_t buf_bytes = (size_t)CAP * sizeof(T);
@@ -284,7 +284,7 @@ __device__ __forceinline__ bool warp_distinct_sort(T* buf, unsigned a, unsigned 
 }
 
 template <class T, int MULT>
-__global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
+__global__ void __launch_bounds__(kTileThreads * MULT, MULT == 1 ? 2 : 1)
     k_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, const TileDesc* __restrict__ tiles,
                 const uint32_t* __restrict__ ids, TileOut<T>* __restrict__ tout, unsigned long long* fallbacks,
                 TileRanges<T> rg) {
@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(kTileThreads, MULT == 1 ? 2 : 1)
   if (misc[0]) {
     // a large bin of many distinct keys: full LSD over the varying bits, in place
     if (threadIdx.x == 0 && fallbacks) atomicAdd(fallbacks, 1ull);
-    smem_radix_sort<T, ITEMS>(buf, n, varying_bits(mn, mx), bins, scan_sm, 0);
+    smem_radix_sort<T, NT, ITEMS>(buf, n, varying_bits(mn, mx), bins, scan_sm, 0);
   }
 
   // ---- 5. run-length reduction over the sorted keys ----
@@ -508,7 +508,7 @@ static void tile_sort_with(T* keys, uint32_t* counts, const TileDesc* tiles, con
   const size_t smem = BinSmem<T, MULT>::total;
   cudaFuncSetAttribute(k_tile_sort<T, MULT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(k_tile_sort<T, MULT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  if (n) k_tile_sort<T, MULT><<<n, kTileThreads, smem, s>>>(keys, counts, tiles, ids, out, fallbacks, rg);
+  if (n) k_tile_sort<T, MULT><<<n, BinSmem<T, MULT>::NT, smem, s>>>(keys, counts, tiles, ids, out, fallbacks, rg);
 }
 
 template <class T>
