@@ -145,14 +145,20 @@ __device__ __forceinline__ int put_varint(uint8_t* o, T v) {
   }
 }
 
-// One CTA per tile: per-row sizes, block scan, byte writes.
+// One CTA per tile, 256 rows at a time: per-row sizes, block scan, the rows'
+// bytes assembled in shared memory, then written out with consecutive
+// threads on consecutive bytes (whole sectors, not one scattered byte store
+// per row byte).
 template <class T>
 __global__ void __launch_bounds__(256) k_encode(const T* __restrict__ keys, const uint32_t* __restrict__ counts,
                                                 const TileDesc* __restrict__ tiles, const TileOut<T>* __restrict__ tout,
                                                 const unsigned long long* __restrict__ tile_boff,
                                                 const T* __restrict__ tile_prev, const BucketMeta* __restrict__ meta,
                                                 uint8_t* __restrict__ out, unsigned long long out_cap, DevStatus* st) {
+  // largest row: LEB128 of a key delta plus LEB128 of a u32 count, or the raw first row
+  constexpr int kRowMax = (KeyTraits<T>::kBits + 6) / 7 + 5;
   __shared__ unsigned long long sm[34];
+  __shared__ uint8_t chunk[256 * kRowMax];
   const uint32_t t = blockIdx.x;
   const TileOut<T> o = tout[t];
   if (o.rows == 0) return;
@@ -180,21 +186,25 @@ __global__ void __launch_bounds__(256) k_encode(const T* __restrict__ keys, cons
       }
     }
     unsigned long long tot;
-    const unsigned long long ex = block_exclusive_scan<256, unsigned long long>((unsigned long long)sz, sm, &tot);
-    const unsigned long long at = base + run + ex;
+    const unsigned ex = (unsigned)block_exclusive_scan<256, unsigned long long>((unsigned long long)sz, sm, &tot);
     if (r < o.rows) {
-      if (at + (unsigned long long)sz > out_cap) {
-        dev_fail(st, KITE_DEV_ENCODE_OVERFLOW, t, r, 0);
-      } else if (r == 0 && first_in_bucket) {
-        uint8_t* p = out + at;
-        for (int i = 0; i < (int)sizeof(T); ++i) p[i] = (uint8_t)(key >> (8 * i));
-        for (int i = 0; i < 4; ++i) p[sizeof(T) + i] = (uint8_t)(cnt >> (8 * i));
+      uint8_t* q = chunk + ex;
+      if (r == 0 && first_in_bucket) {
+        for (int i = 0; i < (int)sizeof(T); ++i) q[i] = (uint8_t)(key >> (8 * i));
+        for (int i = 0; i < 4; ++i) q[sizeof(T) + i] = (uint8_t)(cnt >> (8 * i));
       } else {
-        uint8_t* p = out + at;
-        const int n1 = put_varint<T>(p, delta);
-        put_varint<uint64_t>(p + n1, (uint64_t)cnt);
+        const int n1 = put_varint<T>(q, delta);
+        put_varint<uint64_t>(q + n1, (uint64_t)cnt);
       }
     }
+    __syncthreads();
+    const unsigned long long at = base + run;
+    if (at + tot > out_cap) {
+      if (threadIdx.x == 0) dev_fail(st, KITE_DEV_ENCODE_OVERFLOW, t, r0, 0);
+    } else {
+      for (unsigned i = threadIdx.x; i < (unsigned)tot; i += 256) out[at + i] = chunk[i];
+    }
+    __syncthreads();  // the chunk is refilled next round
     run += tot;
   }
 }
