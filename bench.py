@@ -545,6 +545,11 @@ def main():
     achieved = algo_bytes / (avg_ms[dom] / 1e3) / 1e9
     tr = ncu_traffic(name)
     traffic = None
+    try:
+        traffic_src = json.loads((ROOT / "profiles" / "ncu_count_kernels.json").read_text())["source"] + \
+            ", DRAM bytes per k-mer scaled to this step"
+    except Exception:
+        traffic_src = None
     if tr and tr.get("dram_bytes_per_key") is not None:
         # ncu DRAM bytes per k-mer from the committed 1M-read capture, scaled
         # to this step's k-mers (the split's figure is per level)
@@ -553,7 +558,7 @@ def main():
     sort_bytes = stages[3][1] + stages[4][1]
     roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
-                "traffic_source": "profiles/count_kernels_1M_full.md (ncu, 1M reads) scaled per k-mer",
+                "traffic_source": traffic_src,
                 "algorithmic_bytes": algo_bytes, "kernel_ms": avg_ms[dom],
                 "sort_gbs": sort_bytes / (sort_ms / 1e3) / 1e9 if sort_ms > 0 else None,
                 "sort_frac": (sort_bytes / (sort_ms / 1e3) / 1e9) / peak if sort_ms > 0 else None,
