@@ -85,10 +85,18 @@ __global__ void __launch_bounds__(256) k_col_offsets(unsigned* __restrict__ m, u
   if (c >= cols) return;
   const uint32_t r0 = g * kColRows, r1 = min(rows, r0 + kColRows);
   unsigned acc = (unsigned)gsum[(size_t)g * cols + c];
-  for (uint32_t r = r0; r < r1; ++r) {
-    const unsigned v = m[(size_t)r * cols + c];
-    m[(size_t)r * cols + c] = acc;
-    acc += v;
+  // 16 rows loaded before any is rewritten, so the loads are in flight together
+  constexpr uint32_t kB = 16;
+  for (uint32_t r = r0; r < r1; r += kB) {
+    unsigned v[kB];
+#pragma unroll
+    for (uint32_t j = 0; j < kB; ++j) v[j] = r + j < r1 ? m[(size_t)(r + j) * cols + c] : 0u;
+#pragma unroll
+    for (uint32_t j = 0; j < kB; ++j)
+      if (r + j < r1) {
+        m[(size_t)(r + j) * cols + c] = acc;
+        acc += v[j];
+      }
   }
 }
 
