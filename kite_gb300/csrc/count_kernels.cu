@@ -732,8 +732,14 @@ __global__ void __launch_bounds__(kSplitThreads) k_split_hist(TileSplitParams<T>
       key[u] = i < e ? p.keys_in[i] : T(0);
     }
 #pragma unroll
-    for (int u = 0; u < kSplitUnroll; ++u)
-      if (i0 + (uint64_t)u * kSplitThreads < e) atomicAdd(&hist[digit_of_key(spl, lut, lo, sh, key[u])], 1u);
+    for (int u = 0; u < kSplitUnroll; ++u) {
+      const uint64_t i = i0 + (uint64_t)u * kSplitThreads;
+      if (i < e) {
+        const uint32_t d = digit_of_key(spl, lut, lo, sh, key[u]);
+        atomicAdd(&hist[d], 1u);
+        if (p.dig) p.dig[i] = (uint16_t)d;
+      }
+    }
   }
   __syncthreads();
   for (uint32_t d = threadIdx.x; d < D; d += kSplitThreads) p.tile_count[((size_t)r * D + d) * G + g] = hist[d];
@@ -796,9 +802,10 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
     dstart[d] = 0;
     wr[d] = 0;
   }
-  T lo;
-  uint32_t sh;
-  load_digits(p, r, spl, lut, &lo, &sh);  // ends with a barrier
+  T lo = T(0);
+  uint32_t sh = 0;
+  if (p.dig) __syncthreads();  // the histogram pass left every digit
+  else load_digits(p, r, spl, lut, &lo, &sh);  // ends with a barrier
   uint64_t a, e;
   part_range(p.region_off, p.region_count, r, g, G, &a, &e);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -815,8 +822,13 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
       valid[q] = pos < cn;
       key[q] = valid[q] ? p.keys_in[c0 + pos] : T(0);
     }
+    if (p.dig) {
 #pragma unroll
-    for (int q = 0; q < IT; ++q) dg[q] = valid[q] ? digit_of_key(spl, lut, lo, sh, key[q]) : 0u;
+      for (int q = 0; q < IT; ++q) dg[q] = valid[q] ? (unsigned)p.dig[c0 + pos0 + q * 32u] : 0u;
+    } else {
+#pragma unroll
+      for (int q = 0; q < IT; ++q) dg[q] = valid[q] ? digit_of_key(spl, lut, lo, sh, key[q]) : 0u;
+    }
 #pragma unroll
     for (int q = 0; q < IT; ++q) rank[q] = valid[q] ? atomicAdd(&whist[dg[q]], 1u) : 0u;
     __syncthreads();

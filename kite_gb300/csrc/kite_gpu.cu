@@ -114,7 +114,7 @@ struct kite_gpu_ctx {
   DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, splitters2, hist16;
   DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
   DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats, blk_mat, blk_gsum, blk_keys, stage_ctr;
-  DevBuf col_total, sample_first, spans;
+  DevBuf col_total, sample_first, spans, digits;
   HostBuf h_blocks, h_small, h_tiles, h_out, h_meta;
   std::vector<cudaEvent_t> ev;   // stage events
   std::vector<cudaEvent_t> gev;  // sort / encode / copy-out events, 8 per bucket group
@@ -604,6 +604,9 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     tp.G = G;
     tp.tile_count = ctx->tile_count.as<unsigned long long>();
     tp.tile_off = ctx->tile_off.as<unsigned long long>();
+    // the last level's digits: computed once by the histogram, read by the scatter
+    KCU(ctx->digits.ensure(N * 2));
+    tp.dig = ctx->digits.as<uint16_t>();
     launch_split_hist<T>(tp, s);
     st.kernel_launches += 3 + exclusive_scan_u64(tp.tile_count, ctx->tile_off.as<unsigned long long>(), ntg,
                                                  ctx->scan_tmp.as<unsigned long long>(), s);
@@ -939,7 +942,7 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
                     &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out,
                     &ctx->lvl_count, &ctx->lvl_off, &ctx->reg_off, &ctx->reg_cnt, &ctx->sort_stats,
                     &ctx->blk_mat, &ctx->blk_gsum, &ctx->blk_keys, &ctx->stage_ctr,
-                    &ctx->col_total, &ctx->sample_first, &ctx->spans};
+                    &ctx->col_total, &ctx->sample_first, &ctx->spans, &ctx->digits};
   for (DevBuf* b : bufs) b->release();
   ctx->h_blocks.release();
   ctx->h_small.release();

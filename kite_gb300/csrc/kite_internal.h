@@ -108,6 +108,7 @@ struct TileSplitParams {
   uint32_t key_bits;      // 2k: significant key bits
   unsigned long long* tile_count;       // [R*D*G] (digit-major, part-minor)
   const unsigned long long* tile_off;   // exclusive scan of tile_count
+  uint16_t* dig;  // or null; else every key's digit, parallel to keys_in: the histogram writes it, the scatter reads it
 };
 
 // ---- launchers (count_kernels.cu) ----
