@@ -238,33 +238,27 @@ __global__ void k_batch_idx(uint32_t* idx, uint32_t batch, uint32_t n, uint32_t 
   if (b < batch) idx[b] = (uint32_t)(((uint64_t)(start + b) * stride) % n);
 }
 
-__device__ float mlp_eval(const float* __restrict__ P, const float* x) {
-  float h1[kH];
-  for (int j = 0; j < kH; ++j) {
-    float a = P[oB1 + j];
-#pragma unroll
-    for (int i = 0; i < kIn; ++i) a += P[oW1 + j * kIn + i] * x[i];
-    h1[j] = a > 0.f ? a : 0.f;
-  }
-  float y = P[oB3];
-  for (int j = 0; j < kH; ++j) {
-    float a = P[oB2 + j];
-    for (int i = 0; i < kH; ++i) a += P[oW2 + j * kH + i] * h1[i];
-    y += P[oW3 + j] * (a > 0.f ? a : 0.f);
-  }
-  return y;
-}
-
-// One thread per splitter j: bin from the cumulative histogram, then the
+// One warp per splitter j: bin from the cumulative histogram, then the
 // largest 32-bit sub-position whose predicted within-bin fraction stays below
-// the target; the splitter is the first key of the next 48-bit cell.
+// the target; the splitter is the first key of the next 48-bit cell.  Lane l
+// holds hidden units l and l + 32 (weights transposed in shared memory so the
+// lanes read consecutive words); every sum runs over its inputs in index
+// order, one fused multiply-add at a time, so each lane's arithmetic is that of
+// a plain sequential forward pass.
 template <class T>
-__global__ void k_invert(const float* __restrict__ params, const unsigned* __restrict__ cum, uint32_t n, uint32_t S,
-                         uint32_t key_bits, T* __restrict__ spl) {
-  extern __shared__ float P[];
-  for (int i = threadIdx.x; i < kParams; i += blockDim.x) P[i] = params[i];
+__global__ void __launch_bounds__(256) k_invert(const float* __restrict__ params, const unsigned* __restrict__ cum,
+                                                uint32_t n, uint32_t S, uint32_t key_bits, T* __restrict__ spl) {
+  extern __shared__ float P[];  // W1 as [input][hidden], W2 as [input][output]; biases and w3 as given
+  for (int i = threadIdx.x; i < kParams; i += blockDim.x) {
+    float v = params[i];
+    int at = i;
+    if (i < oB1) at = oW1 + (i % kIn) * kH + i / kIn;                        // W1[j][i] -> [i][j]
+    else if (i >= oW2 && i < oB2) at = oW2 + ((i - oW2) % kH) * kH + (i - oW2) / kH;  // W2[j][i] -> [i][j]
+    P[at] = v;
+  }
   __syncthreads();
-  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) / 32 + 1;
   if (j >= S) return;
   const double q = (double)n * j / S;  // sample rank at the cut
   uint32_t lo = 0, hi = (1u << kBinBits) - 1;
@@ -277,14 +271,39 @@ __global__ void k_invert(const float* __restrict__ params, const unsigned* __res
   const double below = b ? cum[b - 1] : 0.0, mass = (double)cum[b] - below;
   const float u = mass > 0 ? (float)((q - below) / mass) : 1.f;
   uint32_t sub = 0;
-  float x[kIn];
   for (int bit = kSubBits - 1; bit >= 0; --bit) {
     const uint32_t cand = sub | (1u << bit);
     const uint64_t v = ((uint64_t)b << kSubBits) | cand;
+    float a0 = P[oB1 + lane], a1 = P[oB1 + lane + 32];
 #pragma unroll
-    for (int i = 0; i < kIn; ++i) x[i] = (float)((v >> (kIn - 1 - i)) & 1ull);
-    if (mlp_eval(P, x) <= u) sub = cand;
+    for (int i = 0; i < kIn; ++i) {
+      const float xi = (float)((v >> (kIn - 1 - i)) & 1ull);
+      a0 += P[oW1 + i * kH + lane] * xi;
+      a1 += P[oW1 + i * kH + lane + 32] * xi;
+    }
+    const float h0 = a0 > 0.f ? a0 : 0.f, h1 = a1 > 0.f ? a1 : 0.f;
+    float c0 = P[oB2 + lane], c1 = P[oB2 + lane + 32];
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
+      const float hv = __shfl_sync(0xffffffffu, h0, i);
+      c0 += P[oW2 + i * kH + lane] * hv;
+      c1 += P[oW2 + i * kH + lane + 32] * hv;
+    }
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
+      const float hv = __shfl_sync(0xffffffffu, h1, i);
+      c0 += P[oW2 + (i + 32) * kH + lane] * hv;
+      c1 += P[oW2 + (i + 32) * kH + lane + 32] * hv;
+    }
+    const float r0 = c0 > 0.f ? c0 : 0.f, r1 = c1 > 0.f ? c1 : 0.f;
+    float y = P[oB3];
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) y += P[oW3 + i] * __shfl_sync(0xffffffffu, r0, i);
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) y += P[oW3 + 32 + i] * __shfl_sync(0xffffffffu, r1, i);
+    if (y <= u) sub = cand;
   }
+  if (lane != 0) return;
   const uint64_t cell = (((uint64_t)b << kSubBits) | sub) + 1;  // first cell above
   T s;
   if (key_bits >= 48) {
@@ -297,29 +316,63 @@ __global__ void k_invert(const float* __restrict__ params, const unsigned* __res
 }
 
 template <class T>
-__global__ void k_tile_hits(const T* __restrict__ sample, uint32_t n, const T* __restrict__ spl, uint32_t S,
-                            unsigned* __restrict__ hits) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  uint32_t j = 0;
-  for (uint32_t step = S >> 1; step; step >>= 1)
-    if (spl[j + step - 1] <= sample[i]) j += step;
-  atomicAdd(&hits[j], 1u);
+__global__ void __launch_bounds__(256) k_tile_hits(const T* __restrict__ sample, uint32_t n,
+                                                   const T* __restrict__ spl, uint32_t S,
+                                                   unsigned* __restrict__ hits) {
+  extern __shared__ __align__(16) uint8_t smraw[];
+  unsigned* h = reinterpret_cast<unsigned*>(smraw);  // S counters of this CTA
+  for (uint32_t t = threadIdx.x; t < S; t += blockDim.x) h[t] = 0;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    // tile = number of the S - 1 splitters <= key (any S)
+    const T x = sample[i];
+    uint32_t lo = 0, hi = S - 1;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (spl[mid] <= x) lo = mid + 1;
+      else hi = mid;
+    }
+    atomicAdd(&h[lo], 1u);
+  }
+  __syncthreads();
+  for (uint32_t t = threadIdx.x; t < S; t += blockDim.x)
+    if (h[t]) atomicAdd(&hits[t], h[t]);
 }
 
-// Sorts the splitters in place (odd-even transposition in one CTA).
+// Sorts the n splitters in place: one CTA, a bitonic network in shared
+// memory over the next power of two (padded with the all-ones key).
 template <class T>
-__global__ void k_sort_splitters(T* spl, uint32_t n) {
-  for (uint32_t round = 0; round < n; ++round) {
-    for (uint32_t i = 2 * threadIdx.x + (round & 1); i + 1 < n; i += 2 * blockDim.x) {
-      const T a = spl[i], b = spl[i + 1];
-      if (b < a) {
-        spl[i] = b;
-        spl[i + 1] = a;
+__global__ void __launch_bounds__(1024) k_sort_splitters(T* spl, uint32_t n) {
+  extern __shared__ __align__(16) uint8_t smraw[];
+  T* v = reinterpret_cast<T*>(smraw);
+  uint32_t np2 = 1;
+  while (np2 < n) np2 <<= 1;
+  for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x) v[i] = i < n ? spl[i] : ~T(0);
+  __syncthreads();
+  for (uint32_t k = 2; k <= np2; k <<= 1)
+    for (uint32_t j = k >> 1; j; j >>= 1) {
+      for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x) {
+        const uint32_t l = i ^ j;
+        if (l > i) {
+          const T a = v[i], b = v[l];
+          if (((i & k) == 0) == (b < a)) {
+            v[i] = b;
+            v[l] = a;
+          }
+        }
       }
+      __syncthreads();
     }
-    __syncthreads();
-  }
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) spl[i] = v[i];
+}
+
+template <class T>
+static size_t splitter_sort_smem(uint32_t n) {
+  uint32_t np2 = 1;
+  while (np2 < n) np2 <<= 1;
+  const size_t bytes = (size_t)np2 * sizeof(T);
+  cudaFuncSetAttribute(k_sort_splitters<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return bytes;
 }
 
 // Bitonic sort of the sample in device memory (padded to a power of two
@@ -381,7 +434,8 @@ int predict_imbalance(MlpModel* m, const T* d_sample, uint32_t n, const T* d_spl
     m->tile_cap = S;
   }
   cudaMemsetAsync(m->tile_hits, 0, (size_t)S * 4, s);
-  k_tile_hits<T><<<(n + 255) / 256, 256, 0, s>>>(d_sample, n, d_spl, S, m->tile_hits);
+  const uint32_t grid = std::min<uint32_t>((n + 255) / 256, 4 * 152);
+  k_tile_hits<T><<<grid, 256, (size_t)S * 4, s>>>(d_sample, n, d_spl, S, m->tile_hits);
   std::vector<unsigned> h(S);
   cudaMemcpyAsync(h.data(), m->tile_hits, (size_t)S * 4, cudaMemcpyDeviceToHost, s);
   if (bounded_sync(s, timeout_ms)) return 1;
@@ -415,8 +469,8 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
   cudaFuncSetAttribute(k_invert<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (m->trained && m->trained_key_bits == key_bits) {
     // the within-bin shape learned on an earlier segment, over this sample's histogram
-    k_invert<T><<<(S + 127) / 128, 128, smem, s>>>(m->params, m->hist, n, S, key_bits, d_spl);
-    k_sort_splitters<T><<<1, 1024, 0, s>>>(d_spl, S - 1);
+    k_invert<T><<<(uint32_t)(((size_t)(S - 1) * 32 + 255) / 256), 256, smem, s>>>(m->params, m->hist, n, S, key_bits, d_spl);
+    k_sort_splitters<T><<<1, 1024, splitter_sort_smem<T>(S - 1), s>>>(d_spl, S - 1);
     rep->launches += 3;
     double pred = 0;
     if (predict_imbalance<T>(m, d_sample, n, d_spl, S, s, timeout_ms, &pred)) return 1;
@@ -454,8 +508,8 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
   int tl = 0;
   if (mlp_train(m, rows, steps, 8192, 2e-3f, s, timeout_ms, &rep->loss, &tl)) return 1;
   rep->launches += tl;
-  k_invert<T><<<(S + 127) / 128, 128, smem, s>>>(m->params, m->hist, n, S, key_bits, d_spl);
-  k_sort_splitters<T><<<1, 1024, 0, s>>>(d_spl, S - 1);
+  k_invert<T><<<(uint32_t)(((size_t)(S - 1) * 32 + 255) / 256), 256, smem, s>>>(m->params, m->hist, n, S, key_bits, d_spl);
+  k_sort_splitters<T><<<1, 1024, splitter_sort_smem<T>(S - 1), s>>>(d_spl, S - 1);
   rep->launches += 2;
   if (predict_imbalance<T>(m, d_sample, n, d_spl, S, s, timeout_ms, &rep->pred_imbalance)) return 1;
   rep->launches += 1;

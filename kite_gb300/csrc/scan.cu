@@ -69,10 +69,18 @@ __global__ void __launch_bounds__(256) k_col_group_scan(unsigned long long* __re
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= cols) return;
   unsigned long long acc = 0;
-  for (uint32_t g = 0; g < groups; ++g) {
-    const unsigned long long v = gsum[(size_t)g * cols + c];
-    gsum[(size_t)g * cols + c] = acc;
-    acc += v;
+  // 16 groups loaded before any is rewritten, so the loads are in flight together
+  constexpr uint32_t kB = 16;
+  for (uint32_t g = 0; g < groups; g += kB) {
+    unsigned long long v[kB];
+#pragma unroll
+    for (uint32_t j = 0; j < kB; ++j) v[j] = g + j < groups ? gsum[(size_t)(g + j) * cols + c] : 0ull;
+#pragma unroll
+    for (uint32_t j = 0; j < kB; ++j)
+      if (g + j < groups) {
+        gsum[(size_t)(g + j) * cols + c] = acc;
+        acc += v[j];
+      }
   }
   total[c] = acc;
 }
