@@ -114,7 +114,7 @@ struct kite_gpu_ctx {
   DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, splitters2, hist16;
   DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
   DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats, blk_mat, blk_gsum, blk_keys, stage_ctr;
-  DevBuf col_total, sample_first, spans, digits;
+  DevBuf col_total, sample_first, spans, digits, tile_lists;
   HostBuf h_blocks, h_small, h_tiles, h_out, h_meta;
   std::vector<cudaEvent_t> ev;   // stage events
   std::vector<cudaEvent_t> gev;  // sort / encode / copy-out events, 8 per bucket group
@@ -473,7 +473,8 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   T* sorted = ctx->keys_a.as<T>();
   T* scratch = ctx->keys_b.as<T>();
   const T* tile_spl = nullptr;  // the splitters that cut every bucket into its S tiles
-  std::vector<TileDesc> ht;
+  std::vector<TileDesc> ht;  // one tile per bucket (S == 1): made on the host
+  uint32_t dev_tiles = 0;    // S > 1: the tiles made on the device
   if (S == 1) {
     for (uint32_t b = 0; b < PT; ++b) ht.push_back(TileDesc{boff[b], (uint32_t)bcount[b], b});
   } else {
@@ -616,18 +617,14 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     launch_make_tiles(ctx->tile_off.as<unsigned long long>(), (uint32_t)nt, S, G, N, ctx->tiles.as<TileDesc>(),
                       ctx->tile_fill.as<uint32_t>(), s);
     KCU(cudaGetLastError());
-    KCU(ctx->h_tiles.ensure(nt * 4 + 64));
-    KCU(cudaMemcpyAsync(ctx->h_tiles.p, ctx->tile_fill.p, nt * 4, cudaMemcpyDeviceToHost, s));
-    rc = wait_stream(ctx, s);
-    if (rc) return rc;
-    const uint32_t* lens = ctx->h_tiles.as<uint32_t>();
-    ht.resize(nt);
-    for (size_t t = 0; t < nt; ++t) ht[t] = TileDesc{0, lens[t], (uint32_t)(t / S)};
+    // the tile lengths stay on the device: the oversized tiles are listed
+    // there and the sort follows without a host round trip
+    dev_tiles = (uint32_t)nt;
     sorted = level_out;
     scratch = level_in;
   }
   KCU(cudaEventRecord(ctx->ev[4], s));
-  const uint32_t ntiles = (uint32_t)ht.size();
+  const uint32_t ntiles = dev_tiles ? dev_tiles : (uint32_t)ht.size();
   const uint32_t Sl = ntiles / PT;  // tiles per bucket
   const T kmax = 2 * k >= (uint32_t)KeyTraits<T>::kBits ? ~T(0) : ((T(1) << (2 * k)) - T(1));
   // Bucket groups: each group's tiles are sorted, linked and encoded in turn,
@@ -635,44 +632,66 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   const uint32_t NG = std::min<uint32_t>(kSortGroups, PT);
   std::vector<uint32_t> gb(NG + 1);  // first bucket of each group
   for (uint32_t g = 0; g <= NG; ++g) gb[g] = (uint32_t)((uint64_t)PT * g / NG);
-  // oversized tiles, group by group: first those sorted on chip at twice the
-  // capacity, then those sorted through global memory
+  // Oversized tiles, group by group: those sorted on chip at twice the
+  // capacity (list A) and those sorted through global memory (list B).  From
+  // device-made tiles the lists are made on the device (group g's entries
+  // from index gb[g] * S, counts lcnt[2g], lcnt[2g+1]) and walked by a fixed
+  // grid; from host tiles on the host, one CTA per listed tile.
   std::vector<uint32_t> big, gbig(NG + 1, 0), glarge(NG, 0);
-  for (uint32_t g = 0; g < NG; ++g) {
-    gbig[g] = (uint32_t)big.size();
-    for (uint32_t t = gb[g] * Sl; t < gb[g + 1] * Sl; ++t)
-      if (ht[t].len > CAP && ht[t].len <= 2 * CAP) big.push_back(t);
-    glarge[g] = (uint32_t)big.size() - gbig[g];
-    for (uint32_t t = gb[g] * Sl; t < gb[g + 1] * Sl; ++t)
-      if (ht[t].len > 2 * CAP) big.push_back(t);
-  }
-  gbig[NG] = (uint32_t)big.size();
-  std::vector<uint64_t> range(S, 0);
-  uint64_t tmax = 0, tsum = 0, tne = 0;
-  for (uint32_t t = 0; t < ntiles; ++t) {
-    range[t % S] += ht[t].len;
-    if (ht[t].len) {
-      tmax = std::max<uint64_t>(tmax, ht[t].len);
-      tsum += ht[t].len;
-      tne++;
+  KCU(ctx->big_ids.ensure((size_t)2 * ntiles * 4 + 8));
+  uint32_t* ids_a = ctx->big_ids.as<uint32_t>();
+  uint32_t* ids_b = ids_a + ntiles;
+  unsigned* lcnt = nullptr;
+  const size_t lhead = (size_t)(2 * NG + 8) * 8;  // counts, then the group bounds
+  const size_t lbytes = lhead + (size_t)(3 + S) * 8;
+  if (dev_tiles) {
+    KCU(ctx->tile_lists.ensure(lbytes + 64));
+    lcnt = ctx->tile_lists.as<unsigned>();
+    // [0] largest tile, [1] keys, [2] non-empty tiles, then the S range sums
+    unsigned long long* lstats = reinterpret_cast<unsigned long long*>(ctx->tile_lists.as<uint8_t>() + lhead);
+    KCU(cudaMemsetAsync(ctx->tile_lists.p, 0, lbytes, s));
+    uint32_t* dgb = reinterpret_cast<uint32_t*>(lcnt + 2 * NG);
+    KCU(ctx->h_tiles.ensure(lbytes + 64));
+    std::memcpy(ctx->h_tiles.p, gb.data(), (NG + 1) * 4);
+    KCU(cudaMemcpyAsync(dgb, ctx->h_tiles.p, (NG + 1) * 4, cudaMemcpyHostToDevice, s));
+    launch_tile_lists(ctx->tile_fill.as<uint32_t>(), ntiles, S, dgb, NG, CAP, ids_a, ids_b, lcnt, lstats, lstats + 3,
+                      s);
+    st.kernel_launches += 1;
+    st.tiles = ntiles;
+  } else {
+    for (uint32_t g = 0; g < NG; ++g) {
+      gbig[g] = (uint32_t)big.size();
+      for (uint32_t t = gb[g] * Sl; t < gb[g + 1] * Sl; ++t)
+        if (ht[t].len > CAP && ht[t].len <= 2 * CAP) big.push_back(t);
+      glarge[g] = (uint32_t)big.size() - gbig[g];
+      for (uint32_t t = gb[g] * Sl; t < gb[g + 1] * Sl; ++t)
+        if (ht[t].len > 2 * CAP) big.push_back(t);
     }
-  }
-  st.tiles = ntiles;
-  st.big_tiles = (uint32_t)big.size();
-  st.tile_imbalance = tne ? (double)tmax / ((double)tsum / (double)tne) : 0.0;
-  st.range_imbalance = (double)*std::max_element(range.begin(), range.end()) / ((double)N / S);
-  KCU(ctx->h_tiles.ensure(std::max(ht.size() * sizeof(TileDesc), ht.size() * 4) + big.size() * 4 + 64));
-  if (S == 1) {
+    gbig[NG] = (uint32_t)big.size();
+    uint64_t tmax = 0, tsum = 0, tne = 0;
+    for (uint32_t t = 0; t < ntiles; ++t)
+      if (ht[t].len) {
+        tmax = std::max<uint64_t>(tmax, ht[t].len);
+        tsum += ht[t].len;
+        tne++;
+      }
+    st.tiles = ntiles;
+    st.big_tiles = (uint32_t)big.size();
+    st.tile_imbalance = tne ? (double)tmax / ((double)tsum / (double)tne) : 0.0;
+    st.range_imbalance = 1.0;  // one tile per bucket
+    KCU(ctx->h_tiles.ensure(ht.size() * sizeof(TileDesc) + big.size() * 4 + 64));
     std::memcpy(ctx->h_tiles.p, ht.data(), ht.size() * sizeof(TileDesc));
     KCU(ctx->tiles.ensure(ht.size() * sizeof(TileDesc)));
     KCU(cudaMemcpyAsync(ctx->tiles.p, ctx->h_tiles.p, ht.size() * sizeof(TileDesc), cudaMemcpyHostToDevice, s));
+    if (!big.empty()) {
+      uint8_t* hb2 = ctx->h_tiles.as<uint8_t>() + ht.size() * sizeof(TileDesc);
+      std::memcpy(hb2, big.data(), big.size() * 4);
+      KCU(cudaMemcpyAsync(ids_a, hb2, big.size() * 4, cudaMemcpyHostToDevice, s));
+    }
   }
-  KCU(ctx->big_ids.ensure(big.size() * 4 + 4));
-  if (!big.empty()) {
-    uint8_t* hb2 = ctx->h_tiles.as<uint8_t>() + std::max(ht.size() * sizeof(TileDesc), ht.size() * 4);
-    std::memcpy(hb2, big.data(), big.size() * 4);
-    KCU(cudaMemcpyAsync(ctx->big_ids.p, hb2, big.size() * 4, cudaMemcpyHostToDevice, s));
-  }
+  int sm_count = 0;
+  cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, ctx->cfg.device);
+  const uint32_t walk_grid = (uint32_t)std::max(1, sm_count);
   KCU(ctx->tile_out.ensure((size_t)ntiles * sizeof(TileOut<T>)));
   KCU(ctx->sort_stats.ensure(8));
   KCU(cudaMemsetAsync(ctx->sort_stats.p, 0, 8, s));
@@ -687,7 +706,8 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   ctx->res_on_host = false;
   ctx->res_meta.assign(PT, BucketMeta{});
   st.kernel_launches += 1 + (uint64_t)NG * 3 + (uint64_t)NG * 3;  // memset, per group: sort, link, offsets, encode
-  for (uint32_t g = 0; g < NG; ++g) st.kernel_launches += (glarge[g] ? 1 : 0) + (gbig[g + 1] - gbig[g] > glarge[g] ? 1 : 0);
+  for (uint32_t g = 0; g < NG; ++g)
+    st.kernel_launches += dev_tiles ? 2 : (glarge[g] ? 1 : 0) + (gbig[g + 1] - gbig[g] > glarge[g] ? 1 : 0);
   cudaEvent_t* gev = ctx->gev.data();  // per group: sort, large, link | encode | copy start/end
   TileOut<T>* tout = ctx->tile_out.as<TileOut<T>>();
   BucketMeta* meta = ctx->meta.as<BucketMeta>();
@@ -700,12 +720,20 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     launch_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>() + t0, nt, tout + t0,
                         ctx->sort_stats.as<unsigned long long>(), TileRanges<T>{tile_spl, Sl, t0, kmax}, s);
     cudaEventRecord(gev[8 * g + 1], s);
-    launch_tile_sort_large<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(),
-                              ctx->big_ids.as<uint32_t>() + gbig[g], glarge[g], tout,
-                              ctx->sort_stats.as<unsigned long long>(), TileRanges<T>{tile_spl, Sl, 0, kmax}, s);
-    launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(),
-                            ctx->big_ids.as<uint32_t>() + gbig[g] + glarge[g], gbig[g + 1] - gbig[g] - glarge[g], tout,
-                            ctx->status.as<DevStatus>(), s);
+    if (dev_tiles) {
+      launch_tile_sort_large<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ids_a + t0, walk_grid,
+                                lcnt + 2 * g, tout, ctx->sort_stats.as<unsigned long long>(),
+                                TileRanges<T>{tile_spl, Sl, 0, kmax}, s);
+      launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(), ids_b + t0,
+                              walk_grid, lcnt + 2 * g + 1, tout, ctx->status.as<DevStatus>(), s);
+    } else {
+      launch_tile_sort_large<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ids_a + gbig[g],
+                                glarge[g], nullptr, tout, ctx->sort_stats.as<unsigned long long>(),
+                                TileRanges<T>{tile_spl, Sl, 0, kmax}, s);
+      launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(),
+                              ids_a + gbig[g] + glarge[g], gbig[g + 1] - gbig[g] - glarge[g], nullptr, tout,
+                              ctx->status.as<DevStatus>(), s);
+    }
     cudaEventRecord(gev[8 * g + 2], s);
     // ---- K5: per-bucket tile links, byte offsets from the group's start
     launch_tile_link<T>(tout + t0, nb, Sl, ctx->tile_boff.as<unsigned long long>() + t0, ctx->tile_prev.as<T>() + t0,
@@ -777,10 +805,22 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   }
   KCU(cudaEventRecord(ctx->ev[7], s));
   KCU(cudaMemcpyAsync(ctx->h_small.p, ctx->sort_stats.p, 8, cudaMemcpyDeviceToHost, s));
+  if (dev_tiles) KCU(cudaMemcpyAsync(ctx->h_tiles.p, ctx->tile_lists.p, lbytes, cudaMemcpyDeviceToHost, s));
   rc = wait_stream(ctx, s);
   if (!rc && to_host) rc = wait_stream(ctx, ctx->copy_stream);
   if (rc) return rc;
   std::memcpy(&st.sort_fallbacks, ctx->h_small.p, 8);
+  if (dev_tiles) {
+    const unsigned* hc = ctx->h_tiles.as<unsigned>();
+    const unsigned long long* hs2 = reinterpret_cast<const unsigned long long*>(ctx->h_tiles.as<uint8_t>() + lhead);
+    uint32_t nbig = 0;
+    for (uint32_t g = 0; g < 2 * NG; ++g) nbig += hc[g];
+    st.big_tiles = nbig;
+    st.tile_imbalance = hs2[2] ? (double)hs2[0] / ((double)hs2[1] / (double)hs2[2]) : 0.0;
+    unsigned long long rmax = 0;
+    for (uint32_t t = 0; t < S; ++t) rmax = std::max(rmax, hs2[3 + t]);
+    st.range_imbalance = (double)rmax / ((double)N / S);
+  }
   rc = check_status(ctx, "count");
   if (rc) return rc;
   for (uint32_t g = 0; g < NG; ++g) {
@@ -942,7 +982,7 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
                     &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out,
                     &ctx->lvl_count, &ctx->lvl_off, &ctx->reg_off, &ctx->reg_cnt, &ctx->sort_stats,
                     &ctx->blk_mat, &ctx->blk_gsum, &ctx->blk_keys, &ctx->stage_ctr,
-                    &ctx->col_total, &ctx->sample_first, &ctx->spans, &ctx->digits};
+                    &ctx->col_total, &ctx->sample_first, &ctx->spans, &ctx->digits, &ctx->tile_lists};
   for (DevBuf* b : bufs) b->release();
   ctx->h_blocks.release();
   ctx->h_small.release();

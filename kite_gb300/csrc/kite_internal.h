@@ -182,15 +182,23 @@ template <class T>
 void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
                       unsigned long long* fallbacks, TileRanges<T> rg, cudaStream_t s);
 // Tiles of tile_capacity < len <= 2 * tile_capacity, listed in ids: the same
-// on-chip sort with twice the shared memory (one CTA per SM).
+// on-chip sort with twice the shared memory (one CTA per SM).  With nids_dev,
+// the list's length is on the device and the nids CTAs walk it in turn.
 template <class T>
 void launch_tile_sort_large(T* keys, uint32_t* counts, const TileDesc* tiles, const uint32_t* ids, uint32_t nids,
-                            TileOut<T>* out, unsigned long long* fallbacks, TileRanges<T> rg, cudaStream_t s);
+                            const unsigned* nids_dev, TileOut<T>* out, unsigned long long* fallbacks,
+                            TileRanges<T> rg, cudaStream_t s);
 // Oversized tiles (more keys than 2 * tile_capacity): one CTA per tile, LSD
-// passes through global memory with `scratch` (>= largest tile keys).
+// passes through global memory with `scratch` (>= largest tile keys); with
+// nbig_dev as above.
 template <class T>
 void launch_big_tile_sort(T* keys, uint32_t* counts, T* scratch, const TileDesc* tiles, const uint32_t* big_ids,
-                          uint32_t nbig, TileOut<T>* out, DevStatus* st, cudaStream_t s);
+                          uint32_t nbig, const unsigned* nbig_dev, TileOut<T>* out, DevStatus* st, cudaStream_t s);
+// Per bucket group, the tiles above capacity (lists and counts on the
+// device) and the tile statistics; see k_tile_lists.
+void launch_tile_lists(const uint32_t* lens, uint32_t ntiles, uint32_t S, const uint32_t* gb, uint32_t NG,
+                       uint32_t cap, uint32_t* ids, uint32_t* ids2, unsigned* cnt, unsigned long long* stats,
+                       unsigned long long* range, cudaStream_t s);
 
 // ---- encode_kernels.cu ----
 struct BucketMeta {

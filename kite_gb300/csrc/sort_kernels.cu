@@ -284,10 +284,9 @@ __device__ __forceinline__ bool warp_distinct_sort(T* buf, unsigned a, unsigned 
 }
 
 template <class T, int MULT>
-__global__ void __launch_bounds__(kTileThreads * MULT, MULT == 1 ? 2 : 1)
-    k_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, const TileDesc* __restrict__ tiles,
-                const uint32_t* __restrict__ ids, TileOut<T>* __restrict__ tout, unsigned long long* fallbacks,
-                TileRanges<T> rg) {
+__device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, uint32_t* __restrict__ counts,
+                                          const TileDesc* __restrict__ tiles, TileOut<T>* __restrict__ tout,
+                                          unsigned long long* fallbacks, const TileRanges<T>& rg) {
   using L = BinSmem<T, MULT>;
   constexpr int NT = L::NT, NW = L::NW, ITEMS = L::ITEMS;
   extern __shared__ __align__(16) uint8_t sm[];
@@ -299,7 +298,6 @@ __global__ void __launch_bounds__(kTileThreads * MULT, MULT == 1 ? 2 : 1)
   unsigned* misc = reinterpret_cast<unsigned*>(scan64 + 64);  // [0] LSD fallback, [1] large bins
   unsigned short* large = reinterpret_cast<unsigned short*>(misc + 4);
 
-  const uint32_t tid = ids ? ids[blockIdx.x] : blockIdx.x;
   const TileDesc td = tiles[tid];
   const unsigned n = td.len;
   if (n > (unsigned)L::CAP) return;  // oversized tiles take a larger path
@@ -502,34 +500,55 @@ __global__ void __launch_bounds__(kTileThreads * MULT, MULT == 1 ? 2 : 1)
   }
 }
 
+// One CTA per tile: tile blockIdx.x (+ the launch's first) or ids[blockIdx.x];
+// with a device count, CTAs walk ids[0 .. *nids) in turn.
 template <class T, int MULT>
-static void tile_sort_with(T* keys, uint32_t* counts, const TileDesc* tiles, const uint32_t* ids, uint32_t n,
-                           TileOut<T>* out, unsigned long long* fallbacks, TileRanges<T> rg, cudaStream_t s) {
+__global__ void __launch_bounds__(kTileThreads * MULT, MULT == 1 ? 2 : 1)
+    k_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, const TileDesc* __restrict__ tiles,
+                const uint32_t* __restrict__ ids, const unsigned* __restrict__ nids, TileOut<T>* __restrict__ tout,
+                unsigned long long* fallbacks, TileRanges<T> rg) {
+  if (nids) {
+    const unsigned cnt = *nids;
+    for (unsigned i = blockIdx.x; i < cnt; i += gridDim.x) {
+      sort_tile<T, MULT>(ids[i], keys, counts, tiles, tout, fallbacks, rg);
+      __syncthreads();  // shared memory is reused by the next tile
+    }
+  } else {
+    sort_tile<T, MULT>(ids ? ids[blockIdx.x] : blockIdx.x, keys, counts, tiles, tout, fallbacks, rg);
+  }
+}
+
+template <class T, int MULT>
+static void tile_sort_with(T* keys, uint32_t* counts, const TileDesc* tiles, const uint32_t* ids,
+                           const unsigned* nids, uint32_t n, TileOut<T>* out, unsigned long long* fallbacks,
+                           TileRanges<T> rg, cudaStream_t s) {
   const size_t smem = BinSmem<T, MULT>::total;
   cudaFuncSetAttribute(k_tile_sort<T, MULT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(k_tile_sort<T, MULT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  if (n) k_tile_sort<T, MULT><<<n, BinSmem<T, MULT>::NT, smem, s>>>(keys, counts, tiles, ids, out, fallbacks, rg);
+  if (n) k_tile_sort<T, MULT><<<n, BinSmem<T, MULT>::NT, smem, s>>>(keys, counts, tiles, ids, nids, out, fallbacks, rg);
 }
 
 template <class T>
 void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
                       unsigned long long* fallbacks, TileRanges<T> rg, cudaStream_t s) {
-  tile_sort_with<T, 1>(keys, counts, tiles, nullptr, ntiles, out, fallbacks, rg, s);
+  tile_sort_with<T, 1>(keys, counts, tiles, nullptr, nullptr, ntiles, out, fallbacks, rg, s);
 }
 template <class T>
 void launch_tile_sort_large(T* keys, uint32_t* counts, const TileDesc* tiles, const uint32_t* ids, uint32_t nids,
-                            TileOut<T>* out, unsigned long long* fallbacks, TileRanges<T> rg, cudaStream_t s) {
-  tile_sort_with<T, 2>(keys, counts, tiles, ids, nids, out, fallbacks, rg, s);
+                            const unsigned* nids_dev, TileOut<T>* out, unsigned long long* fallbacks,
+                            TileRanges<T> rg, cudaStream_t s) {
+  tile_sort_with<T, 2>(keys, counts, tiles, ids, nids_dev, nids, out, fallbacks, rg, s);
 }
 template void launch_tile_sort<uint64_t>(uint64_t*, uint32_t*, const TileDesc*, uint32_t, TileOut<uint64_t>*,
                                          unsigned long long*, TileRanges<uint64_t>, cudaStream_t);
 template void launch_tile_sort<u128>(u128*, uint32_t*, const TileDesc*, uint32_t, TileOut<u128>*, unsigned long long*,
                                      TileRanges<u128>, cudaStream_t);
 template void launch_tile_sort_large<uint64_t>(uint64_t*, uint32_t*, const TileDesc*, const uint32_t*, uint32_t,
-                                               TileOut<uint64_t>*, unsigned long long*, TileRanges<uint64_t>,
-                                               cudaStream_t);
+                                               const unsigned*, TileOut<uint64_t>*, unsigned long long*,
+                                               TileRanges<uint64_t>, cudaStream_t);
 template void launch_tile_sort_large<u128>(u128*, uint32_t*, const TileDesc*, const uint32_t*, uint32_t,
-                                           TileOut<u128>*, unsigned long long*, TileRanges<u128>, cudaStream_t);
+                                           const unsigned*, TileOut<u128>*, unsigned long long*, TileRanges<u128>,
+                                           cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Oversized tiles: one CTA, LSD passes through global memory.  Each pass
@@ -538,10 +557,9 @@ template void launch_tile_sort_large<u128>(u128*, uint32_t*, const TileDesc*, co
 // Then a chunked run-length reduction with carries between chunks.
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void __launch_bounds__(kTileThreads, 1)
-    k_big_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, T* __restrict__ scratch,
-                    const TileDesc* __restrict__ tiles, const uint32_t* __restrict__ big_ids,
-                    TileOut<T>* __restrict__ tout, DevStatus* st) {
+__device__ __forceinline__ void big_sort_tile(uint32_t tid, T* __restrict__ keys, uint32_t* __restrict__ counts,
+                                              T* __restrict__ scratch, const TileDesc* __restrict__ tiles,
+                                              TileOut<T>* __restrict__ tout, DevStatus* st) {
   using L = TileSmem<T>;
   constexpr int NT = L::NT, ITEMS = L::ITEMS, CAP = L::CAP;
   extern __shared__ __align__(16) uint8_t sm[];
@@ -553,7 +571,6 @@ __global__ void __launch_bounds__(kTileThreads, 1)
   unsigned* dtot = reinterpret_cast<unsigned*>(sm + L::buf_bytes + L::hist_bytes);        // 256 (head area)
   unsigned* dstart = dtot + 256;                                                          // 256
 
-  const uint32_t tid = big_ids[blockIdx.x];
   const TileDesc td = tiles[tid];
   const unsigned long long n = td.len;
   T* src = keys + td.start;
@@ -701,16 +718,67 @@ __global__ void __launch_bounds__(kTileThreads, 1)
   (void)st;
 }
 
+// One CTA per listed tile, or (device count) CTAs walking the list in turn.
+template <class T>
+__global__ void __launch_bounds__(kTileThreads, 1)
+    k_big_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, T* __restrict__ scratch,
+                    const TileDesc* __restrict__ tiles, const uint32_t* __restrict__ big_ids,
+                    const unsigned* __restrict__ nids, TileOut<T>* __restrict__ tout, DevStatus* st) {
+  if (nids) {
+    const unsigned cnt = *nids;
+    for (unsigned i = blockIdx.x; i < cnt; i += gridDim.x) {
+      big_sort_tile<T>(big_ids[i], keys, counts, scratch, tiles, tout, st);
+      __syncthreads();  // shared memory is reused by the next tile
+    }
+  } else {
+    big_sort_tile<T>(big_ids[blockIdx.x], keys, counts, scratch, tiles, tout, st);
+  }
+}
+
 template <class T>
 void launch_big_tile_sort(T* keys, uint32_t* counts, T* scratch, const TileDesc* tiles, const uint32_t* big_ids,
-                          uint32_t nbig, TileOut<T>* out, DevStatus* st, cudaStream_t s) {
+                          uint32_t nbig, const unsigned* nbig_dev, TileOut<T>* out, DevStatus* st, cudaStream_t s) {
   const size_t smem = TileSmem<T>::total;
   cudaFuncSetAttribute(k_big_tile_sort<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (nbig) k_big_tile_sort<T><<<nbig, kTileThreads, smem, s>>>(keys, counts, scratch, tiles, big_ids, out, st);
+  if (nbig)
+    k_big_tile_sort<T><<<nbig, kTileThreads, smem, s>>>(keys, counts, scratch, tiles, big_ids, nbig_dev, out, st);
 }
 template void launch_big_tile_sort<uint64_t>(uint64_t*, uint32_t*, uint64_t*, const TileDesc*, const uint32_t*,
-                                             uint32_t, TileOut<uint64_t>*, DevStatus*, cudaStream_t);
+                                             uint32_t, const unsigned*, TileOut<uint64_t>*, DevStatus*,
+                                             cudaStream_t);
 template void launch_big_tile_sort<u128>(u128*, uint32_t*, u128*, const TileDesc*, const uint32_t*, uint32_t,
-                                         TileOut<u128>*, DevStatus*, cudaStream_t);
+                                         const unsigned*, TileOut<u128>*, DevStatus*, cudaStream_t);
+
+// Oversized tiles listed on the device, per bucket group: group g (buckets
+// gb[g] .. gb[g+1]) lists its tiles above the on-chip capacity (up to twice
+// it) from ids[gb[g] * S] on and those above twice it from ids2[gb[g] * S] on,
+// with the counts in cnt[2g] and cnt[2g + 1].  Also the tile statistics:
+// stats[0] largest tile, [1] keys, [2] non-empty tiles, range[t] keys in tile
+// index t of every bucket.
+__global__ void k_tile_lists(const uint32_t* __restrict__ lens, uint32_t ntiles, uint32_t S,
+                             const uint32_t* __restrict__ gb, uint32_t NG, uint32_t cap, uint32_t* __restrict__ ids,
+                             uint32_t* __restrict__ ids2, unsigned* __restrict__ cnt,
+                             unsigned long long* __restrict__ stats, unsigned long long* __restrict__ range) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const uint32_t len = lens[t];
+  if (len == 0) return;
+  const uint32_t b = t / S;
+  uint32_t g = 0;
+  while (g + 1 < NG && gb[g + 1] <= b) ++g;
+  if (len > 2 * cap) ids2[(size_t)gb[g] * S + atomicAdd(&cnt[2 * g + 1], 1u)] = t;
+  else if (len > cap) ids[(size_t)gb[g] * S + atomicAdd(&cnt[2 * g], 1u)] = t;
+  atomicMax(&stats[0], (unsigned long long)len);
+  atomicAdd(&stats[1], (unsigned long long)len);
+  atomicAdd(&stats[2], 1ull);
+  atomicAdd(&range[t % S], (unsigned long long)len);
+}
+
+void launch_tile_lists(const uint32_t* lens, uint32_t ntiles, uint32_t S, const uint32_t* gb, uint32_t NG,
+                       uint32_t cap, uint32_t* ids, uint32_t* ids2, unsigned* cnt, unsigned long long* stats,
+                       unsigned long long* range, cudaStream_t s) {
+  if (ntiles)
+    k_tile_lists<<<(ntiles + 255) / 256, 256, 0, s>>>(lens, ntiles, S, gb, NG, cap, ids, ids2, cnt, stats, range);
+}
 
 }  // namespace kite
