@@ -594,7 +594,7 @@ def main():
     pbase = pinned.data_ptr()
     d2h = [0]
 
-    e2e_parts = {"submit_s": 0.0, "finish_s": 0.0, "d2h_ms": 0.0}
+    e2e_parts = {"submit_s": 0.0, "finish_s": 0.0, "d2h_ms": 0.0, "stage_ms": [0.0] * 8}
 
     def e2e_step(cc):
         t_a = time.perf_counter()
@@ -609,7 +609,9 @@ def main():
             out_bytes += n
         cc.finish(collect=True, callback=cb, raw=True)
         e2e_parts["finish_s"] += time.perf_counter() - t_b
-        e2e_parts["d2h_ms"] += cc.stats()["stage_ms"][7]
+        sm = cc.stats()["stage_ms"]
+        e2e_parts["d2h_ms"] += sm[7]
+        e2e_parts["stage_ms"] = [a + b for a, b in zip(e2e_parts["stage_ms"], sm)]
         d2h[0] = out_bytes
 
     ce = gpu.Counter(kk, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED,
@@ -617,7 +619,7 @@ def main():
     e2e_step(ce)
     ce.synchronize()
     for key in e2e_parts:
-        e2e_parts[key] = 0.0
+        e2e_parts[key] = [0.0] * 8 if key == "stage_ms" else 0.0
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -654,7 +656,9 @@ def main():
                         "ms_per_step": te / args.steps * 1e3,
                         "submit_ms": e2e_parts["submit_s"] / args.steps * 1e3,
                         "finish_ms": e2e_parts["finish_s"] / args.steps * 1e3,
-                        "d2h_ms": e2e_parts["d2h_ms"] / args.steps},
+                        "d2h_ms": e2e_parts["d2h_ms"] / args.steps,
+                        # device stages of the end-to-end count (the first two include waiting for the copies)
+                        "stage_ms": {stages[i][0]: round(e2e_parts["stage_ms"][i] / args.steps, 3) for i in stages}},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "splitters": splitters,
                 "tiles": {"tiles": st["tiles"], "per_bucket": st["tiles_per_bucket"], "big": st["big_tiles"],

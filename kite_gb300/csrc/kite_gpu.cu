@@ -89,7 +89,7 @@ struct Chunk {
 enum Stage { ST_LINES = 0, ST_HIST, ST_SCATTER, ST_SPLIT, ST_SORT, ST_BIG, ST_ENCODE, ST_D2H, ST_COUNT };
 
 // Bucket groups of the sort / encode / copy-out pipeline.
-constexpr uint32_t kSortGroups = 4;
+constexpr uint32_t kSortGroups = 8;
 
 }  // namespace
 
