@@ -150,3 +150,16 @@ def test_segments_flush(gpu, orc):
             rows.setdefault(m["partition_id"], []).append(p)
         assert c.stats()["segments"] >= 2
     assert max(len(v) for v in rows.values()) >= 2
+
+
+@pytest.mark.parametrize("mode", ["sampled", "learned"])
+def test_skewed_clustered_tiles(gpu, orc, mode):
+    # AT-rich low-complexity keys (k=63, u128) in 2 partitions: hundreds of
+    # key-range tiles per bucket, keys clustered inside them; thousands of
+    # tiles have bins with many distinct keys and take the LSD fallback.
+    # Bytes must match the oracle with either splitter method.
+    fq = synth.skewed_workload(seed=6, n_reads=12_000, genome_len=400_000)
+    sm = gpu.SPLIT_SAMPLED if mode == "sampled" else gpu.SPLIT_LEARNED
+    st = assert_parity(gpu, orc, fq, 63, True, 2, splitter_mode=sm, imbalance_bound=100.0)
+    assert st["tiles_per_bucket"] > 32
+
