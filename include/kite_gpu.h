@@ -20,6 +20,10 @@
  *                              (load_partition_counts, per-input filter,
  *                              merge_vectors_total, serialize_partition_chunk
  *                              src/kiteops/mod.rs:433-859)
+ *   kite_gpu_dump           <- run_dump src/dump/mod.rs:183-520 through
+ *                              stream_partition_slabs src/dump/merge.rs:282-428
+ *                              (LoserTreeMerger src/dump/loser_tree.rs:141-175,
+ *                              decode_kmer_any src/dump/decoder.rs:27-50)
  *
  * Conventions: every function returns 0 (KITE_OK) or a negative KITE_ERR_*
  * code; no exception crosses the ABI; a context owns all of its device memory
@@ -175,6 +179,18 @@ int kite_gpu_result_partition(kite_gpu_ctx* ctx, uint32_t partition, kite_chunk_
  * non-empty partition, emitted in partition order. */
 int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n, kite_gpu_emit_fn emit,
                    void* user);
+
+/* `kite dump` of one .kite input (same k, canonical, partitions and key width
+ * as the context): per partition, its chunks merged by key with saturating
+ * u32 sums of equal keys, the header min/max applied to the summed count,
+ * then one line "<kmer>\t<count>\n" per key in ascending key order (k bases,
+ * 2-bit codes most significant first as A, C, G, T).  emit is called once per
+ * partition that has lines, in ascending partition order, with meta
+ * {partition_id, codec 0, row_count = lines, raw_bytes = TSV bytes, key_min /
+ * key_max = its first and last key} and the TSV bytes (valid during the
+ * call).  stats.stage_ms[0..4]: decode, tile planning, merge, formatting,
+ * copy to the host. */
+int kite_gpu_dump(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, kite_gpu_emit_fn emit, void* user);
 
 int kite_gpu_get_stats(kite_gpu_ctx* ctx, kite_gpu_stats* out);
 

@@ -1129,7 +1129,17 @@ int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n,
   cudaSetDevice(ctx->cfg.device);
   std::string msg;
   int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, inputs, n, ctx->stream, ctx->cfg.timeout_ms,
-                     emit, user, &msg, &ctx->stats);
+                     false, emit, user, &msg, &ctx->stats);
+  if (rc) ctx->err = msg;
+  return rc;
+}
+
+int kite_gpu_dump(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, kite_gpu_emit_fn emit, void* user) {
+  if (!ctx || !input) return KITE_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->cfg.device);
+  std::string msg;
+  int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, input, 1, ctx->stream, ctx->cfg.timeout_ms, true, emit, user,
+                     &msg, &ctx->stats);
   if (rc) ctx->err = msg;
   return rc;
 }

@@ -21,8 +21,20 @@
 //             merged ranks by binary search (ties broken by stream order),
 //             per-input sums, filter, cross-input sums, overflow check.
 //   encode    the count path's DVLE link + encode kernels.
+//
+// The same decode / tile / merge stages serve `kite dump` (one input):
+//   LoserTreeMerger src/dump/loser_tree.rs:141-175  the chunks of a partition
+//                           merged by key, equal keys summed with saturating
+//                           u32 adds (= the u64 sum clamped to u32::MAX)
+//   stream_partition_slabs src/dump/merge.rs:282-428  header min/max applied
+//                           to that summed count, then one TSV line per row
+//   decode_kmer_any src/dump/decoder.rs:27-50  the key's 2-bit codes MSB
+//                           first as ACGT, "<kmer>\t<count>\n"
+// with a formatting pass in place of the DVLE encode.
 #include <algorithm>
 #include <cstring>
+#include <memory>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -38,6 +50,14 @@ constexpr uint32_t kSeg = 2048;          // decode segment bytes
 constexpr int kMergeThreads = 512;
 constexpr uint32_t kMergeCap = 4096;      // rows per merge tile
 constexpr uint32_t kMaxTileStreams = 256; // streams per tile (inputs x chunks)
+constexpr int kTsvThreads = 256;          // rows per formatting round
+
+// Decimal digits of a count.
+__host__ __device__ __forceinline__ unsigned dec_digits(uint32_t v) {
+  unsigned d = 1;
+  for (uint32_t p = 10; d < 10 && v >= p; p *= 10) ++d;
+  return d;
+}
 
 struct StreamDesc {
   uint64_t byte_off;   // payload offset in the device byte buffer
@@ -207,12 +227,16 @@ struct MergeSmem {
   static constexpr size_t total = keys + cnts + tag + perm + ((head + 15) & ~(size_t)15) + seg + misc;
 };
 
-template <class T>
+// DUMP = false: `kite merge` (per-input filter on the per-input sum, u64
+// totals, overflow above u32 recorded).  DUMP = true: `kite dump` of one
+// input (the sum clamped to u32 first, the header filter on the clamped
+// count; rest_bytes of a tile = its TSV bytes, lines of line_k + 2 + digits).
+template <class T, bool DUMP>
 __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
     const T* __restrict__ keys, const unsigned long long* __restrict__ counts, const MergeTile* __restrict__ tiles,
     const TileStream* __restrict__ ts, const InputFilter* __restrict__ filt, T* __restrict__ out_keys,
     uint32_t* __restrict__ out_counts, TileOut<T>* __restrict__ tout, unsigned long long* __restrict__ overflow,
-    DevStatus* st) {
+    DevStatus* st, uint32_t line_k) {
   using L = MergeSmem<T>;
   constexpr int NT = kMergeThreads;
   extern __shared__ __align__(16) uint8_t sm[];
@@ -323,7 +347,8 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
         if (in != cur_in) {
           if (cur_in != 0xffffffffu) {
             const InputFilter f = filt[cur_in];
-            const bool ok = !(f.has_min && part < f.min_count) && !(f.has_max && part > f.max_count);
+            const unsigned long long eff = DUMP && part > 0xffffffffull ? 0xffffffffull : part;
+            const bool ok = !(f.has_min && eff < f.min_count) && !(f.has_max && eff > f.max_count);
             if (ok) {
               total = (total > ~0ull - part) ? ~0ull : total + part;
               present = true;
@@ -342,7 +367,8 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
     const unsigned idx = block_exclusive_scan<NT, unsigned>(present ? 1u : 0u, scan_b, &tot);
     if (present) {
       const unsigned long long o = out_base + idx;
-      if (total > 0xffffffffull) atomicMin(overflow, ((unsigned long long)blockIdx.x << 32) | (o & 0xffffffffull));
+      if (!DUMP && total > 0xffffffffull)
+        atomicMin(overflow, ((unsigned long long)blockIdx.x << 32) | (o & 0xffffffffull));
       const uint32_t c32 = total > 0xffffffffull ? 0xffffffffu : (uint32_t)total;
       out_keys[mt.out_off + o] = key;
       out_counts[mt.out_off + o] = c32;
@@ -355,7 +381,9 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
       const unsigned long long o = out_base + u;
       const T kk = out_keys[mt.out_off + o];
       const uint32_t cc = out_counts[mt.out_off + o];
-      if (o > 0) {
+      if (DUMP) {
+        rest += line_k + 2 + dec_digits(cc);
+      } else if (o > 0) {
         const T pk = out_keys[mt.out_off + o - 1];
         rest += (unsigned long long)(varint_len((T)(kk - pk)) + varint_len((uint64_t)cc));
       }
@@ -386,6 +414,53 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
   }
 }
 
+// TSV lines of one merged tile: rows in rounds of kTsvThreads, each round's
+// lines assembled in shared memory (block scan of the line lengths), then
+// stored as one contiguous run of bytes at the tile's output offset.
+template <class T>
+__global__ void __launch_bounds__(kTsvThreads) k_tsv_tiles(const T* __restrict__ keys,
+                                                           const uint32_t* __restrict__ counts,
+                                                           const MergeTile* __restrict__ tiles,
+                                                           const TileOut<T>* __restrict__ tout,
+                                                           const unsigned long long* __restrict__ tboff, uint32_t k,
+                                                           uint8_t* __restrict__ out) {
+  constexpr int NT = kTsvThreads;
+  extern __shared__ __align__(16) uint8_t sm[];
+  unsigned* scan = reinterpret_cast<unsigned*>(sm);
+  char* buf = reinterpret_cast<char*>(sm + 256);
+  const uint64_t base = tiles[blockIdx.x].out_off;
+  const uint32_t rows = tout[blockIdx.x].rows;
+  unsigned long long dst = tboff[blockIdx.x];
+  for (uint32_t r0 = 0; r0 < rows; r0 += NT) {
+    const uint32_t r = r0 + threadIdx.x;
+    T key = T(0);
+    uint32_t c = 0;
+    unsigned len = 0;
+    if (r < rows) {
+      key = keys[base + r];
+      c = counts[base + r];
+      len = k + 2 + dec_digits(c);
+    }
+    unsigned tot;
+    const unsigned o = block_exclusive_scan<NT, unsigned>(len, scan, &tot);
+    if (len) {
+      char* p = buf + o;
+      for (uint32_t i = 0; i < k; ++i) p[i] = "ACGT"[(unsigned)(key >> (2 * (k - 1 - i))) & 3u];
+      p[k] = '\t';
+      uint32_t v = c;
+      for (unsigned i = len - 2; i > k; --i) {
+        p[i] = (char)('0' + v % 10);
+        v /= 10;
+      }
+      p[len - 1] = '\n';
+    }
+    __syncthreads();
+    for (unsigned i = threadIdx.x; i < tot; i += NT) out[dst + i] = (uint8_t)buf[i];
+    dst += tot;
+    __syncthreads();
+  }
+}
+
 template <class T>
 struct Key128 {
   static unsigned __int128 to(T v) { return (unsigned __int128)v; }
@@ -410,7 +485,7 @@ struct Dev {
 
 template <class T>
 int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, int n, cudaStream_t s,
-                uint32_t timeout_ms,
+                uint32_t timeout_ms, bool dump,
                 kite_gpu_emit_fn emit, void* user, std::string* msg, kite_gpu_stats* stat) {
   auto fail = [&](int code, const std::string& m) {
     *msg = m;
@@ -423,6 +498,19 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   } while (0)
   auto sync = [&]() { return bounded_sync(s, timeout_ms); };
   const uint32_t head_bytes = sizeof(T) + 4;
+  // stage timing: [0] decode, [1] tile planning, [2] merge, [3] encode or
+  // TSV formatting, [4] copy of the output to the host (events 0-3 back to
+  // back, then 4-6 around the last two stages)
+  cudaEvent_t sev[7];
+  for (auto& e : sev)
+    if (cudaEventCreate(&e) != cudaSuccess) return fail(KITE_ERR_CUDA, "event create");
+  struct EvGuard {
+    cudaEvent_t* e;
+    ~EvGuard() {
+      for (int i = 0; i < 7; ++i) cudaEventDestroy(e[i]);
+    }
+  } ev_guard{sev};
+  for (int i = 0; i < 12; ++i) stat->stage_ms[i] = 0;
   // ---- streams (one per input chunk), bytes to the device ----
   std::vector<StreamDesc> streams;
   std::vector<uint64_t> in_base(n);
@@ -470,6 +558,7 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     if (in_span[i].second > in_span[i].first)
       MCU(cudaMemcpyAsync(d_bytes.as<uint8_t>() + in_base[i], in[i].base + in_span[i].first,
                           in_span[i].second - in_span[i].first, cudaMemcpyHostToDevice, s));
+  MCU(cudaEventRecord(sev[0], s));
   // ---- decode segments ----
   std::vector<SegDesc> segs;
   std::vector<uint32_t> raw_ids;
@@ -558,6 +647,7 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
                                                           d_keys.as<T>(), d_counts.as<unsigned long long>(), dst);
     launches++;
   }
+  MCU(cudaEventRecord(sev[1], s));
   // ---- tiles: global splitters from a row sample, refined by bisection ----
   std::vector<uint32_t> part_first_stream(P + 1, 0);
   {
@@ -716,15 +806,17 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   MCU(cudaMemcpyAsync(d_filt.p, filt.data(), n * sizeof(InputFilter), cudaMemcpyHostToDevice, s));
   MCU(cudaMemsetAsync(d_over.p, 0xff, 8, s));
   const size_t smem = MergeSmem<T>::total;
-  cudaFuncSetAttribute(k_merge_tiles<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto kmerge = dump ? k_merge_tiles<T, true> : k_merge_tiles<T, false>;
+  cudaFuncSetAttribute(kmerge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  MCU(cudaEventRecord(sev[2], s));
   if (ntiles) {
-    k_merge_tiles<T><<<ntiles, kMergeThreads, smem, s>>>(d_keys.as<T>(), d_counts.as<unsigned long long>(),
-                                                         d_mt.as<MergeTile>(), d_ts.as<TileStream>(),
-                                                         d_filt.as<InputFilter>(), d_okeys.as<T>(),
-                                                         d_ocounts.as<uint32_t>(), d_tout.as<TileOut<T>>(),
-                                                         d_over.as<unsigned long long>(), dst);
+    kmerge<<<ntiles, kMergeThreads, smem, s>>>(d_keys.as<T>(), d_counts.as<unsigned long long>(),
+                                               d_mt.as<MergeTile>(), d_ts.as<TileStream>(), d_filt.as<InputFilter>(),
+                                               d_okeys.as<T>(), d_ocounts.as<uint32_t>(), d_tout.as<TileOut<T>>(),
+                                               d_over.as<unsigned long long>(), dst, key_bits / 2);
     launches++;
   }
+  MCU(cudaEventRecord(sev[3], s));
   DevStatus hst{};
   unsigned long long over = 0;
   std::vector<TileOut<T>> htout(ntiles);
@@ -735,8 +827,80 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   cudaFreeAsync(dst, s);
   if (hst.code) {
     char b[160];
-    snprintf(b, sizeof b, "merge: device status %u (%u, %u, %u)", hst.code, hst.a, hst.b, hst.c);
+    snprintf(b, sizeof b, "%s: device status %u (%u, %u, %u)", dump ? "dump" : "merge", hst.code, hst.a, hst.b,
+             hst.c);
     return fail(hst.code == KITE_DEV_BAD_INPUT ? KITE_ERR_BAD_INPUT : KITE_ERR_DEVICE, b);
+  }
+  auto stage_times = [&]() {
+    static const int pairs[5][2] = {{0, 1}, {1, 2}, {2, 3}, {4, 5}, {5, 6}};
+    float ms = 0;
+    for (int i = 0; i < 5; ++i)
+      if (cudaEventElapsedTime(&ms, sev[pairs[i][0]], sev[pairs[i][1]]) == cudaSuccess) stat->stage_ms[i] = ms;
+  };
+  if (dump) {
+    // ---- TSV: tile byte offsets in (partition, key) order, then formatting ----
+    std::vector<unsigned long long> tboff(ntiles + 1);
+    std::vector<uint64_t> prow(P, 0), pbytes(P, 0);
+    unsigned long long acc = 0;
+    uint64_t out_rows = 0;
+    for (uint32_t t = 0; t < ntiles; ++t) {
+      tboff[t] = acc;
+      acc += htout[t].rest_bytes;
+      prow[mts[t].partition] += htout[t].rows;
+      pbytes[mts[t].partition] += htout[t].rest_bytes;
+      out_rows += htout[t].rows;
+    }
+    tboff[ntiles] = acc;
+    if (!d_boff.ensure((ntiles + 1) * 8) || !d_out.ensure(acc + 16)) return fail(KITE_ERR_OOM, "dump output");
+    if (ntiles && acc) MCU(cudaMemcpyAsync(d_boff.p, tboff.data(), (ntiles + 1) * 8, cudaMemcpyHostToDevice, s));
+    MCU(cudaEventRecord(sev[4], s));
+    if (ntiles && acc) {
+      const size_t tsm = 256 + (size_t)kTsvThreads * (key_bits / 2 + 12);
+      k_tsv_tiles<T><<<ntiles, kTsvThreads, tsm, s>>>(d_okeys.as<T>(), d_ocounts.as<uint32_t>(), d_mt.as<MergeTile>(),
+                                                      d_tout.as<TileOut<T>>(), d_boff.as<unsigned long long>(),
+                                                      key_bits / 2, d_out.as<uint8_t>());
+      launches++;
+    }
+    MCU(cudaEventRecord(sev[5], s));
+    std::unique_ptr<uint8_t[]> hout(new (std::nothrow) uint8_t[acc + 1]);
+    if (!hout) return fail(KITE_ERR_OOM, "dump host buffer");
+    if (acc) MCU(cudaMemcpyAsync(hout.get(), d_out.p, acc, cudaMemcpyDeviceToHost, s));
+    MCU(cudaEventRecord(sev[6], s));
+    if (sync()) return fail(KITE_ERR_TIMEOUT, "dump wait");
+    MCU(cudaGetLastError());
+    stage_times();
+    stat->d2h_bytes += acc;
+    stat->rows = out_rows;
+    stat->payload_bytes = acc;
+    stat->tiles = ntiles;
+    stat->kernel_launches = launches;
+    if (!emit) return KITE_OK;
+    uint64_t off = 0;
+    for (uint32_t p = 0; p < P; ++p) {
+      if (!prow[p]) continue;
+      // key range of the partition's lines: first row of its first non-empty
+      // tile, last row of its last one
+      kite_chunk_meta cm{};
+      cm.partition_id = p;
+      cm.codec = 0;
+      cm.row_count = prow[p];
+      cm.raw_bytes = pbytes[p];
+      bool first = true;
+      for (uint32_t t = tile_first[p]; t < tile_first[p + 1]; ++t) {
+        if (!htout[t].rows) continue;
+        const unsigned __int128 a = (unsigned __int128)htout[t].first_key, b = (unsigned __int128)htout[t].last_key;
+        if (first) {
+          cm.key_min_lo[0] = (uint64_t)a;
+          cm.key_min_lo[1] = (uint64_t)(a >> 64);
+          first = false;
+        }
+        cm.key_max_lo[0] = (uint64_t)b;
+        cm.key_max_lo[1] = (uint64_t)(b >> 64);
+      }
+      if (emit(user, &cm, hout.get() + off, (size_t)pbytes[p])) return fail(KITE_ERR_CALLBACK, "emit callback aborted");
+      off += pbytes[p];
+    }
+    return KITE_OK;
   }
   if (over != ~0ull) {
     // first overflowing row in (partition, key) order: name its key like the reference
@@ -773,14 +937,18 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   DevStatus* est = nullptr;
   MCU(cudaMallocAsync(&est, sizeof(DevStatus), s));
   MCU(cudaMemsetAsync(est, 0, sizeof(DevStatus), s));
+  MCU(cudaEventRecord(sev[4], s));
   launch_encode<T>(d_okeys.as<T>(), d_ocounts.as<uint32_t>(), d_tds.as<TileDesc>(), d_tout.as<TileOut<T>>(),
                    d_boff.as<unsigned long long>(), d_prev.as<T>(), d_meta.as<BucketMeta>(), ntiles,
                    d_out.as<uint8_t>(), out_bytes, est, s);
   launches++;
+  MCU(cudaEventRecord(sev[5], s));
   std::vector<uint8_t> hout(out_bytes);
   if (out_bytes) MCU(cudaMemcpyAsync(hout.data(), d_out.p, out_bytes, cudaMemcpyDeviceToHost, s));
+  MCU(cudaEventRecord(sev[6], s));
   MCU(cudaMemcpyAsync(&hst, est, sizeof hst, cudaMemcpyDeviceToHost, s));
   if (sync()) return fail(KITE_ERR_TIMEOUT, "merge wait");
+  stage_times();
   cudaFreeAsync(est, s);
   if (hst.code) return fail(KITE_ERR_DEVICE, "merge encode failed");
   stat->d2h_bytes += out_bytes;
@@ -818,9 +986,10 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
 }  // namespace
 
 int merge_run(int k, uint32_t partitions, const kite_gpu_merge_input* inputs, int n, cudaStream_t s,
-              uint32_t timeout_ms, kite_gpu_emit_fn emit, void* user, std::string* msg, kite_gpu_stats* st) {
-  if (k <= 31) return merge_typed<uint64_t>(partitions, 2 * k, inputs, n, s, timeout_ms, emit, user, msg, st);
-  return merge_typed<u128>(partitions, 2 * k, inputs, n, s, timeout_ms, emit, user, msg, st);
+              uint32_t timeout_ms, bool dump, kite_gpu_emit_fn emit, void* user, std::string* msg,
+              kite_gpu_stats* st) {
+  if (k <= 31) return merge_typed<uint64_t>(partitions, 2 * k, inputs, n, s, timeout_ms, dump, emit, user, msg, st);
+  return merge_typed<u128>(partitions, 2 * k, inputs, n, s, timeout_ms, dump, emit, user, msg, st);
 }
 
 }  // namespace kite

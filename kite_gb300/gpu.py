@@ -28,7 +28,7 @@ EXPORTED = [
     "kite_gpu_alloc_pinned", "kite_gpu_free_pinned", "kite_gpu_count_submit", "kite_gpu_wait_ticket",
     "kite_gpu_count_submit_device", "kite_gpu_count_finish", "kite_gpu_result_partition", "kite_gpu_merge",
     "kite_gpu_get_stats", "kite_gpu_synchronize", "kite_gpu_count_submit_sample",
-    "kite_gpu_count_submit_device_sample", "kite_gpu_sample_totals",
+    "kite_gpu_count_submit_device_sample", "kite_gpu_sample_totals", "kite_gpu_dump",
 ]
 
 
@@ -109,6 +109,7 @@ def lib() -> C.CDLL:
         L.kite_gpu_result_partition.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(ChunkMeta),
                                                 C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
         L.kite_gpu_merge.argtypes = [C.c_void_p, C.POINTER(MergeInput), C.c_int, EMIT, C.c_void_p]
+        L.kite_gpu_dump.argtypes = [C.c_void_p, C.POINTER(MergeInput), EMIT, C.c_void_p]
         L.kite_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
         L.kite_gpu_synchronize.argtypes = [C.c_void_p]
         _lib = L
@@ -241,6 +242,30 @@ class Counter:
         cb = EMIT(_emit)
         self._check(self._L.kite_gpu_merge(self._h, arr, len(inputs), cb, None))
         return out
+
+    def dump(self, image, callback=None, base: int | None = None) -> bytes:
+        """`kite dump -o -` of one kitefile.KiteImage on the GPU: the TSV of
+        every partition in order.  With a callback, it gets (meta, host
+        address, length) of each partition's TSV (valid during the call) and
+        nothing is returned.  `base`: optional host address holding the
+        image's bytes (no copy)."""
+        mi, keep = image.merge_input(base)
+        parts = []
+
+        def _emit(user, meta, data, n):
+            try:
+                if callback is not None:
+                    callback(meta.contents.as_dict(), C.cast(data, C.c_void_p).value, n)
+                else:
+                    parts.append(C.string_at(data, n))
+                return 0
+            except Exception:  # pragma: no cover - surfaced as KITE_ERR_CALLBACK
+                return 1
+
+        cb = EMIT(_emit)
+        self._check(self._L.kite_gpu_dump(self._h, C.byref(mi), cb, None))
+        del keep
+        return b"".join(parts)
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -345,14 +345,21 @@ int cmd_merge(int argc, char** argv) {
 }
 
 // ---------------------------------------------------------------------------
-// dump (run_dump src/dump/mod.rs:183-520): partitions in order, TSV lines
+// dump (run_dump src/dump/mod.rs:183-520): partitions in order, TSV lines,
+// merged, filtered and formatted on the GPU (kite_gpu_dump)
 // ---------------------------------------------------------------------------
+int dump_write(void* user, const kite_chunk_meta*, const uint8_t* data, size_t len) {
+  return fwrite(data, 1, len, static_cast<FILE*>(user)) == len ? 0 : 1;
+}
+
 int cmd_dump(int argc, char** argv) {
   std::string in, out;
+  int device = 0;
   for (int i = 2; i < argc; ++i) {
     std::string a = argv[i];
     if ((a == "-i" || a == "--input") && i + 1 < argc) in = argv[++i];
     else if ((a == "-o" || a == "--output") && i + 1 < argc) out = argv[++i];
+    else if (a == "--device" && i + 1 < argc) device = (int)parse_u64(a, argv[++i]);
     else if ((a == "-t" || a == "--threads" || a == "--buffer") && i + 1 < argc) ++i;
     else if (a == "-p" || a == "--progress" || a == "--test-mode") continue;
     else die("unexpected argument '" + a + "' found");
@@ -368,17 +375,23 @@ int cmd_dump(int argc, char** argv) {
   fprintf(stderr, "[kite dump] k=%d, partitions=%u, total_chunks=%llu\n", h.k, h.partitions, (unsigned long long)tc);
   fprintf(stderr, "[kite dump] header filters min=%s, max=%s\n", opt_str(h.has_min, h.min_count).c_str(),
           opt_str(h.has_max, h.max_count).c_str());
+  if (h.key_width != 64 && h.key_width != 128) die("dump of 256-bit keys is not supported on the GPU path");
   FILE* f = out == "-" ? stdout : fopen(out.c_str(), "wb");
   if (!f) die("failed to create " + out);
-  char* buf = nullptr;
-  size_t cap = 0;
   const double t0 = now_s();
-  for (uint32_t p = 0; p < h.partitions; ++p) {
-    size_t len = 0;
-    if (kite_dump_partition(r, p, &buf, &cap, &len) < 0) die(kite_host_last_error());
-    if (len && fwrite(buf, 1, len, f) != len) die("write failed");
-  }
-  free(buf);
+  kite_gpu_cfg cfg{};
+  cfg.device = device;
+  cfg.k = h.k;
+  cfg.canonical = h.canonical;
+  cfg.partitions = h.partitions;
+  kite_gpu_ctx* ctx = nullptr;
+  if (kite_gpu_open(&cfg, &ctx) != KITE_OK) die("failed to open the GPU dump context");
+  kite_gpu_merge_input mi{};
+  kite_reader_merge_input(r, &mi);
+  const int rc = kite_gpu_dump(ctx, &mi, dump_write, f);
+  if (rc == KITE_ERR_CALLBACK) die("write failed");
+  if (rc != KITE_OK) die(kite_gpu_last_error(ctx));
+  kite_gpu_close(ctx);
   if (f == stdout) fflush(stdout);
   else fclose(f);
   kite_reader_close(r);
