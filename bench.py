@@ -383,7 +383,7 @@ def run_merge_bench(args, world, rank, local):
         layout = chunk_layout(data)
         pinned = torch.frombuffer(bytearray(data), dtype=torch.uint8).pin_memory()
         base = pinned.data_ptr()
-        w = host.Writer(None, K, CANONICAL, PARTITIONS, 8, 7, 16 << 20, 2)
+        w = host.Writer(None, K, CANONICAL, PARTITIONS, 64, 7, 16 << 20, 2)
         with gpu.Counter(K, CANONICAL, PARTITIONS, device=local, arena_bytes=len(data) + (64 << 20)) as c:
             for o, l in layout:
                 c.submit((base + o, l))
@@ -445,6 +445,108 @@ def run_merge_bench(args, world, rank, local):
     return 0
 
 
+DUMP_METRIC = "dump TSV lines/s (kite dump -o - of the 10M-read k=31 count)"
+
+
+def run_dump_bench(args, world, rank, local):
+    """kite dump of the 10M-read count's .kite image (counted once on this
+    GPU, written in memory by the host writer): one step = one
+    kite_gpu_dump call from the image in pinned host memory to the TSV of
+    every partition in host memory (H2D, decode, per-partition merge with
+    saturating sums, header filter, TSV formatting, D2H)."""
+    import torch
+    from kite_gb300 import gpu, host
+    from kite_gb300.kitefile import KiteImage
+    data = gen_workload(args.reads, seed=2 + rank)
+    layout = chunk_layout(data)
+    pinned = torch.frombuffer(bytearray(data), dtype=torch.uint8).pin_memory()
+    base = pinned.data_ptr()
+    w = host.Writer(None, K, CANONICAL, PARTITIONS, 64, 7, 16 << 20, 2, 2, 1_000_000)
+    with gpu.Counter(K, CANONICAL, PARTITIONS, device=local, arena_bytes=len(data) + (64 << 20)) as c:
+        for o, l in layout:
+            c.submit((base + o, l))
+        for m, p in c.finish():
+            w.append(m, p)
+    w.finalize()
+    image = w.image()
+    w.close()
+    del pinned, data
+    ki = KiteImage.parse(image)
+    pin = torch.empty(len(image), dtype=torch.uint8).pin_memory()
+    pin.numpy()[:] = np.frombuffer(image, dtype=np.uint8)
+    out = {"lines": 0, "bytes": 0}
+
+    def cb(meta, addr, n):
+        out["lines"] += meta["row_count"]
+        out["bytes"] += n
+
+    c = gpu.Counter(K, CANONICAL, PARTITIONS, device=local)
+    for _ in range(args.warmup):
+        out["lines"] = out["bytes"] = 0
+        c.dump(ki, callback=cb, base=pin.data_ptr())
+    torch.cuda.synchronize()
+    barrier(world)
+    stage = [0.0] * 5
+    launches = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out["lines"] = out["bytes"] = 0
+        c.dump(ki, callback=cb, base=pin.data_ptr())
+        st = c.stats()
+        launches += st["kernel_launches"]
+        stage = [a + b for a, b in zip(stage, st["stage_ms"][:5])]
+    c.synchronize()
+    barrier(world)
+    dt = max_over_ranks(world, (time.perf_counter() - t0) / args.steps)
+    c.close()
+    stage = [x / args.steps for x in stage]
+    lines, tsv = out["lines"], out["bytes"]
+    rows_in, payload = ki.total_rows, sum(ch.encoded_bytes for ch in ki.chunks)
+    dev_ms = sum(stage[:4])
+    value = sum_over_ranks(world, lines) / (dev_ms / 1e3)
+    e2e = sum_over_ranks(world, lines) / dt
+    # algorithmic bytes per stage: decode reads the payload and writes (key,
+    # u64 count) rows; the merge reads those and writes (key, u32 count); the
+    # formatting reads (key, count) and writes the TSV
+    names = ["k_seg_decode", "tile planning", "k_merge_tiles<dump>", "k_tsv_tiles", "copy to host"]
+    algo = {0: payload + rows_in * 16, 2: rows_in * 16 + lines * 12, 3: lines * 12 + tsv}
+    dom = max(algo, key=lambda i: stage[i])
+    peak, peak_src = peaks()
+    achieved = algo[dom] / (stage[dom] / 1e3) / 1e9
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+        oracle.lib()
+        # bounded sample: the image of a 1M-read count of the same workload
+        sdata = bytes(gen_workload(1_000_000, seed=2))
+        simg, _ = oracle.count_kite(sdata, K, CANONICAL, PARTITIONS, min_count=2, max_count=1_000_000)
+        t1 = time.perf_counter()
+        tsv_s = oracle.dump(simg)
+        secs = time.perf_counter() - t1
+        cpu = {"value": tsv_s.count(b"\n") / secs, "unit": "lines/s", "cores": 1, "kind": "port",
+               "sample": "oracle dump of the .kite image of a 1M-read count of the same workload (1 thread)",
+               "seconds": secs}
+    if rank == 0:
+        line = {"metric": DUMP_METRIC, "value": value, "unit": "lines/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded)",
+                "config": {"workload": f"kite dump of the .kite image of the {args.reads:,}-read count (k=31 "
+                                       "canonical, 256 partitions, header min 2 / max 1,000,000)",
+                           "rows_in": rows_in, "lines_out": lines, "image_bytes": len(image), "tsv_bytes": tsv,
+                           "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
+                "e2e": {"value": e2e, "unit": "lines/s", "h2d_bytes_per_step": len(image), "d2h_bytes_per_step": tsv,
+                        "ms_per_step": dt * 1e3},
+                "gpu_launches": launches,
+                "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                             "algorithmic_bytes": algo[dom], "kernel_ms": stage[dom],
+                             "stage_ms": {names[i]: round(stage[i], 3) for i in range(5)}},
+                "cpu_baseline": cpu}
+        print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -456,7 +558,7 @@ def main():
     ap.add_argument("--partitions", type=int, default=PARTITIONS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-splitter-compare", action="store_true")
-    ap.add_argument("--workload", default="repeats", choices=["repeats", "skewed", "merge", "batch"])
+    ap.add_argument("--workload", default="repeats", choices=["repeats", "skewed", "merge", "batch", "dump"])
     ap.add_argument("--batch-scale", type=float, default=0.25, help="read-count scale of the batch samples")
     ap.add_argument("--autotune-out", default=None, help="write the batch autotuner's table here (JSON)")
     ap.add_argument("--merge-scale", type=float, default=1.0, help="read-count scale of the merge databases")
@@ -474,6 +576,8 @@ def main():
     from kite_gb300 import gpu
     if args.workload == "merge":
         return run_merge_bench(args, world, rank, local)
+    if args.workload == "dump":
+        return run_dump_bench(args, world, rank, local)
     if args.workload == "batch":
         return run_batch_bench(args, world, rank, local)
 

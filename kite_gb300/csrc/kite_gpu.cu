@@ -115,7 +115,7 @@ struct kite_gpu_ctx {
   DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
   DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats, blk_mat, blk_gsum, blk_keys, stage_ctr;
   DevBuf col_total, sample_first, spans, digits, tile_lists;
-  HostBuf h_blocks, h_small, h_tiles, h_out, h_meta;
+  HostBuf h_blocks, h_small, h_tiles, h_out, h_meta, h_dump;
   std::vector<cudaEvent_t> ev;   // stage events
   std::vector<cudaEvent_t> gev;  // sort / encode / copy-out events, 8 per bucket group
 
@@ -989,6 +989,7 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
   ctx->h_tiles.release();
   ctx->h_out.release();
   ctx->h_meta.release();
+  ctx->h_dump.release();
   mlp_destroy(ctx->mlp);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   cudaStreamDestroy(ctx->copy_stream);
@@ -1138,8 +1139,11 @@ int kite_gpu_dump(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, kite_gpu
   if (!ctx || !input) return KITE_ERR_BAD_INPUT;
   cudaSetDevice(ctx->cfg.device);
   std::string msg;
+  auto staging = [ctx](size_t bytes) -> uint8_t* {
+    return ctx->h_dump.ensure(bytes) == cudaSuccess ? ctx->h_dump.as<uint8_t>() : nullptr;
+  };
   int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, input, 1, ctx->stream, ctx->cfg.timeout_ms, true, emit, user,
-                     &msg, &ctx->stats);
+                     &msg, &ctx->stats, staging);
   if (rc) ctx->err = msg;
   return rc;
 }

@@ -160,6 +160,8 @@ int count_matrix_offsets(unsigned* m, uint32_t rows, uint32_t cols, unsigned lon
 // Waits for the work queued on s, polling with a deadline: 0 ok, -1 CUDA
 // error, -3 timeout.
 int bounded_sync(cudaStream_t s, uint32_t timeout_ms);
+// Waits for one recorded event: 0, -1 (CUDA error) or -3 (timeout).
+int bounded_event_wait(cudaEvent_t e, uint32_t timeout_ms);
 
 // ---- sort_kernels.cu ----
 constexpr int kTileThreads = 512;

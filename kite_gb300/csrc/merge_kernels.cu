@@ -485,8 +485,8 @@ struct Dev {
 
 template <class T>
 int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, int n, cudaStream_t s,
-                uint32_t timeout_ms, bool dump,
-                kite_gpu_emit_fn emit, void* user, std::string* msg, kite_gpu_stats* stat) {
+                uint32_t timeout_ms, bool dump, kite_gpu_emit_fn emit, void* user, std::string* msg,
+                kite_gpu_stats* stat, const StagingFn& staging) {
   auto fail = [&](int code, const std::string& m) {
     *msg = m;
     return code;
@@ -862,44 +862,103 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
       launches++;
     }
     MCU(cudaEventRecord(sev[5], s));
-    std::unique_ptr<uint8_t[]> hout(new (std::nothrow) uint8_t[acc + 1]);
-    if (!hout) return fail(KITE_ERR_OOM, "dump host buffer");
-    if (acc) MCU(cudaMemcpyAsync(hout.get(), d_out.p, acc, cudaMemcpyDeviceToHost, s));
-    MCU(cudaEventRecord(sev[6], s));
-    if (sync()) return fail(KITE_ERR_TIMEOUT, "dump wait");
-    MCU(cudaGetLastError());
-    stage_times();
-    stat->d2h_bytes += acc;
+    stat->d2h_bytes += emit ? acc : 0;
     stat->rows = out_rows;
     stat->payload_bytes = acc;
     stat->tiles = ntiles;
     stat->kernel_launches = launches;
-    if (!emit) return KITE_OK;
-    uint64_t off = 0;
-    for (uint32_t p = 0; p < P; ++p) {
-      if (!prow[p]) continue;
-      // key range of the partition's lines: first row of its first non-empty
-      // tile, last row of its last one
-      kite_chunk_meta cm{};
-      cm.partition_id = p;
-      cm.codec = 0;
-      cm.row_count = prow[p];
-      cm.raw_bytes = pbytes[p];
-      bool first = true;
-      for (uint32_t t = tile_first[p]; t < tile_first[p + 1]; ++t) {
-        if (!htout[t].rows) continue;
-        const unsigned __int128 a = (unsigned __int128)htout[t].first_key, b = (unsigned __int128)htout[t].last_key;
-        if (first) {
-          cm.key_min_lo[0] = (uint64_t)a;
-          cm.key_min_lo[1] = (uint64_t)(a >> 64);
-          first = false;
-        }
-        cm.key_max_lo[0] = (uint64_t)b;
-        cm.key_max_lo[1] = (uint64_t)(b >> 64);
-      }
-      if (emit(user, &cm, hout.get() + off, (size_t)pbytes[p])) return fail(KITE_ERR_CALLBACK, "emit callback aborted");
-      off += pbytes[p];
+    if (!emit || acc == 0) {
+      MCU(cudaEventRecord(sev[6], s));
+      if (sync()) return fail(KITE_ERR_TIMEOUT, "dump wait");
+      MCU(cudaGetLastError());
+      stage_times();
+      return KITE_OK;
     }
+    // ---- copy-out in groups of whole partitions through two pinned halves:
+    // group i+2 is queued once group i has been emitted, so the copy of the
+    // next group overlaps the callback's work on this one
+    uint64_t maxpart = 0;
+    for (uint32_t p = 0; p < P; ++p) maxpart = std::max(maxpart, pbytes[p]);
+    const uint64_t half = std::max<uint64_t>(std::min<uint64_t>(acc, 256ull << 20), maxpart);
+    std::vector<uint32_t> gfirst{0};  // first partition of every group
+    std::vector<uint64_t> goff{0};
+    {
+      uint64_t g = 0, off = 0;
+      for (uint32_t p = 0; p < P; ++p) {
+        if (g + pbytes[p] > half) {
+          gfirst.push_back(p);
+          goff.push_back(off);
+          g = 0;
+        }
+        g += pbytes[p];
+        off += pbytes[p];
+      }
+      gfirst.push_back(P);
+      goff.push_back(off);
+    }
+    const uint32_t ngroups = (uint32_t)gfirst.size() - 1;
+    uint8_t* stage = staging ? staging(ngroups > 1 ? 2 * half : half) : nullptr;
+    std::unique_ptr<uint8_t[]> fallback;
+    if (!stage) {
+      // no pinned staging offered: one pageable buffer for everything
+      fallback.reset(new (std::nothrow) uint8_t[acc]);
+      if (!fallback) return fail(KITE_ERR_OOM, "dump host buffer");
+    }
+    auto group_dst = [&](uint32_t g) { return stage ? stage + (g & 1) * half : fallback.get() + goff[g]; };
+    cudaEvent_t cev[2];
+    for (auto& e : cev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return fail(KITE_ERR_CUDA, "event");
+    struct CevGuard {
+      cudaEvent_t* e;
+      ~CevGuard() {
+        cudaEventDestroy(e[0]);
+        cudaEventDestroy(e[1]);
+      }
+    } cev_guard{cev};
+    auto queue_copy = [&](uint32_t g) -> cudaError_t {
+      const uint64_t n = goff[g + 1] - goff[g];
+      cudaError_t e = n ? cudaMemcpyAsync(group_dst(g), d_out.as<uint8_t>() + goff[g], n, cudaMemcpyDeviceToHost, s)
+                        : cudaSuccess;
+      if (e == cudaSuccess) e = cudaEventRecord(cev[g & 1], s);
+      return e;
+    };
+    MCU(queue_copy(0));
+    if (ngroups > 1) MCU(queue_copy(1));
+    for (uint32_t g = 0; g < ngroups; ++g) {
+      const int w = bounded_event_wait(cev[g & 1], timeout_ms);
+      if (w) return fail(w == -3 ? KITE_ERR_TIMEOUT : KITE_ERR_CUDA, "dump copy wait");
+      const uint8_t* src = group_dst(g);
+      uint64_t off = 0;
+      for (uint32_t p = gfirst[g]; p < gfirst[g + 1]; ++p) {
+        if (!prow[p]) continue;
+        // key range of the partition's lines: first row of its first non-empty
+        // tile, last row of its last one
+        kite_chunk_meta cm{};
+        cm.partition_id = p;
+        cm.codec = 0;
+        cm.row_count = prow[p];
+        cm.raw_bytes = pbytes[p];
+        bool first = true;
+        for (uint32_t t = tile_first[p]; t < tile_first[p + 1]; ++t) {
+          if (!htout[t].rows) continue;
+          const unsigned __int128 a = (unsigned __int128)htout[t].first_key, b = (unsigned __int128)htout[t].last_key;
+          if (first) {
+            cm.key_min_lo[0] = (uint64_t)a;
+            cm.key_min_lo[1] = (uint64_t)(a >> 64);
+            first = false;
+          }
+          cm.key_max_lo[0] = (uint64_t)b;
+          cm.key_max_lo[1] = (uint64_t)(b >> 64);
+        }
+        if (emit(user, &cm, src + off, (size_t)pbytes[p])) return fail(KITE_ERR_CALLBACK, "emit callback aborted");
+        off += pbytes[p];
+      }
+      if (g + 2 < ngroups) MCU(queue_copy(g + 2));
+    }
+    MCU(cudaEventRecord(sev[6], s));
+    if (sync()) return fail(KITE_ERR_TIMEOUT, "dump wait");
+    MCU(cudaGetLastError());
+    stage_times();
     return KITE_OK;
   }
   if (over != ~0ull) {
@@ -987,9 +1046,10 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
 
 int merge_run(int k, uint32_t partitions, const kite_gpu_merge_input* inputs, int n, cudaStream_t s,
               uint32_t timeout_ms, bool dump, kite_gpu_emit_fn emit, void* user, std::string* msg,
-              kite_gpu_stats* st) {
-  if (k <= 31) return merge_typed<uint64_t>(partitions, 2 * k, inputs, n, s, timeout_ms, dump, emit, user, msg, st);
-  return merge_typed<u128>(partitions, 2 * k, inputs, n, s, timeout_ms, dump, emit, user, msg, st);
+              kite_gpu_stats* st, const StagingFn& staging) {
+  if (k <= 31)
+    return merge_typed<uint64_t>(partitions, 2 * k, inputs, n, s, timeout_ms, dump, emit, user, msg, st, staging);
+  return merge_typed<u128>(partitions, 2 * k, inputs, n, s, timeout_ms, dump, emit, user, msg, st, staging);
 }
 
 }  // namespace kite

@@ -146,6 +146,12 @@ int bounded_sync(cudaStream_t s, uint32_t timeout_ms) {
     cudaEventDestroy(e);
     return -1;
   }
+  const int rc = bounded_event_wait(e, timeout_ms);
+  cudaEventDestroy(e);
+  return rc;
+}
+
+int bounded_event_wait(cudaEvent_t e, uint32_t timeout_ms) {
   const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
   int rc = 0;
   for (int spins = 0;; ++spins) {
@@ -161,7 +167,6 @@ int bounded_sync(cudaStream_t s, uint32_t timeout_ms) {
     }
     if (spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
-  cudaEventDestroy(e);
   return rc;
 }
 

@@ -138,7 +138,10 @@ class Writer:
     def image(self) -> bytes:
         n = C.c_size_t()
         p = self._L.kite_writer_image(self._w, C.byref(n))
-        return C.string_at(p, n.value) if p else b""
+        if not p or n.value == 0:
+            return b""
+        # a sized array, not string_at (whose length is a C int: images pass 2 GB)
+        return bytes((C.c_uint8 * n.value).from_address(C.addressof(p.contents)))
 
     def close(self) -> None:
         if self._w:

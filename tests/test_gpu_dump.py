@@ -139,3 +139,26 @@ def test_dump_tile_refinement_and_meta(gpu, orc):
         assert m["row_count"] == len(lines) and m["raw_bytes"] == len(tsv) and m["codec"] == 0
         assert m["key_min"] == _kmer_value(lines[0].split(b"\t")[0])
         assert m["key_max"] == _kmer_value(lines[-1].split(b"\t")[0])
+
+
+def test_dump_streams_groups(gpu, orc):
+    # a TSV of ~0.8 GB leaves the device in several groups of whole
+    # partitions through the two pinned staging halves (256 MB each)
+    g = synth.genome_iid(np.random.default_rng(17), 20_000_000)
+    fq = bytes(host.synth_reads(g, 300_000, 150, 0.01, 0.001, 0.5, seed=17))
+    w = host.Writer(None, 31, True, 64, 64, 7, 16 << 20, 2)
+    with gpu.Counter(31, True, 64) as c:
+        c.submit(fq)
+        for m, p in c.finish():
+            w.append(m, p)
+    w.worker_drain()
+    w.finalize()
+    img = w.image()
+    w.close()
+    with gpu.Counter(31, True, 64) as c:
+        parts = []
+        c.dump(KiteImage.parse(img), callback=lambda m, addr, n: parts.append(ctypes.string_at(addr, n)))
+        st = c.stats()
+    tsv = b"".join(parts)
+    assert st["payload_bytes"] == len(tsv) > (600 << 20)
+    assert tsv == orc.dump(img)
