@@ -207,6 +207,30 @@ __global__ void k_lower_bound(const T* __restrict__ keys, const uint64_t* __rest
   out[i] = lo;
 }
 
+// Row position of every splitter in every stream: pos[s * (S + 1) + j] is
+// lower_bound(spl[j - 1]) in stream s's rows for 1 <= j < S, the stream's
+// first row for j = 0 and its end for j = S.
+template <class T>
+__global__ void k_range_positions(const T* __restrict__ keys, const StreamDesc* __restrict__ streams, uint32_t nst,
+                                  const T* __restrict__ spl, uint32_t S, uint64_t* __restrict__ pos) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)nst * (S + 1)) return;
+  const uint32_t si = (uint32_t)(i / (S + 1)), j = (uint32_t)(i % (S + 1));
+  const StreamDesc sd = streams[si];
+  uint64_t lo = sd.row_off, hi = sd.row_off + sd.rows;
+  if (j == 0 || j == S) {
+    pos[i] = j == 0 ? lo : hi;
+    return;
+  }
+  const T key = spl[j - 1];
+  while (lo < hi) {
+    const uint64_t mid = lo + (hi - lo) / 2;
+    if (keys[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  pos[i] = lo;
+}
+
 template <class T>
 __global__ void k_sample_rows(const T* __restrict__ keys, uint64_t nrows, uint32_t nsample, T* __restrict__ out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -661,9 +685,10 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   uint32_t S = 1;
   while ((double)total_rows / ((double)P * S) > 0.25 * kMergeCap && S < 4096) S <<= 1;
   std::vector<T> spl;
+  Dev d_spl;
   if (S > 1 && total_rows) {
     const uint32_t ns = (uint32_t)std::min<uint64_t>(total_rows, 1u << 20);
-    Dev d_sample, d_spl, d_hist;
+    Dev d_sample, d_hist;
     if (!d_sample.ensure(ns * sizeof(T)) || !d_spl.ensure(S * sizeof(T)) || !d_hist.ensure(65536 * 4))
       return fail(KITE_ERR_OOM, "merge splitters");
     k_sample_rows<T><<<(ns + 255) / 256, 256, 0, s>>>(d_keys.as<T>(), total_rows, ns, d_sample.as<T>());
@@ -673,31 +698,71 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
                                               d_hist.as<unsigned>(), s);
     spl.resize(S - 1);
     MCU(cudaMemcpyAsync(spl.data(), d_spl.p, (S - 1) * sizeof(T), cudaMemcpyDeviceToHost, s));
-    if (sync()) return fail(KITE_ERR_TIMEOUT, "merge splitter wait");
+  } else {
+    S = 1;
   }
-  // ranges per partition: [lo_key, hi_key) with an "unbounded" flag for the top
+  // ---- first cut on the device: the row position of every splitter in every
+  // stream (one binary search each), read back as one matrix
+  const size_t SP = (size_t)S + 1;
+  std::vector<uint64_t> pos((size_t)nst * SP);
+  if (nst && S > 1) {
+    Dev d_pos;
+    if (!d_pos.ensure(pos.size() * 8)) return fail(KITE_ERR_OOM, "merge range positions");
+    const uint64_t nq = pos.size();
+    k_range_positions<T><<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(d_keys.as<T>(), d_streams.as<StreamDesc>(), nst,
+                                                                     d_spl.as<T>(), S, d_pos.as<uint64_t>());
+    launches++;
+    MCU(cudaMemcpyAsync(pos.data(), d_pos.p, nq * 8, cudaMemcpyDeviceToHost, s));
+    if (sync()) return fail(KITE_ERR_TIMEOUT, "merge range wait");
+  } else {
+    if (sync()) return fail(KITE_ERR_TIMEOUT, "merge splitter wait");
+    for (uint32_t si = 0; si < nst; ++si) {
+      pos[si * SP] = streams[si].row_off;
+      pos[si * SP + 1] = streams[si].row_off + streams[si].rows;
+    }
+  }
+  // A finished range: partition, low key, and the offset of its per-stream
+  // [lo, hi) row positions in dlo / dhi (one entry per stream of the
+  // partition).  Ranges above the on-chip capacity are bisected by key.
+  struct Done {
+    uint32_t p;
+    T lo;
+    uint64_t off;
+  };
   struct Range {
     uint32_t p;
     T lo, hi;
     bool open_hi;
-    std::vector<uint64_t> lo_pos, hi_pos;  // per stream of p
   };
-  std::vector<Range> work, done;
+  std::vector<Done> done;
+  std::vector<uint64_t> dlo, dhi;
+  std::vector<Range> work;
   for (uint32_t p = 0; p < P; ++p) {
-    if (part_first_stream[p] == part_first_stream[p + 1]) continue;
-    T lo = 0;
+    const uint32_t f = part_first_stream[p], nstr = part_first_stream[p + 1] - f;
+    if (!nstr) continue;
     for (uint32_t j = 0; j < S; ++j) {
-      Range r;
-      r.p = p;
-      r.lo = lo;
-      r.open_hi = j + 1 == S;
-      r.hi = r.open_hi ? T(0) : spl[j];
-      if (!r.open_hi && r.hi <= r.lo) continue;  // empty (repeated splitter)
-      work.push_back(r);
-      if (!r.open_hi) lo = r.hi;
+      const T lo = j ? spl[j - 1] : T(0);
+      const bool open_hi = j + 1 == S;
+      const T hi = open_hi ? T(0) : spl[j];
+      if (!open_hi && hi <= lo) continue;  // empty (repeated splitter)
+      uint64_t rows = 0;
+      for (uint32_t k2 = 0; k2 < nstr; ++k2) rows += pos[(f + k2) * SP + j + 1] - pos[(f + k2) * SP + j];
+      if (rows == 0) continue;
+      if (rows <= kMergeCap && nstr <= kMaxTileStreams) {
+        done.push_back(Done{p, lo, (uint64_t)dlo.size()});
+        for (uint32_t k2 = 0; k2 < nstr; ++k2) {
+          dlo.push_back(pos[(f + k2) * SP + j]);
+          dhi.push_back(pos[(f + k2) * SP + j + 1]);
+        }
+      } else {
+        work.push_back(Range{p, lo, hi, open_hi});
+      }
     }
   }
+  std::vector<uint64_t>().swap(pos);
+  const size_t first_cut = done.size();  // in (partition, key) order
   Dev d_qlo, d_qhi, d_qkey, d_qout;
+  std::vector<uint64_t> lp, hp;
   for (int round = 0; !work.empty() && round < 200; ++round) {
     // queries: for every range and stream, lower_bound(lo) and lower_bound(hi)
     std::vector<uint64_t> qlo, qhi;
@@ -728,13 +793,13 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     size_t q = 0;
     for (auto& r : work) {
       uint64_t rows = 0;
-      r.lo_pos.clear();
-      r.hi_pos.clear();
+      lp.clear();
+      hp.clear();
       for (uint32_t si = part_first_stream[r.p]; si < part_first_stream[r.p + 1]; ++si) {
         const uint64_t a = qout[q++], b0 = qout[q++];
         const uint64_t b = r.open_hi ? streams[si].row_off + streams[si].rows : b0;
-        r.lo_pos.push_back(a);
-        r.hi_pos.push_back(b);
+        lp.push_back(a);
+        hp.push_back(b);
         rows += b - a;
       }
       const uint32_t nstr = part_first_stream[r.p + 1] - part_first_stream[r.p];
@@ -750,34 +815,46 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
       } else {
         if (rows > kMergeCap || nstr > kMaxTileStreams)
           return fail(KITE_ERR_UNSUPPORTED, "merge tile cannot be split below the on-chip capacity");
-        done.push_back(std::move(r));
+        if (rows) {
+          done.push_back(Done{r.p, r.lo, (uint64_t)dlo.size()});
+          dlo.insert(dlo.end(), lp.begin(), lp.end());
+          dhi.insert(dhi.end(), hp.begin(), hp.end());
+        }
       }
     }
     work.swap(next);
   }
   if (!work.empty()) return fail(KITE_ERR_UNSUPPORTED, "merge tile refinement did not converge");
-  std::sort(done.begin(), done.end(), [](const Range& a, const Range& b) { return a.p != b.p ? a.p < b.p : a.lo < b.lo; });
+  {
+    auto by_key = [](const Done& a, const Done& b) { return a.p != b.p ? a.p < b.p : a.lo < b.lo; };
+    std::sort(done.begin() + first_cut, done.end(), by_key);
+    std::inplace_merge(done.begin(), done.begin() + first_cut, done.end(), by_key);
+  }
   // ---- tile lists ----
   std::vector<MergeTile> mts;
   std::vector<TileStream> tss;
   std::vector<TileDesc> tds;
   std::vector<uint32_t> tile_first(P + 1, 0);
+  mts.reserve(done.size());
+  tds.reserve(done.size());
   uint64_t out_off = 0;
   {
     size_t di = 0;
     for (uint32_t p = 0; p < P; ++p) {
       tile_first[p] = (uint32_t)mts.size();
+      const uint32_t f = part_first_stream[p], nstr = part_first_stream[p + 1] - f;
       while (di < done.size() && done[di].p == p) {
-        const Range& r = done[di++];
+        const Done& r = done[di++];
         MergeTile mt{};
         mt.out_off = out_off;
         mt.first_ts = (uint32_t)tss.size();
         mt.partition = p;
         uint64_t rows = 0;
-        for (size_t k2 = 0; k2 < r.lo_pos.size(); ++k2) {
-          if (r.hi_pos[k2] == r.lo_pos[k2]) continue;
-          tss.push_back(TileStream{r.lo_pos[k2], r.hi_pos[k2], streams[part_first_stream[p] + k2].input, 0});
-          rows += r.hi_pos[k2] - r.lo_pos[k2];
+        for (uint32_t k2 = 0; k2 < nstr; ++k2) {
+          const uint64_t lo = dlo[r.off + k2], hi = dhi[r.off + k2];
+          if (hi == lo) continue;
+          tss.push_back(TileStream{lo, hi, streams[f + k2].input, 0});
+          rows += hi - lo;
         }
         mt.nts = (uint32_t)(tss.size() - mt.first_ts);
         mt.rows_in = (uint32_t)rows;
