@@ -26,6 +26,7 @@ enum : unsigned int {
   KITE_DEV_BAD_INPUT = 4,
   KITE_DEV_ENCODE_OVERFLOW = 5,
   KITE_DEV_COUNT_OVERFLOW = 6,  // merged count exceeds u32 (merge path)
+  KITE_DEV_SHORT_VARINTS = 7,   // a DVLE chunk holds fewer varints than its rows need (merge path)
 };
 
 __device__ __forceinline__ void dev_fail(DevStatus* st, unsigned code, unsigned a = 0, unsigned b = 0,

@@ -12,8 +12,9 @@
 //
 // GPU structure:
 //   decode    payload bytes cut into 2 KiB segments; per-segment varint
-//             terminator counts and delta sums, per-stream scans, then a decode
-//             pass that writes (key, u64 count) rows.  A "stream" is one chunk.
+//             terminator counts and parity sums, per-stream scans on the
+//             device, then a pass that writes (key, u64 count) rows.  A
+//             "stream" is one chunk.
 //   tiles     key-range tiles per partition from global splitters, refined by
 //             bisection until every tile fits on chip; each stream is
 //             binary-searched for the tile edges.
@@ -97,24 +98,120 @@ struct MergeTile {
 
 __device__ __forceinline__ bool is_term(uint8_t b) { return (b & 0x80u) == 0; }
 
-__global__ void k_seg_terms(const uint8_t* __restrict__ bytes, const SegDesc* __restrict__ segs, uint32_t nseg,
-                            uint32_t* __restrict__ terms) {
+// Warp shuffle-up of a 64- or 128-bit value, a wrapping inclusive warp sum,
+// and a broadcast from one lane.
+template <class T>
+__device__ __forceinline__ T shfl_up_t(T v, int d) {
+  if constexpr (sizeof(T) == 8) {
+    return (T)__shfl_up_sync(0xffffffffu, (unsigned long long)v, d);
+  } else {
+    const unsigned long long lo = __shfl_up_sync(0xffffffffu, (unsigned long long)v, d);
+    const unsigned long long hi = __shfl_up_sync(0xffffffffu, (unsigned long long)(v >> 64), d);
+    return ((T)hi << 64) | (T)lo;
+  }
+}
+template <class T>
+__device__ __forceinline__ T warp_incl_sum(T v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T y = shfl_up_t(v, o);
+    if (lane >= o) v += y;
+  }
+  return v;
+}
+template <class T>
+__device__ __forceinline__ T warp_bcast_t(T v, int src) {
+  if constexpr (sizeof(T) == 8) {
+    return (T)__shfl_sync(0xffffffffu, (unsigned long long)v, src);
+  } else {
+    const unsigned long long lo = __shfl_sync(0xffffffffu, (unsigned long long)v, src);
+    const unsigned long long hi = __shfl_sync(0xffffffffu, (unsigned long long)(v >> 64), src);
+    return ((T)hi << 64) | (T)lo;
+  }
+}
+
+// Pass A, one thread per segment: the varints whose terminator lies in the
+// segment, and the wrapping sums of those at even / odd positions within the
+// segment (which of the two are key deltas follows from the parity of the
+// segment's first varint index, known after the per-stream scan).
+template <class T>
+__global__ void k_seg_pass_a(const uint8_t* __restrict__ bytes, const SegDesc* __restrict__ segs, uint32_t nseg,
+                             const StreamDesc* __restrict__ streams, uint32_t* __restrict__ terms,
+                             T* __restrict__ sum_even, T* __restrict__ sum_odd) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg) return;
   const SegDesc d = segs[s];
-  uint32_t c = 0;
-  for (uint64_t p = d.start; p < d.end; ++p) c += is_term(bytes[p]);
-  terms[s] = c;
+  const StreamDesc sd = streams[d.stream];
+  const uint64_t area = sd.byte_off + sd.head;
+  // start of the first varint owned by this segment
+  uint64_t p = d.start;
+  while (p > area && !is_term(bytes[p - 1])) --p;
+  const uint64_t lim = sd.byte_off + sd.byte_len;
+  uint32_t n = 0;
+  T se = 0, so = 0;
+  while (p < d.end) {
+    T val = 0;
+    unsigned sh = 0;
+    uint64_t q = p;
+    while (q < lim) {
+      const uint8_t b = bytes[q++];
+      if (sh < (unsigned)KeyTraits<T>::kBits) val |= (T)(b & 0x7f) << sh;
+      sh += 7;
+      if (is_term(b)) break;
+    }
+    if (q > d.end) break;  // terminator in the next segment: that segment owns this varint
+    if (n & 1u) so += val;
+    else se += val;
+    ++n;
+    p = q;
+  }
+  terms[s] = n;
+  sum_even[s] = se;
+  sum_odd[s] = so;
 }
 
-// Decodes the varints whose terminator lies in the segment.  varint index v
-// (within the stream's varint area): even = key delta of row v/2+1, odd =
-// count of row (v-1)/2+1.  MODE 0 sums the deltas, MODE 1 writes rows.
-template <class T, int MODE>
-__global__ void k_seg_decode(const uint8_t* __restrict__ bytes, const SegDesc* __restrict__ segs, uint32_t nseg,
-                             const StreamDesc* __restrict__ streams, const unsigned long long* __restrict__ vstart,
-                             T* __restrict__ dsum, const T* __restrict__ kstart, T* __restrict__ keys,
-                             unsigned long long* __restrict__ counts, DevStatus* st) {
+// Per stream (one warp each): first varint index and start key of every
+// segment (exclusive scans of the terminator counts and of the delta sums),
+// and the check that the stream holds the 2 * (rows - 1) varints its rows need.
+template <class T>
+__global__ void k_stream_seg_scan(const uint32_t* __restrict__ terms, const T* __restrict__ sum_even,
+                                  const T* __restrict__ sum_odd, const uint32_t* __restrict__ seg_first,
+                                  const StreamDesc* __restrict__ streams, const T* __restrict__ first_keys,
+                                  uint32_t nst, unsigned long long* __restrict__ vstart, T* __restrict__ kstart,
+                                  DevStatus* st) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t si = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (si >= nst) return;
+  const StreamDesc sd = streams[si];
+  const uint32_t f = seg_first[si], e = seg_first[si + 1];
+  unsigned long long cv = 0;
+  T ck = f < e ? first_keys[si] : T(0);
+  for (uint32_t b = f; b < e; b += 32) {
+    const uint32_t s = b + lane;
+    const unsigned long long t = s < e ? terms[s] : 0ull;
+    const unsigned long long ti = warp_incl_sum<unsigned long long>(t);
+    const unsigned long long v = cv + ti - t;
+    T dv = 0;
+    if (s < e) dv = (v & 1ull) ? sum_odd[s] : sum_even[s];
+    const T di = warp_incl_sum(dv);
+    if (s < e) {
+      vstart[s] = v;
+      kstart[s] = ck + (di - dv);
+    }
+    cv += __shfl_sync(0xffffffffu, ti, 31);
+    ck += warp_bcast_t(di, 31);
+  }
+  if (lane == 0 && sd.head && sd.rows && cv < 2 * (sd.rows - 1)) dev_fail(st, KITE_DEV_SHORT_VARINTS, si);
+}
+
+// Pass B, one thread per segment: (key, u64 count) rows of the varints whose
+// terminator lies in the segment.  Varint index v (within the stream's varint
+// area): even = key delta of row v/2+1, odd = count of row (v-1)/2+1.
+template <class T>
+__global__ void k_seg_rows(const uint8_t* __restrict__ bytes, const SegDesc* __restrict__ segs, uint32_t nseg,
+                           const StreamDesc* __restrict__ streams, const unsigned long long* __restrict__ vstart,
+                           const T* __restrict__ kstart, T* __restrict__ keys, unsigned long long* __restrict__ counts) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg) return;
   const SegDesc d = segs[s];
@@ -124,7 +221,7 @@ __global__ void k_seg_decode(const uint8_t* __restrict__ bytes, const SegDesc* _
   uint64_t p = d.start;
   while (p > area && !is_term(bytes[p - 1])) --p;
   unsigned long long v = vstart[s];
-  T acc = MODE == 1 ? kstart[s] : T(0);
+  T acc = kstart[s];
   const uint64_t nvar = sd.rows ? 2 * (sd.rows - 1) : 0;
   while (p < d.end) {
     // decode one varint (delta up to 19 bytes for u128, 10 for u64)
@@ -142,14 +239,13 @@ __global__ void k_seg_decode(const uint8_t* __restrict__ bytes, const SegDesc* _
     if (v >= nvar) break;  // bytes after the last row are ignored, as the reference decodes row_count rows
     if ((v & 1ull) == 0) {
       acc += val;  // wrapping add, as the reference's wrapping_add
-      if (MODE == 1) keys[sd.row_off + v / 2 + 1] = acc;
-    } else if (MODE == 1) {
+      keys[sd.row_off + v / 2 + 1] = acc;
+    } else {
       counts[sd.row_off + (v - 1) / 2 + 1] = (unsigned long long)(uint64_t)val;
     }
     ++v;
     p = q;
   }
-  if (MODE == 0) dsum[s] = acc;
 }
 
 // Head row of every DVLE stream and all rows of RAW streams.
@@ -576,7 +672,8 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
         streams.push_back(sd);
       }
   stat->h2d_bytes += total_bytes;
-  Dev d_bytes, d_streams, d_segs, d_terms, d_vstart, d_dsum, d_kstart, d_keys, d_counts, d_first, d_raw;
+  Dev d_bytes, d_streams, d_segs, d_terms, d_vstart, d_dsum, d_dsum2, d_sfirst, d_kstart, d_keys, d_counts, d_first,
+      d_raw;
   if (!d_bytes.ensure(total_bytes + 64)) return fail(KITE_ERR_OOM, "device bytes");
   for (int i = 0; i < n; ++i)
     if (in_span[i].second > in_span[i].first)
@@ -610,67 +707,42 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   if (!raw_ids.empty())
     MCU(cudaMemcpyAsync(d_raw.p, raw_ids.data(), raw_ids.size() * 4, cudaMemcpyHostToDevice, s));
   int launches = 0;
-  if (nseg) {
-    k_seg_terms<<<(nseg + 255) / 256, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_segs.as<SegDesc>(), nseg,
-                                                    d_terms.as<uint32_t>());
-    launches++;
-  }
-  std::vector<uint32_t> terms(nseg);
-  if (nseg) MCU(cudaMemcpyAsync(terms.data(), d_terms.p, nseg * 4, cudaMemcpyDeviceToHost, s));
-  if (sync()) return fail(KITE_ERR_TIMEOUT, "merge decode wait");
-  // per-stream varint starts; the varint count must be 2*(rows-1)
-  std::vector<unsigned long long> vstart(nseg);
-  for (uint32_t si = 0; si < nst; ++si) {
-    unsigned long long v = 0;
-    for (uint32_t g = seg_first[si]; g < seg_first[si + 1]; ++g) {
-      vstart[g] = v;
-      v += terms[g];
-    }
-    const StreamDesc& sd = streams[si];
-    if (sd.head && sd.rows && v < 2 * (sd.rows - 1))
-      return fail(KITE_ERR_BAD_INPUT, sizeof(T) == 8 ? "invalid u64 DVLE delta" : "invalid u128 DVLE delta");
-  }
   DevStatus* dst = nullptr;
   MCU(cudaMallocAsync(&dst, sizeof(DevStatus), s));
   MCU(cudaMemsetAsync(dst, 0, sizeof(DevStatus), s));
-  if (nseg) {
-    MCU(cudaMemcpyAsync(d_vstart.p, vstart.data(), nseg * 8, cudaMemcpyHostToDevice, s));
-    k_seg_decode<T, 0><<<(nseg + 255) / 256, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_segs.as<SegDesc>(), nseg,
-                                                          d_streams.as<StreamDesc>(),
-                                                          d_vstart.as<unsigned long long>(), d_dsum.as<T>(), nullptr,
-                                                          nullptr, nullptr, dst);
+  if (nst) {
+    k_stream_heads<T><<<(nst + 255) / 256, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_streams.as<StreamDesc>(), nst,
+                                                        d_keys.as<T>(), d_counts.as<unsigned long long>(),
+                                                        d_first.as<T>());
     launches++;
   }
-  k_stream_heads<T><<<(nst + 255) / 256, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_streams.as<StreamDesc>(), nst,
-                                                      d_keys.as<T>(), d_counts.as<unsigned long long>(),
-                                                      d_first.as<T>());
-  launches++;
   if (!raw_ids.empty()) {
     k_raw_rows<T><<<(unsigned)raw_ids.size(), 256, 0, s>>>(d_bytes.as<uint8_t>(), d_streams.as<StreamDesc>(),
                                                            d_raw.as<uint32_t>(), (uint32_t)raw_ids.size(),
                                                            d_keys.as<T>(), d_counts.as<unsigned long long>());
     launches++;
   }
-  std::vector<T> dsum(nseg), first(nst);
-  if (nseg) MCU(cudaMemcpyAsync(dsum.data(), d_dsum.p, nseg * sizeof(T), cudaMemcpyDeviceToHost, s));
-  MCU(cudaMemcpyAsync(first.data(), d_first.p, nst * sizeof(T), cudaMemcpyDeviceToHost, s));
-  if (sync()) return fail(KITE_ERR_TIMEOUT, "merge decode wait");
-  std::vector<T> kstart(nseg);
-  for (uint32_t si = 0; si < nst; ++si) {
-    T acc = first[si];
-    for (uint32_t g = seg_first[si]; g < seg_first[si + 1]; ++g) {
-      kstart[g] = acc;
-      acc += dsum[g];
-    }
-  }
+  // DVLE varints: pass A (per-segment counts and parity sums), per-stream
+  // scans on the device, pass B (rows); no host round trip
   if (nseg) {
-    MCU(cudaMemcpyAsync(d_kstart.p, kstart.data(), nseg * sizeof(T), cudaMemcpyHostToDevice, s));
-    k_seg_decode<T, 1><<<(nseg + 255) / 256, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_segs.as<SegDesc>(), nseg,
-                                                          d_streams.as<StreamDesc>(),
-                                                          d_vstart.as<unsigned long long>(), nullptr, d_kstart.as<T>(),
-                                                          d_keys.as<T>(), d_counts.as<unsigned long long>(), dst);
-    launches++;
+    if (!d_dsum2.ensure(nseg * sizeof(T) + 16) || !d_sfirst.ensure((nst + 1) * 4 + 8))
+      return fail(KITE_ERR_OOM, "merge decode buffers");
+    MCU(cudaMemcpyAsync(d_sfirst.p, seg_first.data(), (nst + 1) * 4, cudaMemcpyHostToDevice, s));
+    const unsigned gsegs = (nseg + 255) / 256;
+    k_seg_pass_a<T><<<gsegs, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_segs.as<SegDesc>(), nseg,
+                                          d_streams.as<StreamDesc>(), d_terms.as<uint32_t>(), d_dsum.as<T>(),
+                                          d_dsum2.as<T>());
+    k_stream_seg_scan<T><<<(nst + 7) / 8, 256, 0, s>>>(d_terms.as<uint32_t>(), d_dsum.as<T>(), d_dsum2.as<T>(),
+                                                       d_sfirst.as<uint32_t>(), d_streams.as<StreamDesc>(),
+                                                       d_first.as<T>(), nst, d_vstart.as<unsigned long long>(),
+                                                       d_kstart.as<T>(), dst);
+    k_seg_rows<T><<<gsegs, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_segs.as<SegDesc>(), nseg,
+                                        d_streams.as<StreamDesc>(), d_vstart.as<unsigned long long>(),
+                                        d_kstart.as<T>(), d_keys.as<T>(), d_counts.as<unsigned long long>());
+    launches += 3;
   }
+  DevStatus hdec{};
+  MCU(cudaMemcpyAsync(&hdec, dst, sizeof hdec, cudaMemcpyDeviceToHost, s));
   MCU(cudaEventRecord(sev[1], s));
   // ---- tiles: global splitters from a row sample, refined by bisection ----
   std::vector<uint32_t> part_first_stream(P + 1, 0);
@@ -760,6 +832,9 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     }
   }
   std::vector<uint64_t>().swap(pos);
+  // the decode's status arrived with the sync above
+  if (hdec.code == KITE_DEV_SHORT_VARINTS)
+    return fail(KITE_ERR_BAD_INPUT, sizeof(T) == 8 ? "invalid u64 DVLE delta" : "invalid u128 DVLE delta");
   const size_t first_cut = done.size();  // in (partition, key) order
   Dev d_qlo, d_qhi, d_qkey, d_qout;
   std::vector<uint64_t> lp, hp;
