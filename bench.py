@@ -675,15 +675,27 @@ def main():
                          imbalance_bound=10.0, stream=stream.cuda_stream)
         device_step(cl)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        reps = 2
-        for _ in range(reps):
-            device_step(cl)
-        torch.cuda.synchronize()
-        tl = (time.perf_counter() - t0) / reps
+
+        def timed_step(cc):
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            a0.record(stream)
+            device_step(cc)
+            a1.record(stream)
+            torch.cuda.synchronize()
+            return a0.elapsed_time(a1) / 1e3
+
+        # the same clock for both: CUDA events around one step each, three
+        # interleaved steps per method, median
+        t_s, t_l = [], []
+        for _ in range(3):
+            t_s.append(timed_step(c))
+            t_l.append(timed_step(cl))
+        ts, tl = statistics.median(t_s), statistics.median(t_l)
         stl = cl.stats()
         cl.close()
-        splitters = {"sampled": {"kmers_per_s": value / world, "tile_imbalance": st["tile_imbalance"],
+        splitters = {"timing": "CUDA events around one device-resident step, median of 3 interleaved steps each",
+                     "sampled": {"kmers_per_s": kmers / ts, "tile_imbalance": st["tile_imbalance"],
                                  "range_imbalance": st["range_imbalance"],
                                  "big_tiles": st["big_tiles"]},
                      "learned": {"kmers_per_s": kmers / tl, "tile_imbalance": stl["tile_imbalance"],

@@ -98,6 +98,27 @@ struct MergeTile {
 
 __device__ __forceinline__ bool is_term(uint8_t b) { return (b & 0x80u) == 0; }
 
+// Bytes of the payload buffer read through 16-byte aligned loads kept in
+// registers: a thread walking its segment byte by byte issues one memory
+// request per 16 bytes.  The buffer is allocated with padding past its last
+// byte, so the aligned block of any byte offset inside it is readable.
+struct ByteReader {
+  const uint4* base;
+  uint64_t blk = ~0ull;
+  uint4 w;
+  __device__ __forceinline__ explicit ByteReader(const uint8_t* b) : base(reinterpret_cast<const uint4*>(b)) {}
+  __device__ __forceinline__ uint8_t at(uint64_t q) {
+    const uint64_t b = q >> 4;
+    if (b != blk) {
+      w = __ldg(base + b);
+      blk = b;
+    }
+    const unsigned i = (unsigned)(q & 15u);
+    const unsigned word = i < 8 ? (i < 4 ? w.x : w.y) : (i < 12 ? w.z : w.w);
+    return (uint8_t)(word >> (8 * (i & 3u)));
+  }
+};
+
 // Warp shuffle-up of a 64- or 128-bit value, a wrapping inclusive warp sum,
 // and a broadcast from one lane.
 template <class T>
@@ -144,9 +165,10 @@ __global__ void k_seg_pass_a(const uint8_t* __restrict__ bytes, const SegDesc* _
   const SegDesc d = segs[s];
   const StreamDesc sd = streams[d.stream];
   const uint64_t area = sd.byte_off + sd.head;
+  ByteReader rd(bytes);
   // start of the first varint owned by this segment
   uint64_t p = d.start;
-  while (p > area && !is_term(bytes[p - 1])) --p;
+  while (p > area && !is_term(rd.at(p - 1))) --p;
   const uint64_t lim = sd.byte_off + sd.byte_len;
   uint32_t n = 0;
   T se = 0, so = 0;
@@ -155,7 +177,7 @@ __global__ void k_seg_pass_a(const uint8_t* __restrict__ bytes, const SegDesc* _
     unsigned sh = 0;
     uint64_t q = p;
     while (q < lim) {
-      const uint8_t b = bytes[q++];
+      const uint8_t b = rd.at(q++);
       if (sh < (unsigned)KeyTraits<T>::kBits) val |= (T)(b & 0x7f) << sh;
       sh += 7;
       if (is_term(b)) break;
@@ -217,9 +239,10 @@ __global__ void k_seg_rows(const uint8_t* __restrict__ bytes, const SegDesc* __r
   const SegDesc d = segs[s];
   const StreamDesc sd = streams[d.stream];
   const uint64_t area = sd.byte_off + sd.head;
+  ByteReader rd(bytes);
   // start of the first varint owned by this segment
   uint64_t p = d.start;
-  while (p > area && !is_term(bytes[p - 1])) --p;
+  while (p > area && !is_term(rd.at(p - 1))) --p;
   unsigned long long v = vstart[s];
   T acc = kstart[s];
   const uint64_t nvar = sd.rows ? 2 * (sd.rows - 1) : 0;
@@ -230,7 +253,7 @@ __global__ void k_seg_rows(const uint8_t* __restrict__ bytes, const SegDesc* __r
     uint64_t q = p;
     const uint64_t lim = sd.byte_off + sd.byte_len;
     while (q < lim) {
-      const uint8_t b = bytes[q++];
+      const uint8_t b = rd.at(q++);
       if (sh < (unsigned)KeyTraits<T>::kBits) val |= (T)(b & 0x7f) << sh;
       sh += 7;
       if (is_term(b)) break;
