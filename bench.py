@@ -445,6 +445,91 @@ def run_merge_bench(args, world, rank, local):
     return 0
 
 
+INGEST_METRIC = "host ingest: decompressed FASTQ GB/s of the BGZF reader (parallel inflate)"
+
+
+def _bgzf_bytes(data: bytes, block: int = 65280, level: int = 1) -> bytes:
+    """BGZF members (gzip with the BC extra subfield) of 65,280-byte blocks."""
+    import struct
+    import zlib
+    out = []
+    for o in range(0, len(data), block):
+        piece = data[o:o + block]
+        co = zlib.compressobj(level, zlib.DEFLATED, -15)
+        comp = co.compress(piece) + co.flush()
+        head = struct.pack("<BBBBIBBHBBHH", 0x1F, 0x8B, 8, 4, 0, 0, 0xFF, 6, 0x42, 0x43, 2, 18 + len(comp) + 7)
+        out.append(head + comp + struct.pack("<II", zlib.crc32(piece) & 0xFFFFFFFF, len(piece)))
+    return b"".join(out)
+
+
+def run_ingest_bench(args, world, rank, local):
+    """Host ingest (the reader that feeds pinned buffers): decompressed GB/s of
+    the BGZF reader at 1..N inflate threads against the serial gzip reader on
+    the same reads, and the `kite count` command line end to end (file to
+    .kite) on gzip and BGZF copies of the same FASTQ."""
+    import gzip as gz
+    from kite_gb300 import CLI, host
+    if rank != 0:
+        return 0
+    n_reads = min(args.reads, 2_000_000)
+    data = bytes(gen_workload(n_reads, seed=2))
+    tmp = Path(tempfile.mkdtemp(prefix="kite_ingest_"))
+    plain, gzf, bgzf = tmp / "r.fq", tmp / "r.fq.gz", tmp / "r.bgzf.fq.gz"
+    plain.write_bytes(data)
+    with gz.open(gzf, "wb", compresslevel=1) as f:
+        f.write(data)
+    bgzf.write_bytes(_bgzf_bytes(data))
+    chunk = 64 << 20
+    cores = os.cpu_count() or 1
+
+    def reader_gbs(path, threads):
+        best = 0.0
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            n = sum(len(c) for c in host.read_chunks(path, chunk, threads))
+            best = max(best, n / (time.perf_counter() - t0) / 1e9)
+            assert n == len(data)
+        return best
+
+    gz_gbs = reader_gbs(gzf, 1)
+    plain_gbs = reader_gbs(plain, 1)
+    per_threads = {t: reader_gbs(bgzf, t) for t in sorted({1, 2, 4, 8, max(1, cores // 2), cores})}
+    best_t = max(per_threads, key=per_threads.get)
+
+    def cli_count(path):
+        out = tmp / "o.kite"
+        t0 = time.perf_counter()
+        r = subprocess.run([str(CLI), "count", "-i", str(path), "-o", str(out), "-k", "31", "--canonical", "true",
+                            "--partitions", str(PARTITIONS), "--memory", "64G", "--device", str(local)],
+                           capture_output=True, text=True)
+        dt = time.perf_counter() - t0
+        if r.returncode != 0:
+            raise RuntimeError(r.stderr[-2000:])
+        kmers = int(r.stderr.split("kmers=")[1].split()[0])
+        return kmers / dt, dt
+    cli = {name: cli_count(p) for name, p in (("gzip", gzf), ("bgzf", bgzf), ("plain", plain))}
+    line = {"metric": INGEST_METRIC, "value": per_threads[best_t], "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": 0, "ms_per_step": len(data) / per_threads[best_t] / 1e6,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"{n_reads:,} reads of the 10M-read workload's shape ({len(data) / 1e9:.2f} GB "
+                                   "FASTQ) as plain, gzip (level 1) and BGZF (65,280-byte blocks, level 1); "
+                                   "64 MiB chunks", "host_cores": cores, "best_threads": best_t,
+                       "parallelism": "host threads"},
+            "bgzf_gbs_by_threads": {str(k): round(v, 3) for k, v in per_threads.items()},
+            "gzip_serial_gbs": round(gz_gbs, 3), "plain_gbs": round(plain_gbs, 3),
+            "cli_count_kmers_per_s": {k: v[0] for k, v in cli.items()},
+            "cli_count_seconds": {k: round(v[1], 3) for k, v in cli.items()},
+            "cpu_baseline": {"value": gz_gbs, "unit": "GB/s", "cores": 1, "kind": "port",
+                             "sample": "the serial gzip reader (zlib gzread) on the same reads"}}
+    print(json.dumps(line))
+    for p in (plain, gzf, bgzf, tmp / "o.kite"):
+        if p.exists():
+            p.unlink()
+    tmp.rmdir()
+    return 0
+
+
 DUMP_METRIC = "dump TSV lines/s (kite dump -o - of the 10M-read k=31 count)"
 
 
@@ -558,7 +643,8 @@ def main():
     ap.add_argument("--partitions", type=int, default=PARTITIONS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-splitter-compare", action="store_true")
-    ap.add_argument("--workload", default="repeats", choices=["repeats", "skewed", "merge", "batch", "dump"])
+    ap.add_argument("--workload", default="repeats",
+                    choices=["repeats", "skewed", "merge", "batch", "dump", "ingest"])
     ap.add_argument("--batch-scale", type=float, default=0.25, help="read-count scale of the batch samples")
     ap.add_argument("--autotune-out", default=None, help="write the batch autotuner's table here (JSON)")
     ap.add_argument("--merge-scale", type=float, default=1.0, help="read-count scale of the merge databases")
@@ -578,6 +664,8 @@ def main():
         return run_merge_bench(args, world, rank, local)
     if args.workload == "dump":
         return run_dump_bench(args, world, rank, local)
+    if args.workload == "ingest":
+        return run_ingest_bench(args, world, rank, local)
     if args.workload == "batch":
         return run_batch_bench(args, world, rank, local)
 

@@ -18,6 +18,7 @@ EXPORTED = [
     "kite_reader_open", "kite_reader_open_image", "kite_reader_close", "kite_reader_header",
     "kite_reader_merge_input", "kite_dump_partition", "kite_detect_compression", "kite_input_open",
     "kite_input_next", "kite_input_max_chunk", "kite_input_close", "kite_sample_avg_read_len", "kite_synth_reads",
+    "kite_input_set_threads",
 ]
 
 
@@ -153,6 +154,38 @@ class Writer:
             self.close()
         except Exception:
             pass
+
+
+def read_chunks(path: str, chunk_size: int, threads: int = 0) -> list:
+    """The FASTQ chunks the host reader produces for a file (plain, gzip or
+    BGZF), in order."""
+    L = lib()
+    L.kite_input_open.restype = C.c_void_p
+    L.kite_input_open.argtypes = [C.c_char_p, C.c_uint64]
+    L.kite_input_next.restype = C.c_int64
+    L.kite_input_next.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+    L.kite_input_max_chunk.restype = C.c_uint64
+    L.kite_input_max_chunk.argtypes = [C.c_void_p]
+    L.kite_input_set_threads.argtypes = [C.c_void_p, C.c_uint]
+    L.kite_input_close.argtypes = [C.c_void_p]
+    h = L.kite_input_open(str(path).encode(), chunk_size)
+    if not h:
+        raise RuntimeError(err())
+    try:
+        if threads:
+            L.kite_input_set_threads(h, threads)
+        cap = L.kite_input_max_chunk(h) + 64
+        buf = C.create_string_buffer(cap)
+        out = []
+        while True:
+            n = L.kite_input_next(h, buf, cap)
+            if n < 0:
+                raise RuntimeError(err())
+            if n == 0:
+                return out
+            out.append(C.string_at(buf, n))
+    finally:
+        L.kite_input_close(h)
 
 
 def dump_image(image: bytes) -> bytes:

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cerrno>
+#include <deque>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -737,6 +738,117 @@ int kite_detect_compression(const char* path) {
 
 }  // extern "C"
 
+// ---------------------------------------------------------------------------
+// BGZF (decompress_bgzf_parallel src/count/bgzf.rs:149-258): block headers
+// scanned (scan_bgzf_blocks :54-85), batches of 8192 blocks inflated on a
+// thread pool, output appended block by block in file order and cut by
+// find_fastq_split_near (:124-135) whenever at least a chunk is held.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kBgzfBatch = 8192;
+
+size_t split_4lines(const uint8_t* d, size_t n) {
+  size_t nl = 0, last = 0;
+  for (size_t i = 0; i < n; ++i)
+    if (d[i] == '\n' && (++nl & 3) == 0) last = i + 1;
+  return last;
+}
+
+size_t split_near(const uint8_t* d, size_t n, size_t target) {
+  const size_t b = split_4lines(d, std::min(target + 8192, n));
+  return b > 0 ? b : split_4lines(d, n);
+}
+
+// Block (offset, size) pairs; false with the reference's message on data
+// that is not a BGZF block.  A truncated final block is skipped.
+bool scan_bgzf(const uint8_t* d, size_t n, std::vector<std::pair<size_t, size_t>>& blocks, std::string& err) {
+  size_t pos = 0;
+  while (pos + 18 <= n) {
+    const uint8_t* h = d + pos;
+    if (!(h[0] == 0x1f && h[1] == 0x8b && (h[3] & 0x04) && h[12] == 0x42 && h[13] == 0x43 && h[14] == 0x02 &&
+          h[15] == 0x00)) {
+      err = "Non-BGZF data at offset " + std::to_string(pos) + " (expected gzip+BGZF header)";
+      return false;
+    }
+    const size_t bsize = ((size_t)h[16] | ((size_t)h[17] << 8)) + 1;
+    if (pos + bsize > n) break;
+    blocks.push_back({pos, bsize});
+    pos += bsize;
+  }
+  return true;
+}
+
+// One gzip member into out; on a decode error the bytes decoded so far stay.
+bool inflate_member(const uint8_t* raw, size_t n, std::vector<uint8_t>& out) {
+  out.clear();
+#if KITE_HAVE_ZLIB
+  z_stream zs{};
+  if (inflateInit2(&zs, 15 + 16) != Z_OK) return false;
+  zs.next_in = const_cast<uint8_t*>(raw);
+  zs.avail_in = (uInt)n;
+  int r = Z_OK;
+  while (r == Z_OK) {
+    const size_t have = out.size();
+    out.resize(have + 65536);
+    zs.next_out = out.data() + have;
+    zs.avail_out = 65536;
+    r = inflate(&zs, Z_NO_FLUSH);
+    out.resize(have + (65536 - zs.avail_out));
+    if (r == Z_BUF_ERROR && zs.avail_in == 0) break;
+  }
+  inflateEnd(&zs);
+  return r == Z_STREAM_END;
+#else
+  (void)raw;
+  (void)n;
+  return false;
+#endif
+}
+
+// Mapped (or read) bytes of a whole file.
+struct FileBytes {
+  const uint8_t* p = nullptr;
+  size_t n = 0;
+  void* map = nullptr;
+  std::vector<uint8_t> copy;
+  bool open(const char* path) {
+    const int fd = ::open(path, O_RDONLY);
+    if (fd < 0) return false;
+    struct stat st {};
+    if (fstat(fd, &st) != 0) {
+      ::close(fd);
+      return false;
+    }
+    n = (size_t)st.st_size;
+    if (n) {
+      map = mmap(nullptr, n, PROT_READ, MAP_PRIVATE, fd, 0);
+      if (map == MAP_FAILED) {
+        map = nullptr;
+        copy.resize(n);
+        size_t got = 0;
+        while (got < n) {
+          const ssize_t r = ::read(fd, copy.data() + got, n - got);
+          if (r <= 0) break;
+          got += (size_t)r;
+        }
+        copy.resize(got);
+        n = got;
+        p = copy.data();
+      } else {
+        p = static_cast<const uint8_t*>(map);
+      }
+    }
+    ::close(fd);
+    return true;
+  }
+  ~FileBytes() {
+    if (map) munmap(map, n);
+  }
+};
+
+}  // namespace
+
 struct kite_input {
   FILE* f = nullptr;
 #if KITE_HAVE_ZLIB
@@ -745,6 +857,48 @@ struct kite_input {
   uint64_t chunk = 0;
   std::vector<uint8_t> carry;
   bool eof = false;
+  // BGZF
+  bool bgzf = false;
+  FileBytes file;
+  std::vector<std::pair<size_t, size_t>> blocks;
+  size_t next_block = 0;
+  unsigned threads = 1;
+  std::deque<std::vector<uint8_t>> ready;
+  std::string bgzf_err;
+  // Inflates the next batch of blocks in parallel and cuts what it can into
+  // ready chunks; after the last block, the rest of the carry is a chunk.
+  void bgzf_fill() {
+    const size_t nb = std::min(kBgzfBatch, blocks.size() - next_block);
+    if (nb == 0) {
+      if (!carry.empty()) ready.push_back(std::move(carry));
+      carry.clear();
+      eof = true;
+      return;
+    }
+    std::vector<std::vector<uint8_t>> outs(nb);
+    std::atomic<size_t> idx{0};
+    auto work = [&]() {
+      for (size_t i; (i = idx.fetch_add(1)) < nb;) {
+        const auto& b = blocks[next_block + i];
+        inflate_member(file.p + b.first, b.second, outs[i]);
+      }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < threads; ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    next_block += nb;
+    for (auto& o : outs) {
+      if (o.empty()) continue;
+      carry.insert(carry.end(), o.begin(), o.end());
+      while (carry.size() >= chunk) {
+        const size_t split = split_near(carry.data(), carry.size(), chunk);
+        if (split == 0) break;
+        ready.emplace_back(carry.begin(), carry.begin() + split);
+        carry.erase(carry.begin(), carry.begin() + split);
+      }
+    }
+  }
   size_t read_raw(uint8_t* dst, size_t want) {
     size_t total = 0;
 #if KITE_HAVE_ZLIB
@@ -779,6 +933,25 @@ kite_input* kite_input_open(const char* path, uint64_t chunk_size) {
   if (comp < 0) return nullptr;
   auto* in = new kite_input();
   in->chunk = chunk_size;
+  if (comp == KITE_INPUT_BGZF) {
+#if KITE_HAVE_ZLIB
+    if (!in->file.open(path)) {
+      set_err(std::string("failed to open input FASTQ.\nInput: ") + path);
+      delete in;
+      return nullptr;
+    }
+    in->bgzf = true;
+    in->threads = std::max(1u, std::thread::hardware_concurrency() / 2);
+    // a scan error is reported by the first read, as the reference's reader
+    // thread reports it, and no chunk follows
+    if (!scan_bgzf(in->file.p, in->file.n, in->blocks, in->bgzf_err)) in->blocks.clear();
+    return in;
+#else
+    set_err("gzip input needs zlib, which this build lacks");
+    delete in;
+    return nullptr;
+#endif
+  }
   if (comp == KITE_INPUT_PLAIN) {
     in->f = fopen(path, "rb");
     if (!in->f) {
@@ -805,11 +978,36 @@ kite_input* kite_input_open(const char* path, uint64_t chunk_size) {
   return in;
 }
 
-uint64_t kite_input_max_chunk(const kite_input* in) { return in->chunk + in->chunk; }
+uint64_t kite_input_max_chunk(const kite_input* in) {
+  // BGZF chunks may exceed the target by one block (64 KiB) and the cut window
+  return in->chunk + std::max<uint64_t>(in->chunk, 1u << 17);
+}
+
+int kite_input_set_threads(kite_input* in, unsigned threads) {
+  if (!in) return -1;
+  in->threads = std::max(1u, threads);
+  return 0;
+}
 
 // next_chunk: carry + chunk_size new bytes; on a full read cut after the last
 // 4k-th newline and carry the rest (src/count/decompress.rs:36-81).
 int64_t kite_input_next(kite_input* in, uint8_t* dst, size_t cap) {
+  if (in->bgzf) {
+    if (!in->bgzf_err.empty()) {
+      fprintf(stderr, "[kite count] bgzf_decompress_error: %s\n", in->bgzf_err.c_str());
+      in->bgzf_err.clear();
+      in->eof = true;
+      return 0;
+    }
+    while (in->ready.empty() && !in->eof) in->bgzf_fill();
+    if (in->ready.empty()) return 0;
+    std::vector<uint8_t>& c = in->ready.front();
+    if (c.size() > cap) return set_err("input buffer too small");
+    memcpy(dst, c.data(), c.size());
+    const int64_t n = (int64_t)c.size();
+    in->ready.pop_front();
+    return n;
+  }
   const size_t c = in->carry.size();
   if (cap < c + in->chunk) return set_err("input buffer too small");
   if (c) memcpy(dst, in->carry.data(), c);
@@ -846,37 +1044,61 @@ void kite_input_close(kite_input* in) {
 // sample_input src/count/mod.rs:1018-1079 (plain/gzip): 8 MiB chunks until
 // >= 200,000 reads or >= 32 MiB decompressed; mean sequence-line length.
 double kite_sample_avg_read_len(const char* path, int comp) {
-  (void)comp;
-  kite_input* in = kite_input_open(path, 8 * MiB);
-  if (!in) return 150.0;
-  std::vector<uint8_t> buf(16 * MiB + 64);
   uint64_t reads = 0, bases = 0, decomp = 0;
-  while (reads < 200000 && decomp < 32 * MiB) {
-    int64_t n = kite_input_next(in, buf.data(), buf.size());
-    if (n <= 0) break;
-    decomp += (uint64_t)n;
-    if (buf[0] != '@') continue;
+  auto count_seqs = [&](const uint8_t* buf, size_t n) {
+    if (n == 0 || buf[0] != '@') return;
     int state = 0;
     size_t seq_start = 0;
-    for (int64_t i = 0; i < n; ++i) {
+    for (size_t i = 0; i < n; ++i) {
       if (buf[i] != '\n') continue;
       if (state == 0) {
         state = 1;
-        seq_start = (size_t)i + 1;
+        seq_start = i + 1;
       } else if (state == 1) {
-        if ((size_t)i > seq_start) {
+        if (i > seq_start) {
           reads++;
-          bases += (size_t)i - seq_start;
+          bases += i - seq_start;
         }
         state = 2;
       } else {
         state = state == 2 ? 3 : 0;
       }
     }
-    if (state == 1 && seq_start < (size_t)n) {
+    if (state == 1 && seq_start < n) {
       reads++;
-      bases += (size_t)n - seq_start;
+      bases += n - seq_start;
     }
+  };
+  if (comp == KITE_INPUT_BGZF) {
+    // sample_bgzf_input src/count/mod.rs:1081-1123: block by block, complete
+    // records only, until 200,000 reads or 32 MiB decompressed
+    FileBytes fb;
+    if (!fb.open(path)) return 150.0;
+    std::vector<std::pair<size_t, size_t>> blocks;
+    std::string err;
+    if (!scan_bgzf(fb.p, fb.n, blocks, err)) return 150.0;
+    std::vector<uint8_t> carry, out;
+    for (const auto& b : blocks) {
+      if (!inflate_member(fb.p + b.first, b.second, out)) break;
+      decomp += out.size();
+      carry.insert(carry.end(), out.begin(), out.end());
+      const size_t split = split_4lines(carry.data(), carry.size());
+      if (split > 0) {
+        count_seqs(carry.data(), split);
+        carry.erase(carry.begin(), carry.begin() + split);
+      }
+      if (reads >= 200000 || decomp >= 32 * MiB) break;
+    }
+    return reads == 0 ? 150.0 : (double)bases / (double)reads;
+  }
+  kite_input* in = kite_input_open(path, 8 * MiB);
+  if (!in) return 150.0;
+  std::vector<uint8_t> buf(16 * MiB + 64);
+  while (reads < 200000 && decomp < 32 * MiB) {
+    int64_t n = kite_input_next(in, buf.data(), buf.size());
+    if (n <= 0) break;
+    decomp += (uint64_t)n;
+    count_seqs(buf.data(), (size_t)n);
   }
   kite_input_close(in);
   return reads ? (double)bases / (double)reads : 150.0;

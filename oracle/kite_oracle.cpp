@@ -239,10 +239,119 @@ struct ChunkedReader {
 static ByteSource* open_source(const std::string& path, Compression c) {
   if (c == PLAIN) return new FileSource(path);
 #if ORC_HAVE_ZLIB
-  return new GzSource(path);  // gzread continues across gzip members (BGZF too)
+  return new GzSource(path);  // gzread continues across gzip members
 #else
   throw Error("gzip input needs zlib, which this build lacks");
 #endif
+}
+
+// ---------------------------------------------------------------------------
+// BGZF input:
+//   is_bgzf_header / scan_bgzf_blocks  src/count/bgzf.rs:37-85
+//   find_fastq_split_near              src/count/bgzf.rs:124-135
+//   decompress_bgzf_parallel           src/count/bgzf.rs:149-258: blocks
+//     inflated one by one here; the reference's batches and thread pool do
+//     not move a chunk boundary, since it appends block by block and cuts
+//     after every block
+//   sample_bgzf_input                  src/count/mod.rs:1081-1123
+// ---------------------------------------------------------------------------
+static std::vector<uint8_t> read_whole_file(const std::string& path) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) throw Error("failed to open input FASTQ.\nInput: " + path);
+  std::vector<uint8_t> d;
+  uint8_t buf[1 << 16];
+  size_t r;
+  while ((r = fread(buf, 1, sizeof buf, f)) > 0) d.insert(d.end(), buf, buf + r);
+  fclose(f);
+  return d;
+}
+
+static std::vector<std::pair<size_t, size_t>> scan_bgzf_blocks(const std::vector<uint8_t>& d) {
+  std::vector<std::pair<size_t, size_t>> blocks;
+  size_t pos = 0;
+  while (pos + 18 <= d.size()) {
+    const uint8_t* h = d.data() + pos;
+    const bool hdr = h[0] == 0x1f && h[1] == 0x8b && (h[3] & 0x04) && h[12] == 0x42 && h[13] == 0x43 &&
+                     h[14] == 0x02 && h[15] == 0x00;
+    if (!hdr) throw Error("Non-BGZF data at offset " + std::to_string(pos) + " (expected gzip+BGZF header)");
+    const size_t bsize = ((size_t)h[16] | ((size_t)h[17] << 8)) + 1;
+    if (pos + bsize > d.size()) break;  // truncated final block: skipped
+    blocks.push_back({pos, bsize});
+    pos += bsize;
+  }
+  return blocks;
+}
+
+// One gzip member; on a decode error the bytes decoded so far are kept (the
+// reference ignores read_to_end's error in the count path).  Returns false
+// on that error.
+static bool inflate_member(const uint8_t* raw, size_t n, std::vector<uint8_t>& out) {
+  out.clear();
+#if ORC_HAVE_ZLIB
+  z_stream zs{};
+  if (inflateInit2(&zs, 15 + 16) != Z_OK) return false;
+  zs.next_in = const_cast<uint8_t*>(raw);
+  zs.avail_in = (uInt)n;
+  uint8_t buf[1 << 16];
+  int r = Z_OK;
+  while (r == Z_OK) {
+    zs.next_out = buf;
+    zs.avail_out = sizeof buf;
+    r = inflate(&zs, Z_NO_FLUSH);
+    out.insert(out.end(), buf, buf + (sizeof buf - zs.avail_out));
+    if (r == Z_BUF_ERROR && zs.avail_in == 0) break;
+  }
+  inflateEnd(&zs);
+  return r == Z_STREAM_END;
+#else
+  (void)raw;
+  (void)n;
+  throw Error("gzip input needs zlib, which this build lacks");
+#endif
+}
+
+static size_t find_fastq_split_near(const uint8_t* d, size_t n, size_t target) {
+  const size_t scan_end = std::min(target + 8192, n);
+  const size_t b = find_fastq_split_4lines(d, scan_end);
+  return b > 0 ? b : find_fastq_split_4lines(d, n);
+}
+
+// Chunks of a BGZF file; a scan error is reported like the reference's
+// reader thread and yields no chunks.
+static void bgzf_chunks(const std::string& path, size_t target, std::vector<std::vector<uint8_t>>& chunks) {
+  const std::vector<uint8_t> d = read_whole_file(path);
+  std::vector<std::pair<size_t, size_t>> blocks;
+  try {
+    blocks = scan_bgzf_blocks(d);
+  } catch (const Error& e) {
+    fprintf(stderr, "[kite count] bgzf_decompress_error: %s\n", e.what());
+    return;
+  }
+  std::vector<uint8_t> carry, out;
+  for (auto& b : blocks) {
+    inflate_member(d.data() + b.first, b.second, out);
+    if (out.empty()) continue;
+    carry.insert(carry.end(), out.begin(), out.end());
+    while (carry.size() >= target) {
+      const size_t split = find_fastq_split_near(carry.data(), carry.size(), target);
+      if (split == 0) break;
+      chunks.emplace_back(carry.begin(), carry.begin() + split);
+      carry.erase(carry.begin(), carry.begin() + split);
+    }
+  }
+  if (!carry.empty()) chunks.push_back(carry);
+}
+
+static void read_all_chunks(const std::string& path, Compression c, size_t chunk_size,
+                            std::vector<std::vector<uint8_t>>& store) {
+  if (c == BGZF) {
+    bgzf_chunks(path, chunk_size, store);
+    return;
+  }
+  std::unique_ptr<ByteSource> src(open_source(path, c));
+  ChunkedReader rd(src.get(), chunk_size);
+  std::vector<uint8_t> chunk;
+  while (rd.next_chunk(chunk)) store.push_back(chunk);
 }
 
 // ---------------------------------------------------------------------------
@@ -316,6 +425,26 @@ static double sample_avg_read_len(const std::string& path, Compression c) {
   // sample_input: 8 MiB chunks until >= 200k reads or >= 32 MiB decompressed.
   uint64_t reads = 0, bases = 0;
   size_t decomp = 0;
+  if (c == BGZF) {
+    // sample_bgzf_input: block by block, complete records only; errors propagate
+    const std::vector<uint8_t> d = read_whole_file(path);
+    std::vector<uint8_t> carry, out;
+    for (auto& b : scan_bgzf_blocks(d)) {
+      if (!inflate_member(d.data() + b.first, b.second, out)) throw Error("invalid gzip data in a BGZF block");
+      decomp += out.size();
+      carry.insert(carry.end(), out.begin(), out.end());
+      const size_t split = find_fastq_split_4lines(carry.data(), carry.size());
+      if (split > 0) {
+        parse_sequences(carry.data(), split, [&](const uint8_t*, size_t n) {
+          reads++;
+          bases += n;
+        });
+        carry.erase(carry.begin(), carry.begin() + split);
+      }
+      if (reads >= 200000 || decomp >= 32 * MIB) break;
+    }
+    return reads == 0 ? 150.0 : (double)bases / (double)reads;
+  }
   std::unique_ptr<ByteSource> src(open_source(path, c));
   ChunkedReader rd(src.get(), 8 * MIB);
   std::vector<uint8_t> chunk;
@@ -1244,6 +1373,30 @@ long long orc_parse_sequences(const uint8_t* d, size_t n, uint64_t* starts, uint
 
 size_t orc_find_fastq_split(const uint8_t* d, size_t n) { return find_fastq_split_4lines(d, n); }
 
+// Chunk lengths the reference's reader produces for a file (plain, gzip or
+// BGZF): the number of chunks, up to cap lengths written; -1 on error.
+int64_t orc_read_chunks(const char* path, size_t chunk_size, uint64_t* lens, size_t cap) {
+  try {
+    std::vector<std::vector<uint8_t>> store;
+    read_all_chunks(path, detect_compression(path), chunk_size, store);
+    for (size_t i = 0; i < store.size() && i < cap; ++i) lens[i] = store[i].size();
+    return (int64_t)store.size();
+  } catch (const Error& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
+// sample_input's mean read length for a file; < 0 on error.
+double orc_sample_avg_read_len(const char* path) {
+  try {
+    return sample_avg_read_len(path, detect_compression(path));
+  } catch (const Error& e) {
+    g_err = e.what();
+    return -1.0;
+  }
+}
+
 // k-mers of one sequence; keys as (lo, hi) u64 pairs.  wide=1 uses the u128
 // iterator (k <= 64), else the u64 iterator (k <= 32).
 size_t orc_kmers(const uint8_t* s, size_t n, unsigned k, int canonical, int wide, uint64_t* out, size_t cap) {
@@ -1565,11 +1718,8 @@ static int cmd_count(int argc, char** argv) {
   size_t lanes = std::min<size_t>(std::max<size_t>((workers + 7) / 8, 2), 6);
   Writer w(h, plan.staging_bytes, lanes);
   auto t0 = std::chrono::steady_clock::now();
-  std::unique_ptr<ByteSource> src(open_source(in, comp));
-  ChunkedReader rd(src.get(), plan.chunk_size_bytes);
   std::vector<std::vector<uint8_t>> store;
-  std::vector<uint8_t> chunk;
-  while (rd.next_chunk(chunk)) store.push_back(chunk);
+  read_all_chunks(in, comp, plan.chunk_size_bytes, store);
   std::vector<std::pair<const uint8_t*, size_t>> chunks;
   for (auto& c : store) chunks.push_back({c.data(), c.size()});
   CountStats st;

@@ -22,6 +22,7 @@ def run(args, check=True):
 
 @pytest.fixture(scope="module")
 def fastq(tmp_path_factory, built):
+    from test_bgzf import write_bgzf
     d = tmp_path_factory.mktemp("cli")
     fq = synth.small_workload(seed=21, n_reads=8000, genome_len=60_000)
     plain = d / "reads.fq"
@@ -29,7 +30,9 @@ def fastq(tmp_path_factory, built):
     gz = d / "reads.fq.gz"
     with gzip.open(gz, "wb", compresslevel=1) as f:
         f.write(fq)
-    return d, plain, gz
+    bgzf = d / "reads.bgzf.fq.gz"
+    write_bgzf(bgzf, fq, 30_000)
+    return d, plain, gz, bgzf
 
 
 @pytest.mark.gpu
@@ -39,10 +42,10 @@ def fastq(tmp_path_factory, built):
     ["-k", "31", "--canonical", "true", "--partitions", "64", "--buffer", "1"],
     ["-k", "55", "--canonical", "true", "--partitions", "32"],
 ])
-@pytest.mark.parametrize("which", ["plain", "gz"])
+@pytest.mark.parametrize("which", ["plain", "gz", "bgzf"])
 def test_count_matches_oracle(gpu, orc, fastq, args, which):
-    d, plain, gz = fastq
-    src = plain if which == "plain" else gz
+    d, plain, gz, bgzf = fastq
+    src = {"plain": plain, "gz": gz, "bgzf": bgzf}[which]
     out = d / f"gpu_{which}_{'_'.join(args).replace('-', '')}.kite"
     ref = d / f"ref_{which}_{'_'.join(args).replace('-', '')}.kite"
     common = ["-i", src, "--memory", "64G", "-t", "3", *args]
@@ -81,13 +84,13 @@ def test_merge_matches_oracle(gpu, orc, tmp_path):
     (["-k", "21", "--mode", "compact"], "zstd"),
 ])
 def test_count_argument_errors(built, fastq, args, msg):
-    d, plain, _ = fastq
+    d, plain, _, _ = fastq
     r = run([CLI, "count", "-i", plain, "-o", d / "x.kite", *args], check=False)
     assert r.returncode != 0 and msg.encode() in r.stderr
 
 
 def test_count_output_name_error(built, fastq):
-    d, plain, _ = fastq
+    d, plain, _, _ = fastq
     r = run([CLI, "count", "-i", plain, "-o", d / "x.bin"], check=False)
     assert r.returncode != 0 and b"output must end with .kite" in r.stderr
 
