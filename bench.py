@@ -486,7 +486,7 @@ def run_ingest_bench(args, world, rank, local):
         best = 0.0
         for _ in range(max(1, args.steps)):
             t0 = time.perf_counter()
-            n = sum(len(c) for c in host.read_chunks(path, chunk, threads))
+            n = sum(host.read_chunks(path, chunk, threads, collect=False))
             best = max(best, n / (time.perf_counter() - t0) / 1e9)
             assert n == len(data)
         return best

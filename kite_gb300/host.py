@@ -156,9 +156,10 @@ class Writer:
             pass
 
 
-def read_chunks(path: str, chunk_size: int, threads: int = 0) -> list:
+def read_chunks(path: str, chunk_size: int, threads: int = 0, collect: bool = True) -> list:
     """The FASTQ chunks the host reader produces for a file (plain, gzip or
-    BGZF), in order."""
+    BGZF), in order; with collect False, only their lengths (the reader
+    still writes every chunk into a buffer, as it fills a pinned one)."""
     L = lib()
     L.kite_input_open.restype = C.c_void_p
     L.kite_input_open.argtypes = [C.c_char_p, C.c_uint64]
@@ -183,7 +184,7 @@ def read_chunks(path: str, chunk_size: int, threads: int = 0) -> list:
                 raise RuntimeError(err())
             if n == 0:
                 return out
-            out.append(C.string_at(buf, n))
+            out.append(C.string_at(buf, n) if collect else n)
     finally:
         L.kite_input_close(h)
 

@@ -748,10 +748,17 @@ namespace {
 
 constexpr size_t kBgzfBatch = 8192;
 
+// Byte after the last 4k-th newline of d[0, n) (0 if none): find_fastq_split_4lines.
 size_t split_4lines(const uint8_t* d, size_t n) {
   size_t nl = 0, last = 0;
-  for (size_t i = 0; i < n; ++i)
-    if (d[i] == '\n' && (++nl & 3) == 0) last = i + 1;
+  const uint8_t* p = d;
+  const uint8_t* e = d + n;
+  while (p < e) {
+    const void* q = memchr(p, '\n', (size_t)(e - p));
+    if (!q) break;
+    p = static_cast<const uint8_t*>(q) + 1;
+    if ((++nl & 3) == 0) last = (size_t)(p - d);
+  }
   return last;
 }
 
@@ -777,6 +784,30 @@ bool scan_bgzf(const uint8_t* d, size_t n, std::vector<std::pair<size_t, size_t>
     pos += bsize;
   }
   return true;
+}
+
+// One gzip member into dst[0, cap): the bytes written, or ~0 when the member
+// does not end exactly at cap bytes of output (a decode error, or an output
+// size other than cap).
+size_t inflate_member_into(const uint8_t* raw, size_t n, uint8_t* dst, size_t cap) {
+#if KITE_HAVE_ZLIB
+  z_stream zs{};
+  if (inflateInit2(&zs, 15 + 16) != Z_OK) return ~(size_t)0;
+  zs.next_in = const_cast<uint8_t*>(raw);
+  zs.avail_in = (uInt)n;
+  zs.next_out = dst;
+  zs.avail_out = (uInt)cap;
+  const int r = inflate(&zs, Z_FINISH);
+  const size_t got = cap - zs.avail_out;
+  inflateEnd(&zs);
+  return r == Z_STREAM_END && got == cap ? got : ~(size_t)0;
+#else
+  (void)raw;
+  (void)n;
+  (void)dst;
+  (void)cap;
+  return ~(size_t)0;
+#endif
 }
 
 // One gzip member into out; on a decode error the bytes decoded so far stay.
@@ -857,47 +888,85 @@ struct kite_input {
   uint64_t chunk = 0;
   std::vector<uint8_t> carry;
   bool eof = false;
-  // BGZF
+  // BGZF: decompressed bytes of the current batch (after the uncut rest of
+  // the previous one) in asm_buf, cut into chunks (offset, length)
   bool bgzf = false;
   FileBytes file;
   std::vector<std::pair<size_t, size_t>> blocks;
   size_t next_block = 0;
   unsigned threads = 1;
-  std::deque<std::vector<uint8_t>> ready;
+  std::vector<uint8_t> asm_buf;
+  size_t asm_len = 0;   // valid bytes in asm_buf
+  size_t asm_pos = 0;   // start of the uncut bytes
+  std::deque<std::pair<size_t, size_t>> ready;
   std::string bgzf_err;
-  // Inflates the next batch of blocks in parallel and cuts what it can into
-  // ready chunks; after the last block, the rest of the carry is a chunk.
+  // Inflates the next batch of blocks and cuts what it can into ready chunks,
+  // as the reference does after every appended block; after the last block
+  // the uncut rest is a chunk.  Each block inflates straight to its place
+  // (its gzip ISIZE field gives its output size); a batch where a block does
+  // not decode to exactly that size is assembled again block by block.
   void bgzf_fill() {
+    if (asm_pos) {
+      memmove(asm_buf.data(), asm_buf.data() + asm_pos, asm_len - asm_pos);
+      asm_len -= asm_pos;
+      asm_pos = 0;
+    }
     const size_t nb = std::min(kBgzfBatch, blocks.size() - next_block);
     if (nb == 0) {
-      if (!carry.empty()) ready.push_back(std::move(carry));
-      carry.clear();
+      if (asm_len) ready.push_back({0, asm_len});
+      asm_pos = asm_len;
       eof = true;
       return;
     }
-    std::vector<std::vector<uint8_t>> outs(nb);
+    std::vector<size_t> off(nb + 1);
+    off[0] = asm_len;
+    for (size_t i = 0; i < nb; ++i) {
+      const auto& b = blocks[next_block + i];
+      const uint8_t* t = file.p + b.first + b.second - 4;
+      size_t isize = (size_t)t[0] | ((size_t)t[1] << 8) | ((size_t)t[2] << 16) | ((size_t)t[3] << 24);
+      if (isize > 65536) isize = 65536;  // not a BGZF block size: the check below catches it
+      off[i + 1] = off[i] + isize;
+    }
+    if (asm_buf.size() < off[nb]) asm_buf.resize(off[nb]);
     std::atomic<size_t> idx{0};
+    std::atomic<bool> exact{true};
     auto work = [&]() {
       for (size_t i; (i = idx.fetch_add(1)) < nb;) {
         const auto& b = blocks[next_block + i];
-        inflate_member(file.p + b.first, b.second, outs[i]);
+        const size_t want = off[i + 1] - off[i];
+        if (inflate_member_into(file.p + b.first, b.second, asm_buf.data() + off[i], want) != want)
+          exact.store(false);
       }
     };
     std::vector<std::thread> pool;
     for (unsigned t = 1; t < threads; ++t) pool.emplace_back(work);
     work();
     for (auto& t : pool) t.join();
-    next_block += nb;
-    for (auto& o : outs) {
-      if (o.empty()) continue;
-      carry.insert(carry.end(), o.begin(), o.end());
-      while (carry.size() >= chunk) {
-        const size_t split = split_near(carry.data(), carry.size(), chunk);
-        if (split == 0) break;
-        ready.emplace_back(carry.begin(), carry.begin() + split);
-        carry.erase(carry.begin(), carry.begin() + split);
+    if (!exact.load()) {
+      // block by block: each block's actual output, partial on a decode error
+      std::vector<uint8_t> o;
+      size_t len = off[0];
+      for (size_t i = 0; i < nb; ++i) {
+        const auto& b = blocks[next_block + i];
+        inflate_member(file.p + b.first, b.second, o);
+        if (asm_buf.size() < len + o.size()) asm_buf.resize(len + o.size());
+        if (!o.empty()) memcpy(asm_buf.data() + len, o.data(), o.size());
+        len += o.size();
+        off[i + 1] = len;
       }
     }
+    next_block += nb;
+    for (size_t i = 0; i < nb; ++i) {
+      const size_t end = off[i + 1];
+      if (end == off[i]) continue;
+      while (end - asm_pos >= chunk) {
+        const size_t split = split_near(asm_buf.data() + asm_pos, end - asm_pos, chunk);
+        if (split == 0) break;
+        ready.push_back({asm_pos, split});
+        asm_pos += split;
+      }
+    }
+    asm_len = off[nb];
   }
   size_t read_raw(uint8_t* dst, size_t want) {
     size_t total = 0;
@@ -1001,12 +1070,11 @@ int64_t kite_input_next(kite_input* in, uint8_t* dst, size_t cap) {
     }
     while (in->ready.empty() && !in->eof) in->bgzf_fill();
     if (in->ready.empty()) return 0;
-    std::vector<uint8_t>& c = in->ready.front();
-    if (c.size() > cap) return set_err("input buffer too small");
-    memcpy(dst, c.data(), c.size());
-    const int64_t n = (int64_t)c.size();
+    const auto c = in->ready.front();
+    if (c.second > cap) return set_err("input buffer too small");
+    memcpy(dst, in->asm_buf.data() + c.first, c.second);
     in->ready.pop_front();
-    return n;
+    return (int64_t)c.second;
   }
   const size_t c = in->carry.size();
   if (cap < c + in->chunk) return set_err("input buffer too small");
@@ -1024,9 +1092,7 @@ int64_t kite_input_next(kite_input* in, uint8_t* dst, size_t cap) {
     in->eof = true;
     return (int64_t)len;
   }
-  size_t nl = 0, last = 0;
-  for (size_t i = 0; i < len; ++i)
-    if (dst[i] == '\n' && (++nl & 3) == 0) last = i + 1;
+  const size_t last = split_4lines(dst, len);
   if (last == 0 || last >= len) return (int64_t)len;
   in->carry.assign(dst + last, dst + len);
   return (int64_t)last;

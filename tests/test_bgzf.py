@@ -106,3 +106,21 @@ def test_plain_and_gzip_chunks_match_oracle(orc, tmp_path, reads, kind):
     got = host.read_chunks(p, 100_000)
     assert b"".join(got) == reads
     assert [len(c) for c in got] == oracle_chunk_lens(orc, p, 100_000)
+
+
+def test_block_with_wrong_isize(orc, tmp_path, reads):
+    # a block whose trailer states the wrong output size still yields its
+    # bytes (the trailer check fails after the data), as the reference's
+    # decoder keeps what it read; the batch is assembled block by block
+    raw = bytearray()
+    blocks = [bgzf_block(reads[o:o + 30_000]) for o in range(0, len(reads), 30_000)]
+    bad = bytearray(blocks[3])
+    bad[-4:] = struct.pack("<I", 1234)
+    blocks[3] = bytes(bad)
+    for b in blocks:
+        raw += b
+    p = tmp_path / "w.fq.gz"
+    p.write_bytes(bytes(raw))
+    got = host.read_chunks(p, 100_000, 4)
+    assert [len(c) for c in got] == oracle_chunk_lens(orc, p, 100_000)
+    assert b"".join(got) == reads
