@@ -20,6 +20,8 @@
  *                              (load_partition_counts, per-input filter,
  *                              merge_vectors_total, serialize_partition_chunk
  *                              src/kiteops/mod.rs:433-859)
+ *   kite_gpu_histo          <- run_histo src/histo/mod.rs:16-169 (one input)
+ *   kite_gpu_query          <- run_query src/query/mod.rs:15-96 (many keys)
  *   kite_gpu_dump           <- run_dump src/dump/mod.rs:183-520 through
  *                              stream_partition_slabs src/dump/merge.rs:282-428
  *                              (LoserTreeMerger src/dump/loser_tree.rs:141-175,
@@ -191,6 +193,24 @@ int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n,
  * call).  stats.stage_ms[0..4]: decode, tile planning, merge, formatting,
  * copy to the host. */
 int kite_gpu_dump(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, kite_gpu_emit_fn emit, void* user);
+
+/* Called once per count value with the number of keys that have it. */
+typedef int (*kite_gpu_histo_fn)(void* user, uint64_t count, uint64_t keys);
+
+/* `kite histo` of one .kite input: per partition its chunks summed by key in
+ * u64 (saturating; load_partition_counts src/kiteops/mod.rs:433-473), the
+ * header min/max applied to that sum (apply_reader_filter_to_rows :103-108),
+ * then the frequency of every count; emit is called for each count present,
+ * ascending. */
+int kite_gpu_histo(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, kite_gpu_histo_fn emit, void* user);
+
+/* `kite query` for n keys at once (already encoded, canonical where the
+ * database is: keys[2i] low and keys[2i+1] high 64 bits, high 0 for k <= 31):
+ * counts[i] = the u64 sum of key i over its partition's chunks, 0 when absent
+ * (no header filter; the caller reports it, as run_query does).  Only the
+ * partitions the keys fall in are decoded. */
+int kite_gpu_query(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, const uint64_t* keys, size_t n,
+                   uint64_t* counts);
 
 int kite_gpu_get_stats(kite_gpu_ctx* ctx, kite_gpu_stats* out);
 

@@ -1130,7 +1130,7 @@ int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n,
   cudaSetDevice(ctx->cfg.device);
   std::string msg;
   int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, inputs, n, ctx->stream, ctx->cfg.timeout_ms,
-                     false, emit, user, &msg, &ctx->stats);
+                     kMergeModeMerge, emit, user, &msg, &ctx->stats);
   if (rc) ctx->err = msg;
   return rc;
 }
@@ -1142,8 +1142,53 @@ int kite_gpu_dump(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, kite_gpu
   auto staging = [ctx](size_t bytes) -> uint8_t* {
     return ctx->h_dump.ensure(bytes) == cudaSuccess ? ctx->h_dump.as<uint8_t>() : nullptr;
   };
-  int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, input, 1, ctx->stream, ctx->cfg.timeout_ms, true, emit, user,
-                     &msg, &ctx->stats, staging);
+  int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, input, 1, ctx->stream, ctx->cfg.timeout_ms, kMergeModeDump,
+                     emit, user, &msg, &ctx->stats, staging);
+  if (rc) ctx->err = msg;
+  return rc;
+}
+
+int kite_gpu_histo(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, kite_gpu_histo_fn emit, void* user) {
+  if (!ctx || !input) return KITE_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->cfg.device);
+  std::string msg;
+  MergeExtra ex;
+  ex.histo = emit;
+  ex.user = user;
+  int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, input, 1, ctx->stream, ctx->cfg.timeout_ms, kMergeModeHisto,
+                     nullptr, nullptr, &msg, &ctx->stats, nullptr, &ex);
+  if (rc) ctx->err = msg;
+  return rc;
+}
+
+int kite_gpu_query(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, const uint64_t* keys, size_t n,
+                   uint64_t* counts) {
+  if (!ctx || !input || (n && (!keys || !counts))) return KITE_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->cfg.device);
+  const uint32_t P = ctx->cfg.partitions;
+  unsigned bits = 0;
+  while ((1u << bits) < P) ++bits;
+  // partition of every key (KmerWord::to_bucket src/count/kmer.rs:67-71,
+  // :111-116: u128 keys fold their halves first); only those are decoded
+  std::vector<uint32_t> parts(n);
+  std::vector<uint64_t> pfirst(P), pcount(P, 0);
+  for (size_t i = 0; i < n; ++i) {
+    const uint64_t x = ctx->cfg.k <= 31 ? keys[2 * i] : (keys[2 * i] ^ keys[2 * i + 1]);
+    parts[i] = bits ? (uint32_t)((x * 0x9E3779B97F4A7C15ull) >> (64 - bits)) : 0u;
+  }
+  for (uint32_t p = 0; p < P; ++p) pfirst[p] = input->part_first[p];
+  for (size_t i = 0; i < n; ++i) pcount[parts[i]] = input->part_count[parts[i]];
+  kite_gpu_merge_input sub = *input;
+  sub.part_first = pfirst.data();
+  sub.part_count = pcount.data();
+  std::string msg;
+  MergeExtra ex;
+  ex.keys = keys;
+  ex.parts = parts.data();
+  ex.nq = n;
+  ex.counts_out = counts;
+  int rc = merge_run(ctx->cfg.k, P, &sub, 1, ctx->stream, ctx->cfg.timeout_ms, kMergeModeQuery, nullptr, nullptr,
+                     &msg, &ctx->stats, nullptr, &ex);
   if (rc) ctx->err = msg;
   return rc;
 }

@@ -13,11 +13,25 @@ namespace kite {
 // Pinned host staging of at least the given bytes (nullptr if it cannot be had).
 using StagingFn = std::function<uint8_t*(size_t)>;
 
+// Modes of merge_run (the merge kernel's kModeMerge / kModeDump / kModeHisto / kModeRows).
+enum : int { kMergeModeMerge = 0, kMergeModeDump = 1, kMergeModeHisto = 2, kMergeModeQuery = 3 };
+
+// Inputs and outputs of the histo and query modes.
+struct MergeExtra {
+  kite_gpu_histo_fn histo = nullptr;  // histo: called per count in ascending order
+  void* user = nullptr;
+  const uint64_t* keys = nullptr;     // query: (lo, hi) words per key
+  const uint32_t* parts = nullptr;    // query: partition of each key
+  size_t nq = 0;
+  uint64_t* counts_out = nullptr;     // query: u64 sum per key, 0 when absent
+};
+
 // k selects the key width (u64 for k <= 31, else u128) and the splitter key
-// bits.  dump: one input, TSV lines per partition instead of DVLE chunks,
-// copied out through `staging` in groups of whole partitions.
+// bits.  Dump: one input, TSV lines per partition instead of DVLE chunks,
+// copied out through `staging` in groups of whole partitions.  Histo and
+// query: one input, results through `ex`.
 int merge_run(int k, uint32_t partitions, const kite_gpu_merge_input* inputs, int n, cudaStream_t s,
-              uint32_t timeout_ms, bool dump, kite_gpu_emit_fn emit, void* user, std::string* msg,
-              kite_gpu_stats* st, const StagingFn& staging = nullptr);
+              uint32_t timeout_ms, int mode, kite_gpu_emit_fn emit, void* user, std::string* msg,
+              kite_gpu_stats* st, const StagingFn& staging = nullptr, const MergeExtra* ex = nullptr);
 
 }  // namespace kite

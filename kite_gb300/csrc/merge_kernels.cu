@@ -52,6 +52,25 @@ constexpr int kMergeThreads = 512;
 constexpr uint32_t kMergeCap = 4096;      // rows per merge tile
 constexpr uint32_t kMaxTileStreams = 256; // streams per tile (inputs x chunks)
 constexpr int kTsvThreads = 256;          // rows per formatting round
+constexpr uint32_t kHistBins = 1024;      // histo: counts below this binned on chip, larger ones listed
+
+// What the merge kernel makes of each merged key group.
+enum MergeMode : int {
+  kModeMerge = 0,  // kite merge: per-input filter, u64 sums, u32 overflow recorded
+  kModeDump = 1,   // kite dump: sum clamped to u32, then the header filter; TSV byte counts
+  kModeHisto = 2,  // kite histo: per-input filter on the u64 sum, then count -> frequency
+  kModeRows = 3,   // kite query: every key with its u64 sum, no filter
+};
+
+// Outputs of the histo and query modes.
+struct MergeAux {
+  unsigned long long* hist;      // kHistBins frequencies (histo)
+  unsigned long long* spill;     // counts >= kHistBins, one entry per key (histo)
+  unsigned long long* spill_n;   // entries written to spill
+  unsigned long long spill_cap;
+  unsigned long long* counts64;  // u64 sum of every output row (query)
+  uint32_t line_k;               // k, for TSV line lengths (dump)
+};
 
 // Decimal digits of a count.
 __host__ __device__ __forceinline__ unsigned dec_digits(uint32_t v) {
@@ -367,19 +386,25 @@ struct MergeSmem {
   // every region starts 16-byte aligned (misc holds 8-byte scan values)
   static constexpr size_t seg = ((size_t)(kMaxTileStreams + 1) * 4 + kMaxTileStreams * 4 + 15) & ~(size_t)15;
   static constexpr size_t misc = 64 * 8;
-  static constexpr size_t total = keys + cnts + tag + perm + ((head + 15) & ~(size_t)15) + seg + misc;
+  static constexpr size_t hist = (size_t)kHistBins * 4;  // histo mode: per-CTA bins of the small counts
+  static constexpr size_t total = keys + cnts + tag + perm + ((head + 15) & ~(size_t)15) + seg + misc + hist;
 };
 
-// DUMP = false: `kite merge` (per-input filter on the per-input sum, u64
-// totals, overflow above u32 recorded).  DUMP = true: `kite dump` of one
-// input (the sum clamped to u32 first, the header filter on the clamped
-// count; rest_bytes of a tile = its TSV bytes, lines of line_k + 2 + digits).
-template <class T, bool DUMP>
+// MODE kModeMerge: `kite merge` (per-input filter on the per-input sum, u64
+// totals, overflow above u32 recorded).  kModeDump: `kite dump` of one input
+// (the sum clamped to u32 first, the header filter on the clamped count;
+// rest_bytes of a tile = its TSV bytes, lines of k + 2 + digits).
+// kModeHisto: `kite histo` of one input (load_partition_counts' u64 sum,
+// apply_reader_filter_to_rows on it, then the count's frequency; no rows
+// written).  kModeRows: `kite query` (every key with its u64 sum in
+// aux.counts64, no filter).
+template <class T, int MODE>
 __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
     const T* __restrict__ keys, const unsigned long long* __restrict__ counts, const MergeTile* __restrict__ tiles,
     const TileStream* __restrict__ ts, const InputFilter* __restrict__ filt, T* __restrict__ out_keys,
     uint32_t* __restrict__ out_counts, TileOut<T>* __restrict__ tout, unsigned long long* __restrict__ overflow,
-    DevStatus* st, uint32_t line_k) {
+    DevStatus* st, MergeAux aux) {
+  constexpr bool DUMP = MODE == kModeDump;
   using L = MergeSmem<T>;
   constexpr int NT = kMergeThreads;
   extern __shared__ __align__(16) uint8_t sm[];
@@ -392,6 +417,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
                                                  ((L::head + 15) & ~(size_t)15));
   uint32_t* sinput = sstart + kMaxTileStreams + 1;
   unsigned long long* misc = reinterpret_cast<unsigned long long*>(reinterpret_cast<uint8_t*>(sstart) + L::seg);
+  unsigned* hbin = reinterpret_cast<unsigned*>(reinterpret_cast<uint8_t*>(misc) + L::misc);
 
   const MergeTile mt = tiles[blockIdx.x];
   const uint32_t nts = mt.nts, n = mt.rows_in;
@@ -415,6 +441,8 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
     }
     sstart[nts] = a;
   }
+  if (MODE == kModeHisto)
+    for (uint32_t b = threadIdx.x; b < kHistBins; b += NT) hbin[b] = 0;
   __syncthreads();
   // load rows of every stream
   for (uint32_t i = 0; i < nts; ++i) {
@@ -491,7 +519,8 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
           if (cur_in != 0xffffffffu) {
             const InputFilter f = filt[cur_in];
             const unsigned long long eff = DUMP && part > 0xffffffffull ? 0xffffffffull : part;
-            const bool ok = !(f.has_min && eff < f.min_count) && !(f.has_max && eff > f.max_count);
+            const bool ok = MODE == kModeRows ||
+                            (!(f.has_min && eff < f.min_count) && !(f.has_max && eff > f.max_count));
             if (ok) {
               total = (total > ~0ull - part) ? ~0ull : total + part;
               present = true;
@@ -510,29 +539,40 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
     const unsigned idx = block_exclusive_scan<NT, unsigned>(present ? 1u : 0u, scan_b, &tot);
     if (present) {
       const unsigned long long o = out_base + idx;
-      if (!DUMP && total > 0xffffffffull)
-        atomicMin(overflow, ((unsigned long long)blockIdx.x << 32) | (o & 0xffffffffull));
-      const uint32_t c32 = total > 0xffffffffull ? 0xffffffffu : (uint32_t)total;
-      out_keys[mt.out_off + o] = key;
-      out_counts[mt.out_off + o] = c32;
+      if (MODE == kModeHisto) {
+        if (total < kHistBins) {
+          atomicAdd(&hbin[total], 1u);
+        } else {
+          const unsigned long long j = atomicAdd(aux.spill_n, 1ull);
+          if (j < aux.spill_cap) aux.spill[j] = total;
+        }
+      } else {
+        if (MODE == kModeMerge && total > 0xffffffffull)
+          atomicMin(overflow, ((unsigned long long)blockIdx.x << 32) | (o & 0xffffffffull));
+        const uint32_t c32 = total > 0xffffffffull ? 0xffffffffu : (uint32_t)total;
+        out_keys[mt.out_off + o] = key;
+        out_counts[mt.out_off + o] = c32;
+        if (MODE == kModeRows) aux.counts64[mt.out_off + o] = total;
+      }
     }
     __syncthreads();
     // DVLE sizes of the rows after the tile's first (the previous row may come
     // from the previous round; both are already in global memory and visible
     // to the whole CTA after the barrier).
+    if (MODE == kModeMerge || MODE == kModeDump)
     for (unsigned u = threadIdx.x; u < tot; u += NT) {
       const unsigned long long o = out_base + u;
       const T kk = out_keys[mt.out_off + o];
       const uint32_t cc = out_counts[mt.out_off + o];
       if (DUMP) {
-        rest += line_k + 2 + dec_digits(cc);
+        rest += aux.line_k + 2 + dec_digits(cc);
       } else if (o > 0) {
         const T pk = out_keys[mt.out_off + o - 1];
         rest += (unsigned long long)(varint_len((T)(kk - pk)) + varint_len((uint64_t)cc));
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0 && tot) {
+    if (MODE != kModeHisto && threadIdx.x == 0 && tot) {
       if (!have_prev) {
         first_key = out_keys[mt.out_off + out_base];
         first_count = out_counts[mt.out_off + out_base];
@@ -544,6 +584,11 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
     __syncthreads();
   }
   (void)prev_last;
+  if (MODE == kModeHisto) {
+    // the CTA's small-count bins into the global histogram
+    for (uint32_t b = threadIdx.x; b < kHistBins; b += NT)
+      if (hbin[b]) atomicAdd(&aux.hist[b], (unsigned long long)hbin[b]);
+  }
   unsigned long long rest_total;
   block_exclusive_scan<NT, unsigned long long>(rest, misc + 8, &rest_total);
   if (threadIdx.x == 0) {
@@ -604,6 +649,40 @@ __global__ void __launch_bounds__(kTsvThreads) k_tsv_tiles(const T* __restrict__
   }
 }
 
+// kite query lookups: key q of partition qp[q] in the merged rows of that
+// partition's non-empty tiles (tile_first / tile_key0 / tile_off / tile_rows,
+// first keys ascending within a partition); its u64 sum, 0 when absent.
+template <class T>
+__global__ void k_query_rows(const T* __restrict__ keys, const unsigned long long* __restrict__ counts64,
+                             const uint32_t* __restrict__ tile_first, const T* __restrict__ tile_key0,
+                             const unsigned long long* __restrict__ tile_off, const uint32_t* __restrict__ tile_rows,
+                             const T* __restrict__ qk, const uint32_t* __restrict__ qp, uint32_t nq,
+                             unsigned long long* __restrict__ out) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const T key = qk[q];
+  const uint32_t p = qp[q];
+  uint32_t lo = tile_first[p], hi = tile_first[p + 1];
+  // last tile whose first key is <= key
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (tile_key0[mid] <= key) lo = mid + 1;
+    else hi = mid;
+  }
+  unsigned long long c = 0;
+  if (lo > tile_first[p]) {
+    const uint32_t t = lo - 1;
+    unsigned long long a = tile_off[t], b = a + tile_rows[t];
+    while (a < b) {
+      const unsigned long long mid = a + (b - a) / 2;
+      if (keys[mid] < key) a = mid + 1;
+      else b = mid;
+    }
+    if (a < tile_off[t] + tile_rows[t] && keys[a] == key) c = counts64[a];
+  }
+  out[q] = c;
+}
+
 template <class T>
 struct Key128 {
   static unsigned __int128 to(T v) { return (unsigned __int128)v; }
@@ -628,8 +707,9 @@ struct Dev {
 
 template <class T>
 int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, int n, cudaStream_t s,
-                uint32_t timeout_ms, bool dump, kite_gpu_emit_fn emit, void* user, std::string* msg,
-                kite_gpu_stats* stat, const StagingFn& staging) {
+                uint32_t timeout_ms, int mode, kite_gpu_emit_fn emit, void* user, std::string* msg,
+                kite_gpu_stats* stat, const StagingFn& staging, const MergeExtra* ex) {
+  const bool dump = mode == kModeDump;
   auto fail = [&](int code, const std::string& m) {
     *msg = m;
     return code;
@@ -981,14 +1061,32 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   MCU(cudaMemcpyAsync(d_filt.p, filt.data(), n * sizeof(InputFilter), cudaMemcpyHostToDevice, s));
   MCU(cudaMemsetAsync(d_over.p, 0xff, 8, s));
   const size_t smem = MergeSmem<T>::total;
-  auto kmerge = dump ? k_merge_tiles<T, true> : k_merge_tiles<T, false>;
+  auto kmerge = mode == kModeDump    ? k_merge_tiles<T, kModeDump>
+                : mode == kModeHisto ? k_merge_tiles<T, kModeHisto>
+                : mode == kModeRows  ? k_merge_tiles<T, kModeRows>
+                                     : k_merge_tiles<T, kModeMerge>;
   cudaFuncSetAttribute(kmerge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  MergeAux aux{};
+  aux.line_k = key_bits / 2;
+  Dev d_hist, d_spill, d_c64;
+  if (mode == kModeHisto) {
+    if (!d_hist.ensure((kHistBins + 1) * 8) || !d_spill.ensure(out_off * 8 + 8)) return fail(KITE_ERR_OOM, "histo buffers");
+    MCU(cudaMemsetAsync(d_hist.p, 0, (kHistBins + 1) * 8, s));
+    aux.hist = d_hist.as<unsigned long long>();
+    aux.spill_n = aux.hist + kHistBins;
+    aux.spill = d_spill.as<unsigned long long>();
+    aux.spill_cap = out_off;
+  }
+  if (mode == kModeRows) {
+    if (!d_c64.ensure(out_off * 8 + 8)) return fail(KITE_ERR_OOM, "query buffers");
+    aux.counts64 = d_c64.as<unsigned long long>();
+  }
   MCU(cudaEventRecord(sev[2], s));
   if (ntiles) {
     kmerge<<<ntiles, kMergeThreads, smem, s>>>(d_keys.as<T>(), d_counts.as<unsigned long long>(),
                                                d_mt.as<MergeTile>(), d_ts.as<TileStream>(), d_filt.as<InputFilter>(),
                                                d_okeys.as<T>(), d_ocounts.as<uint32_t>(), d_tout.as<TileOut<T>>(),
-                                               d_over.as<unsigned long long>(), dst, key_bits / 2);
+                                               d_over.as<unsigned long long>(), dst, aux);
     launches++;
   }
   MCU(cudaEventRecord(sev[3], s));
@@ -1012,6 +1110,89 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     for (int i = 0; i < 5; ++i)
       if (cudaEventElapsedTime(&ms, sev[pairs[i][0]], sev[pairs[i][1]]) == cudaSuccess) stat->stage_ms[i] = ms;
   };
+  stat->tiles = ntiles;
+  if (mode == kModeHisto) {
+    // ---- count -> frequency: the small bins, then the listed large counts ----
+    std::vector<unsigned long long> hb(kHistBins + 1);
+    MCU(cudaMemcpyAsync(hb.data(), d_hist.p, (kHistBins + 1) * 8, cudaMemcpyDeviceToHost, s));
+    if (sync()) return fail(KITE_ERR_TIMEOUT, "histo wait");
+    const unsigned long long ns = std::min<unsigned long long>(hb[kHistBins], out_off);
+    std::vector<unsigned long long> big(ns);
+    MCU(cudaEventRecord(sev[4], s));
+    if (ns) MCU(cudaMemcpyAsync(big.data(), d_spill.p, ns * 8, cudaMemcpyDeviceToHost, s));
+    MCU(cudaEventRecord(sev[5], s));
+    MCU(cudaEventRecord(sev[6], s));
+    if (sync()) return fail(KITE_ERR_TIMEOUT, "histo wait");
+    stage_times();
+    std::sort(big.begin(), big.end());
+    uint64_t keys_out = 0;
+    for (uint32_t b = 0; b < kHistBins; ++b) keys_out += hb[b];
+    stat->rows = keys_out + ns;
+    stat->kernel_launches = launches;
+    if (!ex || !ex->histo) return KITE_OK;
+    for (uint32_t b = 0; b < kHistBins; ++b)
+      if (hb[b] && ex->histo(ex->user, b, hb[b])) return fail(KITE_ERR_CALLBACK, "histo callback aborted");
+    for (size_t i = 0; i < big.size();) {
+      size_t j = i;
+      while (j < big.size() && big[j] == big[i]) ++j;
+      if (ex->histo(ex->user, big[i], j - i)) return fail(KITE_ERR_CALLBACK, "histo callback aborted");
+      i = j;
+    }
+    return KITE_OK;
+  }
+  if (mode == kModeRows) {
+    // ---- query lookups over the non-empty tiles of each partition ----
+    std::vector<uint32_t> qtf(P + 1, 0), qrows;
+    std::vector<T> qkey0;
+    std::vector<unsigned long long> qoff;
+    for (uint32_t p = 0; p < P; ++p) {
+      qtf[p] = (uint32_t)qrows.size();
+      for (uint32_t t = tile_first[p]; t < tile_first[p + 1]; ++t)
+        if (htout[t].rows) {
+          qkey0.push_back(htout[t].first_key);
+          qoff.push_back(mts[t].out_off);
+          qrows.push_back(htout[t].rows);
+        }
+    }
+    qtf[P] = (uint32_t)qrows.size();
+    const uint32_t nq = (uint32_t)ex->nq, nt = (uint32_t)qrows.size();
+    std::vector<T> qk(nq);
+    std::vector<uint32_t> qp(nq);
+    for (uint32_t q = 0; q < nq; ++q) {
+      qk[q] = (T)(((unsigned __int128)ex->keys[2 * q + 1] << 64) | ex->keys[2 * q]);
+      qp[q] = ex->parts[q];
+    }
+    Dev d_qtf, d_qk0, d_qoff, d_qrows, d_qk, d_qp, d_qout;
+    if (!d_qtf.ensure((P + 1) * 4) || !d_qk0.ensure(nt * sizeof(T) + 16) || !d_qoff.ensure(nt * 8 + 8) ||
+        !d_qrows.ensure(nt * 4 + 8) || !d_qk.ensure(nq * sizeof(T) + 16) || !d_qp.ensure(nq * 4 + 8) ||
+        !d_qout.ensure(nq * 8 + 8))
+      return fail(KITE_ERR_OOM, "query buffers");
+    MCU(cudaMemcpyAsync(d_qtf.p, qtf.data(), (P + 1) * 4, cudaMemcpyHostToDevice, s));
+    if (nt) {
+      MCU(cudaMemcpyAsync(d_qk0.p, qkey0.data(), nt * sizeof(T), cudaMemcpyHostToDevice, s));
+      MCU(cudaMemcpyAsync(d_qoff.p, qoff.data(), nt * 8, cudaMemcpyHostToDevice, s));
+      MCU(cudaMemcpyAsync(d_qrows.p, qrows.data(), nt * 4, cudaMemcpyHostToDevice, s));
+    }
+    MCU(cudaEventRecord(sev[4], s));
+    if (nq) {
+      MCU(cudaMemcpyAsync(d_qk.p, qk.data(), nq * sizeof(T), cudaMemcpyHostToDevice, s));
+      MCU(cudaMemcpyAsync(d_qp.p, qp.data(), nq * 4, cudaMemcpyHostToDevice, s));
+      k_query_rows<T><<<(nq + 255) / 256, 256, 0, s>>>(d_okeys.as<T>(), d_c64.as<unsigned long long>(),
+                                                       d_qtf.as<uint32_t>(), d_qk0.as<T>(),
+                                                       d_qoff.as<unsigned long long>(), d_qrows.as<uint32_t>(),
+                                                       d_qk.as<T>(), d_qp.as<uint32_t>(), nq,
+                                                       d_qout.as<unsigned long long>());
+      launches++;
+    }
+    MCU(cudaEventRecord(sev[5], s));
+    if (nq) MCU(cudaMemcpyAsync(ex->counts_out, d_qout.p, nq * 8, cudaMemcpyDeviceToHost, s));
+    MCU(cudaEventRecord(sev[6], s));
+    if (sync()) return fail(KITE_ERR_TIMEOUT, "query wait");
+    MCU(cudaGetLastError());
+    stage_times();
+    stat->kernel_launches = launches;
+    return KITE_OK;
+  }
   if (dump) {
     // ---- TSV: tile byte offsets in (partition, key) order, then formatting ----
     std::vector<unsigned long long> tboff(ntiles + 1);
@@ -1220,11 +1401,12 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
 }  // namespace
 
 int merge_run(int k, uint32_t partitions, const kite_gpu_merge_input* inputs, int n, cudaStream_t s,
-              uint32_t timeout_ms, bool dump, kite_gpu_emit_fn emit, void* user, std::string* msg,
-              kite_gpu_stats* st, const StagingFn& staging) {
+              uint32_t timeout_ms, int mode, kite_gpu_emit_fn emit, void* user, std::string* msg,
+              kite_gpu_stats* st, const StagingFn& staging, const MergeExtra* ex) {
   if (k <= 31)
-    return merge_typed<uint64_t>(partitions, 2 * k, inputs, n, s, timeout_ms, dump, emit, user, msg, st, staging);
-  return merge_typed<u128>(partitions, 2 * k, inputs, n, s, timeout_ms, dump, emit, user, msg, st, staging);
+    return merge_typed<uint64_t>(partitions, 2 * k, inputs, n, s, timeout_ms, mode, emit, user, msg, st, staging,
+                                 ex);
+  return merge_typed<u128>(partitions, 2 * k, inputs, n, s, timeout_ms, mode, emit, user, msg, st, staging, ex);
 }
 
 }  // namespace kite

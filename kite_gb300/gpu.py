@@ -28,7 +28,8 @@ EXPORTED = [
     "kite_gpu_alloc_pinned", "kite_gpu_free_pinned", "kite_gpu_count_submit", "kite_gpu_wait_ticket",
     "kite_gpu_count_submit_device", "kite_gpu_count_finish", "kite_gpu_result_partition", "kite_gpu_merge",
     "kite_gpu_get_stats", "kite_gpu_synchronize", "kite_gpu_count_submit_sample",
-    "kite_gpu_count_submit_device_sample", "kite_gpu_sample_totals", "kite_gpu_dump",
+    "kite_gpu_count_submit_device_sample", "kite_gpu_sample_totals", "kite_gpu_dump", "kite_gpu_histo",
+    "kite_gpu_query",
 ]
 
 
@@ -82,6 +83,7 @@ class MergeInput(C.Structure):
 
 
 EMIT = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(ChunkMeta), C.POINTER(C.c_uint8), C.c_size_t)
+HISTO = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_uint64)
 
 
 def lib() -> C.CDLL:
@@ -110,6 +112,9 @@ def lib() -> C.CDLL:
                                                 C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
         L.kite_gpu_merge.argtypes = [C.c_void_p, C.POINTER(MergeInput), C.c_int, EMIT, C.c_void_p]
         L.kite_gpu_dump.argtypes = [C.c_void_p, C.POINTER(MergeInput), EMIT, C.c_void_p]
+        L.kite_gpu_histo.argtypes = [C.c_void_p, C.POINTER(MergeInput), HISTO, C.c_void_p]
+        L.kite_gpu_query.argtypes = [C.c_void_p, C.POINTER(MergeInput), C.POINTER(C.c_uint64), C.c_size_t,
+                                     C.POINTER(C.c_uint64)]
         L.kite_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
         L.kite_gpu_synchronize.argtypes = [C.c_void_p]
         _lib = L
@@ -266,6 +271,34 @@ class Counter:
         self._check(self._L.kite_gpu_dump(self._h, C.byref(mi), cb, None))
         del keep
         return b"".join(parts)
+
+    def histo(self, image, base: int | None = None) -> dict:
+        """`kite histo` of one kitefile.KiteImage on the GPU: {count: keys}."""
+        mi, keep = image.merge_input(base)
+        out = {}
+
+        def _emit(user, count, keys):
+            out[int(count)] = int(keys)
+            return 0
+
+        cb = HISTO(_emit)
+        self._check(self._L.kite_gpu_histo(self._h, C.byref(mi), cb, None))
+        del keep
+        return out
+
+    def query(self, image, keys: list, base: int | None = None) -> list:
+        """u64 counts of encoded keys (ints; canonical where the database is)
+        in one kitefile.KiteImage, 0 when absent."""
+        mi, keep = image.merge_input(base)
+        n = len(keys)
+        arr = (C.c_uint64 * (2 * max(n, 1)))()
+        for i, key in enumerate(keys):
+            arr[2 * i] = key & (2 ** 64 - 1)
+            arr[2 * i + 1] = key >> 64
+        out = (C.c_uint64 * max(n, 1))()
+        self._check(self._L.kite_gpu_query(self._h, C.byref(mi), arr, n, out))
+        del keep
+        return [int(out[i]) for i in range(n)]
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <string>
 #include <sys/stat.h>
 #include <unistd.h>
@@ -468,10 +469,171 @@ void on_sigint(int) {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// histo (run_histo src/histo/mod.rs:16-169): per input, counts summed per key
+// over its chunks, header filter, count -> frequency on the GPU
+// (kite_gpu_histo); one row per count over all inputs, one column per input.
+// Labels: --label, else file names without the suffixes of
+// infer_sample_labels (src/kiteops/mod.rs:123-165).
+// ---------------------------------------------------------------------------
+std::string label_from_path(const std::string& path, size_t index) {
+  const size_t slash = path.find_last_of('/');
+  std::string name = slash == std::string::npos ? path : path.substr(slash + 1);
+  for (const char* suf : {".fastq.gz", ".fq.gz", ".fastq", ".fq", ".kite", ".tsv", ".txt", ".gz"}) {
+    const size_t l = strlen(suf);
+    if (name.size() >= l && name.compare(name.size() - l, l, suf) == 0) {
+      name.resize(name.size() - l);
+      break;
+    }
+  }
+  return name.empty() ? "sample" + std::to_string(index + 1) : name;
+}
+
+int histo_add(void* user, uint64_t count, uint64_t keys) {
+  (*static_cast<std::map<uint64_t, uint64_t>*>(user))[count] = keys;
+  return 0;
+}
+
+int cmd_histo(int argc, char** argv) {
+  std::vector<std::string> ins, labels;
+  std::string out;
+  int device = 0;
+  for (int i = 2; i < argc; ++i) {
+    std::string a = argv[i];
+    if (a == "-i" || a == "--input") {
+      while (i + 1 < argc && argv[i + 1][0] != '-') ins.push_back(argv[++i]);
+    } else if (a == "--label") {
+      while (i + 1 < argc && argv[i + 1][0] != '-') labels.push_back(argv[++i]);
+    } else if ((a == "-o" || a == "--output") && i + 1 < argc) out = argv[++i];
+    else if (a == "--device" && i + 1 < argc) device = (int)parse_u64(a, argv[++i]);
+    else if ((a == "-t" || a == "--threads") && i + 1 < argc) ++i;
+    else if (a == "-p" || a == "--progress" || a == "--test-mode") continue;
+    else die("unexpected argument '" + a + "' found");
+  }
+  if (ins.empty() || out.empty()) die("the following required arguments were not provided: --input, --output");
+  if (!labels.empty() && labels.size() != ins.size())
+    die("--label count (" + std::to_string(labels.size()) + ") must match input count (" +
+        std::to_string(ins.size()) + ")");
+  if (labels.empty())
+    for (size_t i = 0; i < ins.size(); ++i) labels.push_back(label_from_path(ins[i], i));
+  print_command("histo", argc, argv);
+  const double t0 = now_s();
+  std::vector<std::map<uint64_t, uint64_t>> hs(ins.size());
+  std::map<uint64_t, int> bins;
+  for (size_t i = 0; i < ins.size(); ++i) {
+    kite_reader* r = kite_reader_open(ins[i].c_str());
+    if (!r) die(kite_host_last_error());
+    kite_header_info h{};
+    uint64_t tc = 0, tr = 0;
+    kite_reader_header(r, &h, &tc, &tr);
+    if (h.key_width != 64 && h.key_width != 128) die("histo of 256-bit keys is not supported on the GPU path");
+    kite_gpu_cfg cfg{};
+    cfg.device = device;
+    cfg.k = h.k;
+    cfg.canonical = h.canonical;
+    cfg.partitions = h.partitions;
+    kite_gpu_ctx* ctx = nullptr;
+    if (kite_gpu_open(&cfg, &ctx) != KITE_OK) die("failed to open the GPU histo context");
+    kite_gpu_merge_input mi{};
+    kite_reader_merge_input(r, &mi);
+    if (kite_gpu_histo(ctx, &mi, histo_add, &hs[i]) != KITE_OK) die(kite_gpu_last_error(ctx));
+    kite_gpu_close(ctx);
+    kite_reader_close(r);
+    for (auto& kv : hs[i]) bins[kv.first] = 1;
+  }
+  FILE* f = out == "-" ? stdout : fopen(out.c_str(), "wb");
+  if (!f) die("failed to create " + out);
+  fprintf(f, "count");
+  for (auto& l : labels) fprintf(f, "\t%s", l.c_str());
+  fprintf(f, "\n");
+  for (auto& b : bins) {
+    fprintf(f, "%llu", (unsigned long long)b.first);
+    for (auto& h : hs) {
+      auto it = h.find(b.first);
+      fprintf(f, "\t%llu", (unsigned long long)(it == h.end() ? 0 : it->second));
+    }
+    fprintf(f, "\n");
+  }
+  if (f == stdout) fflush(stdout);
+  else fclose(f);
+  fprintf(stderr, "[kite histo] done in %.3fs (bins=%zu, output=%s)\n", now_s() - t0, bins.size(), out.c_str());
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// query (run_query src/query/mod.rs:15-96): encode_query_kmer
+// (src/kiteops/mod.rs:302-348: length k, ACGT only, canonical if the
+// database is), its partition, its summed count (kite_gpu_query), and the
+// report with the header filter's verdict.
+// ---------------------------------------------------------------------------
+int cmd_query(int argc, char** argv) {
+  std::string in, kmer;
+  int device = 0;
+  for (int i = 2; i < argc; ++i) {
+    std::string a = argv[i];
+    if ((a == "-i" || a == "--input") && i + 1 < argc) in = argv[++i];
+    else if ((a == "-k" || a == "--kmer") && i + 1 < argc) kmer = argv[++i];
+    else if (a == "--device" && i + 1 < argc) device = (int)parse_u64(a, argv[++i]);
+    else if (a == "--test-mode") continue;
+    else die("unexpected argument '" + a + "' found");
+  }
+  if (in.empty() || kmer.empty()) die("the following required arguments were not provided: --input, --kmer");
+  print_command("query", argc, argv);
+  fprintf(stderr, "[kite query] opening: %s\n[kite query] query:   %s\n", in.c_str(), kmer.c_str());
+  const double t0 = now_s();
+  kite_reader* r = kite_reader_open(in.c_str());
+  if (!r) die(kite_host_last_error());
+  kite_header_info h{};
+  uint64_t tc = 0, tr = 0;
+  kite_reader_header(r, &h, &tc, &tr);
+  if (h.key_width != 64 && h.key_width != 128) die("query of 256-bit keys is not supported on the GPU path");
+  if (kmer.size() != (size_t)h.k)
+    die("query k-mer length " + std::to_string(kmer.size()) + " does not match database k=" + std::to_string(h.k));
+  unsigned __int128 fwd = 0, rev = 0;
+  for (size_t i = 0; i < kmer.size(); ++i) {
+    const char c = kmer[i];
+    const char* pos = strchr("ACGT", c >= 'a' && c <= 'z' ? c - 32 : c);
+    if (!pos || c == 0) die("query k-mer contains non-ACGT characters");
+    const unsigned b = (unsigned)(pos - "ACGT");
+    fwd = (fwd << 2) | b;
+    rev |= (unsigned __int128)(3 - b) << (2 * i);
+  }
+  const unsigned __int128 key = h.canonical && rev < fwd ? rev : fwd;
+  const uint64_t kw[2] = {(uint64_t)key, (uint64_t)(key >> 64)};
+  unsigned bits = 0;
+  while ((1u << bits) < h.partitions) ++bits;
+  const uint64_t x = h.key_width == 64 ? kw[0] : (kw[0] ^ kw[1]);
+  const uint64_t part = bits ? (x * 0x9E3779B97F4A7C15ull) >> (64 - bits) : 0;
+  kite_gpu_cfg cfg{};
+  cfg.device = device;
+  cfg.k = h.k;
+  cfg.canonical = h.canonical;
+  cfg.partitions = h.partitions;
+  kite_gpu_ctx* ctx = nullptr;
+  if (kite_gpu_open(&cfg, &ctx) != KITE_OK) die("failed to open the GPU query context");
+  kite_gpu_merge_input mi{};
+  kite_reader_merge_input(r, &mi);
+  uint64_t count = 0;
+  if (kite_gpu_query(ctx, &mi, kw, 1, &count) != KITE_OK) die(kite_gpu_last_error(ctx));
+  kite_gpu_close(ctx);
+  std::string ks(h.k, 'A');
+  for (int i = 0; i < h.k; ++i) ks[i] = "ACGT"[(unsigned)(key >> (2 * (h.k - 1 - i))) & 3u];
+  const bool pass = !(h.has_min && count < h.min_count) && !(h.has_max && count > h.max_count);
+  printf("Kite Query\n  Database:           %s\n  Query:              %s\n  Partition:          %llu\n"
+         "  Count:              %llu\n  Header Min Count:   %s\n  Header Max Count:   %s\n  Header Filter:      %s\n",
+         in.c_str(), ks.c_str(), (unsigned long long)part, (unsigned long long)count,
+         opt_str(h.has_min, h.min_count).c_str(), opt_str(h.has_max, h.max_count).c_str(),
+         count == 0 ? "not present" : (pass ? "included" : "excluded from downstream analysis/output"));
+  fflush(stdout);
+  kite_reader_close(r);
+  fprintf(stderr, "[kite query] done in %.3fs\n", now_s() - t0);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   std::signal(SIGINT, on_sigint);  // ctrl-c exits 130 (src/main.rs:21-25)
   if (argc < 2) {
-    fprintf(stderr, "Usage: kite <count|merge|dump|info> [OPTIONS]\n");
+    fprintf(stderr, "Usage: kite <count|merge|dump|histo|query|info> [OPTIONS]\n");
     return 2;
   }
   const std::string cmd = argv[1];
@@ -480,6 +642,8 @@ int main(int argc, char** argv) {
     if (cmd == "merge") return cmd_merge(argc, argv);
     if (cmd == "dump") return cmd_dump(argc, argv);
     if (cmd == "info") return cmd_info(argc, argv);
+    if (cmd == "histo") return cmd_histo(argc, argv);
+    if (cmd == "query") return cmd_query(argc, argv);
     fprintf(stderr, "error: unrecognized subcommand '%s'\n", cmd.c_str());
     return 2;
   } catch (const Fail& f) {

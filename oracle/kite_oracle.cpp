@@ -28,6 +28,7 @@
 #include <cstring>
 #include <deque>
 #include <functional>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
@@ -1356,9 +1357,92 @@ using namespace orc;
 
 static thread_local std::string g_err;
 
+// ---------------------------------------------------------------------------
+// histo: run_histo src/histo/mod.rs:16-169 for one input: per partition
+// load_partition_counts (u64 saturating sums), apply_reader_filter_to_rows
+// (src/kiteops/mod.rs:103-108) on those sums, then count -> frequency.
+// query: run_query src/query/mod.rs:15-96: encode_query_kmer
+// (src/kiteops/mod.rs:302-348), bucket_for_key, load_partition_counts and a
+// binary search; the header filter only labels the result.
+// ---------------------------------------------------------------------------
+static std::map<uint64_t, uint64_t> histo_of(const Reader& r) {
+  std::map<uint64_t, uint64_t> h;
+  for (size_t p = 0; p < r.h.partitions; ++p)
+    for (auto& x : load_partition_counts(r, p))
+      if (passes(x.second, r.h)) h[x.second] += 1;
+  return h;
+}
+
+static uint64_t query_key(const Reader& r, u128 key, size_t* partition) {
+  unsigned bits = 0;
+  while ((1ull << bits) < r.h.partitions) ++bits;
+  const size_t p = r.h.key_width == 64 ? bucket_of((uint64_t)key, bits) : bucket_of(key, bits);
+  if (partition) *partition = p;
+  const auto rows = load_partition_counts(r, p);
+  auto it = std::lower_bound(rows.begin(), rows.end(), key, [](const Row& a, u128 k) { return a.first < k; });
+  return it != rows.end() && it->first == key ? it->second : 0;
+}
+
+static u128 encode_query_kmer(const std::string& seq, const Header& h) {
+  if (seq.size() != h.k)
+    throw Error("query k-mer length " + std::to_string(seq.size()) + " does not match database k=" +
+                std::to_string(h.k));
+  for (char c : seq)
+    if (!strchr("ACGTacgt", c) || c == 0) throw Error("query k-mer contains non-ACGT characters");
+  u128 key = 0;
+  size_t n = 0;
+  if (h.key_width == 64)
+    scan_kmers<uint64_t>((const uint8_t*)seq.data(), seq.size(), h.k, h.canonical != 0, [&](uint64_t x) {
+      key = x;
+      n++;
+    });
+  else
+    scan_kmers<u128>((const uint8_t*)seq.data(), seq.size(), h.k, h.canonical != 0, [&](u128 x) {
+      key = x;
+      n++;
+    });
+  if (n != 1) throw Error("failed to encode query k-mer");
+  return key;
+}
+
 extern "C" {
 
 const char* orc_last_error() { return g_err.c_str(); }
+
+// histo of one .kite image: bins ascending into counts / freqs (up to cap);
+// returns the number of bins, -1 on error.
+long long orc_histo_kite(const uint8_t* img, size_t n, uint64_t* counts, uint64_t* freqs, size_t cap) {
+  try {
+    Reader r;
+    r.open(img, n);
+    size_t i = 0;
+    const auto h = histo_of(r);
+    for (auto& kv : h) {
+      if (i < cap) {
+        counts[i] = kv.first;
+        freqs[i] = kv.second;
+      }
+      ++i;
+    }
+    return (long long)h.size();
+  } catch (const Error& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
+// u64 sums of encoded keys ((lo, hi) words each) in one .kite image, 0 when absent.
+int orc_query_kite(const uint8_t* img, size_t n, const uint64_t* keys, size_t nq, uint64_t* out) {
+  try {
+    Reader r;
+    r.open(img, n);
+    for (size_t i = 0; i < nq; ++i) out[i] = query_key(r, ((u128)keys[2 * i + 1] << 64) | keys[2 * i], nullptr);
+    return 0;
+  } catch (const Error& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
 
 // Parse a FASTQ chunk: returns the number of sequence slices (start offset and
 // length pairs written to out, up to cap), or -1 if the chunk is rejected.
@@ -1783,6 +1867,85 @@ static int cmd_merge(int argc, char** argv) {
   return 0;
 }
 
+static std::string label_of(const std::string& path, size_t index) {
+  std::string name = path.substr(path.find_last_of('/') == std::string::npos ? 0 : path.find_last_of('/') + 1);
+  for (const char* suf : {".fastq.gz", ".fq.gz", ".fastq", ".fq", ".kite", ".tsv", ".txt", ".gz"}) {
+    const size_t l = strlen(suf);
+    if (name.size() >= l && name.compare(name.size() - l, l, suf) == 0) {
+      name.resize(name.size() - l);
+      break;
+    }
+  }
+  return name.empty() ? "sample" + std::to_string(index + 1) : name;
+}
+
+static int cmd_histo(int argc, char** argv) {
+  std::vector<std::string> ins, labels;
+  std::string out;
+  for (int i = 0; i < argc; ++i) {
+    std::string a = argv[i];
+    if (a == "-i" || a == "--input") {
+      while (i + 1 < argc && argv[i + 1][0] != '-') ins.push_back(argv[++i]);
+    } else if (a == "--label") {
+      while (i + 1 < argc && argv[i + 1][0] != '-') labels.push_back(argv[++i]);
+    } else if ((a == "-o" || a == "--output") && i + 1 < argc) out = argv[++i];
+    else if ((a == "-t" || a == "--threads") && i + 1 < argc) ++i;
+    else if (a == "-p" || a == "--progress" || a == "--test-mode") continue;
+    else throw Error("unknown argument " + a);
+  }
+  if (labels.empty())
+    for (size_t i = 0; i < ins.size(); ++i) labels.push_back(label_of(ins[i], i));
+  std::vector<std::map<uint64_t, uint64_t>> hs;
+  std::map<uint64_t, int> bins;
+  for (auto& in : ins) {
+    auto bytes = read_file(in);
+    Reader r;
+    r.open(bytes.data(), bytes.size());
+    hs.push_back(histo_of(r));
+    for (auto& kv : hs.back()) bins[kv.first] = 1;
+  }
+  std::string t = "count";
+  for (auto& l : labels) t += "\t" + l;
+  t += "\n";
+  for (auto& b : bins) {
+    t += std::to_string(b.first);
+    for (auto& h : hs) {
+      auto it = h.find(b.first);
+      t += "\t" + std::to_string(it == h.end() ? 0 : it->second);
+    }
+    t += "\n";
+  }
+  std::vector<uint8_t> v(t.begin(), t.end());
+  write_file(out, v);
+  return 0;
+}
+
+static int cmd_query(int argc, char** argv) {
+  std::string in, kmer;
+  for (int i = 0; i < argc; ++i) {
+    std::string a = argv[i];
+    if ((a == "-i" || a == "--input") && i + 1 < argc) in = argv[++i];
+    else if ((a == "-k" || a == "--kmer") && i + 1 < argc) kmer = argv[++i];
+    else if (a == "--test-mode") continue;
+    else throw Error("unknown argument " + a);
+  }
+  auto bytes = read_file(in);
+  Reader r;
+  r.open(bytes.data(), bytes.size());
+  const u128 key = encode_query_kmer(kmer, r.h);
+  size_t p = 0;
+  const uint64_t c = query_key(r, key, &p);
+  std::vector<char> ks(r.h.k + 1, 0);
+  decode_kmer(key, r.h.k, ks.data());
+  auto opt = [](bool has, uint32_t v) { return has ? std::to_string(v) : std::string("none"); };
+  printf("Kite Query\n  Database:           %s\n  Query:              %s\n  Partition:          %zu\n"
+         "  Count:              %llu\n  Header Min Count:   %s\n  Header Max Count:   %s\n  Header Filter:      %s\n",
+         in.c_str(), ks.data(), p, (unsigned long long)c, opt(r.h.has_min, r.h.min_count).c_str(),
+         opt(r.h.has_max, r.h.max_count).c_str(),
+         c == 0 ? "not present" : (passes(c, r.h) ? "included" : "excluded from downstream analysis/output"));
+  return 0;
+}
+
 static int cmd_info(int argc, char** argv) {
   std::string in;
   for (int i = 0; i < argc; ++i)
@@ -1804,6 +1967,8 @@ int main(int argc, char** argv) {
     if (cmd == "dump") return cmd_dump(argc - 2, argv + 2);
     if (cmd == "merge") return cmd_merge(argc - 2, argv + 2);
     if (cmd == "info") return cmd_info(argc - 2, argv + 2);
+    if (cmd == "histo") return cmd_histo(argc - 2, argv + 2);
+    if (cmd == "query") return cmd_query(argc - 2, argv + 2);
     usage();
     return 2;
   } catch (const std::exception& e) {
