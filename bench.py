@@ -598,6 +598,27 @@ def run_dump_bench(args, world, rank, local):
     dom = max(algo, key=lambda i: stage[i])
     peak, peak_src = peaks()
     achieved = algo[dom] / (stage[dom] / 1e3) / 1e9
+    # kite histo and a batch of kite query lookups on the same image
+    c = gpu.Counter(K, CANONICAL, PARTITIONS, device=local)
+    c.histo(ki, base=pin.data_ptr())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = c.histo(ki, base=pin.data_ptr())
+    histo_s = time.perf_counter() - t0
+    hst = c.stats()
+    rng = np.random.default_rng(7)
+    present = [ch.key_min for ch in ki.chunks] + [ch.key_max for ch in ki.chunks]
+    qkeys = present * (500_000 // max(1, len(present))) + [int(x) for x in rng.integers(0, 2 ** 62, size=500_000,
+                                                                                          dtype=np.uint64)]
+    c.query(ki, qkeys[:1000], base=pin.data_ptr())
+    t0 = time.perf_counter()
+    qc = c.query(ki, qkeys, base=pin.data_ptr())
+    query_s = time.perf_counter() - t0
+    c.close()
+    tables = {"histo": {"rows_per_s": rows_in / histo_s, "seconds": histo_s, "bins": len(hist),
+                        "stage_ms": {names[i]: round(hst["stage_ms"][i], 3) for i in range(3)}},
+              "query": {"keys": len(qkeys), "keys_per_s": len(qkeys) / query_s, "seconds": query_s,
+                        "found": sum(1 for x in qc if x)}}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         sys.path.insert(0, str(ROOT / "oracle"))
@@ -612,6 +633,15 @@ def run_dump_bench(args, world, rank, local):
         cpu = {"value": tsv_s.count(b"\n") / secs, "unit": "lines/s", "cores": 1, "kind": "port",
                "sample": "oracle dump of the .kite image of a 1M-read count of the same workload (1 thread)",
                "seconds": secs}
+        import ctypes as C
+        L = oracle.lib()
+        L.orc_histo_kite.restype = C.c_longlong
+        L.orc_histo_kite.argtypes = [C.c_char_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t]
+        t1 = time.perf_counter()
+        L.orc_histo_kite(simg, len(simg), None, None, 0)
+        hs = time.perf_counter() - t1
+        tables["histo"]["cpu_baseline"] = {"rows_per_s": KiteImage.parse(simg).total_rows / hs, "seconds": hs,
+                                           "sample": "oracle histo of the same 1M-read image (1 thread)"}
     if rank == 0:
         line = {"metric": DUMP_METRIC, "value": value, "unit": "lines/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak",
@@ -627,7 +657,7 @@ def run_dump_bench(args, world, rank, local):
                              "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
                              "algorithmic_bytes": algo[dom], "kernel_ms": stage[dom],
                              "stage_ms": {names[i]: round(stage[i], 3) for i in range(5)}},
-                "cpu_baseline": cpu}
+                "cpu_baseline": cpu, "histo_query": tables}
         print(json.dumps(line))
     return 0
 
