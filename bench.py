@@ -838,10 +838,10 @@ def main():
         e2e_parts["submit_s"] += t_b - t_a
         out_bytes = 0
 
-        def cb(meta, addr, n):
+        def cb(pid, addr, n):
             nonlocal out_bytes
             out_bytes += n
-        cc.finish(collect=True, callback=cb, raw=True)
+        cc.finish(collect=True, callback=cb, raw=True, meta=False)
         e2e_parts["finish_s"] += time.perf_counter() - t_b
         sm = cc.stats()["stage_ms"]
         e2e_parts["d2h_ms"] += sm[7]

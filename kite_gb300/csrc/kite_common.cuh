@@ -97,6 +97,12 @@ __device__ __forceinline__ T shfl_key(T v, int src) {
   return make_key<T>(lo, hi);
 }
 template <class T>
+__device__ __forceinline__ T shfl_up_key(T v, int d) {
+  const uint64_t lo = __shfl_up_sync(0xffffffffu, (unsigned long long)(uint64_t)v, d);
+  const uint64_t hi = sizeof(T) == 8 ? 0 : __shfl_up_sync(0xffffffffu, (unsigned long long)hi64(v), d);
+  return make_key<T>(lo, hi);
+}
+template <class T>
 __device__ __forceinline__ T shfl_xor_key(T v, int m) {
   const uint64_t lo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)v, m);
   const uint64_t hi = sizeof(T) == 8 ? 0 : __shfl_xor_sync(0xffffffffu, (unsigned long long)hi64(v), m);

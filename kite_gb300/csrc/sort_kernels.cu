@@ -479,13 +479,23 @@ __device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, ui
   if (threadIdx.x == 0) head[U] = (unsigned short)n;
   __syncthreads();
   unsigned long long rest = 0;
-  for (unsigned v = threadIdx.x; v < U; v += NT) {
-    const unsigned i = head[v];
-    const unsigned c = (unsigned)head[v + 1] - i;
-    const T key = buf[i];
-    g[v] = key;
-    gc[v] = c;
-    if (v > 0) rest += (unsigned long long)(varint_len(T(key - buf[head[v - 1]])) + varint_len((uint64_t)c));
+  // a warp takes 32 consecutive rows: the next row's start and the previous
+  // row's key come from the neighbouring lanes (the warp's ends read them)
+  for (unsigned v0 = threadIdx.x - (unsigned)lane; v0 < U; v0 += NT) {
+    const unsigned v = v0 + (unsigned)lane;
+    const bool act = v < U;
+    const unsigned i = act ? (unsigned)head[v] : 0u;
+    const T key = act ? buf[i] : T(0);
+    unsigned nxt = __shfl_down_sync(0xffffffffu, i, 1);
+    if (lane == 31 || v + 1 >= U) nxt = act ? (unsigned)head[v + 1] : 0u;
+    T prev = shfl_up_key(key, 1);
+    if (lane == 0 && act && v > 0) prev = buf[head[v - 1]];
+    if (act) {
+      const unsigned c = nxt - i;
+      g[v] = key;
+      gc[v] = c;
+      if (v > 0) rest += (unsigned long long)(varint_len(T(key - prev)) + varint_len((uint64_t)c));
+    }
   }
   unsigned long long rest_total;
   block_exclusive_scan<NT, unsigned long long>(rest, scan64, &rest_total);

@@ -179,17 +179,20 @@ class Counter:
         self._check(self._L.kite_gpu_sample_totals(self._h, sample, out))
         return tuple(int(x) for x in out)
 
-    def finish(self, collect: bool = True, callback=None, raw: bool = False) -> list:
+    def finish(self, collect: bool = True, callback=None, raw: bool = False, meta: bool = True) -> list:
         """Count the segment; returns [(meta dict, payload bytes)] per non-empty
         partition when collect, else keeps results on the device.  With raw and
         a callback, the callback gets (meta, host address, length) of the
         payload in the library's host buffer (valid during the call) instead of
-        a copy."""
+        a copy; with meta False as well, (partition id, host address, length)."""
         out = []
 
-        def _emit(user, meta, data, n):
+        def _emit(user, m_ptr, data, n):
             try:
-                m = meta.contents.as_dict()
+                if raw and callback is not None and not meta:
+                    callback(m_ptr.contents.partition_id, C.cast(data, C.c_void_p).value, n)
+                    return 0
+                m = m_ptr.contents.as_dict()
                 if raw and callback is not None:
                     callback(m, C.cast(data, C.c_void_p).value, n)
                     return 0
