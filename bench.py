@@ -778,12 +778,24 @@ def main():
         traffic = tr["dram_bytes_per_key"] * kmers * (st.get("split_levels", 1) if tr.get("per_level") else 1)
     sort_ms = avg_ms[3] + avg_ms[4] + avg_ms[5]
     sort_bytes = stages[3][1] + stages[4][1]
+    # the bytes a least-significant-digit radix sort with 16-bit digits would
+    # move over the same keys (a histogram read of N·w, then a read and a
+    # write of N·w per pass, p = ceil(2k / 16) passes) plus the run-length
+    # pass (read N·w, write d·(w + 4)): the sort expressed as effective
+    # bandwidth against the multi-pass method, over the measured split +
+    # tile sort time
+    w_key = 8 if kk <= 31 else 16
+    p16 = -(-2 * kk // 16)
+    lsd16_bytes = st["kmers"] * w_key * (1 + 2 * p16) + st["kmers"] * w_key + st["rows"] * (w_key + 4)
     roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                 "traffic_source": traffic_src,
                 "algorithmic_bytes": algo_bytes, "kernel_ms": avg_ms[dom],
                 "sort_gbs": sort_bytes / (sort_ms / 1e3) / 1e9 if sort_ms > 0 else None,
                 "sort_frac": (sort_bytes / (sort_ms / 1e3) / 1e9) / peak if sort_ms > 0 else None,
+                "sort_lsd16_bytes": lsd16_bytes,
+                "sort_lsd16_gbs": lsd16_bytes / (sort_ms / 1e3) / 1e9 if sort_ms > 0 else None,
+                "sort_lsd16_frac": (lsd16_bytes / (sort_ms / 1e3) / 1e9) / peak if sort_ms > 0 else None,
                 "stage_ms": {stages[i][0]: round(avg_ms[i], 4) for i in stages}}
 
     # ---- learned vs sampled splitters on the same input (identical output) ----
