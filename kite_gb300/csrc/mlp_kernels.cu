@@ -503,8 +503,7 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
   k_make_features<T><<<(rows + 255) / 256, 256, 0, s>>>(sorted, rows, rows, 1, key_bits, m->hist2, m->feats,
                                                          m->target, m->scale);
   rep->launches += 3;
-  int steps = 400;
-  if (const char* e = getenv("KITE_MLP_STEPS")) steps = std::max(1, atoi(e));
+  const int steps = 400;
   int tl = 0;
   if (mlp_train(m, rows, steps, 8192, 2e-3f, s, timeout_ms, &rep->loss, &tl)) return 1;
   rep->launches += tl;
