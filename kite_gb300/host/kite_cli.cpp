@@ -104,7 +104,7 @@ int cmd_count(int argc, char** argv) {
         " --max " + std::to_string(mx));
   if (k > 64) die("k > 64 (256-bit keys) is not supported by the GPU counting path");
   if (partitions == 1) die("invalid partition count: --partitions 1 leaves no partition bits for routing");
-  if (mode != "fast") die("--mode " + mode + " needs zstd, which this build does not include; use --mode fast");
+  if (mode != "fast") die("--mode " + mode + " needs zstd, which this binary is not compiled with; use --mode fast");
   const bool to_null = out == "/dev/null";
   if (!to_null && (out.size() < 5 || out.compare(out.size() - 5, 5, ".kite") != 0))
     die("invalid count output path: output must end with .kite, or be /dev/null for benchmark runs.\nGot: " + out +
@@ -564,7 +564,7 @@ int cmd_histo(int argc, char** argv) {
 // query (run_query src/query/mod.rs:15-96): encode_query_kmer
 // (src/kiteops/mod.rs:302-348: length k, ACGT only, canonical if the
 // database is), its partition, its summed count (kite_gpu_query), and the
-// report with the header filter's verdict.
+// report with the header filter's outcome.
 // ---------------------------------------------------------------------------
 int cmd_query(int argc, char** argv) {
   std::string in, kmer;

@@ -1016,7 +1016,7 @@ kite_input* kite_input_open(const char* path, uint64_t chunk_size) {
     if (!scan_bgzf(in->file.p, in->file.n, in->blocks, in->bgzf_err)) in->blocks.clear();
     return in;
 #else
-    set_err("gzip input needs zlib, which this build lacks");
+    set_err("gzip input needs zlib, which this binary is not compiled with");
     delete in;
     return nullptr;
 #endif
@@ -1039,7 +1039,7 @@ kite_input* kite_input_open(const char* path, uint64_t chunk_size) {
     }
     gzbuffer(in->gz, 1 << 20);
 #else
-    set_err("gzip input needs zlib, which this build lacks");
+    set_err("gzip input needs zlib, which this binary is not compiled with");
     delete in;
     return nullptr;
 #endif

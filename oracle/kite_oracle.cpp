@@ -242,7 +242,7 @@ static ByteSource* open_source(const std::string& path, Compression c) {
 #if ORC_HAVE_ZLIB
   return new GzSource(path);  // gzread continues across gzip members
 #else
-  throw Error("gzip input needs zlib, which this build lacks");
+  throw Error("gzip input needs zlib, which this binary is not compiled with");
 #endif
 }
 
@@ -307,7 +307,7 @@ static bool inflate_member(const uint8_t* raw, size_t n, std::vector<uint8_t>& o
 #else
   (void)raw;
   (void)n;
-  throw Error("gzip input needs zlib, which this build lacks");
+  throw Error("gzip input needs zlib, which this binary is not compiled with");
 #endif
 }
 

@@ -47,7 +47,7 @@ def test_u128_matches_u64(orc):
 
 
 def test_u256_style_n_reset_counts(orc):
-    # src/count/kmer.rs:607-621 uses k=65 (U256, out of this build's scope);
+    # src/count/kmer.rs:607-621 uses k=65 (U256 keys, beyond the k <= 64 covered here);
     # the same window arithmetic at k=50/64 on the u128 path.
     seq = "A" * 150
     seq = seq[:60] + "N" + seq[61:]
