@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(256) k_encode(const T* __restrict__ keys, cons
   const T* k = keys + td.start;
   const uint32_t* c = counts + td.start;
   unsigned long long run = 0;
+  unsigned* scan32 = reinterpret_cast<unsigned*>(sm);
   for (uint32_t r0 = 0; r0 < o.rows; r0 += 256) {
     const uint32_t r = r0 + threadIdx.x;
     int sz = 0;
@@ -185,8 +186,8 @@ __global__ void __launch_bounds__(256) k_encode(const T* __restrict__ keys, cons
         sz = varint_len(delta) + varint_len((uint64_t)cnt);
       }
     }
-    unsigned long long tot;
-    const unsigned ex = (unsigned)block_exclusive_scan<256, unsigned long long>((unsigned long long)sz, sm, &tot);
+    unsigned tot;
+    const unsigned ex = block_exclusive_scan<256, unsigned>((unsigned)sz, scan32, &tot);
     if (r < o.rows) {
       uint8_t* q = chunk + ex;
       if (r == 0 && first_in_bucket) {
@@ -202,7 +203,22 @@ __global__ void __launch_bounds__(256) k_encode(const T* __restrict__ keys, cons
     if (at + tot > out_cap) {
       if (threadIdx.x == 0) dev_fail(st, KITE_DEV_ENCODE_OVERFLOW, t, r0, 0);
     } else {
-      for (unsigned i = threadIdx.x; i < (unsigned)tot; i += 256) out[at + i] = chunk[i];
+      // 4-byte stores on 4-byte aligned addresses; the unaligned head and
+      // tail bytes one by one
+      uint8_t* dst = out + at;
+      const unsigned head = (unsigned)((4u - ((uintptr_t)dst & 3u)) & 3u);
+      if (tot < head + 8u) {
+        for (unsigned i = threadIdx.x; i < tot; i += 256) dst[i] = chunk[i];
+      } else {
+        const unsigned body = (tot - head) & ~3u, tail = tot - head - body;
+        if (threadIdx.x < head) dst[threadIdx.x] = chunk[threadIdx.x];
+        if (threadIdx.x < tail) dst[head + body + threadIdx.x] = chunk[head + body + threadIdx.x];
+        uint32_t* dw = reinterpret_cast<uint32_t*>(dst + head);
+        for (unsigned i = threadIdx.x; i < body / 4; i += 256) {
+          const uint8_t* b = chunk + head + 4 * i;
+          dw[i] = (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+        }
+      }
     }
     __syncthreads();  // the chunk is refilled next round
     run += tot;
