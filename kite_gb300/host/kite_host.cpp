@@ -939,7 +939,11 @@ struct kite_input {
       }
     };
     std::vector<std::thread> pool;
-    for (unsigned t = 1; t < threads; ++t) pool.emplace_back(work);
+    try {
+      for (unsigned t = 1; t < threads; ++t) pool.emplace_back(work);
+    } catch (...) {
+      // no more threads to be had: the ones running and this one finish the batch
+    }
     work();
     for (auto& t : pool) t.join();
     if (!exact.load()) {
