@@ -125,3 +125,40 @@ def test_cli_histo_and_query(gpu, orc, tmp_path):
     assert r.returncode != 0 and b"query k-mer length 4 does not match database k=25" in r.stderr
     r = run([CLI, "query", "-i", files[0], "-k", "N" * 25], check=False)
     assert r.returncode != 0 and b"query k-mer contains non-ACGT characters" in r.stderr
+
+
+def test_histo_query_dump_of_segmented_u128_count(gpu, orc):
+    # k=45 (u128 keys) counted in several segments (small arena): partitions
+    # hold several chunks; histo, query and dump all sum them
+    from kite_gb300 import host, ingest
+    fq = synth.small_workload(seed=14, n_reads=5000, genome_len=25_000)
+    w = host.Writer(None, 45, True, 8, 128, 7, 16 << 20, 2, None, 6)
+    with gpu.Counter(45, True, 8, arena_bytes=256 * 1024) as c:
+        for o, l in ingest.split_chunks(fq, 100_000):
+            try:
+                c.submit(fq[o:o + l])
+            except gpu.KiteGpuError as e:
+                assert e.code == -9
+                for m, p in c.finish():
+                    w.append(m, p)
+                c.submit(fq[o:o + l])
+        for m, p in c.finish():
+            w.append(m, p)
+    w.worker_drain()
+    w.finalize()
+    img = w.image()
+    w.close()
+    ki = KiteImage.parse(img)
+    assert max(ki.part_count) >= 2
+    assert gpu_histo(gpu, img) == orc_histo(orc, img)
+    keys = [ch.key_min for ch in ki.chunks] + [ch.key_max for ch in ki.chunks] + [12345, 2 ** 80 + 7]
+    assert gpu_query(gpu, img, keys) == orc_query(orc, img, keys)
+    with gpu.Counter(45, True, 8) as c:
+        assert c.dump(ki) == orc.dump(img)
+
+
+def test_histo_query_empty(gpu, orc):
+    img = build_image(21, False, 16, [])
+    assert gpu_histo(gpu, img) == {} == orc_histo(orc, img)
+    assert gpu_query(gpu, img, [0, 5, 2 ** 40]) == [0, 0, 0]
+    assert gpu_query(gpu, img, []) == []
