@@ -607,9 +607,9 @@ def run_dump_bench(args, world, rank, local):
     histo_s = time.perf_counter() - t0
     hst = c.stats()
     rng = np.random.default_rng(7)
-    present = [ch.key_min for ch in ki.chunks] + [ch.key_max for ch in ki.chunks]
-    qkeys = present * (500_000 // max(1, len(present))) + [int(x) for x in rng.integers(0, 2 ** 62, size=500_000,
-                                                                                          dtype=np.uint64)]
+    present = np.array([ch.key_min for ch in ki.chunks] + [ch.key_max for ch in ki.chunks], dtype=np.uint64)
+    qkeys = np.concatenate([np.tile(present, 500_000 // max(1, len(present))),
+                            rng.integers(0, 2 ** 62, size=500_000, dtype=np.uint64)])
     c.query(ki, qkeys[:1000], base=pin.data_ptr())
     t0 = time.perf_counter()
     qc = c.query(ki, qkeys, base=pin.data_ptr())

@@ -289,19 +289,26 @@ class Counter:
         del keep
         return out
 
-    def query(self, image, keys: list, base: int | None = None) -> list:
-        """u64 counts of encoded keys (ints; canonical where the database is)
-        in one kitefile.KiteImage, 0 when absent."""
+    def query(self, image, keys, base: int | None = None) -> list:
+        """u64 counts of encoded keys (ints, or a numpy uint64 array for
+        k <= 31; canonical where the database is) in one kitefile.KiteImage,
+        0 when absent."""
+        import numpy as np
         mi, keep = image.merge_input(base)
         n = len(keys)
-        arr = (C.c_uint64 * (2 * max(n, 1)))()
-        for i, key in enumerate(keys):
-            arr[2 * i] = key & (2 ** 64 - 1)
-            arr[2 * i + 1] = key >> 64
-        out = (C.c_uint64 * max(n, 1))()
-        self._check(self._L.kite_gpu_query(self._h, C.byref(mi), arr, n, out))
+        words = np.zeros(2 * max(n, 1), dtype=np.uint64)
+        if n and isinstance(keys, np.ndarray) and keys.dtype == np.uint64:
+            words[0:2 * n:2] = keys
+        else:
+            for i, key in enumerate(keys):
+                words[2 * i] = key & (2 ** 64 - 1)
+                words[2 * i + 1] = key >> 64
+        out = np.zeros(max(n, 1), dtype=np.uint64)
+        u64p = C.POINTER(C.c_uint64)
+        self._check(self._L.kite_gpu_query(self._h, C.byref(mi), words.ctypes.data_as(u64p), n,
+                                           out.ctypes.data_as(u64p)))
         del keep
-        return [int(out[i]) for i in range(n)]
+        return out[:n].tolist()
 
     def close(self) -> None:
         if getattr(self, "_h", None):
