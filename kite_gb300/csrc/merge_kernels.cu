@@ -643,7 +643,22 @@ __global__ void __launch_bounds__(kTsvThreads) k_tsv_tiles(const T* __restrict__
       p[len - 1] = '\n';
     }
     __syncthreads();
-    for (unsigned i = threadIdx.x; i < tot; i += NT) out[dst + i] = (uint8_t)buf[i];
+    // 4-byte stores on 4-byte aligned addresses; the unaligned head and tail
+    // bytes one by one
+    uint8_t* d8 = out + dst;
+    const unsigned head = (unsigned)((4u - ((uintptr_t)d8 & 3u)) & 3u);
+    if (tot < head + 8u) {
+      for (unsigned i = threadIdx.x; i < tot; i += NT) d8[i] = (uint8_t)buf[i];
+    } else {
+      const unsigned body = (tot - head) & ~3u, tail = tot - head - body;
+      if (threadIdx.x < head) d8[threadIdx.x] = (uint8_t)buf[threadIdx.x];
+      if (threadIdx.x < tail) d8[head + body + threadIdx.x] = (uint8_t)buf[head + body + threadIdx.x];
+      uint32_t* dw = reinterpret_cast<uint32_t*>(d8 + head);
+      for (unsigned i = threadIdx.x; i < body / 4; i += NT) {
+        const uint8_t* b = reinterpret_cast<const uint8_t*>(buf) + head + 4 * i;
+        dw[i] = (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+      }
+    }
     dst += tot;
     __syncthreads();
   }
