@@ -810,6 +810,8 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   if (!rc && to_host) rc = wait_stream(ctx, ctx->copy_stream);
   if (rc) return rc;
   std::memcpy(&st.sort_fallbacks, ctx->h_small.p, 8);
+  // the tile sort adds 2^40 to its statistics when a tile's bulk load did not complete
+  if (st.sort_fallbacks >> 40) return fail(ctx, KITE_ERR_TIMEOUT, "tile sort: a bulk load of a tile did not complete");
   if (dev_tiles) {
     const unsigned* hc = ctx->h_tiles.as<unsigned>();
     const unsigned long long* hs2 = reinterpret_cast<const unsigned long long*>(ctx->h_tiles.as<uint8_t>() + lhead);

@@ -140,14 +140,16 @@ struct BinSmem {
   static constexpr int ITEMS = tile_items<T>();
   static constexpr int CAP = NT * ITEMS;
   static constexpr int NW = NT / 32;
-  static constexpr size_t buf_bytes = (size_t)CAP * sizeof(T);
+  // the keys, plus 16 bytes: the bulk copy of a tile starts at the 16-byte
+  // boundary at or below its first key
+  static constexpr size_t buf_bytes = (size_t)CAP * sizeof(T) + 16;
   // bin counters; later the u16 run heads (CAP + 1 entries), or the LSD
   // fallback's per-warp digit histograms (256 * NW counters)
   static constexpr size_t head_need = ((size_t)(CAP + 1) * 2 + 15) & ~(size_t)15;
   static constexpr size_t bin_bytes = ((size_t)kBins * 2 > head_need ? (size_t)kBins * 2 : head_need) + 16;
   static constexpr size_t fbit_bytes = kBins / 8;
   static constexpr unsigned MAXLARGE = CAP / (kSmallBin + 1) + 1;  // marked bins above kSmallBin keys
-  static constexpr size_t misc_bytes = 64 * 8 + 16 + ((MAXLARGE * 2 + 15) & ~(size_t)15);
+  static constexpr size_t misc_bytes = 64 * 8 + 16 + ((MAXLARGE * 2 + 15) & ~(size_t)15) + 16;  // + mbarrier
   static constexpr size_t total = buf_bytes + bin_bytes + fbit_bytes + misc_bytes;
   static_assert((size_t)(CAP + 1) * 2 <= bin_bytes, "run heads must fit the bin area");
   static_assert((size_t)256 * NW * 4 <= bin_bytes, "LSD histograms must fit the bin area");
@@ -283,6 +285,37 @@ __device__ __forceinline__ bool warp_distinct_sort(T* buf, unsigned a, unsigned 
   return true;
 }
 
+// ---- bulk (TMA) copy of a tile's keys into shared memory, completed on an
+// mbarrier (PTX cp.async.bulk / mbarrier) ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  // earlier generic-proxy accesses to the destination come before the copy
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+// Waits for phase `parity` of the barrier, giving up after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+constexpr uint32_t kBulkWaitPolls = 1u << 18;                // a bulk copy from device memory ends long before
+constexpr unsigned long long kBulkTimeoutFlag = 1ull << 40;  // added to the sort statistics on a timeout
+
 template <class T, int MULT>
 __device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, uint32_t* __restrict__ counts,
                                           const TileDesc* __restrict__ tiles, TileOut<T>* __restrict__ tout,
@@ -297,6 +330,7 @@ __device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, ui
   unsigned* scan_sm = reinterpret_cast<unsigned*>(scan64);
   unsigned* misc = reinterpret_cast<unsigned*>(scan64 + 64);  // [0] LSD fallback, [1] large bins
   unsigned short* large = reinterpret_cast<unsigned short*>(misc + 4);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L::total - 16);
 
   const TileDesc td = tiles[tid];
   const unsigned n = td.len;
@@ -329,28 +363,31 @@ __device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, ui
     return b < (unsigned)kBins ? b : (unsigned)kBins - 1u;
   };
 
-  // ---- 1. load with the bin histogram; 2. scan, key scatter into bin order ----
+  // ---- 1. bulk load with the bin histogram; 2. scan, key scatter into bin order ----
+  // The tile's keys arrive by one bulk copy of the 16-byte aligned span that
+  // holds them (key buffers are allocated with slack past their end), while
+  // the threads clear the bins.
+  const uintptr_t ga = reinterpret_cast<uintptr_t>(g);
+  const uintptr_t s0 = ga & ~(uintptr_t)15, s1 = (ga + (uintptr_t)n * sizeof(T) + 15) & ~(uintptr_t)15;
+  const T* tk = reinterpret_cast<const T*>(sm + (ga - s0));  // the tile's keys in shared memory
+  if (threadIdx.x == 0) mbar_init(bar);
   for (int b = threadIdx.x; b < kBins / 2; b += NT) bins[b] = 0;
   for (int b = threadIdx.x; b < kBins / 32; b += NT) fbits[b] = 0;
   if (threadIdx.x < 4) misc[threadIdx.x] = 0;
   __syncthreads();
-  // kLoadBatch independent loads in flight per thread
-  for (unsigned i0 = threadIdx.x; i0 < n; i0 += NT * kLoadBatch) {
-    T v[kLoadBatch];
-#pragma unroll
-    for (int u = 0; u < kLoadBatch; ++u) {
-      const unsigned i = i0 + u * NT;
-      v[u] = i < n ? g[i] : T(0);
+  if (threadIdx.x == 0) bulk_load(sm, reinterpret_cast<const void*>(s0), (uint32_t)(s1 - s0), bar);
+  const bool arrived = mbar_wait(bar, 0, kBulkWaitPolls);
+  if (__syncthreads_or(!arrived)) {
+    // the copy did not complete: wait once more for it to leave shared memory
+    // alone, report, and leave the tile unsorted (the count then fails)
+    if (threadIdx.x == 0) {
+      mbar_wait(bar, 0, kBulkWaitPolls);
+      if (fallbacks) atomicAdd(fallbacks, kBulkTimeoutFlag);
     }
-#pragma unroll
-    for (int u = 0; u < kLoadBatch; ++u) {
-      const unsigned i = i0 + u * NT;
-      if (i < n) {
-        buf[i] = v[u];
-        bin_add(bins, bin_at(v[u]));
-      }
-    }
+    __syncthreads();
+    return;
   }
+  for (unsigned i = threadIdx.x; i < n; i += NT) bin_add(bins, bin_at(tk[i]));
   __syncthreads();
   {
     constexpr int G = kBins / 2 / (4 * NT);  // uint4 groups (8 bins each) per thread
