@@ -632,6 +632,12 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   const uint32_t NG = std::min<uint32_t>(kSortGroups, PT);
   std::vector<uint32_t> gb(NG + 1);  // first bucket of each group
   for (uint32_t g = 0; g <= NG; ++g) gb[g] = (uint32_t)((uint64_t)PT * g / NG);
+  if (NG == 8 && PT >= 64) {
+    // tapering groups (weights 6,6,6,6,6,5,3,2 of 40): the last copy to the
+    // host, which nothing overlaps, carries a twentieth of the payload
+    static const uint32_t cw[9] = {0, 6, 12, 18, 24, 30, 35, 38, 40};
+    for (uint32_t g = 0; g <= NG; ++g) gb[g] = (uint32_t)((uint64_t)PT * cw[g] / 40);
+  }
   // Oversized tiles, group by group: those sorted on chip at twice the
   // capacity (list A) and those sorted through global memory (list B).  From
   // device-made tiles the lists are made on the device (group g's entries
