@@ -100,13 +100,14 @@ __device__ __forceinline__ void smem_radix_sort(T* buf, unsigned n, int nbits, u
 
 // ---------------------------------------------------------------------------
 // Tile sort by binning.  One CTA per tile of n <= CAP keys:
-//  1. load the tile into shared memory, counting the keys per bin on the way:
+//  1. load the tile into shared memory (one bulk copy), then count the keys per bin:
 //     bin = (key - lo) >> s with 16384 bins spanning the tile's key range
 //     [lo, hi] (its splitters);
 //  2. an exclusive scan of the bin counts; then the keys themselves are
-//     scattered into bin order (re-read from global memory, where the tile
-//     still sits in L2).  Bins are key-ordered; order inside a bin is
-//     arbitrary, so every later pass reads shared memory directly;
+//     scattered into bin order (every thread first takes its keys from the
+//     staged tile into registers, so none is overwritten before it is read).
+//     Bins are key-ordered; order inside a bin is arbitrary, so every later
+//     pass reads shared memory directly;
 //  3. a bin holding more than one distinct key is found where two different
 //     neighbours share it, and marked (a shared bit per bin);
 //  4. a marked bin of at most kSmallBin keys (typically two colliding
@@ -419,16 +420,19 @@ __device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, ui
     }
   }
   __syncthreads();
-  for (unsigned i0 = threadIdx.x; i0 < n; i0 += NT * kLoadBatch) {
-    T v[kLoadBatch];
+  {
+    // every thread takes its keys from the staged tile before any is
+    // overwritten, then scatters them into bin order
+    T v[ITEMS];
 #pragma unroll
-    for (int u = 0; u < kLoadBatch; ++u) {
-      const unsigned i = i0 + u * NT;
-      v[u] = i < n ? g[i] : T(0);
+    for (int u = 0; u < ITEMS; ++u) {
+      const unsigned i = threadIdx.x + u * NT;
+      v[u] = i < n ? tk[i] : T(0);
     }
+    __syncthreads();
 #pragma unroll
-    for (int u = 0; u < kLoadBatch; ++u)
-      if (i0 + u * NT < n) buf[bin_add(bins, bin_at(v[u]))] = v[u];
+    for (int u = 0; u < ITEMS; ++u)
+      if (threadIdx.x + u * NT < n) buf[bin_add(bins, bin_at(v[u]))] = v[u];
   }
   __syncthreads();
   // bin_get(b) is now the end of bin b; its start is the end of bin b - 1 (0 for b = 0)
