@@ -43,20 +43,11 @@ METRIC = "exact k-mers/s at k=31 (canonical, 10M x 150 bp reads)"
 UNIT = "k-mers/s"
 
 
-_GENOMES = {}
-
-
 def gen_workload(n_reads: int, seed: int = 2, genome_seed: int | None = None):
     """Reads of the 10M-read workload's shape; the genome comes from
     genome_seed (default: seed), the reads from seed."""
-    from kite_gb300 import host, synth
-    gs = seed if genome_seed is None else genome_seed
-    if gs not in _GENOMES:
-        _GENOMES.clear()
-        _GENOMES[gs] = synth.genome_with_repeats(np.random.default_rng(gs), 50_000_000)
-    data = host.synth_reads(_GENOMES[gs], n_reads, READ_LEN, 0.01, 0.001, 0.5, seed=seed,
-                            threads=max(1, os.cpu_count() or 1))
-    return data
+    from kite_gb300 import synth
+    return synth.repeats_reads(n_reads, seed=seed, genome_seed=genome_seed)
 
 
 # --workload skewed: learned vs sampled splitters on skewed u128 keys: 20 Mbp
@@ -132,10 +123,10 @@ def peaks() -> tuple:
     return 6800.0, "fallback"
 
 
-def stage_bytes(st: dict, fastq_bytes: int) -> dict:
-    """Algorithmic bytes per stage for one step (w = 8-byte keys): the bytes
-    each stage must read and write at minimum, per the kernels that ran."""
-    w = 8
+def stage_bytes(st: dict, fastq_bytes: int, w: int = 8) -> dict:
+    """Algorithmic bytes per stage for one step (w = key bytes: 8 for k <= 31,
+    16 above): the bytes each stage must read and write at minimum, per the
+    kernels that ran."""
     N = st["kmers"]
     d = st["rows"]
     E = st["payload_bytes"]
@@ -147,7 +138,8 @@ def stage_bytes(st: dict, fastq_bytes: int) -> dict:
         2: ("k_bucket_scatter" if staged else "k_extract<scatter>", 2 * N * w if staged else fastq_bytes + N * w),
         3: ("k_split_hist+k_split_scatter", 3 * N * w * levels),
         4: ("k_tile_sort", N * w + d * (w + 4)),
-        5: ("k_big_tile_sort", 0),
+        # tiles above the on-chip capacity: their keys in, their rows out
+        5: ("k_big_tile_sort", st.get("big_tile_keys", 0) * w + st.get("big_tile_rows", 0) * (w + 4)),
         6: ("k_encode", d * (w + 4) + E),
     }
 
@@ -202,7 +194,11 @@ def sum_over_ranks(world, v: float) -> float:
     return float(t.item())
 
 
-def cpu_baseline(data, layout, reads_sample: int, threads: int, k: int = K, read_len: int = READ_LEN) -> dict:
+def cpu_baseline(data, layout, reads_sample: int, threads: int, k: int = K, read_len: int = READ_LEN,
+                 partitions: int = PARTITIONS) -> dict:
+    """The oracle port of the reference's count (per-thread hash-bucket
+    workers, sort, RLE, DVLE, writer) timed on the first reads_sample reads
+    (all of them when reads_sample covers the workload)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
     oracle.lib()
@@ -211,33 +207,87 @@ def cpu_baseline(data, layout, reads_sample: int, threads: int, k: int = K, read
     n = min(len(data), reads_sample * rec_len)
     sample = bytes(memoryview(data)[:n])
     workers = max(1, threads - 2)  # reader + writer threads as in the reference plan
-    r = oracle.count_buffer(sample, k, CANONICAL, PARTITIONS, workers)
+    r = oracle.count_buffer(sample, k, CANONICAL, partitions, workers)
     secs = r["ns"] / 1e9
+    what = "the whole workload" if n == len(data) else "first"
     return {"value": r["kmers"] / secs, "unit": UNIT, "cores": workers, "kind": "port",
-            "sample": f"first {reads_sample:,} reads ({n / 1e6:.0f} MB) of the workload, {workers} worker threads",
-            "seconds": secs, "kmers": r["kmers"]}
+            "sample": f"{what} {n // rec_len:,} reads ({n / 1e6:.0f} MB) of the workload, {workers} worker threads",
+            "seconds": secs, "kmers": r["kmers"], "full": n == len(data)}
+
+
+def parity_full(count_collect, data, k: int, partitions: int) -> dict:
+    """Byte comparison of the GPU's partition payloads with the oracle's
+    (orc_count_parts: the single-worker count's payload of every partition,
+    made with all host threads) on the whole workload.  count_collect(cb)
+    runs one GPU count calling cb(meta, host address, length) per partition.
+    Runs outside every timed region."""
+    import ctypes as C
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    t0 = time.perf_counter()
+    ref = oracle.count_parts(data, k, CANONICAL, partitions, os.cpu_count() or 1)
+    t_oracle = time.perf_counter() - t0
+    seen, bad = set(), []
+
+    def cb(m, addr, n):
+        p = m["partition_id"]
+        seen.add(p)
+        same = (m["row_count"] == ref.rows[p] and n == ref.bytes[p] and m["key_min"] == ref.key_min[p]
+                and m["key_max"] == ref.key_max[p])
+        if same and n:
+            a = np.frombuffer((C.c_uint8 * n).from_address(addr), dtype=np.uint8)
+            b = np.frombuffer(ref.payload(p), dtype=np.uint8)
+            same = bool(np.array_equal(a, b))
+        if not same:
+            bad.append(p)
+
+    count_collect(cb)
+    want = set(ref.nonempty())
+    ok = not bad and seen == want
+    out = {"ok": ok, "partitions_compared": len(seen), "rows": int(sum(ref.rows)), "payload_bytes": int(ref.total),
+           "kmers": int(ref.kmers), "oracle_seconds": round(t_oracle, 2),
+           "method": "GPU partition payloads (DVLE bytes, rows, key range) compared byte for byte with the "
+                     "oracle's single-worker count of the whole workload"}
+    if not ok:
+        out["mismatched_partitions"] = sorted(set(bad) | (seen ^ want))[:20]
+    ref.close()
+    return out
+
+
+REF_MAX_STEPS, REF_MAX_WARMUP = 5, 1
 
 
 def run_reference(args):
+    """The oracle port of the reference's count on the host cores, on the
+    GPU arm's whole workload (10M reads).  One step is a full count of it
+    (several seconds), so at most REF_MAX_STEPS timed steps after at most
+    REF_MAX_WARMUP warm-up steps run; the line says how many."""
     world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    reads_sample = args.ref_reads
-    data = gen_workload(reads_sample)
-    layout = None
+    reads = args.ref_reads or args.reads
+    data = gen_workload(reads)
+    steps, warmup = min(args.steps, REF_MAX_STEPS), min(args.warmup, REF_MAX_WARMUP)
     vals = []
-    for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(data, layout, reads_sample, threads)
-        if i >= args.warmup:
+    for i in range(warmup + steps):
+        cb = cpu_baseline(data, None, reads, threads)
+        if i >= warmup:
             vals.append(cb)
     v = statistics.median(c["value"] for c in vals)
     ms = statistics.median(c["seconds"] for c in vals) * 1e3
-    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+    full = vals[0]["full"] and reads == args.reads
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": steps,
+            "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": f"same shape as the GPU arm, bounded sample of {reads_sample:,} reads",
-                       "k": K, "canonical": CANONICAL, "partitions": PARTITIONS},
+            "config": {"workload": (f"the GPU arm's workload: {reads:,} x {READ_LEN} bp reads, 50 Mbp genome with "
+                                    "20% repeats, 1% subs, 0.1% N, strand 50/50; k=31 canonical")
+                       if full else f"same shape as the GPU arm, bounded sample of {reads:,} reads",
+                       "reads": reads, "k": K, "canonical": CANONICAL, "partitions": PARTITIONS,
+                       "same_config": full},
+            "steps_requested": args.steps, "warmup_requested": args.warmup,
+            "steps_note": f"one step is a full CPU count of the workload; timed steps capped at {REF_MAX_STEPS}, "
+                          f"warm-up at {REF_MAX_WARMUP}",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
                              "sample": vals[0]["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -669,7 +719,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--reads", type=int, default=10_000_000)
-    ap.add_argument("--ref-reads", type=int, default=2_000_000)
+    ap.add_argument("--ref-reads", type=int, default=0,
+                    help="reads of the CPU baseline and the reference arm (0 = the whole workload)")
+    ap.add_argument("--no-parity", action="store_true", help="skip the full-size comparison with the oracle")
     ap.add_argument("--partitions", type=int, default=PARTITIONS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-splitter-compare", action="store_true")
@@ -759,7 +811,7 @@ def main():
     value = sum_over_ranks(world, kmers * args.steps) / (ms_total / 1e3)
 
     # ---- roofline of the dominant kernel ----
-    stages = stage_bytes(st, total)
+    stages = stage_bytes(st, total, 8 if kk <= 31 else 16)
     avg_ms = {i: stage_sum[i] / args.steps for i in stages}
     dom = max(stages, key=lambda i: avg_ms[i])
     name, algo_bytes = stages[dom]
@@ -802,7 +854,7 @@ def main():
     splitters = None
     if not args.no_splitter_compare:
         cl = gpu.Counter(kk, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_LEARNED,
-                         imbalance_bound=10.0, stream=stream.cuda_stream)
+                         stream=stream.cuda_stream)
         device_step(cl)
         torch.cuda.synchronize()
 
@@ -833,6 +885,16 @@ def main():
                                  "big_tiles": stl["big_tiles"], "mlp_loss": stl["mlp_loss"],
                                  "predicted_imbalance": stl["mlp_pred_imbalance"],
                                  "used": stl["splitter_used"] == gpu.SPLIT_LEARNED}}
+
+    # ---- the whole workload's output against the oracle (untimed) ----
+    parity = None
+    if rank == 0 and not args.no_parity:
+        def count_collect(cb):
+            for (o, l), d in zip(layout, offs):
+                c.submit_device(base + d, l)
+            c.finish(collect=True, callback=cb, raw=True)
+            torch.cuda.synchronize()
+        parity = parity_full(count_collect, data, kk, args.partitions)
 
     # ---- e2e through the C ABI from pinned host memory ----
     pinned = torch.empty(total, dtype=torch.uint8).pin_memory()
@@ -879,8 +941,8 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cb = cpu_baseline(data, layout, args.ref_reads // (4 if skewed else 1), os.cpu_count() or 1, kk,
-                          SKEWED["read_len"] if skewed else READ_LEN)
+        cb = cpu_baseline(data, layout, args.ref_reads or args.reads, os.cpu_count() or 1, kk,
+                          SKEWED["read_len"] if skewed else READ_LEN, args.partitions)
         cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     if rank == 0:
@@ -906,6 +968,7 @@ def main():
                         # device stages of the end-to-end count (the first two include waiting for the copies)
                         "stage_ms": {stages[i][0]: round(e2e_parts["stage_ms"][i] / args.steps, 3) for i in stages}},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+                "parity": parity,
                 "splitters": splitters,
                 "tiles": {"tiles": st["tiles"], "per_bucket": st["tiles_per_bucket"], "big": st["big_tiles"],
                           "imbalance": st["tile_imbalance"], "sort_fallbacks": st["sort_fallbacks"]}}

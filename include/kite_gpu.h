@@ -112,6 +112,8 @@ typedef struct {
   uint32_t split_levels;             /* key-range split passes over the keys (0, 1 or 2) */
   uint32_t staged_scatter;           /* 1: keys staged by the histogram pass, then a ranked bucket scatter */
   uint32_t mlp_reused;               /* 1: the learned CDF of an earlier segment was kept (no training) */
+  uint64_t big_tile_keys;            /* keys in tiles above the on-chip capacity */
+  uint64_t big_tile_rows;            /* unique rows those tiles reduced to */
 } kite_gpu_stats;
 
 /* Merge input: one .kite file's partition table, with payloads in host memory

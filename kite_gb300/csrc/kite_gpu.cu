@@ -478,10 +478,10 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   if (S == 1) {
     for (uint32_t b = 0; b < PT; ++b) ht.push_back(TileDesc{boff[b], (uint32_t)bcount[b], b});
   } else {
-    // Splitters: SAMPLED = histogram only; LEARNED = train the CDF, keep it
-    // unless its predicted max/mean tile load exceeds imbalance_bound (then the
-    // histogram); AUTO = histogram unless its own prediction exceeds the
-    // bound, then as LEARNED.
+    // Splitters: SAMPLED = histogram only; LEARNED = train the CDF and keep
+    // it unless its predicted max/mean tile load exceeds imbalance_bound AND
+    // the histogram's prediction is lower (then the histogram); AUTO =
+    // histogram unless its own prediction exceeds the bound, then as LEARNED.
     KCU(ctx->splitters.ensure((size_t)S * sizeof(T)));
     KCU(ctx->splitters2.ensure((size_t)S * sizeof(T)));
     KCU(ctx->hist16.ensure((size_t)65536 * 4));
@@ -510,9 +510,16 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
       st.mlp_pred_imbalance = rep.pred_imbalance;
       st.mlp_reused = rep.reused ? 1u : 0u;
       learned = rep.pred_imbalance <= bound;
-      if (!learned && mode == KITE_SPLIT_LEARNED)
+      if (!learned && mode == KITE_SPLIT_LEARNED) {
         st.kernel_launches += compute_hist_splitters<T>(ctx->sample.as<T>(), nsample, 2 * k, S, hist_spl,
                                                         ctx->hist16.as<unsigned>(), s);
+        if (predict_imbalance<T>(ctx->mlp, ctx->sample.as<T>(), nsample, hist_spl, S, s, ctx->cfg.timeout_ms,
+                                 &hist_imb))
+          return fail(ctx, KITE_ERR_TIMEOUT, "splitter evaluation did not finish");
+        st.kernel_launches += 1;
+      }
+      // above the bound the network still wins when the histogram predicts worse
+      if (!learned && hist_imb >= 0.0 && rep.pred_imbalance < hist_imb) learned = true;
     }
     st.hist_pred_imbalance = hist_imb;
     st.splitter_used = learned ? KITE_SPLIT_LEARNED : KITE_SPLIT_SAMPLED;
@@ -649,18 +656,19 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   uint32_t* ids_b = ids_a + ntiles;
   unsigned* lcnt = nullptr;
   const size_t lhead = (size_t)(2 * NG + 8) * 8;  // counts, then the group bounds
-  const size_t lbytes = lhead + (size_t)(3 + S) * 8;
+  const size_t lbytes = lhead + (size_t)(4 + S) * 8;
   if (dev_tiles) {
     KCU(ctx->tile_lists.ensure(lbytes + 64));
     lcnt = ctx->tile_lists.as<unsigned>();
-    // [0] largest tile, [1] keys, [2] non-empty tiles, then the S range sums
+    // [0] largest tile, [1] keys, [2] non-empty tiles, [3] keys in tiles above
+    // capacity, then the S range sums
     unsigned long long* lstats = reinterpret_cast<unsigned long long*>(ctx->tile_lists.as<uint8_t>() + lhead);
     KCU(cudaMemsetAsync(ctx->tile_lists.p, 0, lbytes, s));
     uint32_t* dgb = reinterpret_cast<uint32_t*>(lcnt + 2 * NG);
     KCU(ctx->h_tiles.ensure(lbytes + 64));
     std::memcpy(ctx->h_tiles.p, gb.data(), (NG + 1) * 4);
     KCU(cudaMemcpyAsync(dgb, ctx->h_tiles.p, (NG + 1) * 4, cudaMemcpyHostToDevice, s));
-    launch_tile_lists(ctx->tile_fill.as<uint32_t>(), ntiles, S, dgb, NG, CAP, ids_a, ids_b, lcnt, lstats, lstats + 3,
+    launch_tile_lists(ctx->tile_fill.as<uint32_t>(), ntiles, S, dgb, NG, CAP, ids_a, ids_b, lcnt, lstats, lstats + 4,
                       s);
     st.kernel_launches += 1;
     st.tiles = ntiles;
@@ -683,6 +691,7 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
       }
     st.tiles = ntiles;
     st.big_tiles = (uint32_t)big.size();
+    for (uint32_t t : big) st.big_tile_keys += ht[t].len;
     st.tile_imbalance = tne ? (double)tmax / ((double)tsum / (double)tne) : 0.0;
     st.range_imbalance = 1.0;  // one tile per bucket
     KCU(ctx->h_tiles.ensure(ht.size() * sizeof(TileDesc) + big.size() * 4 + 64));
@@ -699,8 +708,8 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, ctx->cfg.device);
   const uint32_t walk_grid = (uint32_t)std::max(1, sm_count);
   KCU(ctx->tile_out.ensure((size_t)ntiles * sizeof(TileOut<T>)));
-  KCU(ctx->sort_stats.ensure(8));
-  KCU(cudaMemsetAsync(ctx->sort_stats.p, 0, 8, s));
+  KCU(ctx->sort_stats.ensure(16));
+  KCU(cudaMemsetAsync(ctx->sort_stats.p, 0, 16, s));
   KCU(ctx->tile_boff.ensure((size_t)ntiles * 8));
   KCU(ctx->tile_prev.ensure((size_t)ntiles * sizeof(T)));
   KCU(ctx->meta.ensure((size_t)PT * sizeof(BucketMeta)));
@@ -731,14 +740,15 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
                                 lcnt + 2 * g, tout, ctx->sort_stats.as<unsigned long long>(),
                                 TileRanges<T>{tile_spl, Sl, 0, kmax}, s);
       launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(), ids_b + t0,
-                              walk_grid, lcnt + 2 * g + 1, tout, ctx->status.as<DevStatus>(), s);
+                              walk_grid, lcnt + 2 * g + 1, tout, ctx->status.as<DevStatus>(),
+                              ctx->sort_stats.as<unsigned long long>(), s);
     } else {
       launch_tile_sort_large<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ids_a + gbig[g],
                                 glarge[g], nullptr, tout, ctx->sort_stats.as<unsigned long long>(),
                                 TileRanges<T>{tile_spl, Sl, 0, kmax}, s);
       launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(),
                               ids_a + gbig[g] + glarge[g], gbig[g + 1] - gbig[g] - glarge[g], nullptr, tout,
-                              ctx->status.as<DevStatus>(), s);
+                              ctx->status.as<DevStatus>(), ctx->sort_stats.as<unsigned long long>(), s);
     }
     cudaEventRecord(gev[8 * g + 2], s);
     // ---- K5: per-bucket tile links, byte offsets from the group's start
@@ -810,12 +820,13 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     total_bytes += gbytes;
   }
   KCU(cudaEventRecord(ctx->ev[7], s));
-  KCU(cudaMemcpyAsync(ctx->h_small.p, ctx->sort_stats.p, 8, cudaMemcpyDeviceToHost, s));
+  KCU(cudaMemcpyAsync(ctx->h_small.p, ctx->sort_stats.p, 16, cudaMemcpyDeviceToHost, s));
   if (dev_tiles) KCU(cudaMemcpyAsync(ctx->h_tiles.p, ctx->tile_lists.p, lbytes, cudaMemcpyDeviceToHost, s));
   rc = wait_stream(ctx, s);
   if (!rc && to_host) rc = wait_stream(ctx, ctx->copy_stream);
   if (rc) return rc;
   std::memcpy(&st.sort_fallbacks, ctx->h_small.p, 8);
+  std::memcpy(&st.big_tile_rows, ctx->h_small.as<uint8_t>() + 8, 8);
   // the tile sort adds 2^40 to its statistics when a tile's bulk load did not complete
   if (st.sort_fallbacks >> 40) return fail(ctx, KITE_ERR_TIMEOUT, "tile sort: a bulk load of a tile did not complete");
   if (dev_tiles) {
@@ -826,7 +837,8 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     st.big_tiles = nbig;
     st.tile_imbalance = hs2[2] ? (double)hs2[0] / ((double)hs2[1] / (double)hs2[2]) : 0.0;
     unsigned long long rmax = 0;
-    for (uint32_t t = 0; t < S; ++t) rmax = std::max(rmax, hs2[3 + t]);
+    for (uint32_t t = 0; t < S; ++t) rmax = std::max(rmax, hs2[4 + t]);
+    st.big_tile_keys = hs2[3];
     st.range_imbalance = (double)rmax / ((double)N / S);
   }
   rc = check_status(ctx, "count");

@@ -179,7 +179,9 @@ struct TileRanges {
   T kmax;
 };
 
-// `fallbacks` (device counter) counts tiles that took the LSD fallback.
+// `fallbacks` (device counters): [0] tiles that took the LSD fallback (plus
+// 2^40 for a tile whose bulk load did not complete), [1] rows of the tiles
+// above the on-chip capacity (double-capacity and global-memory sorts).
 template <class T>
 void launch_tile_sort(T* keys, uint32_t* counts, const TileDesc* tiles, uint32_t ntiles, TileOut<T>* out,
                       unsigned long long* fallbacks, TileRanges<T> rg, cudaStream_t s);
@@ -192,10 +194,11 @@ void launch_tile_sort_large(T* keys, uint32_t* counts, const TileDesc* tiles, co
                             TileRanges<T> rg, cudaStream_t s);
 // Oversized tiles (more keys than 2 * tile_capacity): one CTA per tile, LSD
 // passes through global memory with `scratch` (>= largest tile keys); with
-// nbig_dev as above.
+// nbig_dev as above; sort_stats[1] gains the rows they make.
 template <class T>
 void launch_big_tile_sort(T* keys, uint32_t* counts, T* scratch, const TileDesc* tiles, const uint32_t* big_ids,
-                          uint32_t nbig, const unsigned* nbig_dev, TileOut<T>* out, DevStatus* st, cudaStream_t s);
+                          uint32_t nbig, const unsigned* nbig_dev, TileOut<T>* out, DevStatus* st,
+                          unsigned long long* sort_stats, cudaStream_t s);
 // Per bucket group, the tiles above capacity (lists and counts on the
 // device) and the tile statistics; see k_tile_lists.
 void launch_tile_lists(const uint32_t* lens, uint32_t ntiles, uint32_t S, const uint32_t* gb, uint32_t NG,

@@ -1,23 +1,41 @@
-// Learned CDF over the k-mer key space: a small FP32 MLP trained on the GPU
-// by hand-written forward / backward / Adam kernels, then inverted into
+// Learned CDF over the k-mer key space: a small FP32 network trained on the
+// GPU by hand-written forward / backward / Adam kernels, then inverted into
 // tile splitters.  No counterpart in the reference: it only moves tile
 // boundaries, so counts stay exact whatever it predicts.
 //
-// Model.  Let V(key) be the top 48 of the 2k key bits; its top 16 bits are the
-// key's bin b, the next 32 bits its place inside the bin.  With C(b) and m(b)
-// the sample counts below and inside bin b (from the sample histogram),
-//     F(key) = ( C(b) + m(b) * g(V(key)) ) / n
-// where g is the MLP: 48 features in {0,1} -> 64 ReLU -> 64 ReLU -> 1.  The
-// histogram places the mass of every bin; the network learns how that mass is
-// spread inside a bin, which is what a histogram cannot resolve when one bin
-// holds more than a tile's share of keys (low-complexity, AT-rich k-mers).
-// Loss = mean over the sample of (F_hat - rank/n)^2, i.e. the global CDF
-// error, so heavy bins dominate training.
+// Key view.  V(key) = the top 48 of the 2k key bits (zero-padded below for
+// k < 24), bits x_0 (most significant) .. x_47.  The top 16 bits are the
+// key's bin b.
 //
-// Splitter j: the bin holding quantile j/S from the histogram, then a
-// bit-by-bit search of g inside the bin for the within-bin target.  The
-// predicted max/mean tile load of the sample decides between these splitters
-// and the histogram ones.
+// Model: a two-stage learned index over V.
+//  Stage 1 (counts of the counter's key sample, up to 2^22 keys of the
+//   segment's first chunk): C(b), m(b) = sample keys below / inside bin b;
+//   every heavy bin (more than a quarter of a tile's share of the sample)
+//   also gets counts of its 256 sub-cells (the next 8 bits).
+//  Stage 2 (the network): an autoregressive density over the bits below the
+//   bin: for each bit i >= 16 it predicts P(x_i = 1 | x_0 .. x_{i-1}).  The
+//   network is a masked MLP (48 inputs -> 64 ReLU -> 64 ReLU -> 32 logits):
+//   hidden unit k has degree d(k) = 16 + k/2 and sees only inputs i < d(k)
+//   (first layer) or first-layer units of degree <= d(k) (second layer), and
+//   output o (bit 16 + o) sees only second-layer units of degree <= 16 + o,
+//   so each output depends on the bits above its own (Germain et al., MADE,
+//   2015).  The within-cell CDF it defines,
+//       g(V) = sum over set bits i of V below the cell of
+//              P(prefix x_0..x_{i-1}) * P(x_i = 0 | prefix)  / P(cell),
+//   is monotone in V by construction (it is the distribution function of a
+//   proper distribution over the bits), and it inverts exactly by
+//   arithmetic decoding, bit by bit.
+//  F(key) = (C(b) [+ the sub-cell counts below, heavy bins] + m * g(V)) / n.
+// Training: maximum likelihood (binary cross-entropy of every bit i >= 16
+// given the bits above it) over the whole sample, minibatches of 8192 keys,
+// Adam.  The training steps are captured once as a CUDA graph (the step
+// counter lives on the device) and replayed.
+//
+// Splitter j: the bin (and heavy bins' sub-cell) holding quantile j/S of the
+// sample from the stage-1 counts, then the bits below it decoded from the
+// network's conditionals so that g reaches the quantile's within-cell
+// fraction.  The predicted max/mean tile load of the sample decides between
+// these splitters and the histogram ones.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -29,32 +47,56 @@
 
 namespace kite {
 
-static constexpr int kIn = 48, kH = 64;
-static constexpr int kBinBits = 16, kSubBits = 32;
-static constexpr uint32_t kTrainRows = 1u << 20;  // training rows taken from the sorted key sample
-static constexpr int kParams = kIn * kH + kH + kH * kH + kH + kH + 1;
+static constexpr int kIn = 48, kH = 64, kB0 = 16, kOut = kIn - kB0;  // 32 predicted bits
+static constexpr int kBinBits = 16;
+static constexpr int kSubBits = 8;           // sub-cells of a heavy bin
+static constexpr int kSubCells = 1 << kSubBits;
+static constexpr int kParams = kIn * kH + kH + kH * kH + kH + kOut * kH + kOut;
+static constexpr uint32_t kBatch = 8192;
+static constexpr int kTrainSteps = 4000;
+static constexpr int kStepsPerGraph = 50;
+static constexpr float kLr = 3e-3f;
 
-// parameter offsets
+// parameter offsets: W1 [kH][kIn], b1, W2 [kH][kH], b2, W3 [kOut][kH], b3
 static constexpr int oW1 = 0, oB1 = oW1 + kIn * kH, oW2 = oB1 + kH, oB2 = oW2 + kH * kH, oW3 = oB2 + kH,
-                     oB3 = oW3 + kH;
+                     oB3 = oW3 + kOut * kH;
+
+// Degrees and masks.  Hidden unit k (either layer) has degree 16 + k/2.
+__host__ __device__ constexpr int deg_of(int k) { return kB0 + k / 2; }
+// first layer: unit j sees inputs i < deg(j)
+__host__ __device__ constexpr int w1_inputs(int j) { return deg_of(j); }
+// second layer: unit k sees first-layer units j with deg(j) <= deg(k), i.e. j <= (k | 1)
+__host__ __device__ constexpr int w2_inputs(int k) { return (k | 1) + 1; }
+// output o (bit 16 + o) sees second-layer units k with deg(k) <= 16 + o, i.e. k < 2o + 2
+__host__ __device__ constexpr int w3_inputs(int o) { return 2 * o + 2 < kH ? 2 * o + 2 : kH; }
+__host__ __device__ constexpr bool param_live(int p) {
+  return p < oB1   ? (p % kIn) < w1_inputs(p / kIn)
+         : p < oW2 ? true
+         : p < oB2 ? ((p - oW2) % kH) < w2_inputs((p - oW2) / kH)
+         : p < oW3 ? true
+         : p < oB3 ? ((p - oW3) % kH) < w3_inputs((p - oW3) / kH)
+                   : true;
+}
 
 struct MlpModel {
   float* params = nullptr;  // device
   float* grads = nullptr;
   float* m = nullptr;
   float* v = nullptr;
-  float* feats = nullptr;   // [n, kIn]
-  float* target = nullptr;  // [n] within-bin fraction
-  float* scale = nullptr;   // [n] m(b)/n
-  float* loss = nullptr;    // [1]
-  uint32_t cap = 0;
-  void* keys_sorted = nullptr;
-  size_t keys_cap = 0;
+  float* loss = nullptr;     // [0] running sum of the step, [1] last step's loss
+  unsigned* step = nullptr;  // training step counter (device)
+  uint64_t* views = nullptr; // 48-bit views of the sample keys
+  uint32_t views_cap = 0;
   unsigned* tile_hits = nullptr;
   uint32_t tile_cap = 0;
-  uint32_t* batch_idx = nullptr;
-  unsigned* hist = nullptr;   // [65536] sample histogram, then inclusive cumulative
-  unsigned* hist2 = nullptr;  // [65536] the same over the sorted training subset
+  unsigned* hist = nullptr;      // [65536] sample counts per bin, then inclusive cumulative
+  int* heavy_idx = nullptr;      // [65536] heavy-bin slot or -1
+  unsigned* sub = nullptr;       // [heavy slots][256] sub-cell counts, then inclusive cumulative
+  unsigned* nheavy = nullptr;    // [1]
+  uint32_t sub_cap = 0;          // heavy slots allocated
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  uint32_t graph_n = 0;          // the sample size the graph was captured for
   float last_loss = 0;
   double last_pred_imbalance = 0;
   bool trained = false;
@@ -65,19 +107,20 @@ MlpModel* mlp_create() { return new MlpModel(); }
 
 void mlp_destroy(MlpModel* m) {
   if (!m) return;
+  if (m->graph) cudaGraphExecDestroy(m->graph);
+  if (m->cap_stream) cudaStreamDestroy(m->cap_stream);
   cudaFree(m->params);
   cudaFree(m->grads);
   cudaFree(m->m);
   cudaFree(m->v);
-  cudaFree(m->feats);
-  cudaFree(m->target);
-  cudaFree(m->scale);
   cudaFree(m->loss);
-  cudaFree(m->keys_sorted);
+  cudaFree(m->step);
+  cudaFree(m->views);
   cudaFree(m->tile_hits);
-  cudaFree(m->batch_idx);
   cudaFree(m->hist);
-  cudaFree(m->hist2);
+  cudaFree(m->heavy_idx);
+  cudaFree(m->sub);
+  cudaFree(m->nheavy);
   delete m;
 }
 
@@ -86,11 +129,59 @@ template <class T>
 __device__ __forceinline__ uint64_t view48(T key, uint32_t key_bits) {
   return key_bits >= 48 ? (uint64_t)(key >> (key_bits - 48)) : ((uint64_t)key << (48 - key_bits));
 }
+__device__ __forceinline__ float bit_of(uint64_t v, int i) { return (float)((v >> (kIn - 1 - i)) & 1ull); }
 
+// ---- stage 1 ----------------------------------------------------------------
 template <class T>
-__global__ void k_bin_hist(const T* __restrict__ keys, uint32_t n, uint32_t key_bits, unsigned* __restrict__ hist) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) atomicAdd(&hist[(uint32_t)(view48(keys[i], key_bits) >> kSubBits)], 1u);
+__global__ void k_views(const T* __restrict__ keys, uint32_t n, uint32_t key_bits, uint64_t* __restrict__ views,
+                        unsigned* __restrict__ hist) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint64_t v = view48(keys[i], key_bits);
+    views[i] = v;
+    atomicAdd(&hist[(uint32_t)(v >> (kIn - kBinBits))], 1u);
+  }
+}
+
+// Heavy bins (count > thr) get a slot; the rest -1.  Slots beyond `cap` are
+// not given (those bins are treated as light).
+__global__ void k_heavy(const unsigned* __restrict__ hist, unsigned thr, uint32_t cap, int* __restrict__ heavy_idx,
+                        unsigned* __restrict__ nheavy) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= (1u << kBinBits)) return;
+  int slot = -1;
+  if (hist[b] > thr) {
+    const unsigned s = atomicAdd(nheavy, 1u);
+    if (s < cap) slot = (int)s;
+  }
+  heavy_idx[b] = slot;
+}
+
+__global__ void k_sub_hist(const uint64_t* __restrict__ views, uint32_t n, const int* __restrict__ heavy_idx,
+                           unsigned* __restrict__ sub) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint64_t v = views[i];
+    const int h = heavy_idx[(uint32_t)(v >> (kIn - kBinBits))];
+    if (h >= 0) atomicAdd(&sub[(size_t)h * kSubCells + (uint32_t)((v >> (kIn - kBinBits - kSubBits)) & (kSubCells - 1))], 1u);
+  }
+}
+
+// inclusive cumulative counts of every heavy slot's sub-cells: one warp each
+__global__ void k_sub_cum(unsigned* __restrict__ sub, const unsigned* __restrict__ nheavy, uint32_t cap) {
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x & 31;
+  const uint32_t nh = min(*nheavy, cap);
+  if (w >= nh) return;
+  unsigned* c = sub + (size_t)w * kSubCells;
+  unsigned carry = 0;
+  for (int b0 = 0; b0 < kSubCells; b0 += 32) {
+    unsigned x = c[b0 + lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= (uint32_t)o) x += y;
+    }
+    c[b0 + lane] = x + carry;
+    carry += __shfl_sync(0xffffffffu, x, 31);
+  }
 }
 
 // inclusive cumulative counts, one CTA
@@ -106,106 +197,114 @@ __global__ void __launch_bounds__(1024) k_cum(unsigned* __restrict__ h) {
   }
 }
 
-// Training rows from every `stride`-th key of the sorted sample of n keys:
-// row j describes key i = j * stride (its rank among the n keys).
-template <class T>
-__global__ void k_make_features(const T* __restrict__ sorted, uint32_t n, uint32_t rows, uint32_t stride,
-                                uint32_t key_bits, const unsigned* __restrict__ cum, float* __restrict__ feats,
-                                float* __restrict__ target, float* __restrict__ scale) {
-  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= rows) return;
-  const uint32_t i = j * stride;
-  const uint64_t v = view48(sorted[i], key_bits);
-  const uint32_t b = (uint32_t)(v >> kSubBits);
-  const unsigned hi = cum[b], lo = b ? cum[b - 1] : 0u;
-  const float m = (float)(hi - lo);
-  float* f = feats + (size_t)j * kIn;
-#pragma unroll
-  for (int q = 0; q < kIn; ++q) f[q] = (float)((v >> (kIn - 1 - q)) & 1ull);
-  target[j] = ((float)(i - lo) + 0.5f) / m;
-  scale[j] = m / (float)n;
-}
-
 // ---- forward + backward ------------------------------------------------------
-// One CTA handles kB samples: forward per sample (activations kept in shared
-// memory, feature-major with a padded stride so lanes hit distinct banks),
-// then weight-parallel gradient sums over the CTA's samples (no atomics
-// inside the CTA), one global atomicAdd per parameter per CTA.
-// Per-sample loss: (scale * (y - target))^2 / batch (scale = 1 without array).
+// One CTA handles kB samples (one per thread): the forward pass per sample
+// with activations kept in shared memory (feature-major, padded stride), then
+// weight-parallel gradient sums over the CTA's samples (live weights only;
+// masked ones stay zero), one global atomicAdd per weight per CTA.
+// Loss = mean over the batch and the 32 predicted bits of the binary
+// cross-entropy.  Sample s of the batch is views[idx(s)], idx either given
+// (idx != null) or the strided walk of training step *step.
 static constexpr int kB = 128;        // samples per CTA (== threads)
 static constexpr int kLd = kB + 1;    // padded row stride
-static constexpr size_t kFbSmem = (size_t)(kParams + kIn * kLd + 3 * kH * kLd + kB) * sizeof(float);
+static constexpr size_t kFbSmem = (size_t)(kParams + kIn * kLd + 3 * kH * kLd + kOut * kLd) * sizeof(float);
 
-__global__ void __launch_bounds__(kB) k_fwd_bwd(const float* __restrict__ params, const float* __restrict__ feats,
-                                                const float* __restrict__ target, const float* __restrict__ scale,
-                                                const uint32_t* __restrict__ idx, uint32_t batch,
+__global__ void __launch_bounds__(kB) k_fwd_bwd(const float* __restrict__ params, const uint64_t* __restrict__ views,
+                                                const uint32_t* __restrict__ idx, const unsigned* __restrict__ step,
+                                                uint32_t n, uint32_t stride, uint32_t batch,
                                                 float* __restrict__ grads, float* __restrict__ loss) {
   extern __shared__ float sm[];
-  float* P = sm;                       // parameters
-  float* X = P + kParams;              // [kIn][kLd]
-  float* H1 = X + kIn * kLd;           // [kH][kLd]  (relu output)
-  float* H2 = H1 + kH * kLd;           // [kH][kLd]
-  float* D = H2 + kH * kLd;            // [kH][kLd]  reused: d2 then d1 (pre-activation grads)
-  float* DY = D + kH * kLd;            // [kB]
+  float* P = sm;                      // parameters
+  float* X = P + kParams;             // [kIn][kLd]
+  float* H1 = X + kIn * kLd;          // [kH][kLd]  relu outputs
+  float* H2 = H1 + kH * kLd;          // [kH][kLd]
+  float* D = H2 + kH * kLd;           // [kH][kLd]  pre-activation gradients: layer 2, then layer 1
+  float* DY = D + kH * kLd;           // [kOut][kLd] logit gradients
   const int t = threadIdx.x;
   for (int i = t; i < kParams; i += kB) P[i] = params[i];
   const uint32_t b = blockIdx.x * kB + t;
   const bool live = b < batch;
-  const uint32_t s = live ? idx[b] : 0;
-  for (int i = 0; i < kIn; ++i) X[i * kLd + t] = live ? feats[(size_t)s * kIn + i] : 0.f;
+  uint32_t s = 0;
+  if (live) {
+    if (idx) s = idx[b];
+    else s = (uint32_t)((((uint64_t)(*step) * batch + b) % n) * (uint64_t)stride % n);
+  }
+  const uint64_t v = live ? views[s] : 0ull;
+  for (int i = 0; i < kIn; ++i) X[i * kLd + t] = bit_of(v, i);
   __syncthreads();
   for (int j = 0; j < kH; ++j) {
     float a = P[oB1 + j];
-    for (int i = 0; i < kIn; ++i) a += P[oW1 + j * kIn + i] * X[i * kLd + t];
+    for (int i = 0; i < w1_inputs(j); ++i) a += P[oW1 + j * kIn + i] * X[i * kLd + t];
     H1[j * kLd + t] = a > 0.f ? a : 0.f;
   }
-  float y = P[oB3];
-  for (int j = 0; j < kH; ++j) {
-    float a = P[oB2 + j];
-    for (int i = 0; i < kH; ++i) a += P[oW2 + j * kH + i] * H1[i * kLd + t];
-    const float h = a > 0.f ? a : 0.f;
-    H2[j * kLd + t] = h;
-    y += P[oW3 + j] * h;
+  for (int k = 0; k < kH; ++k) {
+    float a = P[oB2 + k];
+    for (int j = 0; j < w2_inputs(k); ++j) a += P[oW2 + k * kH + j] * H1[j * kLd + t];
+    H2[k * kLd + t] = a > 0.f ? a : 0.f;
   }
-  const float sc = live ? (scale ? scale[s] : 1.f) : 0.f;
-  const float e = live ? sc * (y - target[s]) : 0.f;
-  const float dy = live ? 2.f * e * sc / (float)batch : 0.f;
-  DY[t] = dy;
-  for (int j = 0; j < kH; ++j) D[j * kLd + t] = H2[j * kLd + t] > 0.f ? dy * P[oW3 + j] : 0.f;
+  const float inv = live ? 1.f / ((float)batch * (float)kOut) : 0.f;
+  float l = 0.f;
+  for (int o = 0; o < kOut; ++o) {
+    float a = P[oB3 + o];
+    for (int k = 0; k < w3_inputs(o); ++k) a += P[oW3 + o * kH + k] * H2[k * kLd + t];
+    const float x = X[(kB0 + o) * kLd + t];
+    const float p = 1.f / (1.f + __expf(-a));
+    DY[o * kLd + t] = (p - x) * inv;
+    // binary cross-entropy from the logit: max(a, 0) - x a + log(1 + e^-|a|)
+    l += (fmaxf(a, 0.f) - x * a + log1pf(__expf(-fabsf(a)))) * inv;
+  }
+  for (int k = 0; k < kH; ++k) {
+    float g = 0.f;
+    for (int o = k / 2; o < kOut; ++o) g += DY[o * kLd + t] * P[oW3 + o * kH + k];
+    D[k * kLd + t] = H2[k * kLd + t] > 0.f ? g : 0.f;
+  }
   __syncthreads();
-  for (int w = t; w < kH * kH + kH + kH + 1; w += kB) {
+  // second and third layer gradients
+  for (int w = t; w < kH * kH + kH + kOut * kH + kOut; w += kB) {
     float g = 0.f;
     if (w < kH * kH) {
-      const int j = w / kH, i = w % kH;
-      for (int q = 0; q < kB; ++q) g += D[j * kLd + q] * H1[i * kLd + q];
+      const int k = w / kH, j = w % kH;
+      if (j >= w2_inputs(k)) continue;
+      for (int q = 0; q < kB; ++q) g += D[k * kLd + q] * H1[j * kLd + q];
       atomicAdd(&grads[oW2 + w], g);
     } else if (w < kH * kH + kH) {
-      const int j = w - kH * kH;
-      for (int q = 0; q < kB; ++q) g += D[j * kLd + q];
-      atomicAdd(&grads[oB2 + j], g);
-    } else if (w < kH * kH + 2 * kH) {
-      const int j = w - kH * kH - kH;
-      for (int q = 0; q < kB; ++q) g += DY[q] * H2[j * kLd + q];
-      atomicAdd(&grads[oW3 + j], g);
+      const int k = w - kH * kH;
+      for (int q = 0; q < kB; ++q) g += D[k * kLd + q];
+      atomicAdd(&grads[oB2 + k], g);
+    } else if (w < kH * kH + kH + kOut * kH) {
+      const int r = w - kH * kH - kH, o = r / kH, k = r % kH;
+      if (k >= w3_inputs(o)) continue;
+      for (int q = 0; q < kB; ++q) g += DY[o * kLd + q] * H2[k * kLd + q];
+      atomicAdd(&grads[oW3 + r], g);
     } else {
-      for (int q = 0; q < kB; ++q) g += DY[q];
-      atomicAdd(&grads[oB3], g);
+      const int o = w - kH * kH - kH - kOut * kH;
+      for (int q = 0; q < kB; ++q) g += DY[o * kLd + q];
+      atomicAdd(&grads[oB3 + o], g);
     }
   }
+  // first layer pre-activation gradients (D is rewritten after every thread
+  // has used the second layer's)
   float d1[kH];
-  for (int i = 0; i < kH; ++i) d1[i] = 0.f;
-  for (int j = 0; j < kH; ++j) {
-    const float dj = D[j * kLd + t];
-    if (dj != 0.f)
-      for (int i = 0; i < kH; ++i) d1[i] += dj * P[oW2 + j * kH + i];
+#pragma unroll
+  for (int j = 0; j < kH; ++j) d1[j] = 0.f;
+  for (int k = 0; k < kH; ++k) {
+    const float dk = D[k * kLd + t];
+    const int lim = w2_inputs(k);
+    if (dk != 0.f) {
+#pragma unroll
+      for (int j = 0; j < kH; ++j)
+        if (j < lim) d1[j] += dk * P[oW2 + k * kH + j];
+    }
   }
   __syncthreads();
-  for (int i = 0; i < kH; ++i) D[i * kLd + t] = H1[i * kLd + t] > 0.f ? d1[i] : 0.f;
+#pragma unroll
+  for (int j = 0; j < kH; ++j) D[j * kLd + t] = H1[j * kLd + t] > 0.f ? d1[j] : 0.f;
   __syncthreads();
   for (int w = t; w < kIn * kH + kH; w += kB) {
     float g = 0.f;
     if (w < kIn * kH) {
       const int j = w / kIn, i = w % kIn;
+      if (i >= w1_inputs(j)) continue;
       for (int q = 0; q < kB; ++q) g += D[j * kLd + q] * X[i * kLd + q];
       atomicAdd(&grads[oW1 + w], g);
     } else {
@@ -214,97 +313,132 @@ __global__ void __launch_bounds__(kB) k_fwd_bwd(const float* __restrict__ params
       atomicAdd(&grads[oB1 + j], g);
     }
   }
-  float l = e * e / (float)batch;
   for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
   if ((t & 31) == 0 && l != 0.f) atomicAdd(loss, l);
 }
 
-__global__ void k_adam(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
-                       float lr, float b1, float b2, float eps, float c1, float c2) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= kParams) return;
-  const float gi = g[i];
-  const float mi = b1 * m[i] + (1.f - b1) * gi;
-  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
-  m[i] = mi;
-  v[i] = vi;
-  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
-  g[i] = 0.f;
+// Adam step of the whole parameter vector by one CTA: the step number, the
+// learning rate schedule (halved after half the steps, x0.2 after three
+// quarters) and the bias corrections come from the device step counter,
+// which the CTA then advances; the step's loss moves to loss[1].
+__global__ void __launch_bounds__(1024) k_adam(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m,
+                                               float* __restrict__ v, unsigned* __restrict__ step,
+                                               float* __restrict__ loss, uint32_t total_steps, float lr0) {
+  const unsigned t = *step;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float c1 = 1.f - powf(b1, (float)(t + 1)), c2 = 1.f - powf(b2, (float)(t + 1));
+  const float lr = lr0 * (t > total_steps * 3 / 4 ? 0.2f : (t > total_steps / 2 ? 0.5f : 1.0f));
+  for (int i = threadIdx.x; i < kParams; i += blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    g[i] = 0.f;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *step = t + 1;
+    loss[1] = loss[0];
+    loss[0] = 0.f;
+  }
 }
 
-// Batch indices: a strided walk (stride coprime to n) over the sample.
-__global__ void k_batch_idx(uint32_t* idx, uint32_t batch, uint32_t n, uint32_t start, uint32_t stride) {
-  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < batch) idx[b] = (uint32_t)(((uint64_t)(start + b) * stride) % n);
-}
-
-// One warp per splitter j: bin from the cumulative histogram, then the
-// largest 32-bit sub-position whose predicted within-bin fraction stays below
-// the target; the splitter is the first key of the next 48-bit cell.  Lane l
-// holds hidden units l and l + 32 (weights transposed in shared memory so the
-// lanes read consecutive words); every sum runs over its inputs in index
-// order, one fused multiply-add at a time, so each lane's arithmetic is that of
-// a plain sequential forward pass.
+// ---- inversion ---------------------------------------------------------------
+// One warp per splitter j: the bin holding sample rank q = n j / S from the
+// cumulative counts; for a heavy bin also its sub-cell; then the remaining
+// bits decoded from the network: with the interval [lo, lo + P) of the
+// within-cell fraction covered by the current prefix, bit i is 0 when the
+// target u < lo + P * P(x_i = 0 | prefix).  Lane l holds hidden units l and
+// l + 32; sums run over their inputs in index order.  The splitter is the
+// first key of the next 48-bit cell.
 template <class T>
 __global__ void __launch_bounds__(256) k_invert(const float* __restrict__ params, const unsigned* __restrict__ cum,
+                                                const int* __restrict__ heavy_idx, const unsigned* __restrict__ sub,
                                                 uint32_t n, uint32_t S, uint32_t key_bits, T* __restrict__ spl) {
-  extern __shared__ float P[];  // W1 as [input][hidden], W2 as [input][output]; biases and w3 as given
+  extern __shared__ float P[];  // W1 as [input][hidden], W2 as [input][output]; the rest as given
   for (int i = threadIdx.x; i < kParams; i += blockDim.x) {
-    float v = params[i];
     int at = i;
-    if (i < oB1) at = oW1 + (i % kIn) * kH + i / kIn;                        // W1[j][i] -> [i][j]
-    else if (i >= oW2 && i < oB2) at = oW2 + ((i - oW2) % kH) * kH + (i - oW2) / kH;  // W2[j][i] -> [i][j]
-    P[at] = v;
+    if (i < oB1) at = oW1 + (i % kIn) * kH + i / kIn;                                   // W1[j][i] -> [i][j]
+    else if (i >= oW2 && i < oB2) at = oW2 + ((i - oW2) % kH) * kH + (i - oW2) / kH;   // W2[k][j] -> [j][k]
+    P[at] = params[i];
   }
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) / 32 + 1;
   if (j >= S) return;
   const double q = (double)n * j / S;  // sample rank at the cut
-  uint32_t lo = 0, hi = (1u << kBinBits) - 1;
-  while (lo < hi) {  // first bin whose inclusive cumulative count exceeds q
-    const uint32_t mid = (lo + hi) >> 1;
-    if ((double)cum[mid] > q) hi = mid;
-    else lo = mid + 1;
+  uint32_t lo_b = 0, hi_b = (1u << kBinBits) - 1;
+  while (lo_b < hi_b) {  // first bin whose inclusive cumulative count exceeds q
+    const uint32_t mid = (lo_b + hi_b) >> 1;
+    if ((double)cum[mid] > q) hi_b = mid;
+    else lo_b = mid + 1;
   }
-  const uint32_t b = lo;
-  const double below = b ? cum[b - 1] : 0.0, mass = (double)cum[b] - below;
-  const float u = mass > 0 ? (float)((q - below) / mass) : 1.f;
-  uint32_t sub = 0;
-  for (int bit = kSubBits - 1; bit >= 0; --bit) {
-    const uint32_t cand = sub | (1u << bit);
-    const uint64_t v = ((uint64_t)b << kSubBits) | cand;
+  const uint32_t b = lo_b;
+  double below = b ? cum[b - 1] : 0.0, mass = (double)cum[b] - below;
+  uint64_t v = (uint64_t)b << (kIn - kBinBits);
+  int first = kB0;
+  const int h = heavy_idx[b];
+  if (h >= 0 && mass > 0) {
+    const unsigned* c = sub + (size_t)h * kSubCells;
+    const double r = q - below;
+    uint32_t a = 0, e = kSubCells - 1;
+    while (a < e) {
+      const uint32_t mid = (a + e) >> 1;
+      if ((double)c[mid] > r) e = mid;
+      else a = mid + 1;
+    }
+    const double sb = a ? c[a - 1] : 0.0;
+    below += sb;
+    mass = (double)c[a] - sb;
+    v |= (uint64_t)a << (kIn - kBinBits - kSubBits);
+    first = kB0 + kSubBits;
+  }
+  const double u = mass > 0 ? (q - below) / mass : 1.0;
+  double lo = 0.0, width = 1.0;
+  for (int i = first; i < kIn; ++i) {
+    // forward pass of the prefix v (bits below i are zero and unseen by output i)
     float a0 = P[oB1 + lane], a1 = P[oB1 + lane + 32];
-#pragma unroll
-    for (int i = 0; i < kIn; ++i) {
-      const float xi = (float)((v >> (kIn - 1 - i)) & 1ull);
-      a0 += P[oW1 + i * kH + lane] * xi;
-      a1 += P[oW1 + i * kH + lane + 32] * xi;
+    for (int x = 0; x < w1_inputs((int)lane + 32) && x < i; ++x) {
+      const float xi = bit_of(v, x);
+      if (x < w1_inputs((int)lane)) a0 += P[oW1 + x * kH + lane] * xi;
+      a1 += P[oW1 + x * kH + lane + 32] * xi;
     }
     const float h0 = a0 > 0.f ? a0 : 0.f, h1 = a1 > 0.f ? a1 : 0.f;
     float c0 = P[oB2 + lane], c1 = P[oB2 + lane + 32];
-#pragma unroll 8
-    for (int i = 0; i < 32; ++i) {
-      const float hv = __shfl_sync(0xffffffffu, h0, i);
-      c0 += P[oW2 + i * kH + lane] * hv;
-      c1 += P[oW2 + i * kH + lane + 32] * hv;
+    for (int x = 0; x < 32; ++x) {
+      const float hv = __shfl_sync(0xffffffffu, h0, x);
+      if (x < w2_inputs((int)lane)) c0 += P[oW2 + x * kH + lane] * hv;
+      c1 += P[oW2 + x * kH + lane + 32] * hv;  // every first-layer unit x < 32 is below lane + 32's limit
     }
-#pragma unroll 8
-    for (int i = 0; i < 32; ++i) {
-      const float hv = __shfl_sync(0xffffffffu, h1, i);
-      c0 += P[oW2 + (i + 32) * kH + lane] * hv;
-      c1 += P[oW2 + (i + 32) * kH + lane + 32] * hv;
+    for (int x = 0; x < 32; ++x) {
+      const float hv = __shfl_sync(0xffffffffu, h1, x);
+      if (x + 32 < w2_inputs((int)lane + 32)) c1 += P[oW2 + (x + 32) * kH + lane + 32] * hv;
     }
     const float r0 = c0 > 0.f ? c0 : 0.f, r1 = c1 > 0.f ? c1 : 0.f;
-    float y = P[oB3];
-#pragma unroll 8
-    for (int i = 0; i < 32; ++i) y += P[oW3 + i] * __shfl_sync(0xffffffffu, r0, i);
-#pragma unroll 8
-    for (int i = 0; i < 32; ++i) y += P[oW3 + 32 + i] * __shfl_sync(0xffffffffu, r1, i);
-    if (y <= u) sub = cand;
+    const int o = i - kB0;
+    float y = 0.f;
+    for (int x = 0; x < 32; ++x) {
+      const float a = __shfl_sync(0xffffffffu, r0, x);
+      if (x < w3_inputs(o)) y += P[oW3 + o * kH + x] * a;
+    }
+    for (int x = 0; x < 32; ++x) {
+      const float a = __shfl_sync(0xffffffffu, r1, x);
+      if (x + 32 < w3_inputs(o)) y += P[oW3 + o * kH + x + 32] * a;
+    }
+    y += P[oB3 + o];
+    const double p0 = width * (1.0 / (1.0 + exp((double)y)));  // P(bit 0) share of the interval
+    if (u >= lo + p0) {
+      v |= 1ull << (kIn - 1 - i);
+      lo += p0;
+      width -= p0;
+    } else {
+      width = p0;
+    }
   }
   if (lane != 0) return;
-  const uint64_t cell = (((uint64_t)b << kSubBits) | sub) + 1;  // first cell above
+  const uint64_t cell = v + 1;  // first cell above
   T s;
   if (key_bits >= 48) {
     s = cell >= (1ull << 48) ? ((key_bits == (uint32_t)KeyTraits<T>::kBits) ? ~T(0) : (T(1) << key_bits) - T(1))
@@ -375,54 +509,6 @@ static size_t splitter_sort_smem(uint32_t n) {
   return bytes;
 }
 
-// Bitonic sort of the sample in device memory (padded to a power of two
-// with the all-ones key, which sorts last and is dropped).
-template <class T>
-__global__ void k_pad(T* keys, const T* src, uint32_t n, uint32_t np2) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < np2) keys[i] = i < n ? src[i] : ~T(0);
-}
-
-template <class T>
-__global__ void k_bitonic_step(T* keys, uint32_t np2, uint32_t j, uint32_t k) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= np2) return;
-  const uint32_t l = i ^ j;
-  if (l <= i) return;
-  const T a = keys[i], b = keys[l];
-  const bool up = (i & k) == 0;
-  if ((a > b) == up) {
-    keys[i] = b;
-    keys[l] = a;
-  }
-}
-
-namespace {
-
-template <class T>
-int sort_sample(MlpModel* m, const T* d_sample, uint32_t n, cudaStream_t s, T** out) {
-  uint32_t np2 = 1, launches = 1;
-  while (np2 < n) np2 <<= 1;
-  const size_t bytes = (size_t)np2 * sizeof(T);
-  if (m->keys_cap < bytes) {
-    cudaFree(m->keys_sorted);
-    if (cudaMalloc(&m->keys_sorted, bytes) != cudaSuccess) return -1;
-    m->keys_cap = bytes;
-  }
-  T* keys = static_cast<T*>(m->keys_sorted);
-  const uint32_t blocks = (np2 + 255) / 256;
-  k_pad<T><<<blocks, 256, 0, s>>>(keys, d_sample, n, np2);
-  for (uint32_t k = 2; k <= np2; k <<= 1)
-    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-      k_bitonic_step<T><<<blocks, 256, 0, s>>>(keys, np2, j, k);
-      launches++;
-    }
-  *out = keys;
-  return (int)launches;
-}
-
-}  // namespace
-
 template <class T>
 int predict_imbalance(MlpModel* m, const T* d_sample, uint32_t n, const T* d_spl, uint32_t S, cudaStream_t s,
                       uint32_t timeout_ms, double* out) {
@@ -434,7 +520,10 @@ int predict_imbalance(MlpModel* m, const T* d_sample, uint32_t n, const T* d_spl
     m->tile_cap = S;
   }
   cudaMemsetAsync(m->tile_hits, 0, (size_t)S * 4, s);
-  const uint32_t grid = std::min<uint32_t>((n + 255) / 256, 4 * 152);
+  int sms = 152;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const uint32_t grid = std::min<uint32_t>((n + 255) / 256, 4 * (uint32_t)std::max(sms, 1));
   k_tile_hits<T><<<grid, 256, (size_t)S * 4, s>>>(d_sample, n, d_spl, S, m->tile_hits);
   std::vector<unsigned> h(S);
   cudaMemcpyAsync(h.data(), m->tile_hits, (size_t)S * 4, cudaMemcpyDeviceToHost, s);
@@ -449,8 +538,107 @@ template int predict_imbalance<uint64_t>(MlpModel*, const uint64_t*, uint32_t, c
 template int predict_imbalance<u128>(MlpModel*, const u128*, uint32_t, const u128*, uint32_t, cudaStream_t,
                                      uint32_t, double*);
 
-int mlp_train(MlpModel* m, uint32_t n, int steps, uint32_t batch, float lr, cudaStream_t s, uint32_t timeout_ms,
-              float* final_loss, int* launches);
+namespace {
+
+uint32_t coprime_stride(uint32_t n) {
+  auto gcd = [](uint32_t a, uint32_t b) {
+    while (b) {
+      const uint32_t t = a % b;
+      a = b;
+      b = t;
+    }
+    return a;
+  };
+  uint32_t stride = 2654435761u % n;
+  if (stride == 0) stride = 1;
+  while (gcd(stride, n) != 1) stride++;
+  return stride;
+}
+
+// Initial parameters (fixed seed): He-scaled normal weights for the hidden
+// layers, small output weights, zero biases; masked weights are zero and stay
+// zero (their gradients are never formed).
+std::vector<float> initial_params() {
+  std::vector<float> p(kParams, 0.f);
+  uint64_t st = 0x2545F4914F6CDD1Dull;
+  auto uni = [&]() {
+    st = st * 6364136223846793005ull + 1442695040888963407ull;
+    return ((double)(st >> 11) + 0.5) / 9007199254740992.0;
+  };
+  auto normal = [&]() { return std::sqrt(-2.0 * std::log(uni())) * std::cos(6.283185307179586 * uni()); };
+  for (int i = 0; i < oB1; ++i) p[oW1 + i] = (float)(normal() * std::sqrt(2.0 / kIn));
+  for (int i = 0; i < kH * kH; ++i) p[oW2 + i] = (float)(normal() * std::sqrt(2.0 / kH));
+  for (int i = 0; i < kOut * kH; ++i) p[oW3 + i] = (float)(normal() * 0.01);
+  for (int i = 0; i < kParams; ++i)
+    if (!param_live(i)) p[i] = 0.f;
+  return p;
+}
+
+int ensure_training_buffers(MlpModel* m) {
+  if (m->params) return 0;
+  if (cudaMalloc(&m->params, kParams * sizeof(float)) != cudaSuccess) return 1;
+  if (cudaMalloc(&m->grads, kParams * sizeof(float)) != cudaSuccess) return 1;
+  if (cudaMalloc(&m->m, kParams * sizeof(float)) != cudaSuccess) return 1;
+  if (cudaMalloc(&m->v, kParams * sizeof(float)) != cudaSuccess) return 1;
+  if (cudaMalloc(&m->loss, 2 * sizeof(float)) != cudaSuccess) return 1;
+  if (cudaMalloc(&m->step, sizeof(unsigned)) != cudaSuccess) return 1;
+  return 0;
+}
+
+// kStepsPerGraph training steps (forward/backward + Adam each) captured as a
+// graph on the model's own stream, for a sample of n views.
+int capture_steps(MlpModel* m, uint32_t n) {
+  if (m->graph && m->graph_n == n) return 0;
+  if (m->graph) {
+    cudaGraphExecDestroy(m->graph);
+    m->graph = nullptr;
+  }
+  if (!m->cap_stream && cudaStreamCreateWithFlags(&m->cap_stream, cudaStreamNonBlocking) != cudaSuccess) return 1;
+  const uint32_t batch = std::min(kBatch, n);
+  const uint32_t stride = coprime_stride(n);
+  cudaFuncSetAttribute(k_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFbSmem);
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(m->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return 1;
+  for (int i = 0; i < kStepsPerGraph; ++i) {
+    k_fwd_bwd<<<(batch + kB - 1) / kB, kB, kFbSmem, m->cap_stream>>>(m->params, m->views, nullptr, m->step, n,
+                                                                      stride, batch, m->grads, m->loss);
+    k_adam<<<1, 1024, 0, m->cap_stream>>>(m->params, m->grads, m->m, m->v, m->step, m->loss, kTrainSteps, kLr);
+  }
+  if (cudaStreamEndCapture(m->cap_stream, &g) != cudaSuccess) return 1;
+  const cudaError_t e = cudaGraphInstantiate(&m->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    m->graph = nullptr;
+    return 1;
+  }
+  m->graph_n = n;
+  return 0;
+}
+
+// Trains from the initial parameters on the n views; returns the number of
+// graph launches + setup copies, or -1 on failure.
+int train(MlpModel* m, uint32_t n, cudaStream_t s, uint32_t timeout_ms, float* final_loss) {
+  if (ensure_training_buffers(m) || capture_steps(m, n)) return -1;
+  const std::vector<float> p = initial_params();
+  cudaMemcpyAsync(m->params, p.data(), kParams * sizeof(float), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(m->grads, 0, kParams * sizeof(float), s);
+  cudaMemsetAsync(m->m, 0, kParams * sizeof(float), s);
+  cudaMemsetAsync(m->v, 0, kParams * sizeof(float), s);
+  cudaMemsetAsync(m->loss, 0, 2 * sizeof(float), s);
+  cudaMemsetAsync(m->step, 0, sizeof(unsigned), s);
+  int launches = 0;
+  for (int i = 0; i < kTrainSteps; i += kStepsPerGraph) {
+    if (cudaGraphLaunch(m->graph, s) != cudaSuccess) return -1;
+    launches++;
+  }
+  float l[2] = {0.f, 0.f};
+  cudaMemcpyAsync(l, m->loss, sizeof l, cudaMemcpyDeviceToHost, s);
+  if (bounded_sync(s, timeout_ms)) return -1;
+  if (final_loss) *final_loss = l[1];
+  return launches;
+}
+
+}  // namespace
 
 template <class T>
 int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits, uint32_t S, T* d_spl,
@@ -458,18 +646,48 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
   *rep = MlpReport{};
   rep->pred_imbalance = 1e30;
   if (!m || n < 4 * S || n < 1024) return 0;  // too few samples to learn from
+  // ---- stage 1: bin counts and heavy bins' sub-cell counts of the sample
+  const uint32_t heavy_cap = 4 * S + 4;  // bins above a quarter tile: at most 4 S of them
   if (!m->hist && cudaMalloc(&m->hist, sizeof(unsigned) << kBinBits) != cudaSuccess) return 1;
-  if (!m->hist2 && cudaMalloc(&m->hist2, sizeof(unsigned) << kBinBits) != cudaSuccess) return 1;
-  // cumulative bin histogram of the whole sample (its order does not matter)
+  if (!m->heavy_idx && cudaMalloc(&m->heavy_idx, sizeof(int) << kBinBits) != cudaSuccess) return 1;
+  if (!m->nheavy && cudaMalloc(&m->nheavy, sizeof(unsigned)) != cudaSuccess) return 1;
+  if (m->sub_cap < heavy_cap) {
+    cudaFree(m->sub);
+    m->sub = nullptr;
+    m->sub_cap = 0;
+    if (cudaMalloc(&m->sub, (size_t)heavy_cap * kSubCells * sizeof(unsigned)) != cudaSuccess) return 1;
+    m->sub_cap = heavy_cap;
+  }
+  if (m->views_cap < n) {
+    cudaFree(m->views);
+    m->views = nullptr;
+    m->views_cap = 0;
+    if (m->graph) {  // the captured steps read the old buffer
+      cudaGraphExecDestroy(m->graph);
+      m->graph = nullptr;
+    }
+    if (cudaMalloc(&m->views, (size_t)n * sizeof(uint64_t)) != cudaSuccess) return 1;
+    m->views_cap = n;
+  }
+  int sms = 152, dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const uint32_t grid = std::min<uint32_t>((n + 255) / 256, 8 * (uint32_t)std::max(sms, 1));
   cudaMemsetAsync(m->hist, 0, sizeof(unsigned) << kBinBits, s);
-  k_bin_hist<T><<<(n + 255) / 256, 256, 0, s>>>(d_sample, n, key_bits, m->hist);
+  cudaMemsetAsync(m->nheavy, 0, sizeof(unsigned), s);
+  cudaMemsetAsync(m->sub, 0, (size_t)heavy_cap * kSubCells * sizeof(unsigned), s);
+  k_views<T><<<grid, 256, 0, s>>>(d_sample, n, key_bits, m->views, m->hist);
+  const unsigned thr = (unsigned)((double)n / (4.0 * S));
+  k_heavy<<<(1u << kBinBits) / 256, 256, 0, s>>>(m->hist, thr, heavy_cap, m->heavy_idx, m->nheavy);
+  k_sub_hist<<<grid, 256, 0, s>>>(m->views, n, m->heavy_idx, m->sub);
+  k_sub_cum<<<(heavy_cap * 32 + 255) / 256, 256, 0, s>>>(m->sub, m->nheavy, heavy_cap);
   k_cum<<<1, 1024, 0, s>>>(m->hist);
-  rep->launches += 2;
+  rep->launches += 5;
   const size_t smem = kParams * sizeof(float);
   cudaFuncSetAttribute(k_invert<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const uint32_t inv_grid = (uint32_t)(((size_t)(S - 1) * 32 + 255) / 256);
   if (m->trained && m->trained_key_bits == key_bits) {
-    // the within-bin shape learned on an earlier segment, over this sample's histogram
-    k_invert<T><<<(uint32_t)(((size_t)(S - 1) * 32 + 255) / 256), 256, smem, s>>>(m->params, m->hist, n, S, key_bits, d_spl);
+    // the bit conditionals learned on an earlier segment, over this sample's counts
+    k_invert<T><<<inv_grid, 256, smem, s>>>(m->params, m->hist, m->heavy_idx, m->sub, n, S, key_bits, d_spl);
     k_sort_splitters<T><<<1, 1024, splitter_sort_smem<T>(S - 1), s>>>(d_spl, S - 1);
     rep->launches += 3;
     double pred = 0;
@@ -481,33 +699,11 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
       return cudaGetLastError() == cudaSuccess ? 0 : 1;
     }
   }
-  // training rows: the within-bin ranks of a sorted subset of at most
-  // kTrainRows keys (the sample fills in no particular order)
-  const uint32_t rows = n < kTrainRows ? n : kTrainRows;
-  T* sorted = nullptr;
-  const int sl = sort_sample<T>(m, d_sample, rows, s, &sorted);
-  if (sl < 0) return 1;
-  rep->launches += sl;
-  if (m->cap < rows) {
-    cudaFree(m->feats);
-    cudaFree(m->target);
-    cudaFree(m->scale);
-    if (cudaMalloc(&m->feats, (size_t)rows * kIn * sizeof(float)) != cudaSuccess) return 1;
-    if (cudaMalloc(&m->target, (size_t)rows * sizeof(float)) != cudaSuccess) return 1;
-    if (cudaMalloc(&m->scale, (size_t)rows * sizeof(float)) != cudaSuccess) return 1;
-    m->cap = rows;
-  }
-  cudaMemsetAsync(m->hist2, 0, sizeof(unsigned) << kBinBits, s);
-  k_bin_hist<T><<<(rows + 255) / 256, 256, 0, s>>>(sorted, rows, key_bits, m->hist2);
-  k_cum<<<1, 1024, 0, s>>>(m->hist2);
-  k_make_features<T><<<(rows + 255) / 256, 256, 0, s>>>(sorted, rows, rows, 1, key_bits, m->hist2, m->feats,
-                                                         m->target, m->scale);
-  rep->launches += 3;
-  const int steps = 400;
-  int tl = 0;
-  if (mlp_train(m, rows, steps, 8192, 2e-3f, s, timeout_ms, &rep->loss, &tl)) return 1;
+  // ---- stage 2: train the network on every sample key
+  const int tl = train(m, n, s, timeout_ms, &rep->loss);
+  if (tl < 0) return 1;
   rep->launches += tl;
-  k_invert<T><<<(uint32_t)(((size_t)(S - 1) * 32 + 255) / 256), 256, smem, s>>>(m->params, m->hist, n, S, key_bits, d_spl);
+  k_invert<T><<<inv_grid, 256, smem, s>>>(m->params, m->hist, m->heavy_idx, m->sub, n, S, key_bits, d_spl);
   k_sort_splitters<T><<<1, 1024, splitter_sort_smem<T>(S - 1), s>>>(d_spl, S - 1);
   rep->launches += 2;
   if (predict_imbalance<T>(m, d_sample, n, d_spl, S, s, timeout_ms, &rep->pred_imbalance)) return 1;
@@ -523,101 +719,40 @@ template int mlp_splitters<uint64_t>(MlpModel*, const uint64_t*, uint32_t, uint3
 template int mlp_splitters<u128>(MlpModel*, const u128*, uint32_t, uint32_t, uint32_t, u128*, cudaStream_t, uint32_t,
                                  MlpReport*);
 
-// Trains on m->feats / m->target / m->scale (n samples) with Adam; fixed init.
-int mlp_train(MlpModel* m, uint32_t n, int steps, uint32_t batch, float lr, cudaStream_t s, uint32_t timeout_ms,
-              float* final_loss, int* launches) {
-  if (!m->params) {
-    if (cudaMalloc(&m->params, kParams * sizeof(float)) != cudaSuccess) return 1;
-    cudaMalloc(&m->grads, kParams * sizeof(float));
-    cudaMalloc(&m->m, kParams * sizeof(float));
-    cudaMalloc(&m->v, kParams * sizeof(float));
-    cudaMalloc(&m->loss, sizeof(float) * 2);
-    cudaMalloc(&m->batch_idx, (size_t)65536 * 4);
-  }
-  std::vector<float> p(kParams, 0.f);
-  uint64_t st = 0x2545F4914F6CDD1Dull;
-  auto rnd = [&]() {
-    st = st * 6364136223846793005ull + 1442695040888963407ull;
-    return ((double)(st >> 11) / 9007199254740992.0) * 2.0 - 1.0;
-  };
-  for (int i = 0; i < kIn * kH; ++i) p[oW1 + i] = (float)(rnd() * std::sqrt(6.0 / kIn));
-  for (int i = 0; i < kH * kH; ++i) p[oW2 + i] = (float)(rnd() * std::sqrt(6.0 / kH));
-  for (int i = 0; i < kH; ++i) p[oW3 + i] = (float)(rnd() * std::sqrt(3.0 / kH));
-  for (int i = 0; i < kH; ++i) p[oB1 + i] = 0.01f;
-  for (int i = 0; i < kH; ++i) p[oB2 + i] = 0.01f;
-  p[oB3] = 0.5f;
-  cudaMemcpyAsync(m->params, p.data(), kParams * sizeof(float), cudaMemcpyHostToDevice, s);
-  cudaMemsetAsync(m->grads, 0, kParams * sizeof(float), s);
-  cudaMemsetAsync(m->m, 0, kParams * sizeof(float), s);
-  cudaMemsetAsync(m->v, 0, kParams * sizeof(float), s);
-  batch = std::min(std::min(batch, n), 65536u);
-  auto gcd = [](uint32_t a, uint32_t b) {
-    while (b) {
-      uint32_t t = a % b;
-      a = b;
-      b = t;
-    }
-    return a;
-  };
-  uint32_t stride = 2654435761u % n;
-  if (stride == 0) stride = 1;
-  while (gcd(stride, n) != 1) stride++;
-  cudaFuncSetAttribute(k_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFbSmem);
-  const float b1 = 0.9f, b2 = 0.999f;
-  double c1 = 1, c2 = 1;
-  for (int t = 0; t < steps; ++t) {
-    k_batch_idx<<<(batch + 255) / 256, 256, 0, s>>>(m->batch_idx, batch, n, (uint32_t)((uint64_t)t * batch % n),
-                                                    stride);
-    cudaMemsetAsync(m->loss, 0, sizeof(float), s);
-    k_fwd_bwd<<<(batch + kB - 1) / kB, kB, kFbSmem, s>>>(m->params, m->feats, m->target, m->scale, m->batch_idx,
-                                                        batch, m->grads, m->loss);
-    c1 *= b1;
-    c2 *= b2;
-    const float decay = t > steps * 3 / 4 ? 0.2f : (t > steps / 2 ? 0.5f : 1.0f);
-    k_adam<<<(kParams + 255) / 256, 256, 0, s>>>(m->params, m->grads, m->m, m->v, lr * decay, b1, b2, 1e-8f,
-                                                 (float)(1 - c1), (float)(1 - c2));
-  }
-  *launches = 3 * steps;
-  float l = 0;
-  cudaMemcpyAsync(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost, s);
-  if (bounded_sync(s, timeout_ms)) return 1;
-  if (final_loss) *final_loss = l;
-  return cudaGetLastError() == cudaSuccess ? 0 : 1;
-}
-
 }  // namespace kite
 
 // ---- test hooks (C ABI, no counterpart in the reference) -------------------------
-// One forward + backward of the learned-CDF network over n samples (unit
-// scale) against a given parameter vector, so tests can check the
-// hand-written gradients against a CPU float64 reference.
-extern "C" int kite_mlp_grad_check(const float* params, const float* feats, const float* target, uint32_t n,
-                                   float* grads_out, float* loss_out) {
+// One forward + backward of the learned-CDF network over n keys' 48-bit views
+// against a given parameter vector (masked weights must be zero), so tests
+// can check the hand-written gradients against a CPU float64 reference.
+// Returns 0, or -1 on a CUDA failure.
+extern "C" int kite_mlp_grad_check(const float* params, const uint64_t* views, uint32_t n, float* grads_out,
+                                   float* loss_out) {
   using namespace kite;
-  float *dp, *df, *dt, *dg, *dl;
-  uint32_t* di;
-  cudaMalloc(&dp, kParams * 4);
-  cudaMalloc(&df, (size_t)n * kIn * 4);
-  cudaMalloc(&dt, (size_t)n * 4);
-  cudaMalloc(&dg, kParams * 4);
-  cudaMalloc(&dl, 4);
-  cudaMalloc(&di, (size_t)n * 4);
-  std::vector<uint32_t> id(n);
-  for (uint32_t i = 0; i < n; ++i) id[i] = i;
-  cudaMemcpy(dp, params, kParams * 4, cudaMemcpyHostToDevice);
-  cudaMemcpy(df, feats, (size_t)n * kIn * 4, cudaMemcpyHostToDevice);
-  cudaMemcpy(dt, target, (size_t)n * 4, cudaMemcpyHostToDevice);
-  cudaMemcpy(di, id.data(), (size_t)n * 4, cudaMemcpyHostToDevice);
-  cudaMemset(dg, 0, kParams * 4);
-  cudaMemset(dl, 0, 4);
-  cudaFuncSetAttribute(k_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFbSmem);
-  k_fwd_bwd<<<(n + kB - 1) / kB, kB, kFbSmem>>>(dp, df, dt, nullptr, di, n, dg, dl);
-  cudaError_t e = cudaDeviceSynchronize();
-  cudaMemcpy(grads_out, dg, kParams * 4, cudaMemcpyDeviceToHost);
-  cudaMemcpy(loss_out, dl, 4, cudaMemcpyDeviceToHost);
+  float *dp = nullptr, *dg = nullptr, *dl = nullptr;
+  uint64_t* dv = nullptr;
+  uint32_t* di = nullptr;
+  cudaError_t e = cudaMalloc(&dp, kParams * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dv, (size_t)n * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&dg, kParams * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dl, 4);
+  if (e == cudaSuccess) e = cudaMalloc(&di, (size_t)n * 4);
+  if (e == cudaSuccess) {
+    std::vector<uint32_t> id(n);
+    for (uint32_t i = 0; i < n; ++i) id[i] = i;
+    cudaMemcpy(dp, params, kParams * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(dv, views, (size_t)n * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(di, id.data(), (size_t)n * 4, cudaMemcpyHostToDevice);
+    cudaMemset(dg, 0, kParams * 4);
+    cudaMemset(dl, 0, 4);
+    cudaFuncSetAttribute(k_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFbSmem);
+    k_fwd_bwd<<<(n + kB - 1) / kB, kB, kFbSmem>>>(dp, dv, di, nullptr, n, 1, n, dg, dl);
+    e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(grads_out, dg, kParams * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(loss_out, dl, 4, cudaMemcpyDeviceToHost);
+  }
   cudaFree(dp);
-  cudaFree(df);
-  cudaFree(dt);
+  cudaFree(dv);
   cudaFree(dg);
   cudaFree(dl);
   cudaFree(di);

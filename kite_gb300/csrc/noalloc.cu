@@ -20,7 +20,9 @@
 //    between them) race and corrupt each other's results: serialise them.
 //  * the first call on a device looks the array's address up with
 //    cudaGetSymbolAddress (which also loads this module on that device); make
-//    that first call before any stream capture begins.
+//    that first call before any stream capture begins.  The address is kept
+//    with the id of the device's context and looked up again when a new
+//    context replaces it (after cudaDeviceReset, for example).
 //  * the call returns once the work has finished, waiting at most timeout_ms.
 //
 // The kernels are a small-input variant of the context path: one pass finds
@@ -35,6 +37,8 @@
 #include <cstring>
 #include <mutex>
 #include <thread>
+#include <tuple>
+#include <utility>
 
 #include "kite_gpu.h"
 #include "kite_internal.h"
@@ -453,21 +457,82 @@ __global__ void __launch_bounds__(256) k_emit(uint8_t* scr, uint32_t P, T* __res
   }
 }
 
+// Per device: the scratch array's address and the SM count, and the CUDA
+// context they belong to.  A context that is destroyed and made again (for
+// example after cudaDeviceReset) loads this module afresh, so its array can
+// sit elsewhere: the entry is looked up again whenever the device's current
+// context has another id.
+struct DeviceEntry {
+  unsigned long long ctx_id = 0;
+  uint8_t* scratch = nullptr;
+  uint32_t sms = 0;
+};
 std::mutex g_mu;
-uint8_t* g_scratch[kMaxDevices];
+DeviceEntry g_dev[kMaxDevices];
 
-// Address of this device's scratch array; looked up on the device's first
-// call with that device current.
-int scratch_of(int device, uint8_t** out) {
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+// Id of the calling thread's current context (0 when it cannot be had).
+unsigned long long current_ctx_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  }
+  if (!get_current || !get_id) return 0;
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+// Address of this device's scratch array and its SM count, with that device
+// current: looked up on the first call in each context of the device (on
+// every call when the context id is unavailable).
+int device_entry(int device, uint8_t** scratch, uint32_t* sms) {
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch[device]) {
+  DeviceEntry& d = g_dev[device];
+  const unsigned long long id = current_ctx_id();
+  if (!d.scratch || id == 0 || id != d.ctx_id) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || p == nullptr) return KITE_ERR_CUDA;
-    g_scratch[device] = static_cast<uint8_t*>(p);
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || n < 1)
+      return KITE_ERR_CUDA;
+    d.scratch = static_cast<uint8_t*>(p);
+    d.sms = (uint32_t)n;
+    d.ctx_id = id;
   }
-  *out = g_scratch[device];
+  *scratch = d.scratch;
+  *sms = d.sms;
   return KITE_OK;
+}
+
+// Launches kernel f and returns the error of this launch alone (a launch
+// error the caller had left pending is neither reported nor cleared).
+template <class... KArgs, class... Args, size_t... I>
+cudaError_t launch_impl(void (*f)(KArgs...), dim3 g, dim3 b, cudaStream_t s, std::index_sequence<I...>,
+                        Args... args) {
+  std::tuple<KArgs...> t(static_cast<KArgs>(args)...);
+  void* p[sizeof...(KArgs) + 1] = {static_cast<void*>(&std::get<I>(t))...};
+  return cudaLaunchKernel(reinterpret_cast<const void*>(f), g, b, p, 0, s);
+}
+template <class... KArgs, class... Args>
+cudaError_t launch(void (*f)(KArgs...), dim3 g, dim3 b, cudaStream_t s, Args... args) {
+  static_assert(sizeof...(KArgs) == sizeof...(Args), "kernel argument count");
+  return launch_impl(f, g, b, s, std::index_sequence_for<KArgs...>{}, args...);
 }
 
 // Polls the stream until its work is done; no event or other object is made.
@@ -483,9 +548,9 @@ int wait_idle(cudaStream_t s, uint32_t timeout_ms) {
 }
 
 template <class T>
-int run(uint8_t* scr, uint32_t k, bool canonical, uint32_t P, const uint8_t* d_fastq, uint32_t len, void* d_keys,
-        uint32_t* d_counts, uint64_t max_rows, uint32_t* d_part_rows, uint64_t* totals, cudaStream_t s,
-        uint32_t timeout_ms) {
+int run(uint8_t* scr, uint32_t sms, uint32_t k, bool canonical, uint32_t P, const uint8_t* d_fastq, uint32_t len,
+        void* d_keys, uint32_t* d_counts, uint64_t max_rows, uint32_t* d_part_rows, uint64_t* totals,
+        cudaStream_t s, uint32_t timeout_ms) {
   // What accumulates across threads starts at zero on every call.
   if (cudaMemsetAsync(scr + kOffBucketCount, 0, (size_t)P * 4, s) != cudaSuccess ||
       cudaMemsetAsync(scr + kOffBucketFill, 0, (size_t)P * 4, s) != cudaSuccess ||
@@ -495,18 +560,24 @@ int run(uint8_t* scr, uint32_t k, bool canonical, uint32_t P, const uint8_t* d_f
   while ((1u << log2p) < P) ++log2p;
   const uint32_t shift = 64 - log2p;
   const uint32_t max_pieces = len / 4 + 2 + len / kPiece;
-  const uint32_t g_pieces = std::min<uint32_t>((max_pieces + 255) / 256, 4 * 152);
-  const uint32_t g_keys = std::min<uint32_t>(std::max<uint32_t>(len, 1) / 256 + 1, 4 * 152);
-  k_lines<<<1, 1024, 0, s>>>(d_fastq, len, scr);
-  k_extract<T><<<g_pieces, 256, 0, s>>>(d_fastq, k, canonical ? 1u : 0u, shift, scr);
-  k_scan<<<1, 1024, 0, s>>>(reinterpret_cast<uint32_t*>(scr + kOffBucketCount), P,
-                            reinterpret_cast<uint32_t*>(scr + kOffBucketOff));
-  k_scatter<T><<<g_keys, 256, 0, s>>>(shift, scr);
-  k_sort_rle<T><<<P, kSortThreads, 0, s>>>(scr);
-  k_scan<<<1, 1024, 0, s>>>(reinterpret_cast<uint32_t*>(scr + kOffBucketRows), P,
-                            reinterpret_cast<uint32_t*>(scr + kOffRowOff));
-  k_emit<T><<<P, 256, 0, s>>>(scr, P, static_cast<T*>(d_keys), d_counts, max_rows, d_part_rows);
-  if (cudaGetLastError() != cudaSuccess) return KITE_ERR_CUDA;
+  // grid-stride kernels: four CTAs per SM at most
+  const uint32_t g_pieces = std::min<uint32_t>((max_pieces + 255) / 256, 4 * sms);
+  const uint32_t g_keys = std::min<uint32_t>(std::max<uint32_t>(len, 1) / 256 + 1, 4 * sms);
+  uint32_t* const bucket_count = reinterpret_cast<uint32_t*>(scr + kOffBucketCount);
+  uint32_t* const bucket_off = reinterpret_cast<uint32_t*>(scr + kOffBucketOff);
+  uint32_t* const bucket_rows = reinterpret_cast<uint32_t*>(scr + kOffBucketRows);
+  uint32_t* const row_off = reinterpret_cast<uint32_t*>(scr + kOffRowOff);
+  const cudaError_t le[7] = {
+      launch(k_lines, 1, 1024, s, d_fastq, len, scr),
+      launch(k_extract<T>, g_pieces, 256, s, d_fastq, k, canonical ? 1u : 0u, shift, scr),
+      launch(k_scan, 1, 1024, s, bucket_count, P, bucket_off),
+      launch(k_scatter<T>, g_keys, 256, s, shift, scr),
+      launch(k_sort_rle<T>, P, kSortThreads, s, scr),
+      launch(k_scan, 1, 1024, s, bucket_rows, P, row_off),
+      launch(k_emit<T>, P, 256, s, scr, P, static_cast<T*>(d_keys), d_counts, (unsigned long long)max_rows,
+             d_part_rows)};
+  for (const cudaError_t e : le)
+    if (e != cudaSuccess) return KITE_ERR_CUDA;
   int rc = wait_idle(s, timeout_ms);
   if (rc) return rc;
   Counters hc;
@@ -541,16 +612,19 @@ extern "C" int kite_gpu_count_rows_noalloc(int device, int k, int canonical, uin
   if (len > kMaxBytes) return KITE_ERR_UNSUPPORTED;
   int prev = 0;
   if (cudaGetDevice(&prev) != cudaSuccess) return KITE_ERR_CUDA;
-  if (prev != device && cudaSetDevice(device) != cudaSuccess) return KITE_ERR_CUDA;
+  // with the device current its primary context is initialised, so the
+  // context id below is that of the context the kernels will run in
+  if (cudaSetDevice(device) != cudaSuccess) return KITE_ERR_CUDA;
   uint8_t* scr = nullptr;
-  int rc = scratch_of(device, &scr);
+  uint32_t sms = 0;
+  int rc = device_entry(device, &scr, &sms);
   if (rc == KITE_OK) {
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
     const uint32_t t = timeout_ms ? timeout_ms : 600000u;
-    rc = k <= 31 ? run<uint64_t>(scr, (uint32_t)k, canonical != 0, partitions, d_fastq, (uint32_t)len, d_keys,
-                                 d_counts, max_rows, d_partition_rows, totals, s, t)
-                 : run<u128>(scr, (uint32_t)k, canonical != 0, partitions, d_fastq, (uint32_t)len, d_keys, d_counts,
-                             max_rows, d_partition_rows, totals, s, t);
+    rc = k <= 31 ? run<uint64_t>(scr, sms, (uint32_t)k, canonical != 0, partitions, d_fastq, (uint32_t)len,
+                                 d_keys, d_counts, max_rows, d_partition_rows, totals, s, t)
+                 : run<u128>(scr, sms, (uint32_t)k, canonical != 0, partitions, d_fastq, (uint32_t)len, d_keys,
+                             d_counts, max_rows, d_partition_rows, totals, s, t);
   }
   if (prev != device) cudaSetDevice(prev);
   return rc;

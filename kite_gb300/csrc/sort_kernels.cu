@@ -541,6 +541,7 @@ __device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, ui
   unsigned long long rest_total;
   block_exclusive_scan<NT, unsigned long long>(rest, scan64, &rest_total);
   if (threadIdx.x == 0) {
+    if (MULT > 1 && fallbacks) atomicAdd(&fallbacks[1], (unsigned long long)U);  // rows of tiles above capacity
     TileOut<T> o;
     o.first_key = buf[head[0]];
     o.first_count = (unsigned)head[1] - head[0];
@@ -610,7 +611,8 @@ template void launch_tile_sort_large<u128>(u128*, uint32_t*, const TileDesc*, co
 template <class T>
 __device__ __forceinline__ void big_sort_tile(uint32_t tid, T* __restrict__ keys, uint32_t* __restrict__ counts,
                                               T* __restrict__ scratch, const TileDesc* __restrict__ tiles,
-                                              TileOut<T>* __restrict__ tout, DevStatus* st) {
+                                              TileOut<T>* __restrict__ tout, DevStatus* st,
+                                              unsigned long long* sstats) {
   using L = TileSmem<T>;
   constexpr int NT = L::NT, ITEMS = L::ITEMS, CAP = L::CAP;
   extern __shared__ __align__(16) uint8_t sm[];
@@ -636,6 +638,7 @@ __device__ __forceinline__ void big_sort_tile(uint32_t tid, T* __restrict__ keys
   block_minmax<NT>(mn, mx, red);
   if (mn == mx) {  // one key fills the tile: a single row
     if (threadIdx.x == 0) {
+      if (sstats) atomicAdd(&sstats[1], 1ull);
       keys[td.start] = mn;
       counts[td.start] = n > 0xffffffffull ? 0xffffffffu : (uint32_t)n;
       TileOut<T> o;
@@ -758,6 +761,7 @@ __device__ __forceinline__ void big_sort_tile(uint32_t tid, T* __restrict__ keys
   unsigned long long rest_total;
   block_exclusive_scan<NT, unsigned long long>(rest, scan64, &rest_total);
   if (threadIdx.x == 0) {
+    if (sstats) atomicAdd(&sstats[1], U);
     TileOut<T> o;
     o.first_key = ok[0];
     o.first_count = oc[0];
@@ -774,38 +778,42 @@ template <class T>
 __global__ void __launch_bounds__(kTileThreads, 1)
     k_big_tile_sort(T* __restrict__ keys, uint32_t* __restrict__ counts, T* __restrict__ scratch,
                     const TileDesc* __restrict__ tiles, const uint32_t* __restrict__ big_ids,
-                    const unsigned* __restrict__ nids, TileOut<T>* __restrict__ tout, DevStatus* st) {
+                    const unsigned* __restrict__ nids, TileOut<T>* __restrict__ tout, DevStatus* st,
+                    unsigned long long* sstats) {
   if (nids) {
     const unsigned cnt = *nids;
     for (unsigned i = blockIdx.x; i < cnt; i += gridDim.x) {
-      big_sort_tile<T>(big_ids[i], keys, counts, scratch, tiles, tout, st);
+      big_sort_tile<T>(big_ids[i], keys, counts, scratch, tiles, tout, st, sstats);
       __syncthreads();  // shared memory is reused by the next tile
     }
   } else {
-    big_sort_tile<T>(big_ids[blockIdx.x], keys, counts, scratch, tiles, tout, st);
+    big_sort_tile<T>(big_ids[blockIdx.x], keys, counts, scratch, tiles, tout, st, sstats);
   }
 }
 
 template <class T>
 void launch_big_tile_sort(T* keys, uint32_t* counts, T* scratch, const TileDesc* tiles, const uint32_t* big_ids,
-                          uint32_t nbig, const unsigned* nbig_dev, TileOut<T>* out, DevStatus* st, cudaStream_t s) {
+                          uint32_t nbig, const unsigned* nbig_dev, TileOut<T>* out, DevStatus* st,
+                          unsigned long long* sort_stats, cudaStream_t s) {
   const size_t smem = TileSmem<T>::total;
   cudaFuncSetAttribute(k_big_tile_sort<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (nbig)
-    k_big_tile_sort<T><<<nbig, kTileThreads, smem, s>>>(keys, counts, scratch, tiles, big_ids, nbig_dev, out, st);
+    k_big_tile_sort<T><<<nbig, kTileThreads, smem, s>>>(keys, counts, scratch, tiles, big_ids, nbig_dev, out, st,
+                                                         sort_stats);
 }
 template void launch_big_tile_sort<uint64_t>(uint64_t*, uint32_t*, uint64_t*, const TileDesc*, const uint32_t*,
                                              uint32_t, const unsigned*, TileOut<uint64_t>*, DevStatus*,
-                                             cudaStream_t);
+                                             unsigned long long*, cudaStream_t);
 template void launch_big_tile_sort<u128>(u128*, uint32_t*, u128*, const TileDesc*, const uint32_t*, uint32_t,
-                                         const unsigned*, TileOut<u128>*, DevStatus*, cudaStream_t);
+                                         const unsigned*, TileOut<u128>*, DevStatus*, unsigned long long*,
+                                         cudaStream_t);
 
 // Oversized tiles listed on the device, per bucket group: group g (buckets
 // gb[g] .. gb[g+1]) lists its tiles above the on-chip capacity (up to twice
 // it) from ids[gb[g] * S] on and those above twice it from ids2[gb[g] * S] on,
 // with the counts in cnt[2g] and cnt[2g + 1].  Also the tile statistics:
-// stats[0] largest tile, [1] keys, [2] non-empty tiles, range[t] keys in tile
-// index t of every bucket.
+// stats[0] largest tile, [1] keys, [2] non-empty tiles, [3] keys in the tiles
+// above capacity, range[t] keys in tile index t of every bucket.
 __global__ void k_tile_lists(const uint32_t* __restrict__ lens, uint32_t ntiles, uint32_t S,
                              const uint32_t* __restrict__ gb, uint32_t NG, uint32_t cap, uint32_t* __restrict__ ids,
                              uint32_t* __restrict__ ids2, unsigned* __restrict__ cnt,
@@ -819,6 +827,7 @@ __global__ void k_tile_lists(const uint32_t* __restrict__ lens, uint32_t ntiles,
   while (g + 1 < NG && gb[g + 1] <= b) ++g;
   if (len > 2 * cap) ids2[(size_t)gb[g] * S + atomicAdd(&cnt[2 * g + 1], 1u)] = t;
   else if (len > cap) ids[(size_t)gb[g] * S + atomicAdd(&cnt[2 * g], 1u)] = t;
+  if (len > cap) atomicAdd(&stats[3], (unsigned long long)len);
   atomicMax(&stats[0], (unsigned long long)len);
   atomicAdd(&stats[1], (unsigned long long)len);
   atomicAdd(&stats[2], 1ull);

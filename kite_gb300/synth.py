@@ -152,3 +152,20 @@ def metagenome_samples(seed: int = 3, n_samples: int = 16, species: int = 64, sp
                 parts.append(reads_variable(rng, genomes[s], int(c), 100, 250, 0.005))
         out.append(b"".join(parts))
     return out
+
+
+_REPEAT_GENOMES: dict = {}
+
+
+def repeats_reads(n_reads: int, seed: int = 2, genome_seed: int | None = None, threads: int = 0) -> bytearray:
+    """Reads of the repeats workload's shape (150 bp, strand 50/50, 1% subs,
+    0.1% N) from the 50 Mbp repeats genome of genome_seed (default: seed),
+    generated by the host library's multi-threaded generator."""
+    import os
+    from . import host
+    gs = seed if genome_seed is None else genome_seed
+    if gs not in _REPEAT_GENOMES:
+        _REPEAT_GENOMES.clear()
+        _REPEAT_GENOMES[gs] = genome_with_repeats(np.random.default_rng(gs), 50_000_000)
+    return host.synth_reads(_REPEAT_GENOMES[gs], n_reads, 150, 0.01, 0.001, 0.5, seed=seed,
+                            threads=threads or max(1, os.cpu_count() or 1))

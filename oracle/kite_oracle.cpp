@@ -498,7 +498,8 @@ static Plan derive_plan(size_t input_bytes, double avg_read_len, Compression com
     size_t est = (size_t)((double)input_bytes * expansion * (double)E);
     size_t raw = std::max<size_t>((est + target_part - 1) / target_part, 1);
     size_t derived = std::min<size_t>(std::max<size_t>(round_up_pow2(raw), 256), 2048);
-    size_t plan_mb = std::max<long>(buffer_mb > 0 ? buffer_mb : 8, 1);
+    // requested_buffer_mb.unwrap_or(8).max(1) (src/count/mod.rs:929): --buffer 0 plans with 1 MiB
+    size_t plan_mb = buffer_mb >= 0 ? (size_t)std::max<long>(buffer_mb, 1) : 8;
     size_t per_part = plan_mb * MIB + workers * 5 * 1024;
     size_t capped = std::max<size_t>((mem / 4) / std::max<size_t>(per_part, 1), 256);
     capped = floor_pow2(capped);
@@ -991,6 +992,72 @@ static void count_chunks(const std::vector<std::pair<const uint8_t*, size_t>>& c
     st.bases += w->bases;
     st.kmers += w->kmers;
   }
+}
+
+// The payload of every partition as the single-worker count writes it (one
+// flush per partition at flush_all, src/count/worker.rs:284-294: all of the
+// partition's keys sorted, run-length reduced with saturating u32 counts and
+// DVLE-encoded, flush_bucket :296-449), computed with `threads` threads:
+// chunks are scanned in parallel into per-thread buckets, then partitions are
+// sorted and encoded in parallel.  Same bytes as orc_count_kite's payloads,
+// for inputs too large for one worker in a test or a benchmark's parity check.
+struct PartOut {
+  std::vector<uint8_t> payload;
+  uint64_t rows = 0;
+  u128 kmin = 0, kmax = 0;
+};
+
+template <class T>
+static void count_parts(const std::vector<std::pair<const uint8_t*, size_t>>& chunks, unsigned k, bool canonical,
+                        size_t P, size_t threads, std::vector<PartOut>& out, CountStats& st) {
+  threads = std::max<size_t>(threads, 1);
+  std::vector<std::unique_ptr<Worker<T>>> ws;
+  for (size_t i = 0; i < threads; ++i) ws.emplace_back(new Worker<T>(k, canonical, P, SIZE_MAX, nullptr));
+  std::atomic<size_t> next(0);
+  auto scan = [&](size_t wi) {
+    for (;;) {
+      size_t c = next.fetch_add(1);
+      if (c >= chunks.size()) break;
+      ws[wi]->process_chunk(chunks[c].first, chunks[c].second);
+    }
+  };
+  std::vector<std::thread> th;
+  for (size_t i = 0; i < threads; ++i) th.emplace_back(scan, i);
+  for (auto& t : th) t.join();
+  th.clear();
+  for (auto& w : ws) {
+    st.reads += w->reads;
+    st.bases += w->bases;
+    st.kmers += w->kmers;
+  }
+  out.assign(P, PartOut());
+  std::atomic<size_t> next_p(0);
+  auto reduce = [&]() {
+    std::vector<T> all, scratch, keys;
+    std::vector<uint32_t> counts;
+    for (;;) {
+      size_t p = next_p.fetch_add(1);
+      if (p >= P) break;
+      size_t n = 0;
+      for (auto& w : ws) n += w->buckets[p].size();
+      if (n == 0) continue;
+      all.clear();
+      all.reserve(n);
+      for (auto& w : ws) {
+        all.insert(all.end(), w->buckets[p].begin(), w->buckets[p].end());
+        std::vector<T>().swap(w->buckets[p]);
+      }
+      sort_keys(all, k, scratch);
+      rle(all, keys, counts);
+      PartOut& o = out[p];
+      encode_dvle(keys.data(), counts.data(), keys.size(), o.payload);
+      o.rows = keys.size();
+      o.kmin = (u128)keys.front();
+      o.kmax = (u128)keys.back();
+    }
+  };
+  for (size_t i = 0; i < threads; ++i) th.emplace_back(reduce);
+  for (auto& t : th) t.join();
 }
 
 // Split an in-memory FASTQ image into reader chunks the way the chunked
@@ -1671,6 +1738,52 @@ long long orc_count_kite(const uint8_t* d, size_t n, unsigned k, int canonical, 
     return -1;
   }
 }
+
+// Per-partition payloads of the single-worker count (count_parts above) with
+// `threads` threads.  On success returns the total payload bytes, sets *out
+// to a malloc'd buffer with the payloads in partition order (free it with
+// orc_free) and fills meta[6 * P]: per partition rows, bytes, key_min (lo,
+// hi), key_max (lo, hi); stats4 = reads, bases, k-mers, nanoseconds.
+long long orc_count_parts(const uint8_t* d, size_t n, unsigned k, int canonical, size_t partitions, size_t threads,
+                          size_t chunk_size, uint8_t** out, uint64_t* meta, uint64_t* stats4) {
+  try {
+    auto t0 = std::chrono::steady_clock::now();
+    auto chunks = split_chunks(d, n, chunk_size);
+    std::vector<PartOut> parts;
+    CountStats st;
+    if (k <= 31) count_parts<uint64_t>(chunks, k, canonical != 0, partitions, threads, parts, st);
+    else count_parts<u128>(chunks, k, canonical != 0, partitions, threads, parts, st);
+    size_t total = 0;
+    for (auto& p : parts) total += p.payload.size();
+    uint8_t* buf = static_cast<uint8_t*>(malloc(total ? total : 1));
+    if (!buf) throw Error("out of memory");
+    size_t off = 0;
+    for (size_t p = 0; p < partitions; ++p) {
+      const PartOut& o = parts[p];
+      if (!o.payload.empty()) memcpy(buf + off, o.payload.data(), o.payload.size());
+      off += o.payload.size();
+      uint64_t* m = meta + 6 * p;
+      m[0] = o.rows;
+      m[1] = o.payload.size();
+      m[2] = (uint64_t)o.kmin;
+      m[3] = (uint64_t)(o.kmin >> 64);
+      m[4] = (uint64_t)o.kmax;
+      m[5] = (uint64_t)(o.kmax >> 64);
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    stats4[0] = st.reads;
+    stats4[1] = st.bases;
+    stats4[2] = st.kmers;
+    stats4[3] = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(t1 - t0).count();
+    *out = buf;
+    return (long long)total;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
+void orc_free(void* p) { free(p); }
 
 // derive_heuristic_plan restated: out7 = [partitions, chunk_size_bytes,
 // staging_bytes, worker_threads, local_flush_bytes, decomp_threads, lanes].

@@ -68,6 +68,10 @@ def lib() -> C.CDLL:
         L.orc_dump_kite.restype = C.c_longlong
         L.orc_merge_files.argtypes = [C.POINTER(C.c_char_p), C.c_size_t, C.c_size_t, C.c_void_p, C.c_size_t]
         L.orc_merge_files.restype = C.c_longlong
+        L.orc_count_parts.argtypes = [C.c_char_p, C.c_size_t, C.c_uint, C.c_int, C.c_size_t, C.c_size_t, C.c_size_t,
+                                      C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.orc_count_parts.restype = C.c_longlong
+        L.orc_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -123,3 +127,69 @@ def count_buffer(fastq: bytes, k: int, canonical: bool, partitions: int, workers
         raise RuntimeError(err())
     keys = ["reads", "bases", "kmers", "rows", "chunks", "payload_bytes", "ns"]
     return dict(zip(keys, list(st)))
+
+
+class Parts:
+    """Per-partition payloads of the single-worker count (orc_count_parts):
+    meta[p] = (rows, bytes, key_min, key_max), payload(p) a memoryview."""
+
+    def __init__(self, buf, total: int, meta, P: int, stats):
+        self._buf = buf
+        self.total = total
+        self.P = P
+        self.reads, self.bases, self.kmers, ns = stats
+        self.seconds = ns / 1e9
+        self.rows, self.bytes, self.key_min, self.key_max, self.offset = [], [], [], [], []
+        off = 0
+        for p in range(P):
+            m = meta[6 * p:6 * p + 6]
+            self.rows.append(m[0])
+            self.bytes.append(m[1])
+            self.key_min.append(m[2] | (m[3] << 64))
+            self.key_max.append(m[4] | (m[5] << 64))
+            self.offset.append(off)
+            off += m[1]
+        self._view = (C.c_uint8 * max(total, 1)).from_address(buf.value) if total else None
+
+    def payload(self, p: int) -> memoryview:
+        """A view of partition p's payload (valid until close); compare it
+        through bytes() or numpy, not element by element."""
+        if not self.bytes[p]:
+            return memoryview(b"")
+        return memoryview(self._view)[self.offset[p]:self.offset[p] + self.bytes[p]]
+
+    def nonempty(self) -> list:
+        return [p for p in range(self.P) if self.rows[p]]
+
+    def close(self) -> None:
+        if self._buf is not None and self._buf.value:
+            lib().orc_free(self._buf)
+        self._buf = None
+        self._view = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def count_parts(fastq, k: int, canonical: bool, partitions: int, threads: int, chunk_size: int = 64 << 20) -> Parts:
+    """Multi-threaded count with the single-worker count's per-partition
+    payloads (deterministic).  `fastq` is bytes or any object exposing a
+    buffer (bytearray, numpy array)."""
+    L = lib()
+    meta = (C.c_uint64 * (6 * partitions))()
+    st = (C.c_uint64 * 4)()
+    out = C.c_void_p()
+    if isinstance(fastq, bytes):
+        ptr, n = fastq, len(fastq)
+    else:
+        mv = memoryview(fastq).cast("B")
+        n = mv.nbytes
+        ptr = C.cast((C.c_char * n).from_buffer(mv) if not mv.readonly else C.c_char_p(bytes(mv)), C.c_char_p)
+    total = L.orc_count_parts(ptr, n, k, 1 if canonical else 0, partitions, threads, chunk_size, C.byref(out), meta,
+                              st)
+    if total < 0:
+        raise RuntimeError(err())
+    return Parts(out, total, list(meta), partitions, list(st))

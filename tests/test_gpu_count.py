@@ -131,25 +131,39 @@ def test_dense_sequence_fallback(gpu, orc):
 
 
 def test_segments_flush(gpu, orc):
-    # a small arena forces several segments: partitions then hold several
-    # chunks; compare through dump TSV equality (counts summed across chunks)
+    # a small arena forces several segments, so partitions hold several
+    # chunks (one per segment, as the reference's worker flushes a segment
+    # whenever its buffer fills): the summed counts, seen through the oracle's
+    # `dump -o -` of a .kite image holding every chunk, must equal the dump of
+    # the oracle's own count of the same reads
+    from kite_gb300 import host, ingest
     fq = synth.small_workload(seed=5, n_reads=5000, genome_len=30_000)
-    from kite_gb300 import ingest
     chunks = ingest.split_chunks(fq, 100_000)
-    rows = {}
+    emitted = []
     with gpu.Counter(21, False, 8, arena_bytes=256 * 1024) as c:
         for o, l in chunks:
             try:
                 c.submit(fq[o:o + l])
             except gpu.KiteGpuError as e:
                 assert e.code == -9
-                for m, p in c.finish():
-                    rows.setdefault(m["partition_id"], []).append(p)
+                emitted += c.finish()
                 c.submit(fq[o:o + l])
-        for m, p in c.finish():
-            rows.setdefault(m["partition_id"], []).append(p)
+        emitted += c.finish()
         assert c.stats()["segments"] >= 2
-    assert max(len(v) for v in rows.values()) >= 2
+    per_part = {}
+    for m, _ in emitted:
+        per_part[m["partition_id"]] = per_part.get(m["partition_id"], 0) + 1
+    assert max(per_part.values()) >= 2
+    w = host.Writer(None, 21, False, 8, 64, 7, 16 << 20, 2)
+    for m, payload in emitted:
+        w.append(m, payload)
+    w.worker_drain()
+    w.finalize()
+    image = w.image()
+    w.close()
+    ref, _ = orc.count_kite(fq, 21, False, 8)
+    got = orc.dump(image)
+    assert got == orc.dump(ref) and got.count(b"\n") > 1000
 
 
 @pytest.mark.parametrize("mode", ["sampled", "learned"])

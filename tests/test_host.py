@@ -64,7 +64,7 @@ def test_planner_matches_oracle(built, orc, k, comp):
         parts = int(rng.choice([0, 0, 16, 256, 1024]))
         thr = int(rng.choice([1, 2, 3, 8, 16, 64]))
         mem = int(rng.choice([4, 16, 64, 256])) << 30
-        buf = int(rng.choice([-1, -1, 1, 4, 32]))
+        buf = int(rng.choice([-1, -1, 0, 1, 4, 32]))
         out = (C.c_uint64 * 7)()
         rc = L.orc_derive_plan(inb, avg, comp, k, parts, thr, mem, buf, 0, out)
         if rc != 0:

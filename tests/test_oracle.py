@@ -206,3 +206,27 @@ def test_oracle_count_dump_small(orc):
             if "N" not in w:
                 exp[w] = exp.get(w, 0) + 1
     assert counts == exp
+
+
+@pytest.mark.parametrize("k,canonical,P,threads", [(21, False, 16, 1), (31, True, 64, 4), (47, True, 8, 3),
+                                                   (63, True, 2, 8)])
+def test_count_parts_matches_single_worker(built, orc, k, canonical, P, threads):
+    # the multi-threaded per-partition count used for parity at full sizes
+    # gives the single-worker count's payload of every partition
+    from kite_gb300 import synth
+    from kite_gb300.kitefile import KiteImage
+    fq = synth.small_workload(seed=17, n_reads=6000, genome_len=40_000)
+    img, st = orc.count_kite(fq, k, canonical, P, chunk_size=200_000)
+    ki = KiteImage.parse(img)
+    parts = orc.count_parts(fq, k, canonical, P, threads, chunk_size=200_000)
+    assert (parts.reads, parts.bases, parts.kmers) == st
+    for p in range(P):
+        ch = ki.partition_chunks(p)
+        assert len(ch) <= 1
+        if not ch:
+            assert parts.rows[p] == 0
+            continue
+        c = ch[0]
+        assert (parts.rows[p], parts.key_min[p], parts.key_max[p]) == (c.row_count, c.key_min, c.key_max)
+        assert bytes(parts.payload(p)) == ki.payload(c)
+    parts.close()

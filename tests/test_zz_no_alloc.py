@@ -152,3 +152,48 @@ def test_noalloc_limits(gpu):
     assert rc == KITE_ERR_BAD_INPUT and gtot[3] == tot[3] > 10
     rc, got, gtot = noalloc_rows(gpu, data, 25, True, 8)
     assert rc == 0 and got == parts and gtot == tot
+
+
+def _densest_cases():
+    # 65,536 one-base records of 8 bytes: the most sequences a full chunk of
+    # real reads holds, every one a k=1 k-mer
+    one_base = b"@\nA\n+\nI\n" * (MAX_BYTES // 8)
+    # 87,380 empty records (6 bytes) and one 8-byte record: the most sequence
+    # lines a chunk can hold (a record spans four newlines)
+    empties = b"@\n\n+\n\n" * 87_380 + b"@\nC\n+\nI\n"
+    # one sequence line filling the chunk: the most k-mers (one per byte)
+    rng = np.random.default_rng(31)
+    seq = bytes(b"ACGT"[x] for x in rng.integers(0, 4, MAX_BYTES - 6))
+    single = b"@\n" + seq + b"\n+\n\n"
+    # short random reads of 2..9 bases
+    recs = []
+    n = 0
+    while True:
+        L = int(rng.integers(2, 10))
+        r = b"@\n" + bytes(b"ACGT"[x] for x in rng.integers(0, 4, L)) + b"\n+\n" + b"I" * L + b"\n"
+        if n + len(r) > MAX_BYTES - 8:
+            break
+        recs.append(r)
+        n += len(r)
+    short = b"".join(recs)
+    short += b"@\n" + b"G" * ((MAX_BYTES - len(short) - 6) // 2) + b"\n+\n"
+    short += b"I" * (MAX_BYTES - len(short) - 1) + b"\n"
+    return {"one_base": one_base, "empties": empties, "single": single, "short": short}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["one_base", "empties", "single", "short"])
+@pytest.mark.parametrize("k,canonical,P", [(1, False, 2), (2, True, 4), (31, True, 64)])
+def test_noalloc_full_size_chunks(gpu, name, k, canonical, P):
+    # chunks of exactly KITE_NOALLOC_MAX_BYTES that reach the fixed bounds of
+    # the scratch layout: the most sequences, the most k-mers, the most rows
+    data = _densest_cases()[name]
+    assert len(data) == MAX_BYTES
+    parts, tot = context_rows(gpu, data, k, canonical, P)
+    for _ in range(2):
+        rc, got, gtot = noalloc_rows(gpu, data, k, canonical, P)
+        assert rc == 0
+        assert gtot == tot
+        assert sorted(got) == sorted(parts)
+        for p in parts:
+            assert got[p] == parts[p], f"partition {p}"
