@@ -78,6 +78,9 @@ typedef struct {
   uint32_t samples;          /* batched count: samples per segment (0 = 1); see kite_gpu_count_submit_sample */
   double tile_fill;          /* target tile load as a fraction of on-chip capacity (0 = 0.85) */
   int scatter_shape;         /* key-range split scatter launch shape 0..3 (0 = 256 threads x 8 keys) */
+  uint32_t tile_wait_polls;  /* bound of the tile sort's first wait for a tile's bulk load (0 = 2^18 polls);
+                                1 gives up unless the copy has already landed (tests of the timeout path:
+                                the count then returns KITE_ERR_TIMEOUT) */
 } kite_gpu_cfg;
 
 /* One emitted chunk: the arguments of ConcurrentKiteWriter::append_chunk. */

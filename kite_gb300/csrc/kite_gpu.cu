@@ -733,19 +733,19 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     const uint32_t t0 = gb[g] * Sl, nt = (gb[g + 1] - gb[g]) * Sl, nb = gb[g + 1] - gb[g];
     cudaEventRecord(gev[8 * g], s);
     launch_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>() + t0, nt, tout + t0,
-                        ctx->sort_stats.as<unsigned long long>(), TileRanges<T>{tile_spl, Sl, t0, kmax}, s);
+                        ctx->sort_stats.as<unsigned long long>(), TileRanges<T>{tile_spl, Sl, t0, kmax, ctx->cfg.tile_wait_polls}, s);
     cudaEventRecord(gev[8 * g + 1], s);
     if (dev_tiles) {
       launch_tile_sort_large<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ids_a + t0, walk_grid,
                                 lcnt + 2 * g, tout, ctx->sort_stats.as<unsigned long long>(),
-                                TileRanges<T>{tile_spl, Sl, 0, kmax}, s);
+                                TileRanges<T>{tile_spl, Sl, 0, kmax, ctx->cfg.tile_wait_polls}, s);
       launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(), ids_b + t0,
                               walk_grid, lcnt + 2 * g + 1, tout, ctx->status.as<DevStatus>(),
                               ctx->sort_stats.as<unsigned long long>(), s);
     } else {
       launch_tile_sort_large<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>(), ids_a + gbig[g],
                                 glarge[g], nullptr, tout, ctx->sort_stats.as<unsigned long long>(),
-                                TileRanges<T>{tile_spl, Sl, 0, kmax}, s);
+                                TileRanges<T>{tile_spl, Sl, 0, kmax, ctx->cfg.tile_wait_polls}, s);
       launch_big_tile_sort<T>(sorted, ctx->counts.as<uint32_t>(), scratch, ctx->tiles.as<TileDesc>(),
                               ids_a + gbig[g] + glarge[g], gbig[g + 1] - gbig[g] - glarge[g], nullptr, tout,
                               ctx->status.as<DevStatus>(), ctx->sort_stats.as<unsigned long long>(), s);

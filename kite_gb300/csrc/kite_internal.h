@@ -177,6 +177,7 @@ struct TileRanges {
   uint32_t S;
   uint32_t tile0;
   T kmax;
+  uint32_t wait_polls;  // bound of the first wait for a tile's bulk load (1: a single non-blocking test)
 };
 
 // `fallbacks` (device counters): [0] tiles that took the LSD fallback (plus

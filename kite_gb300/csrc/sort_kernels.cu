@@ -301,8 +301,19 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
                : "memory");
 }
-// Waits for phase `parity` of the barrier, giving up after `limit` polls.
+// Waits for phase `parity` of the barrier, giving up after `limit` polls
+// (each a try_wait, which may suspend the thread for a while); limit 1 is a
+// single non-blocking test.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  if (limit == 1) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+  }
   for (uint32_t it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
@@ -315,6 +326,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
   return false;
 }
 constexpr uint32_t kBulkWaitPolls = 1u << 18;                // a bulk copy from device memory ends long before
+constexpr uint32_t kBulkDrainPolls = 1u << 26;               // after a timeout: the copy must leave shared memory
 constexpr unsigned long long kBulkTimeoutFlag = 1ull << 40;  // added to the sort statistics on a timeout
 
 template <class T, int MULT>
@@ -377,13 +389,20 @@ __device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, ui
   if (threadIdx.x < 4) misc[threadIdx.x] = 0;
   __syncthreads();
   if (threadIdx.x == 0) bulk_load(sm, reinterpret_cast<const void*>(s0), (uint32_t)(s1 - s0), bar);
-  const bool arrived = mbar_wait(bar, 0, kBulkWaitPolls);
+  const bool arrived = mbar_wait(bar, 0, rg.wait_polls ? rg.wait_polls : kBulkWaitPolls);
   if (__syncthreads_or(!arrived)) {
-    // the copy did not complete: wait once more for it to leave shared memory
-    // alone, report, and leave the tile unsorted (the count then fails)
+    // the wait gave up: report, wait (with a far larger bound) until the copy
+    // has landed so that no write to this CTA's shared memory is still in
+    // flight when it moves on, and leave the tile empty (the count fails)
     if (threadIdx.x == 0) {
-      mbar_wait(bar, 0, kBulkWaitPolls);
+      mbar_wait(bar, 0, kBulkDrainPolls);
       if (fallbacks) atomicAdd(fallbacks, kBulkTimeoutFlag);
+      TileOut<T> o;  // an empty tile for the link and encode kernels that follow
+      o.first_key = o.last_key = T(0);
+      o.rows = 0;
+      o.first_count = 0;
+      o.rest_bytes = 0;
+      tout[tid] = o;
     }
     __syncthreads();
     return;

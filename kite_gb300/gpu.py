@@ -43,7 +43,7 @@ class Cfg(C.Structure):
     _fields_ = [("device", C.c_int), ("k", C.c_int), ("canonical", C.c_int), ("partitions", C.c_uint32),
                 ("splitter_mode", C.c_int), ("imbalance_bound", C.c_double), ("arena_bytes", C.c_uint64),
                 ("timeout_ms", C.c_uint32), ("stream", C.c_void_p), ("samples", C.c_uint32),
-                ("tile_fill", C.c_double), ("scatter_shape", C.c_int)]
+                ("tile_fill", C.c_double), ("scatter_shape", C.c_int), ("tile_wait_polls", C.c_uint32)]
 
 
 class ChunkMeta(C.Structure):
@@ -131,10 +131,11 @@ class Counter:
     def __init__(self, k: int, canonical: bool, partitions: int, device: int = 0,
                  splitter_mode: int = SPLIT_AUTO, imbalance_bound: float = 1.10, arena_bytes: int = 0,
                  timeout_ms: int = 0, stream: int | None = None, samples: int = 1, tile_fill: float = 0.0,
-                 scatter_shape: int = 0):
+                 scatter_shape: int = 0, tile_wait_polls: int = 0):
         self._L = lib()
         cfg = Cfg(device, k, 1 if canonical else 0, partitions, splitter_mode, imbalance_bound, arena_bytes,
-                  timeout_ms, C.c_void_p(stream) if stream else None, samples, tile_fill, scatter_shape)
+                  timeout_ms, C.c_void_p(stream) if stream else None, samples, tile_fill, scatter_shape,
+                  tile_wait_polls)
         h = C.c_void_p()
         rc = self._L.kite_gpu_open(C.byref(cfg), C.byref(h))
         if rc != KITE_OK:

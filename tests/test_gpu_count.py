@@ -105,8 +105,9 @@ def test_large_tile_on_chip(gpu, orc):
     # 12,001 keys in partition 0: the tile holding the two repeated keys is
     # over the regular on-chip capacity (8192) but within twice it, so it
     # takes the double-capacity on-chip sort.
+    # (sampled splitters: the learned ones cut the two keys apart)
     fq = _rec(b"A" * 21) * 6000 + _rec(b"A" * 20 + b"G") * 6000 + _rec(b"G" * 21)
-    st = assert_parity(gpu, orc, fq, 21, False, 2)
+    st = assert_parity(gpu, orc, fq, 21, False, 2, splitter_mode=gpu.SPLIT_SAMPLED)
     assert st["big_tiles"] >= 1
 
 
@@ -117,7 +118,7 @@ def test_large_bin_many_distinct(gpu, orc):
     from kite_build import bucket
     vals = [v for v in range(400) if bucket(v, 2, False) == 0][:40]
     fq = b"".join(_rec(_kmer(v, 21)) * 10 for v in vals) + _rec(b"G" * 21)
-    st = assert_parity(gpu, orc, fq, 21, False, 2)
+    st = assert_parity(gpu, orc, fq, 21, False, 2, splitter_mode=gpu.SPLIT_SAMPLED)
     assert st["sort_fallbacks"] >= 1
 
 
@@ -177,3 +178,17 @@ def test_skewed_clustered_tiles(gpu, orc, mode):
     st = assert_parity(gpu, orc, fq, 63, True, 2, splitter_mode=sm, imbalance_bound=100.0)
     assert st["tiles_per_bucket"] > 32
 
+
+
+def test_tile_sort_bulk_load_timeout(gpu, orc):
+    # the tile sort's first bounded wait for a tile's bulk load set to one
+    # non-blocking test: the wait gives up, every CTA still waits for its copy
+    # to land before it moves on, and the count returns KITE_ERR_TIMEOUT; the
+    # device stays usable and a normal count afterwards is exact
+    fq = synth.small_workload(seed=1, n_reads=20_000, genome_len=200_000)
+    with gpu.Counter(21, False, 16, tile_wait_polls=1) as c:
+        c.submit(fq)
+        with pytest.raises(gpu.KiteGpuError) as e:
+            c.finish()
+        assert e.value.code == -3 and "bulk load" in str(e.value)
+    assert_parity(gpu, orc, fq, 21, False, 16)
