@@ -12,7 +12,10 @@
  *   kite_derive_plan        <- derive_heuristic_plan src/count/mod.rs:624-864
  *   kite_parse_memory_spec  <- parse_memory_spec src/runtime.rs:6-54
  *   kite_count_passes_filter<- count_passes_filter src/kiteops/mod.rs:44-56
- *   kite_reader_*           <- KiteReader::open src/dump/reader.rs:43-155
+ *   kite_reader_*           <- KiteReader::open src/dump/reader.rs:43-155,
+ *                              run_data_for_decode :162-186 (zstd chunks)
+ *   kite_zstd_chunk         <- CountWorker::flush_bucket's zstd "if smaller"
+ *                              src/count/worker.rs:340-374, :452-501
  *   kite_dump_partition     <- stream_partition_slabs src/dump/merge.rs:282-428
  *   kite_input_*            <- detect_compression src/count/reader.rs:22-51,
  *                              Plain/GzipChunkedReader src/count/decompress.rs:36-138
@@ -77,6 +80,23 @@ int kite_reader_merge_input(const kite_reader* r, kite_gpu_merge_input* mi);
 /* Appends the TSV lines of one partition ("<kmer>\t<count>\n", segments
  * summed with saturating u32, header filter applied). Returns bytes or -1. */
 int64_t kite_dump_partition(const kite_reader* r, uint32_t partition, char** buf, size_t* cap, size_t* len);
+
+/* ---- zstd "if smaller" (count --mode balanced | compact) ------------------ */
+/* CountWorker::flush_bucket src/count/worker.rs:340-374 with its heuristics
+ * compression_level_for / min_compression_input_bytes /
+ * min_compression_savings_bytes :452-501: one chunk's DVLE payload is
+ * zstd-compressed at base_level (balanced 2, compact 5, raised by the
+ * heuristics, at most 6) when it is large enough, and the compressed bytes
+ * are kept only when they save enough.  Returns the compressed length written
+ * to out (the chunk then carries codec | KITE_CODEC_ZSTD, raw_bytes = len),
+ * 0 to keep the payload as it is, -1 on error.  out needs
+ * kite_zstd_bound(len) bytes.  zstd is the system's libzstd.so.1, loaded at
+ * run time; kite_zstd_available says whether it loaded.  Readers decompress
+ * zstd chunks when a file is opened (kite_reader_*). */
+int kite_zstd_available(void);
+size_t kite_zstd_bound(size_t len);
+int64_t kite_zstd_chunk(int k, int base_level, const kite_chunk_meta* meta, const uint8_t* payload, size_t len,
+                        uint8_t* out, size_t cap);
 
 /* ---- input --------------------------------------------------------------- */
 int kite_detect_compression(const char* path); /* KITE_INPUT_* or -1 */

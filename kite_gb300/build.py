@@ -97,11 +97,12 @@ def build(verbose: bool = False, jobs: int | None = None) -> dict:
         _run([nvcc, *ARCH, "-shared", "-cudart", "shared", "-o", str(gpu_so), *map(str, gpu_objs)])
     host_so = LIB / "libkite_host.so"
     if host_objs and _newer(host_so, host_objs):
-        _run([cxx, "-shared", "-o", str(host_so), *map(str, host_objs), *(["-lz"] if zlib else []), "-lpthread"])
+        _run([cxx, "-shared", "-o", str(host_so), *map(str, host_objs), *(["-lz"] if zlib else []), "-lpthread",
+              "-ldl"])
     cli = LIB / "kite"
     if cli_src.exists() and _newer(cli, [cli_obj, host_so, gpu_so]):
         _run([cxx, "-o", str(cli), str(cli_obj), f"-L{LIB}", "-lkite_host", "-lkite_gpu",
-              f"-Wl,-rpath,$ORIGIN", *(["-lz"] if zlib else []), "-lpthread"])
+              f"-Wl,-rpath,$ORIGIN", *(["-lz"] if zlib else []), "-lpthread", "-ldl"])
     if verbose:
         print(f"built {gpu_so}, {host_so}, {cli} (zlib={'yes' if zlib else 'no'})")
     return {"gpu": str(gpu_so), "host": str(host_so), "cli": str(cli), "zlib": zlib}

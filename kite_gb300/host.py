@@ -18,7 +18,7 @@ EXPORTED = [
     "kite_reader_open", "kite_reader_open_image", "kite_reader_close", "kite_reader_header",
     "kite_reader_merge_input", "kite_dump_partition", "kite_detect_compression", "kite_input_open",
     "kite_input_next", "kite_input_max_chunk", "kite_input_close", "kite_sample_avg_read_len", "kite_synth_reads",
-    "kite_input_set_threads",
+    "kite_input_set_threads", "kite_zstd_available", "kite_zstd_bound", "kite_zstd_chunk",
 ]
 
 

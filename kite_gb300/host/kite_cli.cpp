@@ -2,6 +2,8 @@
 // (CountArgs src/cli.rs:137-229, DumpArgs :238-282, MergeArgs :416-451) on the
 // GB300 path.  Counting and merging run on the GPU through include/kite_gpu.h;
 // the .kite layout comes from the host writer (include/kite_host.h).
+#include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <csignal>
 #include <cstdio>
@@ -61,6 +63,56 @@ void print_command(const char* cmd, int argc, char** argv) {
 // ---------------------------------------------------------------------------
 // count
 // ---------------------------------------------------------------------------
+// Chunks of one segment for --mode balanced | compact: copied out of the
+// GPU's emit callback, compressed in parallel (kite_zstd_chunk: the
+// reference's zstd "if smaller"), appended to the writer in their emit order.
+struct ZstdSegment {
+  kite_writer* w;
+  int k, level;
+  unsigned threads;
+  struct Item {
+    kite_chunk_meta meta;
+    std::vector<uint8_t> data, z;
+    int64_t zlen;
+  };
+  std::vector<Item> items;
+  static int collect(void* user, const kite_chunk_meta* meta, const uint8_t* data, size_t len) {
+    auto* s = static_cast<ZstdSegment*>(user);
+    s->items.push_back(Item{*meta, std::vector<uint8_t>(data, data + len), {}, 0});
+    return 0;
+  }
+  int flush() {
+    std::atomic<size_t> next(0);
+    std::atomic<int> failed(0);
+    auto work = [&]() {
+      for (size_t i; (i = next.fetch_add(1)) < items.size();) {
+        Item& it = items[i];
+        it.z.resize(kite_zstd_bound(it.data.size()) + 16);
+        it.zlen = kite_zstd_chunk(k, level, &it.meta, it.data.data(), it.data.size(), it.z.data(), it.z.size());
+        if (it.zlen < 0) failed = 1;
+      }
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < std::max(1u, threads); ++t) th.emplace_back(work);
+    for (auto& t : th) t.join();
+    if (failed) return -1;
+    for (Item& it : items) {
+      int r;
+      if (it.zlen > 0) {
+        kite_chunk_meta m = it.meta;
+        m.codec |= KITE_CODEC_ZSTD;
+        m.raw_bytes = it.data.size();
+        r = kite_writer_append(w, &m, it.z.data(), (size_t)it.zlen);
+      } else {
+        r = kite_writer_append(w, &it.meta, it.data.data(), it.data.size());
+      }
+      if (r != 0) return -1;
+    }
+    items.clear();
+    return 0;
+  }
+};
+
 int cmd_count(int argc, char** argv) {
   std::string in, out, mem, mode = "fast", splitters = "auto";
   int k = 21, device = 0;
@@ -104,7 +156,14 @@ int cmd_count(int argc, char** argv) {
         " --max " + std::to_string(mx));
   if (k > 64) die("k > 64 (256-bit keys) is not supported by the GPU counting path");
   if (partitions == 1) die("invalid partition count: --partitions 1 leaves no partition bits for routing");
-  if (mode != "fast") die("--mode " + mode + " needs zstd, which this binary is not compiled with; use --mode fast");
+  // CountMode::zstd_level src/cli.rs:11-19
+  int zstd_level = 0;
+  if (mode == "balanced") zstd_level = 2;
+  else if (mode == "compact") zstd_level = 5;
+  else if (mode != "fast")
+    die("invalid value '" + mode + "' for '--mode <MODE>'\n  [possible values: fast, balanced, compact]");
+  if (zstd_level && !kite_zstd_available())
+    die("--mode " + mode + " needs zstd (libzstd.so.1), which could not be loaded; use --mode fast");
   const bool to_null = out == "/dev/null";
   if (!to_null && (out.size() < 5 || out.compare(out.size() - 5, 5, ".kite") != 0))
     die("invalid count output path: output must end with .kite, or be /dev/null for benchmark runs.\nGot: " + out +
@@ -142,7 +201,8 @@ int cmd_count(int argc, char** argv) {
   fprintf(stderr, "[kite count] k=%d, canonical=%s, partitions=%llu, min=%s, max=%s\n", k,
           canonical ? "true" : "false", (unsigned long long)plan.partitions, opt_str(has_min, mn).c_str(),
           opt_str(has_max, mx).c_str());
-  fprintf(stderr, "[kite count] mode=fast, codec=dvle-only, device=cuda:%d\n", device);
+  fprintf(stderr, "[kite count] mode=%s, codec=%s, device=cuda:%d\n", mode.c_str(),
+          zstd_level ? "dvle+zstd-if-smaller" : "dvle-only", device);
 
   kite_gpu_cfg cfg{};
   cfg.device = device;
@@ -166,8 +226,13 @@ int cmd_count(int argc, char** argv) {
     if (!b) die("failed to allocate pinned host buffers");
   }
   uint64_t reads = 0, bases = 0, kmers = 0;
+  // balanced / compact: every chunk of the segment through zstd "if smaller"
+  // on the host threads, then appended in partition order
+  ZstdSegment zseg{w, k, zstd_level, (unsigned)total_threads, {}};
   auto finish_segment = [&]() {
-    int r = kite_gpu_count_finish(ctx, kite_writer_emit, w);
+    int r = zstd_level ? kite_gpu_count_finish(ctx, ZstdSegment::collect, &zseg)
+                       : kite_gpu_count_finish(ctx, kite_writer_emit, w);
+    if (r == KITE_OK && zstd_level && zseg.flush() != 0) die(kite_host_last_error());
     if (r != KITE_OK) die(std::string("GPU count failed: ") + kite_gpu_last_error(ctx));
     kite_gpu_stats st{};
     kite_gpu_get_stats(ctx, &st);

@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cerrno>
 #include <deque>
+#include <dlfcn.h>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -46,6 +47,31 @@ inline uint64_t rd(const uint8_t* p, int n) {
   uint64_t v = 0;
   for (int i = 0; i < n; ++i) v |= (uint64_t)p[i] << (8 * i);
   return v;
+}
+
+// zstd, loaded at run time from the system's libzstd.so.1 (the image ships the
+// library without headers).  The few entry points used are declared here with
+// their published prototypes.
+struct Zstd {
+  size_t (*compress)(void*, size_t, const void*, size_t, int) = nullptr;
+  size_t (*decompress)(void*, size_t, const void*, size_t) = nullptr;
+  size_t (*bound)(size_t) = nullptr;
+  unsigned (*is_error)(size_t) = nullptr;
+  bool ok = false;
+};
+const Zstd& zstd() {
+  static const Zstd z = [] {
+    Zstd r;
+    void* h = dlopen("libzstd.so.1", RTLD_NOW | RTLD_LOCAL);
+    if (!h) return r;
+    r.compress = reinterpret_cast<size_t (*)(void*, size_t, const void*, size_t, int)>(dlsym(h, "ZSTD_compress"));
+    r.decompress = reinterpret_cast<size_t (*)(void*, size_t, const void*, size_t)>(dlsym(h, "ZSTD_decompress"));
+    r.bound = reinterpret_cast<size_t (*)(size_t)>(dlsym(h, "ZSTD_compressBound"));
+    r.is_error = reinterpret_cast<unsigned (*)(size_t)>(dlsym(h, "ZSTD_isError"));
+    r.ok = r.compress && r.decompress && r.bound && r.is_error;
+    return r;
+  }();
+  return z;
 }
 
 // KiteHeader::write_to (src/format/header.rs:62-92): 128 bytes, LE.
@@ -329,11 +355,62 @@ struct kite_reader {
   std::vector<uint8_t> own;
   kite_header_info h{};
   uint64_t cio = 0, pto = 0, fo = 0, total_chunks = 0, total_rows = 0;
-  std::vector<uint64_t> c_off, c_len, c_rows, p_first, p_count;
+  std::vector<uint64_t> c_off, c_len, c_rows, c_raw, p_first, p_count;
   std::vector<uint32_t> c_codec;
+  // payloads as the decoders read them: the file's bytes, or, when a chunk is
+  // zstd-compressed, every payload copied into `dec` with those chunks
+  // decompressed (run_data_for_decode src/dump/reader.rs:162-186)
+  const uint8_t* d_base = nullptr;
+  size_t d_len = 0;
+  std::vector<uint64_t> d_off, d_size;
+  std::vector<uint32_t> d_codec;
+  std::vector<uint8_t> dec;
 };
 
 namespace {
+
+// Payloads for the decoders: zero-copy unless some chunk is zstd-compressed.
+int reader_decode(kite_reader* r) {
+  const size_t nc = r->c_off.size();
+  bool any = false;
+  for (size_t c = 0; c < nc; ++c) any |= (r->c_codec[c] & 4u) != 0;
+  r->d_codec = r->c_codec;
+  if (!any) {
+    r->d_base = r->data;
+    r->d_len = r->len;
+    r->d_off = r->c_off;
+    r->d_size = r->c_len;
+    return 0;
+  }
+  const Zstd& z = zstd();
+  if (!z.ok) return set_err("zstd decompress failed: libzstd.so.1 is not available");
+  uint64_t total = 0;
+  for (size_t c = 0; c < nc; ++c) total += (r->c_codec[c] & 4u) ? r->c_raw[c] : r->c_len[c];
+  r->dec.resize(total + 16);
+  r->d_off.resize(nc);
+  r->d_size.resize(nc);
+  uint64_t at = 0;
+  for (size_t c = 0; c < nc; ++c) {
+    const uint8_t* src = r->data + r->c_off[c];
+    r->d_off[c] = at;
+    if (r->c_codec[c] & 4u) {
+      const size_t got = z.decompress(r->dec.data() + at, r->c_raw[c], src, r->c_len[c]);
+      if (z.is_error(got)) return set_err("zstd decompress failed: corrupt chunk " + std::to_string(c));
+      if (got != r->c_raw[c])
+        return set_err("decoded payload size mismatch: got " + std::to_string(got) + ", expected " +
+                       std::to_string(r->c_raw[c]));
+      r->d_size[c] = got;
+      r->d_codec[c] &= ~4u;
+    } else {
+      memcpy(r->dec.data() + at, src, r->c_len[c]);
+      r->d_size[c] = r->c_len[c];
+    }
+    at += r->d_size[c];
+  }
+  r->d_base = r->dec.data();
+  r->d_len = at;
+  return 0;
+}
 
 int reader_parse(kite_reader* r) {
   const uint8_t* p = r->data;
@@ -370,6 +447,7 @@ int reader_parse(kite_reader* r) {
     r->c_codec.push_back((uint32_t)rd(e + 4, 4));
     r->c_off.push_back(rd(e + 8, 8));
     r->c_len.push_back(rd(e + 16, 8));
+    r->c_raw.push_back(rd(e + 24, 8));
     r->c_rows.push_back(rd(e + 32, 8));
   }
   for (uint64_t b = 0; b < P; ++b) {
@@ -384,7 +462,7 @@ int reader_parse(kite_reader* r) {
     r->p_first.push_back(first);
     r->p_count.push_back(cnt);
   }
-  return 0;
+  return reader_decode(r);
 }
 
 }  // namespace
@@ -447,12 +525,12 @@ int kite_reader_header(const kite_reader* r, kite_header_info* h, uint64_t* tc, 
 
 int kite_reader_merge_input(const kite_reader* r, kite_gpu_merge_input* mi) {
   if (!r || !mi) return -1;
-  mi->base = r->data;
-  mi->base_len = r->len;
-  mi->chunk_offset = r->c_off.data();
-  mi->chunk_len = r->c_len.data();
+  mi->base = r->d_base;
+  mi->base_len = r->d_len;
+  mi->chunk_offset = r->d_off.data();
+  mi->chunk_len = r->d_size.data();
   mi->chunk_rows = r->c_rows.data();
-  mi->chunk_codec = r->c_codec.data();
+  mi->chunk_codec = r->d_codec.data();
   mi->part_first = r->p_first.data();
   mi->part_count = r->p_count.data();
   mi->has_min = r->h.has_min;
@@ -525,9 +603,8 @@ int64_t kite_dump_partition(const kite_reader* r, uint32_t p, char** buf, size_t
   };
   std::vector<Stream> ss;
   for (uint64_t c = r->p_first[p]; c < r->p_first[p] + r->p_count[p]; ++c) {
-    if (r->c_codec[c] & 4u) return set_err("zstd chunks are not supported");
-    ss.push_back(Stream{r->data + r->c_off[c], (size_t)r->c_len[c], 0, r->c_rows[c], 0,
-                        (r->c_codec[c] & 2u) != 0, (size_t)(wide ? 20 : 12)});
+    ss.push_back(Stream{r->d_base + r->d_off[c], (size_t)r->d_size[c], 0, r->c_rows[c], 0,
+                        (r->d_codec[c] & 2u) != 0, (size_t)(wide ? 20 : 12)});
   }
   struct Head {
     u128 k;
@@ -569,6 +646,62 @@ int64_t kite_dump_partition(const kite_reader* r, uint32_t p, char** buf, size_t
   }
   return (int64_t)(*len - start);
 }
+
+// ============================================================================
+// zstd "if smaller" for count's balanced / compact modes
+// (CountWorker::flush_bucket src/count/worker.rs:340-374, heuristics :452-501)
+// ============================================================================
+namespace {
+
+size_t min_compression_input_bytes(int k, bool used_dvle, size_t entry_size) {
+  if (entry_size == 12 && used_dvle && k <= 31) return 16 * 1024;
+  if (entry_size == 20 && used_dvle) return 32 * 1024;
+  if (entry_size == 36) return 64 * 1024;
+  return 32 * 1024;
+}
+
+size_t min_compression_savings_bytes(size_t payload, size_t logical, bool used_dvle, size_t entry_size) {
+  const size_t ratio_bias = (logical > payload ? logical - payload : 0) / 32;
+  const size_t floor = (entry_size == 12 && used_dvle) ? 8 * 1024 : (entry_size == 20 && used_dvle) ? 16 * 1024
+                                                                                                     : 32 * 1024;
+  const size_t a = std::max(floor, payload / 100), b = std::min<size_t>(ratio_bias, 24 * 1024);
+  return a > b ? a - b : 0;
+}
+
+int compression_level_for(int base, int k, size_t payload, size_t logical, bool used_dvle, size_t entry_size) {
+  if (base <= 0) return 0;
+  int level = base;
+  if (used_dvle && entry_size == 12 && k <= 31 && payload >= 1024 * 1024) level += 1;
+  if (logical >= payload * 2 && payload >= 4 * 1024 * 1024) level += 1;
+  return std::min(level, 6);
+}
+
+}  // namespace
+
+extern "C" {
+
+int kite_zstd_available(void) { return zstd().ok ? 1 : 0; }
+
+size_t kite_zstd_bound(size_t len) { return zstd().ok ? zstd().bound(len) : 0; }
+
+int64_t kite_zstd_chunk(int k, int base_level, const kite_chunk_meta* meta, const uint8_t* payload, size_t len,
+                        uint8_t* out, size_t cap) {
+  if (!meta || (len && !payload)) return set_err("bad arguments");
+  const bool used_dvle = (meta->codec & KITE_CODEC_DVLE) != 0;
+  const size_t entry = k <= 31 ? 12 : k <= 64 ? 20 : 36;
+  const size_t logical = (size_t)meta->row_count * entry;
+  const int level = compression_level_for(base_level, k, len, logical, used_dvle, entry);
+  if (level <= 0 || len < min_compression_input_bytes(k, used_dvle, entry)) return 0;
+  const Zstd& z = zstd();
+  if (!z.ok) return set_err("zstd compression needs libzstd.so.1, which is not available");
+  if (cap < z.bound(len)) return set_err("zstd output buffer too small");
+  const size_t got = z.compress(out, cap, payload, len, level);
+  if (z.is_error(got)) return 0;  // the reference keeps the payload when compression fails
+  const size_t min_savings = min_compression_savings_bytes(len, logical, used_dvle, entry);
+  return got + min_savings < len ? (int64_t)got : 0;
+}
+
+}  // extern "C"
 
 // ============================================================================
 // Memory spec, planner

@@ -2,7 +2,8 @@
 //
 // A plain CPU restatement of the reference's exact k-mer counting path
 // (jiehua1995/Kite v0.7.5): `kite count`, `kite dump` and `kite merge`
-// for k <= 64 (u64 and u128 keys), fast mode (no zstd).  It exists only so
+// for k <= 64 (u64 and u128 keys), in fast, balanced and compact modes (zstd
+// through the system's libzstd.so.1).  It exists only so
 // that tests/ and bench.py's CPU baseline can check and time the GPU path;
 // nothing under kite_gb300/ links, imports or executes it.
 //
@@ -27,6 +28,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <dlfcn.h>
 #include <functional>
 #include <map>
 #include <memory>
@@ -652,6 +654,59 @@ static uint64_t get_le(const uint8_t* p, int nbytes) {
 }
 static u128 get_le128(const uint8_t* p) { return (u128)get_le(p, 8) | ((u128)get_le(p + 8, 8) << 64); }
 
+// ---------------------------------------------------------------------------
+// zstd (the zstd crate 0.13.3 / libzstd in the reference; here the system's
+// libzstd.so.1 loaded at run time): bulk compress / decompress of one payload.
+// ---------------------------------------------------------------------------
+struct ZstdLib {
+  size_t (*compress)(void*, size_t, const void*, size_t, int) = nullptr;
+  size_t (*decompress)(void*, size_t, const void*, size_t) = nullptr;
+  size_t (*bound)(size_t) = nullptr;
+  unsigned (*is_error)(size_t) = nullptr;
+};
+static const ZstdLib& zstd_lib() {
+  static ZstdLib z = [] {
+    ZstdLib r;
+    if (void* h = dlopen("libzstd.so.1", RTLD_NOW | RTLD_LOCAL)) {
+      r.compress = (size_t(*)(void*, size_t, const void*, size_t, int))dlsym(h, "ZSTD_compress");
+      r.decompress = (size_t(*)(void*, size_t, const void*, size_t))dlsym(h, "ZSTD_decompress");
+      r.bound = (size_t(*)(size_t))dlsym(h, "ZSTD_compressBound");
+      r.is_error = (unsigned (*)(size_t))dlsym(h, "ZSTD_isError");
+    }
+    if (!r.compress || !r.decompress || !r.bound || !r.is_error) throw std::runtime_error("libzstd.so.1 unavailable");
+    return r;
+  }();
+  return z;
+}
+
+// zstd "if smaller" of one flushed bucket: CountWorker::flush_bucket
+// src/count/worker.rs:340-374 with compression_level_for :484-501,
+// min_compression_input_bytes :452-460, min_compression_savings_bytes :462-482.
+// Returns true (and the compressed bytes in z) when the compressed payload is
+// kept.
+static bool zstd_if_smaller(const std::vector<uint8_t>& payload, size_t rows, unsigned k, int base_level,
+                            std::vector<uint8_t>& z) {
+  if (base_level <= 0) return false;
+  const bool used_dvle = true;  // u64 / u128 keys always encode DVLE
+  const size_t es = k <= 31 ? 12 : 20;
+  const size_t pb = payload.size(), logical = rows * es;
+  int level = base_level;
+  if (used_dvle && es == 12 && k <= 31 && pb >= 1024 * 1024) level += 1;
+  if (logical >= pb * 2 && pb >= 4 * 1024 * 1024) level += 1;
+  level = std::min(level, 6);
+  const size_t min_in = (es == 12 && k <= 31) ? 16 * 1024 : 32 * 1024;
+  if (level <= 0 || pb < min_in) return false;
+  const ZstdLib& zl = zstd_lib();
+  z.resize(zl.bound(pb));
+  const size_t got = zl.compress(z.data(), z.size(), payload.data(), pb, level);
+  if (zl.is_error(got)) return false;
+  z.resize(got);
+  const size_t bias = std::min<size_t>((logical > pb ? logical - pb : 0) / 32, 24 * 1024);
+  const size_t floor = std::max<size_t>(es == 12 ? 8 * 1024 : 16 * 1024, pb / 100);
+  const size_t min_savings = floor > bias ? floor - bias : 0;
+  return got + min_savings < pb;
+}
+
 template <class T>
 static void encode_dvle(const T* keys, const uint32_t* counts, size_t n, std::vector<uint8_t>& out) {
   if (n == 0) return;
@@ -904,6 +959,9 @@ struct Worker {
   std::vector<uint32_t> counts;
   std::vector<uint8_t> payload;
 
+  int zstd_level = 0;  // CountMode::zstd_level src/cli.rs:11-19 (fast 0, balanced 2, compact 5)
+  std::vector<uint8_t> zbuf;
+
   Worker(unsigned k_, bool c, size_t P, size_t thr, Writer* wr)
       : k(k_), canonical(c), partitions(P), flush_threshold(thr), w(wr) {
     bits = 0;
@@ -947,9 +1005,14 @@ struct Worker {
     rle(buckets[b], keys, counts);
     payload.clear();
     encode_dvle(keys.data(), counts.data(), keys.size(), payload);
-    if (w)
-      w->append_chunk(b, 2, keys.size(), payload.size(), (u128)keys.front(), 0, (u128)keys.back(), 0,
-                      payload.data(), payload.size());
+    if (w) {
+      if (zstd_if_smaller(payload, keys.size(), k, zstd_level, zbuf))
+        w->append_chunk(b, 2 | 4, keys.size(), payload.size(), (u128)keys.front(), 0, (u128)keys.back(), 0,
+                        zbuf.data(), zbuf.size());
+      else
+        w->append_chunk(b, 2, keys.size(), payload.size(), (u128)keys.front(), 0, (u128)keys.back(), 0,
+                        payload.data(), payload.size());
+    }
     buckets[b].clear();
   }
   void flush_all() {
@@ -968,9 +1031,13 @@ struct CountStats {
 template <class T>
 static void count_chunks(const std::vector<std::pair<const uint8_t*, size_t>>& chunks,
                                          unsigned k, bool canonical, size_t P, size_t workers,
-                                         size_t flush_threshold, Writer* writer, CountStats& st) {
+                                         size_t flush_threshold, Writer* writer, CountStats& st,
+                                         int zstd_level = 0) {
   std::vector<std::unique_ptr<Worker<T>>> ws;
-  for (size_t i = 0; i < workers; ++i) ws.emplace_back(new Worker<T>(k, canonical, P, flush_threshold, writer));
+  for (size_t i = 0; i < workers; ++i) {
+    ws.emplace_back(new Worker<T>(k, canonical, P, flush_threshold, writer));
+    ws.back()->zstd_level = zstd_level;
+  }
   std::atomic<size_t> next(0);
   auto run = [&](size_t wi) {
     for (;;) {
@@ -1127,7 +1194,19 @@ struct Reader {
         l.rows = get_le(ce + 32, 8);
         if (l.len == 0 || l.off + l.len > n) throw Error("partition " + std::to_string(b) + " chunk out of bounds");
         if (l.codec & ~7u) throw Error("partition " + std::to_string(b) + " chunk uses unsupported codec mask");
-        if (l.codec & 4u) throw Error("zstd chunks are not supported by the oracle");
+        if (l.codec & 4u) {
+          // run_data_for_decode src/dump/reader.rs:162-186: the decoded
+          // payload, appended after the file image
+          const ZstdLib& zl = zstd_lib();
+          const size_t at = bytes.size();
+          bytes.resize(at + l.raw);
+          const size_t got = zl.decompress(bytes.data() + at, l.raw, p + l.off, l.len);
+          if (zl.is_error(got)) throw Error("zstd decompress failed");
+          if (got != l.raw) throw Error("decoded payload size mismatch");
+          l.off = at;
+          l.len = l.raw;
+          l.codec &= ~4u;
+        }
         parts[b].push_back(l);
       }
     }
@@ -1872,6 +1951,7 @@ static int cmd_count(int argc, char** argv) {
   uint32_t mn = 0, mx = 0;
   size_t threads = 0, partitions = 0, chunk_kmers = 0, workers_override = 1;
   long buffer_mb = -1;
+  int zstd_level = 0;
   for (int i = 0; i < argc; ++i) {
     std::string a = argv[i];
     auto val = [&]() -> std::string {
@@ -1889,7 +1969,13 @@ static int cmd_count(int argc, char** argv) {
     else if (a == "--chunk-kmers") chunk_kmers = std::stoul(val());
     else if (a == "--memory") mem = val();
     else if (a == "--buffer") buffer_mb = std::stol(val());
-    else if (a == "--mode") { std::string m = val(); if (m != "fast") throw Error("oracle supports --mode fast only"); }
+    else if (a == "--mode") {
+      const std::string m = val();
+      if (m == "fast") zstd_level = 0;
+      else if (m == "balanced") zstd_level = 2;
+      else if (m == "compact") zstd_level = 5;
+      else throw Error("invalid --mode " + m);
+    }
     else if (a == "--workers") workers_override = std::stoul(val());
     else throw Error("unknown argument " + a);
   }
@@ -1920,8 +2006,9 @@ static int cmd_count(int argc, char** argv) {
   std::vector<std::pair<const uint8_t*, size_t>> chunks;
   for (auto& c : store) chunks.push_back({c.data(), c.size()});
   CountStats st;
-  if (k <= 31) count_chunks<uint64_t>(chunks, k, canonical, plan.partitions, workers, plan.local_flush_bytes, &w, st);
-  else count_chunks<u128>(chunks, k, canonical, plan.partitions, workers, plan.local_flush_bytes, &w, st);
+  if (k <= 31)
+    count_chunks<uint64_t>(chunks, k, canonical, plan.partitions, workers, plan.local_flush_bytes, &w, st, zstd_level);
+  else count_chunks<u128>(chunks, k, canonical, plan.partitions, workers, plan.local_flush_bytes, &w, st, zstd_level);
   uint64_t tc = 0, tr = 0;
   auto file = w.finalize(&tc, &tr);
   if (out != "/dev/null") write_file(out, file);

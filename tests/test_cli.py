@@ -81,7 +81,7 @@ def test_merge_matches_oracle(gpu, orc, tmp_path):
     (["-k", "129"], "invalid k-mer length"),
     (["--partitions", "3"], "must be a power of 2"),
     (["--min", "5", "--max", "2"], "--min must be less than or equal to --max"),
-    (["-k", "21", "--mode", "compact"], "zstd"),
+    (["-k", "21", "--mode", "tiny"], "possible values: fast, balanced, compact"),
 ])
 def test_count_argument_errors(built, fastq, args, msg):
     d, plain, _, _ = fastq
@@ -104,3 +104,47 @@ def test_info_marker_edit(built, orc, tmp_path):
     assert "min\tnone" in out and "max\t9" in out
     r = run([CLI, "info", "-i", p, "--set-min", "10"], check=False)
     assert r.returncode != 0 and b"must be <=" in r.stderr
+
+
+def _zstd_chunks(image: bytes) -> int:
+    from kite_gb300.kitefile import KiteImage
+    return sum(1 for ch in KiteImage.parse(image).chunks if ch.codec & 4)
+
+
+@pytest.mark.parametrize("mode", ["balanced", "compact"])
+def test_zstd_modes_read_back(built, orc, tmp_path, mode):
+    # the oracle's count with zstd "if smaller": the host reader decompresses
+    # the zstd chunks and its dump equals the oracle's
+    fq = tmp_path / "z.fq"
+    fq.write_bytes(synth.small_workload(seed=23, n_reads=30_000, genome_len=200_000))
+    out = tmp_path / "z.kite"
+    run([ORACLE, "count", "-i", fq, "-o", out, "-k", "25", "--canonical", "true", "--partitions", "4",
+         "--memory", "64G", "-t", "3", "--mode", mode])
+    image = out.read_bytes()
+    assert _zstd_chunks(image) > 0
+    from kite_gb300 import host
+    assert host.dump_image(image) == orc.dump(image)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["balanced", "compact"])
+@pytest.mark.parametrize("k", [21, 31, 45])
+def test_zstd_modes_match_oracle(gpu, orc, tmp_path, mode, k):
+    # `kite count --mode balanced|compact`: byte-identical .kite files (the
+    # same zstd library on both sides), identical dump, and a merge of zstd
+    # inputs identical to the oracle's
+    fq = tmp_path / "z.fq"
+    fq.write_bytes(synth.small_workload(seed=24, n_reads=40_000, genome_len=300_000))
+    common = ["-i", fq, "-k", str(k), "--canonical", "true", "--partitions", "8", "--memory", "64G", "-t", "3",
+              "--mode", mode]
+    run([CLI, "count", "-o", tmp_path / "g.kite", *common])
+    run([ORACLE, "count", "-o", tmp_path / "r.kite", *common])
+    g = (tmp_path / "g.kite").read_bytes()
+    assert g == (tmp_path / "r.kite").read_bytes()
+    assert _zstd_chunks(g) > 0
+    a = run([CLI, "dump", "-i", tmp_path / "g.kite", "-o", "-"]).stdout
+    assert a == run([ORACLE, "dump", "-i", tmp_path / "r.kite", "-o", "-"]).stdout and len(a) > 0
+    run([CLI, "count", "-o", tmp_path / "f.kite", *common[:-1], "fast"])
+    run([CLI, "merge", "-i", tmp_path / "g.kite", tmp_path / "f.kite", "-o", tmp_path / "m.kite"])
+    run([ORACLE, "merge", "-i", tmp_path / "g.kite", tmp_path / "f.kite", "-o", tmp_path / "n.kite"])
+    assert (tmp_path / "m.kite").read_bytes() == (tmp_path / "n.kite").read_bytes()
