@@ -302,12 +302,13 @@ def run_batch_bench(args, world, rank, local):
     """16 samples of uneven size from a 64-species Zipf(1.2) metagenome
     (300 kbp i.i.d. genomes, reads 100-250 bp, 0.5% substitutions; read
     counts U[0.5M, 8M] x --batch-scale), k=31 canonical, 256 partitions per
-    sample.  One step = all 16 samples counted by one batched launch sequence
+    sample.  One step = all 16 samples counted in batched launch sequences (one,
+    or --batch-groups G groups of samples at full read counts)
     (cfg.samples = 16) with the autotuned tile fill and scatter shape; the
     same samples counted by 16 sequential plain runs are timed beside it."""
     import torch
     from kite_gb300 import autotune, gpu, ingest, synth
-    samples = synth.metagenome_samples(seed=3 + rank, scale=args.batch_scale)
+    samples = synth.metagenome_samples(seed=3 + rank, scale=args.batch_scale, fast=True)
     S = len(samples)
     # device-resident copies, every chunk 16-byte aligned with 16 pad bytes
     chunks = []  # (sample, device offset, length)
@@ -324,10 +325,21 @@ def run_batch_bench(args, world, rank, local):
     stream = torch.cuda.current_stream()
     fastq_bytes = sum(len(x) for x in samples)
 
-    def batched(c):
-        for s, o, d, l in chunks:
-            c.submit_device(base + d, l, sample=s)
-        c.finish(collect=False)
+    # samples in --batch-groups contiguous groups, one launch sequence (one
+    # finish) per group: at the full read counts the working buffers of all
+    # 16 samples at once would not fit in HBM
+    G = max(1, min(args.batch_groups, S))
+    groups = [range(S * g // G, S * (g + 1) // G) for g in range(G)]
+
+    def batched(c, cb=None):
+        for grp in groups:
+            for s, o, d, l in chunks:
+                if s in grp:
+                    c.submit_device(base + d, l, sample=s)
+            if cb is None:
+                c.finish(collect=False)
+            else:
+                c.finish(collect=True, callback=cb, raw=True)
 
     ctxs = {}  # one live context at a time: each holds the batch's working buffers
 
@@ -369,9 +381,48 @@ def run_batch_bench(args, world, rank, local):
     torch.cuda.synchronize()
     barrier(world)
     ms = max_over_ranks(world, e0.elapsed_time(e1)) / args.steps
-    st = c.stats()
-    kmers = st["kmers"]
-    per_sample = [c.sample_totals(s) for s in range(S)]
+    per_sample = []
+    kmers = 0
+    # with --batch-parity, every sample's partitions (one more untimed pass)
+    # against the oracle's count of that sample alone
+    parity = None
+    if args.batch_parity and rank == 0:
+        import ctypes as Cc
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+        got = {}
+
+        def keep(m, addr, n):
+            got[m["partition_id"]] = (m, bytes((Cc.c_uint8 * n).from_address(addr)) if n else b"")
+        batched(c, keep)
+        bad = []
+        t0 = time.perf_counter()
+        for s_ in range(S):
+            ref = oracle.count_parts(samples[s_], K, CANONICAL, PARTITIONS, os.cpu_count() or 1)
+            for p in range(PARTITIONS):
+                g_ = got.get(s_ * PARTITIONS + p)
+                if ref.rows[p] == 0:
+                    if g_ is not None:
+                        bad.append((s_, p))
+                    continue
+                if (g_ is None or g_[0]["row_count"] != ref.rows[p] or g_[0]["key_min"] != ref.key_min[p]
+                        or g_[0]["key_max"] != ref.key_max[p] or g_[1] != bytes(ref.payload(p))):
+                    bad.append((s_, p))
+            ref.close()
+        got.clear()
+        parity = {"ok": not bad, "samples": S, "mismatched": bad[:10],
+                  "oracle_seconds": round(time.perf_counter() - t0, 1),
+                  "method": "every sample's partitions from the batched count compared byte for byte with the "
+                            "oracle's single-worker count of that sample alone"}
+    # per-sample totals of every group's finish
+    for grp in groups:
+        for s_, o, d, l in chunks:
+            if s_ in grp:
+                c.submit_device(base + d, l, sample=s_)
+        c.finish(collect=False)
+        for s_ in grp:
+            per_sample.append(c.sample_totals(s_))
+            kmers += per_sample[-1][2]
     c.close()
     # 16 sequential plain runs of the same samples (one context, one finish each)
     cp = gpu.Counter(K, CANONICAL, PARTITIONS, device=local, splitter_mode=gpu.SPLIT_SAMPLED,
@@ -406,7 +457,7 @@ def run_batch_bench(args, world, rank, local):
                            "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
                 "sequential_plain": {"value": sum_over_ranks(world, kmers) / (ms_seq / 1e3), "unit": UNIT,
                                      "ms_per_step": ms_seq},
-                "batched_over_sequential": ms_seq / ms,
+                "batched_over_sequential": ms_seq / ms, "groups": G, "parity": parity,
                 "autotune": {"chosen": best, "table": table},
                 "gpu_launches": launches}
         print(json.dumps(line))
@@ -510,6 +561,78 @@ def _bgzf_bytes(data: bytes, block: int = 65280, level: int = 1) -> bytes:
         head = struct.pack("<BBBBIBBHBBHH", 0x1F, 0x8B, 8, 4, 0, 0, 0xFF, 6, 0x42, 0x43, 2, 18 + len(comp) + 7)
         out.append(head + comp + struct.pack("<II", zlib.crc32(piece) & 0xFFFFFFFF, len(piece)))
     return b"".join(out)
+
+
+def _gzip_members(data, piece: int = 64 << 20, level: int = 1) -> bytes:
+    """Multi-member gzip of data (pieces compressed on all host threads; the
+    readers decode it as one stream, as MultiGzDecoder does)."""
+    import concurrent.futures as cf
+    import gzip as gz
+    mv = memoryview(data)
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        parts = list(ex.map(lambda o: gz.compress(bytes(mv[o:o + piece]), compresslevel=level, mtime=0),
+                            range(0, len(data), piece)))
+    return b"".join(parts)
+
+
+def _bgzf_parallel(data, block: int = 65280) -> bytes:
+    import concurrent.futures as cf
+    mv = memoryview(data)
+    step = block * 512
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        parts = list(ex.map(lambda o: _bgzf_bytes(bytes(mv[o:o + step]), block), range(0, len(data), step)))
+    return b"".join(parts)
+
+
+def e2e_cli_leg(data, local: int, partitions: int) -> dict:
+    """The drop-in command end to end on this workload as configured: wall
+    time of `kite count` (GPU) from a gzip file and from a BGZF copy of the
+    same reads, including inflate, context setup and the .kite write,
+    against the oracle's command line (the CPU restatement, all host cores)
+    on the gzip file, and the serial gzip reader's own ceiling."""
+    from kite_gb300 import CLI, host
+    tmp = Path(tempfile.mkdtemp(prefix="kite_e2e_"))
+    gzf, bgzf = tmp / "r.fq.gz", tmp / "r.bgzf.fq.gz"
+    gzf.write_bytes(_gzip_members(data))
+    bgzf.write_bytes(_bgzf_parallel(data))
+    cores = os.cpu_count() or 1
+    flags = ["-k", str(K), "--canonical", "true", "--min", "2", "--max", "1000000", "--partitions", str(partitions),
+             "--memory", "64G", "-t", str(cores)]
+
+    def timed(cmd):
+        t0 = time.perf_counter()
+        r = subprocess.run([str(c) for c in cmd], capture_output=True, text=True)
+        dt = time.perf_counter() - t0
+        if r.returncode != 0:
+            raise RuntimeError(r.stderr[-2000:])
+        return int(r.stderr.split("kmers=")[1].split()[0]), dt
+
+    out = {}
+    for name, path in (("gzip", gzf), ("bgzf", bgzf)):
+        timed([CLI, "count", "-i", path, "-o", tmp / "g.kite", *flags, "--device", str(local)])  # warm file cache
+        kmers, dt = timed([CLI, "count", "-i", path, "-o", tmp / "g.kite", *flags, "--device", str(local)])
+        out[name] = {"kmers_per_s": kmers / dt, "seconds": round(dt, 3)}
+    orc = ROOT / "oracle" / "_build" / "kite_oracle"
+    kmers, dt = timed([orc, "count", "-i", gzf, "-o", tmp / "r.kite", *flags, "--workers", str(max(1, cores - 2))])
+    out["oracle_cli_gzip"] = {"kmers_per_s": kmers / dt, "seconds": round(dt, 3), "cores": cores,
+                              "kind": "port"}
+    t0 = time.perf_counter()
+    n = sum(host.read_chunks(gzf, 64 << 20, 1, collect=False))
+    gz_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    nb = sum(host.read_chunks(bgzf, 64 << 20, cores, collect=False))
+    bg_s = time.perf_counter() - t0
+    out["reader_ceiling"] = {"gzip_serial_gbs": round(n / gz_s / 1e9, 3), "gzip_kmers_per_s": kmers / gz_s,
+                             "bgzf_gbs": round(nb / bg_s / 1e9, 3), "bgzf_kmers_per_s": kmers / bg_s,
+                             "threads": cores}
+    out["files"] = {"fastq_bytes": len(data), "gzip_bytes": gzf.stat().st_size, "bgzf_bytes": bgzf.stat().st_size,
+                    "gzip": "multi-member gzip, level 1, 64 MiB members", "bgzf": "65,280-byte blocks, level 1"}
+    out["flags"] = " ".join(flags)
+    for p in (gzf, bgzf, tmp / "g.kite", tmp / "r.kite"):
+        if p.exists():
+            p.unlink()
+    tmp.rmdir()
+    return out
 
 
 def run_ingest_bench(args, world, rank, local):
@@ -722,6 +845,11 @@ def main():
     ap.add_argument("--ref-reads", type=int, default=0,
                     help="reads of the CPU baseline and the reference arm (0 = the whole workload)")
     ap.add_argument("--no-parity", action="store_true", help="skip the full-size comparison with the oracle")
+    ap.add_argument("--no-cli", action="store_true", help="skip the command-line leg (gzip / BGZF files)")
+    ap.add_argument("--batch-groups", type=int, default=1,
+                    help="samples counted in this many launch sequences (one finish each)")
+    ap.add_argument("--batch-parity", action="store_true",
+                    help="compare every sample of the batch with the oracle (untimed)")
     ap.add_argument("--partitions", type=int, default=PARTITIONS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-splitter-compare", action="store_true")
@@ -939,6 +1067,10 @@ def main():
     ce.close()
     c.close()
 
+    cli = None
+    if rank == 0 and world == 1 and not args.no_cli and not skewed:
+        cli = e2e_cli_leg(data, local, args.partitions)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(data, layout, args.ref_reads or args.reads, os.cpu_count() or 1, kk,
@@ -968,7 +1100,7 @@ def main():
                         # device stages of the end-to-end count (the first two include waiting for the copies)
                         "stage_ms": {stages[i][0]: round(e2e_parts["stage_ms"][i] / args.steps, 3) for i in stages}},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-                "parity": parity,
+                "parity": parity, "e2e_cli": cli,
                 "splitters": splitters,
                 "tiles": {"tiles": st["tiles"], "per_bucket": st["tiles_per_bucket"], "big": st["big_tiles"],
                           "imbalance": st["tile_imbalance"], "sort_fallbacks": st["sort_fallbacks"]}}

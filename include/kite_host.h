@@ -120,6 +120,10 @@ double kite_sample_avg_read_len(const char* path, int compression);
 int64_t kite_synth_reads(const uint8_t* genome, uint64_t genome_len, uint64_t n_reads, uint32_t read_len,
                          double sub_rate, double n_rate, double revcomp_frac, uint64_t seed, uint64_t first_index,
                          uint8_t* out, uint64_t cap, int threads);
+/* The same with read lengths uniform in [len_lo, len_hi], records back to back. */
+int64_t kite_synth_reads_var(const uint8_t* genome, uint64_t genome_len, uint64_t n_reads, uint32_t len_lo,
+                             uint32_t len_hi, double sub_rate, double n_rate, double revcomp_frac, uint64_t seed,
+                             uint64_t first_index, uint8_t* out, uint64_t cap, int threads);
 
 #ifdef __cplusplus
 }

@@ -19,6 +19,7 @@ EXPORTED = [
     "kite_reader_merge_input", "kite_dump_partition", "kite_detect_compression", "kite_input_open",
     "kite_input_next", "kite_input_max_chunk", "kite_input_close", "kite_sample_avg_read_len", "kite_synth_reads",
     "kite_input_set_threads", "kite_zstd_available", "kite_zstd_bound", "kite_zstd_chunk",
+    "kite_synth_reads_var",
 ]
 
 
@@ -223,3 +224,25 @@ def synth_reads(genome_codes, n_reads: int, read_len: int, sub_rate: float, n_ra
     if n < 0:
         raise RuntimeError(err())
     return out
+
+
+def synth_reads_var(genome_codes, n_reads: int, len_lo: int, len_hi: int, sub_rate: float, seed: int,
+                    first_index: int = 0, threads: int = 8) -> bytearray:
+    """Reads of lengths uniform in [len_lo, len_hi] sampled from genome_codes
+    (forward strand, substitutions only), multithreaded and deterministic."""
+    import numpy as np
+    g = np.ascontiguousarray(genome_codes, dtype=np.uint8)
+    cap = n_reads * (2 * len_hi + 16)
+    out = bytearray(cap)
+    buf = (C.c_uint8 * len(out)).from_buffer(out)
+    L = lib()
+    L.kite_synth_reads_var.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, C.c_double,
+                                       C.c_double, C.c_double, C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint64,
+                                       C.c_int]
+    L.kite_synth_reads_var.restype = C.c_int64
+    n = L.kite_synth_reads_var(g.ctypes.data, len(g), n_reads, len_lo, len_hi, sub_rate, 0.0, 0.0, seed,
+                               first_index, C.addressof(buf), cap, threads)
+    if n < 0:
+        raise RuntimeError(err())
+    del buf
+    return out[:n]

@@ -1364,4 +1364,69 @@ int64_t kite_synth_reads(const uint8_t* genome, uint64_t glen, uint64_t n_reads,
   return (int64_t)(n_reads * rec);
 }
 
+// Variable read lengths, uniform in [len_lo, len_hi] (drawn first from each
+// read's own stream), records packed back to back; otherwise as
+// kite_synth_reads.  Returns the bytes written, or -1.
+int64_t kite_synth_reads_var(const uint8_t* genome, uint64_t glen, uint64_t n_reads, uint32_t len_lo, uint32_t len_hi,
+                             double sub_rate, double n_rate, double rc_frac, uint64_t seed, uint64_t first_index,
+                             uint8_t* out, uint64_t cap, int threads) {
+  if (len_lo == 0 || len_hi < len_lo || glen < len_hi) return set_err("synth: bad sizes");
+  auto stream = [seed](uint64_t idx) { return seed * 0x9E3779B97F4A7C15ull + idx * 0xD1B54A32D192ED03ull; };
+  auto mix = [](uint64_t& st) {
+    uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  const uint32_t span = len_hi - len_lo + 1;
+  std::vector<uint64_t> off(n_reads + 1, 0);
+  for (uint64_t r = 0; r < n_reads; ++r) {
+    uint64_t st = stream(first_index + r);
+    const uint32_t L = len_lo + (uint32_t)(mix(st) % span);
+    off[r + 1] = off[r] + 2ull * L + 16;
+  }
+  if (off[n_reads] > cap) return set_err("synth: output buffer too small");
+  const int nt = std::max(1, threads);
+  auto work = [&](uint64_t r0, uint64_t r1) {
+    static const char dna[4] = {'A', 'C', 'G', 'T'};
+    for (uint64_t r = r0; r < r1; ++r) {
+      uint64_t st = stream(first_index + r);
+      const uint32_t L = len_lo + (uint32_t)(mix(st) % span);
+      auto unif = [&]() { return (double)(mix(st) >> 11) * (1.0 / 9007199254740992.0); };
+      uint8_t* o = out + off[r];
+      const uint64_t idx = first_index + r;
+      o[0] = '@';
+      o[1] = 'r';
+      for (int d = 0; d < 9; ++d) {
+        uint64_t p = 1;
+        for (int e = 0; e < 8 - d; ++e) p *= 10;
+        o[2 + d] = (uint8_t)('0' + (idx / p) % 10);
+      }
+      o[11] = '\n';
+      const uint64_t start = mix(st) % (glen - L + 1);
+      const bool minus = unif() < rc_frac;
+      uint8_t* sq = o + 12;
+      for (uint32_t i = 0; i < L; ++i) {
+        uint8_t c = minus ? (uint8_t)(3 - genome[start + L - 1 - i]) : genome[start + i];
+        if (sub_rate > 0 && unif() < sub_rate) c = (uint8_t)((c + 1 + mix(st) % 3) & 3);
+        sq[i] = (uint8_t)dna[c];
+        if (n_rate > 0 && unif() < n_rate) sq[i] = 'N';
+      }
+      o[12 + L] = '\n';
+      o[13 + L] = '+';
+      o[14 + L] = '\n';
+      memset(o + 15 + L, 'I', L);
+      o[15 + 2 * L] = '\n';
+    }
+  };
+  std::vector<std::thread> th;
+  const uint64_t per = (n_reads + nt - 1) / nt;
+  for (int t = 0; t < nt; ++t) {
+    const uint64_t a = t * per, b = std::min<uint64_t>(n_reads, a + per);
+    if (a < b) th.emplace_back(work, a, b);
+  }
+  for (auto& x : th) x.join();
+  return (int64_t)off[n_reads];
+}
+
 }  // extern "C"

@@ -135,12 +135,15 @@ def skewed_workload(seed: int = 4, n_reads: int = 4_000_000, genome_len: int = 2
 
 
 def metagenome_samples(seed: int = 3, n_samples: int = 16, species: int = 64, species_len: int = 300_000,
-                       reads_lo: int = 500_000, reads_hi: int = 8_000_000, scale: float = 1.0) -> list[bytes]:
-    """Uneven samples of a Zipf(1.2) metagenome; `scale` shrinks read counts."""
+                       reads_lo: int = 500_000, reads_hi: int = 8_000_000, scale: float = 1.0,
+                       fast: bool = False) -> list:
+    """Uneven samples of a Zipf(1.2) metagenome; `scale` shrinks read counts.
+    fast: reads from the host library's multithreaded generator (same shape,
+    another random stream), for the full read counts."""
     rng = np.random.default_rng(seed)
     genomes = [genome_iid(np.random.default_rng(seed * 1000 + s), species_len) for s in range(species)]
     out = []
-    for _ in range(n_samples):
+    for si in range(n_samples):
         n = max(1, int(rng.integers(reads_lo, reads_hi + 1) * scale))
         ranks = rng.permutation(species) + 1
         w = 1.0 / ranks ** 1.2
@@ -148,7 +151,13 @@ def metagenome_samples(seed: int = 3, n_samples: int = 16, species: int = 64, sp
         per = rng.multinomial(n, w)
         parts = []
         for s, c in enumerate(per):
-            if c:
+            if c and fast:
+                import os
+                from . import host
+                parts.append(host.synth_reads_var(genomes[s], int(c), 100, 250, 0.005,
+                                                  seed=seed * 1_000_003 + si * 1009 + s,
+                                                  threads=max(1, os.cpu_count() or 1)))
+            elif c:
                 parts.append(reads_variable(rng, genomes[s], int(c), 100, 250, 0.005))
         out.append(b"".join(parts))
     return out
