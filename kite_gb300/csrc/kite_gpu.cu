@@ -1149,8 +1149,11 @@ int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n,
   if (!ctx || !inputs || n <= 0) return KITE_ERR_BAD_INPUT;
   cudaSetDevice(ctx->cfg.device);
   std::string msg;
+  MergeExtra ex;
+  ex.mlp = ctx->mlp;
+  ex.splitter_mode = ctx->cfg.splitter_mode;
   int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, inputs, n, ctx->stream, ctx->cfg.timeout_ms,
-                     kMergeModeMerge, emit, user, &msg, &ctx->stats);
+                     kMergeModeMerge, emit, user, &msg, &ctx->stats, nullptr, &ex);
   if (rc) ctx->err = msg;
   return rc;
 }

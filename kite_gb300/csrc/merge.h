@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include "kite_gpu.h"
+#include "mlp.h"
 
 namespace kite {
 
@@ -24,6 +25,8 @@ struct MergeExtra {
   const uint32_t* parts = nullptr;    // query: partition of each key
   size_t nq = 0;
   uint64_t* counts_out = nullptr;     // query: u64 sum per key, 0 when absent
+  MlpModel* mlp = nullptr;            // learned CDF for the tile cut (null: sampled histogram only)
+  int splitter_mode = 0;              // KITE_SPLIT_*: AUTO keeps whichever predicts the lower imbalance
 };
 
 // k selects the key width (u64 for k <= 31, else u128) and the splitter key

@@ -11,9 +11,10 @@
 //                           otherwise one DVLE chunk per non-empty partition.
 //
 // GPU structure:
-//   decode    payload bytes cut into 2 KiB segments; per-segment varint
-//             terminator counts and parity sums, per-stream scans on the
-//             device, then a pass that writes (key, u64 count) rows.  A
+//   decode    payload bytes cut into 8 KiB segments, one warp each;
+//             per-segment varint terminator counts and parity sums,
+//             per-stream scans on the device, then a pass that writes
+//             (key, u64 count) rows.  A
 //             "stream" is one chunk.
 //   tiles     key-range tiles per partition from global splitters, refined by
 //             bisection until every tile fits on chip; each stream is
@@ -47,7 +48,7 @@ namespace kite {
 
 namespace {
 
-constexpr uint32_t kSeg = 2048;          // decode segment bytes
+constexpr uint32_t kSeg = 8192;          // decode segment bytes (one warp each)
 constexpr int kMergeThreads = 512;
 constexpr uint32_t kMergeCap = 4096;      // rows per merge tile
 constexpr uint32_t kMaxTileStreams = 256; // streams per tile (inputs x chunks)
@@ -117,27 +118,6 @@ struct MergeTile {
 
 __device__ __forceinline__ bool is_term(uint8_t b) { return (b & 0x80u) == 0; }
 
-// Bytes of the payload buffer read through 16-byte aligned loads kept in
-// registers: a thread walking its segment byte by byte issues one memory
-// request per 16 bytes.  The buffer is allocated with padding past its last
-// byte, so the aligned block of any byte offset inside it is readable.
-struct ByteReader {
-  const uint4* base;
-  uint64_t blk = ~0ull;
-  uint4 w;
-  __device__ __forceinline__ explicit ByteReader(const uint8_t* b) : base(reinterpret_cast<const uint4*>(b)) {}
-  __device__ __forceinline__ uint8_t at(uint64_t q) {
-    const uint64_t b = q >> 4;
-    if (b != blk) {
-      w = __ldg(base + b);
-      blk = b;
-    }
-    const unsigned i = (unsigned)(q & 15u);
-    const unsigned word = i < 8 ? (i < 4 ? w.x : w.y) : (i < 12 ? w.z : w.w);
-    return (uint8_t)(word >> (8 * (i & 3u)));
-  }
-};
-
 // Warp shuffle-up of a 64- or 128-bit value, a wrapping inclusive warp sum,
 // and a broadcast from one lane.
 template <class T>
@@ -170,46 +150,155 @@ __device__ __forceinline__ T warp_bcast_t(T v, int src) {
     return ((T)hi << 64) | (T)lo;
   }
 }
-
-// Pass A, one thread per segment: the varints whose terminator lies in the
-// segment, and the wrapping sums of those at even / odd positions within the
-// segment (which of the two are key deltas follows from the parity of the
-// segment's first varint index, known after the per-stream scan).
 template <class T>
-__global__ void k_seg_pass_a(const uint8_t* __restrict__ bytes, const SegDesc* __restrict__ segs, uint32_t nseg,
-                             const StreamDesc* __restrict__ streams, uint32_t* __restrict__ terms,
-                             T* __restrict__ sum_even, T* __restrict__ sum_odd) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nseg) return;
-  const SegDesc d = segs[s];
+__device__ __forceinline__ T warp_sum_t(T v) {
+  return warp_bcast_t(warp_incl_sum(v), 31);
+}
+
+// ---- warp-cooperative DVLE decode ----------------------------------------------
+// A segment (kSeg bytes of one stream's varint area) is decoded by one warp in
+// rounds of 512 bytes: every lane loads 16 bytes (one coalesced 512-byte load
+// per warp) into a per-warp shared-memory window that also holds the 32 bytes
+// before the round, marks the terminator bytes (top bit clear) and decodes
+// the varints whose terminator lies in its own 16 bytes, reading back to the
+// previous terminator in the window (a varint is at most 19 bytes).  A varint
+// belongs to the segment holding its terminator; the stream's bytes before
+// its varint area (the raw head row) bound the first varint.  A final varint
+// without a terminator at the stream's end belongs to the last segment.
+constexpr int kDecWarps = 8;                    // warps per decode CTA
+constexpr uint32_t kRound = 512;                // bytes per warp round
+constexpr uint32_t kWinBytes = kRound + 32;     // window: 32 bytes before the round + the round
+
+struct DecWindow {
+  uint8_t b[kWinBytes];
+};
+
+// Terminator bits of 16 bytes (bit i: byte i has its top bit clear).
+__device__ __forceinline__ uint32_t term_bits16(uint4 w) {
+  auto m4 = [](uint32_t x) {
+    const uint32_t t = ~x & 0x80808080u;
+    return ((t >> 7) & 1u) | ((t >> 14) & 2u) | ((t >> 21) & 4u) | ((t >> 28) & 8u);
+  };
+  return m4(w.x) | (m4(w.y) << 4) | (m4(w.z) << 8) | (m4(w.w) << 12);
+}
+
+// Loads the round at `base` (16-byte aligned) into the window: bytes
+// [base - 32, base + 512); blocks at or beyond lim_pad (the padded end of
+// the byte buffer) and before byte 0 read as zero.
+__device__ __forceinline__ void load_round(const uint8_t* __restrict__ bytes, uint64_t base, uint64_t lim_pad,
+                                           DecWindow* win, uint32_t lane) {
+  uint4* wv = reinterpret_cast<uint4*>(win->b);
+  const uint64_t o = base + 16ull * lane;
+  uint4 v = make_uint4(0, 0, 0, 0);
+  if (o < lim_pad) v = *reinterpret_cast<const uint4*>(bytes + o);
+  wv[2 + lane] = v;
+  if (lane < 2) {
+    uint4 p = make_uint4(0, 0, 0, 0);
+    if (base >= 32) p = *reinterpret_cast<const uint4*>(bytes + base - 32 + 16 * lane);
+    wv[lane] = p;
+  }
+  __syncwarp();
+}
+
+// The value of the varint ending at window byte t (32 <= t < 48) of the
+// lane's 48-byte view: bytes from one past the previous boundary bit of
+// `bound` below t up to t.
+template <class T>
+__device__ __forceinline__ T varint_at(const DecWindow* win, uint64_t bound, uint32_t lane_off, int t) {
+  const uint64_t below = bound & ((1ull << t) - 1ull);
+  const int start = below ? 64 - __clzll(below) : 0;
+  T val = 0;
+  unsigned sh = 0;
+  for (int j = start; j <= t; ++j) {
+    const uint8_t b = win->b[lane_off + j];
+    if (sh < (unsigned)KeyTraits<T>::kBits) val |= (T)(b & 0x7f) << sh;
+    sh += 7;
+  }
+  return val;
+}
+
+// Per lane and round: `bound` marks over the lane's 48-byte view (window
+// bytes [16 lane, 16 lane + 48) = stream bytes base - 32 + 16 lane + i) the
+// terminators and every byte before the varint area (so the first varint
+// starts at the area); `own` marks the terminators of the lane's own 16 bytes
+// (view bits 32..47) inside [seg_lo, seg_hi).
+__device__ __forceinline__ void round_masks(const DecWindow* win, uint32_t lane, uint64_t base, uint64_t area,
+                                            uint64_t seg_lo, uint64_t seg_hi, uint64_t& bound, uint32_t& own) {
+  const uint4* wv = reinterpret_cast<const uint4*>(win->b);
+  const uint64_t t0 = term_bits16(wv[lane]), t1 = term_bits16(wv[lane + 1]), t2 = term_bits16(wv[lane + 2]);
+  bound = t0 | (t1 << 16) | (t2 << 32);
+  const uint64_t ob = base + 16ull * lane;  // stream byte of view bit 32
+  const int64_t nb = (int64_t)(32 + area) - (int64_t)ob;  // view bits below the varint area
+  if (nb > 0) bound |= nb >= 48 ? 0xFFFFFFFFFFFFull : ((1ull << nb) - 1ull);
+  const int64_t lo = (int64_t)seg_lo - (int64_t)ob, hi = (int64_t)seg_hi - (int64_t)ob;
+  uint32_t keep = 0xFFFFu;
+  if (lo > 0) keep &= lo >= 16 ? 0u : ~((1u << lo) - 1u);
+  if (hi < 16) keep &= hi <= 0 ? 0u : ((1u << hi) - 1u);
+  own = (uint32_t)t2 & keep;
+}
+
+// Pass A, one warp per segment: the varints the segment owns, and the
+// wrapping sums of those at even / odd positions within the segment (which
+// of the two are key deltas follows from the parity of the segment's first
+// varint index, known after the per-stream scan).
+template <class T>
+__global__ void __launch_bounds__(32 * kDecWarps)
+    k_seg_pass_a(const uint8_t* __restrict__ bytes, uint64_t lim_pad, const SegDesc* __restrict__ segs,
+                 uint32_t nseg, const StreamDesc* __restrict__ streams, uint32_t* __restrict__ terms,
+                 T* __restrict__ sum_even, T* __restrict__ sum_odd) {
+  __shared__ __align__(16) DecWindow wins[kDecWarps];
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint32_t si = blockIdx.x * kDecWarps + wid;
+  if (si >= nseg) return;
+  DecWindow* win = &wins[wid];
+  const SegDesc d = segs[si];
   const StreamDesc sd = streams[d.stream];
-  const uint64_t area = sd.byte_off + sd.head;
-  ByteReader rd(bytes);
-  // start of the first varint owned by this segment
-  uint64_t p = d.start;
-  while (p > area && !is_term(rd.at(p - 1))) --p;
-  const uint64_t lim = sd.byte_off + sd.byte_len;
-  uint32_t n = 0;
+  const uint64_t area = sd.byte_off + sd.head, lim = sd.byte_off + sd.byte_len;
+  uint32_t n = 0;  // varints owned so far (the same in every lane)
   T se = 0, so = 0;
-  while (p < d.end) {
+  for (uint64_t base = d.start & ~15ull; base < d.end; base += kRound) {
+    load_round(bytes, base, lim_pad, win, lane);
+    uint64_t bound;
+    uint32_t own;
+    round_masks(win, lane, base, area, d.start, d.end, bound, own);
+    const uint32_t c = __popc(own);
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    uint32_t idx = n + incl - c;
+    for (uint32_t m = own; m; m &= m - 1, ++idx) {
+      const T v = varint_at<T>(win, bound, 16 * lane, 32 + __ffs(m) - 1);
+      if (idx & 1u) so += v;
+      else se += v;
+    }
+    n += __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+  }
+  // a final varint without its terminator (the stream ends inside it)
+  if (d.end == lim && lim > area && lane == 0 && !is_term(bytes[lim - 1])) {
+    uint64_t p = lim;
+    while (p > area && !is_term(bytes[p - 1])) --p;
     T val = 0;
     unsigned sh = 0;
-    uint64_t q = p;
-    while (q < lim) {
-      const uint8_t b = rd.at(q++);
-      if (sh < (unsigned)KeyTraits<T>::kBits) val |= (T)(b & 0x7f) << sh;
+    for (uint64_t q = p; q < lim; ++q) {
+      if (sh < (unsigned)KeyTraits<T>::kBits) val |= (T)(bytes[q] & 0x7f) << sh;
       sh += 7;
-      if (is_term(b)) break;
     }
-    if (q > d.end) break;  // terminator in the next segment: that segment owns this varint
     if (n & 1u) so += val;
     else se += val;
     ++n;
-    p = q;
   }
-  terms[s] = n;
-  sum_even[s] = se;
-  sum_odd[s] = so;
+  n = __shfl_sync(0xffffffffu, n, 0);
+  se = warp_sum_t(se);
+  so = warp_sum_t(so);
+  if (lane == 0) {
+    terms[si] = n;
+    sum_even[si] = se;
+    sum_odd[si] = so;
+  }
 }
 
 // Per stream (one warp each): first varint index and start key of every
@@ -246,47 +335,77 @@ __global__ void k_stream_seg_scan(const uint32_t* __restrict__ terms, const T* _
   if (lane == 0 && sd.head && sd.rows && cv < 2 * (sd.rows - 1)) dev_fail(st, KITE_DEV_SHORT_VARINTS, si);
 }
 
-// Pass B, one thread per segment: (key, u64 count) rows of the varints whose
-// terminator lies in the segment.  Varint index v (within the stream's varint
-// area): even = key delta of row v/2+1, odd = count of row (v-1)/2+1.
+// Pass B, one warp per segment: (key, u64 count) rows of the varints the
+// segment owns.  Varint index v (within the stream's varint area): even =
+// key delta of row v/2+1, odd = count of row (v-1)/2+1.  Keys are the running
+// wrapping sum of the deltas (as the reference's wrapping_add), from the
+// segment's start key: each round a warp scan of the lanes' delta sums.
 template <class T>
-__global__ void k_seg_rows(const uint8_t* __restrict__ bytes, const SegDesc* __restrict__ segs, uint32_t nseg,
-                           const StreamDesc* __restrict__ streams, const unsigned long long* __restrict__ vstart,
-                           const T* __restrict__ kstart, T* __restrict__ keys, unsigned long long* __restrict__ counts) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nseg) return;
-  const SegDesc d = segs[s];
+__global__ void __launch_bounds__(32 * kDecWarps)
+    k_seg_rows(const uint8_t* __restrict__ bytes, uint64_t lim_pad, const SegDesc* __restrict__ segs,
+               uint32_t nseg, const StreamDesc* __restrict__ streams, const unsigned long long* __restrict__ vstart,
+               const T* __restrict__ kstart, T* __restrict__ keys, unsigned long long* __restrict__ counts) {
+  __shared__ __align__(16) DecWindow wins[kDecWarps];
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint32_t si = blockIdx.x * kDecWarps + wid;
+  if (si >= nseg) return;
+  DecWindow* win = &wins[wid];
+  const SegDesc d = segs[si];
   const StreamDesc sd = streams[d.stream];
-  const uint64_t area = sd.byte_off + sd.head;
-  ByteReader rd(bytes);
-  // start of the first varint owned by this segment
-  uint64_t p = d.start;
-  while (p > area && !is_term(rd.at(p - 1))) --p;
-  unsigned long long v = vstart[s];
-  T acc = kstart[s];
-  const uint64_t nvar = sd.rows ? 2 * (sd.rows - 1) : 0;
-  while (p < d.end) {
-    // decode one varint (delta up to 19 bytes for u128, 10 for u64)
+  const uint64_t area = sd.byte_off + sd.head, lim = sd.byte_off + sd.byte_len;
+  const unsigned long long nvar = sd.rows ? 2ull * (sd.rows - 1) : 0ull;
+  unsigned long long v0 = vstart[si];  // stream varint index of the segment's next owned varint
+  T key = kstart[si];                  // key before that varint
+  for (uint64_t base = d.start & ~15ull; base < d.end; base += kRound) {
+    load_round(bytes, base, lim_pad, win, lane);
+    uint64_t bound;
+    uint32_t own;
+    round_masks(win, lane, base, area, d.start, d.end, bound, own);
+    const uint32_t c = __popc(own);
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    const unsigned long long vl = v0 + incl - c;  // index of the lane's first owned varint
+    // the lane's key deltas, then the key before each lane's first (warp scan)
+    T dsum = 0;
+    {
+      unsigned long long v = vl;
+      for (uint32_t m = own; m; m &= m - 1, ++v)
+        if ((v & 1ull) == 0 && v < nvar) dsum += varint_at<T>(win, bound, 16 * lane, 32 + __ffs(m) - 1);
+    }
+    const T dincl = warp_incl_sum(dsum);
+    T k = key + (dincl - dsum);
+    {
+      unsigned long long v = vl;
+      for (uint32_t m = own; m; m &= m - 1, ++v) {
+        if (v >= nvar) break;  // bytes after the last row are ignored, as the reference decodes row_count rows
+        const T val = varint_at<T>(win, bound, 16 * lane, 32 + __ffs(m) - 1);
+        if ((v & 1ull) == 0) {
+          k += val;
+          keys[sd.row_off + v / 2 + 1] = k;
+        } else {
+          counts[sd.row_off + (v - 1) / 2 + 1] = (unsigned long long)(uint64_t)val;
+        }
+      }
+    }
+    key += warp_bcast_t(dincl, 31);
+    v0 += __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+  }
+  if (d.end == lim && lim > area && lane == 0 && !is_term(bytes[lim - 1]) && v0 < nvar) {
+    uint64_t p = lim;
+    while (p > area && !is_term(bytes[p - 1])) --p;
     T val = 0;
     unsigned sh = 0;
-    uint64_t q = p;
-    const uint64_t lim = sd.byte_off + sd.byte_len;
-    while (q < lim) {
-      const uint8_t b = rd.at(q++);
-      if (sh < (unsigned)KeyTraits<T>::kBits) val |= (T)(b & 0x7f) << sh;
+    for (uint64_t q = p; q < lim; ++q) {
+      if (sh < (unsigned)KeyTraits<T>::kBits) val |= (T)(bytes[q] & 0x7f) << sh;
       sh += 7;
-      if (is_term(b)) break;
     }
-    if (q > d.end) break;  // terminator in the next segment: that segment owns this varint
-    if (v >= nvar) break;  // bytes after the last row are ignored, as the reference decodes row_count rows
-    if ((v & 1ull) == 0) {
-      acc += val;  // wrapping add, as the reference's wrapping_add
-      keys[sd.row_off + v / 2 + 1] = acc;
-    } else {
-      counts[sd.row_off + (v - 1) / 2 + 1] = (unsigned long long)(uint64_t)val;
-    }
-    ++v;
-    p = q;
+    if ((v0 & 1ull) == 0) keys[sd.row_off + v0 / 2 + 1] = key + val;
+    else counts[sd.row_off + (v0 - 1) / 2 + 1] = (unsigned long long)(uint64_t)val;
   }
 }
 
@@ -381,7 +500,7 @@ struct MergeSmem {
   static constexpr size_t keys = (size_t)kMergeCap * sizeof(T);
   static constexpr size_t cnts = (size_t)kMergeCap * 8;
   static constexpr size_t tag = (size_t)kMergeCap * 2;
-  static constexpr size_t perm = (size_t)kMergeCap * 2;
+  static constexpr size_t perm = (size_t)kMergeCap * 2 * 2;  // two index arrays (merge rounds ping-pong)
   static constexpr size_t head = (size_t)(kMergeCap + 1) * 2;
   // every region starts 16-byte aligned (misc holds 8-byte scan values)
   static constexpr size_t seg = ((size_t)(kMaxTileStreams + 1) * 4 + kMaxTileStreams * 4 + 15) & ~(size_t)15;
@@ -411,7 +530,8 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
   T* sk = reinterpret_cast<T*>(sm);
   unsigned long long* sc = reinterpret_cast<unsigned long long*>(sm + L::keys);
   uint16_t* stag = reinterpret_cast<uint16_t*>(sm + L::keys + L::cnts);
-  uint16_t* perm = reinterpret_cast<uint16_t*>(sm + L::keys + L::cnts + L::tag);
+  uint16_t* perm_a = reinterpret_cast<uint16_t*>(sm + L::keys + L::cnts + L::tag);
+  uint16_t* perm_b = perm_a + kMergeCap;
   uint16_t* head = reinterpret_cast<uint16_t*>(sm + L::keys + L::cnts + L::tag + L::perm);
   uint32_t* sstart = reinterpret_cast<uint32_t*>(sm + L::keys + L::cnts + L::tag + L::perm +
                                                  ((L::head + 15) & ~(size_t)15));
@@ -455,28 +575,65 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
     }
   }
   __syncthreads();
-  // merged rank of every row: own index + rows of other streams before it
-  for (uint32_t r = threadIdx.x; r < n; r += NT) {
-    const uint32_t a = stag[r];
-    const T key = sk[r];
-    uint32_t rank = r - sstart[a];
-    for (uint32_t b = 0; b < nts; ++b) {
-      if (b == a) continue;
-      uint32_t lo = sstart[b], hi = sstart[b + 1];
-      // streams before a: count keys <= key; after a: keys < key
-      while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        const bool before = b < a ? sk[mid] <= key : sk[mid] < key;
-        if (before) lo = mid + 1;
-        else hi = mid;
+  // Merged order of the rows (ties in stream order): the sorted streams are
+  // merged pairwise in rounds, run 2p with run 2p + 1, each round a merge
+  // path (Green, McColl and Bader, 2012): thread t takes output positions
+  // [t * PER, t * PER + PER) of the tile, finds where that range starts in
+  // both runs of its pair by a diagonal binary search, then merges
+  // sequentially.  Stable (equal keys: the earlier run first), so a group of
+  // equal keys keeps stream order, i.e. input order, then chunk order.
+  constexpr uint32_t PER = kMergeCap / NT;
+  uint16_t* perm = perm_a;
+  {
+    uint16_t* src = perm_a;
+    uint16_t* dst = perm_b;
+    for (uint32_t r = threadIdx.x; r < n; r += NT) src[r] = (uint16_t)r;
+    __syncthreads();
+    for (uint32_t w = 1; w < nts; w <<= 1) {
+      const uint32_t q0 = threadIdx.x * PER;
+      if (q0 < n) {
+        // the pair holding output q0: pairs start at stream multiples of 2w;
+        // the last pair whose first row is <= q0 (empty pairs are passed over)
+        uint32_t p = 0;
+        {
+          uint32_t lo = 0, hi = (nts + 2 * w - 1) / (2 * w) - 1;
+          while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (sstart[min(mid * 2 * w, nts)] <= q0) lo = mid;
+            else hi = mid - 1;
+          }
+          p = lo;
+        }
+        uint32_t q = q0;
+        const uint32_t qend = min(q0 + PER, n);
+        while (q < qend) {
+          const uint32_t a0 = sstart[min(p * 2 * w, nts)], a1 = sstart[min(p * 2 * w + w, nts)],
+                         b1 = sstart[min(p * 2 * w + 2 * w, nts)];
+          const uint32_t la = a1 - a0, lb = b1 - a1, d = q - a0;
+          // i = rows of run A among the pair's first d outputs
+          uint32_t lo = d > lb ? d - lb : 0, hi = d < la ? d : la;
+          while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (sk[src[a0 + mid]] <= sk[src[a1 + d - 1 - mid]]) lo = mid + 1;
+            else hi = mid;
+          }
+          uint32_t i = lo, j = d - lo;
+          const uint32_t stop = min(qend, b1);
+          for (; q < stop; ++q) {
+            const bool take_a = i < la && (j >= lb || sk[src[a0 + i]] <= sk[src[a1 + j]]);
+            dst[q] = take_a ? src[a0 + i++] : src[a1 + j++];
+          }
+          ++p;  // the range continues in the next pair
+        }
       }
-      rank += lo - sstart[b];
+      __syncthreads();
+      uint16_t* t = src;
+      src = dst;
+      dst = t;
     }
-    perm[rank] = (uint16_t)r;
+    perm = src;
   }
-  __syncthreads();
   // key-group heads in merged order
-  constexpr int PER = kMergeCap / NT;
   const uint32_t q0 = threadIdx.x * PER;
   uint32_t nh = 0;
 #pragma unroll
@@ -846,17 +1003,19 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     if (!d_dsum2.ensure(nseg * sizeof(T) + 16) || !d_sfirst.ensure((nst + 1) * 4 + 8))
       return fail(KITE_ERR_OOM, "merge decode buffers");
     MCU(cudaMemcpyAsync(d_sfirst.p, seg_first.data(), (nst + 1) * 4, cudaMemcpyHostToDevice, s));
-    const unsigned gsegs = (nseg + 255) / 256;
-    k_seg_pass_a<T><<<gsegs, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_segs.as<SegDesc>(), nseg,
-                                          d_streams.as<StreamDesc>(), d_terms.as<uint32_t>(), d_dsum.as<T>(),
-                                          d_dsum2.as<T>());
+    const unsigned gsegs = (nseg + kDecWarps - 1) / kDecWarps;
+    const uint64_t lim_pad = total_bytes + 64;  // every aligned 16-byte block below this is readable
+    k_seg_pass_a<T><<<gsegs, 32 * kDecWarps, 0, s>>>(d_bytes.as<uint8_t>(), lim_pad, d_segs.as<SegDesc>(), nseg,
+                                                     d_streams.as<StreamDesc>(), d_terms.as<uint32_t>(),
+                                                     d_dsum.as<T>(), d_dsum2.as<T>());
     k_stream_seg_scan<T><<<(nst + 7) / 8, 256, 0, s>>>(d_terms.as<uint32_t>(), d_dsum.as<T>(), d_dsum2.as<T>(),
                                                        d_sfirst.as<uint32_t>(), d_streams.as<StreamDesc>(),
                                                        d_first.as<T>(), nst, d_vstart.as<unsigned long long>(),
                                                        d_kstart.as<T>(), dst);
-    k_seg_rows<T><<<gsegs, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_segs.as<SegDesc>(), nseg,
-                                        d_streams.as<StreamDesc>(), d_vstart.as<unsigned long long>(),
-                                        d_kstart.as<T>(), d_keys.as<T>(), d_counts.as<unsigned long long>());
+    k_seg_rows<T><<<gsegs, 32 * kDecWarps, 0, s>>>(d_bytes.as<uint8_t>(), lim_pad, d_segs.as<SegDesc>(), nseg,
+                                                   d_streams.as<StreamDesc>(), d_vstart.as<unsigned long long>(),
+                                                   d_kstart.as<T>(), d_keys.as<T>(),
+                                                   d_counts.as<unsigned long long>());
     launches += 3;
   }
   DevStatus hdec{};
@@ -886,6 +1045,29 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     // of the key multiset; key bits from the input k
     launches += 1 + compute_hist_splitters<T>(d_sample.as<T>(), ns, key_bits, S, d_spl.as<T>(),
                                               d_hist.as<unsigned>(), s);
+    stat->splitter_used = KITE_SPLIT_SAMPLED;
+    if (ex && ex->mlp && ex->splitter_mode != KITE_SPLIT_SAMPLED) {
+      // the learned CDF of the row sample cuts the merged key range; kept
+      // when its predicted max/mean tile load is the lower one (LEARNED: always)
+      double hist_imb = 0.0;
+      if (predict_imbalance<T>(ex->mlp, d_sample.as<T>(), ns, d_spl.as<T>(), S, s, timeout_ms, &hist_imb))
+        return fail(KITE_ERR_TIMEOUT, "merge splitter evaluation did not finish");
+      Dev d_spl2;
+      if (!d_spl2.ensure(S * sizeof(T))) return fail(KITE_ERR_OOM, "merge splitters");
+      MlpReport rep;
+      if (mlp_splitters<T>(ex->mlp, d_sample.as<T>(), ns, key_bits, S, d_spl2.as<T>(), s, timeout_ms, &rep))
+        return fail(KITE_ERR_CUDA, "learned splitter training failed");
+      launches += 1 + rep.launches;
+      stat->hist_pred_imbalance = hist_imb;
+      stat->mlp_pred_imbalance = rep.pred_imbalance;
+      stat->mlp_loss = rep.loss;
+      stat->mlp_reused = rep.reused ? 1u : 0u;
+      if (rep.pred_imbalance < 1e29 && (ex->splitter_mode == KITE_SPLIT_LEARNED || rep.pred_imbalance < hist_imb)) {
+        MCU(cudaMemcpyAsync(d_spl.p, d_spl2.p, (S - 1) * sizeof(T), cudaMemcpyDeviceToDevice, s));
+        stat->splitter_used = KITE_SPLIT_LEARNED;
+      }
+      if (sync()) return fail(KITE_ERR_TIMEOUT, "merge splitter wait");
+    }
     spl.resize(S - 1);
     MCU(cudaMemcpyAsync(spl.data(), d_spl.p, (S - 1) * sizeof(T), cudaMemcpyDeviceToHost, s));
   } else {

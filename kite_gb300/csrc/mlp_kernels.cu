@@ -761,3 +761,31 @@ extern "C" int kite_mlp_grad_check(const float* params, const uint64_t* views, u
 
 extern "C" int kite_mlp_param_count(void) { return kite::kParams; }
 extern "C" int kite_mlp_input_count(void) { return kite::kIn; }
+
+// Fits the learned CDF to n 48-bit key views (host array) for S tiles, as
+// the count path does (stage-1 counts, training, inversion), and returns the
+// trained parameters and the S - 1 splitter cells (48-bit views of the
+// splitters) so tests can check the inversion against a CPU evaluation of the
+// same network.  Returns 0, or -1 on failure.
+extern "C" int kite_mlp_fit(const uint64_t* views, uint32_t n, uint32_t S, float* params_out, uint64_t* cells_out,
+                            double* pred_imbalance) {
+  using namespace kite;
+  MlpModel* m = mlp_create();
+  uint64_t *dv = nullptr, *ds = nullptr;
+  int rc = -1;
+  if (cudaMalloc(&dv, (size_t)n * 8) == cudaSuccess && cudaMalloc(&ds, (size_t)S * 8) == cudaSuccess &&
+      cudaMemcpy(dv, views, (size_t)n * 8, cudaMemcpyHostToDevice) == cudaSuccess) {
+    MlpReport rep;
+    if (mlp_splitters<uint64_t>(m, dv, n, 48, S, ds, nullptr, 600000, &rep) == 0 &&
+        cudaDeviceSynchronize() == cudaSuccess &&
+        cudaMemcpy(params_out, m->params, kParams * 4, cudaMemcpyDeviceToHost) == cudaSuccess &&
+        cudaMemcpy(cells_out, ds, (size_t)(S - 1) * 8, cudaMemcpyDeviceToHost) == cudaSuccess) {
+      if (pred_imbalance) *pred_imbalance = rep.pred_imbalance;
+      rc = 0;
+    }
+  }
+  cudaFree(dv);
+  cudaFree(ds);
+  mlp_destroy(m);
+  return rc;
+}
