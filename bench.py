@@ -515,14 +515,35 @@ def run_merge_bench(args, world, rank, local):
         c.merge(kis, callback=cb, bases=bases)
     torch.cuda.synchronize()
     barrier(world)
+    stage = [0.0] * 5
     t0 = time.perf_counter()
     for _ in range(args.steps):
         out_stats["rows"] = out_stats["bytes"] = 0
         c.merge(kis, callback=cb, bases=bases)
+        stage = [x + y for x, y in zip(stage, c.stats()["stage_ms"][:5])]
     c.synchronize()
     barrier(world)
     dt = max_over_ranks(world, (time.perf_counter() - t0) / args.steps)
+    mst = c.stats()
     c.close()
+    stage = [x / args.steps for x in stage]
+    names = ["decode", "tile planning", "merge", "encode", "copy to host"]
+    # algorithmic bytes per device stage: decode reads the payloads and
+    # writes (key, u64 count) rows; the merge reads those and writes (key,
+    # u32 count) rows; the encode reads those and writes the output payloads
+    sbytes = {0: bytes_in + rows_in * 16, 2: rows_in * 16 + out_stats["rows"] * 12,
+              3: out_stats["rows"] * 12 + out_stats["bytes"]}
+    dom = max(sbytes, key=lambda i: stage[i])
+    dev_ms = sum(stage[:4])
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+        r = oracle.merge_images(images, os.cpu_count() or 1)
+        cpu = {"value": r["rows_in"] / r["seconds"], "unit": "rows/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": "the same 8 images in memory: per partition load_partition_counts, the input filters, "
+                         "merge_vectors_total and serialize_partition_chunk, partitions on all host threads",
+               "seconds": round(r["seconds"], 3)}
     value = sum_over_ranks(world, rows_in) / dt
     peak, peak_src = peaks()
     algo = rows_in * 12 + out_stats["rows"] * 12  # decoded rows in + merged rows out, (key, count) as 8+4 B
@@ -539,9 +560,17 @@ def run_merge_bench(args, world, rank, local):
                            "parallelism": f"replicas x{world}"},
                 "e2e": {"value": value, "unit": "rows/s", "h2d_bytes_per_step": bytes_in,
                         "d2h_bytes_per_step": out_stats["bytes"]},
-                "roofline": {"bound": "hbm", "kernel": "merge (whole call)", "achieved": algo / dt / 1e9,
-                             "peak": peak, "unit": "GB/s", "frac": algo / dt / 1e9 / peak, "traffic": None,
-                             "peak_source": peak_src, "algorithmic_bytes": algo}}
+                "device": {"value": rows_in / (dev_ms / 1e3), "unit": "rows/s", "ms_per_step": dev_ms,
+                           "note": "the device stages only (decode, tile planning, merge, encode); the whole "
+                                   "call adds the copies of the inputs in and the output out"},
+                "stage_ms": {names[i]: round(stage[i], 3) for i in range(5)},
+                "splitter_used": "learned" if mst["splitter_used"] == gpu.SPLIT_LEARNED else "sampled",
+                "roofline": {"bound": "hbm", "kernel": names[dom],
+                             "achieved": sbytes[dom] / (stage[dom] / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                             "frac": sbytes[dom] / (stage[dom] / 1e3) / 1e9 / peak, "traffic": None,
+                             "peak_source": peak_src, "algorithmic_bytes": sbytes[dom], "kernel_ms": stage[dom],
+                             "whole_call_gbs": algo / dt / 1e9},
+                "cpu_baseline": cpu}
         print(json.dumps(line))
     return 0
 

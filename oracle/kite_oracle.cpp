@@ -1908,6 +1908,68 @@ long long orc_dump_kite(const uint8_t* img, size_t n, char* out, size_t cap) {
 }
 
 // Merge of .kite files by path (kite merge); writes the output image.
+// The merge of n in-memory .kite images with `threads` threads working on
+// partitions in turn (run_merge's rayon loop over partition batches,
+// src/merge/mod.rs:117-151): per partition load_partition_counts of every
+// input, the input's header filter, merge_vectors_total and
+// serialize_partition_chunk, exactly as merge_files, without the writer.
+// stats4 = rows in, rows out, payload bytes out, nanoseconds (from the
+// images in memory to every payload made).  0 or -1.
+int orc_merge_images(const uint8_t** imgs, const size_t* lens, size_t n, size_t threads, uint64_t* stats4) {
+  try {
+    std::vector<Reader> rs(n);
+    for (size_t i = 0; i < n; ++i) rs[i].open(imgs[i], lens[i]);
+    auto t0 = std::chrono::steady_clock::now();
+    const size_t P = rs[0].h.partitions;
+    std::atomic<size_t> next(0);
+    std::atomic<uint64_t> rows_in(0), rows_out(0), bytes_out(0);
+    std::atomic<int> failed(0);
+    std::mutex emu;
+    std::string err;
+    auto work = [&]() {
+      std::vector<uint8_t> payload;
+      for (size_t p; (p = next.fetch_add(1)) < P;) {
+        try {
+          std::vector<std::vector<Row>> vecs;
+          for (auto& r : rs) {
+            auto rows = load_partition_counts(r, p);
+            rows_in += rows.size();
+            if (r.h.has_min || r.h.has_max) {
+              std::vector<Row> kept;
+              for (auto& x : rows)
+                if (passes(x.second, r.h)) kept.push_back(x);
+              rows.swap(kept);
+            }
+            vecs.push_back(std::move(rows));
+          }
+          auto merged = merge_vectors_total(vecs);
+          if (serialize_partition_chunk(merged, rs[0].h.key_width, payload)) {
+            rows_out += merged.size();
+            bytes_out += payload.size();
+          }
+        } catch (const std::exception& e) {
+          std::lock_guard<std::mutex> g(emu);
+          err = e.what();
+          failed = 1;
+        }
+      }
+    };
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < std::max<size_t>(threads, 1); ++t) th.emplace_back(work);
+    for (auto& t : th) t.join();
+    if (failed) throw Error(err);
+    stats4[0] = rows_in;
+    stats4[1] = rows_out;
+    stats4[2] = bytes_out;
+    stats4[3] = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0)
+                    .count();
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
 long long orc_merge_files(const char** paths, size_t n, size_t lanes, uint8_t* out, size_t cap) {
   try {
     std::vector<std::string> ps;

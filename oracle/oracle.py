@@ -193,3 +193,17 @@ def count_parts(fastq, k: int, canonical: bool, partitions: int, threads: int, c
     if total < 0:
         raise RuntimeError(err())
     return Parts(out, total, list(meta), partitions, list(st))
+
+
+def merge_images(images: list, threads: int) -> dict:
+    """Timed merge of in-memory .kite images with `threads` threads
+    (orc_merge_images): rows in / out, payload bytes out, seconds."""
+    L = lib()
+    L.orc_merge_images.argtypes = [C.POINTER(C.c_char_p), C.POINTER(C.c_size_t), C.c_size_t, C.c_size_t,
+                                   C.POINTER(C.c_uint64)]
+    arr = (C.c_char_p * len(images))(*images)
+    lens = (C.c_size_t * len(images))(*[len(x) for x in images])
+    st = (C.c_uint64 * 4)()
+    if L.orc_merge_images(arr, lens, len(images), threads, st) != 0:
+        raise RuntimeError(err())
+    return {"rows_in": st[0], "rows_out": st[1], "bytes_out": st[2], "seconds": st[3] / 1e9}
