@@ -151,8 +151,7 @@ struct BinSmem {
   static constexpr size_t fbit_bytes = kBins / 8;
   static constexpr unsigned MAXLARGE = CAP / (kSmallBin + 1) + 1;  // marked bins above kSmallBin keys
   static constexpr size_t misc_bytes = 64 * 8 + 16 + ((MAXLARGE * 2 + 15) & ~(size_t)15) + 16;  // + mbarrier
-  static constexpr size_t hbit_bytes = ((size_t)CAP / 8 + 15) & ~(size_t)15;  // run-head flag per key position
-  static constexpr size_t total = buf_bytes + bin_bytes + fbit_bytes + hbit_bytes + misc_bytes;
+  static constexpr size_t total = buf_bytes + bin_bytes + fbit_bytes + misc_bytes;
   static_assert((size_t)(CAP + 1) * 2 <= bin_bytes, "run heads must fit the bin area");
   static_assert((size_t)256 * NW * 4 <= bin_bytes, "LSD histograms must fit the bin area");
   static_assert(kBins / 2 % (4 * NT) == 0, "bin scan takes whole uint4 groups");
@@ -326,26 +325,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
   }
   return false;
 }
-// Run-head flags of positions a + 1 .. e - 1 after the keys of [a, e) were
-// reordered (a and e start bins, so their flags never change).  Other
-// threads update other bits of the same words at the same time: each word
-// is changed by two atomics that touch only this range's bits.
-template <class T>
-__device__ __forceinline__ void head_flags(unsigned* hbits, const T* buf, unsigned a, unsigned e) {
-  unsigned p = a + 1;
-  while (p < e) {
-    const unsigned w = p >> 5, wend = min(e, (w + 1) << 5);
-    unsigned clr = 0, set = 0;
-    for (; p < wend; ++p) {
-      const unsigned bit = 1u << (p & 31);
-      clr |= bit;
-      if (buf[p] != buf[p - 1]) set |= bit;
-    }
-    atomicAnd(&hbits[w], ~clr);
-    if (set) atomicOr(&hbits[w], set);
-  }
-}
-
 constexpr uint32_t kBulkWaitPolls = 1u << 18;                // a bulk copy from device memory ends long before
 constexpr uint32_t kBulkDrainPolls = 1u << 26;               // after a timeout: the copy must leave shared memory
 constexpr unsigned long long kBulkTimeoutFlag = 1ull << 40;  // added to the sort statistics on a timeout
@@ -360,9 +339,7 @@ __device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, ui
   T* buf = reinterpret_cast<T*>(sm);
   unsigned* bins = reinterpret_cast<unsigned*>(sm + L::buf_bytes);
   unsigned* fbits = reinterpret_cast<unsigned*>(sm + L::buf_bytes + L::bin_bytes);
-  unsigned* hbits = reinterpret_cast<unsigned*>(sm + L::buf_bytes + L::bin_bytes + L::fbit_bytes);
-  unsigned long long* scan64 =
-      reinterpret_cast<unsigned long long*>(sm + L::buf_bytes + L::bin_bytes + L::fbit_bytes + L::hbit_bytes);
+  unsigned long long* scan64 = reinterpret_cast<unsigned long long*>(sm + L::buf_bytes + L::bin_bytes + L::fbit_bytes);
   unsigned* scan_sm = reinterpret_cast<unsigned*>(scan64);
   unsigned* misc = reinterpret_cast<unsigned*>(scan64 + 64);  // [0] LSD fallback, [1] large bins
   unsigned short* large = reinterpret_cast<unsigned short*>(misc + 4);
@@ -479,36 +456,19 @@ __device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, ui
   __syncthreads();
   // bin_get(b) is now the end of bin b; its start is the end of bin b - 1 (0 for b = 0)
 
-  // ---- 3. run-head flags (a key differing from its predecessor), and the
-  // bins holding more than one distinct key marked.  Warp w takes positions
-  // w0 + 32 r + lane, so each round's flags are one ballot word.  The flags
-  // stay right wherever a bin holds a single key; inside a marked bin they
-  // are redone once the bin is ordered. ----
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const unsigned rounds = (n + NT - 1) / NT;
-  const unsigned w0 = (unsigned)wid * 32u * rounds;
-  for (unsigned r = 0; r < rounds; ++r) {
-    const unsigned p = w0 + r * 32u + lane;
-    bool h = false;
-    if (p < n) {
-      h = true;
-      if (p > 0) {
-        const T a = buf[p], b = buf[p - 1];
-        h = a != b;
-        if (h) {
-          const unsigned ba = bin_at(a);
-          if (bin_at(b) == ba) {
-            const unsigned bit = 1u << (ba & 31);
-            if (!(atomicOr(&fbits[ba >> 5], bit) & bit)) {
-              const unsigned m = bin_get(bins, ba) - (ba ? bin_get(bins, ba - 1) : 0u);
-              if (m > kSmallBin) large[atomicAdd(&misc[1], 1u)] = (unsigned short)ba;
-            }
-          }
+  // ---- 3. mark the bins holding more than one distinct key ----
+  for (unsigned p = threadIdx.x + 1; p < n; p += NT) {
+    const T a = buf[p], b = buf[p - 1];
+    if (a != b) {
+      const unsigned ba = bin_at(a);
+      if (bin_at(b) == ba) {
+        const unsigned bit = 1u << (ba & 31);
+        if (!(atomicOr(&fbits[ba >> 5], bit) & bit)) {
+          const unsigned m = bin_get(bins, ba) - (ba ? bin_get(bins, ba - 1) : 0u);
+          if (m > kSmallBin) large[atomicAdd(&misc[1], 1u)] = (unsigned short)ba;
         }
       }
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, h);
-    if (lane == 0 && w0 + r * 32u < n) hbits[(w0 + r * 32u) >> 5] = bal;
   }
   __syncthreads();
 
@@ -516,6 +476,7 @@ __device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, ui
   // bits, the listed larger ones by the warps in turn ----
   {
     constexpr int BPT = kBins / NT;
+    const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const unsigned b0 = threadIdx.x * BPT;
     for (unsigned bits = (fbits[b0 >> 5] >> (b0 & 31)) & (BPT == 32 ? 0xffffffffu : ((1u << BPT) - 1u)); bits;
          bits &= bits - 1) {
@@ -533,52 +494,46 @@ __device__ __forceinline__ void sort_tile(uint32_t tid, T* __restrict__ keys, ui
         }
         buf[q] = v;
       }
-      head_flags(hbits, buf, a, e);
     }
     const unsigned nlarge = misc[1];
     for (unsigned li = wid; li < nlarge; li += NW) {
       const unsigned bb = large[li];
       const unsigned a = bb ? bin_get(bins, bb - 1) : 0u, m = bin_get(bins, bb) - a;
-      bool sorted = true;
       if (m <= 32) warp_match_sort(buf, a, m, lane);
       else if (!warp_distinct_sort(buf, a, m, lane)) {
         if (m <= kMaxMixed) warp_count_sort(buf, a, m, lane);
-        else sorted = false;
+        else if (lane == 0) misc[0] = 1;
       }
-      if (!sorted) {
-        if (lane == 0) misc[0] = 1;
-      } else if (lane == 0) {
-        head_flags(hbits, buf, a, a + m);
-      }
-      __syncwarp();
     }
   }
   __syncthreads();
   if (misc[0]) {
-    // a large bin of many distinct keys: full LSD over the varying bits, in
-    // place, then every run-head flag again
+    // a large bin of many distinct keys: full LSD over the varying bits, in place
     if (threadIdx.x == 0 && fallbacks) atomicAdd(fallbacks, 1ull);
     smem_radix_sort<T, NT, ITEMS>(buf, n, varying_bits(mn, mx), bins, scan_sm, 0);
-    for (unsigned r = 0; r < rounds; ++r) {
-      const unsigned p = w0 + r * 32u + lane;
-      const bool h = p < n && (p == 0 || buf[p] != buf[p - 1]);
-      const unsigned bal = __ballot_sync(0xffffffffu, h);
-      if (lane == 0 && w0 + r * 32u < n) hbits[(w0 + r * 32u) >> 5] = bal;
-    }
-    __syncthreads();
   }
 
   // ---- 5. run-length reduction over the sorted keys ----
-  unsigned cnt = 0;
-  for (unsigned r = 0; r < rounds && w0 + r * 32u < n; ++r) cnt += __popc(hbits[(w0 + r * 32u) >> 5]);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned rounds = (n + NT - 1) / NT;
+  const unsigned w0 = (unsigned)wid * 32u * rounds;
+  unsigned hmask = 0, cnt = 0;
+  for (unsigned r = 0; r < rounds; ++r) {
+    const unsigned p = w0 + r * 32u + lane;
+    bool h = false;
+    if (p < n) h = p == 0 || buf[p] != buf[p - 1];
+    hmask |= (unsigned)h << r;
+    cnt += __popc(__ballot_sync(0xffffffffu, h));
+  }
   unsigned U;
   unsigned u = block_exclusive_scan<NT, unsigned>(lane == 0 ? cnt : 0u, scan_sm, &U);
   u = __shfl_sync(0xffffffffu, u, 0);
   unsigned short* head = reinterpret_cast<unsigned short*>(bins);
   const unsigned lt = (1u << lane) - 1u;
-  for (unsigned r = 0; r < rounds && w0 + r * 32u < n; ++r) {
-    const unsigned bal = hbits[(w0 + r * 32u) >> 5];
-    if ((bal >> lane) & 1u) head[u + __popc(bal & lt)] = (unsigned short)(w0 + r * 32u + lane);
+  for (unsigned r = 0; r < rounds; ++r) {
+    const bool h = (hmask >> r) & 1u;
+    const unsigned bal = __ballot_sync(0xffffffffu, h);
+    if (h) head[u + __popc(bal & lt)] = (unsigned short)(w0 + r * 32u + lane);
     u += __popc(bal);
   }
   if (threadIdx.x == 0) head[U] = (unsigned short)n;
