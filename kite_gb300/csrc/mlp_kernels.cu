@@ -10,8 +10,9 @@
 // Model: a two-stage learned index over V.
 //  Stage 1 (counts of the counter's key sample, up to 2^22 keys of the
 //   segment's first chunk): C(b), m(b) = sample keys below / inside bin b;
-//   every heavy bin (more than a quarter of a tile's share of the sample)
-//   also gets counts of its 256 sub-cells (the next 8 bits).
+//   every heavy bin (more than an eighth of a tile's share of the sample)
+//   also gets counts of its 256 sub-cells (the next 8 bits), and every heavy
+//   sub-cell counts of its own next 8 bits.
 //  Stage 2 (the network): an autoregressive density over the bits below the
 //   bin: for each bit i >= 16 it predicts P(x_i = 1 | x_0 .. x_{i-1}).  The
 //   network is a masked MLP (48 inputs -> 64 ReLU -> 64 ReLU -> 32 logits):
@@ -27,8 +28,8 @@
 //   arithmetic decoding, bit by bit.
 //  F(key) = (C(b) [+ the sub-cell counts below, heavy bins] + m * g(V)) / n.
 // Training: maximum likelihood (binary cross-entropy of every bit i >= 16
-// given the bits above it) over the whole sample, minibatches of 8192 keys,
-// Adam.  The training steps are captured once as a CUDA graph (the step
+// given the bits above it) over the whole sample, minibatches of 8192 keys
+// drawn by a hash of (step, index), Adam.  The training steps are captured once as a CUDA graph (the step
 // counter lives on the device) and replayed.
 //
 // Splitter j: the bin (and heavy bins' sub-cell) holding quantile j/S of the
@@ -92,8 +93,10 @@ struct MlpModel {
   unsigned* hist = nullptr;      // [65536] sample counts per bin, then inclusive cumulative
   int* heavy_idx = nullptr;      // [65536] heavy-bin slot or -1
   unsigned* sub = nullptr;       // [heavy slots][256] sub-cell counts, then inclusive cumulative
-  unsigned* nheavy = nullptr;    // [1]
+  unsigned* nheavy = nullptr;    // [2] heavy bins, heavy sub-cells
   uint32_t sub_cap = 0;          // heavy slots allocated
+  int* heavy2_idx = nullptr;     // [heavy slots][256] second-level slot of a heavy sub-cell, or -1
+  unsigned* sub2 = nullptr;      // [second-level slots][256] counts of a heavy sub-cell's next 8 bits
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   uint32_t graph_n = 0;          // the sample size the graph was captured for
@@ -121,6 +124,8 @@ void mlp_destroy(MlpModel* m) {
   cudaFree(m->heavy_idx);
   cudaFree(m->sub);
   cudaFree(m->nheavy);
+  cudaFree(m->heavy2_idx);
+  cudaFree(m->sub2);
   delete m;
 }
 
@@ -130,6 +135,13 @@ __device__ __forceinline__ uint64_t view48(T key, uint32_t key_bits) {
   return key_bits >= 48 ? (uint64_t)(key >> (key_bits - 48)) : ((uint64_t)key << (48 - key_bits));
 }
 __device__ __forceinline__ float bit_of(uint64_t v, int i) { return (float)((v >> (kIn - 1 - i)) & 1ull); }
+// splitmix64 finalizer: the minibatch of step t draws sample mix64(t, b) mod n
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
 
 // ---- stage 1 ----------------------------------------------------------------
 template <class T>
@@ -162,6 +174,34 @@ __global__ void k_sub_hist(const uint64_t* __restrict__ views, uint32_t n, const
     const uint64_t v = views[i];
     const int h = heavy_idx[(uint32_t)(v >> (kIn - kBinBits))];
     if (h >= 0) atomicAdd(&sub[(size_t)h * kSubCells + (uint32_t)((v >> (kIn - kBinBits - kSubBits)) & (kSubCells - 1))], 1u);
+  }
+}
+
+// Heavy sub-cells (count > thr) of the heavy bins get a second-level slot:
+// one thread per (slot, sub-cell), on the raw counts.
+__global__ void k_heavy2(const unsigned* __restrict__ sub, const unsigned* __restrict__ nheavy, uint32_t cap,
+                         unsigned thr, int* __restrict__ heavy2_idx, unsigned* __restrict__ nheavy2) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nh = min(*nheavy, cap);
+  if (i >= cap * kSubCells) return;
+  int slot = -1;
+  if (i / kSubCells < nh && sub[i] > thr) {
+    const unsigned s2 = atomicAdd(nheavy2, 1u);
+    if (s2 < cap) slot = (int)s2;
+  }
+  heavy2_idx[i] = slot;
+}
+
+__global__ void k_sub2_hist(const uint64_t* __restrict__ views, uint32_t n, const int* __restrict__ heavy_idx,
+                            const int* __restrict__ heavy2_idx, unsigned* __restrict__ sub2) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint64_t v = views[i];
+    const int h = heavy_idx[(uint32_t)(v >> (kIn - kBinBits))];
+    if (h < 0) continue;
+    const int h2 = heavy2_idx[(size_t)h * kSubCells + (uint32_t)((v >> (kIn - kBinBits - kSubBits)) & (kSubCells - 1))];
+    if (h2 >= 0)
+      atomicAdd(&sub2[(size_t)h2 * kSubCells + (uint32_t)((v >> (kIn - kBinBits - 2 * kSubBits)) & (kSubCells - 1))],
+                1u);
   }
 }
 
@@ -204,14 +244,14 @@ __global__ void __launch_bounds__(1024) k_cum(unsigned* __restrict__ h) {
 // masked ones stay zero), one global atomicAdd per weight per CTA.
 // Loss = mean over the batch and the 32 predicted bits of the binary
 // cross-entropy.  Sample s of the batch is views[idx(s)], idx either given
-// (idx != null) or the strided walk of training step *step.
+// (idx != null) or drawn by a hash of (training step *step, b, seed).
 static constexpr int kB = 128;        // samples per CTA (== threads)
 static constexpr int kLd = kB + 1;    // padded row stride
 static constexpr size_t kFbSmem = (size_t)(kParams + kIn * kLd + 3 * kH * kLd + kOut * kLd) * sizeof(float);
 
 __global__ void __launch_bounds__(kB) k_fwd_bwd(const float* __restrict__ params, const uint64_t* __restrict__ views,
                                                 const uint32_t* __restrict__ idx, const unsigned* __restrict__ step,
-                                                uint32_t n, uint32_t stride, uint32_t batch,
+                                                uint32_t n, uint32_t seed, uint32_t batch,
                                                 float* __restrict__ grads, float* __restrict__ loss) {
   extern __shared__ float sm[];
   float* P = sm;                      // parameters
@@ -227,7 +267,7 @@ __global__ void __launch_bounds__(kB) k_fwd_bwd(const float* __restrict__ params
   uint32_t s = 0;
   if (live) {
     if (idx) s = idx[b];
-    else s = (uint32_t)((((uint64_t)(*step) * batch + b) % n) * (uint64_t)stride % n);
+    else s = (uint32_t)(mix64(((uint64_t)(*step) << 32) + b + ((uint64_t)seed << 20)) % n);
   }
   const uint64_t v = live ? views[s] : 0ull;
   for (int i = 0; i < kIn; ++i) X[i * kLd + t] = bit_of(v, i);
@@ -356,6 +396,7 @@ __global__ void __launch_bounds__(1024) k_adam(float* __restrict__ p, float* __r
 template <class T>
 __global__ void __launch_bounds__(256) k_invert(const float* __restrict__ params, const unsigned* __restrict__ cum,
                                                 const int* __restrict__ heavy_idx, const unsigned* __restrict__ sub,
+                                                const int* __restrict__ heavy2_idx, const unsigned* __restrict__ sub2,
                                                 uint32_t n, uint32_t S, uint32_t key_bits, T* __restrict__ spl) {
   extern __shared__ float P[];  // W1 as [input][hidden], W2 as [input][output]; the rest as given
   for (int i = threadIdx.x; i < kParams; i += blockDim.x) {
@@ -394,6 +435,22 @@ __global__ void __launch_bounds__(256) k_invert(const float* __restrict__ params
     mass = (double)c[a] - sb;
     v |= (uint64_t)a << (kIn - kBinBits - kSubBits);
     first = kB0 + kSubBits;
+    const int h2 = heavy2_idx[(size_t)h * kSubCells + a];
+    if (h2 >= 0 && mass > 0) {  // a heavy sub-cell: its next 8 bits from counts too
+      const unsigned* c2 = sub2 + (size_t)h2 * kSubCells;
+      const double r2 = q - below;
+      uint32_t a2 = 0, e2 = kSubCells - 1;
+      while (a2 < e2) {
+        const uint32_t mid = (a2 + e2) >> 1;
+        if ((double)c2[mid] > r2) e2 = mid;
+        else a2 = mid + 1;
+      }
+      const double sb2 = a2 ? c2[a2 - 1] : 0.0;
+      below += sb2;
+      mass = (double)c2[a2] - sb2;
+      v |= (uint64_t)a2 << (kIn - kBinBits - 2 * kSubBits);
+      first = kB0 + 2 * kSubBits;
+    }
   }
   const double u = mass > 0 ? (q - below) / mass : 1.0;
   double lo = 0.0, width = 1.0;
@@ -647,15 +704,21 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
   rep->pred_imbalance = 1e30;
   if (!m || n < 4 * S || n < 1024) return 0;  // too few samples to learn from
   // ---- stage 1: bin counts and heavy bins' sub-cell counts of the sample
-  const uint32_t heavy_cap = 4 * S + 4;  // bins above a quarter tile: at most 4 S of them
+  const uint32_t heavy_cap = 8 * S + 8;  // cells above an eighth of a tile: at most 8 S of them per level
   if (!m->hist && cudaMalloc(&m->hist, sizeof(unsigned) << kBinBits) != cudaSuccess) return 1;
   if (!m->heavy_idx && cudaMalloc(&m->heavy_idx, sizeof(int) << kBinBits) != cudaSuccess) return 1;
-  if (!m->nheavy && cudaMalloc(&m->nheavy, sizeof(unsigned)) != cudaSuccess) return 1;
+  if (!m->nheavy && cudaMalloc(&m->nheavy, 2 * sizeof(unsigned)) != cudaSuccess) return 1;
   if (m->sub_cap < heavy_cap) {
     cudaFree(m->sub);
-    m->sub = nullptr;
+    cudaFree(m->sub2);
+    cudaFree(m->heavy2_idx);
+    m->sub = m->sub2 = nullptr;
+    m->heavy2_idx = nullptr;
     m->sub_cap = 0;
-    if (cudaMalloc(&m->sub, (size_t)heavy_cap * kSubCells * sizeof(unsigned)) != cudaSuccess) return 1;
+    if (cudaMalloc(&m->sub, (size_t)heavy_cap * kSubCells * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&m->sub2, (size_t)heavy_cap * kSubCells * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&m->heavy2_idx, (size_t)heavy_cap * kSubCells * sizeof(int)) != cudaSuccess)
+      return 1;
     m->sub_cap = heavy_cap;
   }
   if (m->views_cap < n) {
@@ -673,21 +736,29 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const uint32_t grid = std::min<uint32_t>((n + 255) / 256, 8 * (uint32_t)std::max(sms, 1));
   cudaMemsetAsync(m->hist, 0, sizeof(unsigned) << kBinBits, s);
-  cudaMemsetAsync(m->nheavy, 0, sizeof(unsigned), s);
+  cudaMemsetAsync(m->nheavy, 0, 2 * sizeof(unsigned), s);
   cudaMemsetAsync(m->sub, 0, (size_t)heavy_cap * kSubCells * sizeof(unsigned), s);
+  cudaMemsetAsync(m->sub2, 0, (size_t)heavy_cap * kSubCells * sizeof(unsigned), s);
   k_views<T><<<grid, 256, 0, s>>>(d_sample, n, key_bits, m->views, m->hist);
-  const unsigned thr = (unsigned)((double)n / (4.0 * S));
+  // cells holding more than an eighth of a tile's share of the sample are
+  // counted one level (8 bits) deeper, twice at most
+  const unsigned thr = (unsigned)((double)n / (8.0 * S));
   k_heavy<<<(1u << kBinBits) / 256, 256, 0, s>>>(m->hist, thr, heavy_cap, m->heavy_idx, m->nheavy);
   k_sub_hist<<<grid, 256, 0, s>>>(m->views, n, m->heavy_idx, m->sub);
+  k_heavy2<<<(uint32_t)(((size_t)heavy_cap * kSubCells + 255) / 256), 256, 0, s>>>(
+      m->sub, m->nheavy, heavy_cap, thr, m->heavy2_idx, m->nheavy + 1);
+  k_sub2_hist<<<grid, 256, 0, s>>>(m->views, n, m->heavy_idx, m->heavy2_idx, m->sub2);
   k_sub_cum<<<(heavy_cap * 32 + 255) / 256, 256, 0, s>>>(m->sub, m->nheavy, heavy_cap);
+  k_sub_cum<<<(heavy_cap * 32 + 255) / 256, 256, 0, s>>>(m->sub2, m->nheavy + 1, heavy_cap);
   k_cum<<<1, 1024, 0, s>>>(m->hist);
-  rep->launches += 5;
+  rep->launches += 8;
   const size_t smem = kParams * sizeof(float);
   cudaFuncSetAttribute(k_invert<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const uint32_t inv_grid = (uint32_t)(((size_t)(S - 1) * 32 + 255) / 256);
   if (m->trained && m->trained_key_bits == key_bits) {
     // the bit conditionals learned on an earlier segment, over this sample's counts
-    k_invert<T><<<inv_grid, 256, smem, s>>>(m->params, m->hist, m->heavy_idx, m->sub, n, S, key_bits, d_spl);
+    k_invert<T><<<inv_grid, 256, smem, s>>>(m->params, m->hist, m->heavy_idx, m->sub, m->heavy2_idx, m->sub2, n, S,
+                                            key_bits, d_spl);
     k_sort_splitters<T><<<1, 1024, splitter_sort_smem<T>(S - 1), s>>>(d_spl, S - 1);
     rep->launches += 3;
     double pred = 0;
@@ -703,7 +774,8 @@ int mlp_splitters(MlpModel* m, const T* d_sample, uint32_t n, uint32_t key_bits,
   const int tl = train(m, n, s, timeout_ms, &rep->loss);
   if (tl < 0) return 1;
   rep->launches += tl;
-  k_invert<T><<<inv_grid, 256, smem, s>>>(m->params, m->hist, m->heavy_idx, m->sub, n, S, key_bits, d_spl);
+  k_invert<T><<<inv_grid, 256, smem, s>>>(m->params, m->hist, m->heavy_idx, m->sub, m->heavy2_idx, m->sub2, n, S,
+                                            key_bits, d_spl);
   k_sort_splitters<T><<<1, 1024, splitter_sort_smem<T>(S - 1), s>>>(d_spl, S - 1);
   rep->launches += 2;
   if (predict_imbalance<T>(m, d_sample, n, d_spl, S, s, timeout_ms, &rep->pred_imbalance)) return 1;
