@@ -552,27 +552,45 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
     dev_fail(st, KITE_DEV_TILE_OVERFLOW, blockIdx.x, n, nts);
     return;
   }
-  if (threadIdx.x == 0) {
-    uint32_t a = 0;
-    for (uint32_t i = 0; i < nts; ++i) {
-      sstart[i] = a;
-      sinput[i] = ts[mt.first_ts + i].input;
-      a += (uint32_t)(ts[mt.first_ts + i].hi - ts[mt.first_ts + i].lo);
+  if (threadIdx.x < 32) {
+    // stream starts inside the tile: warp 0 scans the stream lengths
+    uint32_t carry = 0;
+    const uint32_t lane = threadIdx.x;
+    for (uint32_t i0 = 0; i0 < nts; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      uint32_t len = 0;
+      if (i < nts) {
+        const TileStream t = ts[mt.first_ts + i];
+        len = (uint32_t)(t.hi - t.lo);
+        sinput[i] = t.input;
+      }
+      uint32_t incl = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+      }
+      if (i < nts) sstart[i] = carry + incl - len;
+      carry += __shfl_sync(0xffffffffu, incl, 31);
     }
-    sstart[nts] = a;
+    if (lane == 0) sstart[nts] = carry;
   }
   if (MODE == kModeHisto)
     for (uint32_t b = threadIdx.x; b < kHistBins; b += NT) hbin[b] = 0;
   __syncthreads();
-  // load rows of every stream
-  for (uint32_t i = 0; i < nts; ++i) {
-    const TileStream t = ts[mt.first_ts + i];
-    const uint32_t b0 = sstart[i], len = (uint32_t)(t.hi - t.lo);
-    for (uint32_t r = threadIdx.x; r < len; r += NT) {
-      sk[b0 + r] = keys[t.lo + r];
-      sc[b0 + r] = counts[t.lo + r];
-      stag[b0 + r] = (uint16_t)i;
+  // load the rows of every stream: row r of the tile belongs to the last
+  // stream starting at or before it
+  for (uint32_t r = threadIdx.x; r < n; r += NT) {
+    uint32_t lo = 0, hi = nts - 1;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (sstart[mid] <= r) lo = mid;
+      else hi = mid - 1;
     }
+    const uint64_t src = ts[mt.first_ts + lo].lo + (r - sstart[lo]);
+    sk[r] = keys[src];
+    sc[r] = counts[src];
+    stag[r] = (uint16_t)lo;
   }
   __syncthreads();
   // Merged order of the rows (ties in stream order): the sorted streams are
@@ -1032,7 +1050,9 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     part_first_stream[P] = nst;
   }
   uint32_t S = 1;
-  while ((double)total_rows / ((double)P * S) > 0.25 * kMergeCap && S < 4096) S <<= 1;
+  // tiles of about half the on-chip capacity (the refinement below splits the
+  // few that the cut leaves above it)
+  while ((double)total_rows / ((double)P * S) > 0.5 * kMergeCap && S < 4096) S <<= 1;
   std::vector<T> spl;
   Dev d_spl;
   if (S > 1 && total_rows) {
