@@ -1152,8 +1152,11 @@ int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n,
   MergeExtra ex;
   ex.mlp = ctx->mlp;
   ex.splitter_mode = ctx->cfg.splitter_mode;
+  auto staging = [ctx](size_t bytes) -> uint8_t* {
+    return ctx->h_dump.ensure(bytes) == cudaSuccess ? ctx->h_dump.as<uint8_t>() : nullptr;
+  };
   int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, inputs, n, ctx->stream, ctx->cfg.timeout_ms,
-                     kMergeModeMerge, emit, user, &msg, &ctx->stats, nullptr, &ex);
+                     kMergeModeMerge, emit, user, &msg, &ctx->stats, staging, &ex);
   if (rc) ctx->err = msg;
   return rc;
 }

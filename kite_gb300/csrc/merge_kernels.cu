@@ -38,6 +38,7 @@
 #include <memory>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "merge.h"
@@ -1126,12 +1127,28 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     T lo, hi;
     bool open_hi;
   };
-  std::vector<Done> done;
-  std::vector<uint64_t> dlo, dhi;
-  std::vector<Range> work;
-  for (uint32_t p = 0; p < P; ++p) {
+  // First cut, partitions in parallel on the host threads: each range that
+  // fits on chip becomes a finished range of its partition, the rest go to
+  // the bisection below.
+  const unsigned hthreads = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  auto parallel_parts = [&](auto&& fn) {
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < hthreads; ++t)
+      th.emplace_back([&, t]() {
+        for (uint32_t p = t; p < P; p += hthreads) fn(p);
+      });
+    for (auto& x : th) x.join();
+  };
+  struct PartCut {
+    std::vector<Done> done;
+    std::vector<uint64_t> dlo, dhi;
+    std::vector<Range> work;
+  };
+  std::vector<PartCut> cut(P);
+  parallel_parts([&](uint32_t p) {
+    PartCut& c = cut[p];
     const uint32_t f = part_first_stream[p], nstr = part_first_stream[p + 1] - f;
-    if (!nstr) continue;
+    if (!nstr) return;
     for (uint32_t j = 0; j < S; ++j) {
       const T lo = j ? spl[j - 1] : T(0);
       const bool open_hi = j + 1 == S;
@@ -1141,21 +1158,24 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
       for (uint32_t k2 = 0; k2 < nstr; ++k2) rows += pos[(f + k2) * SP + j + 1] - pos[(f + k2) * SP + j];
       if (rows == 0) continue;
       if (rows <= kMergeCap && nstr <= kMaxTileStreams) {
-        done.push_back(Done{p, lo, (uint64_t)dlo.size()});
+        c.done.push_back(Done{p, lo, (uint64_t)c.dlo.size()});
         for (uint32_t k2 = 0; k2 < nstr; ++k2) {
-          dlo.push_back(pos[(f + k2) * SP + j]);
-          dhi.push_back(pos[(f + k2) * SP + j + 1]);
+          c.dlo.push_back(pos[(f + k2) * SP + j]);
+          c.dhi.push_back(pos[(f + k2) * SP + j + 1]);
         }
       } else {
-        work.push_back(Range{p, lo, hi, open_hi});
+        c.work.push_back(Range{p, lo, hi, open_hi});
       }
     }
-  }
+  });
+  std::vector<Done> done;  // ranges finished by the bisection (offsets into dlo / dhi)
+  std::vector<uint64_t> dlo, dhi;
+  std::vector<Range> work;
+  for (uint32_t p = 0; p < P; ++p) work.insert(work.end(), cut[p].work.begin(), cut[p].work.end());
   std::vector<uint64_t>().swap(pos);
   // the decode's status arrived with the sync above
   if (hdec.code == KITE_DEV_SHORT_VARINTS)
     return fail(KITE_ERR_BAD_INPUT, sizeof(T) == 8 ? "invalid u64 DVLE delta" : "invalid u128 DVLE delta");
-  const size_t first_cut = done.size();  // in (partition, key) order
   Dev d_qlo, d_qhi, d_qkey, d_qout;
   std::vector<uint64_t> lp, hp;
   for (int round = 0; !work.empty() && round < 200; ++round) {
@@ -1220,43 +1240,74 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     work.swap(next);
   }
   if (!work.empty()) return fail(KITE_ERR_UNSUPPORTED, "merge tile refinement did not converge");
-  {
-    auto by_key = [](const Done& a, const Done& b) { return a.p != b.p ? a.p < b.p : a.lo < b.lo; };
-    std::sort(done.begin() + first_cut, done.end(), by_key);
-    std::inplace_merge(done.begin(), done.begin() + first_cut, done.end(), by_key);
-  }
-  // ---- tile lists ----
+  // ---- tile lists: per partition (in parallel) its finished ranges in key
+  // order, then the partitions concatenated with their offsets ----
+  std::vector<std::vector<Done>> refined(P);
+  for (const Done& d : done) refined[d.p].push_back(d);
+  struct PartTiles {
+    std::vector<MergeTile> mts;
+    std::vector<TileStream> tss;
+    uint64_t rows = 0;
+  };
+  std::vector<PartTiles> pt(P);
+  parallel_parts([&](uint32_t p) {
+    PartTiles& o = pt[p];
+    PartCut& c = cut[p];
+    std::vector<Done>& rf = refined[p];
+    std::sort(rf.begin(), rf.end(), [](const Done& a, const Done& b) { return a.lo < b.lo; });
+    const uint32_t f = part_first_stream[p], nstr = part_first_stream[p + 1] - f;
+    size_t i = 0, r = 0;
+    while (i < c.done.size() || r < rf.size()) {
+      const bool from_cut = r >= rf.size() || (i < c.done.size() && c.done[i].lo < rf[r].lo);
+      const Done& d = from_cut ? c.done[i++] : rf[r++];
+      const uint64_t* lo_v = from_cut ? c.dlo.data() : dlo.data();
+      const uint64_t* hi_v = from_cut ? c.dhi.data() : dhi.data();
+      MergeTile mt{};
+      mt.out_off = o.rows;  // relative to the partition until concatenated
+      mt.first_ts = (uint32_t)o.tss.size();
+      mt.partition = p;
+      uint64_t rows = 0;
+      for (uint32_t k2 = 0; k2 < nstr; ++k2) {
+        const uint64_t lo = lo_v[d.off + k2], hi = hi_v[d.off + k2];
+        if (hi == lo) continue;
+        o.tss.push_back(TileStream{lo, hi, streams[f + k2].input, 0});
+        rows += hi - lo;
+      }
+      mt.nts = (uint32_t)(o.tss.size() - mt.first_ts);
+      mt.rows_in = (uint32_t)rows;
+      o.rows += rows;
+      o.mts.push_back(mt);
+    }
+    std::vector<Done>().swap(c.done);
+    std::vector<uint64_t>().swap(c.dlo);
+    std::vector<uint64_t>().swap(c.dhi);
+  });
   std::vector<MergeTile> mts;
   std::vector<TileStream> tss;
   std::vector<TileDesc> tds;
   std::vector<uint32_t> tile_first(P + 1, 0);
-  mts.reserve(done.size());
-  tds.reserve(done.size());
   uint64_t out_off = 0;
   {
-    size_t di = 0;
+    size_t nt_all = 0, nts_all = 0;
+    for (uint32_t p = 0; p < P; ++p) {
+      nt_all += pt[p].mts.size();
+      nts_all += pt[p].tss.size();
+    }
+    mts.reserve(nt_all);
+    tds.reserve(nt_all);
+    tss.reserve(nts_all);
     for (uint32_t p = 0; p < P; ++p) {
       tile_first[p] = (uint32_t)mts.size();
-      const uint32_t f = part_first_stream[p], nstr = part_first_stream[p + 1] - f;
-      while (di < done.size() && done[di].p == p) {
-        const Done& r = done[di++];
-        MergeTile mt{};
-        mt.out_off = out_off;
-        mt.first_ts = (uint32_t)tss.size();
-        mt.partition = p;
-        uint64_t rows = 0;
-        for (uint32_t k2 = 0; k2 < nstr; ++k2) {
-          const uint64_t lo = dlo[r.off + k2], hi = dhi[r.off + k2];
-          if (hi == lo) continue;
-          tss.push_back(TileStream{lo, hi, streams[f + k2].input, 0});
-          rows += hi - lo;
-        }
-        mt.nts = (uint32_t)(tss.size() - mt.first_ts);
-        mt.rows_in = (uint32_t)rows;
-        tds.push_back(TileDesc{out_off, 0, p});
-        out_off += rows;
+      const uint32_t ts0 = (uint32_t)tss.size();
+      for (MergeTile mt : pt[p].mts) {
+        mt.out_off += out_off;
+        mt.first_ts += ts0;
+        tds.push_back(TileDesc{mt.out_off, 0, p});
         mts.push_back(mt);
       }
+      tss.insert(tss.end(), pt[p].tss.begin(), pt[p].tss.end());
+      out_off += pt[p].rows;
+      PartTiles().mts.swap(pt[p].mts);
     }
     tile_first[P] = (uint32_t)mts.size();
   }
@@ -1575,8 +1626,16 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
                    d_out.as<uint8_t>(), out_bytes, est, s);
   launches++;
   MCU(cudaEventRecord(sev[5], s));
-  std::vector<uint8_t> hout(out_bytes);
-  if (out_bytes) MCU(cudaMemcpyAsync(hout.data(), d_out.p, out_bytes, cudaMemcpyDeviceToHost, s));
+  // the output to the host: through the caller's pinned staging when given
+  // (a copy at full link speed), else into ordinary host memory
+  uint8_t* hout = staging ? staging(out_bytes + 16) : nullptr;
+  std::unique_ptr<uint8_t[]> hown;
+  if (!hout) {
+    hown.reset(new (std::nothrow) uint8_t[out_bytes + 16]);
+    if (!hown) return fail(KITE_ERR_OOM, "merge output host buffer");
+    hout = hown.get();
+  }
+  if (out_bytes) MCU(cudaMemcpyAsync(hout, d_out.p, out_bytes, cudaMemcpyDeviceToHost, s));
   MCU(cudaEventRecord(sev[6], s));
   MCU(cudaMemcpyAsync(&hst, est, sizeof hst, cudaMemcpyDeviceToHost, s));
   if (sync()) return fail(KITE_ERR_TIMEOUT, "merge wait");
@@ -1609,7 +1668,7 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     cm.key_min_lo[1] = m.kmin_hi;
     cm.key_max_lo[0] = m.kmax_lo;
     cm.key_max_lo[1] = m.kmax_hi;
-    if (emit(user, &cm, hout.data() + m.byte_off, (size_t)m.bytes)) return fail(KITE_ERR_CALLBACK, "emit callback aborted");
+    if (emit(user, &cm, hout + m.byte_off, (size_t)m.bytes)) return fail(KITE_ERR_CALLBACK, "emit callback aborted");
   }
   return KITE_OK;
 #undef MCU
