@@ -99,6 +99,8 @@ struct kite_gpu_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaStream_t copy_stream = nullptr;
+  cudaStream_t aux_stream = nullptr;   // splitters, beside the bucket scatter
+  cudaEvent_t spl_ready = nullptr;
 
   // FASTQ arena (host submissions are copied here)
   DevBuf arena;
@@ -490,11 +492,16 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     T* hist_spl = ctx->splitters.as<T>();
     T* mlp_spl = ctx->splitters2.as<T>();
     double hist_imb = -1.0;
+    // The splitters depend only on the key sample, complete since the bucket
+    // counts were read back: they are made on the side stream, so their
+    // evaluations (which wait on the host) overlap the bucket scatter; the
+    // split waits for them through an event.
+    const cudaStream_t ss = ctx->aux_stream;
     if (mode != KITE_SPLIT_LEARNED) {
       st.kernel_launches +=
-          compute_hist_splitters<T>(ctx->sample.as<T>(), nsample, 2 * k, S, hist_spl, ctx->hist16.as<unsigned>(), s);
+          compute_hist_splitters<T>(ctx->sample.as<T>(), nsample, 2 * k, S, hist_spl, ctx->hist16.as<unsigned>(), ss);
       if (mode == KITE_SPLIT_AUTO) {
-        if (predict_imbalance<T>(ctx->mlp, ctx->sample.as<T>(), nsample, hist_spl, S, s, ctx->cfg.timeout_ms,
+        if (predict_imbalance<T>(ctx->mlp, ctx->sample.as<T>(), nsample, hist_spl, S, ss, ctx->cfg.timeout_ms,
                                  &hist_imb))
           return fail(ctx, KITE_ERR_TIMEOUT, "splitter evaluation did not finish");
         st.kernel_launches += 1;
@@ -503,7 +510,7 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     bool learned = false;
     if (mode == KITE_SPLIT_LEARNED || (mode == KITE_SPLIT_AUTO && hist_imb > bound)) {
       MlpReport rep;
-      if (mlp_splitters<T>(ctx->mlp, ctx->sample.as<T>(), nsample, 2 * k, S, mlp_spl, s, ctx->cfg.timeout_ms, &rep))
+      if (mlp_splitters<T>(ctx->mlp, ctx->sample.as<T>(), nsample, 2 * k, S, mlp_spl, ss, ctx->cfg.timeout_ms, &rep))
         return fail(ctx, KITE_ERR_CUDA, "learned splitter training failed");
       st.kernel_launches += rep.launches;
       st.mlp_loss = rep.loss;
@@ -512,8 +519,8 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
       learned = rep.pred_imbalance <= bound;
       if (!learned && mode == KITE_SPLIT_LEARNED) {
         st.kernel_launches += compute_hist_splitters<T>(ctx->sample.as<T>(), nsample, 2 * k, S, hist_spl,
-                                                        ctx->hist16.as<unsigned>(), s);
-        if (predict_imbalance<T>(ctx->mlp, ctx->sample.as<T>(), nsample, hist_spl, S, s, ctx->cfg.timeout_ms,
+                                                        ctx->hist16.as<unsigned>(), ss);
+        if (predict_imbalance<T>(ctx->mlp, ctx->sample.as<T>(), nsample, hist_spl, S, ss, ctx->cfg.timeout_ms,
                                  &hist_imb))
           return fail(ctx, KITE_ERR_TIMEOUT, "splitter evaluation did not finish");
         st.kernel_launches += 1;
@@ -525,6 +532,8 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     st.splitter_used = learned ? KITE_SPLIT_LEARNED : KITE_SPLIT_SAMPLED;
     const T* chosen = learned ? mlp_spl : hist_spl;
     tile_spl = chosen;
+    KCU(cudaEventRecord(ctx->spl_ready, ss));
+    KCU(cudaStreamWaitEvent(s, ctx->spl_ready, 0));
     // Split into tiles: one level of S digits when S <= 1024, else coarse
     // ranges of 1024 tiles first, then the tiles inside each coarse range.
     // G parts per region (parts of >= 32K keys, G <= 64): the fewest parts
@@ -970,7 +979,9 @@ int kite_gpu_open(const kite_gpu_cfg* cfg, kite_gpu_ctx** out) {
     }
     ctx->own_stream = true;
   }
-  if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->spl_ready, cudaEventDisableTiming) != cudaSuccess) {
     delete ctx;
     return KITE_ERR_CUDA;
   }
@@ -992,6 +1003,7 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
   if (!ctx) return;
   cudaStreamSynchronize(ctx->stream);
   cudaStreamSynchronize(ctx->copy_stream);
+  cudaStreamSynchronize(ctx->aux_stream);
   for (auto e : ctx->ticket_events) cudaEventDestroy(e);
   for (auto e : ctx->ev) cudaEventDestroy(e);
   for (auto e : ctx->gev) cudaEventDestroy(e);
@@ -1013,6 +1025,8 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
   mlp_destroy(ctx->mlp);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   cudaStreamDestroy(ctx->copy_stream);
+  cudaStreamDestroy(ctx->aux_stream);
+  cudaEventDestroy(ctx->spl_ready);
   delete ctx;
 }
 
