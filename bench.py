@@ -1029,19 +1029,23 @@ def main():
         t_s, t_l = [], []
         for _ in range(3):
             t_s.append(timed_step(c))
+            sms = c.stats()["stage_ms"]
             t_l.append(timed_step(cl))
         ts, tl = statistics.median(t_s), statistics.median(t_l)
         stl = cl.stats()
+        sml = stl["stage_ms"]
         cl.close()
         splitters = {"timing": "CUDA events around one device-resident step, median of 3 interleaved steps each",
                      "sampled": {"kmers_per_s": kmers / ts, "tile_imbalance": st["tile_imbalance"],
                                  "range_imbalance": st["range_imbalance"],
-                                 "big_tiles": st["big_tiles"]},
+                                 "big_tiles": st["big_tiles"],
+                                 "stage_ms": {stages[i][0]: round(sms[i], 3) for i in stages}},
                      "learned": {"kmers_per_s": kmers / tl, "tile_imbalance": stl["tile_imbalance"],
                                  "range_imbalance": stl["range_imbalance"], "model_reused": stl["mlp_reused"] == 1,
                                  "big_tiles": stl["big_tiles"], "mlp_loss": stl["mlp_loss"],
                                  "predicted_imbalance": stl["mlp_pred_imbalance"],
-                                 "used": stl["splitter_used"] == gpu.SPLIT_LEARNED}}
+                                 "used": stl["splitter_used"] == gpu.SPLIT_LEARNED,
+                                 "stage_ms": {stages[i][0]: round(sml[i], 3) for i in stages}}}
 
     # ---- the whole workload's output against the oracle (untimed) ----
     parity = None

@@ -114,7 +114,10 @@ template void launch_tile_link<u128>(const TileOut<u128>*, uint32_t, uint32_t, u
                                      BucketMeta*, cudaStream_t);
 
 // Exclusive scan of bucket byte sizes into byte_off (single CTA; P <= 1<<16).
-__global__ void __launch_bounds__(1024) k_bucket_offsets(BucketMeta* meta, uint32_t P) {
+// With a mirror (pinned host memory mapped into the device's address space),
+// the finished records are also written there, so the host reads them when
+// the kernel has completed without a copy that would queue on a copy engine.
+__global__ void __launch_bounds__(1024) k_bucket_offsets(BucketMeta* meta, uint32_t P, BucketMeta* mirror) {
   __shared__ unsigned long long sm[34];
   unsigned long long carry = 0;
   for (uint32_t b0 = 0; b0 < P; b0 += 1024) {
@@ -122,13 +125,16 @@ __global__ void __launch_bounds__(1024) k_bucket_offsets(BucketMeta* meta, uint3
     const unsigned long long v = b < P ? meta[b].bytes : 0;
     unsigned long long tot;
     const unsigned long long ex = block_exclusive_scan<1024, unsigned long long>(v, sm, &tot);
-    if (b < P) meta[b].byte_off = carry + ex;
+    if (b < P) {
+      meta[b].byte_off = carry + ex;
+      if (mirror) mirror[b] = meta[b];
+    }
     carry += tot;
   }
 }
 
-void launch_bucket_offsets(BucketMeta* meta, uint32_t P, unsigned long long*, cudaStream_t s) {
-  k_bucket_offsets<<<1, 1024, 0, s>>>(meta, P);
+void launch_bucket_offsets(BucketMeta* meta, uint32_t P, BucketMeta* host_mirror, cudaStream_t s) {
+  k_bucket_offsets<<<1, 1024, 0, s>>>(meta, P, host_mirror);
 }
 
 template <class T>

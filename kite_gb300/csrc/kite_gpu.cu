@@ -736,6 +736,11 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   TileOut<T>* tout = ctx->tile_out.as<TileOut<T>>();
   BucketMeta* meta = ctx->meta.as<BucketMeta>();
   BucketMeta* hmeta = ctx->h_meta.as<BucketMeta>();
+  // the device's address of the pinned records (mapped host memory): the
+  // offsets kernel writes them there, and nothing queues on a copy engine
+  // behind the previous group's payload copy
+  BucketMeta* hmeta_dev = nullptr;
+  KCU(cudaHostGetDevicePointer(reinterpret_cast<void**>(&hmeta_dev), hmeta, 0));
 
   // ---- K4 tile sort + RLE, K5 link and byte offsets (one group) --------------
   auto queue_sort = [&](uint32_t g) -> cudaError_t {
@@ -763,8 +768,7 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     // ---- K5: per-bucket tile links, byte offsets from the group's start
     launch_tile_link<T>(tout + t0, nb, Sl, ctx->tile_boff.as<unsigned long long>() + t0, ctx->tile_prev.as<T>() + t0,
                         meta + gb[g], s);
-    launch_bucket_offsets(meta + gb[g], nb, nullptr, s);
-    cudaMemcpyAsync(hmeta + gb[g], meta + gb[g], (size_t)nb * sizeof(BucketMeta), cudaMemcpyDeviceToHost, s);
+    launch_bucket_offsets(meta + gb[g], nb, hmeta_dev + gb[g], s);
     cudaEventRecord(gev[8 * g + 3], s);
     return cudaGetLastError();
   };

@@ -224,6 +224,8 @@ void launch_encode(const T* keys, const uint32_t* counts, const TileDesc* tiles,
 template <class T>
 void launch_tile_link_ranges(const TileOut<T>* tout, uint32_t P, const uint32_t* tile_first,
                              unsigned long long* tile_boff, T* tile_prev, BucketMeta* meta, cudaStream_t s);
-void launch_bucket_offsets(BucketMeta* meta, uint32_t P, unsigned long long* tmp, cudaStream_t s);
+// host_mirror: optional device address of mapped pinned host memory that
+// receives a copy of the P finished records
+void launch_bucket_offsets(BucketMeta* meta, uint32_t P, BucketMeta* host_mirror, cudaStream_t s);
 
 }  // namespace kite
