@@ -99,7 +99,7 @@ struct kite_gpu_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaStream_t copy_stream = nullptr;
-  cudaStream_t aux_stream = nullptr;   // splitters, beside the bucket scatter
+  cudaStream_t aux_stream = nullptr;   // splitters, beside the bucket scatter (highest priority)
   cudaEvent_t spl_ready = nullptr;
 
   // FASTQ arena (host submissions are copied here)
@@ -983,8 +983,12 @@ int kite_gpu_open(const kite_gpu_cfg* cfg, kite_gpu_ctx** out) {
     }
     ctx->own_stream = true;
   }
+  // The splitter stream has the highest priority: its small kernels take SMs
+  // as the bucket scatter's CTAs retire instead of waiting for its last wave.
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
   if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&ctx->aux_stream, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->spl_ready, cudaEventDisableTiming) != cudaSuccess) {
     delete ctx;
     return KITE_ERR_CUDA;
