@@ -1050,10 +1050,15 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     }
     part_first_stream[P] = nst;
   }
+  // tiles of three quarters of the on-chip capacity on average (the
+  // refinement below splits the few that the cut leaves above it): the merge
+  // kernel's cost per tile is mostly fixed (stream scan, merge rounds,
+  // barriers), so fuller tiles cost less per row
   uint32_t S = 1;
-  // tiles of about half the on-chip capacity (the refinement below splits the
-  // few that the cut leaves above it)
-  while ((double)total_rows / ((double)P * S) > 0.5 * kMergeCap && S < 4096) S <<= 1;
+  {
+    const double want = (double)total_rows / ((double)P * 0.75 * kMergeCap);
+    if (want > 1.0) S = (uint32_t)std::min(4096.0, std::ceil(want));
+  }
   std::vector<T> spl;
   Dev d_spl;
   if (S > 1 && total_rows) {
