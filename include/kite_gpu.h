@@ -195,8 +195,9 @@ int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n,
  * partition that has lines, in ascending partition order, with meta
  * {partition_id, codec 0, row_count = lines, raw_bytes = TSV bytes, key_min /
  * key_max = its first and last key} and the TSV bytes (valid during the
- * call).  stats.stage_ms[0..4]: decode, tile planning, merge, formatting,
- * copy to the host. */
+ * call).  stats.stage_ms[0..5]: decode kernels, tile planning, merge,
+ * formatting, copy to the host, copy of the input in (which the decode
+ * overlaps). */
 int kite_gpu_dump(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, kite_gpu_emit_fn emit, void* user);
 
 /* Called once per count value with the number of keys that have it. */

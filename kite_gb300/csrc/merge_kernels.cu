@@ -302,20 +302,22 @@ __global__ void __launch_bounds__(32 * kDecWarps)
   }
 }
 
-// Per stream (one warp each): first varint index and start key of every
-// segment (exclusive scans of the terminator counts and of the delta sums),
-// and the check that the stream holds the 2 * (rows - 1) varints its rows need.
+// Per stream of the list sids (one warp each): first varint index and start
+// key of every segment [seg_first, seg_end) of the stream (exclusive scans of
+// the terminator counts and of the delta sums), and the check that the stream
+// holds the 2 * (rows - 1) varints its rows need.
 template <class T>
 __global__ void k_stream_seg_scan(const uint32_t* __restrict__ terms, const T* __restrict__ sum_even,
                                   const T* __restrict__ sum_odd, const uint32_t* __restrict__ seg_first,
-                                  const StreamDesc* __restrict__ streams, const T* __restrict__ first_keys,
-                                  uint32_t nst, unsigned long long* __restrict__ vstart, T* __restrict__ kstart,
-                                  DevStatus* st) {
+                                  const uint32_t* __restrict__ seg_end, const StreamDesc* __restrict__ streams,
+                                  const T* __restrict__ first_keys, const uint32_t* __restrict__ sids, uint32_t nsid,
+                                  unsigned long long* __restrict__ vstart, T* __restrict__ kstart, DevStatus* st) {
   const uint32_t lane = threadIdx.x & 31;
-  const uint32_t si = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  if (si >= nst) return;
+  const uint32_t w = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (w >= nsid) return;
+  const uint32_t si = sids[w];
   const StreamDesc sd = streams[si];
-  const uint32_t f = seg_first[si], e = seg_first[si + 1];
+  const uint32_t f = seg_first[si], e = seg_end[si];
   unsigned long long cv = 0;
   T ck = f < e ? first_keys[si] : T(0);
   for (uint32_t b = f; b < e; b += 32) {
@@ -410,13 +412,14 @@ __global__ void __launch_bounds__(32 * kDecWarps)
   }
 }
 
-// Head row of every DVLE stream and all rows of RAW streams.
+// Head row of every DVLE stream of the list sids.
 template <class T>
 __global__ void k_stream_heads(const uint8_t* __restrict__ bytes, const StreamDesc* __restrict__ streams,
-                               uint32_t nstreams, T* __restrict__ keys, unsigned long long* __restrict__ counts,
-                               T* __restrict__ first_keys) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nstreams) return;
+                               const uint32_t* __restrict__ sids, uint32_t nsid, T* __restrict__ keys,
+                               unsigned long long* __restrict__ counts, T* __restrict__ first_keys) {
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nsid) return;
+  const uint32_t i = sids[w];
   const StreamDesc sd = streams[i];
   if (sd.rows == 0 || sd.head == 0) return;
   const uint8_t* p = bytes + sd.byte_off;
@@ -966,76 +969,124 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
         streams.push_back(sd);
       }
   stat->h2d_bytes += total_bytes;
-  Dev d_bytes, d_streams, d_segs, d_terms, d_vstart, d_dsum, d_dsum2, d_sfirst, d_kstart, d_keys, d_counts, d_first,
-      d_raw;
+  Dev d_bytes, d_streams, d_segs, d_terms, d_vstart, d_dsum, d_dsum2, d_sfirst, d_send, d_sids, d_kstart, d_keys,
+      d_counts, d_first, d_raw;
   if (!d_bytes.ensure(total_bytes + 64)) return fail(KITE_ERR_OOM, "device bytes");
-  for (int i = 0; i < n; ++i)
-    if (in_span[i].second > in_span[i].first)
-      MCU(cudaMemcpyAsync(d_bytes.as<uint8_t>() + in_base[i], in[i].base + in_span[i].first,
-                          in_span[i].second - in_span[i].first, cudaMemcpyHostToDevice, s));
-  MCU(cudaEventRecord(sev[0], s));
-  // ---- decode segments ----
+  // ---- decode segments, grouped by input: each input's bytes come in on a
+  // side stream and its segments are decoded as soon as they have landed, so
+  // the copies of the later inputs overlap the decode of the earlier ones ----
   std::vector<SegDesc> segs;
   std::vector<uint32_t> raw_ids;
-  std::vector<uint32_t> seg_first(streams.size() + 1);
-  for (uint32_t si = 0; si < streams.size(); ++si) {
-    seg_first[si] = (uint32_t)segs.size();
-    const StreamDesc& sd = streams[si];
-    if (sd.rows == 0) continue;
-    if (sd.head == 0) {
-      raw_ids.push_back(si);
-      continue;
+  std::vector<uint32_t> seg_first(streams.size(), 0), seg_end(streams.size(), 0);
+  std::vector<uint32_t> sids;                                   // DVLE streams with rows, input by input
+  std::vector<uint32_t> in_seg(n + 1, 0), in_sid(n + 1, 0);     // per input: its segment and stream-id ranges
+  {
+    std::vector<std::vector<uint32_t>> by_input(n);
+    for (uint32_t si = 0; si < streams.size(); ++si) by_input[streams[si].input].push_back(si);
+    for (int i = 0; i < n; ++i) {
+      in_seg[i] = (uint32_t)segs.size();
+      in_sid[i] = (uint32_t)sids.size();
+      for (uint32_t si : by_input[i]) {
+        const StreamDesc& sd = streams[si];
+        seg_first[si] = seg_end[si] = (uint32_t)segs.size();
+        if (sd.rows == 0) continue;
+        if (sd.head == 0) {
+          raw_ids.push_back(si);
+          continue;
+        }
+        sids.push_back(si);
+        const uint64_t a = sd.byte_off + sd.head, e = sd.byte_off + sd.byte_len;
+        for (uint64_t o = a; o < e; o += kSeg) segs.push_back(SegDesc{o, std::min(o + kSeg, e), si, o == a ? 1u : 0u});
+        seg_end[si] = (uint32_t)segs.size();
+      }
     }
-    const uint64_t a = sd.byte_off + sd.head, e = sd.byte_off + sd.byte_len;
-    for (uint64_t o = a; o < e; o += kSeg) segs.push_back(SegDesc{o, std::min(o + kSeg, e), si, o == a ? 1u : 0u});
+    in_seg[n] = (uint32_t)segs.size();
+    in_sid[n] = (uint32_t)sids.size();
   }
-  seg_first[streams.size()] = (uint32_t)segs.size();
-  const uint32_t nseg = (uint32_t)segs.size(), nst = (uint32_t)streams.size();
+  const uint32_t nseg = (uint32_t)segs.size(), nst = (uint32_t)streams.size(), nsid = (uint32_t)sids.size();
   if (!d_streams.ensure(nst * sizeof(StreamDesc) + 8) || !d_segs.ensure(nseg * sizeof(SegDesc) + 8) ||
       !d_terms.ensure(nseg * 4 + 8) || !d_vstart.ensure(nseg * 8 + 8) || !d_dsum.ensure(nseg * sizeof(T) + 16) ||
-      !d_kstart.ensure(nseg * sizeof(T) + 16) || !d_keys.ensure(total_rows * sizeof(T) + 16) ||
-      !d_counts.ensure(total_rows * 8 + 16) || !d_first.ensure(nst * sizeof(T) + 16) || !d_raw.ensure(raw_ids.size() * 4 + 8))
+      !d_dsum2.ensure(nseg * sizeof(T) + 16) || !d_kstart.ensure(nseg * sizeof(T) + 16) ||
+      !d_keys.ensure(total_rows * sizeof(T) + 16) || !d_counts.ensure(total_rows * 8 + 16) ||
+      !d_first.ensure(nst * sizeof(T) + 16) || !d_raw.ensure(raw_ids.size() * 4 + 8) ||
+      !d_sfirst.ensure(nst * 4 + 8) || !d_send.ensure(nst * 4 + 8) || !d_sids.ensure(nsid * 4 + 8))
     return fail(KITE_ERR_OOM, "merge decode buffers");
   MCU(cudaMemcpyAsync(d_streams.p, streams.data(), nst * sizeof(StreamDesc), cudaMemcpyHostToDevice, s));
   if (nseg) MCU(cudaMemcpyAsync(d_segs.p, segs.data(), nseg * sizeof(SegDesc), cudaMemcpyHostToDevice, s));
+  if (nst) {
+    MCU(cudaMemcpyAsync(d_sfirst.p, seg_first.data(), nst * 4, cudaMemcpyHostToDevice, s));
+    MCU(cudaMemcpyAsync(d_send.p, seg_end.data(), nst * 4, cudaMemcpyHostToDevice, s));
+  }
+  if (nsid) MCU(cudaMemcpyAsync(d_sids.p, sids.data(), nsid * 4, cudaMemcpyHostToDevice, s));
   if (!raw_ids.empty())
     MCU(cudaMemcpyAsync(d_raw.p, raw_ids.data(), raw_ids.size() * 4, cudaMemcpyHostToDevice, s));
   int launches = 0;
   DevStatus* dst = nullptr;
   MCU(cudaMallocAsync(&dst, sizeof(DevStatus), s));
   MCU(cudaMemsetAsync(dst, 0, sizeof(DevStatus), s));
-  if (nst) {
-    k_stream_heads<T><<<(nst + 255) / 256, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_streams.as<StreamDesc>(), nst,
-                                                        d_keys.as<T>(), d_counts.as<unsigned long long>(),
-                                                        d_first.as<T>());
-    launches++;
+  // copy lane: the side stream, one landing event per input, timing events
+  // around the copies ([0], [1]) and around each input's decode ([2 + 2i],
+  // [3 + 2i]: recorded after the wait, so they time the kernels only)
+  struct CopyLane {
+    cudaStream_t cs = nullptr;
+    std::vector<cudaEvent_t> ev, tev;
+    ~CopyLane() {
+      for (auto e : ev) cudaEventDestroy(e);
+      for (auto e : tev) cudaEventDestroy(e);
+      if (cs) cudaStreamDestroy(cs);
+    }
+  } cl;
+  MCU(cudaStreamCreateWithFlags(&cl.cs, cudaStreamNonBlocking));
+  cl.ev.resize(n, nullptr);
+  for (int i = 0; i < n; ++i) MCU(cudaEventCreateWithFlags(&cl.ev[i], cudaEventDisableTiming));
+  cl.tev.resize(2 + 2 * (size_t)n, nullptr);
+  for (auto& e : cl.tev) MCU(cudaEventCreate(&e));
+  MCU(cudaEventRecord(sev[0], s));
+  MCU(cudaEventRecord(cl.tev[0], cl.cs));
+  for (int i = 0; i < n; ++i) {
+    if (in_span[i].second > in_span[i].first)
+      MCU(cudaMemcpyAsync(d_bytes.as<uint8_t>() + in_base[i], in[i].base + in_span[i].first,
+                          in_span[i].second - in_span[i].first, cudaMemcpyHostToDevice, cl.cs));
+    MCU(cudaEventRecord(cl.ev[i], cl.cs));
+  }
+  MCU(cudaEventRecord(cl.tev[1], cl.cs));
+  const uint64_t lim_pad = total_bytes + 64;  // every aligned 16-byte block below this is readable
+  for (int i = 0; i < n; ++i) {
+    MCU(cudaStreamWaitEvent(s, cl.ev[i], 0));
+    MCU(cudaEventRecord(cl.tev[2 + 2 * i], s));
+    const uint32_t s0 = in_seg[i], ns = in_seg[i + 1] - in_seg[i];
+    const uint32_t q0 = in_sid[i], nq = in_sid[i + 1] - in_sid[i];
+    if (nq) {
+      k_stream_heads<T><<<(nq + 255) / 256, 256, 0, s>>>(d_bytes.as<uint8_t>(), d_streams.as<StreamDesc>(),
+                                                         d_sids.as<uint32_t>() + q0, nq, d_keys.as<T>(),
+                                                         d_counts.as<unsigned long long>(), d_first.as<T>());
+      launches++;
+    }
+    if (ns) {
+      // DVLE varints: pass A (per-segment counts and parity sums), the
+      // per-stream scans, pass B (rows); no host round trip
+      const unsigned gsegs = (ns + kDecWarps - 1) / kDecWarps;
+      k_seg_pass_a<T><<<gsegs, 32 * kDecWarps, 0, s>>>(d_bytes.as<uint8_t>(), lim_pad, d_segs.as<SegDesc>() + s0, ns,
+                                                       d_streams.as<StreamDesc>(), d_terms.as<uint32_t>() + s0,
+                                                       d_dsum.as<T>() + s0, d_dsum2.as<T>() + s0);
+      k_stream_seg_scan<T><<<(nq + 7) / 8, 256, 0, s>>>(d_terms.as<uint32_t>(), d_dsum.as<T>(), d_dsum2.as<T>(),
+                                                        d_sfirst.as<uint32_t>(), d_send.as<uint32_t>(),
+                                                        d_streams.as<StreamDesc>(), d_first.as<T>(),
+                                                        d_sids.as<uint32_t>() + q0, nq,
+                                                        d_vstart.as<unsigned long long>(), d_kstart.as<T>(), dst);
+      k_seg_rows<T><<<gsegs, 32 * kDecWarps, 0, s>>>(d_bytes.as<uint8_t>(), lim_pad, d_segs.as<SegDesc>() + s0, ns,
+                                                     d_streams.as<StreamDesc>(), d_vstart.as<unsigned long long>() + s0,
+                                                     d_kstart.as<T>() + s0, d_keys.as<T>(),
+                                                     d_counts.as<unsigned long long>());
+      launches += 3;
+    }
+    MCU(cudaEventRecord(cl.tev[3 + 2 * i], s));
   }
   if (!raw_ids.empty()) {
     k_raw_rows<T><<<(unsigned)raw_ids.size(), 256, 0, s>>>(d_bytes.as<uint8_t>(), d_streams.as<StreamDesc>(),
                                                            d_raw.as<uint32_t>(), (uint32_t)raw_ids.size(),
                                                            d_keys.as<T>(), d_counts.as<unsigned long long>());
     launches++;
-  }
-  // DVLE varints: pass A (per-segment counts and parity sums), per-stream
-  // scans on the device, pass B (rows); no host round trip
-  if (nseg) {
-    if (!d_dsum2.ensure(nseg * sizeof(T) + 16) || !d_sfirst.ensure((nst + 1) * 4 + 8))
-      return fail(KITE_ERR_OOM, "merge decode buffers");
-    MCU(cudaMemcpyAsync(d_sfirst.p, seg_first.data(), (nst + 1) * 4, cudaMemcpyHostToDevice, s));
-    const unsigned gsegs = (nseg + kDecWarps - 1) / kDecWarps;
-    const uint64_t lim_pad = total_bytes + 64;  // every aligned 16-byte block below this is readable
-    k_seg_pass_a<T><<<gsegs, 32 * kDecWarps, 0, s>>>(d_bytes.as<uint8_t>(), lim_pad, d_segs.as<SegDesc>(), nseg,
-                                                     d_streams.as<StreamDesc>(), d_terms.as<uint32_t>(),
-                                                     d_dsum.as<T>(), d_dsum2.as<T>());
-    k_stream_seg_scan<T><<<(nst + 7) / 8, 256, 0, s>>>(d_terms.as<uint32_t>(), d_dsum.as<T>(), d_dsum2.as<T>(),
-                                                       d_sfirst.as<uint32_t>(), d_streams.as<StreamDesc>(),
-                                                       d_first.as<T>(), nst, d_vstart.as<unsigned long long>(),
-                                                       d_kstart.as<T>(), dst);
-    k_seg_rows<T><<<gsegs, 32 * kDecWarps, 0, s>>>(d_bytes.as<uint8_t>(), lim_pad, d_segs.as<SegDesc>(), nseg,
-                                                   d_streams.as<StreamDesc>(), d_vstart.as<unsigned long long>(),
-                                                   d_kstart.as<T>(), d_keys.as<T>(),
-                                                   d_counts.as<unsigned long long>());
-    launches += 3;
   }
   DevStatus hdec{};
   MCU(cudaMemcpyAsync(&hdec, dst, sizeof hdec, cudaMemcpyDeviceToHost, s));
@@ -1382,6 +1433,13 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     float ms = 0;
     for (int i = 0; i < 5; ++i)
       if (cudaEventElapsedTime(&ms, sev[pairs[i][0]], sev[pairs[i][1]]) == cudaSuccess) stat->stage_ms[i] = ms;
+    // [0] the decode kernels alone (the wait for each input's bytes left
+    // out), [5] the copies of the inputs in, which the decode overlaps
+    float dec = 0;
+    for (int i = 0; i < n; ++i)
+      if (cudaEventElapsedTime(&ms, cl.tev[2 + 2 * i], cl.tev[3 + 2 * i]) == cudaSuccess) dec += ms;
+    stat->stage_ms[0] = dec;
+    if (cudaEventElapsedTime(&ms, cl.tev[0], cl.tev[1]) == cudaSuccess) stat->stage_ms[5] = ms;
   };
   stat->tiles = ntiles;
   if (mode == kModeHisto) {
