@@ -100,6 +100,7 @@ struct kite_gpu_ctx {
   bool own_stream = false;
   cudaStream_t copy_stream = nullptr;
   cudaStream_t aux_stream = nullptr;   // splitters, beside the bucket scatter (highest priority)
+  MergePool merge_pool;                // merge / dump / histo / query device buffers, kept across calls
   cudaEvent_t spl_ready = nullptr;
 
   // FASTQ arena (host submissions are copied here)
@@ -1174,6 +1175,7 @@ int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n,
   MergeExtra ex;
   ex.mlp = ctx->mlp;
   ex.splitter_mode = ctx->cfg.splitter_mode;
+  ex.pool = &ctx->merge_pool;
   auto staging = [ctx](size_t bytes) -> uint8_t* {
     return ctx->h_dump.ensure(bytes) == cudaSuccess ? ctx->h_dump.as<uint8_t>() : nullptr;
   };
@@ -1190,8 +1192,10 @@ int kite_gpu_dump(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, kite_gpu
   auto staging = [ctx](size_t bytes) -> uint8_t* {
     return ctx->h_dump.ensure(bytes) == cudaSuccess ? ctx->h_dump.as<uint8_t>() : nullptr;
   };
+  MergeExtra ex;
+  ex.pool = &ctx->merge_pool;
   int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, input, 1, ctx->stream, ctx->cfg.timeout_ms, kMergeModeDump,
-                     emit, user, &msg, &ctx->stats, staging);
+                     emit, user, &msg, &ctx->stats, staging, &ex);
   if (rc) ctx->err = msg;
   return rc;
 }
@@ -1203,6 +1207,7 @@ int kite_gpu_histo(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, kite_gp
   MergeExtra ex;
   ex.histo = emit;
   ex.user = user;
+  ex.pool = &ctx->merge_pool;
   int rc = merge_run(ctx->cfg.k, ctx->cfg.partitions, input, 1, ctx->stream, ctx->cfg.timeout_ms, kMergeModeHisto,
                      nullptr, nullptr, &msg, &ctx->stats, nullptr, &ex);
   if (rc) ctx->err = msg;
@@ -1235,6 +1240,7 @@ int kite_gpu_query(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, const u
   ex.parts = parts.data();
   ex.nq = n;
   ex.counts_out = counts;
+  ex.pool = &ctx->merge_pool;
   int rc = merge_run(ctx->cfg.k, P, &sub, 1, ctx->stream, ctx->cfg.timeout_ms, kMergeModeQuery, nullptr, nullptr,
                      &msg, &ctx->stats, nullptr, &ex);
   if (rc) ctx->err = msg;

@@ -17,6 +17,24 @@ using StagingFn = std::function<uint8_t*(size_t)>;
 // Modes of merge_run (the merge kernel's kModeMerge / kModeDump / kModeHisto / kModeRows).
 enum : int { kMergeModeMerge = 0, kMergeModeDump = 1, kMergeModeHisto = 2, kMergeModeQuery = 3 };
 
+// Device buffers of the merge path kept by a context across calls (grown,
+// never shrunk), so repeated merges, dumps and queries do not pay for
+// allocating and freeing gigabytes every call.
+struct MergePoolSlot {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+struct MergePool {
+  static constexpr int kSlots = 32;
+  MergePoolSlot slot[kSlots];
+  MergePool() = default;
+  MergePool(const MergePool&) = delete;
+  MergePool& operator=(const MergePool&) = delete;
+  ~MergePool() {
+    for (auto& s : slot) cudaFree(s.p);
+  }
+};
+
 // Inputs and outputs of the histo and query modes.
 struct MergeExtra {
   kite_gpu_histo_fn histo = nullptr;  // histo: called per count in ascending order
@@ -27,6 +45,7 @@ struct MergeExtra {
   uint64_t* counts_out = nullptr;     // query: u64 sum per key, 0 when absent
   MlpModel* mlp = nullptr;            // learned CDF for the tile cut (null: sampled histogram only)
   int splitter_mode = 0;              // KITE_SPLIT_*: AUTO keeps whichever predicts the lower imbalance
+  MergePool* pool = nullptr;          // the context's buffers (null: allocated and freed by the call)
 };
 
 // k selects the key width (u64 for k <= 31, else u128) and the splitter key

@@ -883,19 +883,32 @@ struct Key128 {
 };
 
 // ---- host side -----------------------------------------------------------------
+// A device buffer of the call: its own allocation, or a slot of the
+// context's pool (kept after the call).
 struct Dev {
+  MergePoolSlot own;
+  MergePoolSlot* sl = &own;
   void* p = nullptr;
   size_t cap = 0;
+  Dev() = default;
+  Dev(MergePool* pool, int slot) : sl(pool ? &pool->slot[slot] : &own) {}
+  Dev(const Dev&) = delete;
+  Dev& operator=(const Dev&) = delete;
   bool ensure(size_t b) {
-    if (b <= cap) return true;
-    cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    if (cudaMalloc(&p, b + 256) != cudaSuccess) return false;
-    cap = b + 256;
+    if (b > sl->cap) {
+      cudaFree(sl->p);
+      sl->p = nullptr;
+      sl->cap = 0;
+      if (cudaMalloc(&sl->p, b + 256) != cudaSuccess) return false;
+      sl->cap = b + 256;
+    }
+    p = sl->p;
+    cap = sl->cap;
     return true;
   }
-  ~Dev() { cudaFree(p); }
+  ~Dev() {
+    if (sl == &own) cudaFree(own.p);
+  }
   template <class U> U* as() { return static_cast<U*>(p); }
 };
 
@@ -969,8 +982,10 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
         streams.push_back(sd);
       }
   stat->h2d_bytes += total_bytes;
-  Dev d_bytes, d_streams, d_segs, d_terms, d_vstart, d_dsum, d_dsum2, d_sfirst, d_send, d_sids, d_kstart, d_keys,
-      d_counts, d_first, d_raw;
+  MergePool* pool = ex ? ex->pool : nullptr;
+  Dev d_bytes(pool, 0), d_streams(pool, 1), d_segs(pool, 2), d_terms(pool, 3), d_vstart(pool, 4), d_dsum(pool, 5),
+      d_dsum2(pool, 6), d_sfirst(pool, 7), d_send(pool, 8), d_sids(pool, 9), d_kstart(pool, 10), d_keys(pool, 11),
+      d_counts(pool, 12), d_first(pool, 13), d_raw(pool, 14);
   if (!d_bytes.ensure(total_bytes + 64)) return fail(KITE_ERR_OOM, "device bytes");
   // ---- decode segments, grouped by input: each input's bytes come in on a
   // side stream and its segments are decoded as soon as they have landed, so
@@ -1371,7 +1386,9 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   std::vector<InputFilter> filt(n);
   for (int i = 0; i < n; ++i)
     filt[i] = InputFilter{(uint32_t)in[i].has_min, (uint32_t)in[i].has_max, in[i].min_count, in[i].max_count};
-  Dev d_mt, d_ts, d_filt, d_okeys, d_ocounts, d_tout, d_over, d_tds, d_tf, d_boff, d_prev, d_meta, d_out;
+  Dev d_mt(pool, 15), d_ts(pool, 16), d_filt(pool, 17), d_okeys(pool, 18), d_ocounts(pool, 19), d_tout(pool, 20),
+      d_over(pool, 21), d_tds(pool, 22), d_tf(pool, 23), d_boff(pool, 24), d_prev(pool, 25), d_meta(pool, 26),
+      d_out(pool, 27);
   if (!d_mt.ensure(ntiles * sizeof(MergeTile) + 8) || !d_ts.ensure(tss.size() * sizeof(TileStream) + 8) ||
       !d_filt.ensure(n * sizeof(InputFilter)) || !d_okeys.ensure(out_off * sizeof(T) + 16) ||
       !d_ocounts.ensure(out_off * 4 + 16) || !d_tout.ensure(ntiles * sizeof(TileOut<T>) + 16) ||
@@ -1404,6 +1421,206 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   if (mode == kModeRows) {
     if (!d_c64.ensure(out_off * 8 + 8)) return fail(KITE_ERR_OOM, "query buffers");
     aux.counts64 = d_c64.as<unsigned long long>();
+  }
+  if (mode == kModeMerge && ntiles) {
+    // ---- merge, encode and copy-out pipelined over partition groups: group
+    // g's payload copies to the host (on the input copy lane, idle by now)
+    // while group g + 1 merges.  The offsets kernel writes each group's
+    // partition records into mapped pinned memory, so the host sizes the
+    // group's encode without a copy that would queue on a copy engine. ----
+    const uint32_t NG = std::min<uint32_t>(8, P);
+    std::vector<uint32_t> pb(NG + 1);
+    for (uint32_t g = 0; g <= NG; ++g) pb[g] = (uint32_t)((uint64_t)P * g / NG);
+    if (NG == 8 && P >= 64) {
+      // tapering groups (weights 6,6,6,6,6,5,3,2 of 40): the last copy-out,
+      // which nothing overlaps, carries about a twentieth of the output
+      static const uint32_t cw[9] = {0, 6, 12, 18, 24, 30, 35, 38, 40};
+      for (uint32_t g = 0; g <= NG; ++g) pb[g] = (uint32_t)((uint64_t)P * cw[g] / 40);
+    }
+    MCU(cudaMemcpyAsync(d_tds.p, tds.data(), ntiles * sizeof(TileDesc), cudaMemcpyHostToDevice, s));
+    MCU(cudaMemcpyAsync(d_tf.p, tile_first.data(), (P + 1) * 4, cudaMemcpyHostToDevice, s));
+    if (!d_over.ensure((size_t)NG * 8)) return fail(KITE_ERR_OOM, "merge tile buffers");
+    MCU(cudaMemsetAsync(d_over.p, 0xff, (size_t)NG * 8, s));  // per group: its first overflowing row
+    struct HostMem {
+      void* p = nullptr;
+      ~HostMem() {
+        if (p) cudaFreeHost(p);
+      }
+    } hmm;
+    MCU(cudaMallocHost(&hmm.p, (size_t)P * sizeof(BucketMeta)));
+    BucketMeta* hm = static_cast<BucketMeta*>(hmm.p);
+    BucketMeta* hm_dev = nullptr;
+    MCU(cudaHostGetDevicePointer(reinterpret_cast<void**>(&hm_dev), hm, 0));
+    // output buffers: the inputs' payload size to start with (a merged
+    // partition's rows are at most its inputs' rows); a group that needs more
+    // grows them once every queued encode and copy has finished
+    uint64_t cap = std::max<uint64_t>(total_bytes, 1ull << 20) + 16;
+    if (!d_out.ensure(cap)) return fail(KITE_ERR_OOM, "merge output");
+    uint8_t* hout = staging ? staging(cap) : nullptr;
+    std::unique_ptr<uint8_t[]> hown;
+    if (!hout) {
+      hown.reset(new (std::nothrow) uint8_t[cap]);
+      if (!hown) return fail(KITE_ERR_OOM, "merge output host buffer");
+      hout = hown.get();
+    }
+    DevStatus* est = nullptr;
+    MCU(cudaMallocAsync(&est, sizeof(DevStatus), s));
+    MCU(cudaMemsetAsync(est, 0, sizeof(DevStatus), s));
+    struct Evs {
+      std::vector<cudaEvent_t> e;
+      ~Evs() {
+        for (auto x : e) cudaEventDestroy(x);
+      }
+    } gv;
+    gv.e.resize(7 * (size_t)NG, nullptr);
+    for (auto& e : gv.e) MCU(cudaEventCreate(&e));
+    cudaEvent_t* ge = gv.e.data();  // per group: merge, merged, linked | encode start, end | copy start, end
+    MCU(cudaEventRecord(sev[2], s));
+    auto queue_merge = [&](uint32_t g) -> cudaError_t {
+      const uint32_t pa = pb[g], pe = pb[g + 1], ta = tile_first[pa], tb = tile_first[pe];
+      cudaEventRecord(ge[7 * g], s);
+      if (tb > ta)
+        kmerge<<<tb - ta, kMergeThreads, smem, s>>>(d_keys.as<T>(), d_counts.as<unsigned long long>(),
+                                                    d_mt.as<MergeTile>() + ta, d_ts.as<TileStream>(),
+                                                    d_filt.as<InputFilter>(), d_okeys.as<T>(), d_ocounts.as<uint32_t>(),
+                                                    d_tout.as<TileOut<T>>() + ta, d_over.as<unsigned long long>() + g,
+                                                    dst, aux);
+      cudaEventRecord(ge[7 * g + 1], s);
+      if (pe > pa) {
+        launch_tile_link_ranges<T>(d_tout.as<TileOut<T>>(), pe - pa, d_tf.as<uint32_t>() + pa,
+                                   d_boff.as<unsigned long long>(), d_prev.as<T>(), d_meta.as<BucketMeta>() + pa, s);
+        launch_bucket_offsets(d_meta.as<BucketMeta>() + pa, pe - pa, hm_dev + pa, s);
+      }
+      cudaEventRecord(ge[7 * g + 2], s);
+      return cudaGetLastError();
+    };
+    std::vector<uint64_t> gbase(NG, 0);
+    uint64_t total_out = 0, out_rows = 0;
+    MCU(queue_merge(0));
+    for (uint32_t g = 0; g < NG; ++g) {
+      if (g + 1 < NG) MCU(queue_merge(g + 1));
+      launches += 3;
+      if (bounded_event_wait(ge[7 * g + 2], timeout_ms)) return fail(KITE_ERR_TIMEOUT, "merge group wait");
+      const uint32_t pa = pb[g], pe = pb[g + 1], ta = tile_first[pa], tb = tile_first[pe];
+      uint64_t gbytes = 0;
+      for (uint32_t p = pa; p < pe; ++p) {
+        gbytes += hm[p].bytes;
+        out_rows += hm[p].rows;
+      }
+      if (total_out + gbytes + 16 > cap) {
+        // every earlier group's bytes are on the host once the copy lane is
+        // idle: the device buffer is replaced, the host one grown with them
+        if (bounded_sync(s, timeout_ms) || bounded_sync(cl.cs, timeout_ms))
+          return fail(KITE_ERR_TIMEOUT, "merge output wait");
+        const uint64_t ncap = total_out + gbytes + 16 + (total_out + gbytes) / 4;
+        if (!d_out.ensure(ncap)) return fail(KITE_ERR_OOM, "merge output");
+        std::unique_ptr<uint8_t[]> nh(new (std::nothrow) uint8_t[ncap]);
+        if (!nh) return fail(KITE_ERR_OOM, "merge output host buffer");
+        std::memcpy(nh.get(), hout, total_out);
+        hown = std::move(nh);
+        hout = hown.get();
+        cap = ncap;
+      }
+      gbase[g] = total_out;
+      MCU(cudaEventRecord(ge[7 * g + 3], s));
+      // k_encode places a partition's bytes at its record's offset (relative
+      // to the group) plus the tile's: the group's slice of the output
+      if (tb > ta)
+        launch_encode<T>(d_okeys.as<T>(), d_ocounts.as<uint32_t>(), d_tds.as<TileDesc>() + ta,
+                         d_tout.as<TileOut<T>>() + ta, d_boff.as<unsigned long long>() + ta, d_prev.as<T>() + ta,
+                         d_meta.as<BucketMeta>(), tb - ta, d_out.as<uint8_t>() + total_out, gbytes, est, s);
+      MCU(cudaEventRecord(ge[7 * g + 4], s));
+      MCU(cudaStreamWaitEvent(cl.cs, ge[7 * g + 4], 0));
+      MCU(cudaEventRecord(ge[7 * g + 5], cl.cs));
+      if (gbytes)
+        MCU(cudaMemcpyAsync(hout + total_out, d_out.as<uint8_t>() + total_out, gbytes, cudaMemcpyDeviceToHost, cl.cs));
+      MCU(cudaEventRecord(ge[7 * g + 6], cl.cs));
+      total_out += gbytes;
+    }
+    MCU(cudaEventRecord(sev[3], s));
+    std::vector<unsigned long long> overs(NG);
+    DevStatus hst{}, hest{};
+    MCU(cudaMemcpyAsync(&hst, dst, sizeof hst, cudaMemcpyDeviceToHost, s));
+    MCU(cudaMemcpyAsync(&hest, est, sizeof hest, cudaMemcpyDeviceToHost, s));
+    MCU(cudaMemcpyAsync(overs.data(), d_over.p, (size_t)NG * 8, cudaMemcpyDeviceToHost, s));
+    if (bounded_sync(s, timeout_ms) || bounded_sync(cl.cs, timeout_ms)) return fail(KITE_ERR_TIMEOUT, "merge wait");
+    cudaFreeAsync(dst, s);
+    cudaFreeAsync(est, s);
+    if (hst.code) {
+      char b[160];
+      snprintf(b, sizeof b, "merge: device status %u (%u, %u, %u)", hst.code, hst.a, hst.b, hst.c);
+      return fail(hst.code == KITE_DEV_BAD_INPUT ? KITE_ERR_BAD_INPUT : KITE_ERR_DEVICE, b);
+    }
+    for (uint32_t g = 0; g < NG; ++g) {
+      if (overs[g] == ~0ull) continue;
+      // first overflowing row in (partition, key) order: name its key like the reference
+      const uint32_t t = tile_first[pb[g]] + (uint32_t)(overs[g] >> 32), r = (uint32_t)(overs[g] & 0xffffffffu);
+      T key{};
+      MCU(cudaMemcpy(&key, d_okeys.as<T>() + mts[t].out_off + r, sizeof(T), cudaMemcpyDeviceToHost));
+      unsigned __int128 v = (unsigned __int128)key;
+      std::string ks;
+      if (v == 0) ks = "0";
+      while (v) {
+        ks.insert(ks.begin(), (char)('0' + (int)(v % 10)));
+        v /= 10;
+      }
+      return fail(KITE_ERR_COUNT_OVERFLOW, "merged count exceeds u32 for key " + ks);
+    }
+    if (hest.code) return fail(KITE_ERR_DEVICE, "merge encode failed");
+    // stage times: decode, planning and the input copy as the other modes;
+    // merge, link + offsets + encode, and the copy-out summed over the groups
+    {
+      static const int pairs[2][2] = {{0, 1}, {1, 2}};
+      float ms = 0;
+      for (int i = 0; i < 2; ++i)
+        if (cudaEventElapsedTime(&ms, sev[pairs[i][0]], sev[pairs[i][1]]) == cudaSuccess) stat->stage_ms[i] = ms;
+      float dec = 0;
+      for (int i = 0; i < n; ++i)
+        if (cudaEventElapsedTime(&ms, cl.tev[2 + 2 * i], cl.tev[3 + 2 * i]) == cudaSuccess) dec += ms;
+      stat->stage_ms[0] = dec;
+      if (cudaEventElapsedTime(&ms, cl.tev[0], cl.tev[1]) == cudaSuccess) stat->stage_ms[5] = ms;
+      double mg = 0, en = 0, cp = 0;
+      for (uint32_t g = 0; g < NG; ++g) {
+        if (cudaEventElapsedTime(&ms, ge[7 * g], ge[7 * g + 1]) == cudaSuccess) mg += ms;
+        if (cudaEventElapsedTime(&ms, ge[7 * g + 1], ge[7 * g + 2]) == cudaSuccess) en += ms;
+        if (cudaEventElapsedTime(&ms, ge[7 * g + 3], ge[7 * g + 4]) == cudaSuccess) en += ms;
+        if (cudaEventElapsedTime(&ms, ge[7 * g + 5], ge[7 * g + 6]) == cudaSuccess) cp += ms;
+      }
+      stat->stage_ms[2] = mg;
+      stat->stage_ms[3] = en;
+      stat->stage_ms[4] = cp;
+    }
+    stat->d2h_bytes += total_out;
+    stat->rows = out_rows;
+    stat->payload_bytes = total_out;
+    stat->tiles = ntiles;
+    stat->kernel_launches = launches;
+    uint64_t tmax = 0, tsum = 0, tne = 0;
+    for (auto& m : mts)
+      if (m.rows_in) {
+        tmax = std::max<uint64_t>(tmax, m.rows_in);
+        tsum += m.rows_in;
+        tne++;
+      }
+    stat->tile_imbalance = tne ? (double)tmax / ((double)tsum / tne) : 0.0;
+    if (!emit) return KITE_OK;
+    for (uint32_t g = 0; g < NG; ++g)
+      for (uint32_t p = pb[g]; p < pb[g + 1]; ++p) {
+        const BucketMeta& m = hm[p];
+        if (!m.rows) continue;
+        kite_chunk_meta cm{};
+        cm.partition_id = p;
+        cm.codec = KITE_CODEC_DVLE;
+        cm.row_count = m.rows;
+        cm.raw_bytes = m.bytes;
+        cm.key_min_lo[0] = m.kmin_lo;
+        cm.key_min_lo[1] = m.kmin_hi;
+        cm.key_max_lo[0] = m.kmax_lo;
+        cm.key_max_lo[1] = m.kmax_hi;
+        if (emit(user, &cm, hout + gbase[g] + m.byte_off, (size_t)m.bytes))
+          return fail(KITE_ERR_CALLBACK, "emit callback aborted");
+      }
+    return KITE_OK;
   }
   MCU(cudaEventRecord(sev[2], s));
   if (ntiles) {
