@@ -515,19 +515,21 @@ def run_merge_bench(args, world, rank, local):
         c.merge(kis, callback=cb, bases=bases)
     torch.cuda.synchronize()
     barrier(world)
-    stage = [0.0] * 6
+    stage = [0.0] * 10
     t0 = time.perf_counter()
     for _ in range(args.steps):
         out_stats["rows"] = out_stats["bytes"] = 0
         c.merge(kis, callback=cb, bases=bases)
-        stage = [x + y for x, y in zip(stage, c.stats()["stage_ms"][:6])]
+        stage = [x + y for x, y in zip(stage, c.stats()["stage_ms"][:10])]
     c.synchronize()
     barrier(world)
     dt = max_over_ranks(world, (time.perf_counter() - t0) / args.steps)
     mst = c.stats()
     c.close()
     stage = [x / args.steps for x in stage]
-    names = ["decode", "tile planning", "merge", "encode", "copy to host", "copy in (overlapped by the decode)"]
+    names = ["decode", "tile planning", "merge", "encode", "copy to host", "copy in (overlapped by the decode)",
+             "planning: splitters (host wall)", "planning: first cut (host wall)", "planning: bisection (host wall)",
+             "planning: tile lists (host wall)"]
     # algorithmic bytes per device stage: decode reads the payloads and
     # writes (key, u64 count) rows; the merge reads those and writes (key,
     # u32 count) rows; the encode reads those and writes the output payloads
@@ -563,7 +565,7 @@ def run_merge_bench(args, world, rank, local):
                 "device": {"value": rows_in / (dev_ms / 1e3), "unit": "rows/s", "ms_per_step": dev_ms,
                            "note": "the device stages only (decode, tile planning, merge, encode); the whole "
                                    "call adds the copies of the inputs in and the output out"},
-                "stage_ms": {names[i]: round(stage[i], 3) for i in range(6)},
+                "stage_ms": {names[i]: round(stage[i], 3) for i in range(10)},
                 "splitter_used": "learned" if mst["splitter_used"] == gpu.SPLIT_LEARNED else "sampled",
                 "roofline": {"bound": "hbm", "kernel": names[dom],
                              "achieved": sbytes[dom] / (stage[dom] / 1e3) / 1e9, "peak": peak, "unit": "GB/s",

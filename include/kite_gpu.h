@@ -197,7 +197,8 @@ int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n,
  * key_max = its first and last key} and the TSV bytes (valid during the
  * call).  stats.stage_ms[0..5]: decode kernels, tile planning, merge,
  * formatting, copy to the host, copy of the input in (which the decode
- * overlaps). */
+ * overlaps); [6..9] the host wall time of the planning's phases (splitters,
+ * first cut, bisection, tile lists). */
 int kite_gpu_dump(kite_gpu_ctx* ctx, const kite_gpu_merge_input* input, kite_gpu_emit_fn emit, void* user);
 
 /* Called once per count value with the number of keys that have it. */

@@ -34,6 +34,7 @@
 //                           first as ACGT, "<kmer>\t<count>\n"
 // with a formatting pass in place of the DVLE encode.
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -1106,6 +1107,13 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   DevStatus hdec{};
   MCU(cudaMemcpyAsync(&hdec, dst, sizeof hdec, cudaMemcpyDeviceToHost, s));
   MCU(cudaEventRecord(sev[1], s));
+  // planning phases, host wall clock (the decode's kernels run meanwhile until
+  // the first wait): [6] splitters, [7] first cut, [8] bisection, [9] tile lists
+  auto wall = []() { return std::chrono::steady_clock::now(); };
+  auto ms_since = [](std::chrono::steady_clock::time_point a) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+  };
+  auto tp0 = wall();
   // ---- tiles: global splitters from a row sample, refined by bisection ----
   std::vector<uint32_t> part_first_stream(P + 1, 0);
   {
@@ -1165,6 +1173,8 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   } else {
     S = 1;
   }
+  stat->stage_ms[6] = ms_since(tp0);
+  auto tp1 = wall();
   // ---- first cut on the device: the row position of every splitter in every
   // stream (one binary search each), read back as one matrix
   const size_t SP = (size_t)S + 1;
@@ -1239,6 +1249,8 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
       }
     }
   });
+  stat->stage_ms[7] = ms_since(tp1);
+  auto tp2 = wall();
   std::vector<Done> done;  // ranges finished by the bisection (offsets into dlo / dhi)
   std::vector<uint64_t> dlo, dhi;
   std::vector<Range> work;
@@ -1311,6 +1323,8 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     work.swap(next);
   }
   if (!work.empty()) return fail(KITE_ERR_UNSUPPORTED, "merge tile refinement did not converge");
+  stat->stage_ms[8] = ms_since(tp2);
+  auto tp3 = wall();
   // ---- tile lists: per partition (in parallel) its finished ranges in key
   // order, then the partitions concatenated with their offsets ----
   std::vector<std::vector<Done>> refined(P);
@@ -1382,6 +1396,7 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     }
     tile_first[P] = (uint32_t)mts.size();
   }
+  stat->stage_ms[9] = ms_since(tp3);
   const uint32_t ntiles = (uint32_t)mts.size();
   std::vector<InputFilter> filt(n);
   for (int i = 0; i < n; ++i)
