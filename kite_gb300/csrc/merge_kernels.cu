@@ -373,26 +373,44 @@ __global__ void __launch_bounds__(32 * kDecWarps)
       if (lane >= (uint32_t)o) incl += y;
     }
     const unsigned long long vl = v0 + incl - c;  // index of the lane's first owned varint
-    // the lane's key deltas, then the key before each lane's first (warp scan)
+    // the lane's key deltas (kept: a lane owns at most 16 varints, so at most
+    // 8 deltas, the j-th owned varint's delta in slot j / 2 whichever parity
+    // the lane starts on), then the key before each lane's first (warp scan)
     T dsum = 0;
+    T dv[8];
     {
+      uint32_t m = own;
       unsigned long long v = vl;
-      for (uint32_t m = own; m; m &= m - 1, ++v)
-        if ((v & 1ull) == 0 && v < nvar) dsum += varint_at<T>(win, bound, 16 * lane, 32 + __ffs(m) - 1);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        if (m) {
+          const int t = __ffs(m) - 1;
+          m &= m - 1;
+          if ((v & 1ull) == 0 && v < nvar) {
+            dv[j >> 1] = varint_at<T>(win, bound, 16 * lane, 32 + t);
+            dsum += dv[j >> 1];
+          }
+          ++v;
+        }
+      }
     }
     const T dincl = warp_incl_sum(dsum);
     T k = key + (dincl - dsum);
     {
+      uint32_t m = own;
       unsigned long long v = vl;
-      for (uint32_t m = own; m; m &= m - 1, ++v) {
-        if (v >= nvar) break;  // bytes after the last row are ignored, as the reference decodes row_count rows
-        const T val = varint_at<T>(win, bound, 16 * lane, 32 + __ffs(m) - 1);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        if (m == 0 || v >= nvar) break;  // bytes after the last row are ignored, as the reference decodes row_count rows
+        const int t = __ffs(m) - 1;
+        m &= m - 1;
         if ((v & 1ull) == 0) {
-          k += val;
+          k += dv[j >> 1];
           keys[sd.row_off + v / 2 + 1] = k;
         } else {
-          counts[sd.row_off + (v - 1) / 2 + 1] = (unsigned long long)(uint64_t)val;
+          counts[sd.row_off + (v - 1) / 2 + 1] = (unsigned long long)(uint64_t)varint_at<T>(win, bound, 16 * lane, 32 + t);
         }
+        ++v;
       }
     }
     key += warp_bcast_t(dincl, 31);
@@ -674,23 +692,32 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
   }
   if (threadIdx.x == 0) head[G] = (uint16_t)n;
   __syncthreads();
-  // per group: per-input sums (u64 saturating), input filter, total.
-  // Outputs are compacted in group order; groups are handled in rounds of NT.
-  unsigned long long out_base = 0;
-  T prev_last = T(0);
-  bool have_prev = false;
+  // per group: per-input sums (u64 saturating), input filter, total.  Each
+  // thread takes a run of consecutive groups (at most PER: G <= n <= the
+  // capacity), keeping their totals in registers; one block scan compacts
+  // the present ones in group order, and their keys go to shared memory for
+  // the DVLE sizes: over the row counts (read by then) for u64 keys, over the
+  // row keys for u128 (whose group keys are then kept in registers).
+  constexpr bool KEEP_KEYS = sizeof(T) > 8;
   unsigned long long rest = 0;
   T first_key = T(0), last_key = T(0);
   uint32_t first_count = 0;
   unsigned* scan_b = scan32 + 40;
-  for (uint32_t g0 = 0; g0 < G; g0 += NT) {
-    const uint32_t gi = g0 + threadIdx.x;
-    bool present = false;
-    unsigned long long total = 0;
-    T key = T(0);
-    if (gi < G) {
+  const uint32_t gpt = (G + NT - 1) / NT;
+  const uint32_t g_lo = min(G, threadIdx.x * gpt), g_hi = min(G, g_lo + gpt);
+  T gkey[PER];
+  unsigned long long gtot[PER];
+  uint32_t pmask = 0, npres = 0;
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    gkey[i] = T(0);
+    gtot[i] = 0;
+    const uint32_t gi = g_lo + i;
+    if (gi < g_hi) {
       const uint32_t a = head[gi], b = head[gi + 1];
-      key = sk[perm[a]];
+      if (KEEP_KEYS) gkey[i] = sk[perm[a]];
+      bool present = false;
+      unsigned long long total = 0;
       uint32_t cur_in = 0xffffffffu;
       unsigned long long part = 0;
       for (uint32_t q = a; q <= b; ++q) {
@@ -714,11 +741,28 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
           part = (part > ~0ull - c) ? ~0ull : part + c;
         }
       }
+      gtot[i] = total;
+      if (present) {
+        pmask |= 1u << i;
+        ++npres;
+      }
     }
-    unsigned tot;
-    const unsigned idx = block_exclusive_scan<NT, unsigned>(present ? 1u : 0u, scan_b, &tot);
-    if (present) {
-      const unsigned long long o = out_base + idx;
+  }
+  __syncthreads();  // every row count (and for u128 every row key) has been read
+  unsigned tot;
+  const unsigned base = block_exclusive_scan<NT, unsigned>(npres, scan_b, &tot);
+  T* outk = KEEP_KEYS ? sk : reinterpret_cast<T*>(sc);  // the present groups' keys in output order
+  if (!KEEP_KEYS) {
+#pragma unroll
+    for (int i = 0; i < PER; ++i)
+      if ((pmask >> i) & 1u) gkey[i] = sk[perm[head[g_lo + i]]];
+  }
+  {
+    unsigned o = base;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      if (!((pmask >> i) & 1u)) continue;
+      const unsigned long long total = gtot[i];
       if (MODE == kModeHisto) {
         if (total < kHistBins) {
           atomicAdd(&hbin[total], 1u);
@@ -728,42 +772,36 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_tiles(
         }
       } else {
         if (MODE == kModeMerge && total > 0xffffffffull)
-          atomicMin(overflow, ((unsigned long long)blockIdx.x << 32) | (o & 0xffffffffull));
+          atomicMin(overflow, ((unsigned long long)blockIdx.x << 32) | (unsigned long long)o);
         const uint32_t c32 = total > 0xffffffffull ? 0xffffffffu : (uint32_t)total;
-        out_keys[mt.out_off + o] = key;
+        out_keys[mt.out_off + o] = gkey[i];
         out_counts[mt.out_off + o] = c32;
         if (MODE == kModeRows) aux.counts64[mt.out_off + o] = total;
+        if (o == 0) misc[60] = c32;
       }
+      outk[o] = gkey[i];
+      ++o;
     }
-    __syncthreads();
-    // DVLE sizes of the rows after the tile's first (the previous row may come
-    // from the previous round; both are already in global memory and visible
-    // to the whole CTA after the barrier).
-    if (MODE == kModeMerge || MODE == kModeDump)
-    for (unsigned u = threadIdx.x; u < tot; u += NT) {
-      const unsigned long long o = out_base + u;
-      const T kk = out_keys[mt.out_off + o];
-      const uint32_t cc = out_counts[mt.out_off + o];
-      if (DUMP) {
-        rest += aux.line_k + 2 + dec_digits(cc);
-      } else if (o > 0) {
-        const T pk = out_keys[mt.out_off + o - 1];
-        rest += (unsigned long long)(varint_len((T)(kk - pk)) + varint_len((uint64_t)cc));
-      }
-    }
-    __syncthreads();
-    if (MODE != kModeHisto && threadIdx.x == 0 && tot) {
-      if (!have_prev) {
-        first_key = out_keys[mt.out_off + out_base];
-        first_count = out_counts[mt.out_off + out_base];
-      }
-      last_key = out_keys[mt.out_off + out_base + tot - 1];
-      have_prev = true;
-    }
-    out_base += tot;
-    __syncthreads();
   }
-  (void)prev_last;
+  __syncthreads();
+  if (MODE == kModeMerge || MODE == kModeDump) {
+    // DVLE sizes of the rows after the tile's first (TSV line sizes for dump)
+    unsigned o = base;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      if (!((pmask >> i) & 1u)) continue;
+      const uint32_t cc = gtot[i] > 0xffffffffull ? 0xffffffffu : (uint32_t)gtot[i];
+      if (DUMP) rest += aux.line_k + 2 + dec_digits(cc);
+      else if (o > 0) rest += (unsigned long long)(varint_len((T)(gkey[i] - outk[o - 1])) + varint_len((uint64_t)cc));
+      ++o;
+    }
+  }
+  if (MODE != kModeHisto && threadIdx.x == 0 && tot) {
+    first_key = outk[0];
+    first_count = (uint32_t)misc[60];
+    last_key = outk[tot - 1];
+  }
+  const unsigned long long out_base = tot;
   if (MODE == kModeHisto) {
     // the CTA's small-count bins into the global histogram
     for (uint32_t b = threadIdx.x; b < kHistBins; b += NT)
