@@ -183,7 +183,10 @@ int kite_gpu_result_partition(kite_gpu_ctx* ctx, uint32_t partition, kite_chunk_
 /* K-way merge of n inputs (same k, canonical, partitions and key width):
  * per-input header filter before summing, u64 sums, u32 overflow is an error
  * (KITE_ERR_COUNT_OVERFLOW, message names the key), one DVLE chunk per
- * non-empty partition, emitted in partition order. */
+ * non-empty partition, emitted in partition order (after every partition has
+ * been merged, so an overflow emits nothing).  The context keeps the device
+ * buffers of merge, dump, histo and query between calls (grown when a call
+ * needs more, released by kite_gpu_close). */
 int kite_gpu_merge(kite_gpu_ctx* ctx, const kite_gpu_merge_input* inputs, int n, kite_gpu_emit_fn emit,
                    void* user);
 
