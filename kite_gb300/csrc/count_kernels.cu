@@ -904,6 +904,171 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
   }
 }
 
+// The same scatter when the histogram pass has left every key's digit: each
+// digit's run leaves shared memory by one 1-D bulk copy (cp.async.bulk,
+// shared -> global) issued by the digit's owner thread, instead of one store
+// per key, and the stage holds keys only.  A bulk copy starts and ends on
+// 16-byte boundaries at both addresses: runs end on sector boundaries (as
+// above), a run of 8-byte keys starting at an odd key index sends its first
+// key by a plain store, and the stage places every run on the parity of its
+// global position (one pad slot per digit).  The owner waits for its copies
+// to have read the stage before the next batch overwrites it.
+template <class T, int NT_, int IT_, int RADIX_>
+struct BulkScatterSmem {
+  static constexpr int NT = NT_, IT = IT_, RADIX = RADIX_;
+  static constexpr int BATCH = NT * IT;
+  static constexpr int KPS = 32 / (int)sizeof(T);  // keys per sector
+  static constexpr int PAD = sizeof(T) == 8 ? 1 : 0;
+  static constexpr int STAGE = BATCH + RADIX * (KPS - 1) + RADIX * PAD;
+  static constexpr size_t o_stage = 0;
+  static constexpr size_t o_whist = ((size_t)STAGE * sizeof(T) + 15) & ~(size_t)15;
+  static constexpr size_t o_cur = o_whist + (size_t)RADIX * 4;
+  static constexpr size_t o_dtot = o_cur + (size_t)RADIX * 8;
+  static constexpr size_t o_dstart = o_dtot + (size_t)RADIX * 4;
+  static constexpr size_t o_wr = o_dstart + (size_t)RADIX * 4;
+  static constexpr size_t o_held = o_wr + (size_t)RADIX * 2;
+  static constexpr size_t o_scan = (o_held + (size_t)RADIX + 15) & ~(size_t)15;
+  static constexpr size_t total = o_scan + 64 * 4;
+  static_assert(STAGE < 65536, "write counts are 16-bit");
+};
+
+__device__ __forceinline__ void bulk_store_global(void* gdst, const void* ssrc, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst),
+               "r"((uint32_t)__cvta_generic_to_shared(ssrc)), "r"(bytes)
+               : "memory");
+}
+
+template <class T, int NT, int IT, int RADIX>
+__global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT)
+    k_split_scatter_bulk(TileSplitParams<T> p) {
+  using L = BulkScatterSmem<T, NT, IT, RADIX>;
+  constexpr int BATCH = L::BATCH, KPS = L::KPS;
+  constexpr int PER = RADIX > NT ? RADIX / NT : 1;
+  static_assert(RADIX <= NT || RADIX % NT == 0, "digits split evenly over the threads");
+  extern __shared__ __align__(16) uint8_t sm[];
+  T* stage = reinterpret_cast<T*>(sm + L::o_stage);
+  unsigned* whist = reinterpret_cast<unsigned*>(sm + L::o_whist);
+  unsigned long long* cur = reinterpret_cast<unsigned long long*>(sm + L::o_cur);
+  unsigned* dtot = reinterpret_cast<unsigned*>(sm + L::o_dtot);
+  unsigned* dstart = reinterpret_cast<unsigned*>(sm + L::o_dstart);
+  uint16_t* wr = reinterpret_cast<uint16_t*>(sm + L::o_wr);
+  uint8_t* held = sm + L::o_held;
+  unsigned* scan_sm = reinterpret_cast<unsigned*>(sm + L::o_scan);
+  const uint32_t D = p.D, G = p.G;
+  const uint32_t r = blockIdx.x / G, g = blockIdx.x % G;
+  for (uint32_t d = threadIdx.x; d < (uint32_t)RADIX; d += NT) {
+    cur[d] = d < D ? p.tile_off[((size_t)r * D + d) * G + g] : 0ull;
+    whist[d] = 0;  // rank counters
+    dtot[d] = 0;
+    dstart[d] = 0;
+    wr[d] = 0;
+  }
+  __syncthreads();
+  uint64_t a, e;
+  part_range(p.region_off, p.region_count, r, g, G, &a, &e);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned pos0 = (unsigned)wid * 32u * IT + lane;
+  const unsigned d0 = threadIdx.x * PER;
+  T* out = p.keys_out;
+  for (uint64_t c0 = a; c0 < e; c0 += BATCH) {
+    const unsigned cn = (unsigned)((e - c0) < (uint64_t)BATCH ? (e - c0) : (uint64_t)BATCH);
+    T key[IT];
+    unsigned dg[IT], rank[IT];
+    bool valid[IT];
+#pragma unroll
+    for (int q = 0; q < IT; ++q) {
+      const unsigned pos = pos0 + q * 32u;
+      valid[q] = pos < cn;
+      key[q] = valid[q] ? p.keys_in[c0 + pos] : T(0);
+      dg[q] = valid[q] ? (unsigned)p.dig[c0 + pos] : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < IT; ++q) rank[q] = valid[q] ? atomicAdd(&whist[dg[q]], 1u) : 0u;
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the last batch's copies have read the stage
+    __syncthreads();
+    // owned digits: the held-back keys (to registers), the new totals and
+    // stage starts, and how many keys reach a sector boundary
+    T hk[PER][KPS - 1];
+    unsigned nh[PER], nt[PER], sum = 0;
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const unsigned d = d0 + j;
+      nh[j] = nt[j] = 0;
+      if (d < (unsigned)RADIX) {
+        const unsigned w = wr[d];
+        nh[j] = dtot[d] - w;
+        const unsigned hs = dstart[d] + w;
+#pragma unroll
+        for (int k = 0; k < KPS - 1; ++k)
+          if ((unsigned)k < nh[j]) hk[j][k] = stage[hs + k];
+        cur[d] += w;
+        nt[j] = nh[j] + whist[d];
+        whist[d] = 0;
+      }
+      sum += nt[j] + L::PAD;
+    }
+    unsigned total;
+    unsigned ex = block_exclusive_scan<NT, unsigned>(sum, scan_sm, &total);
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const unsigned d = d0 + j;
+      if (d < (unsigned)RADIX) {
+        const unsigned long long cb = cur[d];
+        dstart[d] = L::PAD ? ex + (unsigned)((ex ^ (unsigned)cb) & 1u) : ex;
+        dtot[d] = nt[j];
+        held[d] = (uint8_t)nh[j];
+        const unsigned long long B = (cb + nt[j]) & ~(unsigned long long)(KPS - 1);
+        wr[d] = (uint16_t)(B > cb ? B - cb : 0ull);
+        ex += nt[j] + L::PAD;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const unsigned d = d0 + j;
+#pragma unroll
+      for (int k = 0; k < KPS - 1; ++k)
+        if ((unsigned)k < nh[j]) stage[dstart[d] + k] = hk[j][k];
+    }
+#pragma unroll
+    for (int q = 0; q < IT; ++q)
+      if (valid[q]) stage[dstart[dg[q]] + held[dg[q]] + rank[q]] = key[q];
+    __syncthreads();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the stage writes, before the copies read it
+    bool issued = false;
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const unsigned d = d0 + j;
+      if (d >= (unsigned)RADIX) continue;
+      unsigned w = wr[d];
+      if (!w) continue;
+      unsigned long long cb = cur[d];
+      unsigned s0 = dstart[d];
+      if (L::PAD && (cb & 1ull)) {
+        out[cb] = stage[s0];
+        ++cb;
+        ++s0;
+        --w;
+      }
+      if (w) {
+        bulk_store_global(out + cb, stage + s0, w * (uint32_t)sizeof(T));
+        issued = true;
+      }
+    }
+    if (issued) asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  }
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+  __syncthreads();
+  // the part's last keys of every digit (a partial sector)
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const unsigned d = d0 + j;
+    if (d < (unsigned)RADIX)
+      for (unsigned k = wr[d]; k < dtot[d]; ++k) out[cur[d] + k] = stage[dstart[d] + k];
+  }
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // every copy done before the CTA's memory goes
+}
+
 // Bucket scatter of staged keys, one CTA per extraction block: batches of
 // BATCH keys ranked on chip by partition (shared-memory atomics; order inside a
 // partition does not matter), staged in partition order and written as runs at
@@ -1084,6 +1249,13 @@ template <class T>
 void launch_split_scatter(const TileSplitParams<T>& p, int shape, cudaStream_t s) {
   with_scatter_cfg<T>(p.D, shape, [&](auto cfg) {
     using C = decltype(cfg);
+    if (p.dig) {
+      auto kern = k_split_scatter_bulk<T, C::NT, C::IT, C::RADIX>;
+      const size_t smem = BulkScatterSmem<T, C::NT, C::IT, C::RADIX>::total;
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (p.R * p.G) kern<<<p.R * p.G, C::NT, smem, s>>>(p);
+      return;
+    }
     auto kern = k_split_scatter<T, C::NT, C::IT, C::RADIX>;
     const size_t smem = ScatterSmem<T, C::NT, C::IT, C::RADIX>::total;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
