@@ -379,6 +379,16 @@ __global__ void __launch_bounds__(kExtractThreads, 6) k_extract64(ExtractParams<
       const unsigned long long o0 = __shfl_sync(0xffffffffu, ob, 0);
       if (__shfl_sync(0xffffffffu, out ? 1u : 0u, 0)) wbase = p.keys_stage + o0;
     }
+    // A lane's windows are fixed shifts of the (previous, current) word pair:
+    // the forward k-mer is the low 64 bits of (pw.code:cw.code) >> sft and the
+    // reverse complement the low 64 bits of (cw.rcode:pw.rcode) >> t, both
+    // per-lane constants.  Each is two 32-bit funnel shifts of the 32-bit
+    // words that the shift's word offset selects (chosen once per lane).
+    const uint32_t sft = 2 * (31 - lane);     // 0 .. 62: word offset 0 or 1
+    const bool f_hi = sft >= 32;
+    const uint32_t fsh = sft & 31u;
+    const uint32_t tr = 2 * (33 + lane - k);  // 4 .. 126: word offset 0 .. 3
+    const uint32_t tq = tr >> 5, tsh = tr & 31u;
     unsigned run = 0;
     for (unsigned ls = __ballot_sync(0xffffffffu, (V0 | V1) != 0u); ls; ls &= ls - 1) {
       const int l = __ffs(ls) - 1;
@@ -391,13 +401,20 @@ __global__ void __launch_bounds__(kExtractThreads, 6) k_extract64(ExtractParams<
         uint64_t key = 0;
         if (act) {
           const CodeWords pw = ws[3 * l + h], cw = ws[3 * l + h + 1];
-          const uint32_t sft = 2 * (31 - lane);
-          const uint64_t fwd = (sft ? ((cw.code >> sft) | (pw.code << (64 - sft))) : cw.code) & mask;
+          const uint32_t c0 = (uint32_t)cw.code, c1 = (uint32_t)(cw.code >> 32);
+          const uint32_t p0 = (uint32_t)pw.code, p1 = (uint32_t)(pw.code >> 32);
+          const uint32_t a0 = f_hi ? c1 : c0, a1 = f_hi ? p0 : c1, a2 = f_hi ? p1 : p0;
+          const uint64_t fwd =
+              (((uint64_t)__funnelshift_r(a1, a2, fsh) << 32) | __funnelshift_r(a0, a1, fsh)) & mask;
           key = fwd;
           if (canon) {
-            const uint32_t t = 2 * (33 + lane - k);  // 4 .. 126
+            const uint32_t r0 = (uint32_t)pw.rcode, r1 = (uint32_t)(pw.rcode >> 32);
+            const uint32_t r2 = (uint32_t)cw.rcode, r3 = (uint32_t)(cw.rcode >> 32);
+            const uint32_t b0 = tq == 0 ? r0 : tq == 1 ? r1 : tq == 2 ? r2 : r3;
+            const uint32_t b1 = tq == 0 ? r1 : tq == 1 ? r2 : tq == 2 ? r3 : 0u;
+            const uint32_t b2 = tq == 0 ? r2 : tq == 1 ? r3 : 0u;
             const uint64_t rc =
-                (t < 64 ? ((pw.rcode >> t) | (cw.rcode << (64 - t))) : (cw.rcode >> (t - 64))) & mask;
+                (((uint64_t)__funnelshift_r(b1, b2, tsh) << 32) | __funnelshift_r(b0, b1, tsh)) & mask;
             key = rc < fwd ? rc : fwd;
           }
           atomicAdd(&hist[bucket_of(key, shift)], 1u);
