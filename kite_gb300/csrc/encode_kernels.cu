@@ -151,20 +151,25 @@ __device__ __forceinline__ int put_varint(uint8_t* o, T v) {
   }
 }
 
-// One CTA per tile, 256 rows at a time: per-row sizes, block scan, the rows'
+// One CTA per tile, 1024 rows at a time, each thread four consecutive rows
+// (the previous row's key from the thread's own registers for all but its
+// first): per-row sizes, one block scan per round, each thread's rows'
 // bytes assembled in shared memory, then written out with consecutive
-// threads on consecutive bytes (whole sectors, not one scattered byte store
-// per row byte).
+// threads on consecutive aligned 4-byte words (whole sectors, not one
+// scattered byte store per row byte).
+constexpr int kEncThreads = 256, kEncRows = 4, kEncRound = kEncThreads * kEncRows;
 template <class T>
-__global__ void __launch_bounds__(256) k_encode(const T* __restrict__ keys, const uint32_t* __restrict__ counts,
-                                                const TileDesc* __restrict__ tiles, const TileOut<T>* __restrict__ tout,
-                                                const unsigned long long* __restrict__ tile_boff,
-                                                const T* __restrict__ tile_prev, const BucketMeta* __restrict__ meta,
-                                                uint8_t* __restrict__ out, unsigned long long out_cap, DevStatus* st) {
+__global__ void __launch_bounds__(kEncThreads) k_encode(const T* __restrict__ keys, const uint32_t* __restrict__ counts,
+                                                        const TileDesc* __restrict__ tiles,
+                                                        const TileOut<T>* __restrict__ tout,
+                                                        const unsigned long long* __restrict__ tile_boff,
+                                                        const T* __restrict__ tile_prev,
+                                                        const BucketMeta* __restrict__ meta, uint8_t* __restrict__ out,
+                                                        unsigned long long out_cap, DevStatus* st) {
   // largest row: LEB128 of a key delta plus LEB128 of a u32 count, or the raw first row
   constexpr int kRowMax = (KeyTraits<T>::kBits + 6) / 7 + 5;
   __shared__ unsigned long long sm[34];
-  __shared__ uint8_t chunk[256 * kRowMax];
+  __shared__ uint8_t chunk[kEncRound * kRowMax];
   const uint32_t t = blockIdx.x;
   const TileOut<T> o = tout[t];
   if (o.rows == 0) return;
@@ -176,32 +181,46 @@ __global__ void __launch_bounds__(256) k_encode(const T* __restrict__ keys, cons
   const uint32_t* c = counts + td.start;
   unsigned long long run = 0;
   unsigned* scan32 = reinterpret_cast<unsigned*>(sm);
-  for (uint32_t r0 = 0; r0 < o.rows; r0 += 256) {
-    const uint32_t r = r0 + threadIdx.x;
-    int sz = 0;
-    T key = T(0), delta = T(0);
-    uint32_t cnt = 0;
-    if (r < o.rows) {
-      key = k[r];
-      cnt = c[r];
-      if (r == 0 && first_in_bucket) {
-        sz = KeyTraits<T>::kEntry;
-      } else {
-        const T p = r == 0 ? tprev : k[r - 1];
-        delta = key - p;
-        sz = varint_len(delta) + varint_len((uint64_t)cnt);
+  for (uint32_t r0 = 0; r0 < o.rows; r0 += kEncRound) {
+    const uint32_t rb = r0 + threadIdx.x * kEncRows;  // the thread's first row
+    T key[kEncRows];
+    uint32_t cnt[kEncRows];
+    int sz[kEncRows];
+    unsigned mine = 0;
+    T p = rb < o.rows ? (rb == 0 ? tprev : k[rb - 1]) : T(0);
+#pragma unroll
+    for (int i = 0; i < kEncRows; ++i) {
+      const uint32_t r = rb + i;
+      key[i] = T(0);
+      cnt[i] = 0;
+      sz[i] = 0;
+      if (r < o.rows) {
+        key[i] = k[r];
+        cnt[i] = c[r];
+        sz[i] = (r == 0 && first_in_bucket) ? KeyTraits<T>::kEntry
+                                            : varint_len((T)(key[i] - p)) + varint_len((uint64_t)cnt[i]);
+        p = key[i];
       }
+      mine += (unsigned)sz[i];
     }
     unsigned tot;
-    const unsigned ex = block_exclusive_scan<256, unsigned>((unsigned)sz, scan32, &tot);
-    if (r < o.rows) {
-      uint8_t* q = chunk + ex;
-      if (r == 0 && first_in_bucket) {
-        for (int i = 0; i < (int)sizeof(T); ++i) q[i] = (uint8_t)(key >> (8 * i));
-        for (int i = 0; i < 4; ++i) q[sizeof(T) + i] = (uint8_t)(cnt >> (8 * i));
-      } else {
-        const int n1 = put_varint<T>(q, delta);
-        put_varint<uint64_t>(q + n1, (uint64_t)cnt);
+    unsigned ex = block_exclusive_scan<kEncThreads, unsigned>(mine, scan32, &tot);
+    {
+      T q = rb < o.rows ? (rb == 0 ? tprev : k[rb - 1]) : T(0);
+      uint8_t* w = chunk + ex;
+#pragma unroll
+      for (int i = 0; i < kEncRows; ++i) {
+        const uint32_t r = rb + i;
+        if (r >= o.rows) break;
+        if (r == 0 && first_in_bucket) {
+          for (int j = 0; j < (int)sizeof(T); ++j) w[j] = (uint8_t)(key[i] >> (8 * j));
+          for (int j = 0; j < 4; ++j) w[sizeof(T) + j] = (uint8_t)(cnt[i] >> (8 * j));
+        } else {
+          const int n1 = put_varint<T>(w, (T)(key[i] - q));
+          put_varint<uint64_t>(w + n1, (uint64_t)cnt[i]);
+        }
+        w += sz[i];
+        q = key[i];
       }
     }
     __syncthreads();
@@ -214,15 +233,15 @@ __global__ void __launch_bounds__(256) k_encode(const T* __restrict__ keys, cons
       uint8_t* dst = out + at;
       const unsigned head = (unsigned)((4u - ((uintptr_t)dst & 3u)) & 3u);
       if (tot < head + 8u) {
-        for (unsigned i = threadIdx.x; i < tot; i += 256) dst[i] = chunk[i];
+        for (unsigned i = threadIdx.x; i < tot; i += kEncThreads) dst[i] = chunk[i];
       } else {
         const unsigned body = (tot - head) & ~3u, tail = tot - head - body;
         if (threadIdx.x < head) dst[threadIdx.x] = chunk[threadIdx.x];
         if (threadIdx.x < tail) dst[head + body + threadIdx.x] = chunk[head + body + threadIdx.x];
         uint32_t* dw = reinterpret_cast<uint32_t*>(dst + head);
-        for (unsigned i = threadIdx.x; i < body / 4; i += 256) {
-          const uint8_t* b = chunk + head + 4 * i;
-          dw[i] = (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+        for (unsigned i = threadIdx.x; i < body / 4; i += kEncThreads) {
+          const uint8_t* bb = chunk + head + 4 * i;
+          dw[i] = (uint32_t)bb[0] | ((uint32_t)bb[1] << 8) | ((uint32_t)bb[2] << 16) | ((uint32_t)bb[3] << 24);
         }
       }
     }
@@ -236,7 +255,8 @@ void launch_encode(const T* keys, const uint32_t* counts, const TileDesc* tiles,
                    const unsigned long long* tile_boff, const T* tile_prev, const BucketMeta* meta, uint32_t ntiles,
                    uint8_t* out, unsigned long long out_cap, DevStatus* st, cudaStream_t s) {
   if (ntiles)
-    k_encode<T><<<ntiles, 256, 0, s>>>(keys, counts, tiles, tout, tile_boff, tile_prev, meta, out, out_cap, st);
+    k_encode<T><<<ntiles, kEncThreads, 0, s>>>(keys, counts, tiles, tout, tile_boff, tile_prev, meta, out, out_cap,
+                                                st);
 }
 template void launch_encode<uint64_t>(const uint64_t*, const uint32_t*, const TileDesc*, const TileOut<uint64_t>*,
                                       const unsigned long long*, const uint64_t*, const BucketMeta*, uint32_t,
