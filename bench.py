@@ -215,41 +215,47 @@ def cpu_baseline(data, layout, reads_sample: int, threads: int, k: int = K, read
             "seconds": secs, "kmers": r["kmers"], "full": n == len(data)}
 
 
-def parity_full(count_collect, data, k: int, partitions: int) -> dict:
+def parity_full(collectors: dict, data, k: int, partitions: int) -> dict:
     """Byte comparison of the GPU's partition payloads with the oracle's
     (orc_count_parts: the single-worker count's payload of every partition,
-    made with all host threads) on the whole workload.  count_collect(cb)
-    runs one GPU count calling cb(meta, host address, length) per partition.
-    Runs outside every timed region."""
+    made with all host threads) on the whole workload.  collectors maps a
+    submission path's name to count_collect(cb), which runs one GPU count
+    calling cb(meta, host address, length) per partition.  Runs outside
+    every timed region."""
     import ctypes as C
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
     t0 = time.perf_counter()
     ref = oracle.count_parts(data, k, CANONICAL, partitions, os.cpu_count() or 1)
     t_oracle = time.perf_counter() - t0
-    seen, bad = set(), []
-
-    def cb(m, addr, n):
-        p = m["partition_id"]
-        seen.add(p)
-        same = (m["row_count"] == ref.rows[p] and n == ref.bytes[p] and m["key_min"] == ref.key_min[p]
-                and m["key_max"] == ref.key_max[p])
-        if same and n:
-            a = np.frombuffer((C.c_uint8 * n).from_address(addr), dtype=np.uint8)
-            b = np.frombuffer(ref.payload(p), dtype=np.uint8)
-            same = bool(np.array_equal(a, b))
-        if not same:
-            bad.append(p)
-
-    count_collect(cb)
     want = set(ref.nonempty())
-    ok = not bad and seen == want
-    out = {"ok": ok, "partitions_compared": len(seen), "rows": int(sum(ref.rows)), "payload_bytes": int(ref.total),
+    out = {"ok": True, "partitions_compared": 0, "rows": int(sum(ref.rows)), "payload_bytes": int(ref.total),
            "kmers": int(ref.kmers), "oracle_seconds": round(t_oracle, 2),
            "method": "GPU partition payloads (DVLE bytes, rows, key range) compared byte for byte with the "
-                     "oracle's single-worker count of the whole workload"}
-    if not ok:
-        out["mismatched_partitions"] = sorted(set(bad) | (seen ^ want))[:20]
+                     "oracle's single-worker count of the whole workload, for each submission path",
+           "paths": {}}
+    for name, count_collect in collectors.items():
+        seen, bad = set(), []
+
+        def cb(m, addr, n):
+            p = m["partition_id"]
+            seen.add(p)
+            same = (m["row_count"] == ref.rows[p] and n == ref.bytes[p] and m["key_min"] == ref.key_min[p]
+                    and m["key_max"] == ref.key_max[p])
+            if same and n:
+                a = np.frombuffer((C.c_uint8 * n).from_address(addr), dtype=np.uint8)
+                b = np.frombuffer(ref.payload(p), dtype=np.uint8)
+                same = bool(np.array_equal(a, b))
+            if not same:
+                bad.append(p)
+
+        count_collect(cb)
+        ok = not bad and seen == want
+        out["ok"] = out["ok"] and ok
+        out["partitions_compared"] = max(out["partitions_compared"], len(seen))
+        out["paths"][name] = ok
+        if not ok:
+            out.setdefault("mismatched_partitions", {})[name] = sorted(set(bad) | (seen ^ want))[:20]
     ref.close()
     return out
 
@@ -1049,7 +1055,16 @@ def main():
                                  "used": stl["splitter_used"] == gpu.SPLIT_LEARNED,
                                  "stage_ms": {stages[i][0]: round(sml[i], 3) for i in stages}}}
 
-    # ---- the whole workload's output against the oracle (untimed) ----
+    # ---- e2e counter: the C ABI from pinned host memory ----
+    pinned = torch.empty(total, dtype=torch.uint8).pin_memory()
+    pinned.copy_(host_t)
+    pbase = pinned.data_ptr()
+    d2h = [0]
+    ce = gpu.Counter(kk, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED,
+                     scatter_shape=args.scatter_shape, tile_fill=args.tile_fill)
+
+    # ---- the whole workload's output against the oracle (untimed), from
+    # device-resident chunks and from the pinned host chunks ----
     parity = None
     if rank == 0 and not args.no_parity:
         def count_collect(cb):
@@ -1057,15 +1072,17 @@ def main():
                 c.submit_device(base + d, l)
             c.finish(collect=True, callback=cb, raw=True)
             torch.cuda.synchronize()
-        parity = parity_full(count_collect, data, kk, args.partitions)
 
-    # ---- e2e through the C ABI from pinned host memory ----
-    pinned = torch.empty(total, dtype=torch.uint8).pin_memory()
-    pinned.copy_(host_t)
-    pbase = pinned.data_ptr()
-    d2h = [0]
+        def host_collect(cb):
+            for o, l in layout:
+                ce.submit((pbase + o, l))
+            ce.finish(collect=True, callback=cb, raw=True)
+            ce.synchronize()
+        parity = parity_full({"device_chunks": count_collect, "host_chunks": host_collect}, data, kk,
+                             args.partitions)
 
     e2e_parts = {"submit_s": 0.0, "finish_s": 0.0, "d2h_ms": 0.0, "stage_ms": [0.0] * 8}
+    e2e_pieces = [0]
 
     def e2e_step(cc):
         t_a = time.perf_counter()
@@ -1080,13 +1097,13 @@ def main():
             out_bytes += n
         cc.finish(collect=True, callback=cb, raw=True, meta=False)
         e2e_parts["finish_s"] += time.perf_counter() - t_b
-        sm = cc.stats()["stage_ms"]
+        est = cc.stats()
+        sm = est["stage_ms"]
+        e2e_pieces[0] = est["input_pieces"]
         e2e_parts["d2h_ms"] += sm[7]
         e2e_parts["stage_ms"] = [a + b for a, b in zip(e2e_parts["stage_ms"], sm)]
         d2h[0] = out_bytes
 
-    ce = gpu.Counter(kk, CANONICAL, args.partitions, device=local, splitter_mode=gpu.SPLIT_SAMPLED,
-                     scatter_shape=args.scatter_shape, tile_fill=args.tile_fill)
     e2e_step(ce)
     ce.synchronize()
     for key in e2e_parts:
@@ -1132,7 +1149,9 @@ def main():
                         "submit_ms": e2e_parts["submit_s"] / args.steps * 1e3,
                         "finish_ms": e2e_parts["finish_s"] / args.steps * 1e3,
                         "d2h_ms": e2e_parts["d2h_ms"] / args.steps,
-                        # device stages of the end-to-end count (the first two include waiting for the copies)
+                        "input_pieces": e2e_pieces[0],
+                        # device stages of the end-to-end count (the first two include waiting for the
+                        # copies; with input pieces the bucket scatter runs inside the histogram stage)
                         "stage_ms": {stages[i][0]: round(e2e_parts["stage_ms"][i] / args.steps, 3) for i in stages}},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "parity": parity, "e2e_cli": cli,

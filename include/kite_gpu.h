@@ -117,6 +117,8 @@ typedef struct {
   uint32_t mlp_reused;               /* 1: the learned CDF of an earlier segment was kept (no training) */
   uint64_t big_tile_keys;            /* keys in tiles above the on-chip capacity */
   uint64_t big_tile_rows;            /* unique rows those tiles reduced to */
+  uint32_t input_pieces;             /* host chunks: runs of chunks whose bucket scatter ran while later chunks
+                                        were still copying in (1 = one scatter after the last chunk) */
 } kite_gpu_stats;
 
 /* Merge input: one .kite file's partition table, with payloads in host memory

@@ -719,9 +719,19 @@ __device__ __forceinline__ uint32_t digit_of_key(const T* spl, const uint16_t* l
   return a;
 }
 
-__device__ __forceinline__ void part_range(const unsigned long long* roff, const unsigned long long* rcnt,
-                                           uint32_t r, uint32_t g, uint32_t G, uint64_t* lo, uint64_t* hi) {
-  const uint64_t n = rcnt[r], base = roff[r];
+// Keys of part g of region r: an even share of the region's run, or with
+// input pieces, of its run in piece g / (G / pieces).
+template <class T>
+__device__ __forceinline__ void part_range(const TileSplitParams<T>& p, uint32_t r, uint32_t g, uint64_t* lo,
+                                           uint64_t* hi) {
+  uint32_t G = p.G, idx = r;
+  if (p.pieces > 1) {
+    G = p.G / p.pieces;
+    const uint32_t q = g / G;
+    g -= q * G;
+    idx = q * p.R + r;
+  }
+  const uint64_t n = p.region_count[idx], base = p.region_off[idx];
   *lo = base + n * g / G;
   *hi = base + n * (g + 1) / G;
 }
@@ -739,7 +749,7 @@ __global__ void __launch_bounds__(kSplitThreads) k_split_hist(TileSplitParams<T>
   uint32_t sh;
   load_digits(p, r, spl, lut, &lo, &sh);
   uint64_t a, e;
-  part_range(p.region_off, p.region_count, r, g, G, &a, &e);
+  part_range(p, r, g, &a, &e);
   // kSplitUnroll independent loads in flight per thread before any use
   for (uint64_t i0 = a + threadIdx.x; i0 < e; i0 += (uint64_t)kSplitThreads * kSplitUnroll) {
     T key[kSplitUnroll];
@@ -824,7 +834,7 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT) k
   if (p.dig) __syncthreads();  // the histogram pass left every digit
   else load_digits(p, r, spl, lut, &lo, &sh);  // ends with a barrier
   uint64_t a, e;
-  part_range(p.region_off, p.region_count, r, g, G, &a, &e);
+  part_range(p, r, g, &a, &e);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned pos0 = (unsigned)wid * 32u * IT + lane;
   const unsigned d0 = threadIdx.x * PER;
@@ -982,7 +992,7 @@ __global__ void __launch_bounds__(NT, (IT * sizeof(T) > 64 ? 512 : 1024) / NT)
   }
   __syncthreads();
   uint64_t a, e;
-  part_range(p.region_off, p.region_count, r, g, G, &a, &e);
+  part_range(p, r, g, &a, &e);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned pos0 = (unsigned)wid * 32u * IT + lane;
   const unsigned d0 = threadIdx.x * PER;
@@ -1109,7 +1119,8 @@ __global__ void __launch_bounds__(kBsThreads, 4)
     k_bucket_scatter(const T* __restrict__ keys_stage, const unsigned long long* __restrict__ blk_keys,
                      const unsigned* __restrict__ blk_offs, const BlockDesc* __restrict__ blocks,
                      const unsigned long long* __restrict__ bucket_off, uint32_t P, uint32_t shift,
-                     T* __restrict__ keys_out) {
+                     T* __restrict__ keys_out, const unsigned long long* __restrict__ stage_counter,
+                     unsigned long long stage_cap) {
   using L = BsSmem<T>;
   constexpr int NT = kBsThreads, IT = kBsItems;
   extern __shared__ __align__(16) uint8_t sm[];
@@ -1122,7 +1133,9 @@ __global__ void __launch_bounds__(kBsThreads, 4)
   unsigned* scan_sm = reinterpret_cast<unsigned*>(sm + L::o_scan);
   const uint64_t a = blk_keys[2 * (size_t)blockIdx.x];
   const uint64_t n = blk_keys[2 * (size_t)blockIdx.x + 1];
-  if (n == 0) return;
+  // an unstaged block (a == ~0), or staging over capacity anywhere so far:
+  // the host scatters from the FASTQ instead
+  if (n == 0 || a == ~0ull || (stage_counter && *stage_counter > stage_cap)) return;
   const BlockDesc d = blocks[blockIdx.x];
   const unsigned* row = blk_offs + (size_t)blockIdx.x * P;
   const unsigned* first = blk_offs + (size_t)d.sample_first * P;  // the sample's first block
@@ -1165,19 +1178,52 @@ __global__ void __launch_bounds__(kBsThreads, 4)
 template <class T>
 void launch_bucket_scatter(const T* keys_stage, const unsigned long long* blk_keys, const unsigned* blk_offs,
                            const BlockDesc* blocks, const unsigned long long* bucket_off, uint32_t partitions,
-                           uint32_t shift, uint32_t nblocks, T* keys_out, cudaStream_t s) {
+                           uint32_t shift, uint32_t nblocks, T* keys_out, const unsigned long long* stage_counter,
+                           unsigned long long stage_cap, cudaStream_t s) {
   const size_t smem = BsSmem<T>::total;
   cudaFuncSetAttribute(k_bucket_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (nblocks)
     k_bucket_scatter<T><<<nblocks, kBsThreads, smem, s>>>(keys_stage, blk_keys, blk_offs, blocks, bucket_off,
-                                                          partitions, shift, keys_out);
+                                                          partitions, shift, keys_out, stage_counter, stage_cap);
 }
 template void launch_bucket_scatter<uint64_t>(const uint64_t*, const unsigned long long*, const unsigned*,
                                               const BlockDesc*, const unsigned long long*, uint32_t, uint32_t,
-                                              uint32_t, uint64_t*, cudaStream_t);
+                                              uint32_t, uint64_t*, const unsigned long long*, unsigned long long,
+                                              cudaStream_t);
 template void launch_bucket_scatter<u128>(const u128*, const unsigned long long*, const unsigned*, const BlockDesc*,
                                           const unsigned long long*, uint32_t, uint32_t, uint32_t, u128*,
-                                          cudaStream_t);
+                                          const unsigned long long*, unsigned long long, cudaStream_t);
+
+// Offsets of one input piece's bucket runs (bucket-major inside the piece,
+// the piece after the earlier ones): an exclusive scan of the piece's bucket
+// counts from *base, the counts added to the bucket totals, *base advanced.
+__global__ void __launch_bounds__(256) k_piece_offsets(const unsigned long long* __restrict__ cnt, uint32_t P,
+                                                       unsigned long long* __restrict__ base,
+                                                       unsigned long long* __restrict__ off,
+                                                       unsigned long long* __restrict__ bucket_count) {
+  constexpr int NT = 256;
+  __shared__ unsigned long long sm[NT / 32 + 2];
+  const uint32_t per = (P + NT - 1) / NT, b0 = threadIdx.x * per;
+  unsigned long long acc = 0;
+  for (uint32_t j = 0; j < per; ++j)
+    if (b0 + j < P) acc += cnt[b0 + j];
+  const unsigned long long start = *base;  // every thread reads it before the barrier inside the scan
+  unsigned long long total;
+  unsigned long long at = start + block_exclusive_scan<NT, unsigned long long>(acc, sm, &total);
+  for (uint32_t j = 0; j < per; ++j)
+    if (b0 + j < P) {
+      const unsigned long long c = cnt[b0 + j];
+      off[b0 + j] = at;
+      bucket_count[b0 + j] += c;
+      at += c;
+    }
+  if (threadIdx.x == 0) *base = start + total;
+}
+
+void launch_piece_offsets(const unsigned long long* cnt, uint32_t partitions, unsigned long long* base,
+                          unsigned long long* off, unsigned long long* bucket_count, cudaStream_t s) {
+  k_piece_offsets<<<1, 256, 0, s>>>(cnt, partitions, base, off, bucket_count);
+}
 
 // Batched count: total of bucket b of sample t = the scanned matrix at the
 // next sample's first block (or the column total) minus it at this sample's.

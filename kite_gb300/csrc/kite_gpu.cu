@@ -90,6 +90,8 @@ enum Stage { ST_LINES = 0, ST_HIST, ST_SCATTER, ST_SPLIT, ST_SORT, ST_BIG, ST_EN
 
 // Bucket groups of the sort / encode / copy-out pipeline.
 constexpr uint32_t kSortGroups = 8;
+// Host chunks: runs of chunks whose bucket scatter runs while later chunks copy in.
+constexpr uint32_t kMaxPieces = 8;
 
 }  // namespace
 
@@ -117,7 +119,7 @@ struct kite_gpu_ctx {
   DevBuf keys_a, keys_b, counts, sample, sample_count, splitters, splitters2, hist16;
   DevBuf tile_count, tile_off, tile_fill, tiles, big_ids, tile_out, tile_boff, tile_prev, meta, out;
   DevBuf lvl_count, lvl_off, reg_off, reg_cnt, sort_stats, blk_mat, blk_gsum, blk_keys, stage_ctr;
-  DevBuf col_total, sample_first, spans, digits, tile_lists;
+  DevBuf col_total, sample_first, spans, digits, tile_lists, piece_off, piece_cnt, piece_base;
   HostBuf h_blocks, h_small, h_tiles, h_out, h_meta, h_dump;
   std::vector<cudaEvent_t> ev;   // stage events
   std::vector<cudaEvent_t> gev;  // sort / encode / copy-out events, 8 per bucket group
@@ -336,6 +338,21 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   // overlap the extraction of earlier ones.  Newline prefixes are counted
   // from each chunk's start, which is all the extraction reads of them.
   const bool overlap = !ctx->ext_mode && spans.size() > 1 && ctx->ticket_events.size() == ctx->chunks.size();
+  // Input pieces (host chunks of one sample, staged keys): the chunks fall
+  // into NP runs, and each run's bucket scatter follows its last chunk's
+  // extraction, while later chunks are still copying in.  The key array
+  // then holds the pieces one after another, each bucket-major inside, and
+  // the first split level reads every bucket as one run per piece.  Until the
+  // key total is known, the key array is sized for a full staging buffer.
+  const uint32_t NP = (overlap && NS == 1 && stage_keys) ? std::min<uint32_t>(kMaxPieces, (uint32_t)spans.size()) : 1;
+  std::vector<uint32_t> piece_first(NP + 1, 0);  // first block of each piece
+  if (NP > 1) {
+    KCU(ctx->piece_off.ensure((size_t)NP * P * 8));
+    KCU(ctx->piece_cnt.ensure((size_t)NP * P * 8));
+    KCU(ctx->piece_base.ensure(8));
+    KCU(cudaMemsetAsync(ctx->piece_base.p, 0, 8, s));
+    KCU(ctx->keys_a.ensure(stage_cap * sizeof(T)));
+  }
   unsigned long long* nl = ctx->nl.as<unsigned long long>();
   auto wait_all_copies = [&]() -> cudaError_t {
     cudaEvent_t dep;
@@ -347,7 +364,9 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   };
   if (overlap) {
     KCU(cudaEventRecord(ctx->ev[1], s));  // the newline stage folds into the histogram stage
-    for (const Span& sp : spans) {
+    uint32_t piece = 0;
+    for (size_t i = 0; i < spans.size(); ++i) {
+      const Span& sp = spans[i];
       KCU(cudaStreamWaitEvent(s, ctx->ticket_events[sp.chunk], 0));
       launch_newline_count(base, ctx->blocks.as<BlockDesc>() + sp.first, sp.n, nl + sp.first, s);
       st.kernel_launches += 1 + exclusive_scan_u64(nl + sp.first, nl + sp.first, sp.n,
@@ -355,6 +374,22 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
       ep.block_base = sp.first;
       launch_extract_hist<T>(ep, sp.n, s);
       st.kernel_launches += 1;
+      if (NP > 1 && i + 1 == (size_t)(piece + 1) * spans.size() / NP) {
+        // the piece's blocks: offsets inside the piece, the piece's bucket
+        // runs after the earlier pieces, and its staged keys scattered there
+        const uint32_t r0 = piece_first[piece], rows = sp.first + sp.n - r0;
+        unsigned* m = ctx->blk_mat.as<unsigned>() + (size_t)r0 * P;
+        unsigned long long* pc = ctx->piece_cnt.as<unsigned long long>() + (size_t)piece * P;
+        unsigned long long* po = ctx->piece_off.as<unsigned long long>() + (size_t)piece * P;
+        st.kernel_launches += count_matrix_offsets(m, rows, P, ctx->blk_gsum.as<unsigned long long>(), pc, s);
+        launch_piece_offsets(pc, P, ctx->piece_base.as<unsigned long long>(), po,
+                             ctx->bucket_count.as<unsigned long long>(), s);
+        launch_bucket_scatter<T>(ctx->keys_b.as<T>(), ctx->blk_keys.as<unsigned long long>() + 2 * (size_t)r0, m,
+                                 ctx->blocks.as<BlockDesc>() + r0, po, P, ep.shift, rows, ctx->keys_a.as<T>(),
+                                 ctx->stage_ctr.as<unsigned long long>(), stage_cap, s);
+        st.kernel_launches += 2;
+        piece_first[++piece] = sp.first + sp.n;
+      }
     }
     ep.block_base = 0;
     KCU(wait_all_copies());
@@ -366,7 +401,7 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     launch_extract_hist<T>(ep, nblocks, s);
     st.kernel_launches += 1;
   }
-  if (use_matrix) {
+  if (use_matrix && NP == 1) {
     // column totals straight into the bucket counts for one sample; per
     // (sample, bucket) totals from the sample boundaries for a batch
     KCU(ctx->col_total.ensure((size_t)P * 8));
@@ -389,9 +424,12 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   // bring bucket counts, totals and the sample count to the host
   // host copies: bucket counts, per-sample totals, sample count, staged keys
   const size_t o_tot = (size_t)PT * 8, o_ns = o_tot + NS * sizeof(CountTotals), o_stg = o_ns + 8;
-  const size_t small_bytes = o_stg + 8;
-  KCU(ctx->h_small.ensure(small_bytes + (size_t)PT * 8));
+  const size_t o_pc = o_stg + 8, pc_bytes = NP > 1 ? (size_t)NP * P * 8 : 0;
+  const size_t small_bytes = o_pc + pc_bytes;
+  // then the bucket offsets and (pieces) the pieces' runs in bucket order
+  KCU(ctx->h_small.ensure(small_bytes + (size_t)PT * 8 + pc_bytes));
   uint8_t* hs = ctx->h_small.as<uint8_t>();
+  if (NP > 1) KCU(cudaMemcpyAsync(hs + o_pc, ctx->piece_cnt.p, pc_bytes, cudaMemcpyDeviceToHost, s));
   KCU(cudaMemcpyAsync(hs, ctx->bucket_count.p, (size_t)PT * 8, cudaMemcpyDeviceToHost, s));
   KCU(cudaMemcpyAsync(hs + o_tot, ctx->totals.p, NS * sizeof(CountTotals), cudaMemcpyDeviceToHost, s));
   KCU(cudaMemcpyAsync(hs + o_ns, ctx->sample_count.p, 4, cudaMemcpyDeviceToHost, s));
@@ -443,16 +481,31 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   ep.keys_out = ctx->keys_a.as<T>();
   ep.blk_counts = nullptr;
   ep.blk_offs = (use_matrix && maxb < (1ull << 32)) ? ctx->blk_mat.as<unsigned>() : nullptr;
-  if (stage_keys && ep.blk_offs && staged == N && N <= stage_cap) {
+  const bool staged_ok = stage_keys && ep.blk_offs && staged == N && N <= stage_cap;
+  // pieces > 1: the keys lie piece after piece (their scatters ran with the extraction)
+  uint32_t pieces = 1;
+  const uint64_t* pcnt = reinterpret_cast<const uint64_t*>(hs + o_pc);
+  uint64_t maxpc = maxb;  // the largest run of one bucket in one piece
+  if (NP > 1 && staged_ok) {
+    st.staged_scatter = 1;
+    pieces = NP;
+    maxpc = 0;
+    for (size_t i = 0; i < (size_t)NP * P; ++i) maxpc = std::max<uint64_t>(maxpc, pcnt[i]);
+  } else if (staged_ok) {
     st.staged_scatter = 1;
     launch_bucket_scatter<T>(ctx->keys_b.as<T>(), ctx->blk_keys.as<unsigned long long>(), ep.blk_offs,
                              ctx->blocks.as<BlockDesc>(), ctx->bucket_off.as<unsigned long long>(), P, ep.shift,
-                             nblocks, ctx->keys_a.as<T>(), s);
+                             nblocks, ctx->keys_a.as<T>(), nullptr, 0, s);
+    st.kernel_launches += 1;
   } else {
+    // from the FASTQ again; with pieces the matrix holds offsets inside each
+    // piece, so the keys take their places by atomics
+    if (NP > 1) ep.blk_offs = nullptr;
     ep.keys_stage = nullptr;
     launch_extract_scatter<T>(ep, nblocks, s);
+    st.kernel_launches += 1;
   }
-  st.kernel_launches += 1;
+  st.input_pieces = pieces;
   KCU(cudaGetLastError());
   KCU(cudaEventRecord(ctx->ev[3], s));
 
@@ -473,6 +526,29 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     }
   }
   st.tiles_per_bucket = S;
+  if (S == 1 && pieces > 1) {
+    // one tile per bucket reads each bucket as one run: the staged keys are
+    // scattered again, piece q's run of bucket b after the earlier pieces' runs
+    uint64_t* at = reinterpret_cast<uint64_t*>(hs + small_bytes + (size_t)PT * 8);
+    for (uint32_t b = 0; b < P; ++b) {
+      uint64_t o = boff[b];
+      for (uint32_t q = 0; q < NP; ++q) {
+        at[(size_t)q * P + b] = o;
+        o += pcnt[(size_t)q * P + b];
+      }
+    }
+    KCU(cudaMemcpyAsync(ctx->piece_off.p, at, pc_bytes, cudaMemcpyHostToDevice, s));
+    for (uint32_t q = 0; q < NP; ++q) {
+      const uint32_t r0 = piece_first[q];
+      launch_bucket_scatter<T>(ctx->keys_b.as<T>(), ctx->blk_keys.as<unsigned long long>() + 2 * (size_t)r0,
+                               ctx->blk_mat.as<unsigned>() + (size_t)r0 * P, ctx->blocks.as<BlockDesc>() + r0,
+                               ctx->piece_off.as<unsigned long long>() + (size_t)q * P, P, ep.shift,
+                               piece_first[q + 1] - r0, ctx->keys_a.as<T>(), nullptr, 0, s);
+      st.kernel_launches += 1;
+    }
+    pieces = 1;
+    maxpc = maxb;
+  }
   T* sorted = ctx->keys_a.as<T>();
   T* scratch = ctx->keys_b.as<T>();
   const T* tile_spl = nullptr;  // the splitters that cut every bucket into its S tiles
@@ -569,7 +645,7 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     T* level_out = ctx->keys_b.as<T>();
     if (D1 > 1) {
       // level 1: buckets -> (bucket, coarse range); coarse splitter c is tile splitter (c+1)*D2-1
-      const uint32_t G1 = parts(PT, maxb, D1);
+      const uint32_t G1 = pieces * parts((uint64_t)PT * pieces, maxpc, D1);
       const size_t n1 = (size_t)PT * D1 * G1;
       KCU(ctx->lvl_count.ensure(n1 * 8));
       KCU(ctx->lvl_off.ensure(n1 * 8));
@@ -579,8 +655,9 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
       TileSplitParams<T> t1 = tp;
       t1.keys_in = level_in;
       t1.keys_out = level_out;
-      t1.region_off = ctx->bucket_off.as<unsigned long long>();
-      t1.region_count = ctx->bucket_count.as<unsigned long long>();
+      t1.region_off = (pieces > 1 ? ctx->piece_off : ctx->bucket_off).as<unsigned long long>();
+      t1.region_count = (pieces > 1 ? ctx->piece_cnt : ctx->bucket_count).as<unsigned long long>();
+      t1.pieces = pieces;
       t1.R = PT;
       t1.D = D1;
       t1.G = G1;
@@ -605,9 +682,10 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
       tp.spl_region_stride = D2;
       std::swap(level_in, level_out);
     } else {
-      G = parts(PT, maxb, D2);
-      tp.region_off = ctx->bucket_off.as<unsigned long long>();
-      tp.region_count = ctx->bucket_count.as<unsigned long long>();
+      G = pieces * parts((uint64_t)PT * pieces, maxpc, D2);
+      tp.region_off = (pieces > 1 ? ctx->piece_off : ctx->bucket_off).as<unsigned long long>();
+      tp.region_count = (pieces > 1 ? ctx->piece_cnt : ctx->bucket_count).as<unsigned long long>();
+      tp.pieces = pieces;
       tp.R = PT;
       tp.spl_first = 0;
       tp.spl_region_stride = 0;
@@ -1023,7 +1101,8 @@ void kite_gpu_close(kite_gpu_ctx* ctx) {
                     &ctx->tile_out, &ctx->tile_boff, &ctx->tile_prev, &ctx->meta, &ctx->out,
                     &ctx->lvl_count, &ctx->lvl_off, &ctx->reg_off, &ctx->reg_cnt, &ctx->sort_stats,
                     &ctx->blk_mat, &ctx->blk_gsum, &ctx->blk_keys, &ctx->stage_ctr,
-                    &ctx->col_total, &ctx->sample_first, &ctx->spans, &ctx->digits, &ctx->tile_lists};
+                    &ctx->col_total, &ctx->sample_first, &ctx->spans, &ctx->digits, &ctx->tile_lists,
+                    &ctx->piece_off, &ctx->piece_cnt, &ctx->piece_base};
   for (DevBuf* b : bufs) b->release();
   ctx->h_blocks.release();
   ctx->h_small.release();

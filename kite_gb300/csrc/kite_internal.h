@@ -109,6 +109,12 @@ struct TileSplitParams {
   unsigned long long* tile_count;       // [R*D*G] (digit-major, part-minor)
   const unsigned long long* tile_off;   // exclusive scan of tile_count
   uint16_t* dig;  // or null; else every key's digit, parallel to keys_in: the histogram writes it, the scatter reads it
+  // 0/1: region r's keys are one run at region_off[r].  pieces > 1: keys_in
+  // holds `pieces` input pieces one after another, each bucket-major, and
+  // region r has one run per piece at region_off[q * R + r] (count
+  // region_count[q * R + r]); parts g of the region belong to piece
+  // g / (G / pieces).
+  uint32_t pieces;
 };
 
 // ---- launchers (count_kernels.cu) ----
@@ -123,10 +129,18 @@ void launch_extract_scatter(const ExtractParams<T>& p, uint32_t nblocks, cudaStr
 // Scatter of the staged keys of every block into the bucket regions
 // (partitions <= 256): keys of block b go to bucket_off[k] + blk_offs[b][k]
 // onwards, ranked on chip so that writes are coalesced.
+// stage_counter (or null): the launch does nothing when the staging counter
+// is above stage_cap (some block's keys were not staged).
 template <class T>
 void launch_bucket_scatter(const T* keys_stage, const unsigned long long* blk_keys, const unsigned* blk_offs,
                            const BlockDesc* blocks, const unsigned long long* bucket_off, uint32_t partitions,
-                           uint32_t shift, uint32_t nblocks, T* keys_out, cudaStream_t s);
+                           uint32_t shift, uint32_t nblocks, T* keys_out, const unsigned long long* stage_counter,
+                           unsigned long long stage_cap, cudaStream_t s);
+// One input piece's bucket runs: off[b] = *base + the piece's counts of the
+// buckets below b; bucket_count[b] += cnt[b]; then *base += the piece's
+// total.  One CTA (partitions <= 1024).
+void launch_piece_offsets(const unsigned long long* cnt, uint32_t partitions, unsigned long long* base,
+                          unsigned long long* off, unsigned long long* bucket_count, cudaStream_t s);
 // Batched count: bucket totals of every (sample, bucket) from the scanned
 // count matrix m (rows = blocks, cols = partitions), col_total = column sums.
 void launch_sample_bucket_counts(const unsigned* m, const unsigned long long* col_total, const uint32_t* sample_first,

@@ -66,7 +66,8 @@ class Stats(C.Structure):
                 ("mlp_pred_imbalance", C.c_double), ("hist_pred_imbalance", C.c_double),
                 ("range_imbalance", C.c_double), ("sort_fallbacks", C.c_uint64),
                 ("split_levels", C.c_uint32), ("staged_scatter", C.c_uint32),
-                ("mlp_reused", C.c_uint32), ("big_tile_keys", C.c_uint64), ("big_tile_rows", C.c_uint64)]
+                ("mlp_reused", C.c_uint32), ("big_tile_keys", C.c_uint64), ("big_tile_rows", C.c_uint64),
+                ("input_pieces", C.c_uint32)]
 
     def as_dict(self) -> dict:
         d = {f: getattr(self, f) for f, _ in self._fields_ if f != "stage_ms"}
