@@ -1081,7 +1081,7 @@ def main():
         parity = parity_full({"device_chunks": count_collect, "host_chunks": host_collect}, data, kk,
                              args.partitions)
 
-    e2e_parts = {"submit_s": 0.0, "finish_s": 0.0, "d2h_ms": 0.0, "stage_ms": [0.0] * 8}
+    e2e_parts = {"submit_s": 0.0, "finish_s": 0.0, "d2h_ms": 0.0, "stage_ms": [0.0] * 12}
     e2e_pieces = [0]
 
     def e2e_step(cc):
@@ -1107,7 +1107,7 @@ def main():
     e2e_step(ce)
     ce.synchronize()
     for key in e2e_parts:
-        e2e_parts[key] = [0.0] * 8 if key == "stage_ms" else 0.0
+        e2e_parts[key] = [0.0] * 12 if key == "stage_ms" else 0.0
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -1152,7 +1152,11 @@ def main():
                         "input_pieces": e2e_pieces[0],
                         # device stages of the end-to-end count (the first two include waiting for the
                         # copies; with input pieces the bucket scatter runs inside the histogram stage)
-                        "stage_ms": {stages[i][0]: round(e2e_parts["stage_ms"][i] / args.steps, 3) for i in stages}},
+                        "stage_ms": {stages[i][0]: round(e2e_parts["stage_ms"][i] / args.steps, 3) for i in stages},
+                        # host wall time of the finish call's phases
+                        "host_ms": {name: round(e2e_parts["stage_ms"][i] / args.steps, 3) for i, name in
+                                    ((8, "copy in, extraction, bucket scatter"), (9, "split, sort, encode"),
+                                     (10, "last payload copies"), (11, "emit calls"))}},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "parity": parity, "e2e_cli": cli,
                 "splitters": splitters,

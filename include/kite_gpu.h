@@ -106,7 +106,11 @@ typedef struct {
   uint32_t tiles, big_tiles, tiles_per_bucket, segments;
   double tile_imbalance;             /* max / mean keys per non-empty tile */
   int splitter_used;                 /* KITE_SPLIT_SAMPLED or KITE_SPLIT_LEARNED */
-  double stage_ms[12];               /* per-stage device time of the last finish (events) */
+  double stage_ms[12];               /* count: [0..7] device time per stage (events: newline count, histogram
+                                        pass, bucket scatter, split, tile sort, large tiles, encode, payload
+                                        copy to the host); host wall time [8] until the bucket counts are back
+                                        (the copy in), [9] split + sort + encode, [10] the last payload copies
+                                        after that, [11] the emit calls.  Merge: see kite_gpu_merge */
   uint64_t h2d_bytes, d2h_bytes;
   uint64_t kernel_launches;          /* kernels this library launched in the last finish */
   double mlp_loss, mlp_pred_imbalance, hist_pred_imbalance; /* learned-splitter diagnostics */

@@ -101,7 +101,7 @@ struct kite_gpu_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaStream_t copy_stream = nullptr;
-  cudaStream_t aux_stream = nullptr;   // splitters, beside the bucket scatter (highest priority)
+  cudaStream_t aux_stream = nullptr;   // highest priority: splitters beside the bucket scatter, encodes beside the next sort
   MergePool merge_pool;                // merge / dump / histo / query device buffers, kept across calls
   cudaEvent_t spl_ready = nullptr;
 
@@ -220,8 +220,20 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   st.h2d_bytes = prev_h2d;
   st.d2h_bytes = prev_d2h;
   st.segments = prev_segments + 1;
+  // nothing of this count starts before the side stream's work of an earlier
+  // call (which an error return may have left in flight) is done
+  KCU(cudaEventRecord(ctx->spl_ready, ctx->aux_stream));
+  KCU(cudaStreamWaitEvent(s, ctx->spl_ready, 0));
   for (auto& e : ctx->ev) cudaEventRecord(e, s);  // reset so unused stages read 0
   KCU(cudaEventRecord(ctx->ev[0], s));
+  // host wall phases: [8] until the bucket counts are on the host (the copy
+  // in), [9] the split, sort and encode queued and done on the stream, [10]
+  // the last payload copies after that; [11] (finish) the emit calls
+  using clk = std::chrono::steady_clock;
+  const auto wall0 = clk::now();
+  auto wall_ms = [](clk::time_point a, clk::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+  };
 
   // ---- blocks -------------------------------------------------------------
   uint32_t blk = 16384;  // 256 threads x 64 bytes
@@ -436,6 +448,7 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
   if (stage_keys) KCU(cudaMemcpyAsync(hs + o_stg, ctx->stage_ctr.p, 8, cudaMemcpyDeviceToHost, s));
   int rc = wait_stream(ctx, s);
   if (rc) return rc;
+  const auto wall1 = clk::now();
   uint64_t staged = ~0ull;
   if (stage_keys) std::memcpy(&staged, hs + o_stg, 8);
   std::vector<uint64_t> bcount(PT);
@@ -851,10 +864,18 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     cudaEventRecord(gev[8 * g + 3], s);
     return cudaGetLastError();
   };
+  // With copies to the host, the encodes run on the highest-priority side
+  // stream, each behind its group's sort and offsets, so group g's encode and
+  // then its copy start as soon as the host has read the group's sizes,
+  // beside the sort of group g+1 rather than after it.  Results kept on the
+  // device encode in line on the counting stream (nothing waits on them there,
+  // and the sorts keep the SMs to themselves).
+  const cudaStream_t es = to_host ? ctx->aux_stream : s;
   // Grows a payload buffer to `need` bytes keeping its first `keep` bytes
   // (after every queued encode and copy has finished).
   auto grow_out = [&](uint64_t need, uint64_t keep) -> int {
     int r = wait_stream(ctx, s);
+    if (!r) r = wait_stream(ctx, es);
     if (!r) r = wait_stream(ctx, ctx->copy_stream);
     if (r) return r;
     if (need > ctx->out.cap) {
@@ -895,11 +916,12 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
       if (rc) return rc;
     }
     // ---- K7 DVLE encode of the group, then its copy to the host
-    cudaEventRecord(gev[8 * g + 4], s);
+    KCU(cudaStreamWaitEvent(es, gev[8 * g + 3], 0));
+    cudaEventRecord(gev[8 * g + 4], es);
     launch_encode<T>(sorted, ctx->counts.as<uint32_t>(), ctx->tiles.as<TileDesc>() + t0, tout + t0,
                      ctx->tile_boff.as<unsigned long long>() + t0, ctx->tile_prev.as<T>() + t0, meta, nt,
-                     ctx->out.as<uint8_t>() + total_bytes, gbytes, ctx->status.as<DevStatus>(), s);
-    cudaEventRecord(gev[8 * g + 5], s);
+                     ctx->out.as<uint8_t>() + total_bytes, gbytes, ctx->status.as<DevStatus>(), es);
+    cudaEventRecord(gev[8 * g + 5], es);
     KCU(cudaGetLastError());
     if (to_host) {
       KCU(cudaStreamWaitEvent(ctx->copy_stream, gev[8 * g + 5], 0));
@@ -911,12 +933,18 @@ int run_count(kite_gpu_ctx* ctx, bool to_host) {
     }
     total_bytes += gbytes;
   }
+  // the counting stream takes up the encodes again
+  KCU(cudaStreamWaitEvent(s, gev[8 * (NG - 1) + 5], 0));
   KCU(cudaEventRecord(ctx->ev[7], s));
   KCU(cudaMemcpyAsync(ctx->h_small.p, ctx->sort_stats.p, 16, cudaMemcpyDeviceToHost, s));
   if (dev_tiles) KCU(cudaMemcpyAsync(ctx->h_tiles.p, ctx->tile_lists.p, lbytes, cudaMemcpyDeviceToHost, s));
   rc = wait_stream(ctx, s);
+  const auto wall2 = clk::now();
   if (!rc && to_host) rc = wait_stream(ctx, ctx->copy_stream);
   if (rc) return rc;
+  st.stage_ms[8] = wall_ms(wall0, wall1);
+  st.stage_ms[9] = wall_ms(wall1, wall2);
+  st.stage_ms[10] = wall_ms(wall2, clk::now());
   std::memcpy(&st.sort_fallbacks, ctx->h_small.p, 8);
   std::memcpy(&st.big_tile_rows, ctx->h_small.as<uint8_t>() + 8, 8);
   // the tile sort adds 2^40 to its statistics when a tile's bulk load did not complete
@@ -1207,7 +1235,9 @@ int kite_gpu_count_finish(kite_gpu_ctx* ctx, kite_gpu_emit_fn emit, void* user) 
   if (!ctx) return KITE_ERR_BAD_INPUT;
   cudaSetDevice(ctx->cfg.device);
   int rc = ctx->cfg.k <= 31 ? run_count<uint64_t>(ctx, emit != nullptr) : run_count<u128>(ctx, emit != nullptr);
+  const auto t0 = std::chrono::steady_clock::now();
   if (rc == KITE_OK) rc = emit_results(ctx, emit, user);
+  ctx->stats.stage_ms[11] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   for (auto e : ctx->ticket_events) cudaEventDestroy(e);
   ctx->ticket_events.clear();
   reset_segment(ctx);
@@ -1243,6 +1273,7 @@ int kite_gpu_get_stats(kite_gpu_ctx* ctx, kite_gpu_stats* out) {
 int kite_gpu_synchronize(kite_gpu_ctx* ctx) {
   if (!ctx) return KITE_ERR_BAD_INPUT;
   int rc = wait_stream(ctx, ctx->copy_stream);
+  if (!rc) rc = wait_stream(ctx, ctx->aux_stream);
   if (rc) return rc;
   return wait_stream(ctx, ctx->stream);
 }
