@@ -27,11 +27,13 @@ struct MergePoolSlot {
 struct MergePool {
   static constexpr int kSlots = 32;
   MergePoolSlot slot[kSlots];
+  MergePoolSlot host;  // pinned host memory: the tile stream lists on their way to the device
   MergePool() = default;
   MergePool(const MergePool&) = delete;
   MergePool& operator=(const MergePool&) = delete;
   ~MergePool() {
     for (auto& s : slot) cudaFree(s.p);
+    if (host.p) cudaFreeHost(host.p);
   }
 };
 

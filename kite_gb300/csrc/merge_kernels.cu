@@ -1405,35 +1405,53 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     std::vector<uint64_t>().swap(c.dlo);
     std::vector<uint64_t>().swap(c.dhi);
   });
+  // the partitions' offsets, then every partition's tiles and stream ranges
+  // written in place in parallel, the stream ranges straight into pinned
+  // memory for their copy to the device
   std::vector<MergeTile> mts;
-  std::vector<TileStream> tss;
   std::vector<TileDesc> tds;
   std::vector<uint32_t> tile_first(P + 1, 0);
-  uint64_t out_off = 0;
-  {
-    size_t nt_all = 0, nts_all = 0;
-    for (uint32_t p = 0; p < P; ++p) {
-      nt_all += pt[p].mts.size();
-      nts_all += pt[p].tss.size();
-    }
-    mts.reserve(nt_all);
-    tds.reserve(nt_all);
-    tss.reserve(nts_all);
-    for (uint32_t p = 0; p < P; ++p) {
-      tile_first[p] = (uint32_t)mts.size();
-      const uint32_t ts0 = (uint32_t)tss.size();
-      for (MergeTile mt : pt[p].mts) {
-        mt.out_off += out_off;
-        mt.first_ts += ts0;
-        tds.push_back(TileDesc{mt.out_off, 0, p});
-        mts.push_back(mt);
-      }
-      tss.insert(tss.end(), pt[p].tss.begin(), pt[p].tss.end());
-      out_off += pt[p].rows;
-      PartTiles().mts.swap(pt[p].mts);
-    }
-    tile_first[P] = (uint32_t)mts.size();
+  std::vector<uint64_t> ts_first(P + 1, 0), row_first(P + 1, 0);
+  for (uint32_t p = 0; p < P; ++p) {
+    tile_first[p + 1] = tile_first[p] + (uint32_t)pt[p].mts.size();
+    ts_first[p + 1] = ts_first[p] + pt[p].tss.size();
+    row_first[p + 1] = row_first[p] + pt[p].rows;
   }
+  const uint64_t out_off = row_first[P];
+  const size_t nts_all = (size_t)ts_first[P];
+  mts.resize(tile_first[P]);
+  tds.resize(tile_first[P]);
+  std::vector<TileStream> tss_own;
+  TileStream* tss = nullptr;
+  if (pool) {
+    MergePoolSlot& hs = pool->host;
+    const size_t need = nts_all * sizeof(TileStream) + 64;
+    if (hs.cap < need) {
+      if (hs.p) cudaFreeHost(hs.p);
+      hs.p = nullptr;
+      hs.cap = 0;
+      if (cudaMallocHost(&hs.p, need) != cudaSuccess) return fail(KITE_ERR_OOM, "merge tile lists (pinned)");
+      hs.cap = need;
+    }
+    tss = static_cast<TileStream*>(hs.p);
+  } else {
+    tss_own.resize(nts_all + 1);
+    tss = tss_own.data();
+  }
+  parallel_parts([&](uint32_t p) {
+    PartTiles& o = pt[p];
+    const uint32_t t0 = tile_first[p], s0 = (uint32_t)ts_first[p];
+    for (size_t i = 0; i < o.mts.size(); ++i) {
+      MergeTile mt = o.mts[i];
+      mt.out_off += row_first[p];
+      mt.first_ts += s0;
+      tds[t0 + i] = TileDesc{mt.out_off, 0, p};
+      mts[t0 + i] = mt;
+    }
+    if (!o.tss.empty()) std::memcpy(tss + s0, o.tss.data(), o.tss.size() * sizeof(TileStream));
+    PartTiles().mts.swap(o.mts);
+    PartTiles().tss.swap(o.tss);
+  });
   stat->stage_ms[9] = ms_since(tp3);
   const uint32_t ntiles = (uint32_t)mts.size();
   std::vector<InputFilter> filt(n);
@@ -1442,7 +1460,7 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
   Dev d_mt(pool, 15), d_ts(pool, 16), d_filt(pool, 17), d_okeys(pool, 18), d_ocounts(pool, 19), d_tout(pool, 20),
       d_over(pool, 21), d_tds(pool, 22), d_tf(pool, 23), d_boff(pool, 24), d_prev(pool, 25), d_meta(pool, 26),
       d_out(pool, 27);
-  if (!d_mt.ensure(ntiles * sizeof(MergeTile) + 8) || !d_ts.ensure(tss.size() * sizeof(TileStream) + 8) ||
+  if (!d_mt.ensure(ntiles * sizeof(MergeTile) + 8) || !d_ts.ensure(nts_all * sizeof(TileStream) + 8) ||
       !d_filt.ensure(n * sizeof(InputFilter)) || !d_okeys.ensure(out_off * sizeof(T) + 16) ||
       !d_ocounts.ensure(out_off * 4 + 16) || !d_tout.ensure(ntiles * sizeof(TileOut<T>) + 16) ||
       !d_over.ensure(8) || !d_tds.ensure(ntiles * sizeof(TileDesc) + 8) || !d_tf.ensure((P + 1) * 4) ||
@@ -1450,7 +1468,7 @@ int merge_typed(uint32_t P, uint32_t key_bits, const kite_gpu_merge_input* in, i
     return fail(KITE_ERR_OOM, "merge tile buffers");
   if (ntiles) {
     MCU(cudaMemcpyAsync(d_mt.p, mts.data(), ntiles * sizeof(MergeTile), cudaMemcpyHostToDevice, s));
-    MCU(cudaMemcpyAsync(d_ts.p, tss.data(), tss.size() * sizeof(TileStream), cudaMemcpyHostToDevice, s));
+    MCU(cudaMemcpyAsync(d_ts.p, tss, nts_all * sizeof(TileStream), cudaMemcpyHostToDevice, s));
   }
   MCU(cudaMemcpyAsync(d_filt.p, filt.data(), n * sizeof(InputFilter), cudaMemcpyHostToDevice, s));
   MCU(cudaMemsetAsync(d_over.p, 0xff, 8, s));
