@@ -128,6 +128,11 @@ struct kite_writer {
   kite_header_info h{};
   uint64_t staging = 0, high = 0, low = 0, next_off = 128, staged = 0;
   std::vector<Part> parts;
+  // Emptied staging buffers, kept for the next partition that stages: a
+  // partition usually stages one chunk per segment, so a buffer of its own
+  // would take its page faults on every byte it ever holds, while the
+  // buffers in use at once are bounded by the drain threshold.
+  std::vector<std::vector<uint8_t>> spare;
   FILE* f = nullptr;
   std::vector<uint8_t> image;  // in-memory mode
   bool in_memory = false;
@@ -156,6 +161,8 @@ struct kite_writer {
     }
     s.pending.clear();
     s.buf.clear();
+    spare.push_back(std::move(s.buf));
+    s.buf = std::vector<uint8_t>();
     return 0;
   }
   bool needs_drain() const { return staged >= high; }
@@ -241,6 +248,14 @@ int kite_writer_append(kite_writer* w, const kite_chunk_meta* m, const uint8_t* 
     s.committed.push_back(mm);
   } else {
     kite_writer::Pending pd{s.buf.size(), mm};
+    if (s.buf.capacity() == 0) {
+      if (!w->spare.empty()) {
+        s.buf = std::move(w->spare.back());
+        w->spare.pop_back();
+      } else {
+        s.buf.reserve(w->staging);  // a staged partition never holds more
+      }
+    }
     s.buf.insert(s.buf.end(), data, data + n);
     s.pending.push_back(pd);
     w->staged += n;
