@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cerrno>
+#include <condition_variable>
 #include <deque>
 #include <dlfcn.h>
 #include <cstdio>
@@ -108,8 +109,28 @@ void header_image(const kite_header_info& h, uint64_t cio, uint64_t pto, uint64_
 }  // namespace
 
 // ============================================================================
-// Writer: ConcurrentKiteWriter's layout for a single appending thread.
+// Writer: ConcurrentKiteWriter's layout for a single appending thread.  The
+// byte layout follows from the order in which staged partitions are flushed:
+// each flush takes the next file offset at once, and the bytes go out by
+// positional writes, staged buffers on `write_lanes` threads (at most four)
+// while appends go on, chunks of at least the staging size directly.
 // ============================================================================
+namespace {
+int pwrite_all(int fd, const uint8_t* p, size_t n, uint64_t off) {
+  while (n) {
+    const ssize_t r = pwrite(fd, p, n, (off_t)off);
+    if (r < 0) {
+      if (errno == EINTR) continue;
+      return -1;
+    }
+    p += r;
+    n -= (size_t)r;
+    off += (uint64_t)r;
+  }
+  return 0;
+}
+}  // namespace
+
 struct kite_writer {
   struct Meta {
     uint64_t off, rows, enc, raw;
@@ -134,16 +155,73 @@ struct kite_writer {
   // buffers in use at once are bounded by the drain threshold.
   std::vector<std::vector<uint8_t>> spare;
   FILE* f = nullptr;
+  int fd = -1;
   std::vector<uint8_t> image;  // in-memory mode
   bool in_memory = false;
   bool finalized = false;
+  // write lanes (file mode): staged buffers queued with their offsets
+  struct Job {
+    std::vector<uint8_t> buf;
+    uint64_t off;
+  };
+  std::vector<std::thread> lanes;
+  std::mutex mu;
+  std::condition_variable cv_job, cv_done;
+  std::deque<Job> jobs;
+  uint64_t queued = 0;  // bytes queued or being written
+  bool stop = false;
+  std::string lane_err;
+
+  void lane_loop() {
+    std::unique_lock<std::mutex> lk(mu);
+    for (;;) {
+      cv_job.wait(lk, [&] { return stop || !jobs.empty(); });
+      if (jobs.empty()) return;
+      Job j = std::move(jobs.front());
+      jobs.pop_front();
+      lk.unlock();
+      const int r = pwrite_all(fd, j.buf.data(), j.buf.size(), j.off);
+      const int e = errno;
+      lk.lock();
+      if (r && lane_err.empty()) lane_err = std::string("write failed: ") + strerror(e);
+      queued -= j.buf.size();
+      j.buf.clear();
+      spare.push_back(std::move(j.buf));
+      cv_done.notify_all();
+    }
+  }
+  void start_lanes(uint64_t n) {
+    for (uint64_t i = 0; i < n; ++i) lanes.emplace_back([this] { lane_loop(); });
+  }
+  void stop_lanes() {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      stop = true;
+    }
+    cv_job.notify_all();
+    for (auto& t : lanes) t.join();
+    lanes.clear();
+  }
+  // every queued write done; the first write error, if any
+  int wait_writes() {
+    std::unique_lock<std::mutex> lk(mu);
+    cv_done.wait(lk, [&] { return queued == 0; });
+    return lane_err.empty() ? 0 : set_err(lane_err);
+  }
+  std::vector<uint8_t> take_buffer() {
+    std::lock_guard<std::mutex> lk(mu);
+    if (spare.empty()) return std::vector<uint8_t>();
+    std::vector<uint8_t> b = std::move(spare.back());
+    spare.pop_back();
+    return b;
+  }
 
   int put(const uint8_t* p, size_t n, uint64_t* off) {
     *off = next_off;
     next_off += n;
     if (in_memory) {
       image.insert(image.end(), p, p + n);
-    } else if (n && fwrite(p, 1, n, f) != n) {
+    } else if (n && pwrite_all(fd, p, n, *off)) {
       return set_err(std::string("write failed: ") + strerror(errno));
     }
     return 0;
@@ -151,8 +229,8 @@ struct kite_writer {
   int flush_part(size_t pid) {
     Part& s = parts[pid];
     if (s.buf.empty()) return 0;
-    uint64_t off;
-    if (put(s.buf.data(), s.buf.size(), &off)) return -1;
+    const uint64_t off = next_off;
+    next_off += s.buf.size();
     staged -= s.buf.size();
     for (auto& pd : s.pending) {
       Meta m = pd.m;
@@ -160,8 +238,23 @@ struct kite_writer {
       s.committed.push_back(m);
     }
     s.pending.clear();
-    s.buf.clear();
-    spare.push_back(std::move(s.buf));
+    if (in_memory || lanes.empty()) {
+      if (in_memory) image.insert(image.end(), s.buf.begin(), s.buf.end());
+      else if (pwrite_all(fd, s.buf.data(), s.buf.size(), off))
+        return set_err(std::string("write failed: ") + strerror(errno));
+      s.buf.clear();
+      std::lock_guard<std::mutex> lk(mu);
+      spare.push_back(std::move(s.buf));
+    } else {
+      std::unique_lock<std::mutex> lk(mu);
+      // bounded: no more than the drain threshold waits for the disk
+      cv_done.wait(lk, [&] { return queued <= high; });
+      if (!lane_err.empty()) return set_err(lane_err);
+      queued += s.buf.size();
+      jobs.push_back(Job{std::move(s.buf), off});
+      lk.unlock();
+      cv_job.notify_one();
+    }
     s.buf = std::vector<uint8_t>();
     return 0;
   }
@@ -218,12 +311,14 @@ kite_writer* kite_writer_open(const char* path, const kite_header_info* h, uint6
       delete w;
       return nullptr;
     }
-    if (fwrite(hdr, 1, 128, w->f) != 128) {
+    if (fwrite(hdr, 1, 128, w->f) != 128 || fflush(w->f)) {
       set_err("header write failed");
       fclose(w->f);
       delete w;
       return nullptr;
     }
+    w->fd = fileno(w->f);
+    w->start_lanes(std::max<uint64_t>(1, std::min<uint64_t>(write_lanes, 4)));
   }
   return w;
 }
@@ -249,12 +344,8 @@ int kite_writer_append(kite_writer* w, const kite_chunk_meta* m, const uint8_t* 
   } else {
     kite_writer::Pending pd{s.buf.size(), mm};
     if (s.buf.capacity() == 0) {
-      if (!w->spare.empty()) {
-        s.buf = std::move(w->spare.back());
-        w->spare.pop_back();
-      } else {
-        s.buf.reserve(w->staging);  // a staged partition never holds more
-      }
+      s.buf = w->take_buffer();
+      if (s.buf.capacity() == 0) s.buf.reserve(w->staging);  // a staged partition never holds more
     }
     s.buf.insert(s.buf.end(), data, data + n);
     s.pending.push_back(pd);
@@ -290,6 +381,7 @@ int kite_writer_finalize(kite_writer* w, uint64_t* total_chunks, uint64_t* total
     std::sort(all[p].begin(), all[p].end(),
               [](const kite_writer::Meta& a, const kite_writer::Meta& b) { return a.off < b.off; });
   }
+  if (!w->in_memory && w->wait_writes()) return -1;
   uint64_t data_end = w->next_off, tc = 0, tr = 0;
   for (auto& v : all)
     for (auto& c : v) {
@@ -335,10 +427,9 @@ int kite_writer_finalize(kite_writer* w, uint64_t* total_chunks, uint64_t* total
     w->image.insert(w->image.end(), t.begin(), t.end());
     memcpy(w->image.data(), hdr, 128);
   } else {
-    if (fseeko(w->f, (off_t)data_end, SEEK_SET) || fwrite(t.data(), 1, t.size(), w->f) != t.size() ||
-        fseeko(w->f, 0, SEEK_SET) || fwrite(hdr, 1, 128, w->f) != 128 || fflush(w->f))
+    if (pwrite_all(w->fd, t.data(), t.size(), data_end) || pwrite_all(w->fd, hdr, 128, 0))
       return set_err(std::string("finalize write failed: ") + strerror(errno));
-    if (ftruncate(fileno(w->f), (off_t)(fo + 24))) return set_err("set_len failed");
+    if (ftruncate(w->fd, (off_t)(fo + 24))) return set_err("set_len failed");
   }
   w->finalized = true;
   if (total_chunks) *total_chunks = tc;
@@ -354,6 +445,7 @@ const uint8_t* kite_writer_image(kite_writer* w, size_t* len) {
 
 void kite_writer_close(kite_writer* w) {
   if (!w) return;
+  w->stop_lanes();  // the queued writes finish first
   if (w->f) fclose(w->f);
   delete w;
 }

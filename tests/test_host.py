@@ -93,6 +93,25 @@ def test_writer_layout_matches_oracle(built, orc, staging, lanes):
     assert w.image() == img
 
 
+@pytest.mark.parametrize("staging,lanes", [(16 << 20, 1), (4096, 2), (65536, 4), (300, 3)])
+def test_writer_file_lanes_match_oracle(built, orc, tmp_path, staging, lanes):
+    """The file writer (staged buffers written by positional writes on its
+    write lanes while appends go on) produces the oracle's .kite bytes."""
+    fq = synth.small_workload(seed=5, n_reads=4000, genome_len=60_000)
+    img, _ = orc.count_kite(fq, 21, False, 32, staging_bytes=staging, lanes=lanes)
+    ki = KiteImage.parse(img)
+    path = tmp_path / "w.kite"
+    w = host.Writer(str(path), 21, False, 32, 64, 7, staging, lanes)
+    for p in range(32):
+        for ch in ki.partition_chunks(p):
+            w.append({"partition_id": p, "codec": ch.codec, "row_count": ch.row_count, "raw_bytes": ch.raw_bytes,
+                      "key_min": ch.key_min, "key_max": ch.key_max}, ki.payload(ch))
+    w.worker_drain()
+    w.finalize()
+    w.close()
+    assert path.read_bytes() == img
+
+
 def test_dump_matches_oracle(built, orc):
     fq = synth.small_workload(seed=6, n_reads=2000, genome_len=20_000)
     for k, canon, mn, mx in [(21, False, None, None), (31, True, 2, None), (45, True, 2, 10)]:
