@@ -215,7 +215,10 @@ int cmd_count(int argc, char** argv) {
   if (rc != KITE_OK) die("failed to open the GPU counting context (code " + std::to_string(rc) + ")");
   kite_input* input = kite_input_open(in.c_str(), plan.chunk_size_bytes);
   if (!input) die(kite_host_last_error());
-  kite_input_set_threads(input, (unsigned)plan.decomp_threads);  // BGZF inflate threads
+  // BGZF inflate threads: the plan's split keeps most host threads for
+  // counting workers, but here the GPU counts, so every host thread inflates
+  // (the split changes nothing in the output; the plan's sizes still apply)
+  kite_input_set_threads(input, (unsigned)std::max<uint64_t>(plan.decomp_threads, total_threads));
   // pinned ring: the host inflates/reads chunk i+1 while chunk i is copied
   const int NBUF = 3;
   const size_t cap = (size_t)kite_input_max_chunk(input) + 64;
