@@ -48,7 +48,7 @@ def reads():
 
 @pytest.mark.parametrize("chunk_size", [100_000, 262_144, 1 << 20])
 @pytest.mark.parametrize("block", [65280, 9000])
-@pytest.mark.parametrize("threads", [1, 4])
+@pytest.mark.parametrize("threads", [1, 4, 16])  # 16: every host thread, as `kite count` uses
 def test_chunks_match_oracle(orc, tmp_path, reads, chunk_size, block, threads):
     p = tmp_path / "r.fq.gz"
     write_bgzf(p, reads, block)
