@@ -1152,6 +1152,7 @@ int64_t kite_gpu_count_submit_sample(kite_gpu_ctx* ctx, uint32_t sample, const u
     return fail(ctx, KITE_ERR_BAD_INPUT, "sample index beyond cfg.samples");
   if (ctx->ext_mode) return fail(ctx, KITE_ERR_STATE, "host and device submissions cannot mix in one segment");
   if (len == 0) return ctx->next_ticket++;
+  cudaSetDevice(ctx->cfg.device);  // the caller's thread may not be the one that opened the context
   const uint64_t off = (ctx->arena_used + 15) & ~15ull;
   if (off + len + 16 > ctx->cfg.arena_bytes) {
     if (ctx->chunks.empty() && len + 16 > ctx->cfg.arena_bytes)

@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <string>
 #include <sys/stat.h>
 #include <unistd.h>
@@ -210,9 +211,6 @@ int cmd_count(int argc, char** argv) {
   cfg.canonical = canonical;
   cfg.partitions = (uint32_t)plan.partitions;
   cfg.splitter_mode = split_mode;
-  kite_gpu_ctx* ctx = nullptr;
-  int rc = kite_gpu_open(&cfg, &ctx);
-  if (rc != KITE_OK) die("failed to open the GPU counting context (code " + std::to_string(rc) + ")");
   kite_input* input = kite_input_open(in.c_str(), plan.chunk_size_bytes);
   if (!input) die(kite_host_last_error());
   // BGZF inflate threads: the plan's split keeps most host threads for
@@ -222,12 +220,42 @@ int cmd_count(int argc, char** argv) {
   // pinned ring: the host inflates/reads chunk i+1 while chunk i is copied
   const int NBUF = 3;
   const size_t cap = (size_t)kite_input_max_chunk(input) + 64;
-  std::vector<uint8_t*> ring(NBUF);
+  std::vector<uint8_t*> ring(NBUF, nullptr);
   std::vector<int64_t> ticket(NBUF, -1);
-  for (auto& b : ring) {
-    b = static_cast<uint8_t*>(kite_gpu_alloc_pinned(cap));
-    if (!b) die("failed to allocate pinned host buffers");
+  // The GPU context and the pinned ring are set up on a second thread while
+  // this one reads the first chunks into host memory (at most kEarly of them).
+  kite_gpu_ctx* ctx = nullptr;
+  int rc = KITE_OK;
+  bool ring_ok = true;
+  std::atomic<bool> ready{false};
+  std::thread setup([&]() {
+    rc = kite_gpu_open(&cfg, &ctx);
+    if (rc == KITE_OK)
+      for (auto& b : ring) {
+        b = static_cast<uint8_t*>(kite_gpu_alloc_pinned(cap));
+        if (!b) ring_ok = false;
+      }
+    ready.store(true, std::memory_order_release);
+  });
+  constexpr size_t kEarly = 16;
+  std::vector<std::pair<std::unique_ptr<uint8_t[]>, size_t>> early;
+  bool input_done = false;
+  while (!ready.load(std::memory_order_acquire) && early.size() < kEarly) {
+    std::unique_ptr<uint8_t[]> b(new uint8_t[cap]);
+    const int64_t n = kite_input_next(input, b.get(), cap);
+    if (n < 0) {
+      setup.join();
+      die(kite_host_last_error());
+    }
+    if (n == 0) {
+      input_done = true;
+      break;
+    }
+    early.emplace_back(std::move(b), (size_t)n);
   }
+  setup.join();
+  if (rc != KITE_OK) die("failed to open the GPU counting context (code " + std::to_string(rc) + ")");
+  if (!ring_ok) die("failed to allocate pinned host buffers");
   uint64_t reads = 0, bases = 0, kmers = 0;
   // balanced / compact: every chunk of the segment through zstd "if smaller"
   // on the host threads, then appended in partition order
@@ -243,19 +271,28 @@ int cmd_count(int argc, char** argv) {
     bases += st.bases;
     kmers += st.kmers;
   };
-  for (int slot = 0;; slot = (slot + 1) % NBUF) {
+  auto submit = [&](const uint8_t* p, size_t n) -> int64_t {
+    int64_t t = kite_gpu_count_submit(ctx, p, n);
+    if (t == KITE_ERR_STATE) {  // device arena full: count this segment first
+      finish_segment();
+      t = kite_gpu_count_submit(ctx, p, n);
+    }
+    if (t < 0) die(std::string("submit failed: ") + kite_gpu_last_error(ctx));
+    return t;
+  };
+  // the early chunks: a copy from pageable memory has left the buffer when
+  // the submit returns
+  for (auto& b : early) {
+    submit(b.first.get(), b.second);
+    b.first.reset();
+  }
+  for (int slot = 0; !input_done; slot = (slot + 1) % NBUF) {
     if (ticket[slot] >= 0 && kite_gpu_wait_ticket(ctx, ticket[slot]) != KITE_OK)
       die(std::string("copy wait failed: ") + kite_gpu_last_error(ctx));
     const int64_t n = kite_input_next(input, ring[slot], cap);
     if (n < 0) die(kite_host_last_error());
     if (n == 0) break;
-    int64_t t = kite_gpu_count_submit(ctx, ring[slot], (size_t)n);
-    if (t == KITE_ERR_STATE) {  // device arena full: count this segment first
-      finish_segment();
-      t = kite_gpu_count_submit(ctx, ring[slot], (size_t)n);
-    }
-    if (t < 0) die(std::string("submit failed: ") + kite_gpu_last_error(ctx));
-    ticket[slot] = t;
+    ticket[slot] = submit(ring[slot], (size_t)n);
   }
   finish_segment();
   if (kite_writer_worker_drain(w) != 0) die(kite_host_last_error());
