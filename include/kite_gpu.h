@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define KITE_GPU_ABI_VERSION 1
+#define KITE_GPU_ABI_VERSION 2  /* 2: kite_gpu_stats.input_pieces */
 
 enum {
   KITE_OK = 0,

@@ -22,6 +22,7 @@ ERRORS = {
     -9: "KITE_ERR_STATE",
 }
 SPLIT_AUTO, SPLIT_SAMPLED, SPLIT_LEARNED = 0, 1, 2
+ABI_VERSION = 2  # KITE_GPU_ABI_VERSION: the layouts of the structures below
 
 EXPORTED = [
     "kite_gpu_abi_version", "kite_gpu_device_count", "kite_gpu_open", "kite_gpu_close", "kite_gpu_last_error",
@@ -93,6 +94,8 @@ def lib() -> C.CDLL:
         if not _LIB_PATH.exists():
             raise RuntimeError(f"{_LIB_PATH} is missing: build the CUDA extension first (kite_gb300.build)")
         L = C.CDLL(str(_LIB_PATH))
+        if L.kite_gpu_abi_version() != ABI_VERSION:
+            raise RuntimeError(f"{_LIB_PATH} has C ABI {L.kite_gpu_abi_version()}, this binding {ABI_VERSION}: rebuild")
         L.kite_gpu_open.argtypes = [C.POINTER(Cfg), C.POINTER(C.c_void_p)]
         L.kite_gpu_close.argtypes = [C.c_void_p]
         L.kite_gpu_last_error.argtypes = [C.c_void_p]
