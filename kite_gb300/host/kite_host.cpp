@@ -1140,41 +1140,37 @@ struct kite_input {
   size_t asm_pos = 0;   // start of the uncut bytes
   std::deque<std::pair<size_t, size_t>> ready;
   std::string bgzf_err;
-  // Inflates the next batch of blocks and cuts what it can into ready chunks,
-  // as the reference does after every appended block; after the last block
-  // the uncut rest is a chunk.  Each block inflates straight to its place
-  // (its gzip ISIZE field gives its output size); a batch where a block does
-  // not decode to exactly that size is assembled again block by block.
-  void bgzf_fill() {
-    if (asm_pos) {
-      memmove(asm_buf.data(), asm_buf.data() + asm_pos, asm_len - asm_pos);
-      asm_len -= asm_pos;
-      asm_pos = 0;
-    }
-    const size_t nb = std::min(kBgzfBatch, blocks.size() - next_block);
-    if (nb == 0) {
-      if (asm_len) ready.push_back({0, asm_len});
-      asm_pos = asm_len;
-      eof = true;
-      return;
-    }
-    std::vector<size_t> off(nb + 1);
-    off[0] = asm_len;
+  // Batches are pipelined: while the chunks of one batch are handed out, the
+  // next batch inflates on the pool into the other buffer (nxt_buf), after
+  // room for the bytes the current batch leaves uncut.
+  std::vector<uint8_t> nxt_buf;
+  std::vector<size_t> nxt_off;  // block output ends in nxt_buf, nxt_off[0] = the room left in front
+  size_t nxt_nb = 0;
+  std::thread nxt_thread;
+  bool nxt_pending = false;
+
+  // Inflates blocks [first, first + nb) into buf after `room` bytes; off gets
+  // every block's output end.  Each block inflates straight to its place (its
+  // gzip ISIZE field gives its output size); a batch where a block does not
+  // decode to exactly that size is assembled again block by block.
+  void inflate_batch(size_t first, size_t nb, size_t room, std::vector<uint8_t>& buf, std::vector<size_t>& off) {
+    off.assign(nb + 1, 0);
+    off[0] = room;
     for (size_t i = 0; i < nb; ++i) {
-      const auto& b = blocks[next_block + i];
+      const auto& b = blocks[first + i];
       const uint8_t* t = file.p + b.first + b.second - 4;
       size_t isize = (size_t)t[0] | ((size_t)t[1] << 8) | ((size_t)t[2] << 16) | ((size_t)t[3] << 24);
       if (isize > 65536) isize = 65536;  // not a BGZF block size: the check below catches it
       off[i + 1] = off[i] + isize;
     }
-    if (asm_buf.size() < off[nb]) asm_buf.resize(off[nb]);
+    if (buf.size() < off[nb]) buf.resize(off[nb]);
     std::atomic<size_t> idx{0};
     std::atomic<bool> exact{true};
     auto work = [&]() {
       for (size_t i; (i = idx.fetch_add(1)) < nb;) {
-        const auto& b = blocks[next_block + i];
+        const auto& b = blocks[first + i];
         const size_t want = off[i + 1] - off[i];
-        if (inflate_member_into(file.p + b.first, b.second, asm_buf.data() + off[i], want) != want)
+        if (inflate_member_into(file.p + b.first, b.second, buf.data() + off[i], want) != want)
           exact.store(false);
       }
     };
@@ -1189,17 +1185,53 @@ struct kite_input {
     if (!exact.load()) {
       // block by block: each block's actual output, partial on a decode error
       std::vector<uint8_t> o;
-      size_t len = off[0];
+      size_t len = room;
       for (size_t i = 0; i < nb; ++i) {
-        const auto& b = blocks[next_block + i];
+        const auto& b = blocks[first + i];
         inflate_member(file.p + b.first, b.second, o);
-        if (asm_buf.size() < len + o.size()) asm_buf.resize(len + o.size());
-        if (!o.empty()) memcpy(asm_buf.data() + len, o.data(), o.size());
+        if (buf.size() < len + o.size()) buf.resize(len + o.size());
+        if (!o.empty()) memcpy(buf.data() + len, o.data(), o.size());
         len += o.size();
         off[i + 1] = len;
       }
     }
+  }
+  // Starts the inflate of the batch after next_block, with `room` bytes left
+  // in front of it for the current batch's uncut rest.
+  void start_next(size_t room) {
+    nxt_nb = std::min(kBgzfBatch, blocks.size() - next_block);
+    if (nxt_nb == 0) return;
+    const size_t first = next_block;
+    nxt_pending = true;
+    nxt_thread = std::thread([this, first, room]() { inflate_batch(first, nxt_nb, room, nxt_buf, nxt_off); });
+  }
+  void join_next() {
+    if (nxt_pending) {
+      nxt_thread.join();
+      nxt_pending = false;
+    }
+  }
+  // Called when every ready chunk has been handed out: takes the next batch
+  // (inflated meanwhile), puts the uncut rest in front of it and cuts what it
+  // can into ready chunks, as the reference does after every appended block;
+  // after the last block the uncut rest is a chunk.
+  void bgzf_fill() {
+    const size_t rest = asm_len - asm_pos;
+    if (!nxt_pending) start_next(rest);
+    if (!nxt_pending) {
+      if (rest) ready.push_back({asm_pos, rest});
+      asm_pos = asm_len;
+      eof = true;
+      return;
+    }
+    join_next();
+    // the batch was inflated after room for exactly this rest
+    if (rest) memcpy(nxt_buf.data(), asm_buf.data() + asm_pos, rest);
+    asm_buf.swap(nxt_buf);
+    const size_t nb = nxt_nb;
+    const std::vector<size_t> off = nxt_off;
     next_block += nb;
+    asm_pos = 0;
     for (size_t i = 0; i < nb; ++i) {
       const size_t end = off[i + 1];
       if (end == off[i]) continue;
@@ -1211,7 +1243,10 @@ struct kite_input {
       }
     }
     asm_len = off[nb];
+    // the following batch inflates while these chunks are handed out
+    start_next(asm_len - asm_pos);
   }
+  ~kite_input() { join_next(); }
   size_t read_raw(uint8_t* dst, size_t want) {
     size_t total = 0;
 #if KITE_HAVE_ZLIB
