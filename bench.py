@@ -662,9 +662,15 @@ def e2e_cli_leg(data, local: int, partitions: int) -> dict:
     n = sum(host.read_chunks(gzf, 64 << 20, 1, collect=False))
     gz_s = time.perf_counter() - t0
     t0 = time.perf_counter()
+    nm = sum(host.read_chunks(gzf, 64 << 20, cores, collect=False))
+    gm_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
     nb = sum(host.read_chunks(bgzf, 64 << 20, cores, collect=False))
     bg_s = time.perf_counter() - t0
+    # serial gzip: the reference's reader; the same file's members on every
+    # host thread: this command's reader
     out["reader_ceiling"] = {"gzip_serial_gbs": round(n / gz_s / 1e9, 3), "gzip_kmers_per_s": kmers / gz_s,
+                             "gzip_members_parallel_gbs": round(nm / gm_s / 1e9, 3),
                              "bgzf_gbs": round(nb / bg_s / 1e9, 3), "bgzf_kmers_per_s": kmers / bg_s,
                              "threads": cores}
     out["files"] = {"fastq_bytes": len(data), "gzip_bytes": gzf.stat().st_size, "bgzf_bytes": bgzf.stat().st_size,

@@ -106,8 +106,9 @@ kite_input* kite_input_open(const char* path, uint64_t chunk_size);
  * its length, 0 at end, -1 on error. */
 int64_t kite_input_next(kite_input* in, uint8_t* dst, size_t cap);
 uint64_t kite_input_max_chunk(const kite_input* in);
-/* Inflate threads of a BGZF input (decomp_threads of the plan; default half
- * the host's cores).  Other inputs ignore it. */
+/* Inflate threads of a BGZF input and of a multi-member gzip input (its
+ * members inflate in parallel; default half the host's cores).  Plain input
+ * and single-member gzip ignore it. */
 int kite_input_set_threads(kite_input* in, unsigned threads);
 void kite_input_close(kite_input* in);
 double kite_sample_avg_read_len(const char* path, int compression);

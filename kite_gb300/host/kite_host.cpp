@@ -1113,10 +1113,84 @@ struct FileBytes {
     ::close(fd);
     return true;
   }
-  ~FileBytes() {
+  void close() {
     if (map) munmap(map, n);
+    map = nullptr;
+    p = nullptr;
+    n = 0;
+    std::vector<uint8_t>().swap(copy);
   }
+  ~FileBytes() { close(); }
 };
+
+// A gzip member header at i: magic, deflate, no reserved flag bits, an
+// extra-flags byte deflate writes and a known OS byte.
+bool gz_header_at(const uint8_t* p, size_t n, size_t i) {
+  if (i + 10 > n || p[i] != 0x1f || p[i + 1] != 0x8b || p[i + 2] != 8 || (p[i + 3] & 0xe0)) return false;
+  const uint8_t xfl = p[i + 8], os = p[i + 9];
+  return (xfl == 0 || xfl == 2 || xfl == 4) && (os <= 13 || os == 255);
+}
+
+// Offsets of every position that looks like a gzip member header, ascending
+// (scanned on several threads).
+std::vector<size_t> gz_member_candidates(const uint8_t* p, size_t n) {
+  const unsigned T = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::vector<std::vector<size_t>> part(T);
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < T; ++t)
+    th.emplace_back([&, t]() {
+      const size_t a = n * t / T, b = n * (t + 1) / T;
+      for (size_t i = a; i < b;) {
+        const void* q = memchr(p + i, 0x1f, b - i);
+        if (!q) break;
+        i = (size_t)(static_cast<const uint8_t*>(q) - p);
+        if (gz_header_at(p, n, i)) part[t].push_back(i);
+        ++i;
+      }
+    });
+  for (auto& x : th) x.join();
+  std::vector<size_t> all;
+  for (auto& v : part) all.insert(all.end(), v.begin(), v.end());
+  return all;
+}
+
+#if KITE_HAVE_ZLIB
+// One complete gzip member from p[0, n) into out (at most cap bytes): true
+// when it ends (CRC and size checked); *used = its compressed length.
+bool inflate_whole_member(const uint8_t* p, size_t n, size_t hint, size_t cap, std::vector<uint8_t>& out,
+                          size_t* used) {
+  out.clear();
+  z_stream zs{};
+  if (inflateInit2(&zs, 15 + 16) != Z_OK) return false;
+  out.resize(std::min(std::max<size_t>(hint, 1 << 20), cap));
+  size_t fed = 0, have = 0;
+  int r = Z_OK;
+  while (r == Z_OK) {
+    if (zs.avail_in == 0 && fed < n) {
+      const size_t k = std::min<size_t>(n - fed, 1u << 30);
+      zs.next_in = const_cast<uint8_t*>(p + fed);
+      zs.avail_in = (uInt)k;
+      fed += k;
+    }
+    if (have == out.size()) {
+      if (out.size() >= cap) break;
+      out.resize(std::min(cap, out.size() * 2));
+    }
+    const size_t room = std::min<size_t>(out.size() - have, 1u << 30);
+    zs.next_out = out.data() + have;
+    zs.avail_out = (uInt)room;
+    r = inflate(&zs, Z_NO_FLUSH);
+    have += room - zs.avail_out;
+    if (r == Z_BUF_ERROR && zs.avail_in == 0 && fed >= n) break;
+    if (r == Z_BUF_ERROR && zs.avail_out != 0) break;
+    if (r == Z_BUF_ERROR) r = Z_OK;  // output room only
+  }
+  *used = (size_t)zs.total_in;
+  inflateEnd(&zs);
+  out.resize(have);
+  return r == Z_STREAM_END;
+}
+#endif
 
 }  // namespace
 
@@ -1246,10 +1320,127 @@ struct kite_input {
     // the following batch inflates while these chunks are handed out
     start_next(asm_len - asm_pos);
   }
-  ~kite_input() { join_next(); }
+  ~kite_input() {
+    join_next();
+    gz_stop();
+  }
+
+  // Multi-member gzip: the members, chained from the file's start (each one
+  // starts where the previous one's compressed bytes end), inflate on
+  // `threads` threads up to that many ahead and are handed out in order.
+  // Anything else (a member that does not decode, bytes after the last
+  // member, one thread) goes to the serial reader, opened from the file's
+  // start and skipping the bytes already handed out, so that the byte stream
+  // and its errors are exactly the serial reader's.
+  static constexpr size_t kGzMemberCap = 256u << 20;
+  struct GzTask {
+    std::thread th;
+    bool ok = false;
+    size_t used = 0;
+    std::vector<uint8_t> out;
+  };
+  bool gzpar = false;
+  std::string gz_path;
+  std::vector<size_t> gz_cands;  // offsets that look like member headers
+  size_t gz_next = 0;            // compressed offset of the next member of the chain
+  size_t gz_launched = 0;        // candidates [0, gz_launched) have had a task
+  uint64_t gz_delivered = 0;
+  std::vector<uint8_t> gz_cur;
+  size_t gz_cur_off = 0;
+  std::deque<std::pair<size_t, std::unique_ptr<GzTask>>> gz_tasks;  // (candidate index, task), in order
+
+  void gz_stop() {
+    for (auto& t : gz_tasks)
+      if (t.second->th.joinable()) t.second->th.join();
+    gz_tasks.clear();
+  }
+  void gz_launch(size_t j) {
+    const size_t c = gz_cands[j];
+    // the member's output size, if the next candidate starts the next member
+    const size_t e = j + 1 < gz_cands.size() ? gz_cands[j + 1] : file.n;
+    const uint8_t* q = file.p + e - 4;
+    const size_t hint = e >= c + 18 ? ((size_t)q[0] | ((size_t)q[1] << 8) | ((size_t)q[2] << 16) | ((size_t)q[3] << 24)) : 0;
+    auto t = std::make_unique<GzTask>();
+    GzTask* tp = t.get();
+    tp->th = std::thread([this, c, hint, tp]() {
+#if KITE_HAVE_ZLIB
+      tp->ok = inflate_whole_member(file.p + c, file.n - c, hint, kGzMemberCap, tp->out, &tp->used);
+#endif
+    });
+    gz_tasks.emplace_back(j, std::move(t));
+  }
+  // To the serial reader: from the file's start, the bytes already handed out skipped.
+  void gz_fallback() {
+    gzpar = false;
+    gz_stop();
+    std::vector<uint8_t>().swap(gz_cur);
+    gz_cur_off = 0;
+#if KITE_HAVE_ZLIB
+    gz = gzopen(gz_path.c_str(), "rb");
+    if (!gz) {
+      g_err = "decompress_error: failed to reopen the input";
+      return;
+    }
+    gzbuffer(gz, 1 << 20);
+    std::vector<uint8_t> skip(1 << 20);
+    for (uint64_t left = gz_delivered; left;) {
+      const int r = gzread(gz, skip.data(), (unsigned)std::min<uint64_t>(left, skip.size()));
+      if (r <= 0) break;
+      left -= (uint64_t)r;
+    }
+#endif
+  }
+  // The next member's bytes into gz_cur; false at the chain's end, or when
+  // the serial reader takes over (gzpar then false).
+  bool gz_advance() {
+    if (gz_next == file.n) return false;
+    const auto it = std::lower_bound(gz_cands.begin(), gz_cands.end(), gz_next);
+    if (threads <= 1 || it == gz_cands.end() || *it != gz_next) {
+      gz_fallback();
+      return false;
+    }
+    const size_t j = (size_t)(it - gz_cands.begin());
+    // tasks for the candidates skipped (not member starts) are dropped
+    while (!gz_tasks.empty() && gz_tasks.front().first < j) {
+      gz_tasks.front().second->th.join();
+      gz_tasks.pop_front();
+    }
+    gz_launched = std::max(gz_launched, j);
+    while (gz_launched < gz_cands.size() && gz_launched < j + threads) gz_launch(gz_launched++);
+    GzTask& t = *gz_tasks.front().second;
+    t.th.join();
+    if (!t.ok || t.used == 0) {
+      gz_fallback();
+      return false;
+    }
+    gz_cur.swap(t.out);
+    gz_cur_off = 0;
+    gz_next += t.used;
+    gz_tasks.pop_front();
+    return true;
+  }
+  size_t gz_read_par(uint8_t* dst, size_t want) {
+    size_t total = 0;
+    while (total < want) {
+      if (gz_cur_off < gz_cur.size()) {
+        const size_t m = std::min(want - total, gz_cur.size() - gz_cur_off);
+        memcpy(dst + total, gz_cur.data() + gz_cur_off, m);
+        gz_cur_off += m;
+        total += m;
+        gz_delivered += m;
+        continue;
+      }
+      if (!gz_advance()) break;
+    }
+    return total;
+  }
   size_t read_raw(uint8_t* dst, size_t want) {
     size_t total = 0;
 #if KITE_HAVE_ZLIB
+    if (gzpar) {
+      total = gz_read_par(dst, want);
+      if (gzpar || total == want) return total;  // the chain's end, or filled
+    }
     if (gz) {
       while (total < want) {
         int r = gzread(gz, dst + total, (unsigned)std::min<size_t>(want - total, 1u << 30));
@@ -1310,6 +1501,19 @@ kite_input* kite_input_open(const char* path, uint64_t chunk_size) {
     setvbuf(in->f, nullptr, _IOFBF, 2 << 20);
   } else {
 #if KITE_HAVE_ZLIB
+    // several members: inflated in parallel (the serial reader stays for
+    // one member and for anything the chain does not explain)
+    if (in->file.open(path)) {
+      in->gz_cands = gz_member_candidates(in->file.p, in->file.n);
+      if (in->gz_cands.size() >= 2 && in->gz_cands[0] == 0) {
+        in->gzpar = true;
+        in->gz_path = path;
+        in->threads = std::max(1u, std::thread::hardware_concurrency() / 2);
+        return in;
+      }
+      std::vector<size_t>().swap(in->gz_cands);
+    }
+    in->file.close();
     in->gz = gzopen(path, "rb");
     if (!in->gz) {
       set_err(std::string("failed to open input FASTQ.\nInput: ") + path);
