@@ -674,7 +674,8 @@ def e2e_cli_leg(data, local: int, partitions: int) -> dict:
                              "bgzf_gbs": round(nb / bg_s / 1e9, 3), "bgzf_kmers_per_s": kmers / bg_s,
                              "threads": cores}
     out["files"] = {"fastq_bytes": len(data), "gzip_bytes": gzf.stat().st_size, "bgzf_bytes": bgzf.stat().st_size,
-                    "gzip": "multi-member gzip, level 1, 64 MiB members", "bgzf": "65,280-byte blocks, level 1"}
+                    "gzip": "multi-member gzip, level 1, 64 MiB members (kite count inflates the members in parallel; "
+                            "a single-member file reads serially)", "bgzf": "65,280-byte blocks, level 1"}
     out["flags"] = " ".join(flags)
     for p in (gzf, bgzf, tmp / "g.kite", tmp / "r.kite"):
         if p.exists():
